@@ -1,0 +1,421 @@
+/*
+ * vko_api.c - oracle surfaces, contexts, state and matrices
+ * (TEST INFRASTRUCTURE ONLY).  Matrix functions restate src/vkvg_matrix.c of
+ * vkvg (cairo-derived); state setters restate src/vkvg_context.c:1011-1115.
+ */
+#include "vko_internal.h"
+
+/* ---------------------------------------------------------------- matrices */
+
+void vko_matrix_init(vko_matrix *m, float xx, float yx, float xy, float yy, float x0, float y0) {
+    m->xx = xx;
+    m->yx = yx;
+    m->xy = xy;
+    m->yy = yy;
+    m->x0 = x0;
+    m->y0 = y0;
+}
+void vko_matrix_init_identity(vko_matrix *m) { vko_matrix_init(m, 1, 0, 0, 1, 0, 0); }
+void vko_matrix_init_translate(vko_matrix *m, float tx, float ty) { vko_matrix_init(m, 1, 0, 0, 1, tx, ty); }
+void vko_matrix_init_scale(vko_matrix *m, float sx, float sy) { vko_matrix_init(m, sx, 0, 0, sy, 0, 0); }
+void vko_matrix_init_rotate(vko_matrix *m, float radians) {
+    float s = VKO_SINF(radians), c = VKO_COSF(radians);
+    vko_matrix_init(m, c, s, -s, c, 0, 0);
+}
+/* vkvg_matrix_multiply, src/vkvg_matrix.c:193-205 */
+void vko_matrix_multiply(vko_matrix *result, const vko_matrix *a, const vko_matrix *b) {
+    vko_matrix r;
+    r.xx    = a->xx * b->xx + a->yx * b->xy;
+    r.yx    = a->xx * b->yx + a->yx * b->yy;
+    r.xy    = a->xy * b->xx + a->yy * b->xy;
+    r.yy    = a->xy * b->yx + a->yy * b->yy;
+    r.x0    = a->x0 * b->xx + a->y0 * b->xy + b->x0;
+    r.y0    = a->x0 * b->yx + a->y0 * b->yy + b->y0;
+    *result = r;
+}
+void vko_matrix_translate(vko_matrix *m, float tx, float ty) {
+    vko_matrix t;
+    vko_matrix_init_translate(&t, tx, ty);
+    vko_matrix_multiply(m, &t, m);
+}
+void vko_matrix_scale(vko_matrix *m, float sx, float sy) {
+    vko_matrix t;
+    vko_matrix_init_scale(&t, sx, sy);
+    vko_matrix_multiply(m, &t, m);
+}
+void vko_matrix_rotate(vko_matrix *m, float radians) {
+    vko_matrix t;
+    vko_matrix_init_rotate(&t, radians);
+    vko_matrix_multiply(m, &t, m);
+}
+void vko_matrix_transform_distance(const vko_matrix *m, float *dx, float *dy) {
+    float nx = (m->xx * *dx + m->xy * *dy);
+    float ny = (m->yx * *dx + m->yy * *dy);
+    *dx      = nx;
+    *dy      = ny;
+}
+void vko_matrix_transform_point(const vko_matrix *m, float *x, float *y) {
+    vko_matrix_transform_distance(m, x, y);
+    *x += m->x0;
+    *y += m->y0;
+}
+/* vkvg_matrix_invert, src/vkvg_matrix.c:107-148 */
+int vko_matrix_invert(vko_matrix *m) {
+    if (m->xy == 0. && m->yx == 0.) {
+        m->x0 = -m->x0;
+        m->y0 = -m->y0;
+        if (m->xx != 1.f) {
+            if (m->xx == 0.)
+                return VKO_STATUS_INVALID_MATRIX;
+            m->xx = 1.f / m->xx;
+            m->x0 *= m->xx;
+        }
+        if (m->yy != 1.f) {
+            if (m->yy == 0.)
+                return VKO_STATUS_INVALID_MATRIX;
+            m->yy = 1.f / m->yy;
+            m->y0 *= m->yy;
+        }
+        return VKO_STATUS_SUCCESS;
+    }
+    float det = m->xx * m->yy - m->yx * m->xy;
+    if (!(det * det >= 0.))
+        return VKO_STATUS_INVALID_MATRIX;
+    if (det == 0)
+        return VKO_STATUS_INVALID_MATRIX;
+    float a = m->xx, b = m->yx, c = m->xy, d = m->yy, tx = m->x0, ty = m->y0;
+    vko_matrix_init(m, d, -b, -c, a, c * ty - d * tx, b * tx - a * ty);
+    float s = 1 / det;
+    m->xx *= s;
+    m->yx *= s;
+    m->xy *= s;
+    m->yy *= s;
+    m->x0 *= s;
+    m->y0 *= s;
+    return VKO_STATUS_SUCCESS;
+}
+/* vkvg_matrix_get_scale, src/vkvg_matrix.c:222-229 (double sqrt) */
+void vko_matrix_get_scale(const vko_matrix *m, float *sx, float *sy) {
+    *sx = (float)sqrt(m->xx * m->xx + m->xy * m->xy);
+    *sy = (float)sqrt(m->yx * m->yx + m->yy * m->yy);
+}
+
+/* ---------------------------------------------------------------- surfaces */
+
+vko_surface *vko_surface_create(uint32_t width, uint32_t height, uint32_t samples) {
+    vko_surface *s = (vko_surface *)calloc(1, sizeof(vko_surface));
+    if (!s)
+        return NULL;
+    s->width   = width < 1 ? 1 : width;
+    s->height  = height < 1 ? 1 : height;
+    s->samples = samples == 4 ? 4 : 1;
+    s->refs    = 1;
+    size_t ns  = (size_t)s->width * s->height * s->samples;
+    s->data    = (uint8_t *)calloc(ns, 4);
+    s->stencil = (uint8_t *)calloc(ns, 1);
+    if (!s->data || !s->stencil)
+        s->status = VKO_STATUS_NO_MEMORY;
+    return s;
+}
+static void surface_release(vko_surface *s) {
+    if (!s)
+        return;
+    if (--s->refs > 0)
+        return;
+    free(s->data);
+    free(s->stencil);
+    free(s);
+}
+void     vko_surface_destroy(vko_surface *s) { surface_release(s); }
+int      vko_surface_status(vko_surface *s) { return s ? s->status : VKO_STATUS_NULL_POINTER; }
+uint32_t vko_surface_get_width(vko_surface *s) { return s ? s->width : 0; }
+uint32_t vko_surface_get_height(vko_surface *s) { return s ? s->height : 0; }
+void     vko_surface_clear(vko_surface *s) {
+    if (vko_surface_status(s))
+        return;
+    size_t ns = (size_t)s->width * s->height * s->samples;
+    memset(s->data, 0, ns * 4);
+    memset(s->stencil, 0, ns);
+}
+int vko_surface_read_samples(vko_surface *s, uint8_t *out) {
+    if (vko_surface_status(s) || !out)
+        return VKO_STATUS_INVALID_STATUS;
+    memcpy(out, s->data, (size_t)s->width * s->height * s->samples * 4);
+    return 0;
+}
+int vko_surface_resolve_premult(vko_surface *s, uint8_t *rgba) {
+    if (vko_surface_status(s) || !rgba)
+        return VKO_STATUS_INVALID_STATUS;
+    vko_resolve(s, rgba);
+    return 0;
+}
+/* vkvg_surface_write_to_memory, src/vkvg_surface.c:393-467: resolve, then
+   p = (uchar)(p / (a/255.f)) in double, truncating.  Where vkvg's conversion
+   is undefined (a == 0, or p > a) the oracle writes 0 / clamps to 255. */
+int vko_surface_write_to_memory(vko_surface *s, uint8_t *rgba) {
+    if (vko_surface_status(s))
+        return VKO_STATUS_INVALID_STATUS;
+    if (!rgba)
+        return VKO_STATUS_WRITE_ERROR;
+    vko_resolve(s, rgba);
+    for (size_t p = 0; p < (size_t)s->width * s->height; p++) {
+        uint8_t *q     = rgba + p * 4;
+        double   alpha = (double)q[3] / 255.f;
+        for (int c = 0; c < 3; c++) {
+            if (q[3] == 0) {
+                q[c] = 0;
+                continue;
+            }
+            double v = (double)q[c] / alpha;
+            q[c]     = v >= 255.0 ? 255 : (uint8_t)v;
+        }
+    }
+    return 0;
+}
+int vko_surface_write_to_png(vko_surface *s, const char *path) {
+    if (vko_surface_status(s))
+        return VKO_STATUS_INVALID_STATUS;
+    if (!path)
+        return VKO_STATUS_WRITE_ERROR;
+    uint8_t *img = (uint8_t *)malloc((size_t)s->width * s->height * 4);
+    if (!img)
+        return VKO_STATUS_NO_MEMORY;
+    vko_surface_write_to_memory(s, img);
+    int r = vko_png_write(path, s->width, s->height, img);
+    free(img);
+    return r ? VKO_STATUS_WRITE_ERROR : 0;
+}
+
+/* ---------------------------------------------------------------- contexts */
+
+/* defaults: _init_ctx, src/vkvg_context.c:24-70 */
+vko_context *vko_create(vko_surface *surf) {
+    if (vko_surface_status(surf))
+        return NULL;
+    vko_context *ctx = (vko_context *)calloc(1, sizeof(vko_context));
+    if (!ctx)
+        return NULL;
+    ctx->surf = surf;
+    surf->refs++;
+    ctx->line_width  = 1.f;
+    ctx->miter_limit = 10.f;
+    ctx->op          = VKO_OP_OVER;
+    ctx->fill_rule   = 1; /* NON_ZERO */
+    ctx->cur_color   = 0xff000000u;
+    ctx->opacity     = 1.0f;
+    vko_matrix_init_identity(&ctx->mat);
+    vko_ctx_init_geom(ctx);
+    return ctx;
+}
+int  vko_status(vko_context *ctx) { return ctx ? ctx->status : VKO_STATUS_NULL_POINTER; }
+void vko_keep_draws(vko_context *ctx, int keep) {
+    if (ctx)
+        ctx->keep_draws = keep;
+}
+/* rasterise pending draws in submission order */
+void vko_flush(vko_context *ctx) {
+    if (!ctx)
+        return;
+    for (uint32_t i = ctx->nrastered; i < ctx->ndraws; i++)
+        vko_raster_draw(ctx->surf, &ctx->draws[i]);
+    ctx->nrastered = ctx->ndraws;
+    if (!ctx->keep_draws) {
+        for (uint32_t i = 0; i < ctx->ndraws; i++)
+            vko_draw_free(&ctx->draws[i]);
+        ctx->ndraws = ctx->nrastered = 0;
+    }
+}
+void vko_destroy(vko_context *ctx) {
+    if (!ctx)
+        return;
+    vko_flush(ctx);
+    vko_surface *s = ctx->surf;
+    vko_ctx_free_geom(ctx);
+    free(ctx);
+    surface_release(s);
+}
+
+/* ------------------------------------------------------------------- state */
+
+static uint32_t clamp_byte(float v) {
+    if (!(v > 0.0f))
+        return 0;
+    if (v > 255.0f)
+        return 255;
+    return (uint32_t)v;
+}
+/* CreateRgbaf, src/vkvg_context_internal.h:59-62 (premultiplied, truncating;
+   the oracle clamps products outside [0,255] where vkvg's cast is undefined) */
+static uint32_t create_rgbaf(float r, float g, float b, float a) {
+    return (clamp_byte(a * 255.0f) << 24) | (clamp_byte(b * a * 255.0f) << 16) | (clamp_byte(g * a * 255.0f) << 8) |
+           clamp_byte(r * a * 255.0f);
+}
+void vko_set_source_rgba(vko_context *ctx, float r, float g, float b, float a) {
+    if (vko_status(ctx))
+        return;
+    ctx->cur_color = create_rgbaf(r, g, b, a);
+}
+void vko_set_source_rgb(vko_context *ctx, float r, float g, float b) {
+    if (vko_status(ctx))
+        return;
+    ctx->cur_color = create_rgbaf(r, g, b, 1);
+}
+void vko_set_source_color(vko_context *ctx, uint32_t c) {
+    if (vko_status(ctx))
+        return;
+    ctx->cur_color = c;
+}
+uint32_t vko_get_color(vko_context *ctx) { return ctx ? ctx->cur_color : 0; }
+void     vko_set_line_width(vko_context *ctx, float w) {
+    if (!vko_status(ctx))
+        ctx->line_width = w;
+}
+void vko_set_miter_limit(vko_context *ctx, float l) {
+    if (!vko_status(ctx))
+        ctx->miter_limit = l;
+}
+void vko_set_line_cap(vko_context *ctx, int cap) {
+    if (!vko_status(ctx))
+        ctx->line_cap = cap;
+}
+void vko_set_line_join(vko_context *ctx, int join) {
+    if (!vko_status(ctx))
+        ctx->line_join = join;
+}
+void vko_set_fill_rule(vko_context *ctx, int fr) {
+    if (!vko_status(ctx))
+        ctx->fill_rule = fr;
+}
+void vko_set_operator(vko_context *ctx, int op) {
+    if (!vko_status(ctx))
+        ctx->op = op;
+}
+/* vkvg_set_opacity, src/vkvg_context.c:305-315 */
+void vko_set_opacity(vko_context *ctx, float o) {
+    if (!vko_status(ctx))
+        ctx->opacity = o;
+}
+/* vkvg_set_dash, src/vkvg_context.c:1103-1115 (the array is copied) */
+void vko_set_dash(vko_context *ctx, const float *dashes, uint32_t n, float offset) {
+    if (vko_status(ctx))
+        return;
+    free(ctx->dashes);
+    ctx->dashes      = NULL;
+    ctx->dash_count  = n;
+    ctx->dash_offset = offset;
+    if (n == 0)
+        return;
+    ctx->dashes = (float *)malloc(sizeof(float) * n);
+    if (!ctx->dashes) {
+        ctx->status = VKO_STATUS_NO_MEMORY;
+        return;
+    }
+    memcpy(ctx->dashes, dashes, sizeof(float) * n);
+}
+void vko_set_matrix(vko_context *ctx, const vko_matrix *m) {
+    if (vko_status(ctx) || !m)
+        return;
+    ctx->mat = *m;
+}
+void vko_get_matrix(vko_context *ctx, vko_matrix *m) {
+    if (vko_status(ctx) || !m)
+        return;
+    *m = ctx->mat;
+}
+void vko_identity_matrix(vko_context *ctx) {
+    if (!vko_status(ctx))
+        vko_matrix_init_identity(&ctx->mat);
+}
+/* vkvg_translate / scale / rotate / transform, src/vkvg_context.c:1513-1559 */
+void vko_transform(vko_context *ctx, const vko_matrix *m) {
+    if (vko_status(ctx) || !m)
+        return;
+    vko_matrix r;
+    vko_matrix_multiply(&r, &ctx->mat, m);
+    ctx->mat = r;
+}
+void vko_translate(vko_context *ctx, float dx, float dy) {
+    if (!vko_status(ctx))
+        vko_matrix_translate(&ctx->mat, dx, dy);
+}
+void vko_scale(vko_context *ctx, float sx, float sy) {
+    if (!vko_status(ctx))
+        vko_matrix_scale(&ctx->mat, sx, sy);
+}
+void vko_rotate(vko_context *ctx, float r) {
+    if (!vko_status(ctx))
+        vko_matrix_rotate(&ctx->mat, r);
+}
+
+/* ------------------------------------------------------------- draw access */
+
+uint32_t vko_draw_count(vko_context *ctx) { return ctx ? ctx->ndraws : 0; }
+int      vko_draw_info(vko_context *ctx, uint32_t i, uint32_t *info) {
+    if (!ctx || i >= ctx->ndraws)
+        return -1;
+    vko_draw *d = &ctx->draws[i];
+    info[0]     = (uint32_t)d->kind;
+    info[1]     = d->npts;
+    info[2]     = d->nsub;
+    info[3]     = d->nverts;
+    info[4]     = d->ninds;
+    info[5]     = d->color;
+    info[6]     = (uint32_t)d->convex;
+    return 0;
+}
+int vko_draw_points(vko_context *ctx, uint32_t i, float *xy, uint32_t *sub_counts) {
+    if (!ctx || i >= ctx->ndraws)
+        return -1;
+    vko_draw *d = &ctx->draws[i];
+    if (xy && d->npts)
+        memcpy(xy, d->pts, (size_t)d->npts * 2 * sizeof(float));
+    if (sub_counts && d->nsub)
+        memcpy(sub_counts, d->sub_counts, (size_t)d->nsub * sizeof(uint32_t));
+    return 0;
+}
+int vko_draw_stroke(vko_context *ctx, uint32_t i, float *xy, uint32_t *inds) {
+    if (!ctx || i >= ctx->ndraws)
+        return -1;
+    vko_draw *d = &ctx->draws[i];
+    if (xy && d->nverts)
+        memcpy(xy, d->verts, (size_t)d->nverts * 2 * sizeof(float));
+    if (inds && d->ninds)
+        memcpy(inds, d->inds, (size_t)d->ninds * sizeof(uint32_t));
+    return 0;
+}
+int vko_draw_coverage(vko_context *ctx, uint32_t i, int mode, int32_t *out) {
+    if (!ctx || i >= ctx->ndraws || !out)
+        return -1;
+    vko_draw_coverage_impl(ctx->surf, &ctx->draws[i], mode, out);
+    return 0;
+}
+void vko_snap(vko_context *ctx, uint32_t i, float x, float y, int32_t *fx, int32_t *fy) {
+    const vko_matrix *m = (ctx && i < ctx->ndraws) ? &ctx->draws[i].mat : &ctx->mat;
+    vko_snap_point(m, ctx->surf->width, ctx->surf->height, x, y, fx, fy);
+}
+
+/* portable math evaluation: fn 0 atan2f, 1 acosf, 2 cosf, 3 sinf, 4 asinf, 5 atanf */
+void vko_pmath_eval(int fn, const float *a, const float *b, float *out, uint64_t n) {
+    for (uint64_t i = 0; i < n; i++) {
+        switch (fn) {
+        case 0:
+            out[i] = vko_pm_atan2f(a[i], b[i]);
+            break;
+        case 1:
+            out[i] = vko_pm_acosf(a[i]);
+            break;
+        case 2:
+            out[i] = vko_pm_cosf(a[i]);
+            break;
+        case 3:
+            out[i] = vko_pm_sinf(a[i]);
+            break;
+        case 4:
+            out[i] = vko_pm_asinf(a[i]);
+            break;
+        default:
+            out[i] = vko_pm_atanf(a[i]);
+            break;
+        }
+    }
+}

@@ -1,0 +1,135 @@
+/* Internal structures of the vko oracle (test infrastructure). */
+#ifndef VKO_INTERNAL_H
+#define VKO_INTERNAL_H
+
+#include "vko.h"
+#include "vko_pmath.h"
+
+#include <float.h>
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+/* path element bits, src/vkvg_internal.h:62-68 of vkvg */
+#define VKO_PATH_CLOSED_BIT     0x80000000u
+#define VKO_PATH_HAS_CURVES_BIT 0x40000000u
+#define VKO_PATH_IS_CONVEX_BIT  0x20000000u
+#define VKO_PATH_ELT_MASK       0x1FFFFFFFu
+
+#define VKO_EQUF(a, b) (fabsf((a) - (b)) <= FLT_EPSILON) /* src/vkvg_internal.h:72 */
+
+#define VKO_PIF   3.14159265358979323846f
+#define VKO_PIF_2 1.57079632679489661923f
+#define VKO_2_PIF 0.63661977236758134308f /* 2/pi: src/vkvg_internal.h:45 */
+
+/* vertex fixed point: 8 sub-pixel bits; clamp for far-away vertices */
+#define VKO_SUBPIX      256
+#define VKO_FIX_LIMIT   268435456.0f /* 2^28 units = 2^20 px */
+
+typedef struct {
+    float x, y;
+} v2;
+
+typedef struct {
+    int      kind;
+    int      op;
+    uint32_t color;
+    float    opacity;
+    vko_matrix mat;
+    /* fills */
+    uint32_t npts;
+    float   *pts;
+    uint32_t nsub;
+    uint32_t *sub_counts;
+    int      convex;
+    float    bounds[4];
+    /* strokes */
+    uint32_t nverts;
+    float   *verts;
+    uint32_t ninds;
+    uint32_t *inds;
+} vko_draw;
+
+struct vko_surface_t {
+    int      status;
+    uint32_t refs;
+    uint32_t width, height, samples;
+    uint8_t *data;    /* [y][x][s][4] premultiplied RGBA8 */
+    uint8_t *stencil; /* [y][x][s] */
+};
+
+struct vko_context_t {
+    int          status;
+    vko_surface *surf;
+
+    v2      *points;
+    uint32_t point_count, size_points;
+    uint32_t *pathes;
+    uint32_t path_ptr, segment_ptr, size_pathes;
+    uint32_t subpath_count;
+    int      simple_convex;
+
+    float    line_width, miter_limit;
+    uint32_t dash_count;
+    float    dash_offset;
+    float   *dashes;
+    int      op, line_cap, line_join, fill_rule;
+    uint32_t cur_color;
+    float    opacity;
+    vko_matrix mat;
+
+    /* stroke vertex / index emission buffers */
+    v2      *verts;
+    uint32_t nverts, cap_verts;
+    uint32_t *inds;
+    uint32_t ninds, cap_inds;
+
+    vko_draw *draws;
+    uint32_t  ndraws, cap_draws, nrastered;
+    int       keep_draws;
+};
+
+/* math dispatch */
+extern int vko_math_mode_g;
+static inline float VKO_ATAN2F(float y, float x) { return vko_math_mode_g ? atan2f(y, x) : vko_pm_atan2f(y, x); }
+static inline float VKO_ACOSF(float x) { return vko_math_mode_g ? acosf(x) : vko_pm_acosf(x); }
+static inline float VKO_COSF(float x) { return vko_math_mode_g ? cosf(x) : vko_pm_cosf(x); }
+static inline float VKO_SINF(float x) { return vko_math_mode_g ? sinf(x) : vko_pm_sinf(x); }
+static inline float VKO_POW2F(float x) { return vko_math_mode_g ? powf(x, 2) : x * x; }
+
+/* vec2 helpers, src/vectors.h:103-167 of vkvg */
+static inline v2    v2_add(v2 a, v2 b) { return (v2){a.x + b.x, a.y + b.y}; }
+static inline v2    v2_sub(v2 a, v2 b) { return (v2){a.x - b.x, a.y - b.y}; }
+static inline v2    v2_mul(v2 a, float m) { return (v2){a.x * m, a.y * m}; }
+static inline v2    v2_div(v2 a, float m) { return (v2){a.x / m, a.y / m}; }
+static inline float v2_len(v2 v) { return sqrtf(v.x * v.x + v.y * v.y); }
+static inline v2    v2_norm(v2 a) {
+    float m = sqrtf(a.x * a.x + a.y * a.y);
+    return (v2){a.x / m, a.y / m};
+}
+static inline v2 v2_line_norm(v2 a, v2 b) {
+    v2    d  = {b.x - a.x, b.y - a.y};
+    float md = sqrtf(d.x * d.x + d.y * d.y);
+    d.x /= md;
+    d.y /= md;
+    return d;
+}
+static inline v2    v2_perp(v2 a) { return (v2){a.y, -a.x}; }
+static inline float v2_dot(v2 a, v2 b) { return (a.x * b.x) + (a.y * b.y); }
+static inline int   v2_equ(v2 a, v2 b) { return VKO_EQUF(a.x, b.x) & VKO_EQUF(a.y, b.y); }
+
+/* geometry (vko_geom.c) */
+void vko_ctx_init_geom(vko_context *ctx);
+void vko_ctx_free_geom(vko_context *ctx);
+void vko_draw_free(vko_draw *d);
+
+/* raster (vko_raster.c) */
+void vko_raster_draw(vko_surface *surf, const vko_draw *d);
+void vko_draw_coverage_impl(const vko_surface *surf, const vko_draw *d, int mode, int32_t *out);
+void vko_snap_point(const vko_matrix *m, uint32_t w, uint32_t h, float x, float y, int32_t *fx, int32_t *fy);
+void vko_resolve(const vko_surface *surf, uint8_t *rgba);
+
+/* png (vko_png.c) */
+int vko_png_write(const char *path, uint32_t w, uint32_t h, const uint8_t *rgba);
+
+#endif

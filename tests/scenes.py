@@ -1,0 +1,103 @@
+"""Seeded synthetic scenes for the vkvg path hot path.
+
+A scene is a list of API calls ``(name, *args)`` that is replayed, call for
+call, on any object exposing vkvg's context methods (the GPU library's Python
+binding, or the CPU oracle).  Randomness comes from one splitmix64 stream per
+scene; ``rnd()`` returns (x >> 40) * 2**-24, a float in [0, 1) that is exactly
+representable in fp32, so the same scene is produced in C or Python.
+
+Scenes (sizes follow the benchmark configurations; no public dataset exists
+for this path, so seeded synthetic inputs stand in for real content):
+
+* ``plain_small`` - 512x512 RGBA8, MSAA 4, white background, 64 closed
+  polygons with n ~ U{3..32} vertices uniform in [0,512)^2 (self-intersecting
+  allowed), seed 0.  Each is filled NON_ZERO in an opaque U[0,1) RGB colour,
+  then stroked black at width 4, miter join (limit 10), butt cap.
+* ``curve_heavy`` - 1024x1024, MSAA 4, white background, 2048 closed paths of
+  n ~ U{4..64} cubic Beziers, control points uniform in [0,1024)^2, seed 1.
+  Path i is filled EVEN_ODD when i is even and NON_ZERO when odd, colour RGB
+  U[0,1) with alpha U[0.3,1); then stroked in a second such colour at width
+  U[1,8), join i mod 3 (miter/round/bevel), cap i mod 3 (butt/round/square),
+  dash [10, 5] offset 0 when i mod 4 == 0.
+"""
+
+MASK64 = (1 << 64) - 1
+
+
+class SplitMix64:
+    def __init__(self, seed):
+        self.s = seed & MASK64
+
+    def next(self):
+        self.s = (self.s + 0x9E3779B97F4A7C15) & MASK64
+        z = self.s
+        z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & MASK64
+        z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & MASK64
+        return z ^ (z >> 31)
+
+    def rnd(self):
+        return (self.next() >> 40) * (1.0 / 16777216.0)
+
+    def randint(self, lo, hi):
+        """uniform integer in [lo, hi]"""
+        return lo + int(self.rnd() * (hi - lo + 1))
+
+
+def plain_small(n_polys=64, size=512, seed=0):
+    r = SplitMix64(seed)
+    ops = [("set_source_rgb", 1.0, 1.0, 1.0), ("paint",)]
+    ops += [("set_line_width", 4.0), ("set_line_join", 0), ("set_line_cap", 0), ("set_miter_limit", 10.0),
+            ("set_fill_rule", 1)]
+    for _ in range(n_polys):
+        n = r.randint(3, 32)
+        pts = [(r.rnd() * size, r.rnd() * size) for _ in range(n)]
+        col = (r.rnd(), r.rnd(), r.rnd())
+        ops.append(("move_to",) + pts[0])
+        for p in pts[1:]:
+            ops.append(("line_to",) + p)
+        ops.append(("close_path",))
+        ops.append(("set_source_rgb",) + col)
+        ops.append(("fill_preserve",))
+        ops.append(("set_source_rgb", 0.0, 0.0, 0.0))
+        ops.append(("stroke",))
+    return {"name": "plain_small", "width": size, "height": size, "samples": 4, "ops": ops, "paths": n_polys}
+
+
+def curve_heavy(n_paths=2048, size=1024, seed=1, n_min=4, n_max=64):
+    r = SplitMix64(seed)
+    ops = [("set_source_rgb", 1.0, 1.0, 1.0), ("paint",), ("set_miter_limit", 10.0)]
+    for i in range(n_paths):
+        n = r.randint(n_min, n_max)
+        p0 = (r.rnd() * size, r.rnd() * size)
+        fill = (r.rnd(), r.rnd(), r.rnd(), 0.3 + 0.7 * r.rnd())
+        stroke = (r.rnd(), r.rnd(), r.rnd(), 0.3 + 0.7 * r.rnd())
+        width = 1.0 + 7.0 * r.rnd()
+        ops.append(("move_to",) + p0)
+        for k in range(n):
+            c1 = (r.rnd() * size, r.rnd() * size)
+            c2 = (r.rnd() * size, r.rnd() * size)
+            end = p0 if k == n - 1 else (r.rnd() * size, r.rnd() * size)
+            ops.append(("curve_to",) + c1 + c2 + end)
+        ops.append(("close_path",))
+        ops.append(("set_fill_rule", 0 if i % 2 == 0 else 1))
+        ops.append(("set_source_rgba",) + fill)
+        ops.append(("fill_preserve",))
+        ops.append(("set_line_width", width))
+        ops.append(("set_line_join", i % 3))
+        ops.append(("set_line_cap", i % 3))
+        ops.append(("set_dash", [10.0, 5.0] if i % 4 == 0 else [], 0.0))
+        ops.append(("set_source_rgba",) + stroke)
+        ops.append(("stroke",))
+    return {"name": "curve_heavy", "width": size, "height": size, "samples": 4, "ops": ops, "paths": n_paths}
+
+
+def play(ctx, ops):
+    """Replay a scene's calls on a context object with vkvg method names."""
+    for op in ops:
+        name, args = op[0], op[1:]
+        if name == "set_dash":
+            ctx.set_dash(args[0], args[1])
+        elif name == "set_matrix":
+            ctx.set_matrix(args[0])
+        else:
+            getattr(ctx, name)(*args)
