@@ -311,6 +311,10 @@ static void curve_to_i(vko_context *ctx, float x1, float y1, float x2, float y2,
     set_curve_start(ctx);
     if (path_empty(ctx))
         add_point(ctx, x1, y1);
+    if (path_empty(ctx)) { /* x1 or y1 NaN: vkvg would read a stale point; stop here */
+        set_curve_end(ctx);
+        return;
+    }
     v2    cp = cur_pos(ctx);
     float sx = 1, sy = 1;
     vko_matrix_get_scale(&ctx->mat, &sx, &sy);
@@ -514,9 +518,15 @@ void vko_quadratic_to(vko_context *ctx, float x1, float y1, float x2, float y2) 
         return;
     quadratic_to_i(ctx, x1, y1, x2, y2);
 }
+/* vkvg reads a stale point without a current point; like vkvg_rel_curve_to
+   the oracle reports VKO_STATUS_NO_CURRENT_POINT */
 void vko_rel_quadratic_to(vko_context *ctx, float x1, float y1, float x2, float y2) {
     if (vko_status(ctx))
         return;
+    if (path_empty(ctx)) {
+        ctx->status = VKO_STATUS_NO_CURRENT_POINT;
+        return;
+    }
     v2 cp = cur_pos(ctx);
     quadratic_to_i(ctx, cp.x + x1, cp.y + y1, cp.x + x2, cp.y + y2);
 }
@@ -531,7 +541,8 @@ int vko_rectangle(vko_context *ctx, float x, float y, float w, float h) {
     add_point(ctx, x + w, y);
     add_point(ctx, x + w, y + h);
     add_point(ctx, x, y + h);
-    ctx->pathes[ctx->path_ptr] |= (VKO_PATH_CLOSED_BIT | VKO_PATH_IS_CONVEX_BIT);
+    if (!path_empty(ctx)) /* vkvg flags an empty subpath here when the corners are NaN */
+        ctx->pathes[ctx->path_ptr] |= (VKO_PATH_CLOSED_BIT | VKO_PATH_IS_CONVEX_BIT);
     finish_path(ctx);
     return VKO_STATUS_SUCCESS;
 }
@@ -699,7 +710,8 @@ void vko_ellipse(vko_context *ctx, float radiusX, float radiusY, float x, float 
     add_point(ctx, bottomCenterX, bottomCenterY);
     curve_to_i(ctx, bottomRightX, bottomRightY, topRightX, topRightY, topCenterX, topCenterY);
     curve_to_i(ctx, topLeftX, topLeftY, bottomLeftX, bottomLeftY, bottomCenterX, bottomCenterY);
-    ctx->pathes[ctx->path_ptr] |= VKO_PATH_CLOSED_BIT;
+    if (!path_empty(ctx))
+        ctx->pathes[ctx->path_ptr] |= VKO_PATH_CLOSED_BIT;
     finish_path(ctx);
 }
 
@@ -752,6 +764,12 @@ void vko_path_extents(vko_context *ctx, float *x1, float *y1, float *x2, float *
 
 /* ----------------------------------------------------------------- strokes */
 
+/* vkvg's round-join / round-cap loops never end for a zero or negative arc
+   step (infinite or negative line width) and its dash walk never ends on an
+   infinite segment; the oracle bounds them with the caps the GPU kernels use. */
+#define VKO_ARC_LOOP_CAP  65536u
+#define VKO_DASH_LOOP_CAP (1u << 22)
+
 typedef struct {
     uint32_t iL, iR, cp;
     uint32_t firstIdx;
@@ -763,6 +781,7 @@ typedef struct {
     float    curDashOffset;
     float    totDashLength;
     v2       normal;
+    uint32_t nev; /* joins and caps emitted by this dashed subpath */
 } dash_ctx;
 
 /* _build_vb_step, src/vkvg_context_internal.c:924-1163.  Returns det < 0. */
@@ -907,14 +926,14 @@ static int build_vb_step(vko_context *ctx, stroke_ctx *str, int isCurve) {
                 a += VKO_PIF;
                 float a1 = a + alpha;
                 a -= str->arcStep;
-                while (a > a1) {
+                for (uint32_t it = 0; a > a1 && it < VKO_ARC_LOOP_CAP; it++) {
                     emit_vertex(ctx, (v2){VKO_COSF(a) * str->hw + p0.x, VKO_SINF(a) * str->hw + p0.y});
                     a -= str->arcStep;
                 }
             } else {
                 float a1 = a + alpha;
                 a += str->arcStep;
-                while (a < a1) {
+                for (uint32_t it = 0; a < a1 && it < VKO_ARC_LOOP_CAP; it++) {
                     emit_vertex(ctx, (v2){VKO_COSF(a) * str->hw + p0.x, VKO_SINF(a) * str->hw + p0.y});
                     a += str->arcStep;
                 }
@@ -958,7 +977,7 @@ static void draw_cap(vko_context *ctx, stroke_ctx *str, v2 p0, v2 n, int isStart
                 a = VKO_PIF - a;
             float a1 = a + VKO_PIF;
             a += str->arcStep;
-            while (a < a1) {
+            for (uint32_t it = 0; a < a1 && it < VKO_ARC_LOOP_CAP; it++) {
                 emit_vertex(ctx, (v2){VKO_COSF(a) * str->hw + p0.x, VKO_SINF(a) * str->hw + p0.y});
                 a += str->arcStep;
             }
@@ -986,7 +1005,7 @@ static void draw_cap(vko_context *ctx, stroke_ctx *str, v2 p0, v2 n, int isStart
                 a = VKO_PIF - a;
             float a1 = a - VKO_PIF;
             a -= str->arcStep;
-            while (a > a1) {
+            for (uint32_t it = 0; a > a1 && it < VKO_ARC_LOOP_CAP; it++) {
                 emit_vertex(ctx, (v2){VKO_COSF(a) * str->hw + p0.x, VKO_SINF(a) * str->hw + p0.y});
                 a -= str->arcStep;
             }
@@ -1000,14 +1019,17 @@ static void draw_cap(vko_context *ctx, stroke_ctx *str, v2 p0, v2 n, int isStart
 static void draw_dashed_segment(vko_context *ctx, stroke_ctx *str, dash_ctx *dc, int isCurve) {
     v2 p  = ctx->points[str->cp];
     v2 pR = ctx->points[str->iR];
-    if (!dc->dashOn)
+    if (!dc->dashOn) {
         build_vb_step(ctx, str, isCurve);
+        dc->nev++;
+    }
     v2 d                = v2_sub(pR, p);
     dc->normal          = v2_norm(d);
     float segmentLength = v2_len(d);
-    while (dc->curDashOffset < segmentLength) {
+    while (dc->curDashOffset < segmentLength && dc->nev < VKO_DASH_LOOP_CAP) {
         v2 p0 = v2_add(p, v2_mul(dc->normal, dc->curDashOffset));
         draw_cap(ctx, str, p0, dc->normal, dc->dashOn);
+        dc->nev++;
         dc->dashOn ^= 1;
         dc->curDashOffset += ctx->dashes[dc->curDash];
         if (++dc->curDash == ctx->dash_count)

@@ -1,0 +1,323 @@
+"""GB300-native implementation of vkvg's path hot path.
+
+The product is the C-ABI shared library ``_build/libvkvg_gb300.so`` (declared
+in include/vkvg.h and include/vkvg_gb300.h).  This module loads it with
+ctypes and exposes thin object wrappers whose method names are vkvg's own
+(``ctx.move_to(x, y)`` calls ``vkvg_move_to(ctx, x, y)``).  There is no
+Python or CPU fallback: if the library is missing or no CUDA device is
+present, loading or device creation raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+LIB_PATH = _build.LIB
+_lib = None
+
+_F, _P, _U, _I, _B = C.c_float, C.c_void_p, C.c_uint32, C.c_int, C.c_bool
+
+# name -> (restype, argtypes); every vkvg_public function of include/*.h
+SIGNATURES = {
+    "vkvg_matrix_init_identity": (None, [_P]),
+    "vkvg_matrix_init": (None, [_P, _F, _F, _F, _F, _F, _F]),
+    "vkvg_matrix_init_translate": (None, [_P, _F, _F]),
+    "vkvg_matrix_init_scale": (None, [_P, _F, _F]),
+    "vkvg_matrix_init_rotate": (None, [_P, _F]),
+    "vkvg_matrix_translate": (None, [_P, _F, _F]),
+    "vkvg_matrix_scale": (None, [_P, _F, _F]),
+    "vkvg_matrix_rotate": (None, [_P, _F]),
+    "vkvg_matrix_multiply": (None, [_P, _P, _P]),
+    "vkvg_matrix_transform_distance": (None, [_P, _P, _P]),
+    "vkvg_matrix_transform_point": (None, [_P, _P, _P]),
+    "vkvg_matrix_invert": (_I, [_P]),
+    "vkvg_matrix_get_scale": (None, [_P, _P, _P]),
+    "vkvg_device_create": (_P, [_P]),
+    "vkvg_device_destroy": (None, [_P]),
+    "vkvg_device_status": (_I, [_P]),
+    "vkvg_device_reference": (_P, [_P]),
+    "vkvg_device_get_reference_count": (_U, [_P]),
+    "vkvg_device_set_dpy": (None, [_P, _I, _I]),
+    "vkvg_device_get_dpy": (None, [_P, _P, _P]),
+    "vkvg_device_set_context_cache_size": (None, [_P, _U]),
+    "vkvg_surface_create": (_P, [_P, _U, _U]),
+    "vkvg_surface_create_from_bitmap": (_P, [_P, _P, _U, _U]),
+    "vkvg_surface_status": (_I, [_P]),
+    "vkvg_surface_reference": (_P, [_P]),
+    "vkvg_surface_get_reference_count": (_U, [_P]),
+    "vkvg_surface_destroy": (None, [_P]),
+    "vkvg_surface_clear": (None, [_P]),
+    "vkvg_surface_get_width": (_U, [_P]),
+    "vkvg_surface_get_height": (_U, [_P]),
+    "vkvg_surface_write_to_png": (_I, [_P, C.c_char_p]),
+    "vkvg_surface_write_to_memory": (_I, [_P, _P]),
+    "vkvg_surface_resolve": (None, [_P]),
+    "vkvg_create": (_P, [_P]),
+    "vkvg_destroy": (None, [_P]),
+    "vkvg_status": (_I, [_P]),
+    "vkvg_status_to_string": (C.c_char_p, [_I]),
+    "vkvg_reference": (_P, [_P]),
+    "vkvg_get_reference_count": (_U, [_P]),
+    "vkvg_flush": (None, [_P]),
+    "vkvg_new_path": (None, [_P]),
+    "vkvg_close_path": (None, [_P]),
+    "vkvg_new_sub_path": (None, [_P]),
+    "vkvg_path_extents": (None, [_P, _P, _P, _P, _P]),
+    "vkvg_get_current_point": (None, [_P, _P, _P]),
+    "vkvg_line_to": (None, [_P, _F, _F]),
+    "vkvg_rel_line_to": (None, [_P, _F, _F]),
+    "vkvg_move_to": (None, [_P, _F, _F]),
+    "vkvg_rel_move_to": (None, [_P, _F, _F]),
+    "vkvg_arc": (None, [_P, _F, _F, _F, _F, _F]),
+    "vkvg_arc_negative": (None, [_P, _F, _F, _F, _F, _F]),
+    "vkvg_curve_to": (None, [_P, _F, _F, _F, _F, _F, _F]),
+    "vkvg_rel_curve_to": (None, [_P, _F, _F, _F, _F, _F, _F]),
+    "vkvg_quadratic_to": (None, [_P, _F, _F, _F, _F]),
+    "vkvg_rel_quadratic_to": (None, [_P, _F, _F, _F, _F]),
+    "vkvg_rectangle": (_I, [_P, _F, _F, _F, _F]),
+    "vkvg_rounded_rectangle": (_I, [_P, _F, _F, _F, _F, _F]),
+    "vkvg_rounded_rectangle2": (None, [_P, _F, _F, _F, _F, _F, _F]),
+    "vkvg_ellipse": (None, [_P, _F, _F, _F, _F, _F]),
+    "vkvg_elliptic_arc_to": (None, [_P, _F, _F, _B, _B, _F, _F, _F]),
+    "vkvg_rel_elliptic_arc_to": (None, [_P, _F, _F, _B, _B, _F, _F, _F]),
+    "vkvg_has_current_point": (_B, [_P]),
+    "vkvg_stroke": (None, [_P]),
+    "vkvg_stroke_preserve": (None, [_P]),
+    "vkvg_fill": (None, [_P]),
+    "vkvg_fill_preserve": (None, [_P]),
+    "vkvg_paint": (None, [_P]),
+    "vkvg_clear": (None, [_P]),
+    "vkvg_set_opacity": (None, [_P, _F]),
+    "vkvg_get_opacity": (_F, [_P]),
+    "vkvg_set_source_color": (None, [_P, _U]),
+    "vkvg_set_source_rgba": (None, [_P, _F, _F, _F, _F]),
+    "vkvg_set_source_rgb": (None, [_P, _F, _F, _F]),
+    "vkvg_set_line_width": (None, [_P, _F]),
+    "vkvg_set_miter_limit": (None, [_P, _F]),
+    "vkvg_get_miter_limit": (_F, [_P]),
+    "vkvg_set_line_cap": (None, [_P, _I]),
+    "vkvg_set_line_join": (None, [_P, _I]),
+    "vkvg_set_operator": (None, [_P, _I]),
+    "vkvg_set_fill_rule": (None, [_P, _I]),
+    "vkvg_set_dash": (None, [_P, _P, _U, _F]),
+    "vkvg_get_dash": (None, [_P, _P, _P, _P]),
+    "vkvg_get_line_width": (_F, [_P]),
+    "vkvg_get_line_cap": (_I, [_P]),
+    "vkvg_get_line_join": (_I, [_P]),
+    "vkvg_get_operator": (_I, [_P]),
+    "vkvg_get_fill_rule": (_I, [_P]),
+    "vkvg_get_target": (_P, [_P]),
+    "vkvg_translate": (None, [_P, _F, _F]),
+    "vkvg_scale": (None, [_P, _F, _F]),
+    "vkvg_rotate": (None, [_P, _F]),
+    "vkvg_transform": (None, [_P, _P]),
+    "vkvg_set_matrix": (None, [_P, _P]),
+    "vkvg_get_matrix": (None, [_P, _P]),
+    "vkvg_identity_matrix": (None, [_P]),
+    # vkvg_gb300.h
+    "vkvg_surface_get_device_ptr": (_P, [_P]),
+    "vkvg_surface_get_samples": (_U, [_P]),
+    "vkvg_gb300_frame_capture": (_P, [_P]),
+    "vkvg_gb300_frame_execute": (_I, [_P, _P]),
+    "vkvg_gb300_frame_stats": (_I, [_P, _P]),
+    "vkvg_gb300_frame_timing": (_I, [_P, _P]),
+    "vkvg_gb300_frame_destroy": (None, [_P]),
+    "vkvg_gb300_debug_capture": (None, [_P, _I]),
+    "vkvg_gb300_debug_counts": (_I, [_P, _P]),
+    "vkvg_gb300_debug_points": (_I, [_P, _P, _P]),
+    "vkvg_gb300_debug_subpaths": (_I, [_P, _P, _P, _P]),
+    "vkvg_gb300_debug_draw": (_I, [_P, _U, _P]),
+    "vkvg_gb300_debug_stroke": (_I, [_P, _U, _P, _P]),
+    "vkvg_gb300_debug_coverage": (_I, [_P, _U, _P]),
+    "vkvg_gb300_surface_read_samples": (_I, [_P, _P]),
+    "vkvg_gb300_surface_read_premult": (_I, [_P, _P]),
+    "vkvg_gb300_pmath_eval": (_I, [_I, _P, _P, _P, C.c_uint64, _I]),
+    "vkvg_gb300_kernel_launches": (C.c_uint64, []),
+}
+
+
+class Matrix(C.Structure):
+    _fields_ = [("xx", _F), ("yx", _F), ("xy", _F), ("yy", _F), ("x0", _F), ("y0", _F)]
+
+
+class DeviceCreateInfo(C.Structure):
+    _fields_ = [("samples", C.c_uint32), ("deferredResolve", C.c_bool), ("inst", _P), ("phy", _P),
+                ("vkdev", _P), ("qFamIdx", C.c_uint32), ("qIndex", C.c_uint32), ("threadAware", C.c_bool)]
+
+
+def lib():
+    """Load libvkvg_gb300.so; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError("libvkvg_gb300.so is missing (%s); run __graft_entry__.build() or "
+                               "python vkvg_gb300/build.py" % LIB_PATH)
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _ptr(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class VkvgError(RuntimeError):
+    pass
+
+
+class Device:
+    def __init__(self, samples=4, thread_aware=False):
+        L = lib()
+        info = DeviceCreateInfo(samples=samples, threadAware=thread_aware)
+        self.h = L.vkvg_device_create(C.byref(info))
+        st = L.vkvg_device_status(self.h)
+        if st:
+            raise VkvgError("vkvg_device_create failed: %s" % L.vkvg_status_to_string(st).decode())
+
+    def destroy(self):
+        if self.h:
+            lib().vkvg_device_destroy(self.h)
+            self.h = None
+
+
+class Surface:
+    def __init__(self, dev, width, height):
+        L = lib()
+        self.dev = dev
+        self.h = L.vkvg_surface_create(dev.h, width, height)
+        st = L.vkvg_surface_status(self.h)
+        if st:
+            raise VkvgError("vkvg_surface_create failed: %s" % L.vkvg_status_to_string(st).decode())
+        self.width, self.height = width, height
+        self.samples = L.vkvg_surface_get_samples(self.h)
+
+    def image(self):
+        """vkvg_surface_write_to_memory: resolved, unpremultiplied RGBA8."""
+        out = np.zeros((self.height, self.width, 4), np.uint8)
+        st = lib().vkvg_surface_write_to_memory(self.h, _ptr(out))
+        if st:
+            raise VkvgError("write_to_memory: %d" % st)
+        return out
+
+    def premult(self):
+        out = np.zeros((self.height, self.width, 4), np.uint8)
+        lib().vkvg_gb300_surface_read_premult(self.h, _ptr(out))
+        return out
+
+    def samples_rgba(self):
+        out = np.zeros((self.height, self.width, self.samples, 4), np.uint8)
+        lib().vkvg_gb300_surface_read_samples(self.h, _ptr(out))
+        return out
+
+    def write_png(self, path):
+        return lib().vkvg_surface_write_to_png(self.h, path.encode())
+
+    def context(self):
+        return Context(self)
+
+    def destroy(self):
+        if self.h:
+            lib().vkvg_surface_destroy(self.h)
+            self.h = None
+
+
+class Context:
+    """vkvg context; unknown attributes map to vkvg_<name>(ctx, ...)."""
+
+    def __init__(self, surf):
+        self.L = lib()
+        self.surf = surf
+        self.h = self.L.vkvg_create(surf.h)
+        st = self.L.vkvg_status(self.h)
+        if st:
+            raise VkvgError("vkvg_create failed: %d" % st)
+
+    def __getattr__(self, name):
+        fn = getattr(self.L, "vkvg_" + name)
+        return lambda *a: fn(self.h, *a)
+
+    def set_dash(self, dashes, offset):
+        arr = np.asarray(dashes, dtype=np.float32)
+        self.L.vkvg_set_dash(self.h, _ptr(arr) if len(arr) else None, len(arr), offset)
+
+    def set_matrix(self, m):
+        mm = Matrix(*m)
+        self.L.vkvg_set_matrix(self.h, C.byref(mm))
+
+    def current_point(self):
+        x, y = C.c_float(), C.c_float()
+        self.L.vkvg_get_current_point(self.h, C.byref(x), C.byref(y))
+        return x.value, y.value
+
+    def debug_capture(self, on=True):
+        self.L.vkvg_gb300_debug_capture(self.h, 1 if on else 0)
+
+    def debug_counts(self):
+        out = np.zeros(8, np.uint32)
+        self.L.vkvg_gb300_debug_counts(self.h, _ptr(out))
+        return out
+
+    def debug_points(self):
+        n = int(self.debug_counts()[1])
+        xy = np.zeros((max(n, 1), 2), np.float32)
+        fl = np.zeros(max(n, 1), np.uint8)
+        self.L.vkvg_gb300_debug_points(self.h, _ptr(xy), _ptr(fl))
+        return xy[:n], fl[:n]
+
+    def debug_subpaths(self):
+        n = int(self.debug_counts()[0])
+        a = np.zeros(max(n, 1), np.uint32)
+        b = np.zeros(max(n, 1), np.uint32)
+        c = np.zeros(max(n, 1), np.uint32)
+        self.L.vkvg_gb300_debug_subpaths(self.h, _ptr(a), _ptr(b), _ptr(c))
+        return a[:n], b[:n], c[:n]
+
+    def debug_draw(self, i):
+        info = np.zeros(8, np.uint32)
+        st = self.L.vkvg_gb300_debug_draw(self.h, i, _ptr(info))
+        if st:
+            raise VkvgError("debug_draw %d: %d" % (i, st))
+        return info
+
+    def debug_stroke(self, i):
+        info = self.debug_draw(i)
+        nv, ni = int(info[3]), int(info[4])
+        v = np.zeros((max(nv, 1), 2), np.float32)
+        ix = np.zeros(max(ni, 1), np.uint32)
+        st = self.L.vkvg_gb300_debug_stroke(self.h, i, _ptr(v), _ptr(ix))
+        if st:
+            raise VkvgError("debug_stroke %d: %d" % (i, st))
+        return v[:nv], ix[:ni]
+
+    def debug_coverage(self, i):
+        s = self.surf
+        out = np.zeros((s.height, s.width, s.samples), np.int32)
+        st = self.L.vkvg_gb300_debug_coverage(self.h, i, _ptr(out))
+        if st:
+            raise VkvgError("debug_coverage %d: %d" % (i, st))
+        return out
+
+    def destroy(self):
+        if self.h:
+            self.L.vkvg_destroy(self.h)
+            self.h = None
+
+
+def kernel_launches():
+    return int(lib().vkvg_gb300_kernel_launches())
+
+
+def pmath(fn, a, b=None, device=False):
+    a = np.ascontiguousarray(a, np.float32)
+    b = np.ascontiguousarray(a if b is None else b, np.float32)
+    out = np.empty_like(a)
+    st = lib().vkvg_gb300_pmath_eval(fn, _ptr(a), _ptr(b), _ptr(out), a.size, 1 if device else 0)
+    if st:
+        raise VkvgError("pmath_eval: %d" % st)
+    return out

@@ -1,0 +1,82 @@
+/*
+ * Record layouts shared by the host recorder and the sm_103a kernels.
+ *
+ * A flush ships one "frame" of recorded work to the device as structure-of-
+ * arrays command buffers:
+ *   segments  - one record per path element (point, cubic, arc, elliptic arc)
+ *   subpaths  - contiguous runs of segments, with the closed flag
+ *   draws     - fill / stroke / paint / clear calls in submission order
+ *   pairs     - (draw, subpath) work items of stroke and fill draws
+ * and the kernels expand them: flatten -> stroke expansion -> edge setup and
+ * band binning -> per-band coverage and compositing.
+ */
+#ifndef VKVG_GB300_TYPES_H
+#define VKVG_GB300_TYPES_H
+
+#include <stdint.h>
+
+/* segment kinds (low 4 bits of seg_info) */
+#define GB_SEG_POINT   1u /* one explicit point (move_to, line_to, rectangle corner, arc end point) */
+#define GB_SEG_CUBIC   2u /* adaptive Bezier subdivision + end point */
+#define GB_SEG_ARC     3u /* fixed-step circular arc, seg_n loop points */
+#define GB_SEG_ELLIPSE 4u /* elliptic arc, seg_n points at host-walked angles */
+#define GB_SEG_KIND(i) ((i) & 0xFu)
+/* segment flags */
+#define GB_SEG_CURVED    0x100u /* emitted points lie in a curve segment (curve joins in strokes) */
+#define GB_SEG_DROP_LAST 0x200u /* close_path removed this segment's last point */
+
+/* subpath flags */
+#define GB_SUB_CLOSED 0x1u
+
+/* draw kinds */
+#define GB_DRAW_FILL_EO 0u
+#define GB_DRAW_FILL_NZ 1u
+#define GB_DRAW_STROKE  2u
+#define GB_DRAW_PAINT   3u
+#define GB_DRAW_CLEAR   4u
+
+/* operators (vkvg_operator_t) */
+#define GB_OP_CLEAR      0u
+#define GB_OP_SOURCE     1u
+#define GB_OP_OVER       2u
+#define GB_OP_DIFFERENCE 3u
+
+/* one recorded draw call */
+typedef struct {
+    uint32_t kind;
+    uint32_t op;
+    uint32_t join; /* vkvg_line_join_t */
+    uint32_t cap;  /* vkvg_line_cap_t */
+    uint32_t src;  /* premultiplied RGBA8 source after opacity, byte 0 = R */
+    uint32_t sub_first, sub_count;
+    uint32_t dash_first, dash_count;
+    float    dash_offset;
+    float    hw;       /* line width / 2 */
+    float    lh_max;   /* miter limit * line width */
+    float    arc_step; /* _get_arc_step(hw) under the draw's CTM */
+    float    mat[6];   /* xx yx xy yy x0 y0 */
+    uint32_t pad;
+} gb_draw;
+
+/* stroke event kinds (dashed strokes materialise their events) */
+#define GB_EV_JOIN      0u /* _build_vb_step at cp with (iL, iR) */
+#define GB_EV_CAP_START 1u
+#define GB_EV_CAP_END   2u
+#define GB_EV_CLOSE     3u /* closing join of a closed, undashed subpath (+ index patch) */
+#define GB_EV_NONE      4u
+
+typedef struct {
+    uint32_t kind; /* GB_EV_* | curved << 8 */
+    uint32_t cp, iL, iR;
+    float    px, py, nx, ny; /* cap position and direction */
+} gb_event;
+
+/* bands: 16 sample rows (4 pixel rows at 4x MSAA, 16 at 1x) */
+#define GB_BAND_ROWS 16
+#define GB_TILE_W    256
+
+/* device status word bits */
+#define GB_ERR_CURVE_LIMIT 0x1u /* a cubic exceeded the subdivision work cap */
+#define GB_ERR_OVERFLOW    0x2u
+
+#endif

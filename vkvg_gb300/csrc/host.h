@@ -1,0 +1,159 @@
+/*
+ * Host-side structures of the GB300 vkvg library: device, surface, context,
+ * the per-context path recorder and the kernel pipeline.
+ */
+#ifndef VKVG_GB300_HOST_H
+#define VKVG_GB300_HOST_H
+
+#include "../../include/vkvg.h"
+#include "../../include/vkvg_gb300.h"
+#include "gb_types.h"
+
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <mutex>
+#include <stdint.h>
+#include <string.h>
+#include <vector>
+
+struct f4 {
+    float x, y, z, w;
+};
+
+/* one frame of recorded work, as host structure-of-arrays */
+struct FrameHost {
+    std::vector<uint32_t> seg_info, seg_n, seg_aux;
+    std::vector<f4>       seg_a, seg_b, seg_c;
+    std::vector<uint32_t> sub_seg0, sub_nseg, sub_flags;
+    std::vector<gb_draw>  draws;
+    std::vector<uint32_t> spair_draw, spair_sub, spair_dfirst;
+    std::vector<uint32_t> sdraw_id, sdraw_pair0; /* per stroke draw (+ sentinel in pair0) */
+    std::vector<uint32_t> fpair_draw, fpair_sub;
+    std::vector<float>    dashes, thetas;
+    uint32_t              paths = 0; /* fill + stroke draws */
+    bool                  any_dash = false;
+    void                  clear();
+    bool                  empty() const { return draws.empty(); }
+};
+
+/* grow-only device buffer */
+struct DevBuf {
+    void  *p   = nullptr;
+    size_t cap = 0;
+    bool   grow(size_t bytes);
+    void   release();
+    template <class T> T *as() const { return (T *)p; }
+};
+struct PinnedBuf {
+    void  *p   = nullptr;
+    size_t cap = 0;
+    bool   grow(size_t bytes);
+    void   release();
+};
+
+struct Pipeline {
+    cudaStream_t st = nullptr;
+    DevBuf       in;
+    DevBuf       seg_cnt, seg_off, scratch, pts, pflag, sub_pt0, sub_npts;
+    DevBuf       ev_cnt, ev_off, events, cnt_v, cnt_i, off_v, off_i, verts, inds, ev_ret;
+    DevBuf       fe_cnt, fe_off, edges, edge_draw;
+    DevBuf       sdraw_tri0, sdraw_vbase, tri_a, tri_b, tri_draw;
+    DevBuf       cells, cursor, refs, status, dbg;
+    PinnedBuf    staging, rb;
+    cudaEvent_t  evs[8] = {};
+    /* offsets of the uploaded arrays inside `in` */
+    size_t o_seg_info, o_seg_a, o_seg_b, o_seg_c, o_seg_n, o_seg_aux, o_sub_seg0, o_sub_nseg, o_sub_flags, o_draws,
+        o_spd, o_sps, o_spf, o_sdid, o_sdp0, o_fpd, o_fps, o_dashes, o_thetas;
+    bool     uploaded = false;
+    /* sizes of the last run */
+    uint32_t nseg = 0, nsub = 0, ndraw = 0, nspair = 0, nsdraw = 0, nfpair = 0;
+    uint32_t npts = 0, nev = 0, nverts = 0, ninds = 0, nedges = 0, ntris = 0, nrefs = 0, nbands = 0;
+    uint32_t dev_status = 0;
+    uint64_t launches   = 0;
+    float    ms[4]      = {0, 0, 0, 0};
+
+    bool init();
+    void destroy();
+    /* upload a frame's host arrays (one copy) */
+    cudaError_t upload(const FrameHost &f);
+    /* run the uploaded frame on a surface */
+    cudaError_t run(const FrameHost &f, struct _vkvg_surface_t *surf, bool timing);
+    /* K1 only: flatten the uploaded segments (for vkvg_path_extents) */
+    cudaError_t flatten_only();
+};
+
+struct _vkvg_device_t {
+    vkvg_status_t status;
+    uint32_t      refs;
+    uint32_t      samples;
+    int           cuda_dev;
+    bool          thread_aware;
+    int           hdpi, vdpi;
+    std::mutex    mtx;
+};
+
+struct _vkvg_surface_t {
+    vkvg_status_t status;
+    uint32_t      refs;
+    VkvgDevice    dev;
+    uint32_t      width, height, samples, wpad, nrows, nbands;
+    uint32_t     *d_samples; /* [nrows][wpad] premultiplied RGBA8 */
+    uint32_t     *d_rgba;    /* [height][width] resolved */
+    std::mutex    mtx;
+};
+
+/* reference path state of the open subpath (vkvg's points/pathes arrays,
+   src/vkvg_context_internal.c:132-238, with flattened counts kept symbolic) */
+struct PathState {
+    uint32_t path_sub0 = 0; /* first subpath of the current path */
+    bool     open      = false;
+    uint32_t seg0      = 0;
+    uint32_t exact     = 0; /* points of non-cubic segments */
+    uint32_t ncubic    = 0; /* finite cubics: each adds >= 3 points */
+    float    fx = 0, fy = 0, lx = 0, ly = 0;
+    bool     closed       = false;
+    bool     pending      = false; /* a curve segment is open */
+    uint32_t pending_from = 0;
+};
+
+struct _vkvg_context_t {
+    vkvg_status_t status;
+    uint32_t      refs;
+    VkvgSurface   surf;
+    VkvgDevice    dev;
+
+    /* drawing state (vkvg _init_ctx defaults, src/vkvg_context.c:24-70) */
+    float              line_width  = 1.f;
+    float              miter_limit = 10.f;
+    vkvg_line_cap_t    line_cap    = VKVG_LINE_CAP_BUTT;
+    vkvg_line_join_t   line_join   = VKVG_LINE_JOIN_MITER;
+    vkvg_fill_rule_t   fill_rule   = VKVG_FILL_RULE_NON_ZERO;
+    vkvg_operator_t    op          = VKVG_OPERATOR_OVER;
+    uint32_t           cur_color   = 0xff000000u;
+    float              opacity     = 1.0f;
+    vkvg_matrix_t      mat         = {1, 0, 0, 1, 0, 0};
+    std::vector<float> dashes;
+    float              dash_offset = 0;
+
+    PathState ps;
+    FrameHost frame;
+    Pipeline  pl;
+    bool      debug    = false;
+    bool      have_run = false;
+};
+
+struct _vkvg_gb300_frame_t {
+    FrameHost frame;
+    Pipeline  pl;
+    uint32_t  width, height, samples;
+};
+
+/* pipeline entry used by flush and frame execution */
+vkvg_status_t gb_run_frame(Pipeline &pl, const FrameHost &f, VkvgSurface surf, bool upload, bool timing);
+void          gb_count_launch(uint64_t n);
+/* premultiplied source word after opacity (fragment stage + UNORM8 output) */
+uint32_t gb_source_word(uint32_t color, float opacity);
+int      gb_png_write(const char *path, uint32_t w, uint32_t h, const uint8_t *rgba);
+
+#endif

@@ -1,0 +1,87 @@
+/* Kernel launch entry points (defined in the .cu units). */
+#ifndef VKVG_GB300_LAUNCH_H
+#define VKVG_GB300_LAUNCH_H
+
+#include "gb_types.h"
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+
+struct gb_raster_args {
+    uint32_t        W, H, S, Wpad, nrows, nbands, ndraws, draw_first;
+    uint32_t        init_mode, init_color;
+    const gb_draw  *draws;
+    const uint32_t *cell_off; /* band-major (band * ndraws + draw) offsets, nbands*ndraws + 1 */
+    const uint32_t *refs;
+    const int4     *edges;
+    const int4     *tri_a;
+    const int4     *tri_b;
+    uint32_t       *samples; /* [nrows][Wpad] */
+    uint32_t       *rgba;    /* [H][W] */
+    int32_t        *cov_out; /* debug coverage output [H][W][S] or null */
+    uint32_t        cov_draw;
+};
+
+extern "C" {
+size_t      gb_scan_scratch_words(uint32_t n);
+cudaError_t gb_exclusive_scan(cudaStream_t st, const uint32_t *in, uint32_t n, uint32_t *out, uint32_t *scratch);
+
+cudaError_t gb_launch_flatten_count(cudaStream_t st, uint32_t nseg, const uint32_t *info, const float4 *a,
+                                    const float4 *b, const float4 *c, const uint32_t *n, const uint32_t *aux,
+                                    const float *thetas, uint32_t *counts, uint32_t *status);
+cudaError_t gb_launch_flatten_emit(cudaStream_t st, uint32_t nseg, const uint32_t *info, const float4 *a,
+                                   const float4 *b, const float4 *c, const uint32_t *n, const uint32_t *aux,
+                                   const float *thetas, const uint32_t *offsets, float2 *pts, uint8_t *pflag);
+cudaError_t gb_launch_subpath_ranges(cudaStream_t st, uint32_t nsub, const uint32_t *sub_seg0,
+                                     const uint32_t *sub_nseg, const uint32_t *seg_off, uint32_t *sub_pt0,
+                                     uint32_t *sub_npts);
+
+cudaError_t gb_launch_stroke_pair_events(cudaStream_t st, uint32_t npairs, const uint32_t *pair_draw,
+                                         const uint32_t *pair_sub, const gb_draw *draws, const uint32_t *sub_pt0,
+                                         const uint32_t *sub_npts, const uint32_t *sub_flags, const float2 *pts,
+                                         const uint8_t *pflag, const float *dashes, uint32_t *counts);
+cudaError_t gb_launch_stroke_dash_events(cudaStream_t st, uint32_t npairs, const uint32_t *pair_draw,
+                                         const uint32_t *pair_sub, const gb_draw *draws, const uint32_t *sub_pt0,
+                                         const uint32_t *sub_npts, const uint32_t *sub_flags, const float2 *pts,
+                                         const uint8_t *pflag, const float *dashes, const uint32_t *ev_off,
+                                         gb_event *events);
+cudaError_t gb_launch_stroke_event_count(cudaStream_t st, uint32_t nev, uint32_t npairs, const uint32_t *ev_off,
+                                         const uint32_t *pair_draw, const uint32_t *pair_sub, const gb_draw *draws,
+                                         const uint32_t *sub_pt0, const uint32_t *sub_npts, const uint32_t *sub_flags,
+                                         const float2 *pts, const uint8_t *pflag, const gb_event *events,
+                                         uint32_t *cnt_v, uint32_t *cnt_i);
+cudaError_t gb_launch_stroke_event_emit(cudaStream_t st, uint32_t nev, uint32_t npairs, const uint32_t *ev_off,
+                                        const uint32_t *pair_draw, const uint32_t *pair_sub, const gb_draw *draws,
+                                        const uint32_t *sub_pt0, const uint32_t *sub_npts, const uint32_t *sub_flags,
+                                        const float2 *pts, const uint8_t *pflag, const gb_event *events,
+                                        const uint32_t *off_v, const uint32_t *off_i, const uint32_t *pair_dfirst,
+                                        float2 *verts, uint32_t *inds, uint8_t *ev_ret);
+cudaError_t gb_launch_stroke_close_patch(cudaStream_t st, uint32_t ndraw_s, const uint32_t *draw_pair0,
+                                         const uint32_t *pair_sub, const gb_draw *draws, const uint32_t *pair_draw,
+                                         const uint32_t *sub_npts, const uint32_t *sub_flags, const uint32_t *ev_off,
+                                         const uint32_t *off_v, const uint32_t *off_i, const uint8_t *ev_ret,
+                                         uint32_t *inds);
+cudaError_t gb_launch_stroke_draw_bases(cudaStream_t st, uint32_t ndraw_s, const uint32_t *draw_pair0,
+                                        const uint32_t *ev_off, const uint32_t *off_v, const uint32_t *off_i,
+                                        uint32_t *draw_tri0, uint32_t *draw_vbase);
+
+cudaError_t gb_launch_fill_pair_edges(cudaStream_t st, uint32_t npairs, const uint32_t *pair_sub,
+                                      const uint32_t *sub_npts, uint32_t *counts);
+cudaError_t gb_launch_fill_edges(cudaStream_t st, uint32_t nedges, uint32_t npairs, const uint32_t *e_off,
+                                 const uint32_t *pair_draw, const uint32_t *pair_sub, const gb_draw *draws,
+                                 const uint32_t *sub_pt0, const uint32_t *sub_npts, const float2 *pts, uint32_t W,
+                                 uint32_t H, int4 *edges, uint32_t *edge_draw);
+cudaError_t gb_launch_stroke_tris(cudaStream_t st, uint32_t ntris, uint32_t ndraw_s, const uint32_t *draw_tri0,
+                                  const uint32_t *sdraw_id, const uint32_t *draw_vbase, const gb_draw *draws,
+                                  const float2 *verts, const uint32_t *inds, uint32_t W, uint32_t H, int4 *tri_a,
+                                  int4 *tri_b, uint32_t *tri_draw);
+cudaError_t gb_launch_bin(cudaStream_t st, int scatter, uint32_t nedges, const int4 *edges, const uint32_t *edge_draw,
+                          uint32_t ntris, const int4 *tri_a, const int4 *tri_b, const uint32_t *tri_draw,
+                          uint32_t ndraws, uint32_t W, uint32_t samples, uint32_t nrows, uint32_t *cell,
+                          uint32_t *edge_refs, uint32_t *tri_refs, uint32_t nrefs);
+
+cudaError_t gb_launch_raster(cudaStream_t st, const gb_raster_args *a);
+cudaError_t gb_launch_pmath_eval(cudaStream_t st, int fn, const float *a, const float *b, float *out, uint64_t n);
+}
+
+#endif

@@ -1,0 +1,411 @@
+/*
+ * Frame pipeline: upload the recorded structure-of-arrays command buffers in
+ * one copy, then run K1 flatten -> K2 stroke expansion -> K3 setup and band
+ * binning -> K5 coverage/compositing on the context's stream.  Output sizes
+ * are read back after each count+scan step (four small device->host reads
+ * per frame); buffers only grow.
+ */
+#include "host.h"
+#include "launch.h"
+
+#include <algorithm>
+#include <cstdio>
+
+static std::atomic<uint64_t> g_launches{0};
+void                         gb_count_launch(uint64_t n) { g_launches += n; }
+extern "C" uint64_t          vkvg_gb300_kernel_launches(void) { return g_launches.load(); }
+
+void FrameHost::clear() {
+    seg_info.clear();
+    seg_n.clear();
+    seg_aux.clear();
+    seg_a.clear();
+    seg_b.clear();
+    seg_c.clear();
+    sub_seg0.clear();
+    sub_nseg.clear();
+    sub_flags.clear();
+    draws.clear();
+    spair_draw.clear();
+    spair_sub.clear();
+    spair_dfirst.clear();
+    sdraw_id.clear();
+    sdraw_pair0.clear();
+    fpair_draw.clear();
+    fpair_sub.clear();
+    dashes.clear();
+    thetas.clear();
+    paths    = 0;
+    any_dash = false;
+}
+
+bool DevBuf::grow(size_t bytes) {
+    if (bytes <= cap)
+        return true;
+    size_t nc = std::max(bytes + bytes / 4, (size_t)4096);
+    if (p)
+        cudaFree(p);
+    p   = nullptr;
+    cap = 0;
+    if (cudaMalloc(&p, nc) != cudaSuccess) {
+        p = nullptr;
+        return false;
+    }
+    cap = nc;
+    return true;
+}
+void DevBuf::release() {
+    if (p)
+        cudaFree(p);
+    p   = nullptr;
+    cap = 0;
+}
+bool PinnedBuf::grow(size_t bytes) {
+    if (bytes <= cap)
+        return true;
+    size_t nc = std::max(bytes + bytes / 4, (size_t)4096);
+    if (p)
+        cudaFreeHost(p);
+    p   = nullptr;
+    cap = 0;
+    if (cudaHostAlloc(&p, nc, cudaHostAllocDefault) != cudaSuccess) {
+        p = nullptr;
+        return false;
+    }
+    cap = nc;
+    return true;
+}
+void PinnedBuf::release() {
+    if (p)
+        cudaFreeHost(p);
+    p   = nullptr;
+    cap = 0;
+}
+
+bool Pipeline::init() {
+    if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess)
+        return false;
+    for (auto &e : evs)
+        if (cudaEventCreate(&e) != cudaSuccess)
+            return false;
+    return rb.grow(256) && status.grow(64);
+}
+void Pipeline::destroy() {
+    if (st)
+        cudaStreamSynchronize(st);
+    DevBuf *bufs[] = {&in,     &seg_cnt, &seg_off,   &scratch,    &pts,         &pflag,    &sub_pt0, &sub_npts,
+                      &ev_cnt, &ev_off,  &events,    &cnt_v,      &cnt_i,       &off_v,    &off_i,   &verts,
+                      &inds,   &ev_ret,  &fe_cnt,    &fe_off,     &edges,       &edge_draw, &sdraw_tri0,
+                      &sdraw_vbase, &tri_a, &tri_b, &tri_draw, &cells,   &cursor,   &refs,    &status, &dbg};
+    for (DevBuf *b : bufs)
+        b->release();
+    staging.release();
+    rb.release();
+    for (auto &e : evs)
+        if (e)
+            cudaEventDestroy(e);
+    if (st)
+        cudaStreamDestroy(st);
+    st = nullptr;
+}
+
+template <class T> static size_t put(uint8_t *base, size_t &o, const std::vector<T> &v) {
+    o           = (o + 255) & ~(size_t)255;
+    size_t here = o;
+    if (!v.empty() && base)
+        memcpy(base + o, v.data(), v.size() * sizeof(T));
+    o += v.size() * sizeof(T) + sizeof(T); /* one spare element for sentinels */
+    return here;
+}
+
+cudaError_t Pipeline::upload(const FrameHost &f) {
+    size_t o = 0;
+    /* sizing pass, then copy into pinned staging */
+    for (int pass = 0; pass < 2; pass++) {
+        uint8_t *b = pass ? (uint8_t *)staging.p : nullptr;
+        o          = 0;
+        o_seg_info = put(b, o, f.seg_info);
+        o_seg_a    = put(b, o, f.seg_a);
+        o_seg_b    = put(b, o, f.seg_b);
+        o_seg_c    = put(b, o, f.seg_c);
+        o_seg_n    = put(b, o, f.seg_n);
+        o_seg_aux  = put(b, o, f.seg_aux);
+        o_sub_seg0 = put(b, o, f.sub_seg0);
+        o_sub_nseg = put(b, o, f.sub_nseg);
+        o_sub_flags = put(b, o, f.sub_flags);
+        o_draws    = put(b, o, f.draws);
+        o_spd      = put(b, o, f.spair_draw);
+        o_sps      = put(b, o, f.spair_sub);
+        o_spf      = put(b, o, f.spair_dfirst);
+        o_sdid     = put(b, o, f.sdraw_id);
+        o_sdp0     = put(b, o, f.sdraw_pair0);
+        o_fpd      = put(b, o, f.fpair_draw);
+        o_fps      = put(b, o, f.fpair_sub);
+        o_dashes   = put(b, o, f.dashes);
+        o_thetas   = put(b, o, f.thetas);
+        if (pass == 0) {
+            if (!staging.grow(o) || !in.grow(o))
+                return cudaErrorMemoryAllocation;
+        }
+    }
+    nseg   = (uint32_t)f.seg_info.size();
+    nsub   = (uint32_t)f.sub_seg0.size();
+    ndraw  = (uint32_t)f.draws.size();
+    nspair = (uint32_t)f.spair_draw.size();
+    nsdraw = (uint32_t)f.sdraw_id.size();
+    nfpair = (uint32_t)f.fpair_draw.size();
+    cudaError_t e = cudaMemcpyAsync(in.p, staging.p, o, cudaMemcpyHostToDevice, st);
+    uploaded      = e == cudaSuccess;
+    return e;
+}
+
+#define CK(x)                                                                                                          \
+    do {                                                                                                               \
+        cudaError_t _e = (x);                                                                                          \
+        if (_e != cudaSuccess)                                                                                         \
+            return _e;                                                                                                 \
+    } while (0)
+
+static cudaError_t readback_u32(Pipeline &pl, const uint32_t *dptr, uint32_t *out, int n) {
+    CK(cudaMemcpyAsync(pl.rb.p, dptr, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost, pl.st));
+    CK(cudaStreamSynchronize(pl.st));
+    memcpy(out, pl.rb.p, sizeof(uint32_t) * n);
+    return cudaSuccess;
+}
+static cudaError_t scan(Pipeline &pl, const uint32_t *in, uint32_t n, uint32_t *out) {
+    if (!pl.scratch.grow(gb_scan_scratch_words(n) * 4 + 64))
+        return cudaErrorMemoryAllocation;
+    gb_count_launch(n ? 3 : 0);
+    return gb_exclusive_scan(pl.st, in, n, out, pl.scratch.as<uint32_t>());
+}
+#define GROW(buf, bytes)                                                                                               \
+    do {                                                                                                               \
+        if (!(buf).grow(bytes))                                                                                        \
+            return cudaErrorMemoryAllocation;                                                                          \
+    } while (0)
+
+cudaError_t Pipeline::run(const FrameHost &f, _vkvg_surface_t *surf, bool timing) {
+    const uint8_t *I        = (const uint8_t *)in.p;
+    auto           U        = [&](size_t o) { return (const uint32_t *)(I + o); };
+    const uint32_t *seg_inf = U(o_seg_info);
+    const float4   *sa = (const float4 *)(I + o_seg_a), *sb = (const float4 *)(I + o_seg_b),
+                 *sc = (const float4 *)(I + o_seg_c);
+    const gb_draw *draws = (const gb_draw *)(I + o_draws);
+    const float   *dsh   = (const float *)(I + o_dashes);
+    const float   *th    = (const float *)(I + o_thetas);
+    uint32_t       hv[4];
+
+    CK(cudaMemsetAsync(status.p, 0, 16, st));
+    if (timing)
+        CK(cudaEventRecord(evs[0], st));
+
+    /* ---------------- K1 flatten */
+    GROW(seg_cnt, (size_t)(nseg + 1) * 4);
+    GROW(seg_off, (size_t)(nseg + 1) * 4);
+    CK(gb_launch_flatten_count(st, nseg, seg_inf, sa, sb, sc, U(o_seg_n), U(o_seg_aux), th, seg_cnt.as<uint32_t>(),
+                               status.as<uint32_t>()));
+    gb_count_launch(nseg ? 1 : 0);
+    CK(scan(*this, seg_cnt.as<uint32_t>(), nseg, seg_off.as<uint32_t>()));
+    CK(readback_u32(*this, seg_off.as<uint32_t>() + nseg, hv, 1));
+    npts = hv[0];
+    GROW(pts, (size_t)(npts + 1) * 8);
+    GROW(pflag, (size_t)(npts + 1));
+    GROW(sub_pt0, (size_t)(nsub + 1) * 4);
+    GROW(sub_npts, (size_t)(nsub + 1) * 4);
+    CK(gb_launch_flatten_emit(st, nseg, seg_inf, sa, sb, sc, U(o_seg_n), U(o_seg_aux), th, seg_off.as<uint32_t>(),
+                              pts.as<float2>(), pflag.as<uint8_t>()));
+    CK(gb_launch_subpath_ranges(st, nsub, U(o_sub_seg0), U(o_sub_nseg), seg_off.as<uint32_t>(),
+                                sub_pt0.as<uint32_t>(), sub_npts.as<uint32_t>()));
+    gb_count_launch((nseg ? 1 : 0) + (nsub ? 1 : 0));
+    if (timing)
+        CK(cudaEventRecord(evs[1], st));
+
+    /* ---------------- K2 stroke expansion; fill edge counts alongside */
+    GROW(ev_cnt, (size_t)(nspair + 1) * 4);
+    GROW(ev_off, (size_t)(nspair + 1) * 4);
+    GROW(fe_cnt, (size_t)(nfpair + 1) * 4);
+    GROW(fe_off, (size_t)(nfpair + 1) * 4);
+    CK(gb_launch_stroke_pair_events(st, nspair, U(o_spd), U(o_sps), draws, sub_pt0.as<uint32_t>(),
+                                    sub_npts.as<uint32_t>(), U(o_sub_flags), pts.as<float2>(), pflag.as<uint8_t>(),
+                                    dsh, ev_cnt.as<uint32_t>()));
+    CK(gb_launch_fill_pair_edges(st, nfpair, U(o_fps), sub_npts.as<uint32_t>(), fe_cnt.as<uint32_t>()));
+    gb_count_launch((nspair ? 1 : 0) + (nfpair ? 1 : 0));
+    CK(scan(*this, ev_cnt.as<uint32_t>(), nspair, ev_off.as<uint32_t>()));
+    CK(scan(*this, fe_cnt.as<uint32_t>(), nfpair, fe_off.as<uint32_t>()));
+    CK(cudaMemcpyAsync(rb.p, ev_off.as<uint32_t>() + nspair, 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync((uint8_t *)rb.p + 4, fe_off.as<uint32_t>() + nfpair, 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    memcpy(hv, rb.p, 8);
+    nev    = hv[0];
+    nedges = hv[1];
+    GROW(events, (size_t)(f.any_dash ? nev + 1 : 1) * sizeof(gb_event));
+    if (f.any_dash) {
+        CK(gb_launch_stroke_dash_events(st, nspair, U(o_spd), U(o_sps), draws, sub_pt0.as<uint32_t>(),
+                                        sub_npts.as<uint32_t>(), U(o_sub_flags), pts.as<float2>(),
+                                        pflag.as<uint8_t>(), dsh, ev_off.as<uint32_t>(), events.as<gb_event>()));
+        gb_count_launch(1);
+    }
+    GROW(cnt_v, (size_t)(nev + 1) * 4);
+    GROW(cnt_i, (size_t)(nev + 1) * 4);
+    GROW(off_v, (size_t)(nev + 1) * 4);
+    GROW(off_i, (size_t)(nev + 1) * 4);
+    CK(gb_launch_stroke_event_count(st, nev, nspair, ev_off.as<uint32_t>(), U(o_spd), U(o_sps), draws,
+                                    sub_pt0.as<uint32_t>(), sub_npts.as<uint32_t>(), U(o_sub_flags), pts.as<float2>(),
+                                    pflag.as<uint8_t>(), events.as<gb_event>(), cnt_v.as<uint32_t>(),
+                                    cnt_i.as<uint32_t>()));
+    gb_count_launch(nev ? 1 : 0);
+    CK(scan(*this, cnt_v.as<uint32_t>(), nev, off_v.as<uint32_t>()));
+    CK(scan(*this, cnt_i.as<uint32_t>(), nev, off_i.as<uint32_t>()));
+    CK(cudaMemcpyAsync(rb.p, off_v.as<uint32_t>() + nev, 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync((uint8_t *)rb.p + 4, off_i.as<uint32_t>() + nev, 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    memcpy(hv, rb.p, 8);
+    nverts = hv[0];
+    ninds  = hv[1];
+    ntris  = ninds / 3;
+    GROW(verts, (size_t)(nverts + 1) * 8);
+    GROW(inds, (size_t)(ninds + 1) * 4);
+    GROW(ev_ret, (size_t)(nev + 1));
+    CK(gb_launch_stroke_event_emit(st, nev, nspair, ev_off.as<uint32_t>(), U(o_spd), U(o_sps), draws,
+                                   sub_pt0.as<uint32_t>(), sub_npts.as<uint32_t>(), U(o_sub_flags), pts.as<float2>(),
+                                   pflag.as<uint8_t>(), events.as<gb_event>(), off_v.as<uint32_t>(),
+                                   off_i.as<uint32_t>(), U(o_spf), verts.as<float2>(), inds.as<uint32_t>(),
+                                   ev_ret.as<uint8_t>()));
+    CK(gb_launch_stroke_close_patch(st, nsdraw, U(o_sdp0), U(o_sps), draws, U(o_spd), sub_npts.as<uint32_t>(),
+                                    U(o_sub_flags), ev_off.as<uint32_t>(), off_v.as<uint32_t>(), off_i.as<uint32_t>(),
+                                    ev_ret.as<uint8_t>(), inds.as<uint32_t>()));
+    GROW(sdraw_tri0, (size_t)(nsdraw + 1) * 4);
+    GROW(sdraw_vbase, (size_t)(nsdraw + 1) * 4);
+    if (nsdraw)
+        CK(gb_launch_stroke_draw_bases(st, nsdraw, U(o_sdp0), ev_off.as<uint32_t>(), off_v.as<uint32_t>(),
+                                       off_i.as<uint32_t>(), sdraw_tri0.as<uint32_t>(), sdraw_vbase.as<uint32_t>()));
+    gb_count_launch((nev ? 1 : 0) + (nsdraw ? 2 : 0));
+    if (timing)
+        CK(cudaEventRecord(evs[2], st));
+
+    /* ---------------- K3 primitive setup + binning */
+    const uint32_t W = surf->width, H = surf->height, S = surf->samples;
+    GROW(edges, (size_t)(nedges + 1) * 16);
+    GROW(edge_draw, (size_t)(nedges + 1) * 4);
+    GROW(tri_a, (size_t)(ntris + 1) * 16);
+    GROW(tri_b, (size_t)(ntris + 1) * 16);
+    GROW(tri_draw, (size_t)(ntris + 1) * 4);
+    CK(gb_launch_fill_edges(st, nedges, nfpair, fe_off.as<uint32_t>(), U(o_fpd), U(o_fps), draws,
+                            sub_pt0.as<uint32_t>(), sub_npts.as<uint32_t>(), pts.as<float2>(), W, H, edges.as<int4>(),
+                            edge_draw.as<uint32_t>()));
+    CK(gb_launch_stroke_tris(st, ntris, nsdraw, sdraw_tri0.as<uint32_t>(), U(o_sdid), sdraw_vbase.as<uint32_t>(),
+                             draws, verts.as<float2>(), inds.as<uint32_t>(), W, H, tri_a.as<int4>(), tri_b.as<int4>(),
+                             tri_draw.as<uint32_t>()));
+    gb_count_launch((nedges ? 1 : 0) + (ntris ? 1 : 0));
+    nbands          = surf->nbands;
+    size_t ncells   = (size_t)nbands * ndraw;
+    GROW(cells, (ncells + 1) * 4);
+    GROW(cursor, (ncells + 1) * 4);
+    CK(cudaMemsetAsync(cells.p, 0, (ncells + 1) * 4, st));
+    CK(gb_launch_bin(st, 0, nedges, edges.as<int4>(), edge_draw.as<uint32_t>(), ntris, tri_a.as<int4>(),
+                     tri_b.as<int4>(), tri_draw.as<uint32_t>(), ndraw, W, S, surf->nrows, cells.as<uint32_t>(),
+                     nullptr, nullptr, 0u));
+    gb_count_launch((nedges ? 1 : 0) + (ntris ? 1 : 0));
+    CK(scan(*this, cells.as<uint32_t>(), (uint32_t)ncells, cursor.as<uint32_t>()));
+    CK(readback_u32(*this, cursor.as<uint32_t>() + ncells, hv, 1));
+    nrefs = hv[0];
+    GROW(refs, (size_t)(nrefs + 1) * 4);
+    /* cells <- offsets (kept for the raster), cursor <- running copy */
+    CK(cudaMemcpyAsync(cells.p, cursor.p, (ncells + 1) * 4, cudaMemcpyDeviceToDevice, st));
+    CK(gb_launch_bin(st, 1, nedges, edges.as<int4>(), edge_draw.as<uint32_t>(), ntris, tri_a.as<int4>(),
+                     tri_b.as<int4>(), tri_draw.as<uint32_t>(), ndraw, W, S, surf->nrows, cursor.as<uint32_t>(),
+                     refs.as<uint32_t>(), refs.as<uint32_t>(), nrefs));
+    gb_count_launch((nedges ? 1 : 0) + (ntris ? 1 : 0));
+    if (timing)
+        CK(cudaEventRecord(evs[3], st));
+
+    /* ---------------- K5 coverage + compositing */
+    gb_raster_args A;
+    memset(&A, 0, sizeof(A));
+    A.W = W;
+    A.H = H;
+    A.S = S;
+    A.Wpad       = surf->wpad;
+    A.nrows      = surf->nrows;
+    A.nbands     = nbands;
+    A.ndraws     = ndraw;
+    A.draw_first = 0;
+    A.init_mode  = 0;
+    if (ndraw > 0) {
+        const gb_draw &d0 = f.draws[0];
+        if (d0.kind == GB_DRAW_CLEAR) {
+            A.init_mode  = 1;
+            A.init_color = 0;
+            A.draw_first = 1;
+        } else if (d0.kind == GB_DRAW_PAINT && (d0.op == GB_OP_OVER || d0.op == GB_OP_SOURCE) &&
+                   (d0.src >> 24) == 255u) {
+            A.init_mode  = 1;
+            A.init_color = d0.src;
+            A.draw_first = 1;
+        }
+    }
+    A.draws    = draws;
+    A.cell_off = cells.as<uint32_t>();
+    A.refs     = refs.as<uint32_t>();
+    A.edges    = edges.as<int4>();
+    A.tri_a    = tri_a.as<int4>();
+    A.tri_b    = tri_b.as<int4>();
+    A.samples  = surf->d_samples;
+    A.rgba     = surf->d_rgba;
+    CK(gb_launch_raster(st, &A));
+    gb_count_launch(1);
+    if (timing)
+        CK(cudaEventRecord(evs[4], st));
+    CK(cudaMemcpyAsync(rb.p, status.p, 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    dev_status = *(uint32_t *)rb.p;
+    if (timing)
+        for (int i = 0; i < 4; i++)
+            cudaEventElapsedTime(&ms[i], evs[i], evs[i + 1]);
+    return cudaGetLastError();
+}
+
+cudaError_t Pipeline::flatten_only() {
+    const uint8_t  *I = (const uint8_t *)in.p;
+    auto            U = [&](size_t o) { return (const uint32_t *)(I + o); };
+    const float4   *sa = (const float4 *)(I + o_seg_a), *sb = (const float4 *)(I + o_seg_b),
+                 *sc = (const float4 *)(I + o_seg_c);
+    const float    *th = (const float *)(I + o_thetas);
+    uint32_t        hv[1];
+    CK(cudaMemsetAsync(status.p, 0, 16, st));
+    GROW(seg_cnt, (size_t)(nseg + 1) * 4);
+    GROW(seg_off, (size_t)(nseg + 1) * 4);
+    CK(gb_launch_flatten_count(st, nseg, U(o_seg_info), sa, sb, sc, U(o_seg_n), U(o_seg_aux), th,
+                               seg_cnt.as<uint32_t>(), status.as<uint32_t>()));
+    CK(scan(*this, seg_cnt.as<uint32_t>(), nseg, seg_off.as<uint32_t>()));
+    CK(readback_u32(*this, seg_off.as<uint32_t>() + nseg, hv, 1));
+    npts = hv[0];
+    GROW(pts, (size_t)(npts + 1) * 8);
+    GROW(pflag, (size_t)(npts + 1));
+    GROW(sub_pt0, (size_t)(nsub + 1) * 4);
+    GROW(sub_npts, (size_t)(nsub + 1) * 4);
+    CK(gb_launch_flatten_emit(st, nseg, U(o_seg_info), sa, sb, sc, U(o_seg_n), U(o_seg_aux), th,
+                              seg_off.as<uint32_t>(), pts.as<float2>(), pflag.as<uint8_t>()));
+    CK(gb_launch_subpath_ranges(st, nsub, U(o_sub_seg0), U(o_sub_nseg), seg_off.as<uint32_t>(),
+                                sub_pt0.as<uint32_t>(), sub_npts.as<uint32_t>()));
+    gb_count_launch((nseg ? 2 : 0) + (nsub ? 1 : 0));
+    return cudaStreamSynchronize(st);
+}
+
+vkvg_status_t gb_run_frame(Pipeline &pl, const FrameHost &f, VkvgSurface surf, bool do_upload, bool timing) {
+    if (f.empty())
+        return VKVG_STATUS_SUCCESS;
+    std::lock_guard<std::mutex> lk(surf->mtx);
+    if (do_upload || !pl.uploaded) {
+        if (pl.upload(f) != cudaSuccess)
+            return VKVG_STATUS_DEVICE_ERROR;
+    }
+    cudaError_t e = pl.run(f, surf, timing);
+    if (e == cudaErrorMemoryAllocation)
+        return VKVG_STATUS_NO_MEMORY;
+    if (e != cudaSuccess) {
+        fprintf(stderr, "vkvg_gb300: CUDA error %s\n", cudaGetErrorString(e));
+        return VKVG_STATUS_DEVICE_ERROR;
+    }
+    return VKVG_STATUS_SUCCESS;
+}

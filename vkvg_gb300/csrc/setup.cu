@@ -1,0 +1,264 @@
+/*
+ * K3 - primitive setup and band binning on sm_103a.
+ *
+ * Fill draws become directed polygon edges (each subpath with more than two
+ * points, closed by its implicit last edge, as vkvg's triangle fan and
+ * glutess contour are); stroke draws become positively oriented triangles
+ * from vkvg's own vertex/index buffers.  Every vertex goes through vkvg's
+ * vertex stage (shaders/vkvg_main.vert:74-79: p' = CTM p, ndc = p'*2/size - 1)
+ * and the viewport transform, then is snapped to 8 sub-pixel bits (round to
+ * nearest even).  This unit is built with -fmad=false so the float steps match
+ * the CPU restatement exactly.
+ *
+ * Binning: the surface is cut into bands of 16 sample rows.  Each primitive is
+ * counted into (band, draw) cells, an exclusive scan in band-major order gives
+ * every band a contiguous, draw-ordered list, and a scatter pass writes the
+ * primitive indices.
+ */
+#include "gb_types.h"
+
+#include <cuda_runtime.h>
+
+#define GB_FIX_LIMIT 268435456.0f /* 2^28 units = 2^20 px */
+
+__device__ __forceinline__ int32_t gb_to_fixed(float v) {
+    float s = v * 256.0f;
+    if (s != s)
+        return 0;
+    if (!(s > -GB_FIX_LIMIT))
+        s = -GB_FIX_LIMIT;
+    if (!(s < GB_FIX_LIMIT))
+        s = GB_FIX_LIMIT;
+    return __float2int_rn(s);
+}
+struct gb_vp {
+    float xx, yx, xy, yy, x0, y0, w, h, hw, hh;
+};
+__device__ __forceinline__ gb_vp make_vp(const gb_draw &d, uint32_t W, uint32_t H) {
+    gb_vp v;
+    v.xx = d.mat[0];
+    v.yx = d.mat[1];
+    v.xy = d.mat[2];
+    v.yy = d.mat[3];
+    v.x0 = d.mat[4];
+    v.y0 = d.mat[5];
+    v.w  = (float)W;
+    v.h  = (float)H;
+    v.hw = (float)W * 0.5f;
+    v.hh = (float)H * 0.5f;
+    return v;
+}
+__device__ __forceinline__ int2 gb_snap(const gb_vp &m, float2 p, bool *finite) {
+    float px = (m.xx * p.x + m.xy * p.y) + m.x0;
+    float py = (m.yx * p.x + m.yy * p.y) + m.y0;
+    if (finite)
+        *finite = !(px != px || py != py);
+    float nx = (px * 2.0f) / m.w - 1.0f;
+    float ny = (py * 2.0f) / m.h - 1.0f;
+    return make_int2(gb_to_fixed(nx * m.hw + m.hw), gb_to_fixed(ny * m.hh + m.hh));
+}
+
+__device__ __forceinline__ uint32_t gb_find(const uint32_t *__restrict__ off, uint32_t n, uint32_t e) {
+    uint32_t lo = 0, hi = n;
+    while (hi - lo > 1) {
+        uint32_t mid = (lo + hi) >> 1;
+        if (off[mid] <= e)
+            lo = mid;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+/* edges per fill (draw, subpath) pair */
+__global__ void gb_fill_pair_edges(uint32_t npairs, const uint32_t *__restrict__ pair_sub,
+                                   const uint32_t *__restrict__ sub_npts, uint32_t *__restrict__ counts) {
+    uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= npairs)
+        return;
+    uint32_t n = sub_npts[pair_sub[p]];
+    counts[p]  = n > 2 ? n : 0;
+}
+/* snapped directed edges; edge j of a subpath joins point j to point j+1 (mod n) */
+__global__ void gb_fill_edges(uint32_t nedges, uint32_t npairs, const uint32_t *__restrict__ e_off,
+                              const uint32_t *__restrict__ pair_draw, const uint32_t *__restrict__ pair_sub,
+                              const gb_draw *__restrict__ draws, const uint32_t *__restrict__ sub_pt0,
+                              const uint32_t *__restrict__ sub_npts, const float2 *__restrict__ pts, uint32_t W,
+                              uint32_t H, int4 *__restrict__ edges, uint32_t *__restrict__ edge_draw) {
+    uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= nedges)
+        return;
+    uint32_t p = gb_find(e_off, npairs, e);
+    uint32_t s = pair_sub[p], d = pair_draw[p];
+    uint32_t j = e - e_off[p], n = sub_npts[s], first = sub_pt0[s];
+    gb_vp    m = make_vp(draws[d], W, H);
+    int2     a = gb_snap(m, pts[first + j], nullptr);
+    int2     b = gb_snap(m, pts[first + (j + 1 == n ? 0 : j + 1)], nullptr);
+    edges[e]     = make_int4(a.x, a.y, b.x, b.y);
+    edge_draw[e] = d;
+}
+/* snapped, positively oriented stroke triangles; degenerate or non-finite
+   triangles are marked with w = 0 */
+__global__ void gb_stroke_tris(uint32_t ntris, uint32_t ndraw_s, const uint32_t *__restrict__ draw_tri0,
+                               const uint32_t *__restrict__ sdraw_id, const uint32_t *__restrict__ draw_vbase,
+                               const gb_draw *__restrict__ draws, const float2 *__restrict__ verts,
+                               const uint32_t *__restrict__ inds, uint32_t W, uint32_t H, int4 *__restrict__ tri_a,
+                               int4 *__restrict__ tri_b, uint32_t *__restrict__ tri_draw) {
+    uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ntris)
+        return;
+    uint32_t k  = gb_find(draw_tri0, ndraw_s, t);
+    uint32_t d  = sdraw_id[k];
+    gb_vp    m  = make_vp(draws[d], W, H);
+    uint32_t vb = draw_vbase[k], nv = draw_vbase[k + 1] - vb;
+    uint32_t i0 = inds[3 * t], i1 = inds[3 * t + 1], i2 = inds[3 * t + 2];
+    bool     inb = i0 < nv && i1 < nv && i2 < nv;
+    if (!inb)
+        i0 = i1 = i2 = 0;
+    bool     f0, f1, f2;
+    int2     a  = gb_snap(m, verts[vb + i0], &f0);
+    int2     b  = gb_snap(m, verts[vb + i1], &f1);
+    int2     c  = gb_snap(m, verts[vb + i2], &f2);
+    long long area = (long long)(b.x - a.x) * (long long)(c.y - a.y) - (long long)(c.x - a.x) * (long long)(b.y - a.y);
+    int valid = (inb && f0 && f1 && f2 && area != 0) ? 1 : 0;
+    if (area < 0) {
+        int2 tmp = b;
+        b        = c;
+        c        = tmp;
+    }
+    tri_a[t]    = make_int4(a.x, a.y, b.x, b.y);
+    tri_b[t]    = make_int4(c.x, c.y, valid, 0);
+    tri_draw[t] = d;
+}
+
+/* sample-row range [r0, r1] crossed by the half-open y interval [ylo, yhi) */
+__device__ __forceinline__ void gb_row_range(int32_t ylo, int32_t yhi, uint32_t samples, int32_t *r0, int32_t *r1) {
+    long long off  = samples == 4 ? 32 : 128;
+    long long step = samples == 4 ? 64 : 256;
+    long long a = (long long)ylo - off, b = (long long)yhi - off;
+    /* ceil(a / step) */
+    long long ca = a >= 0 ? (a + step - 1) / step : -((-a) / step);
+    long long cb = b >= 0 ? (b + step - 1) / step : -((-b) / step);
+    *r0          = (int32_t)(ca < -2147483647LL ? -2147483647LL : ca);
+    *r1          = (int32_t)((cb - 1) > 2147483647LL ? 2147483647LL : cb - 1);
+}
+
+/* band range of a primitive, or false if it can touch no sample */
+__device__ __forceinline__ bool gb_prim_bands(int32_t ylo, int32_t yhi, int32_t xmin, int32_t xmax, bool is_tri,
+                                              uint32_t W, uint32_t samples, uint32_t nrows, uint32_t *b0,
+                                              uint32_t *b1) {
+    if (yhi <= ylo)
+        return false;
+    int32_t r0, r1;
+    gb_row_range(ylo, yhi, samples, &r0, &r1);
+    if (r0 < 0)
+        r0 = 0;
+    if (r1 > (int32_t)nrows - 1)
+        r1 = (int32_t)nrows - 1;
+    if (r0 > r1)
+        return false;
+    /* a crossing left of every sample adds nothing; a triangle right of every
+       sample covers nothing (an edge there still adds to whole rows) */
+    if (xmax < 32)
+        return false;
+    if (is_tri && (long long)xmin > (long long)W * 256)
+        return false;
+    *b0 = (uint32_t)r0 / GB_BAND_ROWS;
+    *b1 = (uint32_t)r1 / GB_BAND_ROWS;
+    return true;
+}
+
+template <bool SCATTER>
+__global__ void gb_bin_edges(uint32_t nedges, const int4 *__restrict__ edges, const uint32_t *__restrict__ edge_draw,
+                             uint32_t ndraws, uint32_t W, uint32_t samples, uint32_t nrows,
+                             uint32_t *__restrict__ cell, uint32_t *__restrict__ refs, uint32_t nrefs) {
+    uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= nedges)
+        return;
+    int4     ed = edges[e];
+    uint32_t b0, b1;
+    int32_t  ylo = min(ed.y, ed.w), yhi = max(ed.y, ed.w);
+    if (!gb_prim_bands(ylo, yhi, min(ed.x, ed.z), max(ed.x, ed.z), false, W, samples, nrows, &b0, &b1))
+        return;
+    uint32_t d = edge_draw[e];
+    for (uint32_t b = b0; b <= b1; b++) {
+        uint32_t slot = atomicAdd(&cell[(size_t)b * ndraws + d], 1u);
+        if (SCATTER && slot < nrefs)
+            refs[slot] = e;
+    }
+}
+template <bool SCATTER>
+__global__ void gb_bin_tris(uint32_t ntris, const int4 *__restrict__ tri_a, const int4 *__restrict__ tri_b,
+                            const uint32_t *__restrict__ tri_draw, uint32_t ndraws, uint32_t W, uint32_t samples,
+                            uint32_t nrows, uint32_t *__restrict__ cell, uint32_t *__restrict__ refs,
+                            uint32_t nrefs) {
+    uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ntris)
+        return;
+    int4 a = tri_a[t], b = tri_b[t];
+    if (!b.z)
+        return;
+    int32_t  ylo = min(min(a.y, a.w), b.y), yhi = max(max(a.y, a.w), b.y);
+    int32_t  xlo = min(min(a.x, a.z), b.x), xhi = max(max(a.x, a.z), b.x);
+    uint32_t b0, b1;
+    if (!gb_prim_bands(ylo, yhi, xlo, xhi, true, W, samples, nrows, &b0, &b1))
+        return;
+    uint32_t d = tri_draw[t];
+    for (uint32_t bb = b0; bb <= b1; bb++) {
+        uint32_t slot = atomicAdd(&cell[(size_t)bb * ndraws + d], 1u);
+        if (SCATTER && slot < nrefs)
+            refs[slot] = t;
+    }
+}
+
+extern "C" {
+cudaError_t gb_launch_fill_pair_edges(cudaStream_t st, uint32_t npairs, const uint32_t *pair_sub,
+                                      const uint32_t *sub_npts, uint32_t *counts) {
+    if (!npairs)
+        return cudaSuccess;
+    gb_fill_pair_edges<<<(npairs + 255) / 256, 256, 0, st>>>(npairs, pair_sub, sub_npts, counts);
+    return cudaGetLastError();
+}
+cudaError_t gb_launch_fill_edges(cudaStream_t st, uint32_t nedges, uint32_t npairs, const uint32_t *e_off,
+                                 const uint32_t *pair_draw, const uint32_t *pair_sub, const gb_draw *draws,
+                                 const uint32_t *sub_pt0, const uint32_t *sub_npts, const float2 *pts, uint32_t W,
+                                 uint32_t H, int4 *edges, uint32_t *edge_draw) {
+    if (!nedges)
+        return cudaSuccess;
+    gb_fill_edges<<<(nedges + 255) / 256, 256, 0, st>>>(nedges, npairs, e_off, pair_draw, pair_sub, draws, sub_pt0,
+                                                         sub_npts, pts, W, H, edges, edge_draw);
+    return cudaGetLastError();
+}
+cudaError_t gb_launch_stroke_tris(cudaStream_t st, uint32_t ntris, uint32_t ndraw_s, const uint32_t *draw_tri0,
+                                  const uint32_t *sdraw_id, const uint32_t *draw_vbase, const gb_draw *draws,
+                                  const float2 *verts, const uint32_t *inds, uint32_t W, uint32_t H, int4 *tri_a,
+                                  int4 *tri_b, uint32_t *tri_draw) {
+    if (!ntris)
+        return cudaSuccess;
+    gb_stroke_tris<<<(ntris + 255) / 256, 256, 0, st>>>(ntris, ndraw_s, draw_tri0, sdraw_id, draw_vbase, draws, verts,
+                                                         inds, W, H, tri_a, tri_b, tri_draw);
+    return cudaGetLastError();
+}
+cudaError_t gb_launch_bin(cudaStream_t st, int scatter, uint32_t nedges, const int4 *edges, const uint32_t *edge_draw,
+                          uint32_t ntris, const int4 *tri_a, const int4 *tri_b, const uint32_t *tri_draw,
+                          uint32_t ndraws, uint32_t W, uint32_t samples, uint32_t nrows, uint32_t *cell,
+                          uint32_t *edge_refs, uint32_t *tri_refs, uint32_t nrefs) {
+    if (nedges) {
+        if (scatter)
+            gb_bin_edges<true><<<(nedges + 255) / 256, 256, 0, st>>>(nedges, edges, edge_draw, ndraws, W, samples,
+                                                                      nrows, cell, edge_refs, nrefs);
+        else
+            gb_bin_edges<false><<<(nedges + 255) / 256, 256, 0, st>>>(nedges, edges, edge_draw, ndraws, W, samples,
+                                                                       nrows, cell, nullptr, 0u);
+    }
+    if (ntris) {
+        if (scatter)
+            gb_bin_tris<true><<<(ntris + 255) / 256, 256, 0, st>>>(ntris, tri_a, tri_b, tri_draw, ndraws, W, samples,
+                                                                    nrows, cell, tri_refs, nrefs);
+        else
+            gb_bin_tris<false><<<(ntris + 255) / 256, 256, 0, st>>>(ntris, tri_a, tri_b, tri_draw, ndraws, W, samples,
+                                                                     nrows, cell, nullptr, 0u);
+    }
+    return cudaGetLastError();
+}
+}
