@@ -1,0 +1,328 @@
+#!/usr/bin/env python
+"""Benchmark of the vkvg path hot path on GB300.
+
+Workload (one step = one frame): the curve-heavy scene - a 1024x1024 RGBA8
+surface at 4x MSAA painted white, then 2,048 closed paths of U{4..64} cubic
+Beziers with control points uniform in [0,1024)^2 (seed 1), each filled
+(even-odd / non-zero alternating, alpha U[0.3,1)) and stroked (width U[1,8),
+joins and caps cycled, every 4th path dashed [10,5]).  Synthetic seeded data
+(vkvg_gb300/scenes.py); no public dataset exists for this path.
+
+value  - paths/s with the recorded command buffers resident in HBM
+         (vkvg_gb300_frame_execute: flatten -> stroke -> setup/binning ->
+         raster/composite), device time from CUDA events on the library's
+         stream, L2 flushed (a 256 MiB buffer is zeroed) before every step.
+e2e    - paths/s through the public C API from host memory: each step replays
+         the scene's vkvg_* calls (vkvg_gb300_replay_stream), flushes (H2D copy
+         + kernels) and reads the image back (vkvg_surface_write_to_memory);
+         wall-clock time.
+roofline - the raster/composite kernel (dominant) against the measured HBM
+         copy bandwidth; algorithmic bytes = 8 B per flattened point and per
+         stroke vertex read once, plus the RGBA8 surface read and written.
+cpu_baseline - the CPU restatement of vkvg's path code (oracle/) on a bounded
+         sample (the first 64 paths of the same scene), all host threads.
+
+`--impl reference` times that CPU implementation alone (vkvg itself cannot be
+built or run here: no Vulkan stack and its vkh / glutess submodules are empty).
+Multi-GPU: replicas only (one independent frame per GPU).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
+FALLBACK_HBM_GBS = 6800.0
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--paths", type=int, default=2048)
+    p.add_argument("--size", type=int, default=1024)
+    p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    return p.parse_args()
+
+
+def hbm_peak():
+    try:
+        with open(PEAKS_FILE) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 6:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = max(mx, float(parts[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[2:6]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_sample(n_paths, size, threads, reps=1):
+    """Time the CPU restatement on the first n_paths paths of the scene."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_bind as ob
+    from vkvg_gb300 import scenes
+
+    sc = scenes.curve_heavy(n_paths=n_paths, size=size, seed=1)
+    L = ob.lib()
+    L.vko_set_math_mode(0)
+    L.vko_set_raster_mode(0)
+    L.vko_set_threads(threads)
+    times = []
+    for _ in range(reps):
+        surf = ob.OracleSurface(size, size, 4)
+        ctx = surf.context()
+        t0 = time.perf_counter()
+        scenes.play(ctx, sc["ops"])
+        ctx.flush()
+        times.append(time.perf_counter() - t0)
+        ctx.destroy()
+        surf.destroy()
+    return n_paths / min(times), min(times)
+
+
+def run_reference(a, rank):
+    """CPU implementation of the path (the oracle port), all host threads."""
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    n_paths = 64
+    for _ in range(a.warmup):
+        cpu_sample(n_paths, a.size, threads)
+    t = 0.0
+    for _ in range(a.steps):
+        _, dt = cpu_sample(n_paths, a.size, threads)
+        t += dt
+    value = n_paths * a.steps / t
+    line = {
+        "impl": "reference", "metric": "paths/s", "value": value, "unit": "paths/s", "n_gpus": a.gpus,
+        "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1000.0 * t / a.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "fp32/int64/u8", "data": "synthetic",
+        "config": {"workload": "curve_heavy_%dx%d_msaa4" % (a.size, a.size), "paths_per_frame": a.paths,
+                   "sample": "first %d paths of the scene per step" % n_paths},
+        "cpu_baseline": {"value": value, "unit": "paths/s", "cores": threads, "kind": "port",
+                         "sample": "first %d of %d paths, full %dx%d surface" % (n_paths, a.paths, a.size, a.size)},
+        "e2e": {"value": value, "unit": "paths/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "vkvg itself is unavailable on this box (Vulkan-only; vkh/glutess submodules empty); the timed "
+                "CPU implementation restates its path geometry and raster state",
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    a = parse()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if a.impl == "reference":
+        run_reference(a, rank)
+        return
+
+    import ctypes as C
+
+    import numpy as np
+    import torch
+
+    import vkvg_gb300 as gb
+    from vkvg_gb300 import scenes
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    gb._build.build()
+    L = gb.lib()
+    sc = scenes.curve_heavy(n_paths=a.paths, size=a.size, seed=1)
+    cmds, args = scenes.encode(sc["ops"])
+    cptr, aptr = cmds.ctypes.data_as(C.c_void_p), args.ctypes.data_as(C.c_void_p)
+
+    dev = gb.Device(samples=4)
+    surf = gb.Surface(dev, a.size, a.size)
+    ctx = surf.context()
+    st = L.vkvg_gb300_replay_stream(ctx.h, cptr, len(cmds), aptr, len(args))
+    assert st == 0, st
+    frame = L.vkvg_gb300_frame_capture(ctx.h)
+    assert frame
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    def l2_flush():
+        flush.zero_()
+        torch.cuda.synchronize()
+
+    timing = np.zeros(8, np.float32)
+    stats = np.zeros(16, np.uint64)
+    for _ in range(a.warmup):
+        l2_flush()
+        assert L.vkvg_gb300_frame_execute(frame, surf.h) == 0
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    l0 = gb.kernel_launches()
+    tot = np.zeros(5)
+    for _ in range(a.steps):
+        l2_flush()
+        assert L.vkvg_gb300_frame_execute(frame, surf.h) == 0
+        L.vkvg_gb300_frame_timing(frame, timing.ctypes.data_as(C.c_void_p))
+        tot += timing[:5]
+    launches = gb.kernel_launches() - l0
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clk = clocks.stop()
+    L.vkvg_gb300_frame_stats(frame, stats.ctypes.data_as(C.c_void_p))
+    ms = tot[4] / a.steps
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    paths = int(stats[0])
+    value = paths * world / (ms / 1000.0)
+
+    # ---- end to end through the C API with host buffers
+    img = np.zeros((a.size, a.size, 4), np.uint8)
+    iptr = img.ctypes.data_as(C.c_void_p)
+    ectx = surf.context()
+
+    def e2e_step():
+        s = L.vkvg_gb300_replay_stream(ectx.h, cptr, len(cmds), aptr, len(args))
+        assert s == 0, s
+        L.vkvg_flush(ectx.h)
+        assert L.vkvg_surface_write_to_memory(surf.h, iptr) == 0
+
+    for _ in range(a.warmup):
+        e2e_step()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    e_steps = max(3, a.steps // 2)
+    t0 = time.perf_counter()
+    for _ in range(e_steps):
+        e2e_step()
+    e_t = (time.perf_counter() - t0) / e_steps
+    if dist:
+        t = torch.tensor([e_t], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e_t = float(t.item())
+    e2e_value = paths * world / e_t
+    h2d = int(stats[12])
+    d2h = a.size * a.size * 4
+
+    # ---- roofline of the raster/composite kernel
+    peak, peak_kind = hbm_peak()
+    nflat, nsv = int(stats[1]), int(stats[2])
+    raster_bytes = 8 * nflat + 8 * nsv + 8 * a.size * a.size
+    raster_ms = tot[3] / a.steps
+    achieved = raster_bytes / (raster_ms / 1000.0) / 1e9
+    frame_bytes = 8 * len(cmds) + 16 * nflat + 16 * nsv + 8 * a.size * a.size
+    traffic = None
+    tfile = os.path.join(ROOT, "profiles", "raster_curve_heavy_1024.md")
+    if os.path.exists(tfile):
+        for ln in open(tfile):
+            if ln.startswith("dram_bytes_per_launch:"):
+                try:
+                    traffic = int(ln.split(":")[1].split()[0])
+                except ValueError:
+                    traffic = None
+
+    line = {
+        "metric": "paths/s", "value": value, "unit": "paths/s", "n_gpus": world, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "fp32/int64/u8", "data": "synthetic (seeded scene generator, seed 1)",
+        "config": {"workload": "curve_heavy_%dx%d_msaa4" % (a.size, a.size), "paths_per_frame": paths,
+                   "cubics_per_path": "U{4..64}", "parallelism": "replicas" if world > 1 else "single",
+                   "l2": "flushed before each step (256 MiB write)",
+                   "flattened_points": nflat, "stroke_vertices": nsv, "stroke_triangles": int(stats[10]),
+                   "fill_edges": int(stats[4]), "bin_refs": int(stats[5])},
+        "stage_ms": {"flatten": tot[0] / a.steps, "stroke": tot[1] / a.steps, "setup_bin": tot[2] / a.steps,
+                     "raster": raster_ms},
+        "mpx_per_s": a.size * a.size * world / (ms / 1000.0) / 1e6,
+        "e2e": {"value": e2e_value, "unit": "paths/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "ms_per_step": e_t * 1000.0},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "kernel": "gb_raster", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
+                     "algorithmic_bytes": raster_bytes,
+                     "frame_frac": frame_bytes / (ms / 1000.0) / 1e9 / peak},
+        "clocks": clk,
+    }
+    if rank == 0 and not a.no_cpu:
+        threads = os.cpu_count() or 1
+        v, _ = cpu_sample(64, a.size, threads)
+        line["cpu_baseline"] = {"value": v, "unit": "paths/s", "cores": threads, "kind": "port",
+                                "sample": "first 64 of %d paths, full %dx%d surface, 4x MSAA" % (paths, a.size,
+                                                                                                  a.size)}
+    L.vkvg_gb300_frame_destroy(frame)
+    ectx.destroy()
+    ctx.destroy()
+    surf.destroy()
+    dev.destroy()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

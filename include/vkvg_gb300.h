@@ -34,12 +34,62 @@ vkvg_public vkvg_status_t vkvg_gb300_frame_execute(VkvgFrame frame, VkvgSurface 
 /* Counters of the last execution: out[0] paths (fill/stroke draws), out[1]
    flattened points, out[2] stroke vertices, out[3] stroke indices, out[4] fill
    edges, out[5] bin references, out[6] segments, out[7] draws, out[8] kernel
-   launches of the last execution. */
+   launches of the last execution, out[9] subpaths, out[10] stroke triangles,
+   out[11] device status word, out[12] bytes of the uploaded command buffers. */
 vkvg_public vkvg_status_t vkvg_gb300_frame_stats(VkvgFrame frame, uint64_t out[16]);
-/* Average device time per kernel class of the last execution, in ms:
-   out[0] flatten, out[1] stroke, out[2] setup+binning, out[3] raster. */
+/* Device time of the last execution on the library's stream, in ms:
+   out[0] flatten, out[1] stroke, out[2] setup+binning, out[3] raster,
+   out[4] whole frame (first kernel to last, including size read-backs). */
 vkvg_public vkvg_status_t vkvg_gb300_frame_timing(VkvgFrame frame, float out[8]);
 vkvg_public void          vkvg_gb300_frame_destroy(VkvgFrame frame);
+
+/* ---- command-stream replay ---------------------------------------------------
+ * Stands in for vkvg_replay (include/vkvg.h:1965) over a flat wire format:
+ * cmds[] holds vkvg's recording command codes (VKVG_CMD_*, the values of
+ * src/recording/vkvg_record_internal.h:28-90) and args[] their float
+ * arguments in call order (enums as float values, the vkvg_set_source_color
+ * word as the bits of one float; VKVG_CMD_SET_DASH takes count, offset, then
+ * count dash lengths).
+ * Each command calls the matching vkvg_* function on ctx.  Returns the first
+ * error: VKVG_STATUS_INVALID_INDEX for an unknown code or short args. */
+#define VKVG_CMD_NEW_PATH          0x0101
+#define VKVG_CMD_NEW_SUB_PATH      0x0102
+#define VKVG_CMD_CLOSE_PATH        0x0103
+#define VKVG_CMD_MOVE_TO           0x0104
+#define VKVG_CMD_LINE_TO           0x0105
+#define VKVG_CMD_RECTANGLE         0x0106
+#define VKVG_CMD_ARC               0x0107
+#define VKVG_CMD_ARC_NEG           0x0108
+#define VKVG_CMD_CURVE_TO          0x010A
+#define VKVG_CMD_QUADRATIC_TO      0x010B
+#define VKVG_CMD_ELLIPTICAL_ARC_TO 0x010C
+#define VKVG_CMD_SET_LINE_WIDTH    0x1101
+#define VKVG_CMD_SET_MITER_LIMIT   0x1102
+#define VKVG_CMD_SET_LINE_JOIN     0x1103
+#define VKVG_CMD_SET_LINE_CAP      0x1104
+#define VKVG_CMD_SET_OPERATOR      0x1105
+#define VKVG_CMD_SET_FILL_RULE     0x1106
+#define VKVG_CMD_SET_DASH          0x1107
+#define VKVG_CMD_TRANSLATE         0x2001
+#define VKVG_CMD_ROTATE            0x2002
+#define VKVG_CMD_SCALE             0x2003
+#define VKVG_CMD_IDENTITY_MATRIX   0x2005
+#define VKVG_CMD_SET_MATRIX        0x2006
+#define VKVG_CMD_REL_MOVE_TO       0x0504
+#define VKVG_CMD_REL_LINE_TO       0x0505
+#define VKVG_CMD_REL_CURVE_TO      0x050A
+#define VKVG_CMD_REL_QUADRATIC_TO  0x050B
+#define VKVG_CMD_PAINT             0x0201
+#define VKVG_CMD_FILL              0x0202
+#define VKVG_CMD_STROKE            0x0203
+#define VKVG_CMD_CLEAR             0x0206
+#define VKVG_CMD_FILL_PRESERVE     0x0602
+#define VKVG_CMD_STROKE_PRESERVE   0x0603
+#define VKVG_CMD_SET_SOURCE_RGB    0x0801
+#define VKVG_CMD_SET_SOURCE_RGBA   0x0802
+#define VKVG_CMD_SET_SOURCE_COLOR  0x0803
+vkvg_public vkvg_status_t vkvg_gb300_replay_stream(VkvgContext ctx, const uint32_t *cmds, uint32_t ncmds,
+                                                   const float *args, uint64_t nargs);
 
 /* ---- parity hooks (no vkvg counterpart) ----------------------------------
  * With debug capture on, a context keeps the device buffers of its last flush

@@ -2,7 +2,7 @@
 per-stage results for comparison (test infrastructure)."""
 import numpy as np
 
-import scenes
+from vkvg_gb300 import scenes
 
 
 def run_gpu(gb, sc, debug=True):

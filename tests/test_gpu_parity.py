@@ -9,7 +9,7 @@ import numpy as np
 import pytest
 
 import parity_util as pu
-import scenes
+from vkvg_gb300 import scenes
 
 pytestmark = pytest.mark.gpu
 
@@ -63,5 +63,20 @@ def test_image_bit_exact(gb, vko, idx):
     sc = small_scenes()[idx]
     dev, surf, ctx = pu.run_gpu(gb, sc)
     osurf, octx = pu.run_oracle(vko, sc)
+    assert np.array_equal(surf.samples_rgba(), osurf.samples_rgba())
+    assert np.array_equal(surf.image(), osurf.image())
+
+
+def test_curve_heavy_full_size_bit_exact(gb, vko):
+    """The full 1024x1024, 2,048-path benchmark scene: every stroke/fill draw's
+    geometry and the final 4x MSAA samples equal the oracle's."""
+    import os
+
+    sc = scenes.curve_heavy()
+    dev, surf, ctx = pu.run_gpu(gb, sc)
+    osurf, octx = pu.run_oracle(vko, sc, threads=os.cpu_count() or 1)
+    assert ctx.debug_counts()[5] == 0
+    errs = pu.compare_geometry(ctx, octx)
+    assert not errs, errs[:10]
     assert np.array_equal(surf.samples_rgba(), osurf.samples_rgba())
     assert np.array_equal(surf.image(), osurf.image())

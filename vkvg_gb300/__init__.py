@@ -124,6 +124,7 @@ SIGNATURES = {
     "vkvg_gb300_frame_stats": (_I, [_P, _P]),
     "vkvg_gb300_frame_timing": (_I, [_P, _P]),
     "vkvg_gb300_frame_destroy": (None, [_P]),
+    "vkvg_gb300_replay_stream": (_I, [_P, _P, _U, _P, C.c_uint64]),
     "vkvg_gb300_debug_capture": (None, [_P, _I]),
     "vkvg_gb300_debug_counts": (_I, [_P, _P]),
     "vkvg_gb300_debug_points": (_I, [_P, _P, _P]),

@@ -280,6 +280,7 @@ vkvg_status_t vkvg_gb300_frame_stats(VkvgFrame fr, uint64_t out[16]) {
     out[9]            = p.nsub;
     out[10]           = p.ntris;
     out[11]           = p.dev_status;
+    out[12]           = p.upload_bytes;
     return VKVG_STATUS_SUCCESS;
 }
 
@@ -287,7 +288,7 @@ vkvg_status_t vkvg_gb300_frame_timing(VkvgFrame fr, float out[8]) {
     if (!fr || !out)
         return VKVG_STATUS_NULL_POINTER;
     for (int i = 0; i < 8; i++)
-        out[i] = i < 4 ? fr->pl.ms[i] : 0.f;
+        out[i] = i < 5 ? fr->pl.ms[i] : 0.f;
     return VKVG_STATUS_SUCCESS;
 }
 
@@ -296,6 +297,113 @@ void vkvg_gb300_frame_destroy(VkvgFrame fr) {
         return;
     fr->pl.destroy();
     delete fr;
+}
+
+/* ------------------------------------------------------- command replay */
+
+vkvg_status_t vkvg_gb300_replay_stream(VkvgContext ctx, const uint32_t *cmds, uint32_t ncmds, const float *args,
+                                       uint64_t nargs) {
+    if (vkvg_status(ctx))
+        return vkvg_status(ctx);
+    if ((!cmds && ncmds) || (!args && nargs))
+        return VKVG_STATUS_NULL_POINTER;
+    uint64_t a = 0;
+#define NEED(k)                                                                                                            do {                                                                                                                       if (a + (k) > nargs)                                                                                                       return VKVG_STATUS_INVALID_INDEX;                                                                              } while (0)
+    const float *A = args;
+    for (uint32_t i = 0; i < ncmds; i++) {
+        switch (cmds[i]) {
+        case VKVG_CMD_NEW_PATH: vkvg_new_path(ctx); break;
+        case VKVG_CMD_NEW_SUB_PATH: vkvg_new_sub_path(ctx); break;
+        case VKVG_CMD_CLOSE_PATH: vkvg_close_path(ctx); break;
+        case VKVG_CMD_MOVE_TO: NEED(2); vkvg_move_to(ctx, A[a], A[a + 1]); a += 2; break;
+        case VKVG_CMD_LINE_TO: NEED(2); vkvg_line_to(ctx, A[a], A[a + 1]); a += 2; break;
+        case VKVG_CMD_REL_MOVE_TO: NEED(2); vkvg_rel_move_to(ctx, A[a], A[a + 1]); a += 2; break;
+        case VKVG_CMD_REL_LINE_TO: NEED(2); vkvg_rel_line_to(ctx, A[a], A[a + 1]); a += 2; break;
+        case VKVG_CMD_RECTANGLE: NEED(4); vkvg_rectangle(ctx, A[a], A[a + 1], A[a + 2], A[a + 3]); a += 4; break;
+        case VKVG_CMD_ARC: NEED(5); vkvg_arc(ctx, A[a], A[a + 1], A[a + 2], A[a + 3], A[a + 4]); a += 5; break;
+        case VKVG_CMD_ARC_NEG:
+            NEED(5);
+            vkvg_arc_negative(ctx, A[a], A[a + 1], A[a + 2], A[a + 3], A[a + 4]);
+            a += 5;
+            break;
+        case VKVG_CMD_CURVE_TO:
+            NEED(6);
+            vkvg_curve_to(ctx, A[a], A[a + 1], A[a + 2], A[a + 3], A[a + 4], A[a + 5]);
+            a += 6;
+            break;
+        case VKVG_CMD_REL_CURVE_TO:
+            NEED(6);
+            vkvg_rel_curve_to(ctx, A[a], A[a + 1], A[a + 2], A[a + 3], A[a + 4], A[a + 5]);
+            a += 6;
+            break;
+        case VKVG_CMD_QUADRATIC_TO:
+            NEED(4);
+            vkvg_quadratic_to(ctx, A[a], A[a + 1], A[a + 2], A[a + 3]);
+            a += 4;
+            break;
+        case VKVG_CMD_REL_QUADRATIC_TO:
+            NEED(4);
+            vkvg_rel_quadratic_to(ctx, A[a], A[a + 1], A[a + 2], A[a + 3]);
+            a += 4;
+            break;
+        case VKVG_CMD_ELLIPTICAL_ARC_TO: /* x, y, large, sweep, rx, ry, phi */
+            NEED(7);
+            vkvg_elliptic_arc_to(ctx, A[a], A[a + 1], A[a + 2] != 0, A[a + 3] != 0, A[a + 4], A[a + 5], A[a + 6]);
+            a += 7;
+            break;
+        case VKVG_CMD_SET_LINE_WIDTH: NEED(1); vkvg_set_line_width(ctx, A[a++]); break;
+        case VKVG_CMD_SET_MITER_LIMIT: NEED(1); vkvg_set_miter_limit(ctx, A[a++]); break;
+        case VKVG_CMD_SET_LINE_JOIN: NEED(1); vkvg_set_line_join(ctx, (vkvg_line_join_t)(int)A[a++]); break;
+        case VKVG_CMD_SET_LINE_CAP: NEED(1); vkvg_set_line_cap(ctx, (vkvg_line_cap_t)(int)A[a++]); break;
+        case VKVG_CMD_SET_OPERATOR: NEED(1); vkvg_set_operator(ctx, (vkvg_operator_t)(int)A[a++]); break;
+        case VKVG_CMD_SET_FILL_RULE: NEED(1); vkvg_set_fill_rule(ctx, (vkvg_fill_rule_t)(int)A[a++]); break;
+        case VKVG_CMD_SET_DASH: {
+            NEED(2);
+            uint32_t n   = (uint32_t)A[a];
+            float    off = A[a + 1];
+            a += 2;
+            NEED(n);
+            vkvg_set_dash(ctx, n ? A + a : nullptr, n, off);
+            a += n;
+            break;
+        }
+        case VKVG_CMD_TRANSLATE: NEED(2); vkvg_translate(ctx, A[a], A[a + 1]); a += 2; break;
+        case VKVG_CMD_SCALE: NEED(2); vkvg_scale(ctx, A[a], A[a + 1]); a += 2; break;
+        case VKVG_CMD_ROTATE: NEED(1); vkvg_rotate(ctx, A[a++]); break;
+        case VKVG_CMD_IDENTITY_MATRIX: vkvg_identity_matrix(ctx); break;
+        case VKVG_CMD_SET_MATRIX: {
+            NEED(6);
+            vkvg_matrix_t m = {A[a], A[a + 1], A[a + 2], A[a + 3], A[a + 4], A[a + 5]};
+            vkvg_set_matrix(ctx, &m);
+            a += 6;
+            break;
+        }
+        case VKVG_CMD_PAINT: vkvg_paint(ctx); break;
+        case VKVG_CMD_FILL: vkvg_fill(ctx); break;
+        case VKVG_CMD_STROKE: vkvg_stroke(ctx); break;
+        case VKVG_CMD_CLEAR: vkvg_clear(ctx); break;
+        case VKVG_CMD_FILL_PRESERVE: vkvg_fill_preserve(ctx); break;
+        case VKVG_CMD_STROKE_PRESERVE: vkvg_stroke_preserve(ctx); break;
+        case VKVG_CMD_SET_SOURCE_RGB: NEED(3); vkvg_set_source_rgb(ctx, A[a], A[a + 1], A[a + 2]); a += 3; break;
+        case VKVG_CMD_SET_SOURCE_RGBA:
+            NEED(4);
+            vkvg_set_source_rgba(ctx, A[a], A[a + 1], A[a + 2], A[a + 3]);
+            a += 4;
+            break;
+        case VKVG_CMD_SET_SOURCE_COLOR: {
+            NEED(1);
+            uint32_t c;
+            memcpy(&c, &A[a++], 4);
+            vkvg_set_source_color(ctx, c);
+            break;
+        }
+        default: return VKVG_STATUS_INVALID_INDEX;
+        }
+        if (vkvg_status(ctx))
+            return vkvg_status(ctx);
+    }
+#undef NEED
+    return VKVG_STATUS_SUCCESS;
 }
 
 /* ------------------------------------------------------- portable math */

@@ -71,7 +71,8 @@ struct Pipeline {
     uint32_t npts = 0, nev = 0, nverts = 0, ninds = 0, nedges = 0, ntris = 0, nrefs = 0, nbands = 0;
     uint32_t dev_status = 0;
     uint64_t launches   = 0;
-    float    ms[4]      = {0, 0, 0, 0};
+    uint64_t upload_bytes = 0;
+    float    ms[5]      = {0, 0, 0, 0, 0};
 
     bool init();
     void destroy();

@@ -154,6 +154,7 @@ cudaError_t Pipeline::upload(const FrameHost &f) {
     nspair = (uint32_t)f.spair_draw.size();
     nsdraw = (uint32_t)f.sdraw_id.size();
     nfpair = (uint32_t)f.fpair_draw.size();
+    upload_bytes  = o;
     cudaError_t e = cudaMemcpyAsync(in.p, staging.p, o, cudaMemcpyHostToDevice, st);
     uploaded      = e == cudaSuccess;
     return e;
@@ -359,9 +360,11 @@ cudaError_t Pipeline::run(const FrameHost &f, _vkvg_surface_t *surf, bool timing
     CK(cudaMemcpyAsync(rb.p, status.p, 4, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     dev_status = *(uint32_t *)rb.p;
-    if (timing)
+    if (timing) {
         for (int i = 0; i < 4; i++)
             cudaEventElapsedTime(&ms[i], evs[i], evs[i + 1]);
+        cudaEventElapsedTime(&ms[4], evs[0], evs[4]);
+    }
     return cudaGetLastError();
 }
 

@@ -1,4 +1,4 @@
-"""Seeded synthetic scenes for the vkvg path hot path.
+"""Seeded synthetic scenes for the vkvg path hot path (benchmarks and tests).
 
 A scene is a list of API calls ``(name, *args)`` that is replayed, call for
 call, on any object exposing vkvg's context methods (the GPU library's Python
@@ -101,3 +101,38 @@ def play(ctx, ops):
             ctx.set_matrix(args[0])
         else:
             getattr(ctx, name)(*args)
+
+
+# vkvg recording command codes (src/recording/vkvg_record_internal.h:28-90),
+# the wire format of vkvg_gb300_replay_stream
+CMD = {
+    "new_path": 0x0101, "new_sub_path": 0x0102, "close_path": 0x0103, "move_to": 0x0104, "line_to": 0x0105,
+    "rectangle": 0x0106, "arc": 0x0107, "arc_negative": 0x0108, "curve_to": 0x010A, "quadratic_to": 0x010B,
+    "elliptic_arc_to": 0x010C, "set_line_width": 0x1101, "set_miter_limit": 0x1102, "set_line_join": 0x1103,
+    "set_line_cap": 0x1104, "set_operator": 0x1105, "set_fill_rule": 0x1106, "set_dash": 0x1107,
+    "translate": 0x2001, "rotate": 0x2002, "scale": 0x2003, "identity_matrix": 0x2005, "set_matrix": 0x2006,
+    "rel_move_to": 0x0504, "rel_line_to": 0x0505, "rel_curve_to": 0x050A, "rel_quadratic_to": 0x050B,
+    "paint": 0x0201, "fill": 0x0202, "stroke": 0x0203, "clear": 0x0206, "fill_preserve": 0x0602,
+    "stroke_preserve": 0x0603, "set_source_rgb": 0x0801, "set_source_rgba": 0x0802, "set_source_color": 0x0803,
+}
+
+
+def encode(ops):
+    """scene calls -> (cmds uint32[], args float32[]) for vkvg_gb300_replay_stream"""
+    import struct
+
+    import numpy as np
+
+    cmds, args = [], []
+    for op in ops:
+        name, a = op[0], op[1:]
+        cmds.append(CMD[name])
+        if name == "set_dash":
+            args += [float(len(a[0])), float(a[1])] + [float(v) for v in a[0]]
+        elif name == "set_matrix":
+            args += [float(v) for v in a[0]]
+        elif name == "set_source_color":
+            args.append(struct.unpack("<f", struct.pack("<I", a[0]))[0])
+        else:
+            args += [float(v) for v in a]
+    return np.array(cmds, np.uint32), np.array(args, np.float32)
