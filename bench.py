@@ -237,7 +237,7 @@ def main():
         t = torch.tensor([ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
-    paths = int(stats[0])
+    paths = a.paths  # each path is filled and stroked (two draws)
     value = paths * world / (ms / 1000.0)
 
     # ---- end to end through the C API with host buffers

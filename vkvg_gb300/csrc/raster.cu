@@ -11,13 +11,23 @@
  * every sample with x < x_c (a sample on the edge counts as if moved by
  * (+e, +e^2), which is the top-left rule).  Summed over a closed polygon this
  * is its winding number; summed over positively oriented triangles it is the
- * number of covering triangles.  Each edge touching the band drops its
- * crossings into shared-memory counters (one exact division per edge, then an
- * incremental remainder walk down the rows), and a 16-lane suffix scan turns
- * counters into per-sample windings.  The fill rule then decides how many
- * times vkvg's blend is applied: even-odd -> w & 1 (the stencil-INVERT fan of
- * _poly_fill), non-zero -> w != 0 (glutess' NONZERO tessellation), stroke -> w
- * (each overlapping stroke triangle blends once under pipe_OVER).
+ * number of covering triangles.  Each (edge, sample row) pair of the band is
+ * one work item that drops its crossing into a shared-memory counter; a
+ * 16-lane suffix scan turns counters into per-sample windings.  The fill rule
+ * then decides how many times vkvg's blend is applied: even-odd -> w & 1 (the
+ * stencil-INVERT fan of _poly_fill), non-zero -> w != 0 (glutess' NONZERO
+ * tessellation), stroke -> w (each overlapping stroke triangle blends once
+ * under pipe_OVER).
+ *
+ * Draws are processed in batches of RB_D: the crossings of all draws of a
+ * batch are accumulated into separate counter planes in one phase, then each
+ * thread applies the batch's draws to its samples in order.  Stroke triangles
+ * lying wholly left or right of the tile are skipped (a closed triangle right
+ * of every sample adds +1 and -1 to each row it crosses).
+ *
+ * Crossing x = x0 + dx*(sy-y0)/dy is found exactly: an fp32 quotient estimate
+ * (error < 0.75 for |q| < 2^22) corrected by one exact 64-bit product test;
+ * larger quotients take an exact 64-bit division.
  *
  * Blend (src/vkvg_device_internal.c:200-209, ONE / ONE_MINUS_SRC_ALPHA on
  * premultiplied UNORM8): d' = s + floor((d*(255-sa) + 127) / 255) per channel,
@@ -29,73 +39,56 @@
 
 #include <cuda_runtime.h>
 
+#define RB_D        4               /* draws per batch */
+#define CNT_W       (GB_TILE_W + 4) /* counter k (1..256) lives at [k + 3]: 16-byte aligned runs */
+#define CNT_PLANE   (GB_BAND_ROWS * CNT_W)
+#define RASTER_SMEM (RB_D * CNT_PLANE * 4)
 
-
-#define CNT_PAD 4 /* counter k (1..256) lives at [r][k + 3]: 16-byte aligned runs */
-
-__device__ __forceinline__ long long floordiv_ll(long long a, long long b) {
-    long long q = a / b;
-    if ((a % b != 0) && (a < 0))
-        q--;
-    return q;
+/* ceil(num / den) for den > 0, exact */
+__device__ __forceinline__ long long ceil_div_exact(long long num, int32_t den) {
+    float qf = __ll2float_rn(num) / (float)den;
+    if (fabsf(qf) < 4194304.0f) {
+        long long c = (long long)ceilf(qf);
+        long long p = c * (long long)den;
+        if (p < num)
+            c++;
+        else if (p - den >= num)
+            c--;
+        return c;
+    }
+    long long q = num / den, r = num % den;
+    return r > 0 ? q + 1 : q;
 }
 
-/* accumulate one directed edge's crossings of the tile's sample rows */
-__device__ __forceinline__ void acc_edge(int32_t x0, int32_t y0, int32_t x1, int32_t y1, int32_t band_r0,
-                                         int32_t nrows, uint32_t S, int32_t X0, int32_t TW,
-                                         int32_t (*cnt)[GB_TILE_W + CNT_PAD]) {
+/* one (edge, sample row) item: add the edge's crossing of row R */
+__device__ __forceinline__ void acc_row(int32_t x0, int32_t y0, int32_t x1, int32_t y1, int32_t R, uint32_t S,
+                                        int32_t X0, int32_t TW, int32_t *__restrict__ row_cnt) {
     if (y0 == y1)
         return;
-    int32_t   dir  = y0 < y1 ? 1 : -1;
-    int32_t   ylo  = min(y0, y1), yhi = max(y0, y1);
-    long long off  = S == 4 ? 32 : 128;
-    long long step = S == 4 ? 64 : 256;
-    /* rows with ylo <= sy < yhi */
-    long long a  = (long long)ylo - off, b = (long long)yhi - off;
-    long long ra = -floordiv_ll(-a, step);
-    long long rb = -floordiv_ll(-b, step) - 1;
-    long long lo = band_r0, hi = min(band_r0 + GB_BAND_ROWS - 1, nrows - 1);
-    if (ra < lo)
-        ra = lo;
-    if (rb > hi)
-        rb = hi;
-    if (ra > rb)
+    const int32_t sy  = S == 4 ? 32 + 64 * R : 128 + 256 * R;
+    const int32_t ylo = min(y0, y1), yhi = max(y0, y1);
+    if (sy < ylo || sy >= yhi)
         return;
-    int32_t   xmin = min(x0, x1), xmax = max(x0, x1);
-    long long tx_lo = (long long)X0 * 256 + 32, tx_hi = (long long)(X0 + TW - 1) * 256 + 224;
-    if ((long long)xmax < tx_lo)
-        return; /* crossings left of every tile sample */
-    if ((long long)xmin > tx_hi) {
-        for (long long R = ra; R <= rb; R++)
-            atomicAdd(&cnt[R - band_r0][TW + 3], dir);
+    const int32_t dir   = y0 < y1 ? 1 : -1;
+    const int32_t tx_lo = X0 * 256 + 32, tx_hi = (X0 + TW - 1) * 256 + 224;
+    if (max(x0, x1) < tx_lo)
+        return; /* crossing left of every tile sample */
+    if (min(x0, x1) > tx_hi) {
+        atomicAdd(&row_cnt[TW + 3], dir);
         return;
     }
-    long long dx = (long long)x1 - x0, dy = (long long)y1 - y0;
-    long long den = dy < 0 ? -dy : dy;
-    long long dxn = dy < 0 ? -dx : dx;
-    long long sy0 = off + step * ra;
-    long long num = dxn * (sy0 - y0);
-    long long c   = -floordiv_ll(-num, den); /* ceil(num/den) */
-    long long rem = c * den - num;
-    long long dl  = dxn * step;
-    long long qd  = floordiv_ll(dl, den);
-    long long rd  = dl - qd * den;
-    for (long long R = ra; R <= rb; R++) {
-        long long ox = S == 4 ? ((R & 3) == 0 ? 96 : (R & 3) == 1 ? 224 : (R & 3) == 2 ? 32 : 160) : 128;
-        long long M  = (long long)x0 + c - 1;
-        long long kg = ((M - ox) >> 8) + 1;
-        long long kt = kg - X0;
-        if (kt > TW)
-            kt = TW;
-        if (kt > 0)
-            atomicAdd(&cnt[R - band_r0][kt + 3], dir);
-        rem -= rd;
-        c += qd;
-        if (rem < 0) {
-            rem += den;
-            c += 1;
-        }
-    }
+    const int32_t   dy  = y1 - y0;
+    const int32_t   den = dy < 0 ? -dy : dy;
+    const int32_t   dxn = dy < 0 ? x0 - x1 : x1 - x0;
+    const long long num = (long long)dxn * (long long)(sy - y0);
+    const long long c   = ceil_div_exact(num, den);
+    const int32_t   ox  = S == 4 ? ((R & 3) == 0 ? 96 : (R & 3) == 1 ? 224 : (R & 3) == 2 ? 32 : 160) : 128;
+    const long long M   = (long long)x0 + c - 1; /* largest covered sample x */
+    long long       kt  = ((M - ox) >> 8) + 1 - X0;
+    if (kt > TW)
+        kt = TW;
+    if (kt > 0)
+        atomicAdd(&row_cnt[kt + 3], dir);
 }
 
 __device__ __forceinline__ uint32_t div255_2x(uint32_t x) {
@@ -117,26 +110,26 @@ __device__ __forceinline__ uint32_t blend(uint32_t d, uint32_t s, uint32_t inv, 
     return __vaddus4(s, t);
 }
 
-__global__ void __launch_bounds__(256) gb_raster(gb_raster_args A) {
-    __shared__ __align__(16) int32_t  cnt[GB_BAND_ROWS][GB_TILE_W + CNT_PAD];
-    __shared__ __align__(16) uint32_t stage[GB_BAND_ROWS * GB_TILE_W];
+__global__ void __launch_bounds__(256, 3) gb_raster(gb_raster_args A) {
+    extern __shared__ __align__(16) int32_t smem[];
 
     const uint32_t t = threadIdx.x, r = t >> 4, g = t & 15;
-    const uint32_t band = blockIdx.y;
-    const int32_t  X0   = (int32_t)(blockIdx.x * GB_TILE_W);
-    const int32_t  TW   = min((int32_t)GB_TILE_W, (int32_t)A.W - X0);
-    const int32_t  R    = (int32_t)(band * GB_BAND_ROWS + r);
-    const bool     row_ok = R < (int32_t)A.nrows;
-    const int32_t  col0   = (int32_t)(16 * g);
-    const int32_t  ncols  = row_ok ? max(0, min(16, TW - col0)) : 0;
+    const uint32_t band    = blockIdx.y;
+    const int32_t  X0      = (int32_t)(blockIdx.x * GB_TILE_W);
+    const int32_t  TW      = min((int32_t)GB_TILE_W, (int32_t)A.W - X0);
+    const int32_t  R       = (int32_t)(band * GB_BAND_ROWS + r);
+    const bool     row_ok  = R < (int32_t)A.nrows;
+    const int32_t  col0    = (int32_t)(16 * g);
+    const int32_t  ncols   = row_ok ? max(0, min(16, TW - col0)) : 0;
     const int32_t  band_r0 = (int32_t)(band * GB_BAND_ROWS);
+    const int32_t  tx_lo = X0 * 256 + 32, tx_hi = (X0 + TW - 1) * 256 + 224;
+    const uint32_t nd    = A.ndraws;
+    const size_t   cb    = (size_t)band * nd;
+    const bool     dbg   = A.cov_out != nullptr;
+    const uint32_t rpp   = A.S == 4 ? 4 : 1;
 
-    /* skip bands no draw touches (unless a paint / clear covers everything) */
-    const uint32_t nd  = A.ndraws;
-    const size_t   cb  = (size_t)band * nd;
-
-    uint32_t col[16];
-    uint32_t *srow = A.samples + (size_t)(R < (int32_t)A.nrows ? R : 0) * A.Wpad + X0 + col0;
+    uint32_t  col[16];
+    uint32_t *srow = A.samples + (size_t)(row_ok ? R : 0) * A.Wpad + X0 + col0;
     if (A.init_mode == 1) {
 #pragma unroll
         for (int c = 0; c < 16; c++)
@@ -156,98 +149,135 @@ __global__ void __launch_bounds__(256) gb_raster(gb_raster_args A) {
         for (int c = 0; c < 16; c++)
             col[c] = c < ncols ? srow[c] : 0u;
     }
-    for (uint32_t i = t; i < GB_BAND_ROWS * (GB_TILE_W + CNT_PAD); i += blockDim.x)
-        (&cnt[0][0])[i] = 0;
+    for (uint32_t i = t; i < RB_D * CNT_PLANE; i += blockDim.x)
+        smem[i] = 0;
     __syncthreads();
 
-    const bool     dbg   = A.cov_out != nullptr;
-    const uint32_t dlo   = dbg ? A.cov_draw : A.draw_first;
-    const uint32_t dhi   = dbg ? A.cov_draw + 1 : nd;
-    const uint32_t rppx  = A.S == 4 ? 4 : 1;
-    for (uint32_t d = dlo; d < dhi; d++) {
-        const gb_draw &D    = A.draws[d];
-        const uint32_t kind = D.kind;
-        const uint32_t src = D.src, inv = 255u - (src >> 24), op = D.op;
-        if (kind == GB_DRAW_PAINT) {
-            if (dbg) {
-                for (int c = 0; c < ncols; c++)
-                    A.cov_out[((size_t)(R / rppx) * A.W + X0 + col0 + c) * A.S + R % rppx] = 1;
+    const uint32_t dlo = dbg ? A.cov_draw : A.draw_first;
+    const uint32_t dhi = dbg ? A.cov_draw + 1 : nd;
+    for (uint32_t d0 = dlo; d0 < dhi; d0 += RB_D) {
+        const uint32_t nb = min((uint32_t)RB_D, dhi - d0);
+        /* ---- accumulate crossings of the batch */
+        bool any = false;
+        for (uint32_t j = 0; j < nb; j++) {
+            const uint32_t d    = d0 + j;
+            const uint32_t kind = A.draws[d].kind;
+            if (kind == GB_DRAW_PAINT || kind == GB_DRAW_CLEAR)
+                continue;
+            const uint32_t lo = A.cell_off[cb + d], hi = A.cell_off[cb + d + 1];
+            if (lo == hi)
+                continue;
+            any            = true;
+            int32_t *plane = smem + j * CNT_PLANE;
+            if (kind == GB_DRAW_STROKE) {
+                const uint32_t n = (hi - lo) * 48u;
+                for (uint32_t it = t; it < n; it += blockDim.x) {
+                    const uint32_t rr = it & 15, q = it >> 4;
+                    const uint32_t i = lo + q / 3u, e = q % 3u;
+                    const int32_t  RR = band_r0 + (int32_t)rr;
+                    if (RR >= (int32_t)A.nrows)
+                        continue;
+                    const uint32_t tr  = A.refs[i];
+                    const int4     ta  = A.tri_a[tr], tb = A.tri_b[tr];
+                    const int32_t  xmn = min(min(ta.x, ta.z), tb.x), xmx = max(max(ta.x, ta.z), tb.x);
+                    if (xmx < tx_lo || xmn > tx_hi)
+                        continue;
+                    int32_t ax, ay, bx, by;
+                    if (e == 0) {
+                        ax = ta.x, ay = ta.y, bx = ta.z, by = ta.w;
+                    } else if (e == 1) {
+                        ax = ta.z, ay = ta.w, bx = tb.x, by = tb.y;
+                    } else {
+                        ax = tb.x, ay = tb.y, bx = ta.x, by = ta.y;
+                    }
+                    acc_row(ax, ay, bx, by, RR, A.S, X0, TW, plane + rr * CNT_W);
+                }
+            } else {
+                const uint32_t n = (hi - lo) * 16u;
+                for (uint32_t it = t; it < n; it += blockDim.x) {
+                    const uint32_t rr = it & 15;
+                    const int32_t  RR = band_r0 + (int32_t)rr;
+                    if (RR >= (int32_t)A.nrows)
+                        continue;
+                    const int4 ed = A.edges[A.refs[lo + (it >> 4)]];
+                    acc_row(ed.x, ed.y, ed.z, ed.w, RR, A.S, X0, TW, plane + rr * CNT_W);
+                }
+            }
+        }
+        if (any)
+            __syncthreads();
+        /* ---- apply the batch's draws in order */
+        for (uint32_t j = 0; j < nb; j++) {
+            const uint32_t d    = d0 + j;
+            const gb_draw &D    = A.draws[d];
+            const uint32_t kind = D.kind;
+            const uint32_t src = D.src, inv = 255u - (src >> 24), op = D.op;
+            if (kind == GB_DRAW_PAINT) {
+                if (dbg) {
+                    for (int c = 0; c < ncols; c++)
+                        A.cov_out[((size_t)(R / rpp) * A.W + X0 + col0 + c) * A.S + R % rpp] = 1;
+                    continue;
+                }
+#pragma unroll
+                for (int c = 0; c < 16; c++)
+                    col[c] = blend(col[c], src, inv, op);
                 continue;
             }
+            if (kind == GB_DRAW_CLEAR) {
 #pragma unroll
-            for (int c = 0; c < 16; c++)
-                col[c] = blend(col[c], src, inv, op);
-            continue;
-        }
-        if (kind == GB_DRAW_CLEAR) {
-#pragma unroll
-            for (int c = 0; c < 16; c++)
-                col[c] = 0u;
-            continue;
-        }
-        const uint32_t lo = A.cell_off[cb + d], hi = A.cell_off[cb + d + 1];
-        if (lo == hi)
-            continue;
-        if (kind == GB_DRAW_STROKE) {
-            for (uint32_t i = lo + t; i < hi; i += blockDim.x) {
-                uint32_t tr = A.refs[i];
-                int4     ta = A.tri_a[tr], tb = A.tri_b[tr];
-                acc_edge(ta.x, ta.y, ta.z, ta.w, band_r0, (int32_t)A.nrows, A.S, X0, TW, cnt);
-                acc_edge(ta.z, ta.w, tb.x, tb.y, band_r0, (int32_t)A.nrows, A.S, X0, TW, cnt);
-                acc_edge(tb.x, tb.y, ta.x, ta.y, band_r0, (int32_t)A.nrows, A.S, X0, TW, cnt);
+                for (int c = 0; c < 16; c++)
+                    col[c] = 0u;
+                continue;
             }
-        } else {
-            for (uint32_t i = lo + t; i < hi; i += blockDim.x) {
-                int4 e = A.edges[A.refs[i]];
-                acc_edge(e.x, e.y, e.z, e.w, band_r0, (int32_t)A.nrows, A.S, X0, TW, cnt);
+            const uint32_t lo = A.cell_off[cb + d], hi = A.cell_off[cb + d + 1];
+            if (lo == hi)
+                continue;
+            int4   *cp = reinterpret_cast<int4 *>(smem + j * CNT_PLANE + r * CNT_W + col0 + 4);
+            int32_t v[16];
+            int32_t L = 0;
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                int4 x       = cp[q];
+                v[4 * q]     = x.x;
+                v[4 * q + 1] = x.y;
+                v[4 * q + 2] = x.z;
+                v[4 * q + 3] = x.w;
+                L += x.x + x.y + x.z + x.w;
             }
-        }
-        __syncthreads();
-        /* counters k = col0+1 .. col0+16 */
-        int32_t   v[16];
-        int4     *cp = reinterpret_cast<int4 *>(&cnt[r][col0 + 4]);
-        int32_t   L  = 0;
+            int32_t incl = L;
 #pragma unroll
-        for (int q = 0; q < 4; q++) {
-            int4 x       = cp[q];
-            v[4 * q]     = x.x;
-            v[4 * q + 1] = x.y;
-            v[4 * q + 2] = x.z;
-            v[4 * q + 3] = x.w;
-            L += x.x + x.y + x.z + x.w;
-        }
-        int32_t incl = L;
-#pragma unroll
-        for (int o = 1; o < 16; o <<= 1) {
-            int32_t u = __shfl_down_sync(0xffffffffu, incl, o, 16);
-            if (g + o < 16)
-                incl += u;
-        }
-        int32_t w = incl - L;
-#pragma unroll
-        for (int c = 15; c >= 0; c--) {
-            w += v[c];
-            int32_t k;
-            if (kind == GB_DRAW_FILL_EO)
-                k = w & 1;
-            else if (kind == GB_DRAW_FILL_NZ)
-                k = w != 0;
-            else
-                k = w > 0 ? w : 0;
-            if (c >= ncols)
-                k = 0;
-            if (dbg) {
-                if (c < ncols)
-                    A.cov_out[((size_t)(R / rppx) * A.W + X0 + col0 + c) * A.S + R % rppx] = w;
-                k = 0;
+            for (int o = 1; o < 16; o <<= 1) {
+                int32_t u = __shfl_down_sync(0xffffffffu, incl, o, 16);
+                if (g + o < 16)
+                    incl += u;
             }
-            for (int j = 0; j < k; j++)
-                col[c] = blend(col[c], src, inv, op);
-        }
+            int32_t w = incl - L;
 #pragma unroll
-        for (int q = 0; q < 4; q++)
-            cp[q] = make_int4(0, 0, 0, 0);
-        __syncthreads();
+            for (int c = 15; c >= 0; c--) {
+                w += v[c];
+                int32_t k;
+                if (kind == GB_DRAW_FILL_EO)
+                    k = w & 1;
+                else if (kind == GB_DRAW_FILL_NZ)
+                    k = w != 0;
+                else
+                    k = w > 0 ? w : 0;
+                if (c >= ncols)
+                    k = 0;
+                if (dbg) {
+                    if (c < ncols)
+                        A.cov_out[((size_t)(R / rpp) * A.W + X0 + col0 + c) * A.S + R % rpp] = w;
+                    k = 0;
+                }
+                for (int jj = 0; jj < k; jj++)
+                    col[c] = blend(col[c], src, inv, op);
+            }
+#pragma unroll
+            for (int q = 0; q < 4; q++)
+                cp[q] = make_int4(0, 0, 0, 0);
+        }
+        if (any)
+            __syncthreads();
     }
     if (dbg)
         return;
@@ -264,12 +294,13 @@ __global__ void __launch_bounds__(256) gb_raster(gb_raster_args A) {
             if (c < ncols)
                 srow[c] = col[c];
     }
-    /* resolve */
+    /* resolve through shared memory (aliases the counter planes) */
+    __syncthreads();
+    uint32_t *stage = reinterpret_cast<uint32_t *>(smem);
 #pragma unroll
     for (int c = 0; c < 16; c++)
         stage[r * GB_TILE_W + col0 + c] = col[c];
     __syncthreads();
-    const uint32_t rpp   = A.S == 4 ? 4 : 1;
     const uint32_t prows = GB_BAND_ROWS / rpp;
     const uint32_t npx   = prows * GB_TILE_W;
     for (uint32_t q = t * 4; q < npx; q += blockDim.x * 4) {
@@ -303,9 +334,16 @@ __global__ void __launch_bounds__(256) gb_raster(gb_raster_args A) {
 }
 
 extern "C" cudaError_t gb_launch_raster(cudaStream_t st, const gb_raster_args *a) {
+    static bool configured = false;
+    if (!configured) {
+        cudaError_t e = cudaFuncSetAttribute(gb_raster, cudaFuncAttributeMaxDynamicSharedMemorySize, RASTER_SMEM);
+        if (e != cudaSuccess)
+            return e;
+        configured = true;
+    }
     if (a->nbands == 0)
         return cudaSuccess;
     dim3 grid((a->W + GB_TILE_W - 1) / GB_TILE_W, a->nbands);
-    gb_raster<<<grid, 256, 0, st>>>(*a);
+    gb_raster<<<grid, 256, RASTER_SMEM, st>>>(*a);
     return cudaGetLastError();
 }
