@@ -11,9 +11,10 @@
  * every sample with x < x_c (a sample on the edge counts as if moved by
  * (+e, +e^2), which is the top-left rule).  Summed over a closed polygon this
  * is its winding number; summed over positively oriented triangles it is the
- * number of covering triangles.  Each (edge, sample row) pair of the band is
- * one work item that drops its crossing into a shared-memory counter; a
- * 16-lane suffix scan turns counters into per-sample windings.  The fill rule
+ * number of covering triangles.  One thread per primitive of the band walks
+ * its edges down the band's sample rows and drops each crossing into a
+ * shared-memory counter; a 16-lane suffix scan turns counters into per-sample
+ * windings.  The fill rule
  * then decides how many times vkvg's blend is applied: even-odd -> w & 1 (the
  * stencil-INVERT fan of _poly_fill), non-zero -> w != 0 (glutess' NONZERO
  * tessellation), stroke -> w (each overlapping stroke triangle blends once
@@ -25,9 +26,10 @@
  * lying wholly left or right of the tile are skipped (a closed triangle right
  * of every sample adds +1 and -1 to each row it crosses).
  *
- * Crossing x = x0 + dx*(sy-y0)/dy is found exactly: an fp32 quotient estimate
- * (error < 0.75 for |q| < 2^22) corrected by one exact 64-bit product test;
- * larger quotients take an exact 64-bit division.
+ * Crossing x = x0 + dx*(sy-y0)/dy is found exactly: at the edge's first row an
+ * fp32 quotient estimate (error < 0.75 for |q| < 2^22) corrected by one exact
+ * 64-bit product test (larger quotients take an exact 64-bit division), then a
+ * quotient/remainder walk from row to row.
  *
  * Blend (src/vkvg_device_internal.c:200-209, ONE / ONE_MINUS_SRC_ALPHA on
  * premultiplied UNORM8): d' = s + floor((d*(255-sa) + 127) / 255) per channel,
@@ -60,35 +62,62 @@ __device__ __forceinline__ long long ceil_div_exact(long long num, int32_t den) 
     return r > 0 ? q + 1 : q;
 }
 
-/* one (edge, sample row) item: add the edge's crossing of row R */
-__device__ __forceinline__ void acc_row(int32_t x0, int32_t y0, int32_t x1, int32_t y1, int32_t R, uint32_t S,
-                                        int32_t X0, int32_t TW, int32_t *__restrict__ row_cnt) {
+/* floor(num / den) for den > 0, exact */
+__device__ __forceinline__ long long floor_div_exact(long long num, int32_t den) {
+    return -ceil_div_exact(-num, den);
+}
+
+/* Add one directed edge's crossings of the band's sample rows to the tile's
+   counter plane: the exact crossing at the first row, then an exact
+   quotient/remainder walk from row to row (rows are `step` apart). */
+__device__ __forceinline__ void acc_edge(int32_t x0, int32_t y0, int32_t x1, int32_t y1, int32_t band_r0,
+                                         int32_t nrows, uint32_t S, int32_t X0, int32_t TW,
+                                         int32_t *__restrict__ plane) {
     if (y0 == y1)
         return;
-    const int32_t sy  = S == 4 ? 32 + 64 * R : 128 + 256 * R;
-    const int32_t ylo = min(y0, y1), yhi = max(y0, y1);
-    if (sy < ylo || sy >= yhi)
+    const int32_t dir  = y0 < y1 ? 1 : -1;
+    const int32_t ylo  = min(y0, y1), yhi = max(y0, y1);
+    const int32_t off  = S == 4 ? 32 : 128;
+    const int32_t sh   = S == 4 ? 6 : 8; /* row step 64 or 256 units */
+    /* rows R with ylo <= off + R*step < yhi: ceil division by a power of two */
+    int32_t ra = (int32_t)(((long long)ylo - off + (1 << sh) - 1) >> sh);
+    int32_t rb = (int32_t)(((long long)yhi - off + (1 << sh) - 1) >> sh) - 1;
+    ra         = max(ra, band_r0);
+    rb         = min(rb, min(band_r0 + GB_BAND_ROWS - 1, nrows - 1));
+    if (ra > rb)
         return;
-    const int32_t dir   = y0 < y1 ? 1 : -1;
     const int32_t tx_lo = X0 * 256 + 32, tx_hi = (X0 + TW - 1) * 256 + 224;
     if (max(x0, x1) < tx_lo)
-        return; /* crossing left of every tile sample */
+        return; /* crossings left of every tile sample */
     if (min(x0, x1) > tx_hi) {
-        atomicAdd(&row_cnt[TW + 3], dir);
+        for (int32_t R = ra; R <= rb; R++)
+            atomicAdd(&plane[(R - band_r0) * CNT_W + TW + 3], dir);
         return;
     }
     const int32_t   dy  = y1 - y0;
     const int32_t   den = dy < 0 ? -dy : dy;
     const int32_t   dxn = dy < 0 ? x0 - x1 : x1 - x0;
-    const long long num = (long long)dxn * (long long)(sy - y0);
-    const long long c   = ceil_div_exact(num, den);
-    const int32_t   ox  = S == 4 ? ((R & 3) == 0 ? 96 : (R & 3) == 1 ? 224 : (R & 3) == 2 ? 32 : 160) : 128;
-    const long long M   = (long long)x0 + c - 1; /* largest covered sample x */
-    long long       kt  = ((M - ox) >> 8) + 1 - X0;
-    if (kt > TW)
-        kt = TW;
-    if (kt > 0)
-        atomicAdd(&row_cnt[kt + 3], dir);
+    const int32_t   sy0 = off + (ra << sh);
+    const long long num = (long long)dxn * (long long)(sy0 - y0);
+    long long       c   = ceil_div_exact(num, den); /* crossing - x0 at row ra, rounded up */
+    long long       rem = c * den - num;             /* in [0, den) */
+    const long long dl  = (long long)dxn << sh;
+    const long long qd  = floor_div_exact(dl, den);
+    const long long rd  = dl - qd * den;             /* in [0, den) */
+    for (int32_t R = ra; R <= rb; R++) {
+        const int32_t ox = S == 4 ? ((R & 3) == 0 ? 96 : (R & 3) == 1 ? 224 : (R & 3) == 2 ? 32 : 160) : 128;
+        long long     kt = (((long long)x0 + c - 1 - ox) >> 8) + 1 - X0;
+        if (kt > TW)
+            kt = TW;
+        if (kt > 0)
+            atomicAdd(&plane[(R - band_r0) * CNT_W + (int32_t)kt + 3], dir);
+        rem -= rd;
+        c += qd;
+        if (rem < 0) {
+            rem += den;
+            c += 1;
+        }
+    }
 }
 
 __device__ __forceinline__ uint32_t div255_2x(uint32_t x) {
@@ -170,37 +199,20 @@ __global__ void __launch_bounds__(256, 3) gb_raster(gb_raster_args A) {
             any            = true;
             int32_t *plane = smem + j * CNT_PLANE;
             if (kind == GB_DRAW_STROKE) {
-                const uint32_t n = (hi - lo) * 48u;
-                for (uint32_t it = t; it < n; it += blockDim.x) {
-                    const uint32_t rr = it & 15, q = it >> 4;
-                    const uint32_t i = lo + q / 3u, e = q % 3u;
-                    const int32_t  RR = band_r0 + (int32_t)rr;
-                    if (RR >= (int32_t)A.nrows)
-                        continue;
+                for (uint32_t i = lo + t; i < hi; i += blockDim.x) {
                     const uint32_t tr  = A.refs[i];
                     const int4     ta  = A.tri_a[tr], tb = A.tri_b[tr];
                     const int32_t  xmn = min(min(ta.x, ta.z), tb.x), xmx = max(max(ta.x, ta.z), tb.x);
                     if (xmx < tx_lo || xmn > tx_hi)
-                        continue;
-                    int32_t ax, ay, bx, by;
-                    if (e == 0) {
-                        ax = ta.x, ay = ta.y, bx = ta.z, by = ta.w;
-                    } else if (e == 1) {
-                        ax = ta.z, ay = ta.w, bx = tb.x, by = tb.y;
-                    } else {
-                        ax = tb.x, ay = tb.y, bx = ta.x, by = ta.y;
-                    }
-                    acc_row(ax, ay, bx, by, RR, A.S, X0, TW, plane + rr * CNT_W);
+                        continue; /* wholly left or right: no net coverage in the tile */
+                    acc_edge(ta.x, ta.y, ta.z, ta.w, band_r0, (int32_t)A.nrows, A.S, X0, TW, plane);
+                    acc_edge(ta.z, ta.w, tb.x, tb.y, band_r0, (int32_t)A.nrows, A.S, X0, TW, plane);
+                    acc_edge(tb.x, tb.y, ta.x, ta.y, band_r0, (int32_t)A.nrows, A.S, X0, TW, plane);
                 }
             } else {
-                const uint32_t n = (hi - lo) * 16u;
-                for (uint32_t it = t; it < n; it += blockDim.x) {
-                    const uint32_t rr = it & 15;
-                    const int32_t  RR = band_r0 + (int32_t)rr;
-                    if (RR >= (int32_t)A.nrows)
-                        continue;
-                    const int4 ed = A.edges[A.refs[lo + (it >> 4)]];
-                    acc_row(ed.x, ed.y, ed.z, ed.w, RR, A.S, X0, TW, plane + rr * CNT_W);
+                for (uint32_t i = lo + t; i < hi; i += blockDim.x) {
+                    const int4 ed = A.edges[A.refs[i]];
+                    acc_edge(ed.x, ed.y, ed.z, ed.w, band_r0, (int32_t)A.nrows, A.S, X0, TW, plane);
                 }
             }
         }
