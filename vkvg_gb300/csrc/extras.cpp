@@ -150,7 +150,10 @@ vkvg_status_t vkvg_gb300_debug_coverage(VkvgContext ctx, uint32_t i, int32_t *ou
     A.ndraws   = p.ndraw;
     A.draws    = (const gb_draw *)((const uint8_t *)p.in.p + p.o_draws);
     A.cell_off = p.cells.as<uint32_t>();
-    A.xings    = p.refs.as<uint32_t>();
+    A.refs     = p.refs.as<uint32_t>();
+    A.edges    = p.edges.as<int4>();
+    A.tri_a    = p.tri_a.as<int4>();
+    A.tri_b    = p.tri_b.as<int4>();
     A.samples  = s->d_samples;
     A.rgba     = s->d_rgba;
     A.cov_out  = p.dbg.as<int32_t>();

@@ -12,7 +12,10 @@ struct gb_raster_args {
     uint32_t        init_mode, init_color;
     const gb_draw  *draws;
     const uint32_t *cell_off; /* band-major (band * ndraws + draw) offsets, nbands*ndraws + 1 */
-    const uint32_t *xings;    /* crossing records (k << 5 | up-bit << 4 | row in band) */
+    const uint32_t *refs;
+    const int4     *edges;
+    const int4     *tri_a;
+    const int4     *tri_b;
     uint32_t       *samples; /* [nrows][Wpad] */
     uint32_t       *rgba;    /* [H][W] */
     int32_t        *cov_out; /* debug coverage output [H][W][S] or null */
@@ -72,10 +75,10 @@ cudaError_t gb_launch_stroke_tris(cudaStream_t st, uint32_t ntris, uint32_t ndra
                                   const uint32_t *sdraw_id, const uint32_t *draw_vbase, const gb_draw *draws,
                                   const float2 *verts, const uint32_t *inds, uint32_t W, uint32_t H, int4 *tri_a,
                                   int4 *tri_b, uint32_t *tri_draw);
-cudaError_t gb_launch_xings(cudaStream_t st, int emit, uint32_t nedges, const int4 *edges, const uint32_t *edge_draw,
-                            uint32_t ntris, const int4 *tri_a, const int4 *tri_b, const uint32_t *tri_draw,
-                            uint32_t ndraws, uint32_t W, uint32_t S, uint32_t nrows, uint32_t *cell, uint32_t *recs,
-                            uint32_t nrecs);
+cudaError_t gb_launch_bin(cudaStream_t st, int scatter, uint32_t nedges, const int4 *edges, const uint32_t *edge_draw,
+                          uint32_t ntris, const int4 *tri_a, const int4 *tri_b, const uint32_t *tri_draw,
+                          uint32_t ndraws, uint32_t W, uint32_t samples, uint32_t nrows, uint32_t *cell,
+                          uint32_t *edge_refs, uint32_t *tri_refs, uint32_t nrefs);
 
 cudaError_t gb_launch_raster(cudaStream_t st, const gb_raster_args *a);
 cudaError_t gb_launch_pmath_eval(cudaStream_t st, int fn, const float *a, const float *b, float *out, uint64_t n);

@@ -1,8 +1,7 @@
 /*
  * Frame pipeline: upload the recorded structure-of-arrays command buffers in
- * one copy, then run K1 flatten -> K2 stroke expansion -> K3 setup and
- * per-band crossing records -> K5 coverage/compositing on the context's
- * stream.  Output sizes
+ * one copy, then run K1 flatten -> K2 stroke expansion -> K3 setup and band
+ * binning -> K5 coverage/compositing on the context's stream.  Output sizes
  * are read back after each count+scan step (four small device->host reads
  * per frame); buffers only grow.
  */
@@ -304,9 +303,9 @@ cudaError_t Pipeline::run(const FrameHost &f, _vkvg_surface_t *surf, bool timing
     GROW(cells, (ncells + 1) * 4);
     GROW(cursor, (ncells + 1) * 4);
     CK(cudaMemsetAsync(cells.p, 0, (ncells + 1) * 4, st));
-    CK(gb_launch_xings(st, 0, nedges, edges.as<int4>(), edge_draw.as<uint32_t>(), ntris, tri_a.as<int4>(),
-                       tri_b.as<int4>(), tri_draw.as<uint32_t>(), ndraw, W, S, surf->nrows, cells.as<uint32_t>(),
-                       nullptr, 0u));
+    CK(gb_launch_bin(st, 0, nedges, edges.as<int4>(), edge_draw.as<uint32_t>(), ntris, tri_a.as<int4>(),
+                     tri_b.as<int4>(), tri_draw.as<uint32_t>(), ndraw, W, S, surf->nrows, cells.as<uint32_t>(),
+                     nullptr, nullptr, 0u));
     gb_count_launch((nedges ? 1 : 0) + (ntris ? 1 : 0));
     CK(scan(*this, cells.as<uint32_t>(), (uint32_t)ncells, cursor.as<uint32_t>()));
     CK(readback_u32(*this, cursor.as<uint32_t>() + ncells, hv, 1));
@@ -314,9 +313,9 @@ cudaError_t Pipeline::run(const FrameHost &f, _vkvg_surface_t *surf, bool timing
     GROW(refs, (size_t)(nrefs + 1) * 4);
     /* cells <- offsets (kept for the raster), cursor <- running copy */
     CK(cudaMemcpyAsync(cells.p, cursor.p, (ncells + 1) * 4, cudaMemcpyDeviceToDevice, st));
-    CK(gb_launch_xings(st, 1, nedges, edges.as<int4>(), edge_draw.as<uint32_t>(), ntris, tri_a.as<int4>(),
-                       tri_b.as<int4>(), tri_draw.as<uint32_t>(), ndraw, W, S, surf->nrows, cursor.as<uint32_t>(),
-                       refs.as<uint32_t>(), nrefs));
+    CK(gb_launch_bin(st, 1, nedges, edges.as<int4>(), edge_draw.as<uint32_t>(), ntris, tri_a.as<int4>(),
+                     tri_b.as<int4>(), tri_draw.as<uint32_t>(), ndraw, W, S, surf->nrows, cursor.as<uint32_t>(),
+                     refs.as<uint32_t>(), refs.as<uint32_t>(), nrefs));
     gb_count_launch((nedges ? 1 : 0) + (ntris ? 1 : 0));
     if (timing)
         CK(cudaEventRecord(evs[3], st));
@@ -348,7 +347,10 @@ cudaError_t Pipeline::run(const FrameHost &f, _vkvg_surface_t *surf, bool timing
     }
     A.draws    = draws;
     A.cell_off = cells.as<uint32_t>();
-    A.xings    = refs.as<uint32_t>();
+    A.refs     = refs.as<uint32_t>();
+    A.edges    = edges.as<int4>();
+    A.tri_a    = tri_a.as<int4>();
+    A.tri_b    = tri_b.as<int4>();
     A.samples  = surf->d_samples;
     A.rgba     = surf->d_rgba;
     CK(gb_launch_raster(st, &A));

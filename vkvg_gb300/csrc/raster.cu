@@ -6,20 +6,23 @@
  * Warp r owns sample row r; lane l owns its 32 consecutive samples, whose
  * premultiplied RGBA8 values stay in registers for the whole frame.
  *
- * Coverage is exact integer arithmetic.  The crossing kernels (setup.cu)
- * record, for every edge and every sample row it crosses, k = the number of
- * that row's samples lying left of the crossing, and the edge's direction.
- * An edge adds its direction to every sample left of its crossing (a sample
- * on the edge counts as if moved by (+e, +e^2): the top-left rule), so the
- * suffix sum of the records over a row is the winding number for a closed
- * polygon, or the covering-triangle count for positively oriented triangles.
- * Per draw, the CTA drops the draw's records of its band into shared-memory
- * counters, each warp suffix-scans its row with shuffles, and the fill rule
+ * Coverage is exact integer arithmetic on the snapped 24.8 vertices: an edge
+ * crossing sample row y at x_c adds its direction (+1 downward, -1 upward) to
+ * every sample with x < x_c (a sample on the edge counts as if moved by
+ * (+e, +e^2), which is the top-left rule).  Summed over a closed polygon this
+ * is its winding number; summed over positively oriented triangles it is the
+ * number of covering triangles.  Every (primitive, sample row) pair of a
+ * draw's band primitives is one work item: each edge crossing is computed
+ * exactly (an fp32 quotient estimate corrected by one 64-bit product test)
+ * and its direction is added to a shared-memory counter at the last sample
+ * left of the crossing.  Each lane then loads its 32 counters, the warp
+ * suffix-sums the lane totals with shuffles, and every lane walks its run
+ * right to left with one branch-free select per sample.  The fill rule
  * decides how many times vkvg's blend is applied per sample: even-odd ->
  * w & 1 (the stencil-INVERT fan of _poly_fill), non-zero -> w != 0 (glutess'
  * NONZERO tessellation), stroke -> w (each overlapping stroke triangle blends
- * once under pipe_OVER).  Lanes whose counters no record touched take a
- * uniform-winding fast path.  XT_D draws share one pair of barriers.
+ * once under pipe_OVER).  XT_D draws share one pair of barriers; a warp with
+ * no crossing and zero winding skips a draw.
  *
  * Blend (src/vkvg_device_internal.c:200-209, ONE / ONE_MINUS_SRC_ALPHA on
  * premultiplied UNORM8): d' = s + floor((d*(255-sa) + 127) / 255) per channel,
@@ -28,40 +31,127 @@
  */
 #include "gb_types.h"
 #include "launch.h"
+#include "xdiv.cuh"
 
 #include <cuda_runtime.h>
 
 #define XT_W        1024                 /* tile width in pixels */
 #define XT_THREADS  512                  /* 16 warps: one per sample row */
 #define XT_D        2                    /* draws per barrier pair */
-#define XCNT_W      (XT_W + 4)           /* counter k (1..1024) at [k + 3]: 16-byte aligned lane runs */
-#define XPLANE      (GB_BAND_ROWS * XCNT_W + GB_BAND_ROWS) /* counters + one touched mask per row */
+#define XPLANE      (GB_BAND_ROWS * XT_W) /* one crossing counter per tile sample */
 #define RASTER_SMEM (XT_D * XPLANE * 4)
 
-__device__ __forceinline__ uint32_t div255_2x(uint32_t x) {
-    /* per 16-bit lane: floor(x / 255) for x <= 65152 */
-    return ((x + ((x >> 8) & 0x00FF00FFu) + 0x00010001u) >> 8) & 0x00FF00FFu;
-}
-/* t = floor((d * inv + 127) / 255) per channel */
+/* blend modes: ADD is exact when every colour byte of the source is <= its
+   alpha byte (then s + t never carries); CLEAR is ADD with s = 0, inv = 0 */
+#define BM_ADD  0
+#define BM_SADD 1
+#define BM_SSUB 2
+
+/* t = floor((d * inv + 127) / 255) per channel, two channels per 32-bit
+   lane: floor(x / 255) = (x + (x >> 8) + 1) >> 8 for x <= 65152 */
 __device__ __forceinline__ uint32_t scaled_dst(uint32_t d, uint32_t inv) {
     uint32_t rb = (d & 0x00FF00FFu) * inv + 0x007F007Fu;
     uint32_t ag = ((d >> 8) & 0x00FF00FFu) * inv + 0x007F007Fu;
-    return div255_2x(rb) | (div255_2x(ag) << 8);
+    rb          = rb + ((rb >> 8) & 0x00FF00FFu) + 0x00010001u;
+    ag          = ag + ((ag >> 8) & 0x00FF00FFu) + 0x00010001u;
+    return ((rb >> 8) & 0x00FF00FFu) | (ag & 0xFF00FF00u);
 }
-__device__ __forceinline__ uint32_t blend(uint32_t d, uint32_t s, uint32_t inv, uint32_t op) {
-    if (op == GB_OP_CLEAR)
-        return 0u;
+template <int M> __device__ __forceinline__ uint32_t blend(uint32_t d, uint32_t s, uint32_t inv) {
     uint32_t t = scaled_dst(d, inv);
-    if (op == GB_OP_DIFFERENCE)
-        return __vsubus4(s, t);
-    return __vaddus4(s, t);
+    if (M == BM_ADD)
+        return s + t;
+    if (M == BM_SADD)
+        return __vaddus4(s, t);
+    return __vsubus4(s, t);
 }
-__device__ __forceinline__ int32_t rule(uint32_t kind, int32_t w) {
-    if (kind == GB_DRAW_FILL_EO)
-        return w & 1;
-    if (kind == GB_DRAW_FILL_NZ)
-        return w != 0;
-    return w > 0 ? w : 0;
+
+/* counter of tile sample p (0..1023) inside its row: each lane's 32-sample
+   run is eight 16-byte slots, rotated by the lane index so that the eight
+   lanes of one 128-byte phase hit distinct banks */
+__device__ __forceinline__ uint32_t swz(uint32_t p) {
+    return (p & ~31u) | (((((p >> 2) & 7u) ^ ((p >> 5) & 7u))) << 2) | (p & 3u);
+}
+
+/* one edge crossing sample row R (band row rr): add dir at the last tile
+   sample left of the crossing, so that the suffix sum from sample c is the
+   winding contribution at c */
+__device__ __forceinline__ void acc_row(int32_t x0, int32_t y0, int32_t x1, int32_t y1, int32_t sy, uint32_t rr,
+                                        int32_t ox, int32_t X0, int32_t TW, int32_t tx_lo, int32_t tx_hi,
+                                        int32_t *__restrict__ plane) {
+    const int32_t ylo = min(y0, y1), yhi = max(y0, y1);
+    if (sy < ylo || sy >= yhi)
+        return; /* also drops horizontal edges */
+    if (max(x0, x1) < tx_lo)
+        return; /* crossing left of every tile sample */
+    const int32_t dir = y0 < y1 ? 1 : -1;
+    int32_t       k;
+    if (min(x0, x1) > tx_hi) {
+        k = TW;
+    } else {
+        const int32_t   dy  = y1 - y0;
+        const int32_t   den = dy < 0 ? -dy : dy;
+        const int32_t   dxn = dy < 0 ? x0 - x1 : x1 - x0;
+        const long long c   = gb_ceil_muldiv(dxn, sy - y0, den);
+        const long long kt  = (((long long)x0 + c - 1 - ox) >> 8) + 1 - X0; /* tile samples left of crossing */
+        if (kt <= 0)
+            return;
+        k = kt > TW ? TW : (int32_t)kt;
+    }
+    atomicAdd(&plane[rr * XT_W + swz((uint32_t)(k - 1))], dir);
+}
+
+/* sum of v over the lanes above this one */
+__device__ __forceinline__ int32_t warp_suffix_excl(int32_t v, uint32_t l) {
+    int32_t incl = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int32_t u = __shfl_down_sync(0xffffffffu, incl, o);
+        if (l + o < 32)
+            incl += u;
+    }
+    return incl - v;
+}
+
+/* fills: blend once where (w & fmask) != 0 (fmask 1: even-odd, ~0: non-zero) */
+template <int M>
+__device__ __forceinline__ void fill_run(uint32_t (&col)[32], const int4 (&cn)[8], int32_t E, int32_t fmask,
+                                         uint32_t src, uint32_t inv) {
+    int32_t w = E;
+#pragma unroll
+    for (int q = 7; q >= 0; q--) {
+#pragma unroll
+        for (int e = 3; e >= 0; e--) {
+            const int c = 4 * q + e;
+            w += e == 3 ? cn[q].w : e == 2 ? cn[q].z : e == 1 ? cn[q].y : cn[q].x;
+            const uint32_t nb = blend<M>(col[c], src, inv);
+            col[c]            = (w & fmask) ? nb : col[c];
+        }
+    }
+}
+/* strokes: blend w times (w = number of covering triangles) */
+template <int M>
+__device__ __forceinline__ void stroke_run(uint32_t (&col)[32], const int4 (&cn)[8], int32_t E, uint32_t src,
+                                           uint32_t inv) {
+    int32_t kmax = 1;
+    for (int32_t rep = 0; rep < kmax; rep++) {
+        int32_t w = E;
+#pragma unroll
+        for (int q = 7; q >= 0; q--) {
+#pragma unroll
+            for (int e = 3; e >= 0; e--) {
+                const int c = 4 * q + e;
+                w += e == 3 ? cn[q].w : e == 2 ? cn[q].z : e == 1 ? cn[q].y : cn[q].x;
+                const uint32_t nb = blend<M>(col[c], src, inv);
+                col[c]            = w > rep ? nb : col[c];
+                kmax              = max(kmax, w);
+            }
+        }
+    }
+}
+template <int M> __device__ __forceinline__ void paint_run(uint32_t (&col)[32], uint32_t src, uint32_t inv) {
+#pragma unroll
+    for (int c = 0; c < 32; c++)
+        col[c] = blend<M>(col[c], src, inv);
 }
 
 __global__ void __launch_bounds__(XT_THREADS, 1) gb_raster(gb_raster_args A) {
@@ -75,10 +165,18 @@ __global__ void __launch_bounds__(XT_THREADS, 1) gb_raster(gb_raster_args A) {
     const bool     row_ok  = R < (int32_t)A.nrows;
     const int32_t  col0    = (int32_t)(32 * l);
     const int32_t  ncols   = row_ok ? max(0, min(32, TW - col0)) : 0;
+    const int32_t  band_r0 = (int32_t)(band * GB_BAND_ROWS);
+    const int32_t  tx_lo = X0 * 256 + 32, tx_hi = (X0 + TW - 1) * 256 + 224;
     const uint32_t nd      = A.ndraws;
     const size_t   cb      = (size_t)band * nd;
     const bool     dbg     = A.cov_out != nullptr;
     const uint32_t rpp     = A.S == 4 ? 4 : 1;
+    /* sample row geometry of the item rows this thread handles (rr = t & 15) */
+    const uint32_t irr = t & 15;
+    const int32_t  iR  = band_r0 + (int32_t)irr;
+    const bool     iok = iR < (int32_t)A.nrows;
+    const int32_t  isy = A.S == 4 ? 32 + 64 * iR : 128 + 256 * iR;
+    const int32_t  iox = A.S == 4 ? ((iR & 3) == 0 ? 96 : (iR & 3) == 1 ? 224 : (iR & 3) == 2 ? 32 : 160) : 128;
 
     uint32_t  col[32];
     uint32_t *srow = A.samples + (size_t)(row_ok ? R : 0) * A.Wpad + X0 + col0;
@@ -109,26 +207,40 @@ __global__ void __launch_bounds__(XT_THREADS, 1) gb_raster(gb_raster_args A) {
     const uint32_t dhi = dbg ? A.cov_draw + 1 : nd;
     for (uint32_t d0 = dlo; d0 < dhi; d0 += XT_D) {
         const uint32_t nb = min((uint32_t)XT_D, dhi - d0);
-        /* ---- drop the batch's crossing records into the counters */
+        /* ---- accumulate the batch's crossings: one item per (primitive, band row) */
         bool any = false;
         for (uint32_t j = 0; j < nb; j++) {
-            const uint32_t d  = d0 + j;
+            const uint32_t d    = d0 + j;
+            const uint32_t kind = A.draws[d].kind;
+            if (kind == GB_DRAW_PAINT || kind == GB_DRAW_CLEAR)
+                continue;
             const uint32_t lo = A.cell_off[cb + d], hi = A.cell_off[cb + d + 1];
             if (lo == hi)
                 continue;
-            any             = true;
-            int32_t  *plane = smem + j * XPLANE;
-            uint32_t *touch = reinterpret_cast<uint32_t *>(plane + GB_BAND_ROWS * XCNT_W);
-            for (uint32_t i = lo + t; i < hi; i += XT_THREADS) {
-                const uint32_t rec = A.xings[i];
-                int32_t        k   = (int32_t)(rec >> 5) - X0;
-                if (k <= 0)
-                    continue; /* no sample of this tile lies left of the crossing */
-                if (k > TW)
-                    k = TW;
-                const uint32_t rr = rec & (GB_BAND_ROWS - 1);
-                atomicAdd(&plane[rr * XCNT_W + k + 3], (rec & 16u) ? 1 : -1);
-                atomicOr(&touch[rr], 1u << ((k - 1) >> 5));
+            any            = true;
+            int32_t *plane = smem + j * XPLANE;
+            if (!iok)
+                continue;
+            const uint32_t n = (hi - lo) * 16u;
+            if (kind == GB_DRAW_STROKE) {
+                for (uint32_t it = t; it < n; it += XT_THREADS) {
+                    const uint32_t tr = A.refs[lo + (it >> 4)];
+                    const int4     ta = A.tri_a[tr], tb = A.tri_b[tr];
+                    const int32_t  ymn = min(min(ta.y, ta.w), tb.y), ymx = max(max(ta.y, ta.w), tb.y);
+                    if (isy < ymn || isy >= ymx)
+                        continue;
+                    const int32_t xmn = min(min(ta.x, ta.z), tb.x), xmx = max(max(ta.x, ta.z), tb.x);
+                    if (xmx < tx_lo || xmn > tx_hi)
+                        continue; /* wholly left or right: no net coverage in the tile */
+                    acc_row(ta.x, ta.y, ta.z, ta.w, isy, irr, iox, X0, TW, tx_lo, tx_hi, plane);
+                    acc_row(ta.z, ta.w, tb.x, tb.y, isy, irr, iox, X0, TW, tx_lo, tx_hi, plane);
+                    acc_row(tb.x, tb.y, ta.x, ta.y, isy, irr, iox, X0, TW, tx_lo, tx_hi, plane);
+                }
+            } else {
+                for (uint32_t it = t; it < n; it += XT_THREADS) {
+                    const int4 ed = A.edges[A.refs[lo + (it >> 4)]];
+                    acc_row(ed.x, ed.y, ed.z, ed.w, isy, irr, iox, X0, TW, tx_lo, tx_hi, plane);
+                }
             }
         }
         if (any)
@@ -138,16 +250,25 @@ __global__ void __launch_bounds__(XT_THREADS, 1) gb_raster(gb_raster_args A) {
             const uint32_t d    = d0 + j;
             const gb_draw &D    = A.draws[d];
             const uint32_t kind = D.kind;
-            const uint32_t src = D.src, inv = 255u - (src >> 24), op = D.op;
+            uint32_t       src = D.src, inv = 255u - (src >> 24);
+            const uint32_t op  = D.op;
+            if (op == GB_OP_CLEAR)
+                src = 0u, inv = 0u;
+            const uint32_t sa = src >> 24;
+            const bool     pm = (src & 0xFFu) <= sa && ((src >> 8) & 0xFFu) <= sa && ((src >> 16) & 0xFFu) <= sa;
+            const int      bm = op == GB_OP_DIFFERENCE ? BM_SSUB : pm ? BM_ADD : BM_SADD;
             if (kind == GB_DRAW_PAINT) {
                 if (dbg) {
                     for (int c = 0; c < ncols; c++)
                         A.cov_out[((size_t)(R / rpp) * A.W + X0 + col0 + c) * A.S + R % rpp] = 1;
                     continue;
                 }
-#pragma unroll
-                for (int c = 0; c < 32; c++)
-                    col[c] = blend(col[c], src, inv, op);
+                if (bm == BM_ADD)
+                    paint_run<BM_ADD>(col, src, inv);
+                else if (bm == BM_SADD)
+                    paint_run<BM_SADD>(col, src, inv);
+                else
+                    paint_run<BM_SSUB>(col, src, inv);
                 continue;
             }
             if (kind == GB_DRAW_CLEAR) {
@@ -159,65 +280,56 @@ __global__ void __launch_bounds__(XT_THREADS, 1) gb_raster(gb_raster_args A) {
             const uint32_t lo = A.cell_off[cb + d], hi = A.cell_off[cb + d + 1];
             if (lo == hi)
                 continue;
-            int32_t       *plane = smem + j * XPLANE;
-            uint32_t      *touch = reinterpret_cast<uint32_t *>(plane + GB_BAND_ROWS * XCNT_W);
-            const uint32_t tm    = touch[r];
-            const bool     mine  = (tm >> l) & 1u;
-            int4          *cp    = reinterpret_cast<int4 *>(plane + r * XCNT_W + col0 + 4);
-            int32_t        L     = 0;
-            if (mine) {
-#pragma unroll
-                for (int q = 0; q < 8; q++) {
-                    int4 x = cp[q];
-                    L += x.x + x.y + x.z + x.w;
-                }
-            }
-            int32_t incl = L;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                int32_t u = __shfl_down_sync(0xffffffffu, incl, o);
-                if (l + o < 32)
-                    incl += u;
-            }
-            const int32_t E = incl - L; /* records right of this lane's samples */
             if (dbg) {
-                int32_t w = E;
+                /* coverage of a single draw: read the counters in place */
+                const int32_t *ci = smem + j * XPLANE + r * XT_W;
+                int32_t        L  = 0;
+                for (int c = 0; c < 32; c++)
+                    L += ci[swz(col0 + c)];
+                int32_t w = warp_suffix_excl(L, l);
                 for (int c = 31; c >= 0; c--) {
-                    if (mine)
-                        w += plane[r * XCNT_W + col0 + c + 4];
+                    w += ci[swz(col0 + c)];
                     if (c < ncols)
                         A.cov_out[((size_t)(R / rpp) * A.W + X0 + col0 + c) * A.S + R % rpp] = w;
                 }
-            } else if (!mine) {
-                const int32_t k = ncols ? rule(kind, E) : 0;
-                for (int jj = 0; jj < k; jj++) {
+                continue;
+            }
+            /* this lane's 32 counters, then clear them for the next batch */
+            int4   *cp = reinterpret_cast<int4 *>(smem + j * XPLANE + r * XT_W + col0);
+            int4    cn[8];
+            int     nzr = 0;
+            int32_t L   = 0;
 #pragma unroll
-                    for (int c = 0; c < 32; c++)
-                        col[c] = blend(col[c], src, inv, op);
-                }
+            for (int q = 0; q < 8; q++) {
+                cn[q] = cp[q ^ (l & 7)];
+                nzr |= cn[q].x | cn[q].y | cn[q].z | cn[q].w;
+                L += cn[q].x + cn[q].y + cn[q].z + cn[q].w;
+            }
+#pragma unroll
+            for (int q = 0; q < 8; q++)
+                cp[q ^ (l & 7)] = make_int4(0, 0, 0, 0);
+            const int32_t E = warp_suffix_excl(L, l); /* winding from crossings right of this lane's run */
+            /* lanes with neither a crossing nor covering winding change nothing;
+               a warp where that holds for every lane skips the draw */
+            const bool work = row_ok && (nzr != 0 || E != 0);
+            if (!__any_sync(0xffffffffu, work))
+                continue;
+            if (kind == GB_DRAW_STROKE) {
+                if (bm == BM_ADD)
+                    stroke_run<BM_ADD>(col, cn, E, src, inv);
+                else if (bm == BM_SADD)
+                    stroke_run<BM_SADD>(col, cn, E, src, inv);
+                else
+                    stroke_run<BM_SSUB>(col, cn, E, src, inv);
             } else {
-                int32_t w = E;
-#pragma unroll
-                for (int q = 7; q >= 0; q--) {
-                    int4 x = cp[q];
-#pragma unroll
-                    for (int e = 3; e >= 0; e--) {
-                        const int c = 4 * q + e;
-                        w += e == 3 ? x.w : e == 2 ? x.z : e == 1 ? x.y : x.x;
-                        int32_t k = c < ncols ? rule(kind, w) : 0;
-                        for (int jj = 0; jj < k; jj++)
-                            col[c] = blend(col[c], src, inv, op);
-                    }
-                }
+                const int32_t fmask = kind == GB_DRAW_FILL_EO ? 1 : -1;
+                if (bm == BM_ADD)
+                    fill_run<BM_ADD>(col, cn, E, fmask, src, inv);
+                else if (bm == BM_SADD)
+                    fill_run<BM_SADD>(col, cn, E, fmask, src, inv);
+                else
+                    fill_run<BM_SSUB>(col, cn, E, fmask, src, inv);
             }
-            if (mine) {
-#pragma unroll
-                for (int q = 0; q < 8; q++)
-                    cp[q] = make_int4(0, 0, 0, 0);
-            }
-            __syncwarp();
-            if (l == 0)
-                touch[r] = 0u;
         }
         if (any)
             __syncthreads();
@@ -237,15 +349,17 @@ __global__ void __launch_bounds__(XT_THREADS, 1) gb_raster(gb_raster_args A) {
             if (c < ncols)
                 srow[c] = col[c];
     }
-    /* resolve through shared memory (aliases the counter planes) */
+    /* resolve through shared memory (aliases the counter planes); lanes
+       write their runs in the same rotated slot order as the counters */
     __syncthreads();
-    uint32_t *stage = reinterpret_cast<uint32_t *>(smem);
+    uint4 *stage4 = reinterpret_cast<uint4 *>(smem) + r * (XT_W / 4) + l * 8;
 #pragma unroll
-    for (int c = 0; c < 32; c++)
-        stage[r * XT_W + col0 + c] = col[c];
+    for (int q = 0; q < 8; q++)
+        stage4[q ^ (l & 7)] = make_uint4(col[4 * q], col[4 * q + 1], col[4 * q + 2], col[4 * q + 3]);
     __syncthreads();
-    const uint32_t prows = GB_BAND_ROWS / rpp;
-    const uint32_t npx   = prows * XT_W;
+    const uint32_t *stage = reinterpret_cast<const uint32_t *>(smem);
+    const uint32_t  prows = GB_BAND_ROWS / rpp;
+    const uint32_t  npx   = prows * XT_W;
     for (uint32_t q = t * 4; q < npx; q += XT_THREADS * 4) {
         uint32_t pr = q / XT_W, px = q % XT_W; /* 4 consecutive pixels px..px+3 */
         uint32_t py = band * prows + pr;
@@ -256,7 +370,7 @@ __global__ void __launch_bounds__(XT_THREADS, 1) gb_raster(gb_raster_args A) {
         for (int k = 0; k < 4; k++) {
             uint32_t s0 = 0, s1 = 0, s2 = 0, s3 = 0;
             for (uint32_t s = 0; s < rpp; s++) {
-                uint32_t v = stage[(pr * rpp + s) * XT_W + px + k];
+                uint32_t v = stage[(pr * rpp + s) * XT_W + swz(px + k)];
                 s0 += v & 0xFFu;
                 s1 += (v >> 8) & 0xFFu;
                 s2 += (v >> 16) & 0xFFu;

@@ -10,14 +10,12 @@
  * nearest even).  This unit is built with -fmad=false so the float steps match
  * the CPU restatement exactly.
  *
- * Crossings: the surface is cut into bands of 16 sample rows.  Every edge's
- * exact crossing of every sample row is computed once per frame and stored as
- * a 32-bit record in its (band, draw) cell: a count pass sizes the cells, an
- * exclusive scan in band-major order gives every band a contiguous,
- * draw-ordered list, and an emit pass writes the records.
+ * Binning: the surface is cut into bands of 16 sample rows.  Each primitive is
+ * counted into (band, draw) cells, an exclusive scan in band-major order gives
+ * every band a contiguous, draw-ordered list, and a scatter pass writes the
+ * primitive indices.
  */
 #include "gb_types.h"
-#include "xdiv.cuh"
 
 #include <cuda_runtime.h>
 
@@ -133,111 +131,84 @@ __global__ void gb_stroke_tris(uint32_t ntris, uint32_t ndraw_s, const uint32_t 
     tri_draw[t] = d;
 }
 
-/* sample rows R (0 <= R < nrows) with ylo <= off + R*step < yhi */
-__device__ __forceinline__ bool gb_rows(int32_t ylo, int32_t yhi, uint32_t S, uint32_t nrows, int32_t *ra,
-                                        int32_t *rb) {
-    const int32_t off = S == 4 ? 32 : 128;
-    const int32_t sh  = S == 4 ? 6 : 8;
-    long long     a   = ((long long)ylo - off + (1 << sh) - 1) >> sh; /* ceil((ylo - off) / step) */
-    long long     b   = (((long long)yhi - off + (1 << sh) - 1) >> sh) - 1;
-    if (a < 0)
-        a = 0;
-    if (b > (long long)nrows - 1)
-        b = (long long)nrows - 1;
-    *ra = (int32_t)a;
-    *rb = (int32_t)b;
-    return a <= b;
+/* sample-row range [r0, r1] crossed by the half-open y interval [ylo, yhi) */
+__device__ __forceinline__ void gb_row_range(int32_t ylo, int32_t yhi, uint32_t samples, int32_t *r0, int32_t *r1) {
+    long long off  = samples == 4 ? 32 : 128;
+    long long step = samples == 4 ? 64 : 256;
+    long long a = (long long)ylo - off, b = (long long)yhi - off;
+    /* ceil(a / step) */
+    long long ca = a >= 0 ? (a + step - 1) / step : -((-a) / step);
+    long long cb = b >= 0 ? (b + step - 1) / step : -((-b) / step);
+    *r0          = (int32_t)(ca < -2147483647LL ? -2147483647LL : ca);
+    *r1          = (int32_t)((cb - 1) > 2147483647LL ? 2147483647LL : cb - 1);
 }
 
-/* One directed edge's crossings of the surface's sample rows.
-   Count pass: add the number of crossings per band to its (band, draw) cell.
-   Emit pass: reserve the slots with one atomic per band and write one 32-bit
-   record per row: (k << 5) | (dir > 0) << 4 | (row within band), where k is
-   the number of samples of that row left of the crossing (clamped to
-   [0, W]); the exact crossing comes from one division at the first row and a
-   quotient/remainder walk down the rows. */
-template <bool EMIT>
-__device__ __forceinline__ void gb_edge_xings(int32_t x0, int32_t y0, int32_t x1, int32_t y1, uint32_t d, uint32_t nd,
-                                              uint32_t W, uint32_t S, uint32_t nrows, uint32_t *__restrict__ cell,
-                                              uint32_t *__restrict__ recs, uint32_t nrecs) {
-    if (y0 == y1)
-        return;
-    if (max(x0, x1) < 32)
-        return; /* left of every sample: adds to none */
-    int32_t ra, rb;
-    if (!gb_rows(min(y0, y1), max(y0, y1), S, nrows, &ra, &rb))
-        return;
-    const uint32_t b0 = (uint32_t)ra / GB_BAND_ROWS, b1 = (uint32_t)rb / GB_BAND_ROWS;
-    if (!EMIT) {
-        for (uint32_t b = b0; b <= b1; b++) {
-            int32_t lo = max(ra, (int32_t)(b * GB_BAND_ROWS)), hi = min(rb, (int32_t)(b * GB_BAND_ROWS + GB_BAND_ROWS - 1));
-            atomicAdd(&cell[(size_t)b * nd + d], (uint32_t)(hi - lo + 1));
-        }
-        return;
-    }
-    const uint32_t  dbit = y0 < y1 ? 16u : 0u;
-    const int32_t   off  = S == 4 ? 32 : 128;
-    const int32_t   sh   = S == 4 ? 6 : 8;
-    const int32_t   dy   = y1 - y0;
-    const int32_t   den  = dy < 0 ? -dy : dy;
-    const int32_t   dxn  = dy < 0 ? x0 - x1 : x1 - x0;
-    const long long num  = (long long)dxn * ((long long)off + ((long long)ra << sh) - y0);
-    long long       c    = gb_ceil_div(num, den); /* crossing - x0 at row ra, rounded up */
-    long long       rem  = c * den - num;         /* in [0, den) */
-    const long long dl   = (long long)dxn << sh;
-    const long long qd   = gb_floor_div(dl, den);
-    const long long rd   = dl - qd * den; /* in [0, den) */
-    int32_t         R    = ra;
-    for (uint32_t b = b0; b <= b1; b++) {
-        int32_t  hi   = min(rb, (int32_t)(b * GB_BAND_ROWS + GB_BAND_ROWS - 1));
-        uint32_t slot = atomicAdd(&cell[(size_t)b * nd + d], (uint32_t)(hi - R + 1));
-        for (; R <= hi; R++) {
-            const int32_t ox = S == 4 ? ((R & 3) == 0 ? 96 : (R & 3) == 1 ? 224 : (R & 3) == 2 ? 32 : 160) : 128;
-            long long     k  = (((long long)x0 + c - 1 - ox) >> 8) + 1; /* samples px*256+ox <= crossing */
-            if (k < 0)
-                k = 0;
-            if (k > (long long)W)
-                k = W;
-            if (slot < nrecs)
-                recs[slot] = ((uint32_t)k << 5) | dbit | (uint32_t)(R & (GB_BAND_ROWS - 1));
-            slot++;
-            rem -= rd;
-            c += qd;
-            if (rem < 0) {
-                rem += den;
-                c += 1;
-            }
-        }
-    }
+/* band range of a primitive, or false if it can touch no sample */
+__device__ __forceinline__ bool gb_prim_bands(int32_t ylo, int32_t yhi, int32_t xmin, int32_t xmax, bool is_tri,
+                                              uint32_t W, uint32_t samples, uint32_t nrows, uint32_t *b0,
+                                              uint32_t *b1) {
+    if (yhi <= ylo)
+        return false;
+    int32_t r0, r1;
+    gb_row_range(ylo, yhi, samples, &r0, &r1);
+    if (r0 < 0)
+        r0 = 0;
+    if (r1 > (int32_t)nrows - 1)
+        r1 = (int32_t)nrows - 1;
+    if (r0 > r1)
+        return false;
+    /* a crossing left of every sample adds nothing; a triangle right of every
+       sample covers nothing (an edge there still adds to whole rows) */
+    if (xmax < 32)
+        return false;
+    if (is_tri && (long long)xmin > (long long)W * 256)
+        return false;
+    *b0 = (uint32_t)r0 / GB_BAND_ROWS;
+    *b1 = (uint32_t)r1 / GB_BAND_ROWS;
+    return true;
 }
 
-template <bool EMIT>
-__global__ void gb_xing_edges(uint32_t nedges, const int4 *__restrict__ edges, const uint32_t *__restrict__ edge_draw,
-                              uint32_t nd, uint32_t W, uint32_t S, uint32_t nrows, uint32_t *__restrict__ cell,
-                              uint32_t *__restrict__ recs, uint32_t nrecs) {
+template <bool SCATTER>
+__global__ void gb_bin_edges(uint32_t nedges, const int4 *__restrict__ edges, const uint32_t *__restrict__ edge_draw,
+                             uint32_t ndraws, uint32_t W, uint32_t samples, uint32_t nrows,
+                             uint32_t *__restrict__ cell, uint32_t *__restrict__ refs, uint32_t nrefs) {
     uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= nedges)
         return;
-    int4 ed = edges[e];
-    gb_edge_xings<EMIT>(ed.x, ed.y, ed.z, ed.w, edge_draw[e], nd, W, S, nrows, cell, recs, nrecs);
+    int4     ed = edges[e];
+    uint32_t b0, b1;
+    int32_t  ylo = min(ed.y, ed.w), yhi = max(ed.y, ed.w);
+    if (!gb_prim_bands(ylo, yhi, min(ed.x, ed.z), max(ed.x, ed.z), false, W, samples, nrows, &b0, &b1))
+        return;
+    uint32_t d = edge_draw[e];
+    for (uint32_t b = b0; b <= b1; b++) {
+        uint32_t slot = atomicAdd(&cell[(size_t)b * ndraws + d], 1u);
+        if (SCATTER && slot < nrefs)
+            refs[slot] = e;
+    }
 }
-template <bool EMIT>
-__global__ void gb_xing_tris(uint32_t ntris, const int4 *__restrict__ tri_a, const int4 *__restrict__ tri_b,
-                             const uint32_t *__restrict__ tri_draw, uint32_t nd, uint32_t W, uint32_t S, uint32_t nrows,
-                             uint32_t *__restrict__ cell, uint32_t *__restrict__ recs, uint32_t nrecs) {
+template <bool SCATTER>
+__global__ void gb_bin_tris(uint32_t ntris, const int4 *__restrict__ tri_a, const int4 *__restrict__ tri_b,
+                            const uint32_t *__restrict__ tri_draw, uint32_t ndraws, uint32_t W, uint32_t samples,
+                            uint32_t nrows, uint32_t *__restrict__ cell, uint32_t *__restrict__ refs,
+                            uint32_t nrefs) {
     uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= ntris)
         return;
     int4 a = tri_a[t], b = tri_b[t];
     if (!b.z)
         return;
-    /* a closed triangle right of every sample adds +1 and -1 per row: nothing */
-    if (min(min(a.x, a.z), b.x) > (int32_t)((W - 1) * 256 + 224))
+    int32_t  ylo = min(min(a.y, a.w), b.y), yhi = max(max(a.y, a.w), b.y);
+    int32_t  xlo = min(min(a.x, a.z), b.x), xhi = max(max(a.x, a.z), b.x);
+    uint32_t b0, b1;
+    if (!gb_prim_bands(ylo, yhi, xlo, xhi, true, W, samples, nrows, &b0, &b1))
         return;
     uint32_t d = tri_draw[t];
-    gb_edge_xings<EMIT>(a.x, a.y, a.z, a.w, d, nd, W, S, nrows, cell, recs, nrecs);
-    gb_edge_xings<EMIT>(a.z, a.w, b.x, b.y, d, nd, W, S, nrows, cell, recs, nrecs);
-    gb_edge_xings<EMIT>(b.x, b.y, a.x, a.y, d, nd, W, S, nrows, cell, recs, nrecs);
+    for (uint32_t bb = b0; bb <= b1; bb++) {
+        uint32_t slot = atomicAdd(&cell[(size_t)bb * ndraws + d], 1u);
+        if (SCATTER && slot < nrefs)
+            refs[slot] = t;
+    }
 }
 
 extern "C" {
@@ -268,25 +239,25 @@ cudaError_t gb_launch_stroke_tris(cudaStream_t st, uint32_t ntris, uint32_t ndra
                                                          inds, W, H, tri_a, tri_b, tri_draw);
     return cudaGetLastError();
 }
-cudaError_t gb_launch_xings(cudaStream_t st, int emit, uint32_t nedges, const int4 *edges, const uint32_t *edge_draw,
-                            uint32_t ntris, const int4 *tri_a, const int4 *tri_b, const uint32_t *tri_draw,
-                            uint32_t ndraws, uint32_t W, uint32_t S, uint32_t nrows, uint32_t *cell, uint32_t *recs,
-                            uint32_t nrecs) {
+cudaError_t gb_launch_bin(cudaStream_t st, int scatter, uint32_t nedges, const int4 *edges, const uint32_t *edge_draw,
+                          uint32_t ntris, const int4 *tri_a, const int4 *tri_b, const uint32_t *tri_draw,
+                          uint32_t ndraws, uint32_t W, uint32_t samples, uint32_t nrows, uint32_t *cell,
+                          uint32_t *edge_refs, uint32_t *tri_refs, uint32_t nrefs) {
     if (nedges) {
-        if (emit)
-            gb_xing_edges<true><<<(nedges + 255) / 256, 256, 0, st>>>(nedges, edges, edge_draw, ndraws, W, S, nrows,
-                                                                       cell, recs, nrecs);
+        if (scatter)
+            gb_bin_edges<true><<<(nedges + 255) / 256, 256, 0, st>>>(nedges, edges, edge_draw, ndraws, W, samples,
+                                                                      nrows, cell, edge_refs, nrefs);
         else
-            gb_xing_edges<false><<<(nedges + 255) / 256, 256, 0, st>>>(nedges, edges, edge_draw, ndraws, W, S, nrows,
-                                                                        cell, nullptr, 0u);
+            gb_bin_edges<false><<<(nedges + 255) / 256, 256, 0, st>>>(nedges, edges, edge_draw, ndraws, W, samples,
+                                                                       nrows, cell, nullptr, 0u);
     }
     if (ntris) {
-        if (emit)
-            gb_xing_tris<true><<<(ntris + 255) / 256, 256, 0, st>>>(ntris, tri_a, tri_b, tri_draw, ndraws, W, S, nrows,
-                                                                     cell, recs, nrecs);
+        if (scatter)
+            gb_bin_tris<true><<<(ntris + 255) / 256, 256, 0, st>>>(ntris, tri_a, tri_b, tri_draw, ndraws, W, samples,
+                                                                    nrows, cell, tri_refs, nrefs);
         else
-            gb_xing_tris<false><<<(ntris + 255) / 256, 256, 0, st>>>(ntris, tri_a, tri_b, tri_draw, ndraws, W, S,
-                                                                      nrows, cell, nullptr, 0u);
+            gb_bin_tris<false><<<(ntris + 255) / 256, 256, 0, st>>>(ntris, tri_a, tri_b, tri_draw, ndraws, W, samples,
+                                                                     nrows, cell, nullptr, 0u);
     }
     return cudaGetLastError();
 }
