@@ -3,8 +3,11 @@
  *
  * One CTA (16 warps) owns a tile of up to 1024 pixels x 16 sample rows (4
  * pixel rows at 4x MSAA) and walks the frame's draws in submission order.
- * Warp r owns sample row r; lane l owns its 32 consecutive samples, whose
- * premultiplied RGBA8 values stay in registers for the whole frame.
+ * Warp w owns the 64-pixel strip [64w, 64w + 64) of all 16 rows; lane l owns
+ * the 32 consecutive samples of row l/2 starting at column 64w + 32(l&1),
+ * whose premultiplied RGBA8 values stay in registers for the whole frame.
+ * Compact 64 x 16 warp footprints let a warp skip a draw that neither crosses
+ * nor covers its strip, which for scribble-like paths is about half of them.
  *
  * Coverage is exact integer arithmetic on the snapped 24.8 vertices: an edge
  * crossing sample row y at x_c adds its direction (+1 downward, -1 upward) to
@@ -13,21 +16,33 @@
  * is its winding number; summed over positively oriented triangles it is the
  * number of covering triangles.  Every (primitive, sample row) pair of a
  * draw's band primitives is one work item: each edge crossing is computed
- * exactly (an fp32 quotient estimate corrected by one 64-bit product test)
+ * exactly (an fp32 quotient estimate corrected by one exact remainder test)
  * and its direction is added to a shared-memory counter at the last sample
- * left of the crossing.  Each lane then loads its 32 counters, the warp
- * suffix-sums the lane totals with shuffles, and every lane walks its run
- * right to left with one branch-free select per sample.  The fill rule
- * decides how many times vkvg's blend is applied per sample: even-odd ->
- * w & 1 (the stencil-INVERT fan of _poly_fill), non-zero -> w != 0 (glutess'
- * NONZERO tessellation), stroke -> w (each overlapping stroke triangle blends
- * once under pipe_OVER).  XT_D draws share one pair of barriers; a warp with
- * no crossing and zero winding skips a draw.
+ * left of the crossing, to the crossing's (row, strip) total, and the strip
+ * is flagged.  After one barrier each lane forms the winding entering its
+ * run from the strip totals to its right, loads its 32 counters (flagged
+ * strips only) and walks its run right to left with one branch-free select
+ * per sample.  The fill rule decides how many times vkvg's blend is applied
+ * per sample: even-odd -> w & 1 (the stencil-INVERT fan of _poly_fill),
+ * non-zero -> w != 0 (glutess' NONZERO tessellation), stroke -> w (each
+ * overlapping stroke triangle blends once under pipe_OVER).
+ *
+ * Counters and flags are double-buffered and strip totals triple-buffered by
+ * draw, so one barrier per draw orders everything: warps that finish a
+ * draw's blend start accumulating the next draw while others still blend.
  *
  * Blend (src/vkvg_device_internal.c:200-209, ONE / ONE_MINUS_SRC_ALPHA on
- * premultiplied UNORM8): d' = s + floor((d*(255-sa) + 127) / 255) per channel,
- * two channels per 32-bit lane, saturating.  At the end the tile writes its
- * samples back and the resolved pixels ((sum + S/2) / S) as 128-bit stores.
+ * premultiplied UNORM8): d' = s + floor((d*(255-sa) + 127) / 255) per channel.
+ * For a source whose colour bytes do not exceed its alpha (every colour set
+ * through the public API) s + t <= 255 and the blend runs on the FMA pipe:
+ * floor((d*inv + 127) / 255) = round(d * inv / 255) (no ties, 255 is odd),
+ * and with k = round(inv * 2^23 / 255) / 2^23 (error <= 2^-24, far below the
+ * 1/510 distance of d*inv/255 from a half-integer) one fmaf of
+ * (2^23 + d) * k + (1.5 * 2^23 + s - k * 2^23) leaves s + t in the low byte
+ * of the float's bits (checked exhaustively over d, inv and s <= sa).  Other
+ * sources and DIFFERENCE use saturating two-channel integer arithmetic.  At
+ * the end the tile writes its samples back and the resolved pixels
+ * ((sum + S/2) / S) as 128-bit stores.
  */
 #include "gb_types.h"
 #include "launch.h"
@@ -35,17 +50,26 @@
 
 #include <cuda_runtime.h>
 
-#define XT_W        1024                 /* tile width in pixels */
-#define XT_THREADS  512                  /* 16 warps: one per sample row */
-#define XT_D        2                    /* draws per barrier pair */
-#define XPLANE      (GB_BAND_ROWS * XT_W) /* one crossing counter per tile sample */
-#define RASTER_SMEM (XT_D * XPLANE * 4)
+#define XT_W       1024 /* tile width in pixels */
+#define XT_THREADS 512  /* 16 warps, one per 64-pixel strip */
+#define XT_STRIPS  16
+#define XPLANE     (GB_BAND_ROWS * XT_W) /* one crossing counter per tile sample */
+#define TOT_ROW    20                    /* strip totals per row, padded against bank conflicts */
+#define TOT_SET    (GB_BAND_ROWS * TOT_ROW)
+/* shared memory: 2 counter planes, 3 strip-total sets, 2 flag sets */
+#define SM_TOT      (2 * XPLANE)
+#define SM_FLAG     (SM_TOT + 3 * TOT_SET)
+#define SM_WORDS    (SM_FLAG + 2 * XT_STRIPS)
+#define RASTER_SMEM (SM_WORDS * 4)
 
-/* blend modes: ADD is exact when every colour byte of the source is <= its
-   alpha byte (then s + t never carries); CLEAR is ADD with s = 0, inv = 0 */
-#define BM_ADD  0
-#define BM_SADD 1
-#define BM_SSUB 2
+#define BM_ADD  0 /* valid premultiplied source: exact on the FMA pipe */
+#define BM_SADD 1 /* saturating add */
+#define BM_SSUB 2 /* DIFFERENCE: saturating subtract */
+
+struct blend_k {
+    uint32_t src, inv;          /* integer modes */
+    float    k, c0, c1, c2, c3; /* BM_ADD */
+};
 
 /* t = floor((d * inv + 127) / 255) per channel, two channels per 32-bit
    lane: floor(x / 255) = (x + (x >> 8) + 1) >> 8 for x <= 65152 */
@@ -56,28 +80,57 @@ __device__ __forceinline__ uint32_t scaled_dst(uint32_t d, uint32_t inv) {
     ag          = ag + ((ag >> 8) & 0x00FF00FFu) + 0x00010001u;
     return ((rb >> 8) & 0x00FF00FFu) | (ag & 0xFF00FF00u);
 }
-template <int M> __device__ __forceinline__ uint32_t blend(uint32_t d, uint32_t s, uint32_t inv) {
-    uint32_t t = scaled_dst(d, inv);
-    if (M == BM_ADD)
-        return s + t;
+template <int M> __device__ __forceinline__ uint32_t blend(uint32_t d, const blend_k &B) {
+    if (M == BM_ADD) {
+        /* byte c of d as the float 2^23 + d_c, then one fmaf per channel */
+        const float    z0 = fmaf(__uint_as_float(__byte_perm(d, 0x4B000000u, 0x7440)), B.k, B.c0);
+        const float    z1 = fmaf(__uint_as_float(__byte_perm(d, 0x4B000000u, 0x7441)), B.k, B.c1);
+        const float    z2 = fmaf(__uint_as_float(__byte_perm(d, 0x4B000000u, 0x7442)), B.k, B.c2);
+        const float    z3 = fmaf(__uint_as_float(__byte_perm(d, 0x4B000000u, 0x7443)), B.k, B.c3);
+        const uint32_t lo = __byte_perm(__float_as_uint(z0), __float_as_uint(z1), 0x0040);
+        const uint32_t hi = __byte_perm(__float_as_uint(z2), __float_as_uint(z3), 0x0040);
+        return __byte_perm(lo, hi, 0x5410);
+    }
+    const uint32_t t = scaled_dst(d, B.inv);
     if (M == BM_SADD)
-        return __vaddus4(s, t);
-    return __vsubus4(s, t);
+        return __vaddus4(B.src, t);
+    return __vsubus4(B.src, t);
 }
 
-/* counter of tile sample p (0..1023) inside its row: each lane's 32-sample
-   run is eight 16-byte slots, rotated by the lane index so that the eight
-   lanes of one 128-byte phase hit distinct banks */
-__device__ __forceinline__ uint32_t swz(uint32_t p) {
-    return (p & ~31u) | (((((p >> 2) & 7u) ^ ((p >> 5) & 7u))) << 2) | (p & 3u);
+__device__ __forceinline__ blend_k make_blend(uint32_t src, uint32_t op, int *mode) {
+    blend_k B;
+    if (op == GB_OP_CLEAR)
+        src = 0u;
+    const uint32_t sa  = src >> 24;
+    const uint32_t inv = op == GB_OP_CLEAR ? 0u : 255u - sa;
+    B.src              = src;
+    B.inv              = inv;
+    const uint32_t kq  = ((inv << 23) + 127u) / 255u; /* round(inv * 2^23 / 255) <= 2^23 */
+    B.k                = (float)kq * (1.0f / 8388608.0f);
+    B.c0               = (float)(12582912 + (int32_t)(src & 0xFFu) - (int32_t)kq);
+    B.c1               = (float)(12582912 + (int32_t)((src >> 8) & 0xFFu) - (int32_t)kq);
+    B.c2               = (float)(12582912 + (int32_t)((src >> 16) & 0xFFu) - (int32_t)kq);
+    B.c3               = (float)(12582912 + (int32_t)sa - (int32_t)kq);
+    const bool pm      = (src & 0xFFu) <= sa && ((src >> 8) & 0xFFu) <= sa && ((src >> 16) & 0xFFu) <= sa;
+    *mode              = op == GB_OP_DIFFERENCE ? BM_SSUB : pm ? BM_ADD : BM_SADD;
+    return B;
 }
 
-/* one edge crossing sample row R (band row rr): add dir at the last tile
+/* counter (or staged sample) of tile sample p in band row rr: each lane run
+   of 32 samples is eight 16-byte slots, rotated by the row and the run's
+   half-strip so that the eight lanes of one 128-byte phase hit distinct banks */
+__device__ __forceinline__ uint32_t swz(uint32_t rr, uint32_t p) {
+    const uint32_t v = ((rr & 3u) << 1) | ((p >> 5) & 1u);
+    return rr * XT_W + (((p >> 2) ^ v) << 2) + (p & 3u);
+}
+
+/* one edge crossing sample row sy (band row rr): add dir at the last tile
    sample left of the crossing, so that the suffix sum from sample c is the
    winding contribution at c */
 __device__ __forceinline__ void acc_row(int32_t x0, int32_t y0, int32_t x1, int32_t y1, int32_t sy, uint32_t rr,
                                         int32_t ox, int32_t X0, int32_t TW, int32_t tx_lo, int32_t tx_hi,
-                                        int32_t *__restrict__ plane) {
+                                        int32_t *__restrict__ plane, int32_t *__restrict__ tot,
+                                        int32_t *__restrict__ flag) {
     const int32_t ylo = min(y0, y1), yhi = max(y0, y1);
     if (sy < ylo || sy >= yhi)
         return; /* also drops horizontal edges */
@@ -97,25 +150,17 @@ __device__ __forceinline__ void acc_row(int32_t x0, int32_t y0, int32_t x1, int3
             return;
         k = kt > TW ? TW : (int32_t)kt;
     }
-    atomicAdd(&plane[rr * XT_W + swz((uint32_t)(k - 1))], dir);
+    const uint32_t p = (uint32_t)(k - 1);
+    atomicAdd(&plane[swz(rr, p)], dir);
+    atomicAdd(&tot[rr * TOT_ROW + (p >> 6)], dir);
+    flag[p >> 6] = 1;
 }
 
-/* sum of v over the lanes above this one */
-__device__ __forceinline__ int32_t warp_suffix_excl(int32_t v, uint32_t l) {
-    int32_t incl = v;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        int32_t u = __shfl_down_sync(0xffffffffu, incl, o);
-        if (l + o < 32)
-            incl += u;
-    }
-    return incl - v;
-}
-
-/* fills: blend once where (w & fmask) != 0 (fmask 1: even-odd, ~0: non-zero) */
+/* fills on a run with crossings: blend where (w & fmask) != 0
+   (fmask 1: even-odd, ~0: non-zero) */
 template <int M>
 __device__ __forceinline__ void fill_run(uint32_t (&col)[32], const int4 (&cn)[8], int32_t E, int32_t fmask,
-                                         uint32_t src, uint32_t inv) {
+                                         const blend_k &B) {
     int32_t w = E;
 #pragma unroll
     for (int q = 7; q >= 0; q--) {
@@ -123,15 +168,14 @@ __device__ __forceinline__ void fill_run(uint32_t (&col)[32], const int4 (&cn)[8
         for (int e = 3; e >= 0; e--) {
             const int c = 4 * q + e;
             w += e == 3 ? cn[q].w : e == 2 ? cn[q].z : e == 1 ? cn[q].y : cn[q].x;
-            const uint32_t nb = blend<M>(col[c], src, inv);
+            const uint32_t nb = blend<M>(col[c], B);
             col[c]            = (w & fmask) ? nb : col[c];
         }
     }
 }
-/* strokes: blend w times (w = number of covering triangles) */
+/* strokes on a run with crossings: blend w times (w = covering triangles) */
 template <int M>
-__device__ __forceinline__ void stroke_run(uint32_t (&col)[32], const int4 (&cn)[8], int32_t E, uint32_t src,
-                                           uint32_t inv) {
+__device__ __forceinline__ void stroke_run(uint32_t (&col)[32], const int4 (&cn)[8], int32_t E, const blend_k &B) {
     int32_t kmax = 1;
     for (int32_t rep = 0; rep < kmax; rep++) {
         int32_t w = E;
@@ -141,29 +185,33 @@ __device__ __forceinline__ void stroke_run(uint32_t (&col)[32], const int4 (&cn)
             for (int e = 3; e >= 0; e--) {
                 const int c = 4 * q + e;
                 w += e == 3 ? cn[q].w : e == 2 ? cn[q].z : e == 1 ? cn[q].y : cn[q].x;
-                const uint32_t nb = blend<M>(col[c], src, inv);
+                const uint32_t nb = blend<M>(col[c], B);
                 col[c]            = w > rep ? nb : col[c];
                 kmax              = max(kmax, w);
             }
         }
     }
 }
-template <int M> __device__ __forceinline__ void paint_run(uint32_t (&col)[32], uint32_t src, uint32_t inv) {
+/* a run without crossings: blend every sample k times */
+template <int M> __device__ __forceinline__ void uniform_run(uint32_t (&col)[32], int32_t k, const blend_k &B) {
+    for (int32_t rep = 0; rep < k; rep++) {
 #pragma unroll
-    for (int c = 0; c < 32; c++)
-        col[c] = blend<M>(col[c], src, inv);
+        for (int c = 0; c < 32; c++)
+            col[c] = blend<M>(col[c], B);
+    }
 }
 
 __global__ void __launch_bounds__(XT_THREADS, 1) gb_raster(gb_raster_args A) {
     extern __shared__ __align__(16) int32_t smem[];
 
-    const uint32_t t = threadIdx.x, r = t >> 5, l = t & 31;
+    const uint32_t t = threadIdx.x, wi = t >> 5, l = t & 31;
+    const uint32_t rl = l >> 1, hh = l & 1; /* blend mapping: band row and half-strip */
     const uint32_t band    = blockIdx.y;
     const int32_t  X0      = (int32_t)(blockIdx.x * XT_W);
     const int32_t  TW      = min((int32_t)XT_W, (int32_t)A.W - X0);
-    const int32_t  R       = (int32_t)(band * GB_BAND_ROWS + r);
+    const int32_t  R       = (int32_t)(band * GB_BAND_ROWS + rl);
     const bool     row_ok  = R < (int32_t)A.nrows;
-    const int32_t  col0    = (int32_t)(32 * l);
+    const int32_t  col0    = (int32_t)(64 * wi + 32 * hh);
     const int32_t  ncols   = row_ok ? max(0, min(32, TW - col0)) : 0;
     const int32_t  band_r0 = (int32_t)(band * GB_BAND_ROWS);
     const int32_t  tx_lo = X0 * 256 + 32, tx_hi = (X0 + TW - 1) * 256 + 224;
@@ -171,7 +219,8 @@ __global__ void __launch_bounds__(XT_THREADS, 1) gb_raster(gb_raster_args A) {
     const size_t   cb      = (size_t)band * nd;
     const bool     dbg     = A.cov_out != nullptr;
     const uint32_t rpp     = A.S == 4 ? 4 : 1;
-    /* sample row geometry of the item rows this thread handles (rr = t & 15) */
+    const uint32_t v_lane  = ((rl & 3u) << 1) | hh; /* slot rotation of this lane's run */
+    /* accumulate mapping: item rows (rr = t & 15) */
     const uint32_t irr = t & 15;
     const int32_t  iR  = band_r0 + (int32_t)irr;
     const bool     iok = iR < (int32_t)A.nrows;
@@ -199,140 +248,148 @@ __global__ void __launch_bounds__(XT_THREADS, 1) gb_raster(gb_raster_args A) {
         for (int c = 0; c < 32; c++)
             col[c] = c < ncols ? srow[c] : 0u;
     }
-    for (uint32_t i = t; i < XT_D * XPLANE; i += XT_THREADS)
+    for (uint32_t i = t; i < SM_WORDS; i += XT_THREADS)
         smem[i] = 0;
     __syncthreads();
 
-    const uint32_t dlo = dbg ? A.cov_draw : A.draw_first;
-    const uint32_t dhi = dbg ? A.cov_draw + 1 : nd;
-    for (uint32_t d0 = dlo; d0 < dhi; d0 += XT_D) {
-        const uint32_t nb = min((uint32_t)XT_D, dhi - d0);
-        /* ---- accumulate the batch's crossings: one item per (primitive, band row) */
-        bool any = false;
-        for (uint32_t j = 0; j < nb; j++) {
-            const uint32_t d    = d0 + j;
-            const uint32_t kind = A.draws[d].kind;
-            if (kind == GB_DRAW_PAINT || kind == GB_DRAW_CLEAR)
+    const uint32_t dlo   = dbg ? A.cov_draw : A.draw_first;
+    const uint32_t dhi   = dbg ? A.cov_draw + 1 : nd;
+    uint32_t       nproc = 0; /* draws with geometry in this band so far */
+    for (uint32_t d = dlo; d < dhi; d++) {
+        const gb_draw &D    = A.draws[d];
+        const uint32_t kind = D.kind;
+        int            bm;
+        if (kind == GB_DRAW_PAINT) {
+            const blend_k B = make_blend(D.src, D.op, &bm);
+            if (dbg) {
+                for (int c = 0; c < ncols; c++)
+                    A.cov_out[((size_t)(R / rpp) * A.W + X0 + col0 + c) * A.S + R % rpp] = 1;
                 continue;
-            const uint32_t lo = A.cell_off[cb + d], hi = A.cell_off[cb + d + 1];
-            if (lo == hi)
-                continue;
-            any            = true;
-            int32_t *plane = smem + j * XPLANE;
-            if (!iok)
-                continue;
+            }
+            if (bm == BM_ADD)
+                uniform_run<BM_ADD>(col, 1, B);
+            else if (bm == BM_SADD)
+                uniform_run<BM_SADD>(col, 1, B);
+            else
+                uniform_run<BM_SSUB>(col, 1, B);
+            continue;
+        }
+        if (kind == GB_DRAW_CLEAR) {
+#pragma unroll
+            for (int c = 0; c < 32; c++)
+                col[c] = 0u;
+            continue;
+        }
+        const uint32_t lo = A.cell_off[cb + d], hi = A.cell_off[cb + d + 1];
+        if (lo == hi)
+            continue;
+        const blend_k B = make_blend(D.src, D.op, &bm);
+        int32_t *plane = smem + (nproc & 1) * XPLANE;
+        int32_t *tot   = smem + SM_TOT + (nproc % 3) * TOT_SET;
+        int32_t *flag  = smem + SM_FLAG + (nproc & 1) * XT_STRIPS;
+
+        /* ---- accumulate: one item per (primitive, band row) */
+        if (iok) {
             const uint32_t n = (hi - lo) * 16u;
             if (kind == GB_DRAW_STROKE) {
                 for (uint32_t it = t; it < n; it += XT_THREADS) {
-                    const uint32_t tr = A.refs[lo + (it >> 4)];
-                    const int4     ta = A.tri_a[tr], tb = A.tri_b[tr];
+                    const uint32_t tr  = A.refs[lo + (it >> 4)];
+                    const int4     ta  = A.tri_a[tr], tb = A.tri_b[tr];
                     const int32_t  ymn = min(min(ta.y, ta.w), tb.y), ymx = max(max(ta.y, ta.w), tb.y);
                     if (isy < ymn || isy >= ymx)
                         continue;
                     const int32_t xmn = min(min(ta.x, ta.z), tb.x), xmx = max(max(ta.x, ta.z), tb.x);
                     if (xmx < tx_lo || xmn > tx_hi)
                         continue; /* wholly left or right: no net coverage in the tile */
-                    acc_row(ta.x, ta.y, ta.z, ta.w, isy, irr, iox, X0, TW, tx_lo, tx_hi, plane);
-                    acc_row(ta.z, ta.w, tb.x, tb.y, isy, irr, iox, X0, TW, tx_lo, tx_hi, plane);
-                    acc_row(tb.x, tb.y, ta.x, ta.y, isy, irr, iox, X0, TW, tx_lo, tx_hi, plane);
+                    acc_row(ta.x, ta.y, ta.z, ta.w, isy, irr, iox, X0, TW, tx_lo, tx_hi, plane, tot, flag);
+                    acc_row(ta.z, ta.w, tb.x, tb.y, isy, irr, iox, X0, TW, tx_lo, tx_hi, plane, tot, flag);
+                    acc_row(tb.x, tb.y, ta.x, ta.y, isy, irr, iox, X0, TW, tx_lo, tx_hi, plane, tot, flag);
                 }
             } else {
                 for (uint32_t it = t; it < n; it += XT_THREADS) {
                     const int4 ed = A.edges[A.refs[lo + (it >> 4)]];
-                    acc_row(ed.x, ed.y, ed.z, ed.w, isy, irr, iox, X0, TW, tx_lo, tx_hi, plane);
+                    acc_row(ed.x, ed.y, ed.z, ed.w, isy, irr, iox, X0, TW, tx_lo, tx_hi, plane, tot, flag);
                 }
             }
         }
-        if (any)
-            __syncthreads();
-        /* ---- apply the batch's draws in order */
-        for (uint32_t j = 0; j < nb; j++) {
-            const uint32_t d    = d0 + j;
-            const gb_draw &D    = A.draws[d];
-            const uint32_t kind = D.kind;
-            uint32_t       src = D.src, inv = 255u - (src >> 24);
-            const uint32_t op  = D.op;
-            if (op == GB_OP_CLEAR)
-                src = 0u, inv = 0u;
-            const uint32_t sa = src >> 24;
-            const bool     pm = (src & 0xFFu) <= sa && ((src >> 8) & 0xFFu) <= sa && ((src >> 16) & 0xFFu) <= sa;
-            const int      bm = op == GB_OP_DIFFERENCE ? BM_SSUB : pm ? BM_ADD : BM_SADD;
-            if (kind == GB_DRAW_PAINT) {
-                if (dbg) {
-                    for (int c = 0; c < ncols; c++)
-                        A.cov_out[((size_t)(R / rpp) * A.W + X0 + col0 + c) * A.S + R % rpp] = 1;
-                    continue;
-                }
-                if (bm == BM_ADD)
-                    paint_run<BM_ADD>(col, src, inv);
-                else if (bm == BM_SADD)
-                    paint_run<BM_SADD>(col, src, inv);
-                else
-                    paint_run<BM_SSUB>(col, src, inv);
-                continue;
+        __syncthreads();
+
+        /* ---- blend.  The previous draw's totals are no longer read by anyone. */
+        if (hh == 0)
+            smem[SM_TOT + ((nproc + 2) % 3) * TOT_SET + rl * TOT_ROW + wi] = 0;
+        nproc++;
+        int32_t Er = 0; /* winding from strips to the right */
+        for (uint32_t w2 = wi + 1; w2 < XT_STRIPS; w2++)
+            Er += tot[rl * TOT_ROW + w2];
+        const bool flagged = flag[wi] != 0;
+
+        if (dbg) {
+            /* coverage of a single draw: read the counters in place */
+            int32_t L = 0;
+            for (int c = 0; c < 32; c++)
+                L += plane[swz(rl, col0 + c)];
+            const int32_t Lp = __shfl_xor_sync(0xffffffffu, L, 1);
+            int32_t       w  = Er + (hh == 0 ? Lp : 0);
+            for (int c = 31; c >= 0; c--) {
+                w += plane[swz(rl, col0 + c)];
+                if (c < ncols)
+                    A.cov_out[((size_t)(R / rpp) * A.W + X0 + col0 + c) * A.S + R % rpp] = w;
             }
-            if (kind == GB_DRAW_CLEAR) {
-#pragma unroll
-                for (int c = 0; c < 32; c++)
-                    col[c] = 0u;
-                continue;
-            }
-            const uint32_t lo = A.cell_off[cb + d], hi = A.cell_off[cb + d + 1];
-            if (lo == hi)
-                continue;
-            if (dbg) {
-                /* coverage of a single draw: read the counters in place */
-                const int32_t *ci = smem + j * XPLANE + r * XT_W;
-                int32_t        L  = 0;
-                for (int c = 0; c < 32; c++)
-                    L += ci[swz(col0 + c)];
-                int32_t w = warp_suffix_excl(L, l);
-                for (int c = 31; c >= 0; c--) {
-                    w += ci[swz(col0 + c)];
-                    if (c < ncols)
-                        A.cov_out[((size_t)(R / rpp) * A.W + X0 + col0 + c) * A.S + R % rpp] = w;
-                }
-                continue;
-            }
-            /* this lane's 32 counters, then clear them for the next batch */
-            int4   *cp = reinterpret_cast<int4 *>(smem + j * XPLANE + r * XT_W + col0);
-            int4    cn[8];
-            int     nzr = 0;
-            int32_t L   = 0;
-#pragma unroll
-            for (int q = 0; q < 8; q++) {
-                cn[q] = cp[q ^ (l & 7)];
-                nzr |= cn[q].x | cn[q].y | cn[q].z | cn[q].w;
-                L += cn[q].x + cn[q].y + cn[q].z + cn[q].w;
-            }
-#pragma unroll
-            for (int q = 0; q < 8; q++)
-                cp[q ^ (l & 7)] = make_int4(0, 0, 0, 0);
-            const int32_t E = warp_suffix_excl(L, l); /* winding from crossings right of this lane's run */
-            /* lanes with neither a crossing nor covering winding change nothing;
-               a warp where that holds for every lane skips the draw */
-            const bool work = row_ok && (nzr != 0 || E != 0);
-            if (!__any_sync(0xffffffffu, work))
-                continue;
-            if (kind == GB_DRAW_STROKE) {
-                if (bm == BM_ADD)
-                    stroke_run<BM_ADD>(col, cn, E, src, inv);
-                else if (bm == BM_SADD)
-                    stroke_run<BM_SADD>(col, cn, E, src, inv);
-                else
-                    stroke_run<BM_SSUB>(col, cn, E, src, inv);
-            } else {
-                const int32_t fmask = kind == GB_DRAW_FILL_EO ? 1 : -1;
-                if (bm == BM_ADD)
-                    fill_run<BM_ADD>(col, cn, E, fmask, src, inv);
-                else if (bm == BM_SADD)
-                    fill_run<BM_SADD>(col, cn, E, fmask, src, inv);
-                else
-                    fill_run<BM_SSUB>(col, cn, E, fmask, src, inv);
-            }
+            continue;
         }
-        if (any)
-            __syncthreads();
+        if (!flagged) {
+            /* no crossing in the strip: every run has the uniform winding Er */
+            int32_t k = 0;
+            if (row_ok)
+                k = kind == GB_DRAW_STROKE ? max(Er, 0) : kind == GB_DRAW_FILL_EO ? (Er & 1) : (Er != 0);
+            if (!__any_sync(0xffffffffu, k > 0))
+                continue;
+            if (bm == BM_ADD)
+                uniform_run<BM_ADD>(col, k, B);
+            else if (bm == BM_SADD)
+                uniform_run<BM_SADD>(col, k, B);
+            else
+                uniform_run<BM_SSUB>(col, k, B);
+            continue;
+        }
+        /* this lane's 32 counters, then clear them for the draw after next */
+        int4   *cp = reinterpret_cast<int4 *>(plane + rl * XT_W + col0);
+        int4    cn[8];
+        int     nzr = 0;
+        int32_t L   = 0;
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+            cn[q] = cp[q ^ v_lane];
+            nzr |= cn[q].x | cn[q].y | cn[q].z | cn[q].w;
+            L += cn[q].x + cn[q].y + cn[q].z + cn[q].w;
+        }
+#pragma unroll
+        for (int q = 0; q < 8; q++)
+            cp[q ^ v_lane] = make_int4(0, 0, 0, 0);
+        __syncwarp();
+        if (l == 0)
+            flag[wi] = 0;
+        const int32_t Lp   = __shfl_xor_sync(0xffffffffu, L, 1);
+        const int32_t E    = Er + (hh == 0 ? Lp : 0); /* winding entering this run from the right */
+        const bool    work = row_ok && (nzr != 0 || E != 0);
+        if (!__any_sync(0xffffffffu, work))
+            continue;
+        if (kind == GB_DRAW_STROKE) {
+            if (bm == BM_ADD)
+                stroke_run<BM_ADD>(col, cn, E, B);
+            else if (bm == BM_SADD)
+                stroke_run<BM_SADD>(col, cn, E, B);
+            else
+                stroke_run<BM_SSUB>(col, cn, E, B);
+        } else {
+            const int32_t fmask = kind == GB_DRAW_FILL_EO ? 1 : -1;
+            if (bm == BM_ADD)
+                fill_run<BM_ADD>(col, cn, E, fmask, B);
+            else if (bm == BM_SADD)
+                fill_run<BM_SADD>(col, cn, E, fmask, B);
+            else
+                fill_run<BM_SSUB>(col, cn, E, fmask, B);
+        }
     }
     if (dbg)
         return;
@@ -350,12 +407,12 @@ __global__ void __launch_bounds__(XT_THREADS, 1) gb_raster(gb_raster_args A) {
                 srow[c] = col[c];
     }
     /* resolve through shared memory (aliases the counter planes); lanes
-       write their runs in the same rotated slot order as the counters */
+       stage their runs in the counters' rotated slot order */
     __syncthreads();
-    uint4 *stage4 = reinterpret_cast<uint4 *>(smem) + r * (XT_W / 4) + l * 8;
+    uint4 *stage4 = reinterpret_cast<uint4 *>(smem + rl * XT_W + col0);
 #pragma unroll
     for (int q = 0; q < 8; q++)
-        stage4[q ^ (l & 7)] = make_uint4(col[4 * q], col[4 * q + 1], col[4 * q + 2], col[4 * q + 3]);
+        stage4[q ^ v_lane] = make_uint4(col[4 * q], col[4 * q + 1], col[4 * q + 2], col[4 * q + 3]);
     __syncthreads();
     const uint32_t *stage = reinterpret_cast<const uint32_t *>(smem);
     const uint32_t  prows = GB_BAND_ROWS / rpp;
@@ -370,7 +427,7 @@ __global__ void __launch_bounds__(XT_THREADS, 1) gb_raster(gb_raster_args A) {
         for (int k = 0; k < 4; k++) {
             uint32_t s0 = 0, s1 = 0, s2 = 0, s3 = 0;
             for (uint32_t s = 0; s < rpp; s++) {
-                uint32_t v = stage[(pr * rpp + s) * XT_W + swz(px + k)];
+                uint32_t v = stage[swz(pr * rpp + s, px + k)];
                 s0 += v & 0xFFu;
                 s1 += (v >> 8) & 0xFFu;
                 s2 += (v >> 16) & 0xFFu;
