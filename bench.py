@@ -294,7 +294,7 @@ def main():
                    "cubics_per_path": "U{4..64}", "parallelism": "replicas" if world > 1 else "single",
                    "l2": "flushed before each step (256 MiB write)",
                    "flattened_points": nflat, "stroke_vertices": nsv, "stroke_triangles": int(stats[10]),
-                   "fill_edges": int(stats[4]), "bin_refs": int(stats[5])},
+                   "fill_edges": int(stats[4]), "bin_units": int(stats[5])},
         "stage_ms": {"flatten": tot[0] / a.steps, "stroke": tot[1] / a.steps, "setup_bin": tot[2] / a.steps,
                      "raster": raster_ms},
         "mpx_per_s": a.size * a.size * world / (ms / 1000.0) / 1e6,

@@ -30,7 +30,7 @@ vkvg_status_t vkvg_gb300_debug_counts(VkvgContext ctx, uint32_t out[8]) {
     out[4]            = p.ninds;
     out[5]            = p.dev_status;
     out[6]            = p.nedges;
-    out[7]            = p.nrefs;
+    out[7]            = p.nunits;
     return VKVG_STATUS_SUCCESS;
 }
 
@@ -150,10 +150,9 @@ vkvg_status_t vkvg_gb300_debug_coverage(VkvgContext ctx, uint32_t i, int32_t *ou
     A.ndraws   = p.ndraw;
     A.draws    = (const gb_draw *)((const uint8_t *)p.in.p + p.o_draws);
     A.cell_off = p.cells.as<uint32_t>();
-    A.refs     = p.refs.as<uint32_t>();
-    A.edges    = p.edges.as<int4>();
-    A.tri_a    = p.tri_a.as<int4>();
-    A.tri_b    = p.tri_b.as<int4>();
+    A.recs     = p.recs.as<int4>();
+    A.nunits   = p.nunits;
+    A.status   = p.status.as<uint32_t>();
     A.samples  = s->d_samples;
     A.rgba     = s->d_rgba;
     A.cov_out  = p.dbg.as<int32_t>();
@@ -273,7 +272,7 @@ vkvg_status_t vkvg_gb300_frame_stats(VkvgFrame fr, uint64_t out[16]) {
     out[2]            = p.nverts;
     out[3]            = p.ninds;
     out[4]            = p.nedges;
-    out[5]            = p.nrefs;
+    out[5]            = p.nunits;
     out[6]            = p.nseg;
     out[7]            = p.ndraw;
     out[8]            = p.launches;

@@ -59,7 +59,7 @@ struct Pipeline {
     DevBuf       ev_cnt, ev_off, events, cnt_v, cnt_i, off_v, off_i, verts, inds, ev_ret;
     DevBuf       fe_cnt, fe_off, edges, edge_draw;
     DevBuf       sdraw_tri0, sdraw_vbase, tri_a, tri_b, tri_draw;
-    DevBuf       cells, cursor, refs, status, dbg;
+    DevBuf       cells, cursor, recs, status, dbg;
     PinnedBuf    staging, rb;
     cudaEvent_t  evs[8] = {};
     /* offsets of the uploaded arrays inside `in` */
@@ -68,7 +68,7 @@ struct Pipeline {
     bool     uploaded = false;
     /* sizes of the last run */
     uint32_t nseg = 0, nsub = 0, ndraw = 0, nspair = 0, nsdraw = 0, nfpair = 0;
-    uint32_t npts = 0, nev = 0, nverts = 0, ninds = 0, nedges = 0, ntris = 0, nrefs = 0, nbands = 0;
+    uint32_t npts = 0, nev = 0, nverts = 0, ninds = 0, nedges = 0, ntris = 0, nunits = 0, nbands = 0;
     uint32_t dev_status = 0;
     uint64_t launches   = 0;
     uint64_t upload_bytes = 0;

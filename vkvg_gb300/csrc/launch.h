@@ -12,10 +12,9 @@ struct gb_raster_args {
     uint32_t        init_mode, init_color;
     const gb_draw  *draws;
     const uint32_t *cell_off; /* band-major (band * ndraws + draw) offsets, nbands*ndraws + 1 */
-    const uint32_t *refs;
-    const int4     *edges;
-    const int4     *tri_a;
-    const int4     *tri_b;
+    const int4     *recs;   /* per-cell primitive records: an edge is one 16-byte unit, a triangle two */
+    uint32_t        nunits; /* record units in recs */
+    uint32_t       *status; /* device status word (GB_ERR_*) */
     uint32_t       *samples; /* [nrows][Wpad] */
     uint32_t       *rgba;    /* [H][W] */
     int32_t        *cov_out; /* debug coverage output [H][W][S] or null */
@@ -78,7 +77,7 @@ cudaError_t gb_launch_stroke_tris(cudaStream_t st, uint32_t ntris, uint32_t ndra
 cudaError_t gb_launch_bin(cudaStream_t st, int scatter, uint32_t nedges, const int4 *edges, const uint32_t *edge_draw,
                           uint32_t ntris, const int4 *tri_a, const int4 *tri_b, const uint32_t *tri_draw,
                           uint32_t ndraws, uint32_t W, uint32_t samples, uint32_t nrows, uint32_t *cell,
-                          uint32_t *edge_refs, uint32_t *tri_refs, uint32_t nrefs);
+                          int4 *recs, uint32_t nunits);
 
 cudaError_t gb_launch_raster(cudaStream_t st, const gb_raster_args *a);
 cudaError_t gb_launch_pmath_eval(cudaStream_t st, int fn, const float *a, const float *b, float *out, uint64_t n);

@@ -96,7 +96,7 @@ void Pipeline::destroy() {
     DevBuf *bufs[] = {&in,     &seg_cnt, &seg_off,   &scratch,    &pts,         &pflag,    &sub_pt0, &sub_npts,
                       &ev_cnt, &ev_off,  &events,    &cnt_v,      &cnt_i,       &off_v,    &off_i,   &verts,
                       &inds,   &ev_ret,  &fe_cnt,    &fe_off,     &edges,       &edge_draw, &sdraw_tri0,
-                      &sdraw_vbase, &tri_a, &tri_b, &tri_draw, &cells,   &cursor,   &refs,    &status, &dbg};
+                      &sdraw_vbase, &tri_a, &tri_b, &tri_draw, &cells,   &cursor,   &recs,    &status, &dbg};
     for (DevBuf *b : bufs)
         b->release();
     staging.release();
@@ -305,17 +305,17 @@ cudaError_t Pipeline::run(const FrameHost &f, _vkvg_surface_t *surf, bool timing
     CK(cudaMemsetAsync(cells.p, 0, (ncells + 1) * 4, st));
     CK(gb_launch_bin(st, 0, nedges, edges.as<int4>(), edge_draw.as<uint32_t>(), ntris, tri_a.as<int4>(),
                      tri_b.as<int4>(), tri_draw.as<uint32_t>(), ndraw, W, S, surf->nrows, cells.as<uint32_t>(),
-                     nullptr, nullptr, 0u));
+                     nullptr, 0u));
     gb_count_launch((nedges ? 1 : 0) + (ntris ? 1 : 0));
     CK(scan(*this, cells.as<uint32_t>(), (uint32_t)ncells, cursor.as<uint32_t>()));
     CK(readback_u32(*this, cursor.as<uint32_t>() + ncells, hv, 1));
-    nrefs = hv[0];
-    GROW(refs, (size_t)(nrefs + 1) * 4);
+    nunits = hv[0];
+    GROW(recs, (size_t)(nunits + 1) * 16);
     /* cells <- offsets (kept for the raster), cursor <- running copy */
     CK(cudaMemcpyAsync(cells.p, cursor.p, (ncells + 1) * 4, cudaMemcpyDeviceToDevice, st));
     CK(gb_launch_bin(st, 1, nedges, edges.as<int4>(), edge_draw.as<uint32_t>(), ntris, tri_a.as<int4>(),
                      tri_b.as<int4>(), tri_draw.as<uint32_t>(), ndraw, W, S, surf->nrows, cursor.as<uint32_t>(),
-                     refs.as<uint32_t>(), refs.as<uint32_t>(), nrefs));
+                     recs.as<int4>(), nunits));
     gb_count_launch((nedges ? 1 : 0) + (ntris ? 1 : 0));
     if (timing)
         CK(cudaEventRecord(evs[3], st));
@@ -347,10 +347,9 @@ cudaError_t Pipeline::run(const FrameHost &f, _vkvg_surface_t *surf, bool timing
     }
     A.draws    = draws;
     A.cell_off = cells.as<uint32_t>();
-    A.refs     = refs.as<uint32_t>();
-    A.edges    = edges.as<int4>();
-    A.tri_a    = tri_a.as<int4>();
-    A.tri_b    = tri_b.as<int4>();
+    A.recs     = recs.as<int4>();
+    A.nunits   = nunits;
+    A.status   = status.as<uint32_t>();
     A.samples  = surf->d_samples;
     A.rgba     = surf->d_rgba;
     CK(gb_launch_raster(st, &A));
@@ -408,6 +407,10 @@ vkvg_status_t gb_run_frame(Pipeline &pl, const FrameHost &f, VkvgSurface surf, b
         return VKVG_STATUS_NO_MEMORY;
     if (e != cudaSuccess) {
         fprintf(stderr, "vkvg_gb300: CUDA error %s\n", cudaGetErrorString(e));
+        return VKVG_STATUS_DEVICE_ERROR;
+    }
+    if (pl.dev_status & GB_ERR_RASTER_WAIT) {
+        fprintf(stderr, "vkvg_gb300: raster staging wait exceeded its limit\n");
         return VKVG_STATUS_DEVICE_ERROR;
     }
     return VKVG_STATUS_SUCCESS;

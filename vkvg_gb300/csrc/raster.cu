@@ -60,7 +60,13 @@
 #define SM_TOT      (2 * XPLANE)
 #define SM_FLAG     (SM_TOT + 3 * TOT_SET)
 #define SM_WORDS    (SM_FLAG + 2 * XT_STRIPS)
-#define RASTER_SMEM (SM_WORDS * 4)
+/* then 2 staging buffers for a cell's records (16-byte units), 2 mbarriers */
+#define STAGE_CAP   2048 /* units per staging buffer: 32 KB */
+#define SM_STAGE    SM_WORDS
+#define SM_CUR      (SM_STAGE + 2 * STAGE_CAP * 4) /* per-warp draw-chunk tables: 16 x 160 words */
+#define SM_MBAR     (SM_CUR + XT_STRIPS * 160)
+#define RASTER_SMEM (SM_MBAR * 4 + 16)
+#define WAIT_LIMIT  (1u << 20) /* mbarrier polls before a staged copy counts as lost */
 
 #define BM_ADD  0 /* valid premultiplied source: exact on the FMA pipe */
 #define BM_SADD 1 /* saturating add */
@@ -124,6 +130,85 @@ __device__ __forceinline__ uint32_t swz(uint32_t rr, uint32_t p) {
     return rr * XT_W + (((p >> 2) ^ v) << 2) + (p & 3u);
 }
 
+/* ---- bulk-copy staging (cp.async.bulk + mbarrier transaction counts) */
+__device__ __forceinline__ void mbar_init(uint32_t bar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void mbar_init_fence() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+/* thread-level: one copy of `bytes` (multiple of 16, both ends 16-byte
+   aligned) from global memory into this CTA's shared memory, completing one
+   phase of the mbarrier at bar */
+__device__ __forceinline__ void stage_copy(uint32_t dst, const void *src, uint32_t bytes, uint32_t bar) {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+                 "l"(src), "r"(bytes), "r"(bar)
+                 : "memory");
+}
+/* wait for the phase with the given parity to complete; false after WAIT_LIMIT polls */
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+    for (uint32_t i = 0; i < WAIT_LIMIT; i++) {
+        uint32_t ok;
+        asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                     "selp.u32 %0, 1, 0, p;\n\t}"
+                     : "=r"(ok)
+                     : "r"(bar), "r"(parity)
+                     : "memory");
+        if (ok)
+            return true;
+    }
+    return false;
+}
+
+/* The band's active draws (with geometry in the band, or paint / clear), 32
+   at a time: each warp keeps the chunk's (kind, lo, hi, src, op) in its own
+   table in shared memory (ct), amask the active ones not yet taken.  All
+   warps walk the same sequence. */
+struct draw_cursor {
+    uint32_t d0, amask;
+};
+__device__ __forceinline__ void cur_load(draw_cursor &c, const gb_raster_args &A, size_t cb, uint32_t dhi,
+                                         uint32_t l, uint32_t *ct) {
+    const uint32_t dl  = c.d0 + l;
+    bool           act = false;
+    uint32_t       kind = 0, lo = 0, hi = 0, src = 0, op = 0;
+    if (dl < dhi) {
+        const gb_draw &D = A.draws[dl];
+        kind             = D.kind;
+        src              = D.src;
+        op               = D.op;
+        lo               = A.cell_off[cb + dl];
+        hi               = A.cell_off[cb + dl + 1];
+        act              = kind == GB_DRAW_PAINT || kind == GB_DRAW_CLEAR || lo != hi;
+    }
+    __syncwarp();
+    ct[l]       = kind;
+    ct[32 + l]  = lo;
+    ct[64 + l]  = hi;
+    ct[96 + l]  = src;
+    ct[128 + l] = op;
+    c.amask    = __ballot_sync(0xffffffffu, act);
+}
+__device__ __forceinline__ bool cur_next(draw_cursor &c, const gb_raster_args &A, size_t cb, uint32_t dhi, uint32_t l,
+                                         uint32_t *ct, uint32_t *d, uint32_t *kind, uint32_t *lo, uint32_t *hi,
+                                         uint32_t *slot) {
+    while (c.amask == 0) {
+        c.d0 += 32;
+        if (c.d0 >= dhi)
+            return false;
+        cur_load(c, A, cb, dhi, l, ct);
+    }
+    const int j = __ffs(c.amask) - 1;
+    c.amask &= c.amask - 1;
+    *d    = c.d0 + (uint32_t)j;
+    *slot = (uint32_t)j;
+    *kind = ct[j];
+    *lo   = ct[32 + j];
+    *hi   = ct[64 + j];
+    return true;
+}
+__device__ __forceinline__ bool is_geom(uint32_t kind) { return kind != GB_DRAW_PAINT && kind != GB_DRAW_CLEAR; }
+
 /* one edge crossing sample row sy (band row rr): add dir at the last tile
    sample left of the crossing, so that the suffix sum from sample c is the
    winding contribution at c */
@@ -156,18 +241,19 @@ __device__ __forceinline__ void acc_row(int32_t x0, int32_t y0, int32_t x1, int3
     flag[p >> 6] = 1;
 }
 
-/* fills on a run with crossings: blend where (w & fmask) != 0
-   (fmask 1: even-odd, ~0: non-zero) */
+/* fills on a run with crossings (its counters at cp, slot rotation v):
+   blend where (w & fmask) != 0 (fmask 1: even-odd, ~0: non-zero) */
 template <int M>
-__device__ __forceinline__ void fill_run(uint32_t (&col)[32], const int4 (&cn)[8], int32_t E, int32_t fmask,
+__device__ __forceinline__ void fill_run(uint32_t (&col)[32], const int4 *cp, uint32_t v, int32_t E, int32_t fmask,
                                          const blend_k &B) {
     int32_t w = E;
 #pragma unroll
     for (int q = 7; q >= 0; q--) {
+        const int4 x = cp[q ^ v];
 #pragma unroll
         for (int e = 3; e >= 0; e--) {
             const int c = 4 * q + e;
-            w += e == 3 ? cn[q].w : e == 2 ? cn[q].z : e == 1 ? cn[q].y : cn[q].x;
+            w += e == 3 ? x.w : e == 2 ? x.z : e == 1 ? x.y : x.x;
             const uint32_t nb = blend<M>(col[c], B);
             col[c]            = (w & fmask) ? nb : col[c];
         }
@@ -175,16 +261,18 @@ __device__ __forceinline__ void fill_run(uint32_t (&col)[32], const int4 (&cn)[8
 }
 /* strokes on a run with crossings: blend w times (w = covering triangles) */
 template <int M>
-__device__ __forceinline__ void stroke_run(uint32_t (&col)[32], const int4 (&cn)[8], int32_t E, const blend_k &B) {
+__device__ __forceinline__ void stroke_run(uint32_t (&col)[32], const int4 *cp, uint32_t v, int32_t E,
+                                           const blend_k &B) {
     int32_t kmax = 1;
     for (int32_t rep = 0; rep < kmax; rep++) {
         int32_t w = E;
 #pragma unroll
         for (int q = 7; q >= 0; q--) {
+            const int4 x = cp[q ^ v];
 #pragma unroll
             for (int e = 3; e >= 0; e--) {
                 const int c = 4 * q + e;
-                w += e == 3 ? cn[q].w : e == 2 ? cn[q].z : e == 1 ? cn[q].y : cn[q].x;
+                w += e == 3 ? x.w : e == 2 ? x.z : e == 1 ? x.y : x.x;
                 const uint32_t nb = blend<M>(col[c], B);
                 col[c]            = w > rep ? nb : col[c];
                 kmax              = max(kmax, w);
@@ -250,147 +338,220 @@ __global__ void __launch_bounds__(XT_THREADS, 1) gb_raster(gb_raster_args A) {
     }
     for (uint32_t i = t; i < SM_WORDS; i += XT_THREADS)
         smem[i] = 0;
+    const uint32_t sm_base = (uint32_t)__cvta_generic_to_shared(smem);
+    const uint32_t bar0    = sm_base + SM_MBAR * 4;
+    if (t == 0) {
+        mbar_init(bar0);
+        mbar_init(bar0 + 8);
+        mbar_init_fence();
+    }
     __syncthreads();
+    /* staging state, identical in every thread: the draw each buffer holds
+       or receives, the parity its mbarrier completes next, copies not yet
+       seen to complete */
+    uint32_t stg_d0 = 0xFFFFFFFFu, stg_d1 = 0xFFFFFFFFu;
+    uint32_t stg_par = 0, stg_pend = 0;
+    auto     stage_cell = [&](uint32_t b, uint32_t d, uint32_t lo, uint32_t units) {
+        if (t == 0)
+            stage_copy(sm_base + (SM_STAGE + b * STAGE_CAP * 4) * 4, A.recs + lo, units * 16u, bar0 + 8 * b);
+        if (b)
+            stg_d1 = d;
+        else
+            stg_d0 = d;
+        stg_pend |= 1u << b;
+    };
 
     const uint32_t dlo   = dbg ? A.cov_draw : A.draw_first;
     const uint32_t dhi   = dbg ? A.cov_draw + 1 : nd;
     uint32_t       nproc = 0; /* draws with geometry in this band so far */
-    for (uint32_t d = dlo; d < dhi; d++) {
-        const gb_draw &D    = A.draws[d];
-        const uint32_t kind = D.kind;
-        int            bm;
-        if (kind == GB_DRAW_PAINT) {
-            const blend_k B = make_blend(D.src, D.op, &bm);
+    uint32_t   *ct = reinterpret_cast<uint32_t *>(smem + SM_CUR + wi * 160);
+    draw_cursor cur;
+    cur.d0 = dlo;
+    cur_load(cur, A, cb, dhi, l, ct);
+    uint32_t nx_d = 0, nx_kind = 0, nx_lo = 0, nx_hi = 0, nx_slot = 0;
+    bool     nx_have = cur_next(cur, A, cb, dhi, l, ct, &nx_d, &nx_kind, &nx_lo, &nx_hi, &nx_slot);
+    {
+        while (nx_have) {
+            const uint32_t d = nx_d, kind = nx_kind, lo = nx_lo, hi = nx_hi;
+            const uint32_t src = ct[96 + nx_slot], op = ct[128 + nx_slot];
+            nx_have = cur_next(cur, A, cb, dhi, l, ct, &nx_d, &nx_kind, &nx_lo, &nx_hi, &nx_slot); /* lookahead */
+            int            bm;
+            if (kind == GB_DRAW_PAINT) {
+                const blend_k B = make_blend(src, op, &bm);
+                if (dbg) {
+                    for (int c = 0; c < ncols; c++)
+                        A.cov_out[((size_t)(R / rpp) * A.W + X0 + col0 + c) * A.S + R % rpp] = 1;
+                    continue;
+                }
+                if (bm == BM_ADD)
+                    uniform_run<BM_ADD>(col, 1, B);
+                else if (bm == BM_SADD)
+                    uniform_run<BM_SADD>(col, 1, B);
+                else
+                    uniform_run<BM_SSUB>(col, 1, B);
+                continue;
+            }
+            if (kind == GB_DRAW_CLEAR) {
+#pragma unroll
+                for (int c = 0; c < 32; c++)
+                    col[c] = 0u;
+                continue;
+            }
+            if (hi > A.nunits || lo > hi) {
+                if (t == 0)
+                    atomicOr(A.status, GB_ERR_OVERFLOW);
+                continue;
+            }
+            const blend_k B = make_blend(src, op, &bm);
+            /* this draw's records: staged now unless prefetched; then prefetch
+               the next geometry draw into the other buffer, whose readers all
+               passed the previous barrier */
+            const uint32_t sb = nproc & 1;
+            const uint32_t su = min(hi - lo, (uint32_t)STAGE_CAP);
+            if ((sb ? stg_d1 : stg_d0) != d)
+                stage_cell(sb, d, lo, su);
+            if (nx_have && is_geom(nx_kind) && nx_lo < nx_hi && nx_hi <= A.nunits)
+                stage_cell(sb ^ 1u, nx_d, nx_lo, min(nx_hi - nx_lo, (uint32_t)STAGE_CAP));
+            if (mbar_wait(bar0 + 8 * sb, (stg_par >> sb) & 1u)) {
+                stg_pend &= ~(1u << sb);
+            } else if (t == 0) {
+                atomicOr(A.status, GB_ERR_RASTER_WAIT);
+            }
+            stg_par ^= 1u << sb;
+            if (sb)
+                stg_d1 = 0xFFFFFFFFu;
+            else
+                stg_d0 = 0xFFFFFFFFu;
+            const int4 *sg = reinterpret_cast<const int4 *>(smem + SM_STAGE) + sb * STAGE_CAP;
+            int32_t *plane = smem + (nproc & 1) * XPLANE;
+            int32_t *tot   = smem + SM_TOT + (nproc % 3) * TOT_SET;
+            int32_t *flag  = smem + SM_FLAG + (nproc & 1) * XT_STRIPS;
+
+            /* ---- accumulate: one item per (primitive, band row) */
+            if (iok) {
+                if (kind == GB_DRAW_STROKE) {
+                    const uint32_t n = ((hi - lo) >> 1) * 16u;
+                    for (uint32_t it = t; it < n; it += XT_THREADS) {
+                        const uint32_t u = (it >> 4) * 2u;
+                        int4           ta, tb;
+                        if (u < su) {
+                            ta = sg[u];
+                            tb = sg[u + 1];
+                        } else {
+                            ta = A.recs[lo + u];
+                            tb = A.recs[lo + u + 1];
+                        }
+                        const int32_t ymn = min(min(ta.y, ta.w), tb.y), ymx = max(max(ta.y, ta.w), tb.y);
+                        if (isy < ymn || isy >= ymx)
+                            continue;
+                        const int32_t xmn = min(min(ta.x, ta.z), tb.x), xmx = max(max(ta.x, ta.z), tb.x);
+                        if (xmx < tx_lo || xmn > tx_hi)
+                            continue; /* wholly left or right: no net coverage in the tile */
+                        acc_row(ta.x, ta.y, ta.z, ta.w, isy, irr, iox, X0, TW, tx_lo, tx_hi, plane, tot, flag);
+                        acc_row(ta.z, ta.w, tb.x, tb.y, isy, irr, iox, X0, TW, tx_lo, tx_hi, plane, tot, flag);
+                        acc_row(tb.x, tb.y, ta.x, ta.y, isy, irr, iox, X0, TW, tx_lo, tx_hi, plane, tot, flag);
+                    }
+                } else {
+                    const uint32_t n = (hi - lo) * 16u;
+                    for (uint32_t it = t; it < n; it += XT_THREADS) {
+                        const uint32_t u  = it >> 4;
+                        const int4     ed = u < su ? sg[u] : A.recs[lo + u];
+                        acc_row(ed.x, ed.y, ed.z, ed.w, isy, irr, iox, X0, TW, tx_lo, tx_hi, plane, tot, flag);
+                    }
+                }
+            }
+            __syncthreads();
+
+            /* ---- blend.  The previous draw's totals are no longer read by anyone. */
+            if (hh == 0)
+                smem[SM_TOT + ((nproc + 2) % 3) * TOT_SET + rl * TOT_ROW + wi] = 0;
+            nproc++;
+            int32_t Er = 0; /* winding from strips to the right */
+            {
+                const int4 *tr4 = reinterpret_cast<const int4 *>(tot + rl * TOT_ROW);
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    const int4 v = tr4[q];
+                    Er += (4 * q > (int)wi ? v.x : 0) + (4 * q + 1 > (int)wi ? v.y : 0) +
+                          (4 * q + 2 > (int)wi ? v.z : 0) + (4 * q + 3 > (int)wi ? v.w : 0);
+                }
+            }
+            const bool flagged = flag[wi] != 0;
+
             if (dbg) {
-                for (int c = 0; c < ncols; c++)
-                    A.cov_out[((size_t)(R / rpp) * A.W + X0 + col0 + c) * A.S + R % rpp] = 1;
+                /* coverage of a single draw: read the counters in place */
+                int32_t L = 0;
+                for (int c = 0; c < 32; c++)
+                    L += plane[swz(rl, col0 + c)];
+                const int32_t Lp = __shfl_xor_sync(0xffffffffu, L, 1);
+                int32_t       w  = Er + (hh == 0 ? Lp : 0);
+                for (int c = 31; c >= 0; c--) {
+                    w += plane[swz(rl, col0 + c)];
+                    if (c < ncols)
+                        A.cov_out[((size_t)(R / rpp) * A.W + X0 + col0 + c) * A.S + R % rpp] = w;
+                }
                 continue;
             }
-            if (bm == BM_ADD)
-                uniform_run<BM_ADD>(col, 1, B);
-            else if (bm == BM_SADD)
-                uniform_run<BM_SADD>(col, 1, B);
-            else
-                uniform_run<BM_SSUB>(col, 1, B);
-            continue;
-        }
-        if (kind == GB_DRAW_CLEAR) {
-#pragma unroll
-            for (int c = 0; c < 32; c++)
-                col[c] = 0u;
-            continue;
-        }
-        const uint32_t lo = A.cell_off[cb + d], hi = A.cell_off[cb + d + 1];
-        if (lo == hi)
-            continue;
-        const blend_k B = make_blend(D.src, D.op, &bm);
-        int32_t *plane = smem + (nproc & 1) * XPLANE;
-        int32_t *tot   = smem + SM_TOT + (nproc % 3) * TOT_SET;
-        int32_t *flag  = smem + SM_FLAG + (nproc & 1) * XT_STRIPS;
-
-        /* ---- accumulate: one item per (primitive, band row) */
-        if (iok) {
-            const uint32_t n = (hi - lo) * 16u;
-            if (kind == GB_DRAW_STROKE) {
-                for (uint32_t it = t; it < n; it += XT_THREADS) {
-                    const uint32_t tr  = A.refs[lo + (it >> 4)];
-                    const int4     ta  = A.tri_a[tr], tb = A.tri_b[tr];
-                    const int32_t  ymn = min(min(ta.y, ta.w), tb.y), ymx = max(max(ta.y, ta.w), tb.y);
-                    if (isy < ymn || isy >= ymx)
-                        continue;
-                    const int32_t xmn = min(min(ta.x, ta.z), tb.x), xmx = max(max(ta.x, ta.z), tb.x);
-                    if (xmx < tx_lo || xmn > tx_hi)
-                        continue; /* wholly left or right: no net coverage in the tile */
-                    acc_row(ta.x, ta.y, ta.z, ta.w, isy, irr, iox, X0, TW, tx_lo, tx_hi, plane, tot, flag);
-                    acc_row(ta.z, ta.w, tb.x, tb.y, isy, irr, iox, X0, TW, tx_lo, tx_hi, plane, tot, flag);
-                    acc_row(tb.x, tb.y, ta.x, ta.y, isy, irr, iox, X0, TW, tx_lo, tx_hi, plane, tot, flag);
-                }
-            } else {
-                for (uint32_t it = t; it < n; it += XT_THREADS) {
-                    const int4 ed = A.edges[A.refs[lo + (it >> 4)]];
-                    acc_row(ed.x, ed.y, ed.z, ed.w, isy, irr, iox, X0, TW, tx_lo, tx_hi, plane, tot, flag);
-                }
-            }
-        }
-        __syncthreads();
-
-        /* ---- blend.  The previous draw's totals are no longer read by anyone. */
-        if (hh == 0)
-            smem[SM_TOT + ((nproc + 2) % 3) * TOT_SET + rl * TOT_ROW + wi] = 0;
-        nproc++;
-        int32_t Er = 0; /* winding from strips to the right */
-        for (uint32_t w2 = wi + 1; w2 < XT_STRIPS; w2++)
-            Er += tot[rl * TOT_ROW + w2];
-        const bool flagged = flag[wi] != 0;
-
-        if (dbg) {
-            /* coverage of a single draw: read the counters in place */
-            int32_t L = 0;
-            for (int c = 0; c < 32; c++)
-                L += plane[swz(rl, col0 + c)];
-            const int32_t Lp = __shfl_xor_sync(0xffffffffu, L, 1);
-            int32_t       w  = Er + (hh == 0 ? Lp : 0);
-            for (int c = 31; c >= 0; c--) {
-                w += plane[swz(rl, col0 + c)];
-                if (c < ncols)
-                    A.cov_out[((size_t)(R / rpp) * A.W + X0 + col0 + c) * A.S + R % rpp] = w;
-            }
-            continue;
-        }
-        if (!flagged) {
-            /* no crossing in the strip: every run has the uniform winding Er */
-            int32_t k = 0;
-            if (row_ok)
-                k = kind == GB_DRAW_STROKE ? max(Er, 0) : kind == GB_DRAW_FILL_EO ? (Er & 1) : (Er != 0);
-            if (!__any_sync(0xffffffffu, k > 0))
+            if (!flagged) {
+                /* no crossing in the strip: every run has the uniform winding Er */
+                int32_t k = 0;
+                if (row_ok)
+                    k = kind == GB_DRAW_STROKE ? max(Er, 0) : kind == GB_DRAW_FILL_EO ? (Er & 1) : (Er != 0);
+                if (!__any_sync(0xffffffffu, k > 0))
+                    continue;
+                if (bm == BM_ADD)
+                    uniform_run<BM_ADD>(col, k, B);
+                else if (bm == BM_SADD)
+                    uniform_run<BM_SADD>(col, k, B);
+                else
+                    uniform_run<BM_SSUB>(col, k, B);
                 continue;
-            if (bm == BM_ADD)
-                uniform_run<BM_ADD>(col, k, B);
-            else if (bm == BM_SADD)
-                uniform_run<BM_SADD>(col, k, B);
-            else
-                uniform_run<BM_SSUB>(col, k, B);
-            continue;
-        }
-        /* this lane's 32 counters, then clear them for the draw after next */
-        int4   *cp = reinterpret_cast<int4 *>(plane + rl * XT_W + col0);
-        int4    cn[8];
-        int     nzr = 0;
-        int32_t L   = 0;
+            }
+            /* this lane's 32 counters: totals first, the blend reads them again;
+               then they are cleared for the draw after next */
+            int4   *cp  = reinterpret_cast<int4 *>(plane + rl * XT_W + col0);
+            int     nzr = 0;
+            int32_t L   = 0;
 #pragma unroll
-        for (int q = 0; q < 8; q++) {
-            cn[q] = cp[q ^ v_lane];
-            nzr |= cn[q].x | cn[q].y | cn[q].z | cn[q].w;
-            L += cn[q].x + cn[q].y + cn[q].z + cn[q].w;
-        }
+            for (int q = 0; q < 8; q++) {
+                const int4 x = cp[q ^ v_lane];
+                nzr |= x.x | x.y | x.z | x.w;
+                L += x.x + x.y + x.z + x.w;
+            }
+            const int32_t Lp   = __shfl_xor_sync(0xffffffffu, L, 1);
+            const int32_t E    = Er + (hh == 0 ? Lp : 0); /* winding entering this run from the right */
+            const bool    work = row_ok && (nzr != 0 || E != 0);
+            if (__any_sync(0xffffffffu, work)) {
+                if (kind == GB_DRAW_STROKE) {
+                    if (bm == BM_ADD)
+                        stroke_run<BM_ADD>(col, cp, v_lane, E, B);
+                    else if (bm == BM_SADD)
+                        stroke_run<BM_SADD>(col, cp, v_lane, E, B);
+                    else
+                        stroke_run<BM_SSUB>(col, cp, v_lane, E, B);
+                } else {
+                    const int32_t fmask = kind == GB_DRAW_FILL_EO ? 1 : -1;
+                    if (bm == BM_ADD)
+                        fill_run<BM_ADD>(col, cp, v_lane, E, fmask, B);
+                    else if (bm == BM_SADD)
+                        fill_run<BM_SADD>(col, cp, v_lane, E, fmask, B);
+                    else
+                        fill_run<BM_SSUB>(col, cp, v_lane, E, fmask, B);
+                }
+            }
 #pragma unroll
-        for (int q = 0; q < 8; q++)
-            cp[q ^ v_lane] = make_int4(0, 0, 0, 0);
-        __syncwarp();
-        if (l == 0)
-            flag[wi] = 0;
-        const int32_t Lp   = __shfl_xor_sync(0xffffffffu, L, 1);
-        const int32_t E    = Er + (hh == 0 ? Lp : 0); /* winding entering this run from the right */
-        const bool    work = row_ok && (nzr != 0 || E != 0);
-        if (!__any_sync(0xffffffffu, work))
-            continue;
-        if (kind == GB_DRAW_STROKE) {
-            if (bm == BM_ADD)
-                stroke_run<BM_ADD>(col, cn, E, B);
-            else if (bm == BM_SADD)
-                stroke_run<BM_SADD>(col, cn, E, B);
-            else
-                stroke_run<BM_SSUB>(col, cn, E, B);
-        } else {
-            const int32_t fmask = kind == GB_DRAW_FILL_EO ? 1 : -1;
-            if (bm == BM_ADD)
-                fill_run<BM_ADD>(col, cn, E, fmask, B);
-            else if (bm == BM_SADD)
-                fill_run<BM_SADD>(col, cn, E, fmask, B);
-            else
-                fill_run<BM_SSUB>(col, cn, E, fmask, B);
+            for (int q = 0; q < 8; q++)
+                cp[q ^ v_lane] = make_int4(0, 0, 0, 0);
+            __syncwarp();
+            if (l == 0)
+                flag[wi] = 0;
         }
     }
+    /* a copy that missed its wait limit may still land: wait for it (again
+       bounded) before the shared memory is reused or released */
+    for (uint32_t b = 0; b < 2; b++)
+        if ((stg_pend >> b) & 1u)
+            mbar_wait(bar0 + 8 * b, ((stg_par >> b) & 1u) ^ 1u);
     if (dbg)
         return;
 

@@ -13,7 +13,7 @@
  * Binning: the surface is cut into bands of 16 sample rows.  Each primitive is
  * counted into (band, draw) cells, an exclusive scan in band-major order gives
  * every band a contiguous, draw-ordered list, and a scatter pass writes the
- * primitive indices.
+ * primitives' records (not indices) into it.
  */
 #include "gb_types.h"
 
@@ -168,10 +168,15 @@ __device__ __forceinline__ bool gb_prim_bands(int32_t ylo, int32_t yhi, int32_t 
     return true;
 }
 
+/* Binning: count (SCATTER false) or write (SCATTER true) each primitive's
+   record into every (band, draw) cell it touches.  Records are 16-byte units:
+   an edge is one unit (x0, y0, x1, y1), a triangle two (tri_a, tri_b), so a
+   cell is one contiguous block that the raster can stage with a single bulk
+   copy. */
 template <bool SCATTER>
 __global__ void gb_bin_edges(uint32_t nedges, const int4 *__restrict__ edges, const uint32_t *__restrict__ edge_draw,
                              uint32_t ndraws, uint32_t W, uint32_t samples, uint32_t nrows,
-                             uint32_t *__restrict__ cell, uint32_t *__restrict__ refs, uint32_t nrefs) {
+                             uint32_t *__restrict__ cell, int4 *__restrict__ recs, uint32_t nunits) {
     uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= nedges)
         return;
@@ -183,15 +188,14 @@ __global__ void gb_bin_edges(uint32_t nedges, const int4 *__restrict__ edges, co
     uint32_t d = edge_draw[e];
     for (uint32_t b = b0; b <= b1; b++) {
         uint32_t slot = atomicAdd(&cell[(size_t)b * ndraws + d], 1u);
-        if (SCATTER && slot < nrefs)
-            refs[slot] = e;
+        if (SCATTER && slot < nunits)
+            recs[slot] = ed;
     }
 }
 template <bool SCATTER>
 __global__ void gb_bin_tris(uint32_t ntris, const int4 *__restrict__ tri_a, const int4 *__restrict__ tri_b,
                             const uint32_t *__restrict__ tri_draw, uint32_t ndraws, uint32_t W, uint32_t samples,
-                            uint32_t nrows, uint32_t *__restrict__ cell, uint32_t *__restrict__ refs,
-                            uint32_t nrefs) {
+                            uint32_t nrows, uint32_t *__restrict__ cell, int4 *__restrict__ recs, uint32_t nunits) {
     uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= ntris)
         return;
@@ -205,9 +209,11 @@ __global__ void gb_bin_tris(uint32_t ntris, const int4 *__restrict__ tri_a, cons
         return;
     uint32_t d = tri_draw[t];
     for (uint32_t bb = b0; bb <= b1; bb++) {
-        uint32_t slot = atomicAdd(&cell[(size_t)bb * ndraws + d], 1u);
-        if (SCATTER && slot < nrefs)
-            refs[slot] = t;
+        uint32_t slot = atomicAdd(&cell[(size_t)bb * ndraws + d], 2u);
+        if (SCATTER && slot + 1 < nunits) {
+            recs[slot]     = a;
+            recs[slot + 1] = b;
+        }
     }
 }
 
@@ -241,12 +247,12 @@ cudaError_t gb_launch_stroke_tris(cudaStream_t st, uint32_t ntris, uint32_t ndra
 }
 cudaError_t gb_launch_bin(cudaStream_t st, int scatter, uint32_t nedges, const int4 *edges, const uint32_t *edge_draw,
                           uint32_t ntris, const int4 *tri_a, const int4 *tri_b, const uint32_t *tri_draw,
-                          uint32_t ndraws, uint32_t W, uint32_t samples, uint32_t nrows, uint32_t *cell,
-                          uint32_t *edge_refs, uint32_t *tri_refs, uint32_t nrefs) {
+                          uint32_t ndraws, uint32_t W, uint32_t samples, uint32_t nrows, uint32_t *cell, int4 *recs,
+                          uint32_t nunits) {
     if (nedges) {
         if (scatter)
             gb_bin_edges<true><<<(nedges + 255) / 256, 256, 0, st>>>(nedges, edges, edge_draw, ndraws, W, samples,
-                                                                      nrows, cell, edge_refs, nrefs);
+                                                                      nrows, cell, recs, nunits);
         else
             gb_bin_edges<false><<<(nedges + 255) / 256, 256, 0, st>>>(nedges, edges, edge_draw, ndraws, W, samples,
                                                                        nrows, cell, nullptr, 0u);
@@ -254,7 +260,7 @@ cudaError_t gb_launch_bin(cudaStream_t st, int scatter, uint32_t nedges, const i
     if (ntris) {
         if (scatter)
             gb_bin_tris<true><<<(ntris + 255) / 256, 256, 0, st>>>(ntris, tri_a, tri_b, tri_draw, ndraws, W, samples,
-                                                                    nrows, cell, tri_refs, nrefs);
+                                                                    nrows, cell, recs, nunits);
         else
             gb_bin_tris<false><<<(ntris + 255) / 256, 256, 0, st>>>(ntris, tri_a, tri_b, tri_draw, ndraws, W, samples,
                                                                      nrows, cell, nullptr, 0u);
