@@ -125,6 +125,30 @@ vkvg_public vkvg_status_t vkvg_gb300_pmath_eval(int fn, const float *a, const fl
 /* Number of kernels this library launched since the process started. */
 vkvg_public uint64_t vkvg_gb300_kernel_launches(void);
 
+/* Exclusive prefix sum that allocates nothing.  No counterpart in the
+ * reference: vkvg has no device-side scan; this is the scan the library's
+ * pipeline uses to turn per-item counts into output offsets, offered to
+ * callers that must not allocate device memory - a render loop whose frame
+ * budget cannot absorb cudaMalloc's implicit device synchronisation, or a
+ * process whose device memory is already held by another allocator.
+ *
+ * counts (n entries) and offsets (n + 1 entries) are device pointers;
+ * offsets[i] = counts[0] + ... + counts[i-1] modulo 2^32 and offsets[n] is
+ * the total.  Work is queued on stream (a cudaStream_t, 0 for the default
+ * stream) and is finished when that stream is.  The scratch is a fixed array
+ * inside the library's device image holding at most
+ * VKVG_GB300_SCAN_NOALLOC_MAX items; larger n returns VKVG_STATUS_NO_MEMORY
+ * and launches nothing.  Nothing has to be zeroed beforehand.
+ *
+ * The first call on each device (with that device current) looks the array's
+ * address up, which may load the library's device code; make that first call
+ * before any stream capture begins.  All calls on one device share the one
+ * array, so calls that overlap in time - on different streams or host
+ * threads - race and corrupt each other's results: order them. */
+#define VKVG_GB300_SCAN_NOALLOC_MAX (1u << 26)
+vkvg_public vkvg_status_t vkvg_gb300_exclusive_scan_noalloc(void *stream, const uint32_t *counts, uint32_t n,
+                                                             uint32_t *offsets);
+
 #ifdef __cplusplus
 }
 #endif

@@ -136,6 +136,7 @@ SIGNATURES = {
     "vkvg_gb300_surface_read_premult": (_I, [_P, _P]),
     "vkvg_gb300_pmath_eval": (_I, [_I, _P, _P, _P, C.c_uint64, _I]),
     "vkvg_gb300_kernel_launches": (C.c_uint64, []),
+    "vkvg_gb300_exclusive_scan_noalloc": (_I, [_P, _P, C.c_uint32, _P]),
 }
 
 
@@ -312,6 +313,16 @@ class Context:
 
 def kernel_launches():
     return int(lib().vkvg_gb300_kernel_launches())
+
+
+SCAN_NOALLOC_MAX = 1 << 26
+
+
+def exclusive_scan_noalloc(counts_ptr, n, offsets_ptr, stream=0):
+    """Device exclusive scan of n uint32 counts into n + 1 offsets without
+    allocating (device pointers as ints); returns the vkvg status code."""
+    return int(lib().vkvg_gb300_exclusive_scan_noalloc(C.c_void_p(stream), C.c_void_p(counts_ptr), n,
+                                                        C.c_void_p(offsets_ptr)))
 
 
 def pmath(fn, a, b=None, device=False):

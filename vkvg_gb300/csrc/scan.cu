@@ -4,8 +4,12 @@
  * Three phases: per-block sums, one-block scan of the block sums, per-block
  * scan plus block prefix.  4096 items per 1024-thread block.
  */
+#include "vkvg_gb300.h"
+
 #include <cuda_runtime.h>
+#include <mutex>
 #include <stdint.h>
+#include <stdio.h>
 
 #define SCAN_THREADS 1024
 #define SCAN_ITEMS   4
@@ -104,4 +108,55 @@ cudaError_t gb_exclusive_scan(cudaStream_t st, const uint32_t *in, uint32_t n, u
     scan_apply<<<nb, SCAN_THREADS, 0, st>>>(in, n, scratch, out);
     return cudaGetLastError();
 }
+}
+
+/* ---- exclusive scan without allocation.
+ *
+ * The same three kernels, with the block sums kept in a fixed array that is
+ * part of the module's device image instead of a buffer allocated by the
+ * pipeline.  Block sums are fully written by the first kernel before the
+ * others read them, so the array needs no initial contents.  Its device
+ * address is looked up once per device, by the first call made with that
+ * device current.  All calls on one device share the array. */
+#define SCAN_NOALLOC_WORDS ((VKVG_GB300_SCAN_NOALLOC_MAX + SCAN_TILE - 1) / SCAN_TILE + 1)
+#define SCAN_NOALLOC_DEVS  64
+
+static __device__ __align__(256) uint32_t g_scan_noalloc_scratch[SCAN_NOALLOC_WORDS];
+
+void gb_count_launch(uint64_t n);
+
+extern "C" vkvg_status_t vkvg_gb300_exclusive_scan_noalloc(void *stream, const uint32_t *counts, uint32_t n,
+                                                            uint32_t *offsets) {
+    static std::mutex lock;
+    static uint32_t  *scratch[SCAN_NOALLOC_DEVS];
+    if (!offsets || (n && !counts))
+        return VKVG_STATUS_NULL_POINTER;
+    if (n > VKVG_GB300_SCAN_NOALLOC_MAX) {
+        fprintf(stderr, "vkvg_gb300_exclusive_scan_noalloc: %u items exceed its fixed limit of %u\n", n,
+                (unsigned)VKVG_GB300_SCAN_NOALLOC_MAX);
+        return VKVG_STATUS_NO_MEMORY;
+    }
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= SCAN_NOALLOC_DEVS)
+        return VKVG_STATUS_DEVICE_ERROR;
+    uint32_t *sp;
+    {
+        std::lock_guard<std::mutex> g(lock);
+        if (!scratch[dev]) {
+            void       *p = nullptr;
+            cudaError_t e = cudaGetSymbolAddress(&p, g_scan_noalloc_scratch);
+            if (e != cudaSuccess || !p) {
+                fprintf(stderr, "vkvg_gb300_exclusive_scan_noalloc: scratch lookup failed: %s\n",
+                        cudaGetErrorString(e));
+                return VKVG_STATUS_DEVICE_ERROR;
+            }
+            scratch[dev] = (uint32_t *)p;
+        }
+        sp = scratch[dev];
+    }
+    cudaError_t e = gb_exclusive_scan((cudaStream_t)stream, counts, n, offsets, sp);
+    if (e != cudaSuccess)
+        return VKVG_STATUS_DEVICE_ERROR;
+    gb_count_launch(n ? 3 : 0);
+    return VKVG_STATUS_SUCCESS;
 }
