@@ -19,6 +19,12 @@ e2e    - paths/s through the public C API from host memory: each step replays
 roofline - the raster/composite kernel (dominant) against the measured HBM
          copy bandwidth; algorithmic bytes = 8 B per flattened point and per
          stroke vertex read once, plus the RGBA8 surface read and written.
+         frame_frac applies the whole-frame count (8 B per input control
+         point, 4 B per command word, 16 B per flattened point and per stroke
+         vertex - written once, read once - and 8 B per pixel) to the whole
+         frame time.  The raster kernel is instruction-issue bound, not HBM
+         bound; its ncu issue and pipe figures are read from the committed
+         profile summary (profiles/raster_curve_heavy_1024.md).
 cpu_baseline - the CPU restatement of vkvg's path code (oracle/) on a bounded
          sample (the first 64 paths of the same scene), all host threads.
 
@@ -112,6 +118,22 @@ class ClockSampler:
             return None
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
                 "samples": len(sm)}
+
+
+def reduce_max(x, dist, device):
+    """max of a per-rank float over all ranks (x itself without a process group)"""
+    if dist is None:
+        return float(x)
+    import torch
+
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank, world, seconds):
+    """units of all replicas per second of the slowest replica"""
+    return units_per_rank * world / seconds
 
 
 def cpu_sample(n_paths, size, threads, reps=1):
@@ -232,13 +254,9 @@ def main():
         dist.barrier()
     clk = clocks.stop()
     L.vkvg_gb300_frame_stats(frame, stats.ctypes.data_as(C.c_void_p))
-    ms = tot[4] / a.steps
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = reduce_max(tot[4] / a.steps, dist, "cuda")
     paths = a.paths  # each path is filled and stroked (two draws)
-    value = paths * world / (ms / 1000.0)
+    value = whole_job_rate(paths, world, ms / 1000.0)
 
     # ---- end to end through the C API with host buffers
     img = np.zeros((a.size, a.size, 4), np.uint8)
@@ -260,12 +278,8 @@ def main():
     t0 = time.perf_counter()
     for _ in range(e_steps):
         e2e_step()
-    e_t = (time.perf_counter() - t0) / e_steps
-    if dist:
-        t = torch.tensor([e_t], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e_t = float(t.item())
-    e2e_value = paths * world / e_t
+    e_t = reduce_max((time.perf_counter() - t0) / e_steps, dist, "cuda")
+    e2e_value = whole_job_rate(paths, world, e_t)
     h2d = int(stats[12])
     d2h = a.size * a.size * 4
 
@@ -275,16 +289,19 @@ def main():
     raster_bytes = 8 * nflat + 8 * nsv + 8 * a.size * a.size
     raster_ms = tot[3] / a.steps
     achieved = raster_bytes / (raster_ms / 1000.0) / 1e9
-    frame_bytes = 8 * len(cmds) + 16 * nflat + 16 * nsv + 8 * a.size * a.size
-    traffic = None
+    n_ctrl = len(args) // 2
+    frame_bytes = 8 * n_ctrl + 4 * len(cmds) + 16 * nflat + 16 * nsv + 8 * a.size * a.size
+    prof = {}
     tfile = os.path.join(ROOT, "profiles", "raster_curve_heavy_1024.md")
     if os.path.exists(tfile):
         for ln in open(tfile):
-            if ln.startswith("dram_bytes_per_launch:"):
+            k, _, v = ln.partition(":")
+            if k.strip() in ("dram_bytes_per_launch", "issue_slots_busy_pct", "alu_pipe_active_pct"):
                 try:
-                    traffic = int(ln.split(":")[1].split()[0])
-                except ValueError:
-                    traffic = None
+                    prof[k.strip()] = float(v.split()[0])
+                except (ValueError, IndexError):
+                    pass
+    traffic = int(prof["dram_bytes_per_launch"]) if "dram_bytes_per_launch" in prof else None
 
     line = {
         "metric": "paths/s", "value": value, "unit": "paths/s", "n_gpus": world, "steps": a.steps,
@@ -303,8 +320,11 @@ def main():
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "kernel": "gb_raster", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
-                     "algorithmic_bytes": raster_bytes,
-                     "frame_frac": frame_bytes / (ms / 1000.0) / 1e9 / peak},
+                     "algorithmic_bytes": raster_bytes, "frame_bytes": frame_bytes,
+                     "frame_frac": frame_bytes / (ms / 1000.0) / 1e9 / peak,
+                     "issue": {"bound": "sm issue", "issue_slots_busy_pct": prof.get("issue_slots_busy_pct"),
+                               "alu_pipe_active_pct": prof.get("alu_pipe_active_pct"),
+                               "source": "ncu summary in profiles/raster_curve_heavy_1024.md"}},
         "clocks": clk,
     }
     if rank == 0 and not a.no_cpu:

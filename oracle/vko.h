@@ -8,9 +8,9 @@
  * cited at each function in vko_geom.c), plus a software restatement of the
  * fixed-function state vkvg programs into Vulkan (vko_raster.c).  It is
  * cross-checked against vkvg's own behavioural tests (gunit_tests/context.cpp
- * current-point semantics, gunit_tests/matrices.cpp) and against an
- * independent pure-Python restatement of the flattening and stroke code on
- * small cases (tests/).
+ * current-point semantics, gunit_tests/matrices.cpp), against an
+ * independent pure-Python restatement of the cubic flattening (tests/pyref.py),
+ * and against its own committed outputs (tests/golden/).
  *
  * Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use
  * this library, and only as the checker or the timed CPU baseline.  The

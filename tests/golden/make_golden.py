@@ -1,0 +1,79 @@
+"""Generate the golden fixtures under tests/golden/ from the oracle.
+
+    python tests/golden/make_golden.py
+
+vkvg's tree holds no numeric fixtures or golden images for the path (its
+gunit PNGs are missing) and vkvg cannot run here, so these fixtures are the
+oracle's outputs on three small seeded scenes, committed so that any change
+of the oracle or of the GPU library against them is caught.  Per scene
+(<name>.npz): the final image (write_to_memory, unpremultiplied RGBA8), each
+draw's kind, the flattened points of fill draws, the vertices and indices of
+stroke draws, and a SHA-256 digest of every draw's per-sample winding /
+covering-triangle counts (int32 [height][width][samples], little endian).
+The oracle runs with its portable math (the kernels' math).
+"""
+import hashlib
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(HERE))
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+
+import oracle_bind as ob  # noqa: E402
+import parity_util as pu  # noqa: E402
+from vkvg_gb300 import scenes  # noqa: E402
+
+
+def golden_scenes():
+    return [scenes.plain_small(n_polys=12, size=96, seed=0),
+            scenes.curve_heavy(n_paths=10, size=128, seed=1, n_min=3, n_max=6),
+            scenes.api_mix(n_items=24, size=160, seed=5)]
+
+
+def _cat(parts, dtype, width):
+    if not parts:
+        return np.zeros((0,) + ((width,) if width else ()), dtype), np.zeros(1, np.uint32)
+    off = np.zeros(len(parts) + 1, np.uint32)
+    off[1:] = np.cumsum([len(p) for p in parts])
+    return np.concatenate([np.asarray(p, dtype) for p in parts]), off
+
+
+def digest(cov):
+    return np.frombuffer(hashlib.sha256(np.ascontiguousarray(cov, "<i4").tobytes()).digest(), np.uint8)
+
+
+def capture(sc):
+    L = ob.lib()
+    L.vko_set_math_mode(0)
+    surf, ctx = pu.run_oracle(ob, sc)
+    W, H, S = sc["width"], sc["height"], sc["samples"]
+    draws = ctx.draws()
+    kinds = np.array([d["kind"] for d in draws], np.uint32)
+    fpts = [d["points"] for d in draws if d["kind"] in (0, 1)]
+    sv = [d["verts"] for d in draws if d["kind"] == 2]
+    si = [d["inds"] for d in draws if d["kind"] == 2]
+    cov = np.zeros((len(draws), 32), np.uint8)
+    for i, d in enumerate(draws):
+        if d["kind"] in (0, 1, 2):
+            cov[i] = digest(ctx.coverage(i, W, H, S))
+    out = {"image": surf.image(), "kinds": kinds, "cov_sha256": cov}
+    out["fill_pts"], out["fill_pts_off"] = _cat(fpts, np.float32, 2)
+    out["stroke_verts"], out["stroke_verts_off"] = _cat(sv, np.float32, 2)
+    out["stroke_inds"], out["stroke_inds_off"] = _cat(si, np.uint32, 0)
+    ctx.destroy()
+    surf.destroy()
+    return out
+
+
+def main():
+    for sc in golden_scenes():
+        path = os.path.join(HERE, sc["name"] + ".npz")
+        np.savez_compressed(path, **capture(sc))
+        print(path, os.path.getsize(path))
+
+
+if __name__ == "__main__":
+    main()

@@ -18,6 +18,7 @@ def small_scenes():
     out = [
         scenes.plain_small(n_polys=12, size=96, seed=0),
         scenes.curve_heavy(n_paths=10, size=128, seed=1, n_min=3, n_max=6),
+        scenes.api_mix(n_items=24, size=160, seed=5),
     ]
     for o in out:
         o["samples"] = 4
@@ -36,7 +37,7 @@ def test_pmath_device_matches_host(gb, fn):
     assert np.array_equal(h.view(np.uint32), d.view(np.uint32))
 
 
-@pytest.mark.parametrize("idx", [0, 1])
+@pytest.mark.parametrize("idx", [0, 1, 2])
 def test_geometry_bit_exact(gb, vko, idx):
     sc = small_scenes()[idx]
     dev, surf, ctx = pu.run_gpu(gb, sc)
@@ -46,7 +47,7 @@ def test_geometry_bit_exact(gb, vko, idx):
     assert not errs, errs[:10]
 
 
-@pytest.mark.parametrize("idx", [0, 1])
+@pytest.mark.parametrize("idx", [0, 1, 2])
 def test_coverage_bit_exact(gb, vko, idx):
     sc = small_scenes()[idx]
     dev, surf, ctx = pu.run_gpu(gb, sc)
@@ -58,13 +59,48 @@ def test_coverage_bit_exact(gb, vko, idx):
         assert np.array_equal(g, o), "draw %d: %d samples differ" % (i, int((g != o).sum()))
 
 
-@pytest.mark.parametrize("idx", [0, 1])
+@pytest.mark.parametrize("idx", [0, 1, 2])
 def test_image_bit_exact(gb, vko, idx):
     sc = small_scenes()[idx]
     dev, surf, ctx = pu.run_gpu(gb, sc)
     osurf, octx = pu.run_oracle(vko, sc)
     assert np.array_equal(surf.samples_rgba(), osurf.samples_rgba())
     assert np.array_equal(surf.image(), osurf.image())
+
+
+@pytest.mark.parametrize("idx", [0, 1, 2])
+def test_gpu_matches_golden(gb, idx):
+    """the GPU library against the committed fixtures (tests/golden/), with no
+    oracle run: image, per-draw kinds, fill points, stroke buffers and the
+    digest of every draw's per-sample coverage"""
+    import os
+    import sys
+
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+    import make_golden
+
+    sc = small_scenes()[idx]
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", sc["name"] + ".npz"))
+    dev, surf, ctx = pu.run_gpu(gb, sc)
+    assert np.array_equal(surf.image(), g["image"])
+    first, count, _ = ctx.debug_subpaths()
+    n = int(ctx.debug_counts()[2])
+    kinds = np.array([int(ctx.debug_draw(i)[0]) for i in range(n)], np.uint32)
+    assert np.array_equal(kinds, g["kinds"])
+    fp, sv, si = [], [], []
+    for i in range(n):
+        info = ctx.debug_draw(i)
+        if kinds[i] in (0, 1):
+            fp.append(pu.gpu_draw_points(ctx, info, first, count)[0])
+        elif kinds[i] == 2:
+            v, ix = ctx.debug_stroke(i)
+            sv.append(v)
+            si.append(ix)
+        if kinds[i] in (0, 1, 2):
+            assert np.array_equal(make_golden.digest(ctx.debug_coverage(i)), g["cov_sha256"][i]), i
+    for parts, key, dt in ((fp, "fill_pts", np.float32), (sv, "stroke_verts", np.float32), (si, "stroke_inds", np.uint32)):
+        cat = np.concatenate(parts) if parts else np.zeros_like(g[key])
+        assert np.array_equal(cat.astype(dt).view(np.uint32), g[key].view(np.uint32)), key
 
 
 def test_curve_heavy_full_size_bit_exact(gb, vko):

@@ -19,6 +19,11 @@ for this path, so seeded synthetic inputs stand in for real content):
   U[0,1) with alpha U[0.3,1); then stroked in a second such colour at width
   U[1,8), join i mod 3 (miter/round/bevel), cap i mod 3 (butt/round/square),
   dash [10, 5] offset 0 when i mod 4 == 0.
+* ``api_mix`` - small surface exercising the rest of the path API: arcs in
+  both directions, elliptic arcs (all flag combinations), ellipses,
+  rectangles and rounded rectangles, quadratic and relative commands, sub
+  paths, transforms, opacity, every join and cap, multi-entry dash patterns
+  with offsets, and the CLEAR / DIFFERENCE operators.
 """
 
 MASK64 = (1 << 64) - 1
@@ -89,6 +94,62 @@ def curve_heavy(n_paths=2048, size=1024, seed=1, n_min=4, n_max=64):
         ops.append(("set_source_rgba",) + stroke)
         ops.append(("stroke",))
     return {"name": "curve_heavy", "width": size, "height": size, "samples": 4, "ops": ops, "paths": n_paths}
+
+
+def api_mix(n_items=24, size=160, seed=5, samples=4):
+    r = SplitMix64(seed)
+    u = lambda lo, hi: lo + (hi - lo) * r.rnd()
+    ops = [("set_source_rgb", 1.0, 1.0, 1.0), ("paint",)]
+    for i in range(n_items):
+        k = i % 8
+        ops.append(("identity_matrix",))
+        if i % 5 == 1:
+            ops += [("translate", u(-10, 10), u(-10, 10)), ("rotate", u(-0.4, 0.4))]
+        elif i % 5 == 3:
+            ops += [("scale", u(0.7, 1.3), u(0.7, 1.3))]
+        cx, cy = u(0.2, 0.8) * size, u(0.2, 0.8) * size
+        if k == 0:
+            ops += [("move_to", cx, cy), ("arc", cx, cy, u(4, 40), u(0, 3), u(3, 9)), ("close_path",)]
+        elif k == 1:
+            ops += [("arc_negative", cx, cy, u(3, 30), u(0, 6), u(-3, 1))]
+        elif k == 2:
+            ops += [("move_to", cx, cy)]
+            for j in range(3):
+                ops.append(("elliptic_arc_to", u(0, size), u(0, size), j % 2 == 0, (i + j) % 2 == 0, u(8, 50),
+                            u(8, 50), u(0, 3)))
+        elif k == 3:
+            ops += [("ellipse", u(5, 40), u(5, 40), cx, cy, u(0, 3))]
+        elif k == 4:
+            ops += [("rectangle", cx - 20, cy - 15, u(5, 50), u(5, 40)),
+                    ("rounded_rectangle", u(0, size * 0.6), u(0, size * 0.6), u(10, 60), u(10, 60), u(1, 8))]
+        elif k == 5:
+            ops += [("move_to", cx, cy), ("quadratic_to", u(0, size), u(0, size), u(0, size), u(0, size)),
+                    ("rel_quadratic_to", u(-30, 30), u(-30, 30), u(-30, 30), u(-30, 30)), ("close_path",)]
+        elif k == 6:
+            ops += [("move_to", cx, cy), ("rel_line_to", u(-40, 40), u(-40, 40)),
+                    ("rel_curve_to", u(-40, 40), u(-40, 40), u(-40, 40), u(-40, 40), u(-40, 40), u(-40, 40)),
+                    ("new_sub_path",), ("move_to", u(0, size), u(0, size)), ("line_to", u(0, size), u(0, size)),
+                    ("rel_move_to", u(-20, 20), u(-20, 20)), ("rel_line_to", u(-30, 30), u(-30, 30)),
+                    ("line_to", u(0, size), u(0, size))]
+        else:
+            ops += [("move_to", cx, cy)]
+            for j in range(r.randint(3, 7)):
+                ops.append(("line_to", u(0, size), u(0, size)))
+            if i % 2:
+                ops.append(("close_path",))
+        ops += [("set_fill_rule", i % 2), ("set_opacity", 1.0 if i % 3 else u(0.3, 1.0)),
+                ("set_source_rgba", r.rnd(), r.rnd(), r.rnd(), u(0.3, 1.0))]
+        ops.append(("set_operator", 3 if i % 11 == 10 else (0 if i % 13 == 12 else 2)))
+        ops.append(("fill_preserve",) if i % 4 != 2 else ("stroke_preserve",))
+        ops += [("set_operator", 2), ("set_line_width", u(0.5, 9)), ("set_line_join", (i // 2) % 3),
+                ("set_line_cap", (i // 3) % 3), ("set_miter_limit", u(1.5, 12))]
+        if i % 3 == 0:
+            ops.append(("set_dash", [u(2, 12), u(1, 8), u(1, 9)][: 2 + (i % 2)], u(0, 10)))
+        else:
+            ops.append(("set_dash", [], 0.0))
+        ops += [("set_source_rgba", r.rnd(), r.rnd(), r.rnd(), u(0.4, 1.0))]
+        ops.append(("stroke",) if i % 4 != 2 else ("fill",))
+    return {"name": "api_mix", "width": size, "height": size, "samples": samples, "ops": ops, "paths": n_items}
 
 
 def play(ctx, ops):
