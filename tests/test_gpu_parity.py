@@ -103,6 +103,32 @@ def test_gpu_matches_golden(gb, idx):
         assert np.array_equal(cat.astype(dt).view(np.uint32), g[key].view(np.uint32)), key
 
 
+def _twice_dashed_scene():
+    """the same paths stroked twice with different dash patterns
+    (stroke_preserve then stroke): a subpath in two dashed stroke pairs"""
+    r = scenes.SplitMix64(21)
+    ops = [("set_source_rgb", 1.0, 1.0, 1.0), ("paint",)]
+    for i in range(6):
+        ops.append(("move_to", r.rnd() * 120, r.rnd() * 120))
+        for _ in range(3):
+            ops.append(("curve_to",) + tuple(r.rnd() * 120 for _ in range(6)))
+        if i % 2:
+            ops.append(("close_path",))
+        ops += [("set_line_width", 1 + 5 * r.rnd()), ("set_line_cap", i % 3), ("set_line_join", (i + 1) % 3),
+                ("set_dash", [6.0, 3.0], 1.5), ("set_source_rgba", 0.8, 0.1, 0.1, 0.6), ("stroke_preserve",),
+                ("set_dash", [2.0, 4.0, 1.0], 0.0), ("set_source_rgba", 0.1, 0.1, 0.8, 0.5), ("stroke",)]
+    return {"name": "twice_dashed", "width": 128, "height": 128, "samples": 4, "ops": ops, "paths": 6}
+
+
+def test_twice_dashed_bit_exact(gb, vko):
+    sc = _twice_dashed_scene()
+    dev, surf, ctx = pu.run_gpu(gb, sc)
+    osurf, octx = pu.run_oracle(vko, sc)
+    errs = pu.compare_geometry(ctx, octx)
+    assert not errs, errs[:10]
+    assert np.array_equal(surf.image(), osurf.image())
+
+
 def test_curve_heavy_full_size_bit_exact(gb, vko):
     """The full 1024x1024, 2,048-path benchmark scene: every stroke/fill draw's
     geometry and the final 4x MSAA samples equal the oracle's."""

@@ -13,6 +13,7 @@
  * points in double - run here with the same portable math the kernels use.
  */
 #include "host.h"
+#include "launch.h"
 #include "pmath.h"
 
 #include <float.h>
@@ -34,6 +35,29 @@ static vkvg_status_t s_invalid_dev_ci = VKVG_STATUS_INVALID_DEVICE_CREATE_INFO;
 
 /* ================================================================ matrices */
 /* src/vkvg_matrix.c (cairo-derived) */
+/* Unpremultiply of vkvg_surface_write_to_memory (src/vkvg_surface.c:393-467,
+   the same loop as write_to_png :372-382): p = (uchar)(p / (a / 255.f)),
+   evaluated in double.  The result depends only on (a, p), so all 65,536
+   cases are evaluated once here with that exact expression and the device
+   applies the table.  Where vkvg's conversion is undefined (a == 0, or
+   p > a so that the quotient exceeds 255) the table holds 0 / 255. */
+const uint8_t *gb_unpremul_table() {
+    static uint8_t        t[65536];
+    static std::once_flag once;
+    std::call_once(once, [] {
+        for (uint32_t a = 0; a < 256; a++)
+            for (uint32_t p = 0; p < 256; p++) {
+                uint8_t r = 0;
+                if (a) {
+                    double alpha = (double)a / 255.f;
+                    double v     = (double)p / alpha;
+                    r            = v >= 255.0 ? 255 : (uint8_t)v;
+                }
+                t[a * 256 + p] = r;
+            }
+    });
+    return t;
+}
 extern "C" {
 void vkvg_matrix_init(vkvg_matrix_t *m, float xx, float yx, float xy, float yy, float x0, float y0) {
     m->xx = xx;
@@ -146,6 +170,14 @@ VkvgDevice vkvg_device_create(vkvg_device_create_info_t *info) {
     cudaGetDevice(&dev->cuda_dev);
     dev->thread_aware = info->threadAware;
     dev->hdpi = dev->vdpi = 96;
+    const uint8_t *lut = gb_unpremul_table();
+    if (cudaMalloc(&dev->d_unpremul, 65536) != cudaSuccess ||
+        cudaMemcpy(dev->d_unpremul, lut, 65536, cudaMemcpyHostToDevice) != cudaSuccess) {
+        if (dev->d_unpremul)
+            cudaFree(dev->d_unpremul);
+        delete dev;
+        return (VkvgDevice)&s_no_memory;
+    }
     return dev;
 }
 vkvg_status_t vkvg_device_status(VkvgDevice dev) { return dev ? dev->status : VKVG_STATUS_NULL_POINTER; }
@@ -154,6 +186,7 @@ void          vkvg_device_destroy(VkvgDevice dev) {
         return;
     if (--dev->refs > 0)
         return;
+    cudaFree(dev->d_unpremul);
     delete dev;
 }
 VkvgDevice vkvg_device_reference(VkvgDevice dev) {
@@ -194,9 +227,12 @@ static VkvgSurface surface_alloc(VkvgDevice dev, uint32_t width, uint32_t height
     s->nbands  = (s->nrows + GB_BAND_ROWS - 1) / GB_BAND_ROWS;
     size_t sb  = (size_t)s->nbands * GB_BAND_ROWS * s->wpad * 4;
     size_t rb  = (size_t)s->width * s->height * 4;
-    if (cudaMalloc(&s->d_samples, sb) != cudaSuccess || cudaMalloc(&s->d_rgba, rb) != cudaSuccess) {
+    if (cudaMalloc(&s->d_samples, sb) != cudaSuccess || cudaMalloc(&s->d_rgba, rb) != cudaSuccess ||
+        cudaMalloc(&s->d_out, rb) != cudaSuccess) {
         if (s->d_samples)
             cudaFree(s->d_samples);
+        if (s->d_rgba)
+            cudaFree(s->d_rgba);
         delete s;
         return (VkvgSurface)&s_no_memory;
     }
@@ -246,6 +282,7 @@ void     vkvg_surface_destroy(VkvgSurface s) {
         return;
     cudaFree(s->d_samples);
     cudaFree(s->d_rgba);
+    cudaFree(s->d_out);
     VkvgDevice dev = s->dev;
     delete s;
     vkvg_device_destroy(dev);
@@ -291,30 +328,18 @@ vkvg_status_t vkvg_gb300_surface_read_samples(VkvgSurface s, uint8_t *out) {
                 memcpy(out + (((size_t)y * s->width + x) * rpp + k) * 4, &h[(size_t)(y * rpp + k) * s->wpad + x], 4);
     return VKVG_STATUS_SUCCESS;
 }
-/* vkvg_surface_write_to_memory, src/vkvg_surface.c:393-467: resolved image,
-   then p = (uchar)(p / (a / 255.f)) in double.  Where vkvg's conversion is
-   undefined (a == 0, or p > a) this writes 0 / clamps to 255. */
 vkvg_status_t vkvg_surface_write_to_memory(VkvgSurface s, unsigned char *const bitmap) {
     if (vkvg_surface_status(s))
         return VKVG_STATUS_INVALID_STATUS;
     if (!bitmap)
         return VKVG_STATUS_WRITE_ERROR;
-    vkvg_status_t r = vkvg_gb300_surface_read_premult(s, bitmap);
-    if (r)
-        return r;
-    size_t n = (size_t)s->width * s->height;
-    for (size_t p = 0; p < n; p++) {
-        uint8_t *q     = bitmap + p * 4;
-        double   alpha = (double)q[3] / 255.f;
-        for (int c = 0; c < 3; c++) {
-            if (q[3] == 0) {
-                q[c] = 0;
-                continue;
-            }
-            double v = (double)q[c] / alpha;
-            q[c]     = v >= 255.0 ? 255 : (uint8_t)v;
-        }
-    }
+    std::lock_guard<std::mutex> lk(s->mtx);
+    size_t                      n = (size_t)s->width * s->height;
+    if (gb_launch_unpremultiply(0, s->d_rgba, n, s->dev->d_unpremul, s->d_out) != cudaSuccess)
+        return VKVG_STATUS_DEVICE_ERROR;
+    gb_count_launch(1);
+    if (cudaMemcpy(bitmap, s->d_out, n * 4, cudaMemcpyDeviceToHost) != cudaSuccess)
+        return VKVG_STATUS_DEVICE_ERROR;
     return VKVG_STATUS_SUCCESS;
 }
 vkvg_status_t vkvg_surface_write_to_png(VkvgSurface s, const char *path) {
@@ -770,6 +795,9 @@ static void stroke_preserve_i(VkvgContext ctx) {
         d.dash_offset = ctx->dash_offset;
         f.dashes.insert(f.dashes.end(), ctx->dashes.begin(), ctx->dashes.end());
         f.any_dash = true;
+        if (d.sub_first < f.dash_sub_hi)
+            f.dash_shared = true; /* e.g. stroke_preserve then stroke, both dashed */
+        f.dash_sub_hi = std::max(f.dash_sub_hi, d.sub_first + d.sub_count);
     }
     uint32_t di = (uint32_t)f.draws.size();
     f.draws.push_back(d);

@@ -33,6 +33,8 @@ struct FrameHost {
     std::vector<float>    dashes, thetas;
     uint32_t              paths = 0; /* fill + stroke draws */
     bool                  any_dash = false;
+    bool                  dash_shared = false; /* a subpath belongs to two dashed stroke pairs */
+    uint32_t              dash_sub_hi = 0;     /* end of the subpath ranges dashed strokes used */
     void                  clear();
     bool                  empty() const { return draws.empty(); }
 };
@@ -60,6 +62,7 @@ struct Pipeline {
     DevBuf       fe_cnt, fe_off, edges, edge_draw;
     DevBuf       sdraw_tri0, sdraw_vbase, tri_a, tri_b, tri_draw;
     DevBuf       cells, cursor, recs, status, dbg;
+    DevBuf       dseglen, dseg, dfin; /* parallel dash walk: per-point lengths / states, per-pair final state */
     PinnedBuf    staging, rb;
     cudaEvent_t  evs[8] = {};
     /* offsets of the uploaded arrays inside `in` */
@@ -91,6 +94,7 @@ struct _vkvg_device_t {
     int           cuda_dev;
     bool          thread_aware;
     int           hdpi, vdpi;
+    uint8_t      *d_unpremul; /* [alpha][channel] -> write_to_memory's unpremultiplied byte */
     std::mutex    mtx;
 };
 
@@ -101,6 +105,7 @@ struct _vkvg_surface_t {
     uint32_t      width, height, samples, wpad, nrows, nbands;
     uint32_t     *d_samples; /* [nrows][wpad] premultiplied RGBA8 */
     uint32_t     *d_rgba;    /* [height][width] resolved */
+    uint32_t     *d_out;     /* [height][width] unpremultiplied, staged for write_to_memory */
     std::mutex    mtx;
 };
 
@@ -155,6 +160,8 @@ vkvg_status_t gb_run_frame(Pipeline &pl, const FrameHost &f, VkvgSurface surf, b
 void          gb_count_launch(uint64_t n);
 /* premultiplied source word after opacity (fragment stage + UNORM8 output) */
 uint32_t gb_source_word(uint32_t color, float opacity);
+/* write_to_memory's unpremultiply for every (alpha, channel) pair, [a * 256 + p] */
+const uint8_t *gb_unpremul_table();
 int      gb_png_write(const char *path, uint32_t w, uint32_t h, const uint8_t *rgba);
 
 #endif

@@ -22,6 +22,9 @@ struct gb_raster_args {
 };
 
 extern "C" {
+/* out[i] = table-unpremultiplied in[i] (RGBA8, alpha in the top byte) */
+cudaError_t gb_launch_unpremultiply(cudaStream_t st, const uint32_t *in, size_t n, const uint8_t *table,
+                                    uint32_t *out);
 size_t      gb_scan_scratch_words(uint32_t n);
 cudaError_t gb_exclusive_scan(cudaStream_t st, const uint32_t *in, uint32_t n, uint32_t *out, uint32_t *scratch);
 
@@ -38,7 +41,19 @@ cudaError_t gb_launch_subpath_ranges(cudaStream_t st, uint32_t nsub, const uint3
 cudaError_t gb_launch_stroke_pair_events(cudaStream_t st, uint32_t npairs, const uint32_t *pair_draw,
                                          const uint32_t *pair_sub, const gb_draw *draws, const uint32_t *sub_pt0,
                                          const uint32_t *sub_npts, const uint32_t *sub_flags, const float2 *pts,
-                                         const uint8_t *pflag, const float *dashes, uint32_t *counts);
+                                         const uint8_t *pflag, const float *dashes, uint32_t *counts,
+                                         int walk_dashes);
+/* dashed subpaths in parallel: segment lengths + sequential dash state (counts
+   of dashed pairs), then the events; see stroke.cu */
+cudaError_t gb_launch_dash_count(cudaStream_t st, uint32_t npairs, const uint32_t *pair_draw, const uint32_t *pair_sub,
+                                 const gb_draw *draws, const uint32_t *sub_pt0, const uint32_t *sub_npts,
+                                 const uint32_t *sub_flags, const float2 *pts, const float *dashes, float *seglen,
+                                 uint4 *dseg, uint4 *dfin, uint32_t *counts);
+cudaError_t gb_launch_dash_emit(cudaStream_t st, uint32_t npairs, const uint32_t *pair_draw, const uint32_t *pair_sub,
+                                const gb_draw *draws, const uint32_t *sub_pt0, const uint32_t *sub_npts,
+                                const uint32_t *sub_flags, const float2 *pts, const uint8_t *pflag,
+                                const float *dashes, const uint4 *dseg, const uint4 *dfin, const uint32_t *ev_off,
+                                gb_event *events);
 cudaError_t gb_launch_stroke_dash_events(cudaStream_t st, uint32_t npairs, const uint32_t *pair_draw,
                                          const uint32_t *pair_sub, const gb_draw *draws, const uint32_t *sub_pt0,
                                          const uint32_t *sub_npts, const uint32_t *sub_flags, const float2 *pts,

@@ -35,8 +35,10 @@ void FrameHost::clear() {
     fpair_sub.clear();
     dashes.clear();
     thetas.clear();
-    paths    = 0;
-    any_dash = false;
+    paths       = 0;
+    any_dash    = false;
+    dash_shared = false;
+    dash_sub_hi = 0;
 }
 
 bool DevBuf::grow(size_t bytes) {
@@ -96,7 +98,7 @@ void Pipeline::destroy() {
     DevBuf *bufs[] = {&in,     &seg_cnt, &seg_off,   &scratch,    &pts,         &pflag,    &sub_pt0, &sub_npts,
                       &ev_cnt, &ev_off,  &events,    &cnt_v,      &cnt_i,       &off_v,    &off_i,   &verts,
                       &inds,   &ev_ret,  &fe_cnt,    &fe_off,     &edges,       &edge_draw, &sdraw_tri0,
-                      &sdraw_vbase, &tri_a, &tri_b, &tri_draw, &cells,   &cursor,   &recs,    &status, &dbg};
+                      &sdraw_vbase, &tri_a, &tri_b, &tri_draw, &cells,   &cursor,   &recs,    &status, &dseglen, &dseg, &dfin, &dbg};
     for (DevBuf *b : bufs)
         b->release();
     staging.release();
@@ -226,9 +228,20 @@ cudaError_t Pipeline::run(const FrameHost &f, _vkvg_surface_t *surf, bool timing
     GROW(ev_off, (size_t)(nspair + 1) * 4);
     GROW(fe_cnt, (size_t)(nfpair + 1) * 4);
     GROW(fe_off, (size_t)(nfpair + 1) * 4);
+    /* dashed pairs: parallel walk unless a subpath is shared by two dashed pairs */
+    const bool fast_dash = f.any_dash && !f.dash_shared;
     CK(gb_launch_stroke_pair_events(st, nspair, U(o_spd), U(o_sps), draws, sub_pt0.as<uint32_t>(),
                                     sub_npts.as<uint32_t>(), U(o_sub_flags), pts.as<float2>(), pflag.as<uint8_t>(),
-                                    dsh, ev_cnt.as<uint32_t>()));
+                                    dsh, ev_cnt.as<uint32_t>(), fast_dash ? 0 : 1));
+    if (fast_dash) {
+        GROW(dseglen, (size_t)(npts + 1) * 4);
+        GROW(dseg, (size_t)(npts + 1) * 16);
+        GROW(dfin, (size_t)(nspair + 1) * 16);
+        CK(gb_launch_dash_count(st, nspair, U(o_spd), U(o_sps), draws, sub_pt0.as<uint32_t>(), sub_npts.as<uint32_t>(),
+                                U(o_sub_flags), pts.as<float2>(), dsh, dseglen.as<float>(), dseg.as<uint4>(),
+                                dfin.as<uint4>(), ev_cnt.as<uint32_t>()));
+        gb_count_launch(2);
+    }
     CK(gb_launch_fill_pair_edges(st, nfpair, U(o_fps), sub_npts.as<uint32_t>(), fe_cnt.as<uint32_t>()));
     gb_count_launch((nspair ? 1 : 0) + (nfpair ? 1 : 0));
     CK(scan(*this, ev_cnt.as<uint32_t>(), nspair, ev_off.as<uint32_t>()));
@@ -240,7 +253,12 @@ cudaError_t Pipeline::run(const FrameHost &f, _vkvg_surface_t *surf, bool timing
     nev    = hv[0];
     nedges = hv[1];
     GROW(events, (size_t)(f.any_dash ? nev + 1 : 1) * sizeof(gb_event));
-    if (f.any_dash) {
+    if (fast_dash) {
+        CK(gb_launch_dash_emit(st, nspair, U(o_spd), U(o_sps), draws, sub_pt0.as<uint32_t>(), sub_npts.as<uint32_t>(),
+                               U(o_sub_flags), pts.as<float2>(), pflag.as<uint8_t>(), dsh, dseg.as<uint4>(),
+                               dfin.as<uint4>(), ev_off.as<uint32_t>(), events.as<gb_event>()));
+        gb_count_launch(1);
+    } else if (f.any_dash) {
         CK(gb_launch_stroke_dash_events(st, nspair, U(o_spd), U(o_sps), draws, sub_pt0.as<uint32_t>(),
                                         sub_npts.as<uint32_t>(), U(o_sub_flags), pts.as<float2>(),
                                         pflag.as<uint8_t>(), dsh, ev_off.as<uint32_t>(), events.as<gb_event>()));

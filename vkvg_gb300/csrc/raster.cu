@@ -608,6 +608,27 @@ __global__ void __launch_bounds__(XT_THREADS, 1) gb_raster(gb_raster_args A) {
     }
 }
 
+/* write_to_memory's unpremultiply: one table lookup per colour channel
+   (the table holds vkvg's double-precision expression for every (a, p)) */
+__global__ void gb_unpremultiply(const uint32_t *__restrict__ in, size_t n, const uint8_t *__restrict__ table,
+                                 uint32_t *__restrict__ out) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    const uint32_t v  = in[i];
+    const uint32_t a  = v >> 24;
+    const uint8_t *ta = table + (a << 8);
+    out[i]            = (uint32_t)__ldg(ta + (v & 0xFFu)) | ((uint32_t)__ldg(ta + ((v >> 8) & 0xFFu)) << 8) |
+             ((uint32_t)__ldg(ta + ((v >> 16) & 0xFFu)) << 16) | (a << 24);
+}
+extern "C" cudaError_t gb_launch_unpremultiply(cudaStream_t st, const uint32_t *in, size_t n, const uint8_t *table,
+                                               uint32_t *out) {
+    if (!n)
+        return cudaSuccess;
+    gb_unpremultiply<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(in, n, table, out);
+    return cudaGetLastError();
+}
+
 extern "C" cudaError_t gb_launch_raster(cudaStream_t st, const gb_raster_args *a) {
     static bool configured = false;
     if (!configured) {

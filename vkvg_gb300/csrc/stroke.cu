@@ -398,7 +398,7 @@ __global__ void gb_stroke_pair_events(uint32_t npairs, const uint32_t *__restric
                                       const uint32_t *__restrict__ sub_pt0, const uint32_t *__restrict__ sub_npts,
                                       const uint32_t *__restrict__ sub_flags, const float2 *__restrict__ pts,
                                       const uint8_t *__restrict__ pflag, const float *__restrict__ dashes,
-                                      uint32_t *__restrict__ counts) {
+                                      uint32_t *__restrict__ counts, int walk_dashes) {
     uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= npairs)
         return;
@@ -413,6 +413,8 @@ __global__ void gb_stroke_pair_events(uint32_t npairs, const uint32_t *__restric
         counts[p] = n;
         return;
     }
+    if (!walk_dashes)
+        return; /* counted by gb_dash_state */
     counts[p] = gb_dash_walk(pts, pflag, sub_pt0[s], n, (sub_flags[s] & GB_SUB_CLOSED) != 0, dashes + d.dash_first,
                              d.dash_count, d.dash_offset, nullptr, 0);
 }
@@ -433,6 +435,152 @@ __global__ void gb_stroke_dash_events(uint32_t npairs, const uint32_t *__restric
         return;
     gb_dash_walk(pts, pflag, sub_pt0[s], n, (sub_flags[s] & GB_SUB_CLOSED) != 0, dashes + d.dash_first, d.dash_count,
                  d.dash_offset, events + ev_off[p], ev_off[p + 1] - ev_off[p]);
+}
+
+/* ---- dashed subpaths in parallel.
+ *
+ * The same computation as gb_dash_walk in three steps: (A) every segment's
+ * length, in parallel; (B) per dashed pair, only the sequential dash
+ * recurrence over those lengths, recording at each segment's first point the
+ * dash state entering it, its event offset within the pair and its number of
+ * dash boundaries; (C) every segment's events replayed from that state, in
+ * parallel.  Each float operation is the one gb_dash_walk performs, in the
+ * same order, so the events are identical.  The per-point records require
+ * that no subpath belongs to two dashed pairs of one frame (the host falls
+ * back to gb_dash_walk otherwise). */
+__global__ void gb_dash_seglen(uint32_t npairs, const uint32_t *__restrict__ pair_draw,
+                               const uint32_t *__restrict__ pair_sub, const gb_draw *__restrict__ draws,
+                               const uint32_t *__restrict__ sub_pt0, const uint32_t *__restrict__ sub_npts,
+                               const uint32_t *__restrict__ sub_flags, const float2 *__restrict__ pts,
+                               float *__restrict__ seglen) {
+    const uint32_t p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (p >= npairs)
+        return;
+    const gb_draw &d = draws[pair_draw[p]];
+    const uint32_t s = pair_sub[p], n = sub_npts[s];
+    if (n < 2 || d.dash_count == 0)
+        return;
+    const uint32_t first = sub_pt0[s];
+    const uint32_t nseg  = n - 1 + ((sub_flags[s] & GB_SUB_CLOSED) ? 1u : 0u);
+    for (uint32_t j = lane; j < nseg; j += 32) {
+        const uint32_t cp = first + j, iR = j < n - 1 ? cp + 1 : first;
+        seglen[cp]        = v_len(v_sub(pts[iR], pts[cp]));
+    }
+}
+__global__ void gb_dash_state(uint32_t npairs, const uint32_t *__restrict__ pair_draw,
+                              const uint32_t *__restrict__ pair_sub, const gb_draw *__restrict__ draws,
+                              const uint32_t *__restrict__ sub_pt0, const uint32_t *__restrict__ sub_npts,
+                              const uint32_t *__restrict__ sub_flags, const float *__restrict__ dash_arr,
+                              const float *__restrict__ seglen, uint4 *__restrict__ dseg, uint4 *__restrict__ dfin,
+                              uint32_t *__restrict__ counts) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= npairs)
+        return;
+    const gb_draw &d = draws[pair_draw[p]];
+    const uint32_t s = pair_sub[p], n = sub_npts[s];
+    if (n < 2 || d.dash_count == 0)
+        return;
+    const float   *dashes = dash_arr + d.dash_first;
+    const uint32_t dcount = d.dash_count;
+    float          tot    = 0;
+    for (uint32_t i = 0; i < dcount; i++)
+        tot += dashes[i];
+    bool           dashOn  = true;
+    uint32_t       curDash = 0;
+    float          curOff  = fmodf(d.dash_offset, tot);
+    uint32_t       ne      = 0;
+    const uint32_t first   = sub_pt0[s];
+    const uint32_t nseg    = n - 1 + ((sub_flags[s] & GB_SUB_CLOSED) ? 1u : 0u);
+    const float    atot    = fabsf(tot);
+    for (uint32_t j = 0; j < nseg; j++) {
+        const uint32_t cp = first + j;
+        uint4          rec = make_uint4(__float_as_uint(curOff), curDash | (dashOn ? 0x80000000u : 0u), ne, 0);
+        if (!dashOn)
+            ne++; /* the segment's join */
+        const float sl = seglen[cp];
+        uint32_t    k  = 0;
+        while (curOff < sl && ne < GB_DASH_LOOP_CAP) {
+            ne++;
+            dashOn = !dashOn;
+            curOff += dashes[curDash];
+            if (++curDash == dcount)
+                curDash = 0;
+            k++;
+        }
+        curOff -= sl;
+        if (!(fabsf(curOff) < atot)) /* fmodf(x, t) is x itself when |x| < |t| */
+            curOff = fmodf(curOff, tot);
+        rec.w    = k;
+        dseg[cp] = rec;
+    }
+    const uint32_t total = ne + (dashOn ? 0u : 1u);
+    dfin[p]   = make_uint4(__float_as_uint(curOff), curDash | (dashOn ? 0x80000000u : 0u), total, 0);
+    counts[p] = total;
+}
+__global__ void gb_dash_emit(uint32_t npairs, const uint32_t *__restrict__ pair_draw,
+                             const uint32_t *__restrict__ pair_sub, const gb_draw *__restrict__ draws,
+                             const uint32_t *__restrict__ sub_pt0, const uint32_t *__restrict__ sub_npts,
+                             const uint32_t *__restrict__ sub_flags, const float2 *__restrict__ pts,
+                             const uint8_t *__restrict__ pflag, const float *__restrict__ dash_arr,
+                             const uint4 *__restrict__ dseg, const uint4 *__restrict__ dfin,
+                             const uint32_t *__restrict__ ev_off, gb_event *__restrict__ events) {
+    const uint32_t p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (p >= npairs)
+        return;
+    const gb_draw &d = draws[pair_draw[p]];
+    const uint32_t s = pair_sub[p], n = sub_npts[s];
+    if (n < 2 || d.dash_count == 0)
+        return;
+    const float   *dashes = dash_arr + d.dash_first;
+    const uint32_t dcount = d.dash_count;
+    const uint32_t first = sub_pt0[s], last = first + n - 1;
+    const uint32_t nseg  = n - 1 + ((sub_flags[s] & GB_SUB_CLOSED) ? 1u : 0u);
+    gb_event      *ev    = events + ev_off[p];
+    const uint32_t cap   = ev_off[p + 1] - ev_off[p];
+    for (uint32_t j = lane; j < nseg; j += 32) {
+        const uint32_t cp = first + j, iR = j < n - 1 ? cp + 1 : first, iL = j == 0 ? last : cp - 1;
+        const bool     curved  = j < n - 1 ? pflag[cp] != 0 : false;
+        const uint4    rec     = dseg[cp];
+        float          curOff  = __uint_as_float(rec.x);
+        uint32_t       curDash = rec.y & 0x7FFFFFFFu;
+        bool           dashOn  = (rec.y >> 31) != 0;
+        uint32_t       e       = rec.z;
+        if (!dashOn) {
+            if (e < cap)
+                ev[e] = {GB_EV_JOIN | (curved ? 0x100u : 0u), cp, iL, iR, 0, 0, 0, 0};
+            e++;
+        }
+        const float2 pc     = pts[cp];
+        const float2 normal = v_norm(v_sub(pts[iR], pc));
+        for (uint32_t k = 0; k < rec.w; k++) {
+            const float2 p0 = v_add(pc, v_mul(normal, curOff));
+            if (e < cap)
+                ev[e] = {dashOn ? GB_EV_CAP_START : GB_EV_CAP_END, 0, 0, 0, p0.x, p0.y, normal.x, normal.y};
+            e++;
+            dashOn = !dashOn;
+            curOff += dashes[curDash];
+            if (++curDash == dcount)
+                curDash = 0;
+        }
+    }
+    if (lane == 0) {
+        const uint4 fin = dfin[p];
+        if ((fin.y >> 31) == 0) { /* the dash is still on: close it at the end */
+            const float    curOff  = __uint_as_float(fin.x);
+            uint32_t       curDash = fin.y & 0x7FFFFFFFu;
+            const uint32_t cpl = first + nseg - 1, iRl = nseg - 1 < n - 1 ? cpl + 1 : first;
+            const float2   normal  = v_norm(v_sub(pts[iRl], pts[cpl]));
+            int32_t        prevDash = (int32_t)curDash - 1;
+            if (prevDash < 0) {
+                curDash  = dcount - 1;
+                prevDash = (int32_t)dcount - 1;
+            }
+            const float  m  = fminf(dashes[prevDash] - curOff, dashes[curDash]);
+            const float2 pe = v_sub(pts[iRl], v_mul(normal, m));
+            if (fin.z - 1 < cap)
+                ev[fin.z - 1] = {GB_EV_CAP_END, 0, 0, 0, pe.x, pe.y, normal.x, normal.y};
+        }
+    }
 }
 
 /* locate the pair of a global event index */
@@ -610,11 +758,35 @@ cudaError_t gb_launch_stroke_draw_bases(cudaStream_t st, uint32_t ndraw_s, const
 cudaError_t gb_launch_stroke_pair_events(cudaStream_t st, uint32_t npairs, const uint32_t *pair_draw,
                                          const uint32_t *pair_sub, const gb_draw *draws, const uint32_t *sub_pt0,
                                          const uint32_t *sub_npts, const uint32_t *sub_flags, const float2 *pts,
-                                         const uint8_t *pflag, const float *dashes, uint32_t *counts) {
+                                         const uint8_t *pflag, const float *dashes, uint32_t *counts,
+                                         int walk_dashes) {
     if (!npairs)
         return cudaSuccess;
     gb_stroke_pair_events<<<(npairs + 127) / 128, 128, 0, st>>>(npairs, pair_draw, pair_sub, draws, sub_pt0, sub_npts,
-                                                                 sub_flags, pts, pflag, dashes, counts);
+                                                                 sub_flags, pts, pflag, dashes, counts, walk_dashes);
+    return cudaGetLastError();
+}
+cudaError_t gb_launch_dash_count(cudaStream_t st, uint32_t npairs, const uint32_t *pair_draw, const uint32_t *pair_sub,
+                                 const gb_draw *draws, const uint32_t *sub_pt0, const uint32_t *sub_npts,
+                                 const uint32_t *sub_flags, const float2 *pts, const float *dashes, float *seglen,
+                                 uint4 *dseg, uint4 *dfin, uint32_t *counts) {
+    if (!npairs)
+        return cudaSuccess;
+    gb_dash_seglen<<<(npairs + 7) / 8, 256, 0, st>>>(npairs, pair_draw, pair_sub, draws, sub_pt0, sub_npts, sub_flags,
+                                                      pts, seglen);
+    gb_dash_state<<<(npairs + 63) / 64, 64, 0, st>>>(npairs, pair_draw, pair_sub, draws, sub_pt0, sub_npts, sub_flags,
+                                                      dashes, seglen, dseg, dfin, counts);
+    return cudaGetLastError();
+}
+cudaError_t gb_launch_dash_emit(cudaStream_t st, uint32_t npairs, const uint32_t *pair_draw, const uint32_t *pair_sub,
+                                const gb_draw *draws, const uint32_t *sub_pt0, const uint32_t *sub_npts,
+                                const uint32_t *sub_flags, const float2 *pts, const uint8_t *pflag,
+                                const float *dashes, const uint4 *dseg, const uint4 *dfin, const uint32_t *ev_off,
+                                gb_event *events) {
+    if (!npairs)
+        return cudaSuccess;
+    gb_dash_emit<<<(npairs + 7) / 8, 256, 0, st>>>(npairs, pair_draw, pair_sub, draws, sub_pt0, sub_npts, sub_flags,
+                                                    pts, pflag, dashes, dseg, dfin, ev_off, events);
     return cudaGetLastError();
 }
 cudaError_t gb_launch_stroke_dash_events(cudaStream_t st, uint32_t npairs, const uint32_t *pair_draw,
