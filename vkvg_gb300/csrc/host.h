@@ -62,7 +62,8 @@ struct Pipeline {
     DevBuf       fe_cnt, fe_off, edges, edge_draw;
     DevBuf       sdraw_tri0, sdraw_vbase, tri_a, tri_b, tri_draw;
     DevBuf       cells, cursor, recs, status, dbg;
-    DevBuf       dseglen, dseg, dfin; /* parallel dash walk: per-point lengths / states, per-pair final state */
+    DevBuf       dseglen, dseg, dfin;
+    DevBuf       tri_idx; /* oriented vertex indices of stroke triangles (edge cancellation) */ /* parallel dash walk: per-point lengths / states, per-pair final state */
     PinnedBuf    staging, rb;
     cudaEvent_t  evs[8] = {};
     /* offsets of the uploaded arrays inside `in` */

@@ -88,7 +88,7 @@ cudaError_t gb_launch_fill_edges(cudaStream_t st, uint32_t nedges, uint32_t npai
 cudaError_t gb_launch_stroke_tris(cudaStream_t st, uint32_t ntris, uint32_t ndraw_s, const uint32_t *draw_tri0,
                                   const uint32_t *sdraw_id, const uint32_t *draw_vbase, const gb_draw *draws,
                                   const float2 *verts, const uint32_t *inds, uint32_t W, uint32_t H, int4 *tri_a,
-                                  int4 *tri_b, uint32_t *tri_draw);
+                                  int4 *tri_b, uint32_t *tri_draw, uint4 *tri_idx, int4 *edges, uint32_t *edge_draw);
 cudaError_t gb_launch_bin(cudaStream_t st, int scatter, uint32_t nedges, const int4 *edges, const uint32_t *edge_draw,
                           uint32_t ntris, const int4 *tri_a, const int4 *tri_b, const uint32_t *tri_draw,
                           uint32_t ndraws, uint32_t W, uint32_t samples, uint32_t nrows, uint32_t *cell,

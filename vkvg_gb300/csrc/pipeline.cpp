@@ -98,7 +98,7 @@ void Pipeline::destroy() {
     DevBuf *bufs[] = {&in,     &seg_cnt, &seg_off,   &scratch,    &pts,         &pflag,    &sub_pt0, &sub_npts,
                       &ev_cnt, &ev_off,  &events,    &cnt_v,      &cnt_i,       &off_v,    &off_i,   &verts,
                       &inds,   &ev_ret,  &fe_cnt,    &fe_off,     &edges,       &edge_draw, &sdraw_tri0,
-                      &sdraw_vbase, &tri_a, &tri_b, &tri_draw, &cells,   &cursor,   &recs,    &status, &dseglen, &dseg, &dfin, &dbg};
+                      &sdraw_vbase, &tri_a, &tri_b, &tri_draw, &cells,   &cursor,   &recs,    &status, &dseglen, &dseg, &dfin, &tri_idx, &dbg};
     for (DevBuf *b : bufs)
         b->release();
     staging.release();
@@ -304,37 +304,41 @@ cudaError_t Pipeline::run(const FrameHost &f, _vkvg_surface_t *surf, bool timing
 
     /* ---------------- K3 primitive setup + binning */
     const uint32_t W = surf->width, H = surf->height, S = surf->samples;
-    GROW(edges, (size_t)(nedges + 1) * 16);
-    GROW(edge_draw, (size_t)(nedges + 1) * 4);
+    /* edges: fill edges, then three slots per stroke triangle */
+    const uint32_t nedge_all = nedges + 3 * ntris;
+    GROW(edges, (size_t)(nedge_all + 1) * 16);
+    GROW(edge_draw, (size_t)(nedge_all + 1) * 4);
     GROW(tri_a, (size_t)(ntris + 1) * 16);
     GROW(tri_b, (size_t)(ntris + 1) * 16);
     GROW(tri_draw, (size_t)(ntris + 1) * 4);
+    GROW(tri_idx, (size_t)(ntris + 1) * 16);
     CK(gb_launch_fill_edges(st, nedges, nfpair, fe_off.as<uint32_t>(), U(o_fpd), U(o_fps), draws,
                             sub_pt0.as<uint32_t>(), sub_npts.as<uint32_t>(), pts.as<float2>(), W, H, edges.as<int4>(),
                             edge_draw.as<uint32_t>()));
     CK(gb_launch_stroke_tris(st, ntris, nsdraw, sdraw_tri0.as<uint32_t>(), U(o_sdid), sdraw_vbase.as<uint32_t>(),
                              draws, verts.as<float2>(), inds.as<uint32_t>(), W, H, tri_a.as<int4>(), tri_b.as<int4>(),
-                             tri_draw.as<uint32_t>()));
-    gb_count_launch((nedges ? 1 : 0) + (ntris ? 1 : 0));
+                             tri_draw.as<uint32_t>(), tri_idx.as<uint4>(), edges.as<int4>() + nedges,
+                             edge_draw.as<uint32_t>() + nedges));
+    gb_count_launch((nedges ? 1 : 0) + (ntris ? 2 : 0));
     nbands          = surf->nbands;
     size_t ncells   = (size_t)nbands * ndraw;
     GROW(cells, (ncells + 1) * 4);
     GROW(cursor, (ncells + 1) * 4);
     CK(cudaMemsetAsync(cells.p, 0, (ncells + 1) * 4, st));
-    CK(gb_launch_bin(st, 0, nedges, edges.as<int4>(), edge_draw.as<uint32_t>(), ntris, tri_a.as<int4>(),
+    CK(gb_launch_bin(st, 0, nedge_all, edges.as<int4>(), edge_draw.as<uint32_t>(), 0, tri_a.as<int4>(),
                      tri_b.as<int4>(), tri_draw.as<uint32_t>(), ndraw, W, S, surf->nrows, cells.as<uint32_t>(),
                      nullptr, 0u));
-    gb_count_launch((nedges ? 1 : 0) + (ntris ? 1 : 0));
+    gb_count_launch(nedge_all ? 1 : 0);
     CK(scan(*this, cells.as<uint32_t>(), (uint32_t)ncells, cursor.as<uint32_t>()));
     CK(readback_u32(*this, cursor.as<uint32_t>() + ncells, hv, 1));
     nunits = hv[0];
     GROW(recs, (size_t)(nunits + 1) * 16);
     /* cells <- offsets (kept for the raster), cursor <- running copy */
     CK(cudaMemcpyAsync(cells.p, cursor.p, (ncells + 1) * 4, cudaMemcpyDeviceToDevice, st));
-    CK(gb_launch_bin(st, 1, nedges, edges.as<int4>(), edge_draw.as<uint32_t>(), ntris, tri_a.as<int4>(),
+    CK(gb_launch_bin(st, 1, nedge_all, edges.as<int4>(), edge_draw.as<uint32_t>(), 0, tri_a.as<int4>(),
                      tri_b.as<int4>(), tri_draw.as<uint32_t>(), ndraw, W, S, surf->nrows, cursor.as<uint32_t>(),
                      recs.as<int4>(), nunits));
-    gb_count_launch((nedges ? 1 : 0) + (ntris ? 1 : 0));
+    gb_count_launch(nedge_all ? 1 : 0);
     if (timing)
         CK(cudaEventRecord(evs[3], st));
 

@@ -15,7 +15,9 @@
  * (+e, +e^2), which is the top-left rule).  Summed over a closed polygon this
  * is its winding number; summed over positively oriented triangles it is the
  * number of covering triangles.  Every (primitive, sample row) pair of a
- * draw's band primitives is one work item: each edge crossing is computed
+ * draw's band edges is one work item (stroke triangles arrive as their
+ * edges, with the edges neighbouring triangles share in opposite directions
+ * already cancelled): each edge crossing is computed
  * exactly (an fp32 quotient estimate corrected by one exact remainder test)
  * and its direction is added to a shared-memory counter at the last sample
  * left of the crossing, to the crossing's (row, strip) total, and the strip
@@ -429,35 +431,11 @@ __global__ void __launch_bounds__(XT_THREADS, 1) gb_raster(gb_raster_args A) {
 
             /* ---- accumulate: one item per (primitive, band row) */
             if (iok) {
-                if (kind == GB_DRAW_STROKE) {
-                    const uint32_t n = ((hi - lo) >> 1) * 16u;
-                    for (uint32_t it = t; it < n; it += XT_THREADS) {
-                        const uint32_t u = (it >> 4) * 2u;
-                        int4           ta, tb;
-                        if (u < su) {
-                            ta = sg[u];
-                            tb = sg[u + 1];
-                        } else {
-                            ta = A.recs[lo + u];
-                            tb = A.recs[lo + u + 1];
-                        }
-                        const int32_t ymn = min(min(ta.y, ta.w), tb.y), ymx = max(max(ta.y, ta.w), tb.y);
-                        if (isy < ymn || isy >= ymx)
-                            continue;
-                        const int32_t xmn = min(min(ta.x, ta.z), tb.x), xmx = max(max(ta.x, ta.z), tb.x);
-                        if (xmx < tx_lo || xmn > tx_hi)
-                            continue; /* wholly left or right: no net coverage in the tile */
-                        acc_row(ta.x, ta.y, ta.z, ta.w, isy, irr, iox, X0, TW, tx_lo, tx_hi, plane, tot, flag);
-                        acc_row(ta.z, ta.w, tb.x, tb.y, isy, irr, iox, X0, TW, tx_lo, tx_hi, plane, tot, flag);
-                        acc_row(tb.x, tb.y, ta.x, ta.y, isy, irr, iox, X0, TW, tx_lo, tx_hi, plane, tot, flag);
-                    }
-                } else {
-                    const uint32_t n = (hi - lo) * 16u;
-                    for (uint32_t it = t; it < n; it += XT_THREADS) {
-                        const uint32_t u  = it >> 4;
-                        const int4     ed = u < su ? sg[u] : A.recs[lo + u];
-                        acc_row(ed.x, ed.y, ed.z, ed.w, isy, irr, iox, X0, TW, tx_lo, tx_hi, plane, tot, flag);
-                    }
+                const uint32_t n = (hi - lo) * 16u;
+                for (uint32_t it = t; it < n; it += XT_THREADS) {
+                    const uint32_t u  = it >> 4;
+                    const int4     ed = u < su ? sg[u] : A.recs[lo + u];
+                    acc_row(ed.x, ed.y, ed.z, ed.w, isy, irr, iox, X0, TW, tx_lo, tx_hi, plane, tot, flag);
                 }
             }
             __syncthreads();

@@ -103,7 +103,8 @@ __global__ void gb_stroke_tris(uint32_t ntris, uint32_t ndraw_s, const uint32_t 
                                const uint32_t *__restrict__ sdraw_id, const uint32_t *__restrict__ draw_vbase,
                                const gb_draw *__restrict__ draws, const float2 *__restrict__ verts,
                                const uint32_t *__restrict__ inds, uint32_t W, uint32_t H, int4 *__restrict__ tri_a,
-                               int4 *__restrict__ tri_b, uint32_t *__restrict__ tri_draw) {
+                               int4 *__restrict__ tri_b, uint32_t *__restrict__ tri_draw,
+                               uint4 *__restrict__ tri_idx) {
     uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= ntris)
         return;
@@ -125,10 +126,67 @@ __global__ void gb_stroke_tris(uint32_t ntris, uint32_t ndraw_s, const uint32_t 
         int2 tmp = b;
         b        = c;
         c        = tmp;
+        uint32_t ti = i1;
+        i1          = i2;
+        i2          = ti;
     }
     tri_a[t]    = make_int4(a.x, a.y, b.x, b.y);
     tri_b[t]    = make_int4(c.x, c.y, valid, 0);
     tri_draw[t] = d;
+    tri_idx[t]  = make_uint4(i0, i1, i2, valid ? d + 1 : 0u); /* oriented vertex indices, draw + 1 if valid */
+}
+
+/* Stroke triangles as directed edges for the coverage count.  A positively
+   oriented triangle's coverage is the winding of its three edges, so a
+   stroke's covering-triangle count is the winding of all its triangles'
+   edges.  Two opposite occurrences of one edge (the same two vertices of one
+   draw, reversed) add exactly opposite crossings at every sample and are
+   dropped: the quad diagonals and the rungs between consecutive quads that
+   vkvg's vertex buffer shares between neighbouring triangles.  An edge is
+   paired only with the reversed edge of the next or previous triangle, and
+   only when the triangles two steps away cannot claim either occurrence, so
+   every occurrence has at most one partner.  Dropped and degenerate slots are
+   written as empty (horizontal) edges, which binning skips. */
+__device__ __forceinline__ bool tri_has(const uint4 &T, uint32_t a, uint32_t b) {
+    return (T.x == a && T.y == b) || (T.y == a && T.z == b) || (T.z == a && T.x == b);
+}
+__global__ void gb_stroke_edges(uint32_t ntris, const int4 *__restrict__ tri_a, const int4 *__restrict__ tri_b,
+                                const uint4 *__restrict__ tri_idx, const uint32_t *__restrict__ tri_draw,
+                                int4 *__restrict__ edges, uint32_t *__restrict__ edge_draw) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ntris)
+        return;
+    const uint4    me = tri_idx[t];
+    const uint32_t d  = tri_draw[t];
+    if (!me.w) {
+        for (int k = 0; k < 3; k++) {
+            edges[3 * t + k]     = make_int4(0, 0, 0, 0);
+            edge_draw[3 * t + k] = d;
+        }
+        return;
+    }
+    const uint4 none = make_uint4(0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0);
+    uint4       nb[4]; /* t-2, t-1, t+1, t+2, valid triangles of the same draw only */
+    for (int k = 0; k < 4; k++) {
+        const int64_t u = (int64_t)t + (k < 2 ? k - 2 : k - 1);
+        nb[k]           = none;
+        if (u >= 0 && u < (int64_t)ntris) {
+            const uint4 T = tri_idx[u];
+            if (T.w == me.w)
+                nb[k] = T;
+        }
+    }
+    const int4 ta = tri_a[t], tb = tri_b[t];
+    const int2 v[3] = {make_int2(ta.x, ta.y), make_int2(ta.z, ta.w), make_int2(tb.x, tb.y)};
+    const uint32_t ix[3] = {me.x, me.y, me.z};
+    for (int k = 0; k < 3; k++) {
+        const uint32_t a = ix[k], b = ix[(k + 1) % 3];
+        const bool     fwd = tri_has(nb[2], b, a) && !tri_has(nb[1], b, a) && !tri_has(nb[3], a, b);
+        const bool     bwd = tri_has(nb[1], b, a) && !tri_has(nb[2], b, a) && !tri_has(nb[0], a, b);
+        const int2     p = v[k], q = v[(k + 1) % 3];
+        edges[3 * t + k]     = (fwd || bwd) ? make_int4(0, 0, 0, 0) : make_int4(p.x, p.y, q.x, q.y);
+        edge_draw[3 * t + k] = d;
+    }
 }
 
 /* sample-row range [r0, r1] crossed by the half-open y interval [ylo, yhi) */
@@ -238,11 +296,12 @@ cudaError_t gb_launch_fill_edges(cudaStream_t st, uint32_t nedges, uint32_t npai
 cudaError_t gb_launch_stroke_tris(cudaStream_t st, uint32_t ntris, uint32_t ndraw_s, const uint32_t *draw_tri0,
                                   const uint32_t *sdraw_id, const uint32_t *draw_vbase, const gb_draw *draws,
                                   const float2 *verts, const uint32_t *inds, uint32_t W, uint32_t H, int4 *tri_a,
-                                  int4 *tri_b, uint32_t *tri_draw) {
+                                  int4 *tri_b, uint32_t *tri_draw, uint4 *tri_idx, int4 *edges, uint32_t *edge_draw) {
     if (!ntris)
         return cudaSuccess;
     gb_stroke_tris<<<(ntris + 255) / 256, 256, 0, st>>>(ntris, ndraw_s, draw_tri0, sdraw_id, draw_vbase, draws, verts,
-                                                         inds, W, H, tri_a, tri_b, tri_draw);
+                                                         inds, W, H, tri_a, tri_b, tri_draw, tri_idx);
+    gb_stroke_edges<<<(ntris + 255) / 256, 256, 0, st>>>(ntris, tri_a, tri_b, tri_idx, tri_draw, edges, edge_draw);
     return cudaGetLastError();
 }
 cudaError_t gb_launch_bin(cudaStream_t st, int scatter, uint32_t nedges, const int4 *edges, const uint32_t *edge_draw,

@@ -467,6 +467,54 @@ __global__ void gb_dash_seglen(uint32_t npairs, const uint32_t *__restrict__ pai
         seglen[cp]        = v_len(v_sub(pts[iR], pts[cp]));
     }
 }
+/* dash entry i of a pattern held in registers (patterns of up to 4 entries) */
+__device__ __forceinline__ float dash_at(const float (&dr)[4], uint32_t i) {
+    return i == 0 ? dr[0] : i == 1 ? dr[1] : i == 2 ? dr[2] : dr[3];
+}
+template <bool REG>
+__device__ __forceinline__ void dash_state_walk(const float *__restrict__ dashes, uint32_t dcount, float doffset,
+                                                uint32_t first, uint32_t nseg, const float *__restrict__ seglen,
+                                                uint4 *__restrict__ dseg, uint4 *__restrict__ fin_out,
+                                                uint32_t *__restrict__ count_out) {
+    float dr[4] = {0, 0, 0, 0};
+    if (REG)
+        for (uint32_t i = 0; i < dcount; i++)
+            dr[i == 0 ? 0 : i == 1 ? 1 : i == 2 ? 2 : 3] = dashes[i];
+    float tot = 0;
+    for (uint32_t i = 0; i < dcount; i++)
+        tot += dashes[i];
+    bool        dashOn  = true;
+    uint32_t    curDash = 0;
+    float       curOff  = fmodf(doffset, tot);
+    uint32_t    ne      = 0;
+    const float atot    = fabsf(tot);
+    float       sl_next = nseg ? seglen[first] : 0.f;
+    for (uint32_t j = 0; j < nseg; j++) {
+        const uint32_t cp  = first + j;
+        const float    sl  = sl_next;
+        sl_next            = j + 1 < nseg ? seglen[cp + 1] : 0.f; /* next length in flight */
+        uint4          rec = make_uint4(__float_as_uint(curOff), curDash | (dashOn ? 0x80000000u : 0u), ne, 0);
+        if (!dashOn)
+            ne++; /* the segment's join */
+        uint32_t k = 0;
+        while (curOff < sl && ne < GB_DASH_LOOP_CAP) {
+            ne++;
+            dashOn = !dashOn;
+            curOff += REG ? dash_at(dr, curDash) : dashes[curDash];
+            if (++curDash == dcount)
+                curDash = 0;
+            k++;
+        }
+        curOff -= sl;
+        if (!(fabsf(curOff) < atot)) /* fmodf(x, t) is x itself when |x| < |t| */
+            curOff = fmodf(curOff, tot);
+        rec.w    = k;
+        dseg[cp] = rec;
+    }
+    const uint32_t total = ne + (dashOn ? 0u : 1u);
+    *fin_out   = make_uint4(__float_as_uint(curOff), curDash | (dashOn ? 0x80000000u : 0u), total, 0);
+    *count_out = total;
+}
 __global__ void gb_dash_state(uint32_t npairs, const uint32_t *__restrict__ pair_draw,
                               const uint32_t *__restrict__ pair_sub, const gb_draw *__restrict__ draws,
                               const uint32_t *__restrict__ sub_pt0, const uint32_t *__restrict__ sub_npts,
@@ -480,42 +528,13 @@ __global__ void gb_dash_state(uint32_t npairs, const uint32_t *__restrict__ pair
     const uint32_t s = pair_sub[p], n = sub_npts[s];
     if (n < 2 || d.dash_count == 0)
         return;
-    const float   *dashes = dash_arr + d.dash_first;
-    const uint32_t dcount = d.dash_count;
-    float          tot    = 0;
-    for (uint32_t i = 0; i < dcount; i++)
-        tot += dashes[i];
-    bool           dashOn  = true;
-    uint32_t       curDash = 0;
-    float          curOff  = fmodf(d.dash_offset, tot);
-    uint32_t       ne      = 0;
-    const uint32_t first   = sub_pt0[s];
-    const uint32_t nseg    = n - 1 + ((sub_flags[s] & GB_SUB_CLOSED) ? 1u : 0u);
-    const float    atot    = fabsf(tot);
-    for (uint32_t j = 0; j < nseg; j++) {
-        const uint32_t cp = first + j;
-        uint4          rec = make_uint4(__float_as_uint(curOff), curDash | (dashOn ? 0x80000000u : 0u), ne, 0);
-        if (!dashOn)
-            ne++; /* the segment's join */
-        const float sl = seglen[cp];
-        uint32_t    k  = 0;
-        while (curOff < sl && ne < GB_DASH_LOOP_CAP) {
-            ne++;
-            dashOn = !dashOn;
-            curOff += dashes[curDash];
-            if (++curDash == dcount)
-                curDash = 0;
-            k++;
-        }
-        curOff -= sl;
-        if (!(fabsf(curOff) < atot)) /* fmodf(x, t) is x itself when |x| < |t| */
-            curOff = fmodf(curOff, tot);
-        rec.w    = k;
-        dseg[cp] = rec;
-    }
-    const uint32_t total = ne + (dashOn ? 0u : 1u);
-    dfin[p]   = make_uint4(__float_as_uint(curOff), curDash | (dashOn ? 0x80000000u : 0u), total, 0);
-    counts[p] = total;
+    const uint32_t nseg = n - 1 + ((sub_flags[s] & GB_SUB_CLOSED) ? 1u : 0u);
+    if (d.dash_count <= 4)
+        dash_state_walk<true>(dash_arr + d.dash_first, d.dash_count, d.dash_offset, sub_pt0[s], nseg, seglen, dseg,
+                              dfin + p, counts + p);
+    else
+        dash_state_walk<false>(dash_arr + d.dash_first, d.dash_count, d.dash_offset, sub_pt0[s], nseg, seglen, dseg,
+                               dfin + p, counts + p);
 }
 __global__ void gb_dash_emit(uint32_t npairs, const uint32_t *__restrict__ pair_draw,
                              const uint32_t *__restrict__ pair_sub, const gb_draw *__restrict__ draws,
@@ -774,7 +793,7 @@ cudaError_t gb_launch_dash_count(cudaStream_t st, uint32_t npairs, const uint32_
         return cudaSuccess;
     gb_dash_seglen<<<(npairs + 7) / 8, 256, 0, st>>>(npairs, pair_draw, pair_sub, draws, sub_pt0, sub_npts, sub_flags,
                                                       pts, seglen);
-    gb_dash_state<<<(npairs + 63) / 64, 64, 0, st>>>(npairs, pair_draw, pair_sub, draws, sub_pt0, sub_npts, sub_flags,
+    gb_dash_state<<<(npairs + 31) / 32, 32, 0, st>>>(npairs, pair_draw, pair_sub, draws, sub_pt0, sub_npts, sub_flags,
                                                       dashes, seglen, dseg, dfin, counts);
     return cudaGetLastError();
 }
