@@ -488,28 +488,37 @@ __device__ __forceinline__ void dash_state_walk(const float *__restrict__ dashes
     float       curOff  = fmodf(doffset, tot);
     uint32_t    ne      = 0;
     const float atot    = fabsf(tot);
-    float       sl_next = nseg ? seglen[first] : 0.f;
-    for (uint32_t j = 0; j < nseg; j++) {
-        const uint32_t cp  = first + j;
-        const float    sl  = sl_next;
-        sl_next            = j + 1 < nseg ? seglen[cp + 1] : 0.f; /* next length in flight */
-        uint4          rec = make_uint4(__float_as_uint(curOff), curDash | (dashOn ? 0x80000000u : 0u), ne, 0);
-        if (!dashOn)
-            ne++; /* the segment's join */
-        uint32_t k = 0;
-        while (curOff < sl && ne < GB_DASH_LOOP_CAP) {
-            ne++;
-            dashOn = !dashOn;
-            curOff += REG ? dash_at(dr, curDash) : dashes[curDash];
-            if (++curDash == dcount)
-                curDash = 0;
-            k++;
+    /* lengths are read 16 at a time so that their latency is paid once per
+       16 segments; the recurrence itself is strictly sequential */
+    for (uint32_t j0 = 0; j0 < nseg; j0 += 16) {
+        float sl16[16];
+#pragma unroll
+        for (int q = 0; q < 16; q++)
+            sl16[q] = j0 + q < nseg ? seglen[first + j0 + q] : 0.f;
+#pragma unroll
+        for (int q = 0; q < 16; q++) {
+            if (j0 + q >= nseg)
+                break;
+            const uint32_t cp  = first + j0 + q;
+            const float    sl  = sl16[q];
+            uint4          rec = make_uint4(__float_as_uint(curOff), curDash | (dashOn ? 0x80000000u : 0u), ne, 0);
+            if (!dashOn)
+                ne++; /* the segment's join */
+            uint32_t k = 0;
+            while (curOff < sl && ne < GB_DASH_LOOP_CAP) {
+                ne++;
+                dashOn = !dashOn;
+                curOff += REG ? dash_at(dr, curDash) : dashes[curDash];
+                if (++curDash == dcount)
+                    curDash = 0;
+                k++;
+            }
+            curOff -= sl;
+            if (!(fabsf(curOff) < atot)) /* fmodf(x, t) is x itself when |x| < |t| */
+                curOff = fmodf(curOff, tot);
+            rec.w    = k;
+            dseg[cp] = rec;
         }
-        curOff -= sl;
-        if (!(fabsf(curOff) < atot)) /* fmodf(x, t) is x itself when |x| < |t| */
-            curOff = fmodf(curOff, tot);
-        rec.w    = k;
-        dseg[cp] = rec;
     }
     const uint32_t total = ne + (dashOn ? 0u : 1u);
     *fin_out   = make_uint4(__float_as_uint(curOff), curDash | (dashOn ? 0x80000000u : 0u), total, 0);
