@@ -488,6 +488,7 @@ __device__ __forceinline__ void dash_state_walk(const float *__restrict__ dashes
     float       curOff  = fmodf(doffset, tot);
     uint32_t    ne      = 0;
     const float atot    = fabsf(tot);
+    float       dv      = REG ? dr[0] : dashes[0]; /* dashes[curDash] */
     /* lengths are read 16 at a time so that their latency is paid once per
        16 segments; the recurrence itself is strictly sequential */
     for (uint32_t j0 = 0; j0 < nseg; j0 += 16) {
@@ -508,9 +509,10 @@ __device__ __forceinline__ void dash_state_walk(const float *__restrict__ dashes
             while (curOff < sl && ne < GB_DASH_LOOP_CAP) {
                 ne++;
                 dashOn = !dashOn;
-                curOff += REG ? dash_at(dr, curDash) : dashes[curDash];
+                curOff += dv; /* dashes[curDash] */
                 if (++curDash == dcount)
                     curDash = 0;
+                dv = REG ? dash_at(dr, curDash) : dashes[curDash]; /* next entry, off the add chain */
                 k++;
             }
             curOff -= sl;
@@ -530,8 +532,10 @@ __global__ void gb_dash_state(uint32_t npairs, const uint32_t *__restrict__ pair
                               const uint32_t *__restrict__ sub_flags, const float *__restrict__ dash_arr,
                               const float *__restrict__ seglen, uint4 *__restrict__ dseg, uint4 *__restrict__ dfin,
                               uint32_t *__restrict__ counts) {
-    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= npairs)
+    /* one warp per pair, lane 0 walking: pairs of one warp would serialise
+       each other's divergent boundary loops */
+    const uint32_t p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (p >= npairs || (threadIdx.x & 31) != 0)
         return;
     const gb_draw &d = draws[pair_draw[p]];
     const uint32_t s = pair_sub[p], n = sub_npts[s];
@@ -802,7 +806,7 @@ cudaError_t gb_launch_dash_count(cudaStream_t st, uint32_t npairs, const uint32_
         return cudaSuccess;
     gb_dash_seglen<<<(npairs + 7) / 8, 256, 0, st>>>(npairs, pair_draw, pair_sub, draws, sub_pt0, sub_npts, sub_flags,
                                                       pts, seglen);
-    gb_dash_state<<<(npairs + 31) / 32, 32, 0, st>>>(npairs, pair_draw, pair_sub, draws, sub_pt0, sub_npts, sub_flags,
+    gb_dash_state<<<(npairs + 3) / 4, 128, 0, st>>>(npairs, pair_draw, pair_sub, draws, sub_pt0, sub_npts, sub_flags,
                                                       dashes, seglen, dseg, dfin, counts);
     return cudaGetLastError();
 }
