@@ -243,43 +243,58 @@ __device__ __forceinline__ void acc_row(int32_t x0, int32_t y0, int32_t x1, int3
     flag[p >> 6] = 1;
 }
 
-/* fills on a run with crossings (its counters at cp, slot rotation v):
-   blend where (w & fmask) != 0 (fmask 1: even-odd, ~0: non-zero) */
+/* Runs with crossings (counters at cp, slot rotation v), right to left in
+   groups of four samples; a group is skipped when no lane of the warp has a
+   sample to blend in it (about three groups in ten of a mixed warp for
+   scribble-like paths), which the vote decides for the whole warp.  Fills
+   blend where (w & fmask) != 0 (fmask 1: even-odd, ~0: non-zero). */
 template <int M>
 __device__ __forceinline__ void fill_run(uint32_t (&col)[32], const int4 *cp, uint32_t v, int32_t E, int32_t fmask,
                                          const blend_k &B) {
     int32_t w = E;
 #pragma unroll
     for (int q = 7; q >= 0; q--) {
-        const int4 x = cp[q ^ v];
-#pragma unroll
-        for (int e = 3; e >= 0; e--) {
-            const int c = 4 * q + e;
-            w += e == 3 ? x.w : e == 2 ? x.z : e == 1 ? x.y : x.x;
-            const uint32_t nb = blend<M>(col[c], B);
-            col[c]            = (w & fmask) ? nb : col[c];
+        const int4    x  = cp[q ^ v];
+        const int32_t w3 = w + x.w, w2 = w3 + x.z, w1 = w2 + x.y, w0 = w1 + x.x;
+        const bool    p3 = (w3 & fmask) != 0, p2 = (w2 & fmask) != 0, p1 = (w1 & fmask) != 0, p0 = (w0 & fmask) != 0;
+        w                = w0;
+        if (__any_sync(0xffffffffu, p0 | p1 | p2 | p3)) {
+            const uint32_t n3 = blend<M>(col[4 * q + 3], B), n2 = blend<M>(col[4 * q + 2], B);
+            const uint32_t n1 = blend<M>(col[4 * q + 1], B), n0 = blend<M>(col[4 * q], B);
+            col[4 * q + 3]    = p3 ? n3 : col[4 * q + 3];
+            col[4 * q + 2]    = p2 ? n2 : col[4 * q + 2];
+            col[4 * q + 1]    = p1 ? n1 : col[4 * q + 1];
+            col[4 * q]        = p0 ? n0 : col[4 * q];
         }
     }
 }
-/* strokes on a run with crossings: blend w times (w = covering triangles) */
+/* strokes: blend w times (w = covering triangles), one pass per blend; the
+   number of passes is the warp's largest w, so that every lane takes part in
+   every vote */
 template <int M>
 __device__ __forceinline__ void stroke_run(uint32_t (&col)[32], const int4 *cp, uint32_t v, int32_t E,
                                            const blend_k &B) {
-    int32_t kmax = 1;
-    for (int32_t rep = 0; rep < kmax; rep++) {
+    int32_t kmax = 1, kwarp = 1;
+    for (int32_t rep = 0; rep < kwarp; rep++) {
         int32_t w = E;
 #pragma unroll
         for (int q = 7; q >= 0; q--) {
-            const int4 x = cp[q ^ v];
-#pragma unroll
-            for (int e = 3; e >= 0; e--) {
-                const int c = 4 * q + e;
-                w += e == 3 ? x.w : e == 2 ? x.z : e == 1 ? x.y : x.x;
-                const uint32_t nb = blend<M>(col[c], B);
-                col[c]            = w > rep ? nb : col[c];
-                kmax              = max(kmax, w);
+            const int4    x  = cp[q ^ v];
+            const int32_t w3 = w + x.w, w2 = w3 + x.z, w1 = w2 + x.y, w0 = w1 + x.x;
+            w                = w0;
+            kmax             = max(kmax, max(max(w3, w2), max(w1, w0)));
+            const bool p3 = w3 > rep, p2 = w2 > rep, p1 = w1 > rep, p0 = w0 > rep;
+            if (__any_sync(0xffffffffu, p0 | p1 | p2 | p3)) {
+                const uint32_t n3 = blend<M>(col[4 * q + 3], B), n2 = blend<M>(col[4 * q + 2], B);
+                const uint32_t n1 = blend<M>(col[4 * q + 1], B), n0 = blend<M>(col[4 * q], B);
+                col[4 * q + 3]    = p3 ? n3 : col[4 * q + 3];
+                col[4 * q + 2]    = p2 ? n2 : col[4 * q + 2];
+                col[4 * q + 1]    = p1 ? n1 : col[4 * q + 1];
+                col[4 * q]        = p0 ? n0 : col[4 * q];
             }
         }
+        if (rep == 0)
+            kwarp = __reduce_max_sync(0xffffffffu, kmax);
     }
 }
 /* a run without crossings: blend every sample k times */
