@@ -129,6 +129,58 @@ def test_twice_dashed_bit_exact(gb, vko):
     assert np.array_equal(surf.image(), osurf.image())
 
 
+@pytest.mark.parametrize("w,h,samples", [(1300, 96, 4), (2100, 40, 4), (333, 77, 1), (17, 9, 4)])
+def test_ragged_and_wide_surfaces_bit_exact(gb, vko, w, h, samples):
+    """surfaces wider than one 1024-pixel raster tile (edges left of a tile,
+    inside it and right of it), widths that are not multiples of 16, heights
+    that end inside a band, and single-sample surfaces"""
+    r = scenes.SplitMix64(w * 7 + h)
+    ops = [("set_source_rgb", 1.0, 1.0, 1.0), ("paint",)]
+    for i in range(14):
+        ops.append(("move_to", r.rnd() * w * 1.2 - 0.1 * w, r.rnd() * h * 1.2 - 0.1 * h))
+        for _ in range(3):
+            ops.append(("curve_to",) + tuple(v for _ in range(3) for v in (r.rnd() * w * 1.2 - 0.1 * w,
+                                                                           r.rnd() * h * 1.2 - 0.1 * h)))
+        ops.append(("close_path",))
+        ops += [("set_fill_rule", i % 2), ("set_source_rgba", r.rnd(), r.rnd(), r.rnd(), 0.4 + 0.6 * r.rnd()),
+                ("fill_preserve",), ("set_line_width", 1 + 6 * r.rnd()), ("set_line_join", i % 3),
+                ("set_line_cap", i % 3), ("set_dash", [7.0, 4.0] if i % 3 == 0 else [], 0.0),
+                ("set_source_rgba", r.rnd(), r.rnd(), r.rnd(), 0.5 + 0.5 * r.rnd()), ("stroke",)]
+    sc = {"name": "ragged", "width": w, "height": h, "samples": samples, "ops": ops, "paths": 14}
+    dev, surf, ctx = pu.run_gpu(gb, sc)
+    osurf, octx = pu.run_oracle(vko, sc)
+    assert ctx.debug_counts()[5] == 0
+    errs = pu.compare_geometry(ctx, octx)
+    assert not errs, errs[:10]
+    n = int(ctx.debug_counts()[2])
+    for i in range(n):
+        if int(ctx.debug_draw(i)[0]) in (0, 1, 2):
+            g = ctx.debug_coverage(i)
+            o = octx.coverage(i, w, h, samples, mode=0)
+            assert np.array_equal(g, o), "draw %d: %d samples differ" % (i, int((g != o).sum()))
+    assert np.array_equal(surf.samples_rgba(), osurf.samples_rgba())
+    assert np.array_equal(surf.image(), osurf.image())
+
+
+def test_empty_and_degenerate_paths(gb, vko):
+    """fills and strokes of empty, single-point, zero-length and NaN paths
+    draw nothing and leave no error; a degenerate-only frame still resolves"""
+    nan = float("nan")
+    ops = [("set_source_rgb", 0.2, 0.3, 0.4), ("paint",), ("fill",), ("stroke",),
+           ("move_to", 10.0, 10.0), ("fill",), ("move_to", 10.0, 10.0), ("stroke",),
+           ("move_to", 5.0, 5.0), ("line_to", 5.0, 5.0), ("line_to", 5.0, 5.0), ("stroke",),
+           ("move_to", 5.0, 5.0), ("line_to", 5.0, 5.0), ("close_path",), ("fill",),
+           ("move_to", nan, 3.0), ("line_to", 20.0, 20.0), ("line_to", 30.0, 5.0), ("fill_preserve",), ("stroke",),
+           ("move_to", 8.0, 8.0), ("curve_to", 8.0, 8.0, 8.0, 8.0, 8.0, 8.0), ("stroke",),
+           ("set_line_width", 0.0), ("move_to", 1.0, 1.0), ("line_to", 30.0, 30.0), ("stroke",)]
+    sc = {"name": "degenerate", "width": 40, "height": 40, "samples": 4, "ops": ops, "paths": 0}
+    dev, surf, ctx = pu.run_gpu(gb, sc)
+    osurf, octx = pu.run_oracle(vko, sc)
+    assert ctx.debug_counts()[5] == 0
+    assert not pu.compare_geometry(ctx, octx)
+    assert np.array_equal(surf.image(), osurf.image())
+
+
 def test_curve_heavy_full_size_bit_exact(gb, vko):
     """The full 1024x1024, 2,048-path benchmark scene: every stroke/fill draw's
     geometry and the final 4x MSAA samples equal the oracle's."""
