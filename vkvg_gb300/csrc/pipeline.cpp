@@ -325,9 +325,8 @@ cudaError_t Pipeline::run(const FrameHost &f, _vkvg_surface_t *surf, bool timing
     GROW(cells, (ncells + 1) * 4);
     GROW(cursor, (ncells + 1) * 4);
     CK(cudaMemsetAsync(cells.p, 0, (ncells + 1) * 4, st));
-    CK(gb_launch_bin(st, 0, nedge_all, edges.as<int4>(), edge_draw.as<uint32_t>(), 0, tri_a.as<int4>(),
-                     tri_b.as<int4>(), tri_draw.as<uint32_t>(), ndraw, W, S, surf->nrows, cells.as<uint32_t>(),
-                     nullptr, 0u));
+    CK(gb_launch_bin(st, 0, nedge_all, edges.as<int4>(), edge_draw.as<uint32_t>(), ndraw, W, S, surf->nrows,
+                     cells.as<uint32_t>(), nullptr, 0u));
     gb_count_launch(nedge_all ? 1 : 0);
     CK(scan(*this, cells.as<uint32_t>(), (uint32_t)ncells, cursor.as<uint32_t>()));
     CK(readback_u32(*this, cursor.as<uint32_t>() + ncells, hv, 1));
@@ -335,9 +334,8 @@ cudaError_t Pipeline::run(const FrameHost &f, _vkvg_surface_t *surf, bool timing
     GROW(recs, (size_t)(nunits + 1) * 16);
     /* cells <- offsets (kept for the raster), cursor <- running copy */
     CK(cudaMemcpyAsync(cells.p, cursor.p, (ncells + 1) * 4, cudaMemcpyDeviceToDevice, st));
-    CK(gb_launch_bin(st, 1, nedge_all, edges.as<int4>(), edge_draw.as<uint32_t>(), 0, tri_a.as<int4>(),
-                     tri_b.as<int4>(), tri_draw.as<uint32_t>(), ndraw, W, S, surf->nrows, cursor.as<uint32_t>(),
-                     recs.as<int4>(), nunits));
+    CK(gb_launch_bin(st, 1, nedge_all, edges.as<int4>(), edge_draw.as<uint32_t>(), ndraw, W, S, surf->nrows,
+                     cursor.as<uint32_t>(), recs.as<int4>(), nunits));
     gb_count_launch(nedge_all ? 1 : 0);
     if (timing)
         CK(cudaEventRecord(evs[3], st));

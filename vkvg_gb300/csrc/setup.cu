@@ -202,9 +202,8 @@ __device__ __forceinline__ void gb_row_range(int32_t ylo, int32_t yhi, uint32_t 
 }
 
 /* band range of a primitive, or false if it can touch no sample */
-__device__ __forceinline__ bool gb_prim_bands(int32_t ylo, int32_t yhi, int32_t xmin, int32_t xmax, bool is_tri,
-                                              uint32_t W, uint32_t samples, uint32_t nrows, uint32_t *b0,
-                                              uint32_t *b1) {
+__device__ __forceinline__ bool gb_prim_bands(int32_t ylo, int32_t yhi, int32_t xmax, uint32_t samples,
+                                              uint32_t nrows, uint32_t *b0, uint32_t *b1) {
     if (yhi <= ylo)
         return false;
     int32_t r0, r1;
@@ -215,22 +214,19 @@ __device__ __forceinline__ bool gb_prim_bands(int32_t ylo, int32_t yhi, int32_t 
         r1 = (int32_t)nrows - 1;
     if (r0 > r1)
         return false;
-    /* a crossing left of every sample adds nothing; a triangle right of every
-       sample covers nothing (an edge there still adds to whole rows) */
+    /* a crossing left of every sample adds nothing (an edge right of every
+       sample still adds to whole rows) */
     if (xmax < 32)
-        return false;
-    if (is_tri && (long long)xmin > (long long)W * 256)
         return false;
     *b0 = (uint32_t)r0 / GB_BAND_ROWS;
     *b1 = (uint32_t)r1 / GB_BAND_ROWS;
     return true;
 }
 
-/* Binning: count (SCATTER false) or write (SCATTER true) each primitive's
-   record into every (band, draw) cell it touches.  Records are 16-byte units:
-   an edge is one unit (x0, y0, x1, y1), a triangle two (tri_a, tri_b), so a
-   cell is one contiguous block that the raster can stage with a single bulk
-   copy. */
+/* Binning: count (SCATTER false) or write (SCATTER true) each edge's record
+   (x0, y0, x1, y1) into every (band, draw) cell it touches, so that a cell is
+   one contiguous block of 16-byte records the raster can stage with a single
+   bulk copy. */
 template <bool SCATTER>
 __global__ void gb_bin_edges(uint32_t nedges, const int4 *__restrict__ edges, const uint32_t *__restrict__ edge_draw,
                              uint32_t ndraws, uint32_t W, uint32_t samples, uint32_t nrows,
@@ -241,7 +237,7 @@ __global__ void gb_bin_edges(uint32_t nedges, const int4 *__restrict__ edges, co
     int4     ed = edges[e];
     uint32_t b0, b1;
     int32_t  ylo = min(ed.y, ed.w), yhi = max(ed.y, ed.w);
-    if (!gb_prim_bands(ylo, yhi, min(ed.x, ed.z), max(ed.x, ed.z), false, W, samples, nrows, &b0, &b1))
+    if (!gb_prim_bands(ylo, yhi, max(ed.x, ed.z), samples, nrows, &b0, &b1))
         return;
     uint32_t d = edge_draw[e];
     for (uint32_t b = b0; b <= b1; b++) {
@@ -250,31 +246,6 @@ __global__ void gb_bin_edges(uint32_t nedges, const int4 *__restrict__ edges, co
             recs[slot] = ed;
     }
 }
-template <bool SCATTER>
-__global__ void gb_bin_tris(uint32_t ntris, const int4 *__restrict__ tri_a, const int4 *__restrict__ tri_b,
-                            const uint32_t *__restrict__ tri_draw, uint32_t ndraws, uint32_t W, uint32_t samples,
-                            uint32_t nrows, uint32_t *__restrict__ cell, int4 *__restrict__ recs, uint32_t nunits) {
-    uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= ntris)
-        return;
-    int4 a = tri_a[t], b = tri_b[t];
-    if (!b.z)
-        return;
-    int32_t  ylo = min(min(a.y, a.w), b.y), yhi = max(max(a.y, a.w), b.y);
-    int32_t  xlo = min(min(a.x, a.z), b.x), xhi = max(max(a.x, a.z), b.x);
-    uint32_t b0, b1;
-    if (!gb_prim_bands(ylo, yhi, xlo, xhi, true, W, samples, nrows, &b0, &b1))
-        return;
-    uint32_t d = tri_draw[t];
-    for (uint32_t bb = b0; bb <= b1; bb++) {
-        uint32_t slot = atomicAdd(&cell[(size_t)bb * ndraws + d], 2u);
-        if (SCATTER && slot + 1 < nunits) {
-            recs[slot]     = a;
-            recs[slot + 1] = b;
-        }
-    }
-}
-
 extern "C" {
 cudaError_t gb_launch_fill_pair_edges(cudaStream_t st, uint32_t npairs, const uint32_t *pair_sub,
                                       const uint32_t *sub_npts, uint32_t *counts) {
@@ -305,7 +276,6 @@ cudaError_t gb_launch_stroke_tris(cudaStream_t st, uint32_t ntris, uint32_t ndra
     return cudaGetLastError();
 }
 cudaError_t gb_launch_bin(cudaStream_t st, int scatter, uint32_t nedges, const int4 *edges, const uint32_t *edge_draw,
-                          uint32_t ntris, const int4 *tri_a, const int4 *tri_b, const uint32_t *tri_draw,
                           uint32_t ndraws, uint32_t W, uint32_t samples, uint32_t nrows, uint32_t *cell, int4 *recs,
                           uint32_t nunits) {
     if (nedges) {
@@ -315,14 +285,6 @@ cudaError_t gb_launch_bin(cudaStream_t st, int scatter, uint32_t nedges, const i
         else
             gb_bin_edges<false><<<(nedges + 255) / 256, 256, 0, st>>>(nedges, edges, edge_draw, ndraws, W, samples,
                                                                        nrows, cell, nullptr, 0u);
-    }
-    if (ntris) {
-        if (scatter)
-            gb_bin_tris<true><<<(ntris + 255) / 256, 256, 0, st>>>(ntris, tri_a, tri_b, tri_draw, ndraws, W, samples,
-                                                                    nrows, cell, recs, nunits);
-        else
-            gb_bin_tris<false><<<(ntris + 255) / 256, 256, 0, st>>>(ntris, tri_a, tri_b, tri_draw, ndraws, W, samples,
-                                                                     nrows, cell, nullptr, 0u);
     }
     return cudaGetLastError();
 }
