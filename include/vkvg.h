@@ -88,6 +88,26 @@ typedef struct {
 typedef struct _vkvg_context_t *VkvgContext;
 typedef struct _vkvg_surface_t *VkvgSurface;
 typedef struct _vkvg_device_t  *VkvgDevice;
+typedef struct _vkvg_pattern_t *VkvgPattern; /* include/vkvg.h:323-329 */
+
+/* include/vkvg.h:156-189 (values identical) */
+typedef enum { VKVG_EXTEND_NONE, VKVG_EXTEND_REPEAT, VKVG_EXTEND_REFLECT, VKVG_EXTEND_PAD } vkvg_extend_t;
+typedef enum {
+    VKVG_FILTER_FAST,
+    VKVG_FILTER_GOOD,
+    VKVG_FILTER_BEST,
+    VKVG_FILTER_NEAREST,
+    VKVG_FILTER_BILINEAR,
+    VKVG_FILTER_GAUSSIAN,
+} vkvg_filter_t;
+typedef enum {
+    VKVG_PATTERN_TYPE_SOLID,
+    VKVG_PATTERN_TYPE_SURFACE,
+    VKVG_PATTERN_TYPE_LINEAR,
+    VKVG_PATTERN_TYPE_RADIAL,
+    VKVG_PATTERN_TYPE_MESH,
+    VKVG_PATTERN_TYPE_RASTER_SOURCE,
+} vkvg_pattern_type_t;
 
 /* matrices: include/vkvg.h:377-514 (cairo semantics) */
 typedef struct {
@@ -200,6 +220,10 @@ vkvg_public float            vkvg_get_opacity(VkvgContext ctx);
 vkvg_public void             vkvg_set_source_color(VkvgContext ctx, uint32_t c);
 vkvg_public void             vkvg_set_source_rgba(VkvgContext ctx, float r, float g, float b, float a);
 vkvg_public void             vkvg_set_source_rgb(VkvgContext ctx, float r, float g, float b);
+/* include/vkvg.h:1388-1394, 1531-1536: a pattern as the source (linear
+   gradients; other pattern types are outside the path hot path) */
+vkvg_public void        vkvg_set_source(VkvgContext ctx, VkvgPattern pat);
+vkvg_public VkvgPattern vkvg_get_source(VkvgContext ctx);
 vkvg_public void             vkvg_set_line_width(VkvgContext ctx, float width);
 vkvg_public void             vkvg_set_miter_limit(VkvgContext ctx, float limit);
 vkvg_public float            vkvg_get_miter_limit(VkvgContext ctx);
@@ -223,6 +247,30 @@ vkvg_public void vkvg_rotate(VkvgContext ctx, float radians);
 vkvg_public void vkvg_transform(VkvgContext ctx, const vkvg_matrix_t *matrix);
 vkvg_public void vkvg_set_matrix(VkvgContext ctx, const vkvg_matrix_t *matrix);
 vkvg_public void vkvg_get_matrix(VkvgContext ctx, vkvg_matrix_t *const matrix);
+
+/* patterns: include/vkvg.h:1749-1900 for linear gradients (up to 16 colour
+   stops; stops beyond that return VKVG_STATUS_INVALID_INDEX where vkvg would
+   write past its array) */
+vkvg_public vkvg_status_t       vkvg_pattern_status(VkvgPattern pat);
+vkvg_public VkvgPattern         vkvg_pattern_reference(VkvgPattern pat);
+vkvg_public uint32_t            vkvg_pattern_get_reference_count(VkvgPattern pat);
+vkvg_public void                vkvg_pattern_destroy(VkvgPattern pat);
+vkvg_public VkvgPattern         vkvg_pattern_create_linear(float x0, float y0, float x1, float y1);
+vkvg_public vkvg_status_t       vkvg_pattern_edit_linear(VkvgPattern pat, float x0, float y0, float x1, float y1);
+vkvg_public vkvg_status_t       vkvg_pattern_get_linear_points(VkvgPattern pat, float *x0, float *y0, float *x1,
+                                                               float *y1);
+vkvg_public vkvg_status_t       vkvg_pattern_add_color_stop(VkvgPattern pat, float offset, float r, float g, float b,
+                                                            float a);
+vkvg_public vkvg_status_t       vkvg_pattern_get_color_stop_count(VkvgPattern pat, uint32_t *count);
+vkvg_public vkvg_status_t       vkvg_pattern_get_color_stop_rgba(VkvgPattern pat, uint32_t index, float *offset,
+                                                                 float *r, float *g, float *b, float *a);
+vkvg_public void                vkvg_pattern_set_extend(VkvgPattern pat, vkvg_extend_t extend);
+vkvg_public vkvg_extend_t       vkvg_pattern_get_extend(VkvgPattern pat);
+vkvg_public void                vkvg_pattern_set_filter(VkvgPattern pat, vkvg_filter_t filter);
+vkvg_public vkvg_filter_t       vkvg_pattern_get_filter(VkvgPattern pat);
+vkvg_public vkvg_pattern_type_t vkvg_pattern_get_type(VkvgPattern pat);
+vkvg_public void                vkvg_pattern_set_matrix(VkvgPattern pat, const vkvg_matrix_t *matrix);
+vkvg_public void                vkvg_pattern_get_matrix(VkvgPattern pat, vkvg_matrix_t *matrix);
 vkvg_public void vkvg_identity_matrix(VkvgContext ctx);
 
 #ifdef __cplusplus

@@ -34,6 +34,7 @@ extern "C" {
 
 typedef struct vko_surface_t vko_surface;
 typedef struct vko_context_t vko_context;
+typedef struct vko_pattern_t vko_pattern;
 
 typedef struct {
     float xx, yx, xy, yy, x0, y0;
@@ -136,6 +137,17 @@ VKO_API void vko_rel_elliptic_arc_to(vko_context *ctx, float x2, float y2, bool 
 VKO_API void vko_ellipse(vko_context *ctx, float rx, float ry, float x, float y, float rot);
 VKO_API int  vko_rectangle(vko_context *ctx, float x, float y, float w, float h);
 VKO_API int  vko_rounded_rectangle(vko_context *ctx, float x, float y, float w, float h, float radius);
+/* patterns (linear gradients), src/vkvg_pattern.c */
+VKO_API vko_pattern *vko_pattern_create_linear(float x0, float y0, float x1, float y1);
+VKO_API int          vko_pattern_status(vko_pattern *pat);
+VKO_API vko_pattern *vko_pattern_reference(vko_pattern *pat);
+VKO_API uint32_t     vko_pattern_get_reference_count(vko_pattern *pat);
+VKO_API void         vko_pattern_destroy(vko_pattern *pat);
+VKO_API int          vko_pattern_edit_linear(vko_pattern *pat, float x0, float y0, float x1, float y1);
+VKO_API int          vko_pattern_add_color_stop(vko_pattern *pat, float offset, float r, float g, float b, float a);
+VKO_API int          vko_pattern_get_color_stop_count(vko_pattern *pat, uint32_t *count);
+VKO_API void         vko_pattern_set_matrix(vko_pattern *pat, const vko_matrix *m);
+VKO_API void         vko_set_source(vko_context *ctx, vko_pattern *pat);
 VKO_API bool vko_has_current_point(vko_context *ctx);
 VKO_API void vko_get_current_point(vko_context *ctx, float *x, float *y);
 VKO_API void vko_path_extents(vko_context *ctx, float *x1, float *y1, float *x2, float *y2);

@@ -229,6 +229,8 @@ void vko_destroy(vko_context *ctx) {
     if (!ctx)
         return;
     vko_flush(ctx);
+    if (ctx->pattern)
+        vko_pattern_destroy(ctx->pattern);
     vko_surface *s = ctx->surf;
     vko_ctx_free_geom(ctx);
     free(ctx);
@@ -250,19 +252,131 @@ static uint32_t create_rgbaf(float r, float g, float b, float a) {
     return (clamp_byte(a * 255.0f) << 24) | (clamp_byte(b * a * 255.0f) << 16) | (clamp_byte(g * a * 255.0f) << 8) |
            clamp_byte(r * a * 255.0f);
 }
+/* ---------------------------------------------------------------- patterns */
+/* src/vkvg_pattern.c (linear gradients) */
+static vko_pattern s_pattern_no_memory = {VKO_STATUS_NO_MEMORY};
+vko_pattern *vko_pattern_create_linear(float x0, float y0, float x1, float y1) {
+    vko_pattern *p = (vko_pattern *)calloc(1, sizeof(vko_pattern));
+    if (!p)
+        return &s_pattern_no_memory;
+    p->refs = 1;
+    p->type = 2; /* VKVG_PATTERN_TYPE_LINEAR */
+    p->cp[0] = x0;
+    p->cp[1] = y0;
+    p->cp[2] = x1;
+    p->cp[3] = y1;
+    vko_matrix_init_identity(&p->matrix);
+    return p;
+}
+int vko_pattern_status(vko_pattern *pat) { return pat ? pat->status : VKO_STATUS_NULL_POINTER; }
+vko_pattern *vko_pattern_reference(vko_pattern *pat) {
+    if (!vko_pattern_status(pat))
+        pat->refs++;
+    return pat;
+}
+uint32_t vko_pattern_get_reference_count(vko_pattern *pat) { return vko_pattern_status(pat) ? 0 : pat->refs; }
+void     vko_pattern_destroy(vko_pattern *pat) {
+    if (vko_pattern_status(pat))
+        return;
+    if (--pat->refs > 0)
+        return;
+    free(pat);
+}
+int vko_pattern_edit_linear(vko_pattern *pat, float x0, float y0, float x1, float y1) {
+    if (vko_pattern_status(pat))
+        return vko_pattern_status(pat);
+    pat->cp[0] = x0;
+    pat->cp[1] = y0;
+    pat->cp[2] = x1;
+    pat->cp[3] = y1;
+    return VKO_STATUS_SUCCESS;
+}
+/* vkvg_pattern_add_color_stop, src/vkvg_pattern.c:149-168: premultiplied
+   stop colour; vkvg writes past its 16-entry array, the oracle refuses */
+int vko_pattern_add_color_stop(vko_pattern *pat, float offset, float r, float g, float b, float a) {
+    if (vko_pattern_status(pat))
+        return vko_pattern_status(pat);
+    if (pat->count >= VKO_GRAD_STOPS)
+        return VKO_STATUS_INVALID_INDEX;
+    float *c                 = pat->colors + 4 * pat->count;
+    c[0]                     = a * r;
+    c[1]                     = a * g;
+    c[2]                     = a * b;
+    c[3]                     = a;
+    pat->stops[pat->count++] = offset;
+    return VKO_STATUS_SUCCESS;
+}
+int vko_pattern_get_color_stop_count(vko_pattern *pat, uint32_t *count) {
+    if (vko_pattern_status(pat))
+        return vko_pattern_status(pat);
+    *count = pat->count;
+    return VKO_STATUS_SUCCESS;
+}
+void vko_pattern_set_matrix(vko_pattern *pat, const vko_matrix *m) {
+    if (vko_pattern_status(pat) || !m)
+        return;
+    pat->matrix     = *m;
+    pat->has_matrix = 1;
+}
+static void set_solid(vko_context *ctx) {
+    if (ctx->pattern)
+        vko_pattern_destroy(ctx->pattern);
+    ctx->pattern = NULL;
+    ctx->grad_on = 0;
+}
+/* vkvg_set_source + _update_cur_pattern (src/vkvg_context.c:1034-1040,
+   src/vkvg_context_internal.c:774-826): the gradient as of now, control
+   points through the inverse pattern matrix (identity if singular) and the
+   CTM, with the target surface's size */
+void vko_set_source(vko_context *ctx, vko_pattern *pat) {
+    if (vko_status(ctx) || vko_pattern_status(pat))
+        return;
+    vko_pattern_reference(pat);
+    set_solid(ctx);
+    ctx->pattern = pat;
+    if (pat->count < 2) {
+        ctx->status = VKO_STATUS_PATTERN_INVALID_GRADIENT;
+        return;
+    }
+    vko_grad *g = &ctx->grad_snap;
+    memset(g, 0, sizeof(*g));
+    float x0 = pat->cp[0], y0 = pat->cp[1], x1 = pat->cp[2], y1 = pat->cp[3];
+    if (pat->has_matrix) {
+        vko_matrix m = pat->matrix;
+        if (vko_matrix_invert(&m) != VKO_STATUS_SUCCESS)
+            vko_matrix_init_identity(&m);
+        vko_matrix_transform_point(&m, &x0, &y0);
+        vko_matrix_transform_point(&m, &x1, &y1);
+    }
+    vko_matrix_transform_point(&ctx->mat, &x0, &y0);
+    vko_matrix_transform_point(&ctx->mat, &x1, &y1);
+    g->cp[0] = x0;
+    g->cp[1] = y0;
+    g->cp[2] = x1;
+    g->cp[3] = y1;
+    g->w     = (float)ctx->surf->width;
+    g->h     = (float)ctx->surf->height;
+    g->count = pat->count;
+    memcpy(g->stops, pat->stops, sizeof(g->stops));
+    memcpy(g->colors, pat->colors, sizeof(g->colors));
+    ctx->grad_on = 1;
+}
 void vko_set_source_rgba(vko_context *ctx, float r, float g, float b, float a) {
     if (vko_status(ctx))
         return;
+    set_solid(ctx);
     ctx->cur_color = create_rgbaf(r, g, b, a);
 }
 void vko_set_source_rgb(vko_context *ctx, float r, float g, float b) {
     if (vko_status(ctx))
         return;
+    set_solid(ctx);
     ctx->cur_color = create_rgbaf(r, g, b, 1);
 }
 void vko_set_source_color(vko_context *ctx, uint32_t c) {
     if (vko_status(ctx))
         return;
+    set_solid(ctx);
     ctx->cur_color = c;
 }
 uint32_t vko_get_color(vko_context *ctx) { return ctx ? ctx->cur_color : 0; }

@@ -1067,6 +1067,11 @@ static vko_draw *new_draw(vko_context *ctx, int kind) {
     d->color   = ctx->cur_color;
     d->opacity = ctx->opacity;
     d->mat     = ctx->mat;
+    if (ctx->grad_on) {
+        d->grad      = 1;
+        d->g         = ctx->grad_snap;
+        d->g.opacity = ctx->opacity;
+    }
     return d;
 }
 

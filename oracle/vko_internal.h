@@ -30,11 +30,39 @@ typedef struct {
     float x, y;
 } v2;
 
+/* a linear gradient as vkvg's fragment stage sees it (shaders/vkvg_main.frag
+   LINEAR, data of _update_cur_pattern): control points in pixels after the
+   inverse pattern matrix and the CTM of vkvg_set_source time, surface size,
+   stops, premultiplied stop colours, the draw's opacity */
+#define VKO_GRAD_STOPS 16
+typedef struct {
+    float    cp[4];
+    float    w, h;
+    uint32_t count;
+    float    opacity;
+    float    stops[VKO_GRAD_STOPS];
+    float    colors[VKO_GRAD_STOPS * 4];
+} vko_grad;
+
+struct vko_pattern_t {
+    int        status;
+    uint32_t   refs;
+    int        type, extend, filter;
+    float      cp[4];
+    uint32_t   count;
+    float      stops[VKO_GRAD_STOPS];
+    float      colors[VKO_GRAD_STOPS * 4];
+    vko_matrix matrix;
+    int        has_matrix;
+};
+
 typedef struct {
     int      kind;
     int      op;
     uint32_t color;
     float    opacity;
+    int      grad; /* the source is the gradient g */
+    vko_grad g;
     vko_matrix mat;
     /* fills */
     uint32_t npts;
@@ -77,6 +105,9 @@ struct vko_context_t {
     uint32_t cur_color;
     float    opacity;
     vko_matrix mat;
+    vko_pattern *pattern;
+    int          grad_on;
+    vko_grad     grad_snap;
 
     /* stroke vertex / index emission buffers */
     v2      *verts;

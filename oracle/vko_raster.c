@@ -398,6 +398,61 @@ static void src_color(const vko_draw *d, uint8_t s[4]) {
         s[c] = (uint8_t)lrintf(v);
     }
 }
+/* Linear gradient source of pixel (px, py), shaders/vkvg_main.frag:83-108:
+   positions normalised by the surface size, signed distance along the
+   gradient axis in units of its length, stop colours combined by GLSL's mix
+   and smoothstep, times opacity, quantised to UNORM8 by round-to-nearest.
+   Plain fp32 operations in the shader's order (no contraction). */
+static float g_smoothstep(float e0, float e1, float x) {
+    float t = (x - e0) / (e1 - e0);
+    t       = fminf(fmaxf(t, 0.0f), 1.0f);
+    return (t * t) * (3.0f - 2.0f * t);
+}
+static float g_mix(float x, float y, float a) { return x * (1.0f - a) + y * a; }
+static void  grad_src(const vko_grad *g, uint32_t px, uint32_t py, uint8_t s[4]) {
+    float p_x = ((float)px + 0.5f) / g->w, p_y = ((float)py + 0.5f) / g->h;
+    float p0x = g->cp[0] / g->w, p0y = g->cp[1] / g->h;
+    float p1x = g->cp[2] / g->w, p1y = g->cp[3] / g->h;
+    float dx = p1x - p0x, dy = p1y - p0y;
+    float l  = sqrtf(dx * dx + dy * dy);
+    float ux = dx / l, uy = dy / l;
+    float dist;
+    if (uy == 0.0f) {
+        float t = (p_x - p0x) / l;
+        dist    = ux < 0.0f ? -t : t;
+    } else {
+        float m  = -ux / uy;
+        float bb = p0y - m * p0x;
+        dist     = ((p_y - m * p_x - bb) / sqrtf(1.0f + m * m)) / l;
+        if (uy < 0.0f)
+            dist = -dist;
+    }
+    float c[4];
+    float t0 = g_smoothstep(g->stops[0], g->stops[1], dist);
+    for (int k = 0; k < 4; k++)
+        c[k] = g_mix(g->colors[k], g->colors[4 + k], t0);
+    for (uint32_t i = 1; i + 1 < g->count; i++) {
+        float t = g_smoothstep(g->stops[i], g->stops[i + 1], dist);
+        for (int k = 0; k < 4; k++)
+            c[k] = g_mix(c[k], g->colors[4 * (i + 1) + k], t);
+    }
+    for (int k = 0; k < 4; k++) {
+        float v = (c[k] * g->opacity) * 255.0f;
+        v       = v > 0.0f ? fminf(v, 255.0f) : 0.0f;
+        s[k]    = (uint8_t)lrintf(v);
+    }
+}
+/* the source of a draw at pixel (px, py): its solid colour or its gradient */
+static inline void draw_src(const vko_draw *d, const uint8_t solid[4], uint32_t px, uint32_t py, uint8_t s[4]) {
+    if (d->grad) {
+        grad_src(&d->g, px, py, s);
+    } else {
+        s[0] = solid[0];
+        s[1] = solid[1];
+        s[2] = solid[2];
+        s[3] = solid[3];
+    }
+}
 static inline void blend(uint8_t *dst, const uint8_t s[4], int op) {
     if (op == VKO_OP_CLEAR) {
         dst[0] = dst[1] = dst[2] = dst[3] = 0;
@@ -448,8 +503,12 @@ static void apply_rows(const job_t *j) {
                 k = wv != 0;
             else
                 k = wv;
-            for (int t = 0; t < k; t++)
-                blend(dst, j->src, op);
+            if (k > 0) {
+                uint8_t sc[4];
+                draw_src(j->d, j->src, (uint32_t)px, py, sc);
+                for (int t = 0; t < k; t++)
+                    blend(dst, sc, op);
+            }
             acc += c[px];
         }
     }
@@ -472,8 +531,11 @@ void vko_raster_draw(vko_surface *surf, const vko_draw *d) {
         return;
     }
     if (d->kind == VKO_DRAW_PAINT) {
-        for (size_t i = 0; i < ns; i++)
-            blend(surf->data + i * 4, src, d->op);
+        for (size_t i = 0; i < ns; i++) {
+            uint8_t sc[4];
+            draw_src(d, src, (uint32_t)((i / S) % w), (uint32_t)(i / S / w), sc);
+            blend(surf->data + i * 4, sc, d->op);
+        }
         return;
     }
     if (vko_raster_mode_g == 1) {
@@ -513,7 +575,9 @@ void vko_raster_draw(vko_surface *surf, const vko_draw *d) {
                     for (uint32_t s = 0; s < S; s++) {
                         size_t i = ((size_t)py * w + (size_t)px) * S + s;
                         if (surf->stencil[i] & 1) {
-                            blend(surf->data + i * 4, src, d->op);
+                            uint8_t sc[4];
+                            draw_src(d, src, (uint32_t)px, (uint32_t)py, sc);
+                            blend(surf->data + i * 4, sc, d->op);
                             surf->stencil[i] &= (uint8_t)~1u;
                         }
                     }
@@ -523,8 +587,12 @@ void vko_raster_draw(vko_surface *surf, const vko_draw *d) {
         vko_draw_coverage_impl(surf, d, 1, cov);
         for (size_t i = 0; i < ns; i++) {
             int k = d->kind == VKO_DRAW_FILL_NZ ? (cov[i] != 0) : cov[i];
-            for (int t = 0; t < k; t++)
-                blend(surf->data + i * 4, src, d->op);
+            if (k > 0) {
+                uint8_t sc[4];
+                draw_src(d, src, (uint32_t)((i / S) % w), (uint32_t)(i / S / w), sc);
+                for (int t = 0; t < k; t++)
+                    blend(surf->data + i * 4, sc, d->op);
+            }
         }
         free(cov);
         return;

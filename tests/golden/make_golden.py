@@ -30,7 +30,8 @@ from vkvg_gb300 import scenes  # noqa: E402
 def golden_scenes():
     return [scenes.plain_small(n_polys=12, size=96, seed=0),
             scenes.curve_heavy(n_paths=10, size=128, seed=1, n_min=3, n_max=6),
-            scenes.api_mix(n_items=24, size=160, seed=5)]
+            scenes.api_mix(n_items=24, size=160, seed=5),
+            scenes.gradient_mix(n_items=14, size=144, seed=9)]
 
 
 def _cat(parts, dtype, width):

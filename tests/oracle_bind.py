@@ -71,6 +71,16 @@ _SIGS = {
     "vko_set_source_rgba": (None, [_P, _F, _F, _F, _F]),
     "vko_set_source_rgb": (None, [_P, _F, _F, _F]),
     "vko_set_source_color": (None, [_P, _U]),
+    "vko_pattern_create_linear": (_P, [_F, _F, _F, _F]),
+    "vko_pattern_status": (C.c_int, [_P]),
+    "vko_pattern_reference": (_P, [_P]),
+    "vko_pattern_get_reference_count": (_U, [_P]),
+    "vko_pattern_destroy": (None, [_P]),
+    "vko_pattern_edit_linear": (C.c_int, [_P, _F, _F, _F, _F]),
+    "vko_pattern_add_color_stop": (C.c_int, [_P, _F, _F, _F, _F, _F]),
+    "vko_pattern_get_color_stop_count": (C.c_int, [_P, _P]),
+    "vko_pattern_set_matrix": (None, [_P, _P]),
+    "vko_set_source": (None, [_P, _P]),
     "vko_set_line_width": (None, [_P, _F]),
     "vko_set_miter_limit": (None, [_P, _F]),
     "vko_set_line_cap": (None, [_P, C.c_int]),
@@ -147,6 +157,17 @@ class OracleContext:
     def set_matrix(self, m):
         mm = Matrix(*m)
         self.L.vko_set_matrix(self.h, C.byref(mm))
+
+    def set_source_linear(self, x0, y0, x1, y1, stops, pmat=None):
+        """a linear gradient pattern as the source (created, used, released)"""
+        p = self.L.vko_pattern_create_linear(x0, y0, x1, y1)
+        for st in stops:
+            self.L.vko_pattern_add_color_stop(p, *st)
+        if pmat is not None:
+            mm = Matrix(*pmat)
+            self.L.vko_pattern_set_matrix(p, C.byref(mm))
+        self.L.vko_set_source(self.h, p)
+        self.L.vko_pattern_destroy(p)
 
     def current_point(self):
         x, y = C.c_float(), C.c_float()

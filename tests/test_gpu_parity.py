@@ -181,6 +181,19 @@ def test_empty_and_degenerate_paths(gb, vko):
     assert np.array_equal(surf.image(), osurf.image())
 
 
+@pytest.mark.parametrize("samples", [4, 1])
+def test_gradient_sources_bit_exact(gb, vko, samples):
+    """linear gradient sources (more distinct gradients than one frame holds,
+    so the recording is flushed in between): samples and image equal the
+    oracle's"""
+    sc = scenes.gradient_mix(n_items=14, size=144, seed=9, samples=samples)
+    dev, surf, ctx = pu.run_gpu(gb, sc)
+    osurf, octx = pu.run_oracle(vko, sc)
+    assert ctx.debug_counts()[5] == 0
+    assert np.array_equal(surf.samples_rgba(), osurf.samples_rgba())
+    assert np.array_equal(surf.image(), osurf.image())
+
+
 def test_curve_heavy_full_size_bit_exact(gb, vko):
     """The full 1024x1024, 2,048-path benchmark scene: every stroke/fill draw's
     geometry and the final 4x MSAA samples equal the oracle's."""

@@ -128,7 +128,8 @@ def test_context_current_point_kat():
 def small_scenes():
     return [scenes.plain_small(n_polys=12, size=96, seed=0),
             scenes.curve_heavy(n_paths=10, size=128, seed=1, n_min=3, n_max=6),
-            scenes.api_mix(n_items=24, size=160, seed=5)]
+            scenes.api_mix(n_items=24, size=160, seed=5),
+            scenes.gradient_mix(n_items=14, size=144, seed=9)]
 
 
 @pytest.mark.parametrize("sc", small_scenes(), ids=lambda s: s["name"])
@@ -228,3 +229,89 @@ def test_portable_math_vs_libm():
     diff = np.abs(a - b)
     assert (diff <= 1).mean() >= 0.999, (diff > 1).mean()
     assert diff.max() <= 2 or (diff > 2).mean() < 1e-3
+
+
+def _np_smoothstep(e0, e1, x):
+    f = np.float32
+    t = (x - f(e0)) / (f(e1) - f(e0))
+    t = np.minimum(np.maximum(t, f(0)), f(1))
+    return (t * t) * (f(3) - f(2) * t)
+
+
+def _np_mix(x, y, a):
+    f = np.float32
+    return x * (f(1) - a) + y * a
+
+
+def test_linear_gradient_kat():
+    """a gradient painted on a cleared surface equals an independent numpy
+    fp32 evaluation of vkvg's LINEAR fragment expression
+    (shaders/vkvg_main.frag:83-108): horizontal and diagonal axes, three stops"""
+    f = np.float32
+    W, H = 64, 24
+    for (x0, y0, x1, y1) in ((8.0, 0.0, 56.0, 0.0), (60.0, 2.0, 4.0, 20.0)):
+        stops = [(0.0, 1.0, 0.0, 0.0, 1.0), (0.4, 0.0, 1.0, 0.0, 0.5), (1.0, 0.0, 0.0, 1.0, 1.0)]
+        surf = ob.OracleSurface(W, H, 4)
+        ctx = surf.context()
+        ctx.set_source_linear(x0, y0, x1, y1, stops)
+        ctx.paint()
+        ctx.flush()
+        got = surf.premult()
+        ctx.destroy()
+        surf.destroy()
+        px = np.arange(W, dtype=f)[None, :].repeat(H, 0)
+        py = np.arange(H, dtype=f)[:, None].repeat(W, 1)
+        p_x, p_y = (px + f(0.5)) / f(W), (py + f(0.5)) / f(H)
+        p0x, p0y, p1x, p1y = f(x0) / f(W), f(y0) / f(H), f(x1) / f(W), f(y1) / f(H)
+        dx, dy = p1x - p0x, p1y - p0y
+        l = np.sqrt(dx * dx + dy * dy)
+        ux, uy = dx / l, dy / l
+        if uy == 0:
+            dist = (p_x - p0x) / l
+            dist = -dist if ux < 0 else dist
+        else:
+            m = -ux / uy
+            bb = p0y - m * p0x
+            dist = ((p_y - m * p_x - bb) / np.sqrt(f(1) + m * m)) / l
+            dist = -dist if uy < 0 else dist
+        cols = [np.array([a * r, a * g, a * b, a], f) for (_, r, g, b, a) in stops]
+        t = _np_smoothstep(stops[0][0], stops[1][0], dist)
+        c = [_np_mix(cols[0][k], cols[1][k], t) for k in range(4)]
+        for i in range(1, len(stops) - 1):
+            t = _np_smoothstep(stops[i][0], stops[i + 1][0], dist)
+            c = [_np_mix(c[k], cols[i + 1][k], t) for k in range(4)]
+        want = np.stack([np.rint(np.clip(ck * f(255), 0, 255)).astype(np.uint8) for ck in c], -1)
+        assert np.array_equal(got, want)
+
+
+def test_pattern_api_semantics():
+    """vkvg's pattern object behaviour (src/vkvg_pattern.c) on both libraries:
+    reference counts, stop count, type and the 16-stop limit"""
+    import vkvg_gb300
+
+    vkvg_gb300._build.build()
+    for L, pre in ((ob.lib(), "vko_"), (vkvg_gb300.lib(), "vkvg_")):
+        f = lambda n: getattr(L, pre + n)
+        p = f("pattern_create_linear")(0.0, 0.0, 10.0, 0.0)
+        assert f("pattern_status")(p) == 0
+        assert f("pattern_get_reference_count")(p) == 1
+        f("pattern_reference")(p)
+        assert f("pattern_get_reference_count")(p) == 2
+        for i in range(16):
+            assert f("pattern_add_color_stop")(p, i / 15.0, 1.0, 0.5, 0.25, 0.5) == 0
+        assert f("pattern_add_color_stop")(p, 1.0, 1.0, 1.0, 1.0, 1.0) == 7  # VKVG_STATUS_INVALID_INDEX
+        n = C.c_uint32()
+        assert f("pattern_get_color_stop_count")(p, C.byref(n)) == 0 and n.value == 16
+        f("pattern_destroy")(p)
+        assert f("pattern_get_reference_count")(p) == 1
+        f("pattern_destroy")(p)
+    L = vkvg_gb300.lib()
+    p = L.vkvg_pattern_create_linear(0.0, 0.0, 1.0, 1.0)
+    assert L.vkvg_pattern_get_type(p) == 2  # VKVG_PATTERN_TYPE_LINEAR
+    L.vkvg_pattern_add_color_stop(p, 0.0, 1.0, 0.5, 0.25, 0.5)
+    o, r, g, b, a = (C.c_float() for _ in range(5))
+    assert L.vkvg_pattern_get_color_stop_rgba(p, 0, C.byref(o), C.byref(r), C.byref(g), C.byref(b), C.byref(a)) == 0
+    assert (r.value, g.value, b.value, a.value) == (0.5, 0.25, 0.125, 0.5)  # premultiplied, as vkvg stores them
+    assert L.vkvg_pattern_get_color_stop_rgba(p, 1, C.byref(o), C.byref(r), C.byref(g), C.byref(b),
+                                              C.byref(a)) == 7
+    L.vkvg_pattern_destroy(p)

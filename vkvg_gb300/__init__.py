@@ -94,6 +94,25 @@ SIGNATURES = {
     "vkvg_set_source_color": (None, [_P, _U]),
     "vkvg_set_source_rgba": (None, [_P, _F, _F, _F, _F]),
     "vkvg_set_source_rgb": (None, [_P, _F, _F, _F]),
+    "vkvg_set_source": (None, [_P, _P]),
+    "vkvg_get_source": (_P, [_P]),
+    "vkvg_pattern_status": (_I, [_P]),
+    "vkvg_pattern_reference": (_P, [_P]),
+    "vkvg_pattern_get_reference_count": (_U, [_P]),
+    "vkvg_pattern_destroy": (None, [_P]),
+    "vkvg_pattern_create_linear": (_P, [_F, _F, _F, _F]),
+    "vkvg_pattern_edit_linear": (_I, [_P, _F, _F, _F, _F]),
+    "vkvg_pattern_get_linear_points": (_I, [_P, _P, _P, _P, _P]),
+    "vkvg_pattern_add_color_stop": (_I, [_P, _F, _F, _F, _F, _F]),
+    "vkvg_pattern_get_color_stop_count": (_I, [_P, _P]),
+    "vkvg_pattern_get_color_stop_rgba": (_I, [_P, _U, _P, _P, _P, _P, _P]),
+    "vkvg_pattern_set_extend": (None, [_P, _I]),
+    "vkvg_pattern_get_extend": (_I, [_P]),
+    "vkvg_pattern_set_filter": (None, [_P, _I]),
+    "vkvg_pattern_get_filter": (_I, [_P]),
+    "vkvg_pattern_get_type": (_I, [_P]),
+    "vkvg_pattern_set_matrix": (None, [_P, _P]),
+    "vkvg_pattern_get_matrix": (None, [_P, _P]),
     "vkvg_set_line_width": (None, [_P, _F]),
     "vkvg_set_miter_limit": (None, [_P, _F]),
     "vkvg_get_miter_limit": (_F, [_P]),
@@ -251,6 +270,17 @@ class Context:
     def set_matrix(self, m):
         mm = Matrix(*m)
         self.L.vkvg_set_matrix(self.h, C.byref(mm))
+
+    def set_source_linear(self, x0, y0, x1, y1, stops, pmat=None):
+        """a linear gradient pattern as the source (created, used, released)"""
+        p = self.L.vkvg_pattern_create_linear(x0, y0, x1, y1)
+        for st in stops:
+            self.L.vkvg_pattern_add_color_stop(p, *st)
+        if pmat is not None:
+            mm = Matrix(*pmat)
+            self.L.vkvg_pattern_set_matrix(p, C.byref(mm))
+        self.L.vkvg_set_source(self.h, p)
+        self.L.vkvg_pattern_destroy(p)
 
     def current_point(self):
         x, y = C.c_float(), C.c_float()

@@ -739,9 +739,27 @@ uint32_t gb_source_word(uint32_t color, float opacity) {
     return out;
 }
 
+static void flush_i(VkvgContext ctx);
+/* the frame's source image for the context's gradient at the current
+   opacity, added if new; a frame holding GB_MAX_GRAD_SOURCES of them is
+   flushed first (the current path carries over) */
+static uint32_t grad_source(VkvgContext ctx) {
+    gb_grad g = ctx->grad_snap;
+    g.opacity = ctx->opacity;
+    std::vector<gb_grad> &v = ctx->frame.grads;
+    for (size_t i = 0; i < v.size(); i++)
+        if (memcmp(&v[i], &g, sizeof(g)) == 0)
+            return (uint32_t)i + 1;
+    if (v.size() >= GB_MAX_GRAD_SOURCES)
+        flush_i(ctx);
+    ctx->frame.grads.push_back(g);
+    return (uint32_t)ctx->frame.grads.size();
+}
 static gb_draw make_draw(VkvgContext ctx, uint32_t kind) {
-    gb_draw d;
+    const uint32_t gsrc = ctx->grad_on ? grad_source(ctx) : 0u;
+    gb_draw        d;
     memset(&d, 0, sizeof(d));
+    d.gsrc      = gsrc;
     d.kind      = kind;
     d.op        = (uint32_t)ctx->op;
     d.join      = (uint32_t)ctx->line_join;
@@ -874,12 +892,14 @@ void vkvg_flush(VkvgContext ctx) {
         return;
     flush_i(ctx);
 }
-void vkvg_destroy(VkvgContext ctx) {
+static void set_solid(VkvgContext ctx);
+void        vkvg_destroy(VkvgContext ctx) {
     if (vkvg_status(ctx))
         return;
     if (--ctx->refs > 0)
         return;
     flush_i(ctx);
+    set_solid(ctx);
     ctx->pl.destroy();
     VkvgSurface s = ctx->surf;
     delete ctx;
@@ -1150,19 +1170,206 @@ static uint32_t create_rgbaf(float r, float g, float b, float a) {
     return (clamp_byte(a * 255.0f) << 24) | (clamp_byte(b * a * 255.0f) << 16) | (clamp_byte(g * a * 255.0f) << 8) |
            clamp_byte(r * a * 255.0f);
 }
+/* ================================================================ patterns */
+/* src/vkvg_pattern.c, linear gradients */
+static void set_solid(VkvgContext ctx) {
+    if (ctx->pattern)
+        vkvg_pattern_destroy(ctx->pattern);
+    ctx->pattern = nullptr;
+    ctx->grad_on = false;
+}
+VkvgPattern vkvg_pattern_create_linear(float x0, float y0, float x1, float y1) {
+    _vkvg_pattern_t *p = new (std::nothrow) _vkvg_pattern_t();
+    if (!p)
+        return (VkvgPattern)&s_no_memory;
+    p->status     = VKVG_STATUS_SUCCESS;
+    p->refs       = 1;
+    p->type       = VKVG_PATTERN_TYPE_LINEAR;
+    p->extend     = VKVG_EXTEND_NONE;
+    p->filter     = VKVG_FILTER_FAST;
+    p->cp[0]      = x0;
+    p->cp[1]      = y0;
+    p->cp[2]      = x1;
+    p->cp[3]      = y1;
+    p->count      = 0;
+    p->matrix     = VKVG_IDENTITY_MATRIX;
+    p->has_matrix = false;
+    return p;
+}
+vkvg_status_t vkvg_pattern_status(VkvgPattern pat) { return pat ? pat->status : VKVG_STATUS_NULL_POINTER; }
+VkvgPattern   vkvg_pattern_reference(VkvgPattern pat) {
+    if (!vkvg_pattern_status(pat))
+        pat->refs++;
+    return pat;
+}
+uint32_t vkvg_pattern_get_reference_count(VkvgPattern pat) { return vkvg_pattern_status(pat) ? 0 : pat->refs; }
+void     vkvg_pattern_destroy(VkvgPattern pat) {
+    if (vkvg_pattern_status(pat))
+        return;
+    if (--pat->refs > 0)
+        return;
+    delete pat;
+}
+vkvg_status_t vkvg_pattern_edit_linear(VkvgPattern pat, float x0, float y0, float x1, float y1) {
+    if (vkvg_pattern_status(pat))
+        return vkvg_pattern_status(pat);
+    if (pat->type != VKVG_PATTERN_TYPE_LINEAR)
+        return VKVG_STATUS_PATTERN_TYPE_MISMATCH;
+    pat->cp[0] = x0;
+    pat->cp[1] = y0;
+    pat->cp[2] = x1;
+    pat->cp[3] = y1;
+    return VKVG_STATUS_SUCCESS;
+}
+vkvg_status_t vkvg_pattern_get_linear_points(VkvgPattern pat, float *x0, float *y0, float *x1, float *y1) {
+    if (vkvg_pattern_status(pat))
+        return vkvg_pattern_status(pat);
+    if (pat->type != VKVG_PATTERN_TYPE_LINEAR)
+        return VKVG_STATUS_PATTERN_TYPE_MISMATCH;
+    if (!x0 || !y0 || !x1 || !y1)
+        return VKVG_STATUS_NULL_POINTER;
+    *x0 = pat->cp[0];
+    *y0 = pat->cp[1];
+    *x1 = pat->cp[2];
+    *y1 = pat->cp[3];
+    return VKVG_STATUS_SUCCESS;
+}
+/* vkvg_pattern_add_color_stop, src/vkvg_pattern.c:149-168: stops keep their
+   premultiplied colour (a*r, a*g, a*b, a) */
+vkvg_status_t vkvg_pattern_add_color_stop(VkvgPattern pat, float offset, float r, float g, float b, float a) {
+    if (vkvg_pattern_status(pat))
+        return vkvg_pattern_status(pat);
+    if (pat->type == VKVG_PATTERN_TYPE_SURFACE || pat->type == VKVG_PATTERN_TYPE_SOLID)
+        return VKVG_STATUS_PATTERN_TYPE_MISMATCH;
+    if (pat->count >= GB_GRAD_STOPS)
+        return VKVG_STATUS_INVALID_INDEX;
+    float *c            = pat->colors + 4 * pat->count;
+    c[0]                = a * r;
+    c[1]                = a * g;
+    c[2]                = a * b;
+    c[3]                = a;
+    pat->stops[pat->count++] = offset;
+    return VKVG_STATUS_SUCCESS;
+}
+vkvg_status_t vkvg_pattern_get_color_stop_count(VkvgPattern pat, uint32_t *count) {
+    if (vkvg_pattern_status(pat))
+        return vkvg_pattern_status(pat);
+    if (pat->type == VKVG_PATTERN_TYPE_SURFACE || pat->type == VKVG_PATTERN_TYPE_SOLID)
+        return VKVG_STATUS_PATTERN_TYPE_MISMATCH;
+    if (!count)
+        return VKVG_STATUS_NULL_POINTER;
+    *count = pat->count;
+    return VKVG_STATUS_SUCCESS;
+}
+vkvg_status_t vkvg_pattern_get_color_stop_rgba(VkvgPattern pat, uint32_t index, float *offset, float *r, float *g,
+                                               float *b, float *a) {
+    if (vkvg_pattern_status(pat))
+        return vkvg_pattern_status(pat);
+    if (pat->type == VKVG_PATTERN_TYPE_SURFACE || pat->type == VKVG_PATTERN_TYPE_SOLID)
+        return VKVG_STATUS_PATTERN_TYPE_MISMATCH;
+    if (index >= pat->count)
+        return VKVG_STATUS_INVALID_INDEX;
+    if (!offset || !r || !g || !b || !a)
+        return VKVG_STATUS_NULL_POINTER;
+    *offset = pat->stops[index];
+    *r      = pat->colors[4 * index];
+    *g      = pat->colors[4 * index + 1];
+    *b      = pat->colors[4 * index + 2];
+    *a      = pat->colors[4 * index + 3];
+    return VKVG_STATUS_SUCCESS;
+}
+void vkvg_pattern_set_extend(VkvgPattern pat, vkvg_extend_t extend) {
+    if (!vkvg_pattern_status(pat))
+        pat->extend = extend;
+}
+vkvg_extend_t vkvg_pattern_get_extend(VkvgPattern pat) {
+    return vkvg_pattern_status(pat) ? (vkvg_extend_t)0 : pat->extend;
+}
+void vkvg_pattern_set_filter(VkvgPattern pat, vkvg_filter_t filter) {
+    if (!vkvg_pattern_status(pat))
+        pat->filter = filter;
+}
+vkvg_filter_t vkvg_pattern_get_filter(VkvgPattern pat) {
+    return vkvg_pattern_status(pat) ? (vkvg_filter_t)0 : pat->filter;
+}
+vkvg_pattern_type_t vkvg_pattern_get_type(VkvgPattern pat) {
+    return vkvg_pattern_status(pat) ? (vkvg_pattern_type_t)0 : pat->type;
+}
+void vkvg_pattern_set_matrix(VkvgPattern pat, const vkvg_matrix_t *matrix) {
+    if (vkvg_pattern_status(pat) || !matrix)
+        return;
+    pat->matrix     = *matrix;
+    pat->has_matrix = true;
+}
+void vkvg_pattern_get_matrix(VkvgPattern pat, vkvg_matrix_t *matrix) {
+    if (vkvg_pattern_status(pat) || !matrix)
+        return;
+    *matrix = pat->has_matrix ? pat->matrix : VKVG_IDENTITY_MATRIX;
+}
+/* vkvg_set_source + _update_cur_pattern (src/vkvg_context.c:1034-1040,
+   src/vkvg_context_internal.c:774-826): the gradient is captured now, its
+   control points through the inverse pattern matrix (identity if singular)
+   and the current CTM, with the target surface's size */
+void vkvg_set_source(VkvgContext ctx, VkvgPattern pat) {
+    if (vkvg_status(ctx) || vkvg_pattern_status(pat))
+        return;
+    vkvg_pattern_reference(pat);
+    set_solid(ctx);
+    ctx->pattern = pat;
+    if (pat->type != VKVG_PATTERN_TYPE_LINEAR) {
+        ctx->status = VKVG_STATUS_PATTERN_TYPE_MISMATCH;
+        return;
+    }
+    if (pat->count < 2) {
+        ctx->status = VKVG_STATUS_PATTERN_INVALID_GRADIENT;
+        return;
+    }
+    gb_grad &g = ctx->grad_snap;
+    memset(&g, 0, sizeof(g));
+    float x0 = pat->cp[0], y0 = pat->cp[1], x1 = pat->cp[2], y1 = pat->cp[3];
+    if (pat->has_matrix) {
+        vkvg_matrix_t m = pat->matrix;
+        if (vkvg_matrix_invert(&m) != VKVG_STATUS_SUCCESS)
+            m = VKVG_IDENTITY_MATRIX;
+        vkvg_matrix_transform_point(&m, &x0, &y0);
+        vkvg_matrix_transform_point(&m, &x1, &y1);
+    }
+    vkvg_matrix_transform_point(&ctx->mat, &x0, &y0);
+    vkvg_matrix_transform_point(&ctx->mat, &x1, &y1);
+    g.cp[0] = x0;
+    g.cp[1] = y0;
+    g.cp[2] = x1;
+    g.cp[3] = y1;
+    g.w     = (float)ctx->surf->width;
+    g.h     = (float)ctx->surf->height;
+    g.count = pat->count;
+    memcpy(g.stops, pat->stops, sizeof(g.stops));
+    memcpy(g.colors, pat->colors, sizeof(g.colors));
+    ctx->grad_on = true;
+}
+/* vkvg_get_source, src/vkvg_context.c:1141-1146: referenced for the caller */
+VkvgPattern vkvg_get_source(VkvgContext ctx) {
+    if (vkvg_status(ctx))
+        return nullptr;
+    vkvg_pattern_reference(ctx->pattern);
+    return ctx->pattern;
+}
 void vkvg_set_source_color(VkvgContext ctx, uint32_t c) {
     if (vkvg_status(ctx))
         return;
+    set_solid(ctx);
     ctx->cur_color = c;
 }
 void vkvg_set_source_rgba(VkvgContext ctx, float r, float g, float b, float a) {
     if (vkvg_status(ctx))
         return;
+    set_solid(ctx);
     ctx->cur_color = create_rgbaf(r, g, b, a);
 }
 void vkvg_set_source_rgb(VkvgContext ctx, float r, float g, float b) {
     if (vkvg_status(ctx))
         return;
+    set_solid(ctx);
     ctx->cur_color = create_rgbaf(r, g, b, 1);
 }
 void vkvg_set_opacity(VkvgContext ctx, float opacity) {

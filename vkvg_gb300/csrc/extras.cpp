@@ -157,7 +157,7 @@ vkvg_status_t vkvg_gb300_debug_coverage(VkvgContext ctx, uint32_t i, int32_t *ou
     A.rgba     = s->d_rgba;
     A.cov_out  = p.dbg.as<int32_t>();
     A.cov_draw = i;
-    if (gb_launch_raster(p.st, &A) != cudaSuccess)
+    if (gb_launch_raster(p.st, &A, 0) != cudaSuccess)
         return VKVG_STATUS_DEVICE_ERROR;
     gb_count_launch(1);
     if (cudaStreamSynchronize(p.st) != cudaSuccess)

@@ -55,8 +55,24 @@ typedef struct {
     float    lh_max;   /* miter limit * line width */
     float    arc_step; /* _get_arc_step(hw) under the draw's CTM */
     float    mat[6];   /* xx yx xy yy x0 y0 */
-    uint32_t pad;
+    uint32_t gsrc;     /* 0: the solid colour src; i + 1: gradient source image i of the frame */
 } gb_draw;
+
+/* A linear gradient as vkvg's fragment stage sees it (shaders/vkvg_main.frag
+   LINEAR case, data of _update_cur_pattern): control points transformed by
+   the pattern's inverse matrix and the CTM at vkvg_set_source time, in
+   pixels; surface size; stops; premultiplied stop colours; the draw's
+   opacity.  One per distinct source image of a frame. */
+#define GB_GRAD_STOPS 16
+typedef struct {
+    float    cp[4]; /* x0 y0 x1 y1 */
+    float    w, h;
+    uint32_t count;
+    float    opacity;
+    float    stops[GB_GRAD_STOPS];
+    float    colors[GB_GRAD_STOPS * 4];
+} gb_grad;
+#define GB_MAX_GRAD_SOURCES 8 /* source images per frame; more flush the frame first */
 
 /* stroke event kinds (dashed strokes materialise their events) */
 #define GB_EV_JOIN      0u /* _build_vb_step at cp with (iL, iR) */

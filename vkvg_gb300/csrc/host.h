@@ -31,6 +31,7 @@ struct FrameHost {
     std::vector<uint32_t> sdraw_id, sdraw_pair0; /* per stroke draw (+ sentinel in pair0) */
     std::vector<uint32_t> fpair_draw, fpair_sub;
     std::vector<float>    dashes, thetas;
+    std::vector<gb_grad>  grads; /* gradient source images of the frame */
     uint32_t              paths = 0; /* fill + stroke draws */
     bool                  any_dash = false;
     bool                  dash_shared = false; /* a subpath belongs to two dashed stroke pairs */
@@ -63,12 +64,13 @@ struct Pipeline {
     DevBuf       sdraw_tri0, sdraw_vbase, tri_a, tri_b, tri_draw;
     DevBuf       cells, cursor, recs, status, dbg;
     DevBuf       dseglen, dseg, dfin;
-    DevBuf       tri_idx; /* oriented vertex indices of stroke triangles (edge cancellation) */ /* parallel dash walk: per-point lengths / states, per-pair final state */
+    DevBuf       tri_idx; /* oriented vertex indices of stroke triangles (edge cancellation) */
+    DevBuf       gsrc;    /* gradient source images of the frame, [n][H][W] */ /* parallel dash walk: per-point lengths / states, per-pair final state */
     PinnedBuf    staging, rb;
     cudaEvent_t  evs[8] = {};
     /* offsets of the uploaded arrays inside `in` */
     size_t o_seg_info, o_seg_a, o_seg_b, o_seg_c, o_seg_n, o_seg_aux, o_sub_seg0, o_sub_nseg, o_sub_flags, o_draws,
-        o_spd, o_sps, o_spf, o_sdid, o_sdp0, o_fpd, o_fps, o_dashes, o_thetas;
+        o_spd, o_sps, o_spf, o_sdid, o_sdp0, o_fpd, o_fps, o_dashes, o_thetas, o_grads;
     bool     uploaded = false;
     /* sizes of the last run */
     uint32_t nseg = 0, nsub = 0, ndraw = 0, nspair = 0, nsdraw = 0, nfpair = 0;
@@ -97,6 +99,21 @@ struct _vkvg_device_t {
     int           hdpi, vdpi;
     uint8_t      *d_unpremul; /* [alpha][channel] -> write_to_memory's unpremultiplied byte */
     std::mutex    mtx;
+};
+
+/* a linear gradient pattern (src/vkvg_pattern.c: vkvg_gradient_t) */
+struct _vkvg_pattern_t {
+    vkvg_status_t       status;
+    uint32_t            refs;
+    vkvg_pattern_type_t type;
+    vkvg_extend_t       extend;
+    vkvg_filter_t       filter;
+    float               cp[4];
+    uint32_t            count;
+    float               stops[GB_GRAD_STOPS];
+    float               colors[GB_GRAD_STOPS * 4]; /* premultiplied */
+    vkvg_matrix_t       matrix;
+    bool                has_matrix;
 };
 
 struct _vkvg_surface_t {
@@ -142,6 +159,9 @@ struct _vkvg_context_t {
     vkvg_matrix_t      mat         = {1, 0, 0, 1, 0, 0};
     std::vector<float> dashes;
     float              dash_offset = 0;
+    VkvgPattern        pattern     = nullptr; /* source pattern, null for the solid colour */
+    bool               grad_on     = false;   /* the source is a gradient snapshot */
+    gb_grad            grad_snap;             /* as of vkvg_set_source (opacity filled per draw) */
 
     PathState ps;
     FrameHost frame;

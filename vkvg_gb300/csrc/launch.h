@@ -19,9 +19,12 @@ struct gb_raster_args {
     uint32_t       *rgba;    /* [H][W] */
     int32_t        *cov_out; /* debug coverage output [H][W][S] or null */
     uint32_t        cov_draw;
+    const uint32_t *gsrc;   /* gradient source images [n][H][W], premultiplied RGBA8 */
 };
 
 extern "C" {
+/* one gradient source image: out[y * W + x] = premultiplied RGBA8 of g at pixel (x, y) */
+cudaError_t gb_launch_gradient_fill(cudaStream_t st, uint32_t W, uint32_t H, const gb_grad *g, uint32_t *out);
 /* out[i] = table-unpremultiplied in[i] (RGBA8, alpha in the top byte) */
 cudaError_t gb_launch_unpremultiply(cudaStream_t st, const uint32_t *in, size_t n, const uint8_t *table,
                                     uint32_t *out);
@@ -93,7 +96,7 @@ cudaError_t gb_launch_bin(cudaStream_t st, int scatter, uint32_t nedges, const i
                           uint32_t ndraws, uint32_t W, uint32_t samples, uint32_t nrows, uint32_t *cell, int4 *recs,
                           uint32_t nunits);
 
-cudaError_t gb_launch_raster(cudaStream_t st, const gb_raster_args *a);
+cudaError_t gb_launch_raster(cudaStream_t st, const gb_raster_args *a, int gradients);
 cudaError_t gb_launch_pmath_eval(cudaStream_t st, int fn, const float *a, const float *b, float *out, uint64_t n);
 }
 

@@ -35,6 +35,7 @@ void FrameHost::clear() {
     fpair_sub.clear();
     dashes.clear();
     thetas.clear();
+    grads.clear();
     paths       = 0;
     any_dash    = false;
     dash_shared = false;
@@ -98,7 +99,7 @@ void Pipeline::destroy() {
     DevBuf *bufs[] = {&in,     &seg_cnt, &seg_off,   &scratch,    &pts,         &pflag,    &sub_pt0, &sub_npts,
                       &ev_cnt, &ev_off,  &events,    &cnt_v,      &cnt_i,       &off_v,    &off_i,   &verts,
                       &inds,   &ev_ret,  &fe_cnt,    &fe_off,     &edges,       &edge_draw, &sdraw_tri0,
-                      &sdraw_vbase, &tri_a, &tri_b, &tri_draw, &cells,   &cursor,   &recs,    &status, &dseglen, &dseg, &dfin, &tri_idx, &dbg};
+                      &sdraw_vbase, &tri_a, &tri_b, &tri_draw, &cells,   &cursor,   &recs,    &status, &dseglen, &dseg, &dfin, &tri_idx, &gsrc, &dbg};
     for (DevBuf *b : bufs)
         b->release();
     staging.release();
@@ -145,6 +146,7 @@ cudaError_t Pipeline::upload(const FrameHost &f) {
         o_fps      = put(b, o, f.fpair_sub);
         o_dashes   = put(b, o, f.dashes);
         o_thetas   = put(b, o, f.thetas);
+        o_grads    = put(b, o, f.grads);
         if (pass == 0) {
             if (!staging.grow(o) || !in.grow(o))
                 return cudaErrorMemoryAllocation;
@@ -372,7 +374,17 @@ cudaError_t Pipeline::run(const FrameHost &f, _vkvg_surface_t *surf, bool timing
     A.status   = status.as<uint32_t>();
     A.samples  = surf->d_samples;
     A.rgba     = surf->d_rgba;
-    CK(gb_launch_raster(st, &A));
+    /* gradient source images: one per distinct (gradient, opacity) of the frame */
+    const uint32_t ngrad = (uint32_t)f.grads.size();
+    if (ngrad) {
+        GROW(gsrc, (size_t)ngrad * W * H * 4);
+        const gb_grad *g = (const gb_grad *)(I + o_grads);
+        for (uint32_t i = 0; i < ngrad; i++)
+            CK(gb_launch_gradient_fill(st, W, H, g + i, gsrc.as<uint32_t>() + (size_t)i * W * H));
+        gb_count_launch(ngrad);
+        A.gsrc = gsrc.as<uint32_t>();
+    }
+    CK(gb_launch_raster(st, &A, ngrad > 0));
     gb_count_launch(1);
     if (timing)
         CK(cudaEventRecord(evs[4], st));

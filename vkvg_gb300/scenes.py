@@ -24,6 +24,10 @@ for this path, so seeded synthetic inputs stand in for real content):
   rectangles and rounded rectangles, quadratic and relative commands, sub
   paths, transforms, opacity, every join and cap, multi-entry dash patterns
   with offsets, and the CLEAR / DIFFERENCE operators.
+* ``gradient_mix`` - linear gradient sources: horizontal, vertical, diagonal
+  and reversed axes, 2 to 5 stops, opacity, pattern matrices and CTMs, a
+  gradient paint, gradient strokes, and more distinct gradients than one
+  frame holds.
 """
 
 MASK64 = (1 << 64) - 1
@@ -152,12 +156,55 @@ def api_mix(n_items=24, size=160, seed=5, samples=4):
     return {"name": "api_mix", "width": size, "height": size, "samples": samples, "ops": ops, "paths": n_items}
 
 
+def gradient_mix(n_items=14, size=144, seed=9, samples=4):
+    r = SplitMix64(seed)
+    u = lambda lo, hi: lo + (hi - lo) * r.rnd()
+
+    def stops():
+        n = 2 + r.randint(0, 3)
+        offs = sorted(r.rnd() for _ in range(n))
+        offs[0], offs[-1] = 0.0, 1.0
+        return [(o, r.rnd(), r.rnd(), r.rnd(), u(0.3, 1.0)) for o in offs]
+
+    ops = [("set_source_rgb", 1.0, 1.0, 1.0), ("paint",),
+           ("set_source_linear", 0.0, 0.0, float(size), 0.0, [(0.0, 0.1, 0.2, 0.9, 0.5), (1.0, 0.9, 0.5, 0.1, 0.5)],
+            None), ("paint",)]
+    for i in range(n_items):
+        ops.append(("identity_matrix",))
+        if i % 4 == 1:
+            ops += [("translate", u(-8, 8), u(-8, 8)), ("rotate", u(-0.5, 0.5))]
+        axis = i % 5
+        x0, y0 = u(0, size), u(0, size)
+        if axis == 0:
+            x1, y1 = x0 + u(20, 100), y0
+        elif axis == 1:
+            x1, y1 = x0, y0 + u(20, 100)
+        elif axis == 2:
+            x1, y1 = x0 - u(20, 100), y0
+        else:
+            x1, y1 = u(0, size), u(0, size)
+        pmat = (u(0.8, 1.2), u(-0.2, 0.2), u(-0.2, 0.2), u(0.8, 1.2), u(-5, 5), u(-5, 5)) if i % 3 == 2 else None
+        ops.append(("move_to", u(0, size), u(0, size)))
+        for _ in range(2):
+            ops.append(("curve_to",) + tuple(u(0, size) for _ in range(6)))
+        ops.append(("close_path",))
+        ops += [("set_source_linear", x0, y0, x1, y1, stops(), pmat), ("set_fill_rule", i % 2),
+                ("set_opacity", 1.0 if i % 2 else u(0.4, 1.0)), ("fill_preserve",),
+                ("set_line_width", u(1, 7)), ("set_line_join", i % 3)]
+        if i % 3 == 0:
+            ops += [("set_source_rgba", r.rnd(), r.rnd(), r.rnd(), u(0.5, 1.0))]
+        ops.append(("stroke",))
+    return {"name": "gradient_mix", "width": size, "height": size, "samples": samples, "ops": ops, "paths": n_items}
+
+
 def play(ctx, ops):
     """Replay a scene's calls on a context object with vkvg method names."""
     for op in ops:
         name, args = op[0], op[1:]
         if name == "set_dash":
             ctx.set_dash(args[0], args[1])
+        elif name == "set_source_linear":
+            ctx.set_source_linear(*args)
         elif name == "set_matrix":
             ctx.set_matrix(args[0])
         else:
