@@ -214,6 +214,15 @@ vkvg_public void vkvg_fill_preserve(VkvgContext ctx);
 vkvg_public void vkvg_paint(VkvgContext ctx);
 vkvg_public void vkvg_clear(VkvgContext ctx);
 
+/* clip: include/vkvg.h:1292-1325 */
+vkvg_public void vkvg_reset_clip(VkvgContext ctx);
+vkvg_public void vkvg_clip(VkvgContext ctx);
+vkvg_public void vkvg_clip_preserve(VkvgContext ctx);
+
+/* graphics state stack: include/vkvg.h:1555-1579 */
+vkvg_public void vkvg_save(VkvgContext ctx);
+vkvg_public void vkvg_restore(VkvgContext ctx);
+
 /* source and line parameters: include/vkvg.h:1334-1545 */
 vkvg_public void             vkvg_set_opacity(VkvgContext ctx, float opacity);
 vkvg_public float            vkvg_get_opacity(VkvgContext ctx);

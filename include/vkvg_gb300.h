@@ -88,6 +88,11 @@ vkvg_public void          vkvg_gb300_frame_destroy(VkvgFrame frame);
 #define VKVG_CMD_SET_SOURCE_RGB    0x0801
 #define VKVG_CMD_SET_SOURCE_RGBA   0x0802
 #define VKVG_CMD_SET_SOURCE_COLOR  0x0803
+#define VKVG_CMD_SAVE              0x0001
+#define VKVG_CMD_RESTORE           0x0002
+#define VKVG_CMD_CLIP              0x0204
+#define VKVG_CMD_RESET_CLIP        0x0205
+#define VKVG_CMD_CLIP_PRESERVE     0x0604
 vkvg_public vkvg_status_t vkvg_gb300_replay_stream(VkvgContext ctx, const uint32_t *cmds, uint32_t ncmds,
                                                    const float *args, uint64_t nargs);
 

@@ -65,8 +65,26 @@ enum {
     VKO_STATUS_INVALID_FONT,
 };
 
-/* draw kinds recorded by the oracle (one per fill/stroke/paint/clear call) */
-enum { VKO_DRAW_FILL_EO = 0, VKO_DRAW_FILL_NZ = 1, VKO_DRAW_STROKE = 2, VKO_DRAW_PAINT = 3, VKO_DRAW_CLEAR = 4 };
+/* draw kinds recorded by the oracle: one per fill/stroke/paint/clear/clip
+   call, and the stencil operations of vkvg_reset_clip / vkvg_save /
+   vkvg_restore in the order vkvg issues them (src/vkvg_context.c:703-733,
+   1251-1512): RESET clears the stencil; SAVE_BIT copies the clip bit into
+   save bit `param`; RESTORE_BIT copies bit `param` into the clip bit; STORE
+   copies the stencil into stencil image `param`; LOAD copies it back */
+enum {
+    VKO_DRAW_FILL_EO     = 0,
+    VKO_DRAW_FILL_NZ     = 1,
+    VKO_DRAW_STROKE      = 2,
+    VKO_DRAW_PAINT       = 3,
+    VKO_DRAW_CLEAR       = 4,
+    VKO_DRAW_CLIP_EO     = 5,
+    VKO_DRAW_CLIP_NZ     = 6,
+    VKO_DRAW_RESET       = 7,
+    VKO_DRAW_SAVE_BIT    = 8,
+    VKO_DRAW_RESTORE_BIT = 9,
+    VKO_DRAW_STORE       = 10,
+    VKO_DRAW_LOAD        = 11
+};
 /* operators: vkvg_operator_t order (include/vkvg.h) */
 enum { VKO_OP_CLEAR = 0, VKO_OP_SOURCE = 1, VKO_OP_OVER = 2, VKO_OP_DIFFERENCE = 3 };
 
@@ -160,6 +178,13 @@ VKO_API void vko_stroke_preserve(vko_context *ctx);
 VKO_API void vko_paint(vko_context *ctx);
 VKO_API void vko_clear(vko_context *ctx);
 
+/* clip and the state stack */
+VKO_API void vko_reset_clip(vko_context *ctx);
+VKO_API void vko_clip(vko_context *ctx);
+VKO_API void vko_clip_preserve(vko_context *ctx);
+VKO_API void vko_save(vko_context *ctx);
+VKO_API void vko_restore(vko_context *ctx);
+
 /* state */
 VKO_API void     vko_set_source_rgba(vko_context *ctx, float r, float g, float b, float a);
 VKO_API void     vko_set_source_rgb(vko_context *ctx, float r, float g, float b);
@@ -174,6 +199,11 @@ VKO_API void     vko_set_opacity(vko_context *ctx, float o);
 VKO_API void     vko_set_dash(vko_context *ctx, const float *dashes, uint32_t n, float offset);
 VKO_API void     vko_set_matrix(vko_context *ctx, const vko_matrix *m);
 VKO_API void     vko_get_matrix(vko_context *ctx, vko_matrix *m);
+VKO_API float    vko_get_line_width(vko_context *ctx);
+VKO_API int      vko_get_line_join(vko_context *ctx);
+VKO_API int      vko_get_line_cap(vko_context *ctx);
+VKO_API int      vko_get_fill_rule(vko_context *ctx);
+VKO_API int      vko_get_operator(vko_context *ctx);
 VKO_API void     vko_identity_matrix(vko_context *ctx);
 VKO_API void     vko_translate(vko_context *ctx, float dx, float dy);
 VKO_API void     vko_scale(vko_context *ctx, float sx, float sy);

@@ -124,6 +124,9 @@ static void surface_release(vko_surface *s) {
         return;
     free(s->data);
     free(s->stencil);
+    for (uint32_t i = 0; i < s->nimages; i++)
+        free(s->images[i]);
+    free(s->images);
     free(s);
 }
 void     vko_surface_destroy(vko_surface *s) { surface_release(s); }
@@ -205,6 +208,15 @@ vko_context *vko_create(vko_surface *surf) {
     ctx->opacity     = 1.0f;
     vko_matrix_init_identity(&ctx->mat);
     vko_ctx_init_geom(ctx);
+    /* the context's first render pass clears the stencil
+       (renderPass_ClearStencil, src/vkvg_context.c:43-49); recorded only when
+       a previous context left something in it */
+    size_t ns = (size_t)surf->width * surf->height * surf->samples;
+    for (size_t i = 0; i < ns; i++)
+        if (surf->stencil[i]) {
+            vko_new_draw(ctx, VKO_DRAW_RESET);
+            break;
+        }
     return ctx;
 }
 int  vko_status(vko_context *ctx) { return ctx ? ctx->status : VKO_STATUS_NULL_POINTER; }
@@ -231,6 +243,14 @@ void vko_destroy(vko_context *ctx) {
     vko_flush(ctx);
     if (ctx->pattern)
         vko_pattern_destroy(ctx->pattern);
+    while (ctx->saved) {
+        vko_saved *sv = ctx->saved;
+        ctx->saved    = sv->next;
+        if (sv->pattern)
+            vko_pattern_destroy(sv->pattern);
+        free(sv->dashes);
+        free(sv);
+    }
     vko_surface *s = ctx->surf;
     vko_ctx_free_geom(ctx);
     free(ctx);
@@ -328,12 +348,16 @@ static void set_solid(vko_context *ctx) {
    src/vkvg_context_internal.c:774-826): the gradient as of now, control
    points through the inverse pattern matrix (identity if singular) and the
    CTM, with the target surface's size */
-void vko_set_source(vko_context *ctx, vko_pattern *pat) {
+static void snap_gradient(vko_context *ctx, vko_pattern *pat);
+void        vko_set_source(vko_context *ctx, vko_pattern *pat) {
     if (vko_status(ctx) || vko_pattern_status(pat))
         return;
     vko_pattern_reference(pat);
     set_solid(ctx);
     ctx->pattern = pat;
+    snap_gradient(ctx, pat);
+}
+static void snap_gradient(vko_context *ctx, vko_pattern *pat) {
     if (pat->count < 2) {
         ctx->status = VKO_STATUS_PATTERN_INVALID_GRADIENT;
         return;
@@ -533,3 +557,143 @@ void vko_pmath_eval(int fn, const float *a, const float *b, float *out, uint64_t
         }
     }
 }
+
+/* ------------------------------------------------- clip and the state stack
+   vkvg_reset_clip / vkvg_clip / vkvg_clip_preserve / vkvg_save / vkvg_restore,
+   src/vkvg_context.c:698-733, 950-976, 1251-1512.  Each stencil pass vkvg
+   issues becomes one draw of the matching VKO_DRAW_* kind, in vkvg's order. */
+static int prev_clip_state(vko_context *ctx) {
+    /* _get_previous_clip_state, src/vkvg_context.c:698-702 */
+    return ctx->saved ? ctx->saved->clip_state : VKO_CLIP_CLEAR;
+}
+static void stencil_draw(vko_context *ctx, int kind, int param) {
+    vko_draw *d = vko_new_draw(ctx, kind);
+    if (d)
+        d->param = param;
+}
+void vko_reset_clip(vko_context *ctx) {
+    if (vko_status(ctx))
+        return;
+    if (ctx->clip_state == VKO_CLIP_CLEAR)
+        return;
+    ctx->clip_state = prev_clip_state(ctx) == VKO_CLIP_CLEAR ? VKO_CLIP_NONE : VKO_CLIP_CLEAR;
+    stencil_draw(ctx, VKO_DRAW_RESET, 0);
+}
+void vko_clip_preserve(vko_context *ctx) {
+    if (vko_status(ctx))
+        return;
+    if (vko_clip_preserve_geom(ctx))
+        ctx->clip_state = VKO_CLIP_CLIP;
+}
+void vko_clip(vko_context *ctx) {
+    if (vko_status(ctx))
+        return;
+    if (vko_clip_preserve_geom(ctx))
+        ctx->clip_state = VKO_CLIP_CLIP;
+    vko_clear_path(ctx);
+}
+void vko_save(vko_context *ctx) {
+    if (vko_status(ctx))
+        return;
+    vko_saved *sv = (vko_saved *)calloc(1, sizeof(vko_saved));
+    if (!sv) {
+        ctx->status = VKO_STATUS_NO_MEMORY;
+        return;
+    }
+    if (ctx->clip_state == VKO_CLIP_CLIP) {
+        sv->clip_state = VKO_CLIP_SAVED;
+        if (ctx->sav_bit > 0 && ctx->sav_bit % 6 == 0) /* a new stencil image */
+            stencil_draw(ctx, VKO_DRAW_STORE, ctx->sav_bit / 6 - 1);
+        stencil_draw(ctx, VKO_DRAW_SAVE_BIT, ctx->sav_bit % 6 + 2);
+        ctx->sav_bit++;
+    } else if (ctx->clip_state == VKO_CLIP_NONE) {
+        sv->clip_state = prev_clip_state(ctx) & 0x03;
+    } else {
+        sv->clip_state = VKO_CLIP_CLEAR;
+    }
+    sv->dash_offset = ctx->dash_offset;
+    sv->dash_count  = ctx->dash_count;
+    if (ctx->dash_count > 0) {
+        sv->dashes = (float *)malloc(sizeof(float) * ctx->dash_count);
+        memcpy(sv->dashes, ctx->dashes, sizeof(float) * ctx->dash_count);
+    }
+    sv->line_width  = ctx->line_width;
+    sv->miter_limit = ctx->miter_limit;
+    sv->op          = ctx->op;
+    sv->line_cap    = ctx->line_cap;
+    sv->fill_rule   = ctx->fill_rule;
+    /* lineJoint of vkvg_context_save_t is never written: calloc's 0 */
+    sv->mat     = ctx->mat;
+    sv->opacity = ctx->opacity;
+    if (ctx->pattern) {
+        sv->pattern = ctx->pattern;
+        vko_pattern_reference(ctx->pattern);
+    } else {
+        sv->cur_color = ctx->cur_color;
+    }
+    sv->next   = ctx->saved;
+    ctx->saved = sv;
+}
+void vko_restore(vko_context *ctx) {
+    if (vko_status(ctx))
+        return;
+    if (!ctx->saved) {
+        ctx->status = VKO_STATUS_INVALID_RESTORE;
+        return;
+    }
+    vko_saved *sv = ctx->saved;
+    ctx->saved    = sv->next;
+    if (ctx->clip_state) {
+        if (ctx->clip_state == VKO_CLIP_CLIP && sv->clip_state == VKO_CLIP_CLEAR)
+            stencil_draw(ctx, VKO_DRAW_RESET, 0);
+        else /* int arithmetic as in C: with sav_bit 0 this names the clip bit */
+            stencil_draw(ctx, VKO_DRAW_RESTORE_BIT, ((int)ctx->sav_bit - 1) % 6 + 2);
+    }
+    if (sv->clip_state == VKO_CLIP_SAVED) {
+        ctx->sav_bit--;
+        if (ctx->sav_bit > 0 && ctx->sav_bit % 6 == 0)
+            stencil_draw(ctx, VKO_DRAW_LOAD, ctx->sav_bit / 6 - 1);
+    }
+    ctx->clip_state  = VKO_CLIP_NONE;
+    ctx->dash_offset = sv->dash_offset;
+    free(ctx->dashes);
+    ctx->dashes     = NULL;
+    ctx->dash_count = sv->dash_count;
+    if (sv->dash_count > 0) {
+        ctx->dashes = (float *)malloc(sizeof(float) * sv->dash_count);
+        memcpy(ctx->dashes, sv->dashes, sizeof(float) * sv->dash_count);
+    }
+    ctx->line_width  = sv->line_width;
+    ctx->miter_limit = sv->miter_limit;
+    ctx->op          = sv->op;
+    ctx->line_cap    = sv->line_cap;
+    ctx->line_join   = sv->line_join;
+    ctx->fill_rule   = sv->fill_rule;
+    ctx->mat         = sv->mat;
+    ctx->opacity     = sv->opacity;
+    if (sv->pattern) {
+        if (sv->pattern != ctx->pattern) {
+            /* _update_cur_pattern: the gradient again with the restored CTM;
+               the saved reference passes to the context */
+            vko_pattern *last = ctx->pattern;
+            ctx->pattern      = sv->pattern;
+            ctx->grad_on      = 0;
+            snap_gradient(ctx, sv->pattern);
+            if (last)
+                vko_pattern_destroy(last);
+        } else {
+            vko_pattern_destroy(sv->pattern);
+        }
+    } else {
+        ctx->cur_color = sv->cur_color;
+        set_solid(ctx);
+    }
+    free(sv->dashes);
+    free(sv);
+}
+
+float vko_get_line_width(vko_context *ctx) { return ctx ? ctx->line_width : 0.f; }
+int   vko_get_line_join(vko_context *ctx) { return ctx ? ctx->line_join : 0; }
+int   vko_get_line_cap(vko_context *ctx) { return ctx ? ctx->line_cap : 0; }
+int   vko_get_fill_rule(vko_context *ctx) { return ctx ? ctx->fill_rule : 0; }
+int   vko_get_operator(vko_context *ctx) { return ctx ? ctx->op : 0; }

@@ -1067,7 +1067,7 @@ static vko_draw *new_draw(vko_context *ctx, int kind) {
     d->color   = ctx->cur_color;
     d->opacity = ctx->opacity;
     d->mat     = ctx->mat;
-    if (ctx->grad_on) {
+    if (ctx->grad_on && kind <= VKO_DRAW_PAINT) {
         d->grad      = 1;
         d->g         = ctx->grad_snap;
         d->g.opacity = ctx->opacity;
@@ -1204,14 +1204,15 @@ static void stroke_preserve(vko_context *ctx) {
 
 /* _fill_preserve, src/vkvg_context.c:796-821, with the EO scissor bounds of
    _poly_fill (src/vkvg_context_internal.c:1583-1655) */
-static void fill_preserve(vko_context *ctx) {
+static int fill_geom(vko_context *ctx, int clip) {
     finish_path(ctx);
     if (!ctx->path_ptr)
-        return;
+        return 0;
     int       eo = ctx->fill_rule == 0;
-    vko_draw *d  = new_draw(ctx, eo ? VKO_DRAW_FILL_EO : VKO_DRAW_FILL_NZ);
+    vko_draw *d  = new_draw(ctx, clip ? (eo ? VKO_DRAW_CLIP_EO : VKO_DRAW_CLIP_NZ)
+                                      : (eo ? VKO_DRAW_FILL_EO : VKO_DRAW_FILL_NZ));
     if (!d)
-        return;
+        return 0;
     uint32_t nsub = 0, ptrPath = 0, first = 0;
     while (ptrPath < ctx->path_ptr) {
         uint32_t cnt = ctx->pathes[ptrPath] & VKO_PATH_ELT_MASK;
@@ -1225,7 +1226,7 @@ static void fill_preserve(vko_context *ctx) {
     d->sub_counts = (uint32_t *)malloc((size_t)(nsub + 1) * sizeof(uint32_t));
     if (!d->pts || !d->sub_counts) {
         ctx->status = VKO_STATUS_NO_MEMORY;
-        return;
+        return 0;
     }
     memcpy(d->pts, ctx->points, (size_t)first * sizeof(v2));
     d->bounds[0] = FLT_MAX;
@@ -1256,7 +1257,14 @@ static void fill_preserve(vko_context *ctx) {
         ptrPath = next_fill_subpath(ctx, ptrPath, cnt);
     }
     d->convex = (ctx->path_ptr == 1 && (ctx->pathes[0] & VKO_PATH_IS_CONVEX_BIT)) ? 1 : 0;
+    return 1;
 }
+static void fill_preserve(vko_context *ctx) { fill_geom(ctx, 0); }
+/* the geometry of _clip_preserve (src/vkvg_context.c:754-795): returns
+   whether the path had anything to clip with */
+int       vko_clip_preserve_geom(vko_context *ctx) { return fill_geom(ctx, 1); }
+vko_draw *vko_new_draw(vko_context *ctx, int kind) { return new_draw(ctx, kind); }
+void      vko_clear_path(vko_context *ctx) { clear_path(ctx); }
 
 void vko_fill_preserve(vko_context *ctx) {
     if (vko_status(ctx))
@@ -1295,6 +1303,8 @@ void vko_paint(vko_context *ctx) {
 void vko_clear(vko_context *ctx) {
     if (vko_status(ctx))
         return;
+    int prev        = ctx->saved ? ctx->saved->clip_state : VKO_CLIP_CLEAR;
+    ctx->clip_state = prev == VKO_CLIP_CLEAR ? VKO_CLIP_NONE : VKO_CLIP_CLEAR;
     new_draw(ctx, VKO_DRAW_CLEAR);
 }
 

@@ -56,8 +56,19 @@ struct vko_pattern_t {
     int        has_matrix;
 };
 
+/* kinds that carry fill geometry, and the even-odd ones */
+#define VKO_FILL_GEOM(k) ((k) == VKO_DRAW_FILL_EO || (k) == VKO_DRAW_FILL_NZ || (k) == VKO_DRAW_CLIP_EO || (k) == VKO_DRAW_CLIP_NZ)
+#define VKO_EO(k)        ((k) == VKO_DRAW_FILL_EO || (k) == VKO_DRAW_CLIP_EO)
+
+/* stencil bits, src/vkvg_device_internal.h:28-30 of vkvg; bits 2..7 are the
+   save bits of vkvg_save */
+#define VKO_STENCIL_FILL 0x1u
+#define VKO_STENCIL_CLIP 0x2u
+#define VKO_STENCIL_ALL  0x3u
+
 typedef struct {
     int      kind;
+    int      param; /* stencil operations: save bit (shift) or image index */
     int      op;
     uint32_t color;
     float    opacity;
@@ -84,7 +95,25 @@ struct vko_surface_t {
     uint32_t width, height, samples;
     uint8_t *data;    /* [y][x][s][4] premultiplied RGBA8 */
     uint8_t *stencil; /* [y][x][s] */
+    uint8_t **images; /* stencil copies of vkvg_save beyond six levels */
+    uint32_t nimages;
 };
+
+/* one vkvg_save level, vkvg_context_save_t (src/vkvg_context_internal.h:101-124) */
+typedef struct vko_saved {
+    struct vko_saved *next;
+    float             line_width, miter_limit, dash_offset, opacity;
+    uint32_t          dash_count;
+    float            *dashes;
+    int               op, line_cap, line_join, fill_rule;
+    vko_matrix        mat;
+    uint32_t          cur_color;
+    vko_pattern      *pattern;
+    int               clip_state;
+} vko_saved;
+
+/* vkvg_clip_state_t, src/vkvg_context_internal.h:95-99 */
+enum { VKO_CLIP_NONE = 0x00, VKO_CLIP_CLEAR = 0x01, VKO_CLIP_CLIP = 0x02, VKO_CLIP_SAVED = 0x06 };
 
 struct vko_context_t {
     int          status;
@@ -108,6 +137,9 @@ struct vko_context_t {
     vko_pattern *pattern;
     int          grad_on;
     vko_grad     grad_snap;
+    int          clip_state; /* curClipState */
+    uint8_t      sav_bit;    /* curSavBit */
+    vko_saved   *saved;      /* pSavedCtxs */
 
     /* stroke vertex / index emission buffers */
     v2      *verts;
@@ -153,6 +185,9 @@ static inline int   v2_equ(v2 a, v2 b) { return VKO_EQUF(a.x, b.x) & VKO_EQUF(a.
 void vko_ctx_init_geom(vko_context *ctx);
 void vko_ctx_free_geom(vko_context *ctx);
 void vko_draw_free(vko_draw *d);
+vko_draw *vko_new_draw(vko_context *ctx, int kind);
+int       vko_clip_preserve_geom(vko_context *ctx);
+void      vko_clear_path(vko_context *ctx);
 
 /* raster (vko_raster.c) */
 void vko_raster_draw(vko_surface *surf, const vko_draw *d);

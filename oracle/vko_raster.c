@@ -19,6 +19,14 @@
  *    once;
  *  - strokes and the other pipe_OVER draws: every covering triangle blends
  *    once (stencil test on the CLIP bit only, :240-246);
+ *  - clip (src/vkvg_context.c:754-795): the path sets the FILL bit of the
+ *    samples it covers that pass the clip test (even-odd: the polyFill fan,
+ *    INVERT; non-zero: pipelineClipping, REPLACE), then a full-screen pass of
+ *    pipelineClipping (:233-239) sets the CLIP bit where FILL is clear and
+ *    zeroes both bits where it is set; vkvg_save / vkvg_restore copy the CLIP
+ *    bit to and from save bits 2..7 with the same pipeline and copy the whole
+ *    stencil to and from images for deeper levels (src/vkvg_context.c:1251-1512);
+ *    stencil clears (vkvg_clear, vkvg_reset_clip) zero every bit;
  *  - blend ONE, ONE_MINUS_SRC_ALPHA on premultiplied UNORM8 (:200-209):
  *    d' = s + round(d*(255-sa)/255) (no ties exist), clamped to 255;
  *    VKVG_OPERATOR_CLEAR writes 0, VKVG_OPERATOR_DIFFERENCE subtracts;
@@ -147,9 +155,22 @@ static void cb_add(void *u, uint32_t px, uint32_t py, uint32_t s) {
     cov_u *c = (cov_u *)u;
     c->acc[((size_t)py * c->w + px) * c->samples + s] += c->add;
 }
+/* one stencil test and update as Vulkan defines them for VK_COMPARE_OP_EQUAL:
+   the test passes when (ref & compare mask) == (stencil & compare mask); the
+   pass or fail op's value is written through the write mask */
+enum { SOP_KEEP, SOP_ZERO, SOP_REPLACE, SOP_INVERT };
+static inline uint8_t stencil_apply(uint8_t st, uint8_t ref, uint8_t cmask, uint8_t wmask, int pass_op, int fail_op) {
+    int     op = ((ref & cmask) == (st & cmask)) ? pass_op : fail_op;
+    uint8_t v  = op == SOP_KEEP ? st : op == SOP_ZERO ? 0 : op == SOP_REPLACE ? ref : (uint8_t)~st;
+    return (uint8_t)((st & ~wmask) | (v & wmask));
+}
+/* pipe_OVER's test with compare mask CLIP and reference 1 (:240-246) */
+static inline int visible(uint8_t st) { return (st & VKO_STENCIL_CLIP) == (1u & VKO_STENCIL_CLIP); }
+/* polyFill: EQUAL on CLIP with reference 0, INVERT through the FILL mask (:226-232) */
 static void cb_invert(void *u, uint32_t px, uint32_t py, uint32_t s) {
-    cov_u *c = (cov_u *)u;
-    c->stencil[((size_t)py * c->w + px) * c->samples + s] ^= 1;
+    cov_u   *c = (cov_u *)u;
+    uint8_t *p = &c->stencil[((size_t)py * c->w + px) * c->samples + s];
+    *p         = stencil_apply(*p, 0, VKO_STENCIL_CLIP, VKO_STENCIL_FILL, SOP_INVERT, SOP_KEEP);
 }
 
 /* ----------------------------------------------------------- scanline mode */
@@ -235,7 +256,7 @@ static edge_t *draw_edges(const vko_surface *surf, const vko_draw *d, uint64_t *
         }                                                                                                              \
         e[n++] = (edge_t){a, b, c, dd};                                                                                \
     } while (0)
-    if (d->kind == VKO_DRAW_FILL_EO || d->kind == VKO_DRAW_FILL_NZ) {
+    if (VKO_FILL_GEOM(d->kind)) {
         uint32_t first = 0;
         for (uint32_t s = 0; s < d->nsub; s++) {
             uint32_t cnt = d->sub_counts[s];
@@ -341,7 +362,7 @@ void vko_draw_coverage_impl(const vko_surface *surf, const vko_draw *d, int mode
         return;
     }
     cov_u u = {w, S, out, 1, NULL};
-    if (d->kind == VKO_DRAW_FILL_EO || d->kind == VKO_DRAW_FILL_NZ) {
+    if (VKO_FILL_GEOM(d->kind)) {
         /* signed fan coverage: sum of orientation signs of the covering fan
            triangles = winding number */
         uint32_t first = 0;
@@ -495,7 +516,8 @@ static void apply_rows(const job_t *j) {
         uint32_t py = gr / rpp, s = gr % rpp;
         for (int32_t px = (int32_t)w - 1; px >= 0; px--) {
             int32_t  wv  = acc;
-            uint8_t *dst = surf->data + (((size_t)py * w + (uint32_t)px) * S + s) * 4;
+            size_t   si  = ((size_t)py * w + (uint32_t)px) * S + s;
+            uint8_t *dst = surf->data + si * 4;
             int      k   = 0;
             if (kind == VKO_DRAW_FILL_EO)
                 k = wv & 1;
@@ -503,7 +525,7 @@ static void apply_rows(const job_t *j) {
                 k = wv != 0;
             else
                 k = wv;
-            if (k > 0) {
+            if (k > 0 && visible(surf->stencil[si])) {
                 uint8_t sc[4];
                 draw_src(j->d, j->src, (uint32_t)px, py, sc);
                 for (int t = 0; t < k; t++)
@@ -519,6 +541,100 @@ static void *job_thread(void *arg) {
     return NULL;
 }
 
+/* the fan triangles of an even-odd path through polyFill; returns whether
+   any subpath had a triangle */
+static int eo_fan_invert(vko_surface *surf, const vko_draw *d) {
+    uint32_t w = surf->width, h = surf->height, S = surf->samples;
+    cov_u    u     = {w, S, NULL, 0, surf->stencil};
+    uint32_t first = 0;
+    int      any   = 0;
+    for (uint32_t s = 0; s < d->nsub; s++) {
+        uint32_t cnt = d->sub_counts[s];
+        if (cnt > 2) {
+            any = 1;
+            int32_t v[6];
+            vko_snap_point(&d->mat, w, h, d->pts[2 * first], d->pts[2 * first + 1], &v[0], &v[1]);
+            for (uint32_t i = 1; i + 1 < cnt; i++) {
+                vko_snap_point(&d->mat, w, h, d->pts[2 * (first + i)], d->pts[2 * (first + i) + 1], &v[2], &v[3]);
+                vko_snap_point(&d->mat, w, h, d->pts[2 * (first + i + 1)], d->pts[2 * (first + i + 1) + 1], &v[4],
+                               &v[5]);
+                raster_tri(w, h, S, v, cb_invert, &u);
+            }
+        }
+        first += cnt;
+    }
+    return any;
+}
+/* clip draws and the stencil passes of reset / save / restore */
+static void stencil_draw(vko_surface *surf, const vko_draw *d) {
+    size_t   ns = (size_t)surf->width * surf->height * surf->samples;
+    uint8_t *st = surf->stencil;
+    switch (d->kind) {
+    case VKO_DRAW_CLIP_EO:
+    case VKO_DRAW_CLIP_NZ:
+        if (vko_raster_mode_g == 1 && d->kind == VKO_DRAW_CLIP_EO) {
+            eo_fan_invert(surf, d);
+        } else {
+            /* non-zero: the covered samples through pipelineClipping with
+               reference FILL, compare mask CLIP, write mask FILL; the
+               scanline mode sets even-odd's FILL the same way from parity */
+            int32_t *cov = (int32_t *)malloc(ns * sizeof(int32_t));
+            vko_draw_coverage_impl(surf, d, vko_raster_mode_g == 1 ? 1 : 0, cov);
+            for (size_t i = 0; i < ns; i++) {
+                int k = d->kind == VKO_DRAW_CLIP_EO ? (cov[i] & 1) : (cov[i] != 0);
+                if (k)
+                    st[i] = stencil_apply(st[i], VKO_STENCIL_FILL, VKO_STENCIL_CLIP, VKO_STENCIL_FILL, SOP_REPLACE,
+                                          SOP_ZERO);
+            }
+            free(cov);
+        }
+        /* full-screen pass: reference CLIP, compare mask FILL, write mask ALL */
+        for (size_t i = 0; i < ns; i++)
+            st[i] = stencil_apply(st[i], VKO_STENCIL_CLIP, VKO_STENCIL_FILL, VKO_STENCIL_ALL, SOP_REPLACE, SOP_ZERO);
+        break;
+    case VKO_DRAW_RESET: memset(st, 0, ns); break;
+    case VKO_DRAW_SAVE_BIT: {
+        uint8_t bit = (uint8_t)(1u << d->param);
+        for (size_t i = 0; i < ns; i++)
+            st[i] = stencil_apply(st[i], VKO_STENCIL_CLIP | bit, VKO_STENCIL_CLIP, bit, SOP_REPLACE, SOP_ZERO);
+        break;
+    }
+    case VKO_DRAW_RESTORE_BIT: {
+        uint8_t bit = (uint8_t)(1u << d->param);
+        for (size_t i = 0; i < ns; i++)
+            st[i] = stencil_apply(st[i], VKO_STENCIL_CLIP | bit, bit, VKO_STENCIL_CLIP, SOP_REPLACE, SOP_ZERO);
+        break;
+    }
+    case VKO_DRAW_STORE: {
+        uint32_t k = (uint32_t)d->param;
+        if (k >= surf->nimages) {
+            uint8_t **t = (uint8_t **)realloc(surf->images, (k + 1) * sizeof(uint8_t *));
+            if (!t)
+                return;
+            for (uint32_t i = surf->nimages; i <= k; i++)
+                t[i] = NULL;
+            surf->images  = t;
+            surf->nimages = k + 1;
+        }
+        if (!surf->images[k])
+            surf->images[k] = (uint8_t *)malloc(ns);
+        if (surf->images[k])
+            memcpy(surf->images[k], st, ns);
+        break;
+    }
+    case VKO_DRAW_LOAD: {
+        uint32_t k = (uint32_t)d->param;
+        if (k < surf->nimages && surf->images[k]) {
+            memcpy(st, surf->images[k], ns);
+            free(surf->images[k]);
+            surf->images[k] = NULL;
+        }
+        break;
+    }
+    default: break;
+    }
+}
+
 /* execute one draw against the surface */
 void vko_raster_draw(vko_surface *surf, const vko_draw *d) {
     uint32_t w = surf->width, h = surf->height, S = surf->samples;
@@ -530,8 +646,14 @@ void vko_raster_draw(vko_surface *surf, const vko_draw *d) {
         memset(surf->stencil, 0, ns);
         return;
     }
+    if (d->kind >= VKO_DRAW_CLIP_EO) {
+        stencil_draw(surf, d);
+        return;
+    }
     if (d->kind == VKO_DRAW_PAINT) {
         for (size_t i = 0; i < ns; i++) {
+            if (!visible(surf->stencil[i]))
+                continue;
             uint8_t sc[4];
             draw_src(d, src, (uint32_t)((i / S) % w), (uint32_t)(i / S / w), sc);
             blend(surf->data + i * 4, sc, d->op);
@@ -541,25 +663,7 @@ void vko_raster_draw(vko_surface *surf, const vko_draw *d) {
     if (vko_raster_mode_g == 1) {
         /* literal pipeline */
         if (d->kind == VKO_DRAW_FILL_EO) {
-            cov_u    u     = {w, S, NULL, 0, surf->stencil};
-            uint32_t first = 0;
-            int      any   = 0;
-            for (uint32_t s = 0; s < d->nsub; s++) {
-                uint32_t cnt = d->sub_counts[s];
-                if (cnt > 2) {
-                    any = 1;
-                    int32_t v[6];
-                    vko_snap_point(&d->mat, w, h, d->pts[2 * first], d->pts[2 * first + 1], &v[0], &v[1]);
-                    for (uint32_t i = 1; i + 1 < cnt; i++) {
-                        vko_snap_point(&d->mat, w, h, d->pts[2 * (first + i)], d->pts[2 * (first + i) + 1], &v[2],
-                                       &v[3]);
-                        vko_snap_point(&d->mat, w, h, d->pts[2 * (first + i + 1)], d->pts[2 * (first + i + 1) + 1],
-                                       &v[4], &v[5]);
-                        raster_tri(w, h, S, v, cb_invert, &u);
-                    }
-                }
-                first += cnt;
-            }
+            int any = eo_fan_invert(surf, d);
             if (!any)
                 return;
             /* cover pass over the scissor of _draw_full_screen_quad */
@@ -587,7 +691,7 @@ void vko_raster_draw(vko_surface *surf, const vko_draw *d) {
         vko_draw_coverage_impl(surf, d, 1, cov);
         for (size_t i = 0; i < ns; i++) {
             int k = d->kind == VKO_DRAW_FILL_NZ ? (cov[i] != 0) : cov[i];
-            if (k > 0) {
+            if (k > 0 && visible(surf->stencil[i])) {
                 uint8_t sc[4];
                 draw_src(d, src, (uint32_t)((i / S) % w), (uint32_t)(i / S / w), sc);
                 for (int t = 0; t < k; t++)

@@ -4,13 +4,18 @@
 
 vkvg's tree holds no numeric fixtures or golden images for the path (its
 gunit PNGs are missing) and vkvg cannot run here, so these fixtures are the
-oracle's outputs on three small seeded scenes, committed so that any change
-of the oracle or of the GPU library against them is caught.  Per scene
-(<name>.npz): the final image (write_to_memory, unpremultiplied RGBA8), each
-draw's kind, the flattened points of fill draws, the vertices and indices of
-stroke draws, and a SHA-256 digest of every draw's per-sample winding /
-covering-triangle counts (int32 [height][width][samples], little endian).
-The oracle runs with its portable math (the kernels' math).
+oracle's outputs on small seeded scenes, committed so that any change of the
+oracle or of the GPU library against them is caught.  Per scene (<name>.npz):
+the final image (write_to_memory, unpremultiplied RGBA8), each draw's kind,
+the flattened points of fill and clip draws, the vertices and indices of
+stroke draws, and a SHA-256 digest of every fill, stroke and clip draw's
+per-sample winding / covering-triangle counts (int32 [height][width][samples],
+little endian).  Draws are the fills, strokes, paints, clears and clip paths;
+the stencil operations of reset_clip / save / restore (kinds 7 and up) are
+left out, as the library splits them differently.  The oracle runs with its
+portable math (the kernels' math).
+
+    python tests/golden/make_golden.py [scene name ...]   # default: all
 """
 import hashlib
 import os
@@ -31,7 +36,11 @@ def golden_scenes():
     return [scenes.plain_small(n_polys=12, size=96, seed=0),
             scenes.curve_heavy(n_paths=10, size=128, seed=1, n_min=3, n_max=6),
             scenes.api_mix(n_items=24, size=160, seed=5),
-            scenes.gradient_mix(n_items=14, size=144, seed=9)]
+            scenes.gradient_mix(n_items=14, size=144, seed=9),
+            scenes.clip_mix(n_items=10, size=128, seed=13)]
+
+STENCIL_OPS = 7
+FILL_KINDS = (0, 1, 5, 6)
 
 
 def _cat(parts, dtype, width):
@@ -51,15 +60,17 @@ def capture(sc):
     L.vko_set_math_mode(0)
     surf, ctx = pu.run_oracle(ob, sc)
     W, H, S = sc["width"], sc["height"], sc["samples"]
-    draws = ctx.draws()
+    every = ctx.draws()
+    idx = [i for i, d in enumerate(every) if d["kind"] < STENCIL_OPS]
+    draws = [every[i] for i in idx]
     kinds = np.array([d["kind"] for d in draws], np.uint32)
-    fpts = [d["points"] for d in draws if d["kind"] in (0, 1)]
+    fpts = [d["points"] for d in draws if d["kind"] in FILL_KINDS]
     sv = [d["verts"] for d in draws if d["kind"] == 2]
     si = [d["inds"] for d in draws if d["kind"] == 2]
     cov = np.zeros((len(draws), 32), np.uint8)
-    for i, d in enumerate(draws):
-        if d["kind"] in (0, 1, 2):
-            cov[i] = digest(ctx.coverage(i, W, H, S))
+    for j, (i, d) in enumerate(zip(idx, draws)):
+        if d["kind"] in FILL_KINDS + (2,):
+            cov[j] = digest(ctx.coverage(i, W, H, S))
     out = {"image": surf.image(), "kinds": kinds, "cov_sha256": cov}
     out["fill_pts"], out["fill_pts_off"] = _cat(fpts, np.float32, 2)
     out["stroke_verts"], out["stroke_verts_off"] = _cat(sv, np.float32, 2)
@@ -70,7 +81,10 @@ def capture(sc):
 
 
 def main():
+    only = set(sys.argv[1:])
     for sc in golden_scenes():
+        if only and sc["name"] not in only:
+            continue
         path = os.path.join(HERE, sc["name"] + ".npz")
         np.savez_compressed(path, **capture(sc))
         print(path, os.path.getsize(path))

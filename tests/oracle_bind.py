@@ -68,6 +68,11 @@ _SIGS = {
     "vko_stroke_preserve": (None, [_P]),
     "vko_paint": (None, [_P]),
     "vko_clear": (None, [_P]),
+    "vko_reset_clip": (None, [_P]),
+    "vko_clip": (None, [_P]),
+    "vko_clip_preserve": (None, [_P]),
+    "vko_save": (None, [_P]),
+    "vko_restore": (None, [_P]),
     "vko_set_source_rgba": (None, [_P, _F, _F, _F, _F]),
     "vko_set_source_rgb": (None, [_P, _F, _F, _F]),
     "vko_set_source_color": (None, [_P, _U]),
@@ -91,6 +96,11 @@ _SIGS = {
     "vko_set_dash": (None, [_P, _P, _U, _F]),
     "vko_set_matrix": (None, [_P, _P]),
     "vko_get_matrix": (None, [_P, _P]),
+    "vko_get_line_width": (_F, [_P]),
+    "vko_get_line_join": (C.c_int, [_P]),
+    "vko_get_line_cap": (C.c_int, [_P]),
+    "vko_get_fill_rule": (C.c_int, [_P]),
+    "vko_get_operator": (C.c_int, [_P]),
     "vko_identity_matrix": (None, [_P]),
     "vko_translate": (None, [_P, _F, _F]),
     "vko_scale": (None, [_P, _F, _F]),
@@ -182,7 +192,7 @@ class OracleContext:
             self.L.vko_draw_info(self.h, i, ptr(info))
             kind, npts, nsub, nverts, ninds, color, convex = [int(v) for v in info[:7]]
             d = {"kind": kind, "color": color, "convex": convex}
-            if kind in (0, 1):
+            if kind in (0, 1, 5, 6):
                 pts = np.zeros((max(npts, 1), 2), np.float32)
                 sub = np.zeros(max(nsub, 1), np.uint32)
                 self.L.vko_draw_points(self.h, i, ptr(pts), ptr(sub))

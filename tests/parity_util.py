@@ -37,21 +37,34 @@ def gpu_draw_points(ctx, info, first, count):
     return (np.concatenate(pts) if pts else np.zeros((0, 2), np.float32)), cnt
 
 
+# draw kinds below this one carry geometry or colour (fills, strokes, paint,
+# clear, clip paths); the stencil operations of reset_clip / save / restore
+# above it may split differently between the library and the oracle
+STENCIL_OPS = 7
+
+
+def geometry_draws(gctx):
+    """indices of the GPU context's draws that are not stencil operations"""
+    n = int(gctx.debug_counts()[2])
+    return [i for i in range(n) if int(gctx.debug_draw(i)[0]) < STENCIL_OPS]
+
+
 def compare_geometry(gctx, octx):
     """bit-exact comparison of flattened points and stroke buffers per draw;
     returns a list of mismatch descriptions"""
     errs = []
-    odraws = octx.draws()
+    odraws = [d for d in octx.draws() if d["kind"] < STENCIL_OPS]
     first, count, flags = gctx.debug_subpaths()
-    ndraw = int(gctx.debug_counts()[2])
-    if ndraw != len(odraws):
-        return ["draw count %d vs oracle %d" % (ndraw, len(odraws))]
-    for i, od in enumerate(odraws):
+    gidx = geometry_draws(gctx)
+    if len(gidx) != len(odraws):
+        return ["draw count %d vs oracle %d" % (len(gidx), len(odraws))]
+    for gi, od in zip(gidx, odraws):
+        i = gi
         info = gctx.debug_draw(i)
         if int(info[0]) != od["kind"]:
             errs.append("draw %d kind %d vs %d" % (i, info[0], od["kind"]))
             continue
-        if od["kind"] in (0, 1):
+        if od["kind"] in (0, 1, 5, 6):
             pts, cnt = gpu_draw_points(gctx, info, first, count)
             if not np.array_equal(cnt, od["subpaths"]):
                 errs.append("draw %d subpath counts differ" % i)

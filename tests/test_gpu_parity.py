@@ -19,6 +19,7 @@ def small_scenes():
         scenes.plain_small(n_polys=12, size=96, seed=0),
         scenes.curve_heavy(n_paths=10, size=128, seed=1, n_min=3, n_max=6),
         scenes.api_mix(n_items=24, size=160, seed=5),
+        scenes.clip_mix(n_items=10, size=128, seed=13),
     ]
     for o in out:
         o["samples"] = 4
@@ -37,7 +38,7 @@ def test_pmath_device_matches_host(gb, fn):
     assert np.array_equal(h.view(np.uint32), d.view(np.uint32))
 
 
-@pytest.mark.parametrize("idx", [0, 1, 2])
+@pytest.mark.parametrize("idx", [0, 1, 2, 3])
 def test_geometry_bit_exact(gb, vko, idx):
     sc = small_scenes()[idx]
     dev, surf, ctx = pu.run_gpu(gb, sc)
@@ -47,19 +48,24 @@ def test_geometry_bit_exact(gb, vko, idx):
     assert not errs, errs[:10]
 
 
-@pytest.mark.parametrize("idx", [0, 1, 2])
+def _oracle_geometry_draws(octx):
+    return [i for i, d in enumerate(octx.draws()) if d["kind"] < pu.STENCIL_OPS]
+
+
+@pytest.mark.parametrize("idx", [0, 1, 2, 3])
 def test_coverage_bit_exact(gb, vko, idx):
     sc = small_scenes()[idx]
     dev, surf, ctx = pu.run_gpu(gb, sc)
     osurf, octx = pu.run_oracle(vko, sc)
-    n = int(ctx.debug_counts()[2])
-    for i in range(n):
+    gi, oi = pu.geometry_draws(ctx), _oracle_geometry_draws(octx)
+    assert len(gi) == len(oi)
+    for i, j in zip(gi, oi):
         g = ctx.debug_coverage(i)
-        o = octx.coverage(i, sc["width"], sc["height"], sc["samples"], mode=0)
+        o = octx.coverage(j, sc["width"], sc["height"], sc["samples"], mode=0)
         assert np.array_equal(g, o), "draw %d: %d samples differ" % (i, int((g != o).sum()))
 
 
-@pytest.mark.parametrize("idx", [0, 1, 2])
+@pytest.mark.parametrize("idx", [0, 1, 2, 3])
 def test_image_bit_exact(gb, vko, idx):
     sc = small_scenes()[idx]
     dev, surf, ctx = pu.run_gpu(gb, sc)
@@ -68,7 +74,7 @@ def test_image_bit_exact(gb, vko, idx):
     assert np.array_equal(surf.image(), osurf.image())
 
 
-@pytest.mark.parametrize("idx", [0, 1, 2])
+@pytest.mark.parametrize("idx", [0, 1, 2, 3])
 def test_gpu_matches_golden(gb, idx):
     """the GPU library against the committed fixtures (tests/golden/), with no
     oracle run: image, per-draw kinds, fill points, stroke buffers and the
@@ -84,20 +90,20 @@ def test_gpu_matches_golden(gb, idx):
     dev, surf, ctx = pu.run_gpu(gb, sc)
     assert np.array_equal(surf.image(), g["image"])
     first, count, _ = ctx.debug_subpaths()
-    n = int(ctx.debug_counts()[2])
-    kinds = np.array([int(ctx.debug_draw(i)[0]) for i in range(n)], np.uint32)
+    gi = pu.geometry_draws(ctx)
+    kinds = np.array([int(ctx.debug_draw(i)[0]) for i in gi], np.uint32)
     assert np.array_equal(kinds, g["kinds"])
     fp, sv, si = [], [], []
-    for i in range(n):
+    for j, i in enumerate(gi):
         info = ctx.debug_draw(i)
-        if kinds[i] in (0, 1):
+        if kinds[j] in make_golden.FILL_KINDS:
             fp.append(pu.gpu_draw_points(ctx, info, first, count)[0])
-        elif kinds[i] == 2:
+        elif kinds[j] == 2:
             v, ix = ctx.debug_stroke(i)
             sv.append(v)
             si.append(ix)
-        if kinds[i] in (0, 1, 2):
-            assert np.array_equal(make_golden.digest(ctx.debug_coverage(i)), g["cov_sha256"][i]), i
+        if kinds[j] in make_golden.FILL_KINDS + (2,):
+            assert np.array_equal(make_golden.digest(ctx.debug_coverage(i)), g["cov_sha256"][j]), i
     for parts, key, dt in ((fp, "fill_pts", np.float32), (sv, "stroke_verts", np.float32), (si, "stroke_inds", np.uint32)):
         cat = np.concatenate(parts) if parts else np.zeros_like(g[key])
         assert np.array_equal(cat.astype(dt).view(np.uint32), g[key].view(np.uint32)), key
@@ -207,3 +213,75 @@ def test_curve_heavy_full_size_bit_exact(gb, vko):
     assert not errs, errs[:10]
     assert np.array_equal(surf.samples_rgba(), osurf.samples_rgba())
     assert np.array_equal(surf.image(), osurf.image())
+
+
+@pytest.mark.parametrize("name", [s["name"] for s in scenes.vkvg_clip_cases()])
+def test_vkvg_clip_cases_bit_exact(gb, vko, name):
+    """vkvg's clip and save/restore demo sequences (tests/clip.c,
+    tests/save_restore.c) at 1024x800: samples and image equal the oracle's"""
+    sc = [s for s in scenes.vkvg_clip_cases() if s["name"] == name][0]
+    dev, surf, ctx = pu.run_gpu(gb, sc)
+    osurf, octx = pu.run_oracle(vko, sc, threads=8)
+    assert ctx.debug_counts()[5] == 0 and ctx.status() == 0
+    assert not pu.compare_geometry(ctx, octx)
+    assert np.array_equal(surf.samples_rgba(), osurf.samples_rgba())
+    assert np.array_equal(surf.image(), osurf.image())
+
+
+@pytest.mark.parametrize("samples,flush_every", [(1, 0), (4, 2), (1, 3)])
+def test_clip_mix_variants_bit_exact(gb, vko, samples, flush_every):
+    """the clip scene at one sample, and flushed every few items so the clip
+    planes, save planes and stencil images cross frames"""
+    sc = scenes.clip_mix(n_items=10, size=120, seed=17, samples=samples, flush_every=flush_every)
+    dev, surf, ctx = pu.run_gpu(gb, sc)
+    osurf, octx = pu.run_oracle(vko, sc)
+    assert ctx.debug_counts()[5] == 0 and ctx.status() == 0
+    assert np.array_equal(surf.samples_rgba(), osurf.samples_rgba())
+    assert np.array_equal(surf.image(), osurf.image())
+
+
+def test_clip_state_on_gpu(gb):
+    """restore's state and statuses through the library: line join back to
+    miter, INVALID_RESTORE without a save, a new context on a clipped surface
+    starting unclipped"""
+    dev = gb.Device(samples=4)
+    surf = gb.Surface(dev, 32, 32)
+    ctx = surf.context()
+    ctx.set_line_width(3.0)
+    ctx.set_line_join(1)
+    ctx.save()
+    ctx.set_line_width(9.0)
+    ctx.restore()
+    assert ctx.get_line_width() == 3.0 and ctx.get_line_join() == 0 and ctx.status() == 0
+    ctx.rectangle(4.0, 4.0, 8.0, 8.0)
+    ctx.clip()
+    ctx.flush()
+    ctx.destroy()
+    ctx2 = surf.context()
+    ctx2.set_source_rgb(0.0, 1.0, 0.0)
+    ctx2.paint()
+    ctx2.flush()
+    assert (surf.image()[..., 1] == 255).all()  # the new context's stencil is clear
+    ctx2.restore()
+    assert ctx2.status() == 3  # VKVG_STATUS_INVALID_RESTORE
+
+
+@pytest.mark.parametrize("which", ["api_mix", "clip_mix"])
+def test_replay_stream_matches_calls(gb, which):
+    """vkvg_gb300_replay_stream of a scene's command codes gives the same
+    samples as the scene's calls"""
+    import ctypes as C
+
+    sc = scenes.api_mix(n_items=24, size=160, seed=5) if which == "api_mix" else \
+        scenes.clip_mix(n_items=10, size=128, seed=13)
+    sc["ops"] = [op for op in sc["ops"] if op[0] in scenes.CMD]  # vkvg records no opacity or pattern calls
+    dev, surf, ctx = pu.run_gpu(gb, sc, debug=False)
+    cmds, args = scenes.encode(sc["ops"])
+    dev2 = gb.Device(samples=sc["samples"])
+    surf2 = gb.Surface(dev2, sc["width"], sc["height"])
+    ctx2 = surf2.context()
+    st = ctx2.L.vkvg_gb300_replay_stream(ctx2.h, cmds.ctypes.data_as(C.c_void_p), len(cmds),
+                                         args.ctypes.data_as(C.c_void_p), len(args))
+    assert st == 0
+    ctx2.flush()
+    assert np.array_equal(surf.samples_rgba(), surf2.samples_rgba())

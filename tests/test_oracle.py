@@ -129,7 +129,8 @@ def small_scenes():
     return [scenes.plain_small(n_polys=12, size=96, seed=0),
             scenes.curve_heavy(n_paths=10, size=128, seed=1, n_min=3, n_max=6),
             scenes.api_mix(n_items=24, size=160, seed=5),
-            scenes.gradient_mix(n_items=14, size=144, seed=9)]
+            scenes.gradient_mix(n_items=14, size=144, seed=9),
+            scenes.clip_mix(n_items=10, size=128, seed=13)]
 
 
 @pytest.mark.parametrize("sc", small_scenes(), ids=lambda s: s["name"])
@@ -142,7 +143,7 @@ def test_literal_equals_scanline(sc):
     draws = c0.draws()
     assert len(draws) == len(c1.draws())
     for i, d in enumerate(draws):
-        if d["kind"] in (0, 1, 2):
+        if d["kind"] in (0, 1, 2, 5, 6):
             ob.lib().vko_set_raster_mode(0)
             a = c0.coverage(i, W, H, S)
             ob.lib().vko_set_raster_mode(1)
@@ -315,3 +316,77 @@ def test_pattern_api_semantics():
     assert L.vkvg_pattern_get_color_stop_rgba(p, 1, C.byref(o), C.byref(r), C.byref(g), C.byref(b),
                                               C.byref(a)) == 7
     L.vkvg_pattern_destroy(p)
+
+
+@pytest.mark.parametrize("sc", scenes.vkvg_clip_cases(width=256, height=200) +
+                         [scenes.clip_mix(n_items=10, size=96, seed=3, samples=1, flush_every=3)],
+                         ids=lambda s: s["name"])
+def test_clip_literal_equals_scanline(sc):
+    """clip scenes: the literal stencil passes and the crossing restatement
+    give the same samples"""
+    s0, c0 = pu.run_oracle(ob, sc, raster_mode=0)
+    s1, c1 = pu.run_oracle(ob, sc, raster_mode=1)
+    ob.lib().vko_set_raster_mode(0)
+    assert c0.status() == 0 and c1.status() == 0
+    assert np.array_equal(s0.samples_rgba(), s1.samples_rgba())
+
+
+def _clip_row(ops, w=16, h=16):
+    """green channel of row 8 after the ops on a fresh 16x16 surface, and the
+    context status"""
+    sc = {"name": "clip_kat", "width": w, "height": h, "samples": 4, "ops": ops, "paths": 0}
+    s, c = pu.run_oracle(ob, sc)
+    row = s.image()[8, :, 1]
+    return "".join("#" if v > 200 else ("+" if v else ".") for v in row), c.status()
+
+
+def test_clip_state_machine_kat():
+    """vkvg's clip / save / restore behaviour (src/vkvg_context.c:698-795,
+    1251-1512) on 16x16 cases, including two outcomes of its state machine
+    that a reader might not expect: a restore finding curClipState "none"
+    leaves the stencil alone (so two nested levels restore only one), and
+    reset_clip clears the save bits of the levels below it"""
+    R = lambda x0, x1: ("rectangle", float(x0), 2.0, float(x1 - x0), 12.0)
+    paint = [("set_source_rgb", 0.0, 1.0, 0.0), ("paint",)]
+    inner, outer = "..######........", "....########...."
+    cases = [
+        ([R(2, 8), ("clip",)] + paint, inner),
+        ([("save",), R(2, 8), ("clip",), ("restore",)] + paint, "#" * 16),
+        ([("save",), R(2, 8), ("clip",), ("save",), R(4, 12), ("clip",), ("restore",)] + paint, inner),
+        ([("save",), R(2, 8), ("clip",), ("save",), R(4, 12), ("clip",), ("restore",), ("restore",)] + paint, inner),
+        ([R(4, 12), ("clip",), ("save",), R(2, 8), ("clip",), ("restore",)] + paint, outer),
+        ([R(2, 8), ("clip",), ("save",), ("reset_clip",), ("restore",)] + paint, "#" * 16),
+        ([R(2, 8), ("clip",), ("reset_clip",)] + paint, "#" * 16),
+        ([R(2, 8), ("clip",), ("clear",)] + paint, "#" * 16),
+        ([R(2, 8), ("clip_preserve",), ("set_source_rgb", 0.0, 1.0, 0.0), ("fill",), ("set_source_rgb", 0.0, 0.5, 0.0),
+          R(4, 12), ("fill",)], "..##++++........"),
+    ]
+    for ops, want in cases:
+        got, st = _clip_row(ops)
+        assert st == 0 and got == want, (ops, got)
+    got, st = _clip_row([("restore",)] + paint)
+    assert st == 3 and got == "." * 16  # VKVG_STATUS_INVALID_RESTORE; later calls do nothing
+
+
+def test_save_restore_state_kat():
+    """vkvg_restore brings back line width, dashes, operator, fill rule, matrix
+    and source, and sets the line join to miter (the field vkvg_save never
+    writes)"""
+    surf = ob.OracleSurface(32, 32, 4)
+    ctx = surf.context()
+    ctx.set_line_width(3.0)
+    ctx.set_line_join(1)
+    ctx.set_fill_rule(0)
+    ctx.save()
+    ctx.set_line_width(7.0)
+    ctx.set_fill_rule(1)
+    ctx.translate(5.0, 5.0)
+    ctx.restore()
+    assert ctx.get_line_width() == 3.0 and ctx.get_line_join() == 0 and ctx.get_fill_rule() == 0
+    m = Mat()
+    ob.lib().vko_get_matrix.argtypes = [C.c_void_p, C.POINTER(Mat)]
+    ob.lib().vko_get_matrix(ctx.h, C.byref(m))
+    assert (m.x0, m.y0) == (0.0, 0.0)
+    assert ctx.status() == 0
+    ctx.destroy()
+    surf.destroy()

@@ -89,6 +89,11 @@ SIGNATURES = {
     "vkvg_fill_preserve": (None, [_P]),
     "vkvg_paint": (None, [_P]),
     "vkvg_clear": (None, [_P]),
+    "vkvg_reset_clip": (None, [_P]),
+    "vkvg_clip": (None, [_P]),
+    "vkvg_clip_preserve": (None, [_P]),
+    "vkvg_save": (None, [_P]),
+    "vkvg_restore": (None, [_P]),
     "vkvg_set_opacity": (None, [_P, _F]),
     "vkvg_get_opacity": (_F, [_P]),
     "vkvg_set_source_color": (None, [_P, _U]),

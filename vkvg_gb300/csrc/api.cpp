@@ -227,12 +227,17 @@ static VkvgSurface surface_alloc(VkvgDevice dev, uint32_t width, uint32_t height
     s->nbands  = (s->nrows + GB_BAND_ROWS - 1) / GB_BAND_ROWS;
     size_t sb  = (size_t)s->nbands * GB_BAND_ROWS * s->wpad * 4;
     size_t rb  = (size_t)s->width * s->height * 4;
+    s->clip_wpr = (s->wpad + 31) / 32;
+    s->plane_words = (size_t)s->nbands * GB_BAND_ROWS * s->clip_wpr;
+    size_t cb      = s->plane_words * 4;
     if (cudaMalloc(&s->d_samples, sb) != cudaSuccess || cudaMalloc(&s->d_rgba, rb) != cudaSuccess ||
-        cudaMalloc(&s->d_out, rb) != cudaSuccess) {
+        cudaMalloc(&s->d_out, rb) != cudaSuccess || cudaMalloc(&s->d_clip, cb) != cudaSuccess) {
         if (s->d_samples)
             cudaFree(s->d_samples);
         if (s->d_rgba)
             cudaFree(s->d_rgba);
+        if (s->d_out)
+            cudaFree(s->d_out);
         delete s;
         return (VkvgSurface)&s_no_memory;
     }
@@ -283,6 +288,8 @@ void     vkvg_surface_destroy(VkvgSurface s) {
     cudaFree(s->d_samples);
     cudaFree(s->d_rgba);
     cudaFree(s->d_out);
+    cudaFree(s->d_clip);
+    s->clip_planes.release();
     VkvgDevice dev = s->dev;
     delete s;
     vkvg_device_destroy(dev);
@@ -355,6 +362,7 @@ vkvg_status_t vkvg_surface_write_to_png(VkvgSurface s, const char *path) {
 }
 
 /* ================================================================ context */
+static void plane_op(VkvgContext ctx, uint32_t kind, uint32_t param);
 VkvgContext vkvg_create(VkvgSurface surf) {
     if (vkvg_surface_status(surf))
         return (VkvgContext)&s_invalid_surf;
@@ -372,6 +380,10 @@ VkvgContext vkvg_create(VkvgSurface surf) {
         return (VkvgContext)&s_device_error;
     }
     vkvg_surface_reference(surf);
+    /* a context's first render pass clears the stencil (renderPass_ClearStencil,
+       src/vkvg_context.c:43-49) */
+    if (surf->clip_active || surf->save_nz)
+        plane_op(ctx, GB_DRAW_CLIP_RESET, 0);
     return ctx;
 }
 vkvg_status_t vkvg_status(VkvgContext ctx) { return !ctx ? VKVG_STATUS_NULL_POINTER : ctx->status; }
@@ -756,7 +768,8 @@ static uint32_t grad_source(VkvgContext ctx) {
     return (uint32_t)ctx->frame.grads.size();
 }
 static gb_draw make_draw(VkvgContext ctx, uint32_t kind) {
-    const uint32_t gsrc = ctx->grad_on ? grad_source(ctx) : 0u;
+    const bool     paints = kind <= GB_DRAW_PAINT; /* clip draws and clears have no source */
+    const uint32_t gsrc   = paints && ctx->grad_on ? grad_source(ctx) : 0u;
     gb_draw        d;
     memset(&d, 0, sizeof(d));
     d.gsrc      = gsrc;
@@ -792,6 +805,31 @@ static void fill_preserve_i(VkvgContext ctx) {
         f.fpair_sub.push_back(s);
     }
     f.paths++;
+}
+/* the fill geometry of _clip_preserve (src/vkvg_context.c:754-795): the
+   current path as an even-odd or non-zero region that the clip keeps */
+static bool clip_preserve_i(VkvgContext ctx) {
+    finish_path(ctx);
+    FrameHost &f = ctx->frame;
+    if (f.sub_seg0.size() == ctx->ps.path_sub0)
+        return false;
+    gb_draw  d  = make_draw(ctx, ctx->fill_rule == VKVG_FILL_RULE_EVEN_ODD ? GB_DRAW_CLIP_EO : GB_DRAW_CLIP_NZ);
+    uint32_t di = (uint32_t)f.draws.size();
+    f.draws.push_back(d);
+    for (uint32_t s = d.sub_first; s < d.sub_first + d.sub_count; s++) {
+        f.fpair_draw.push_back(di);
+        f.fpair_sub.push_back(s);
+    }
+    return true;
+}
+/* a stencil plane operation (GB_DRAW_CLIP_RESET ... GB_DRAW_CLIP_LOAD) */
+static void plane_op(VkvgContext ctx, uint32_t kind, uint32_t param) {
+    gb_draw d;
+    memset(&d, 0, sizeof(d));
+    d.kind      = kind;
+    d.src       = param;
+    d.sub_first = (uint32_t)ctx->frame.sub_seg0.size();
+    ctx->frame.draws.push_back(d);
 }
 /* _stroke_preserve, src/vkvg_context.c:822-948 */
 static void stroke_preserve_i(VkvgContext ctx) {
@@ -900,6 +938,9 @@ void        vkvg_destroy(VkvgContext ctx) {
         return;
     flush_i(ctx);
     set_solid(ctx);
+    for (gb_saved_state &sv : ctx->saved)
+        if (sv.pattern)
+            vkvg_pattern_destroy(sv.pattern);
     ctx->pl.destroy();
     VkvgSurface s = ctx->surf;
     delete ctx;
@@ -1151,10 +1192,127 @@ void vkvg_paint(VkvgContext ctx) {
     }
     ctx->frame.draws.push_back(make_draw(ctx, GB_DRAW_PAINT));
 }
+/* vkvg_clear, src/vkvg_context.c:734-753: colour and the whole stencil */
+static uint8_t prev_clip_state(VkvgContext ctx) {
+    /* _get_previous_clip_state, src/vkvg_context.c:698-702 */
+    return ctx->saved.empty() ? (uint8_t)GB_CLIP_CLEAR : ctx->saved.back().clip_state;
+}
 void vkvg_clear(VkvgContext ctx) {
     if (vkvg_status(ctx))
         return;
+    ctx->clip_state = prev_clip_state(ctx) == GB_CLIP_CLEAR ? GB_CLIP_NONE : GB_CLIP_CLEAR;
     ctx->frame.draws.push_back(make_draw(ctx, GB_DRAW_CLEAR));
+}
+
+/* ---- clip, save and restore (src/vkvg_context.c:719-795, 950-976, 1251-1512).
+   The stencil's bits become the surface's clip planes: the clip bit is the
+   inverse of the visibility plane, save bit 2 + p is save plane p, and each
+   extra stencil image of vkvg_save is a seven-plane image. */
+void vkvg_reset_clip(VkvgContext ctx) {
+    if (vkvg_status(ctx))
+        return;
+    if (ctx->clip_state == GB_CLIP_CLEAR)
+        return;
+    ctx->clip_state = prev_clip_state(ctx) == GB_CLIP_CLEAR ? GB_CLIP_NONE : GB_CLIP_CLEAR;
+    plane_op(ctx, GB_DRAW_CLIP_RESET, 0);
+}
+void vkvg_clip_preserve(VkvgContext ctx) {
+    if (vkvg_status(ctx))
+        return;
+    if (clip_preserve_i(ctx))
+        ctx->clip_state = GB_CLIP_CLIP;
+}
+void vkvg_clip(VkvgContext ctx) {
+    if (vkvg_status(ctx))
+        return;
+    if (clip_preserve_i(ctx))
+        ctx->clip_state = GB_CLIP_CLIP;
+    clear_path(ctx);
+}
+void vkvg_save(VkvgContext ctx) {
+    if (vkvg_status(ctx))
+        return;
+    gb_saved_state sv;
+    if (ctx->clip_state == GB_CLIP_CLIP) {
+        sv.clip_state = GB_CLIP_SAVED;
+        /* a seventh save first copies the whole stencil to a new image */
+        if (ctx->sav_bit > 0 && ctx->sav_bit % GB_CLIP_SAVE_PLANES == 0)
+            plane_op(ctx, GB_DRAW_CLIP_STORE, ctx->sav_bit / GB_CLIP_SAVE_PLANES - 1u);
+        plane_op(ctx, GB_DRAW_CLIP_SAVE, ctx->sav_bit % GB_CLIP_SAVE_PLANES);
+        ctx->sav_bit++;
+    } else if (ctx->clip_state == GB_CLIP_NONE) {
+        sv.clip_state = (uint8_t)(prev_clip_state(ctx) & 0x03u);
+    } else {
+        sv.clip_state = GB_CLIP_CLEAR;
+    }
+    sv.line_width  = ctx->line_width;
+    sv.miter_limit = ctx->miter_limit;
+    sv.dash_offset = ctx->dash_offset;
+    sv.dashes      = ctx->dashes;
+    sv.opacity     = ctx->opacity;
+    sv.line_cap    = ctx->line_cap;
+    sv.fill_rule   = ctx->fill_rule;
+    sv.op          = ctx->op;
+    sv.mat         = ctx->mat;
+    sv.cur_color   = ctx->cur_color;
+    sv.pattern     = ctx->pattern;
+    if (sv.pattern)
+        vkvg_pattern_reference(sv.pattern);
+    ctx->saved.push_back(std::move(sv));
+}
+static void snap_gradient(VkvgContext ctx, VkvgPattern pat);
+void        vkvg_restore(VkvgContext ctx) {
+    if (vkvg_status(ctx))
+        return;
+    if (ctx->saved.empty()) {
+        ctx->status = VKVG_STATUS_INVALID_RESTORE;
+        return;
+    }
+    gb_saved_state sv = std::move(ctx->saved.back());
+    ctx->saved.pop_back();
+    if (ctx->clip_state != GB_CLIP_NONE) {
+        if (ctx->clip_state == GB_CLIP_CLIP && sv.clip_state == GB_CLIP_CLEAR) {
+            plane_op(ctx, GB_DRAW_CLIP_RESET, 0);
+        } else {
+            /* the clip bit from save bit (curSavBit - 1) % 6 + 2; with no
+               save bit in use that expression names the clip bit itself */
+            const int j = (int)ctx->sav_bit - 1;
+            if (j >= 0)
+                plane_op(ctx, GB_DRAW_CLIP_RESTORE, (uint32_t)(j % (int)GB_CLIP_SAVE_PLANES));
+        }
+    }
+    if (sv.clip_state == GB_CLIP_SAVED) {
+        ctx->sav_bit--;
+        if (ctx->sav_bit > 0 && ctx->sav_bit % GB_CLIP_SAVE_PLANES == 0)
+            plane_op(ctx, GB_DRAW_CLIP_LOAD, ctx->sav_bit / GB_CLIP_SAVE_PLANES - 1u);
+    }
+    ctx->clip_state  = GB_CLIP_NONE;
+    ctx->dash_offset = sv.dash_offset;
+    ctx->dashes      = sv.dashes;
+    ctx->line_width  = sv.line_width;
+    ctx->miter_limit = sv.miter_limit;
+    ctx->op          = sv.op;
+    ctx->line_cap    = sv.line_cap;
+    ctx->line_join   = VKVG_LINE_JOIN_MITER; /* the unsaved lineJoint field */
+    ctx->fill_rule   = sv.fill_rule;
+    ctx->mat         = sv.mat;
+    ctx->opacity     = sv.opacity;
+    if (sv.pattern) {
+        if (sv.pattern != ctx->pattern) {
+            /* _update_cur_pattern: the gradient again, with the restored matrix */
+            VkvgPattern last = ctx->pattern;
+            ctx->pattern     = sv.pattern; /* takes the saved reference */
+            ctx->grad_on     = false;
+            snap_gradient(ctx, sv.pattern);
+            if (last)
+                vkvg_pattern_destroy(last);
+        } else {
+            vkvg_pattern_destroy(sv.pattern);
+        }
+    } else {
+        ctx->cur_color = sv.cur_color;
+        set_solid(ctx);
+    }
 }
 
 /* ---- state (src/vkvg_context.c:1004-1140) */
@@ -1316,6 +1474,9 @@ void vkvg_set_source(VkvgContext ctx, VkvgPattern pat) {
     vkvg_pattern_reference(pat);
     set_solid(ctx);
     ctx->pattern = pat;
+    snap_gradient(ctx, pat);
+}
+static void snap_gradient(VkvgContext ctx, VkvgPattern pat) {
     if (pat->type != VKVG_PATTERN_TYPE_LINEAR) {
         ctx->status = VKVG_STATUS_PATTERN_TYPE_MISMATCH;
         return;

@@ -157,7 +157,9 @@ vkvg_status_t vkvg_gb300_debug_coverage(VkvgContext ctx, uint32_t i, int32_t *ou
     A.rgba     = s->d_rgba;
     A.cov_out  = p.dbg.as<int32_t>();
     A.cov_draw = i;
-    if (gb_launch_raster(p.st, &A, 0) != cudaSuccess)
+    gb_clip_args CA;
+    memset(&CA, 0, sizeof(CA));
+    if (gb_launch_raster(p.st, &A, &CA, 0, 0) != cudaSuccess)
         return VKVG_STATUS_DEVICE_ERROR;
     gb_count_launch(1);
     if (cudaStreamSynchronize(p.st) != cudaSuccess)
@@ -381,6 +383,11 @@ vkvg_status_t vkvg_gb300_replay_stream(VkvgContext ctx, const uint32_t *cmds, ui
         case VKVG_CMD_FILL: vkvg_fill(ctx); break;
         case VKVG_CMD_STROKE: vkvg_stroke(ctx); break;
         case VKVG_CMD_CLEAR: vkvg_clear(ctx); break;
+        case VKVG_CMD_CLIP: vkvg_clip(ctx); break;
+        case VKVG_CMD_CLIP_PRESERVE: vkvg_clip_preserve(ctx); break;
+        case VKVG_CMD_RESET_CLIP: vkvg_reset_clip(ctx); break;
+        case VKVG_CMD_SAVE: vkvg_save(ctx); break;
+        case VKVG_CMD_RESTORE: vkvg_restore(ctx); break;
         case VKVG_CMD_FILL_PRESERVE: vkvg_fill_preserve(ctx); break;
         case VKVG_CMD_STROKE_PRESERVE: vkvg_stroke_preserve(ctx); break;
         case VKVG_CMD_SET_SOURCE_RGB: NEED(3); vkvg_set_source_rgb(ctx, A[a], A[a + 1], A[a + 2]); a += 3; break;

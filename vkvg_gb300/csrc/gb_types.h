@@ -34,6 +34,27 @@
 #define GB_DRAW_STROKE  2u
 #define GB_DRAW_PAINT   3u
 #define GB_DRAW_CLEAR   4u
+/* clip: vkvg keeps it in the stencil, a clip bit and six save bits per
+   sample, plus a full copy of the stencil for every further six saves
+   (src/vkvg_context.c:1251-1512).  Here the surface holds it as bit planes,
+   one bit per sample: the visibility plane (the inverse of the clip bit), six
+   save planes (the save bits) and, per stencil copy, an image of seven planes
+   (visibility, then the six save planes).
+     CLIP_EO / CLIP_NZ   visibility &= the path's coverage (geometry as a fill)
+     CLIP_RESET          visibility = all, save planes = 0 (so does CLEAR)
+     CLIP_SAVE    src=p  save plane p = clip bit (= ~visibility)
+     CLIP_RESTORE src=p  visibility = ~save plane p
+     CLIP_STORE   src=k  image k = visibility and the save planes
+     CLIP_LOAD    src=k  visibility and the save planes = image k */
+#define GB_DRAW_CLIP_EO      5u
+#define GB_DRAW_CLIP_NZ      6u
+#define GB_DRAW_CLIP_RESET   7u
+#define GB_DRAW_CLIP_SAVE    8u
+#define GB_DRAW_CLIP_RESTORE 9u
+#define GB_DRAW_CLIP_STORE   10u
+#define GB_DRAW_CLIP_LOAD    11u
+#define GB_CLIP_SAVE_PLANES  6u
+#define GB_CLIP_IMAGE_PLANES 7u
 
 /* operators (vkvg_operator_t) */
 #define GB_OP_CLEAR      0u

@@ -124,6 +124,16 @@ struct _vkvg_surface_t {
     uint32_t     *d_samples; /* [nrows][wpad] premultiplied RGBA8 */
     uint32_t     *d_rgba;    /* [height][width] resolved */
     uint32_t     *d_out;     /* [height][width] unpremultiplied, staged for write_to_memory */
+    /* the stencil as bit planes, one bit per sample, [band rows][clip_wpr]
+       words each: d_clip is the visibility plane; clip_planes holds the six
+       save planes, then seven planes per stencil image */
+    uint32_t     *d_clip;
+    uint32_t      clip_wpr;               /* words per sample row */
+    size_t        plane_words;            /* words per plane */
+    DevBuf        clip_planes;
+    bool          clip_active = false;    /* visibility may not be all ones */
+    uint8_t       save_nz     = 0;        /* bit p: save plane p may be nonzero */
+    std::vector<uint8_t> clip_images;     /* per image: save_nz bits, 0x80 = visibility not all ones */
     std::mutex    mtx;
 };
 
@@ -139,6 +149,25 @@ struct PathState {
     bool     closed       = false;
     bool     pending      = false; /* a curve segment is open */
     uint32_t pending_from = 0;
+};
+
+/* clip states, vkvg_clip_state_t (src/vkvg_context_internal.h:95-99) */
+#define GB_CLIP_NONE  0x00u
+#define GB_CLIP_CLEAR 0x01u
+#define GB_CLIP_CLIP  0x02u
+#define GB_CLIP_SAVED 0x06u
+/* one vkvg_save level, vkvg_context_save_t (src/vkvg_context_internal.h:101-124):
+   the line join is not kept (vkvg_restore sets the field it never saved) */
+struct gb_saved_state {
+    float              line_width, miter_limit, dash_offset, opacity;
+    vkvg_line_cap_t    line_cap;
+    vkvg_fill_rule_t   fill_rule;
+    vkvg_operator_t    op;
+    vkvg_matrix_t      mat;
+    std::vector<float> dashes;
+    uint32_t           cur_color;
+    VkvgPattern        pattern; /* referenced while saved */
+    uint8_t            clip_state;
 };
 
 struct _vkvg_context_t {
@@ -162,6 +191,11 @@ struct _vkvg_context_t {
     VkvgPattern        pattern     = nullptr; /* source pattern, null for the solid colour */
     bool               grad_on     = false;   /* the source is a gradient snapshot */
     gb_grad            grad_snap;             /* as of vkvg_set_source (opacity filled per draw) */
+
+    /* clip and save/restore (vkvg's curClipState, curSavBit, pSavedCtxs) */
+    uint8_t                     clip_state = GB_CLIP_NONE;
+    uint8_t                     sav_bit    = 0;
+    std::vector<gb_saved_state> saved;
 
     PathState ps;
     FrameHost frame;

@@ -21,6 +21,17 @@ struct gb_raster_args {
     uint32_t        cov_draw;
     const uint32_t *gsrc;   /* gradient source images [n][H][W], premultiplied RGBA8 */
 };
+/* the clip planes, a kernel parameter of their own (read by the clipping
+   variant only; kept out of gb_raster_args, whose size the register
+   allocation of the other variants is sensitive to) */
+struct gb_clip_args {
+    uint32_t *clip;        /* visibility plane [band rows][clip_wpr] */
+    uint32_t *clip_planes; /* save planes, then stencil images, plane_words apart */
+    size_t    plane_words;
+    uint32_t  clip_wpr;
+    uint32_t  clip_load; /* at frame start: 0 all visible, 1 load the plane,
+                            2 all visible and save planes zeroed */
+};
 
 extern "C" {
 /* one gradient source image: out[y * W + x] = premultiplied RGBA8 of g at pixel (x, y) */
@@ -96,7 +107,8 @@ cudaError_t gb_launch_bin(cudaStream_t st, int scatter, uint32_t nedges, const i
                           uint32_t ndraws, uint32_t W, uint32_t samples, uint32_t nrows, uint32_t *cell, int4 *recs,
                           uint32_t nunits);
 
-cudaError_t gb_launch_raster(cudaStream_t st, const gb_raster_args *a, int gradients);
+cudaError_t gb_launch_raster(cudaStream_t st, const gb_raster_args *a, const gb_clip_args *c, int gradients,
+                             int clipping);
 cudaError_t gb_launch_pmath_eval(cudaStream_t st, int fn, const float *a, const float *b, float *out, uint64_t n);
 }
 

@@ -354,14 +354,84 @@ cudaError_t Pipeline::run(const FrameHost &f, _vkvg_surface_t *surf, bool timing
     A.ndraws     = ndraw;
     A.draw_first = 0;
     A.init_mode  = 0;
+    /* clip planes: follow which of them may hold anything but their reset
+       value through the frame's draws; a frame that touches a nontrivial
+       plane, or has any clip draw, runs the clipping variant */
+    bool     clip_use = surf->clip_active, act = surf->clip_active;
+    uint8_t  snz      = surf->save_nz;
+    uint32_t nimg     = (uint32_t)surf->clip_images.size();
+    for (const gb_draw &d : f.draws) {
+        switch (d.kind) {
+        case GB_DRAW_CLIP_EO:
+        case GB_DRAW_CLIP_NZ: act = true; clip_use = true; break;
+        case GB_DRAW_CLEAR:
+            clip_use |= act || snz;
+            act = false;
+            snz = 0;
+            break;
+        case GB_DRAW_CLIP_RESET:
+            clip_use = true;
+            act      = false;
+            snz      = 0;
+            break;
+        case GB_DRAW_CLIP_SAVE:
+            clip_use = true;
+            snz      = (uint8_t)(act ? snz | (1u << d.src) : snz & ~(1u << d.src));
+            break;
+        case GB_DRAW_CLIP_RESTORE:
+            clip_use = true;
+            act      = (snz >> d.src) & 1u;
+            break;
+        case GB_DRAW_CLIP_STORE:
+            clip_use = true;
+            if (d.src >= surf->clip_images.size())
+                surf->clip_images.resize(d.src + 1, 0);
+            surf->clip_images[d.src] = (uint8_t)(snz | (act ? 0x80u : 0u));
+            nimg                     = std::max(nimg, d.src + 1);
+            break;
+        case GB_DRAW_CLIP_LOAD: {
+            clip_use          = true;
+            const uint8_t img = d.src < surf->clip_images.size() ? surf->clip_images[d.src] : 0;
+            act               = (img & 0x80u) != 0;
+            snz               = (uint8_t)(img & 0x3Fu);
+            break;
+        }
+        default: break;
+        }
+    }
+    const bool reset0 = ndraw > 0 && f.draws[0].kind == GB_DRAW_CLEAR && surf->save_nz;
+    if (clip_use) {
+        /* planes keep their contents when the store grows */
+        const size_t need = (GB_CLIP_SAVE_PLANES + (size_t)GB_CLIP_IMAGE_PLANES * nimg) * surf->plane_words * 4;
+        DevBuf      &cp   = surf->clip_planes;
+        if (need > cp.cap) {
+            void *np = nullptr;
+            if (cudaMalloc(&np, need) != cudaSuccess)
+                return cudaErrorMemoryAllocation;
+            CK(cudaMemsetAsync(np, 0, need, st));
+            if (cp.p)
+                CK(cudaMemcpyAsync(np, cp.p, cp.cap, cudaMemcpyDeviceToDevice, st));
+            CK(cudaStreamSynchronize(st));
+            cp.release();
+            cp.p   = np;
+            cp.cap = need;
+        }
+    }
+    gb_clip_args CA;
+    CA.clip        = surf->d_clip;
+    CA.clip_planes = surf->clip_planes.as<uint32_t>();
+    CA.plane_words = surf->plane_words;
+    CA.clip_wpr    = surf->clip_wpr;
+    CA.clip_load   = surf->clip_active ? 1u : 0u;
     if (ndraw > 0) {
         const gb_draw &d0 = f.draws[0];
         if (d0.kind == GB_DRAW_CLEAR) {
             A.init_mode  = 1;
             A.init_color = 0;
             A.draw_first = 1;
+            CA.clip_load = reset0 ? 2u : 0u; /* a clear also resets the stencil */
         } else if (d0.kind == GB_DRAW_PAINT && (d0.op == GB_OP_OVER || d0.op == GB_OP_SOURCE) &&
-                   (d0.src >> 24) == 255u) {
+                   (d0.src >> 24) == 255u && d0.gsrc == 0 && !surf->clip_active) {
             A.init_mode  = 1;
             A.init_color = d0.src;
             A.draw_first = 1;
@@ -384,7 +454,9 @@ cudaError_t Pipeline::run(const FrameHost &f, _vkvg_surface_t *surf, bool timing
         gb_count_launch(ngrad);
         A.gsrc = gsrc.as<uint32_t>();
     }
-    CK(gb_launch_raster(st, &A, ngrad > 0));
+    CK(gb_launch_raster(st, &A, &CA, ngrad > 0, clip_use));
+    surf->clip_active = act;
+    surf->save_nz     = snz;
     gb_count_launch(1);
     if (timing)
         CK(cudaEventRecord(evs[4], st));

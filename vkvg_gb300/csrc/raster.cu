@@ -169,8 +169,9 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
 struct draw_cursor {
     uint32_t d0, amask;
 };
-__device__ __forceinline__ void cur_load(draw_cursor &c, const gb_raster_args &A, size_t cb, uint32_t dhi,
-                                         uint32_t l, uint32_t *ct) {
+template <bool CLIP>
+__device__ __forceinline__ void cur_load(draw_cursor &c, const gb_raster_args &A, size_t cb, uint32_t dhi, uint32_t l,
+                                         uint32_t *ct) {
     const uint32_t dl  = c.d0 + l;
     bool           act = false;
     uint32_t       kind = 0, lo = 0, hi = 0, src = 0, op = 0, gs = 0;
@@ -182,7 +183,9 @@ __device__ __forceinline__ void cur_load(draw_cursor &c, const gb_raster_args &A
         gs               = D.gsrc;
         lo               = A.cell_off[cb + dl];
         hi               = A.cell_off[cb + dl + 1];
-        act              = kind == GB_DRAW_PAINT || kind == GB_DRAW_CLEAR || lo != hi;
+        /* paint, clear and the clip kinds act on every band; the others only
+           where they have geometry */
+        act = kind == GB_DRAW_PAINT || (CLIP ? kind >= GB_DRAW_CLEAR : kind == GB_DRAW_CLEAR) || lo != hi;
     }
     __syncwarp();
     ct[l]       = kind;
@@ -193,6 +196,7 @@ __device__ __forceinline__ void cur_load(draw_cursor &c, const gb_raster_args &A
     ct[160 + l] = gs;
     c.amask    = __ballot_sync(0xffffffffu, act);
 }
+template <bool CLIP>
 __device__ __forceinline__ bool cur_next(draw_cursor &c, const gb_raster_args &A, size_t cb, uint32_t dhi, uint32_t l,
                                          uint32_t *ct, uint32_t *d, uint32_t *kind, uint32_t *lo, uint32_t *hi,
                                          uint32_t *slot) {
@@ -200,7 +204,7 @@ __device__ __forceinline__ bool cur_next(draw_cursor &c, const gb_raster_args &A
         c.d0 += 32;
         if (c.d0 >= dhi)
             return false;
-        cur_load(c, A, cb, dhi, l, ct);
+        cur_load<CLIP>(c, A, cb, dhi, l, ct);
     }
     const int j = __ffs(c.amask) - 1;
     c.amask &= c.amask - 1;
@@ -211,7 +215,19 @@ __device__ __forceinline__ bool cur_next(draw_cursor &c, const gb_raster_args &A
     *hi   = ct[64 + j];
     return true;
 }
-__device__ __forceinline__ bool is_geom(uint32_t kind) { return kind != GB_DRAW_PAINT && kind != GB_DRAW_CLEAR; }
+/* the stencil's save bits of a word go to zero (vkvg_reset_clip / vkvg_clear
+   clear the whole stencil attachment) */
+__device__ __forceinline__ void clip_zero_planes(uint32_t *cpl, size_t pw) {
+#pragma unroll
+    for (int p = 0; p < GB_CLIP_SAVE_PLANES; p++)
+        cpl[p * pw] = 0u;
+}
+/* kinds whose records are staged (the variant without clipping sees no clip draws) */
+template <bool CLIP> __device__ __forceinline__ bool is_geom(uint32_t kind) {
+    if (CLIP)
+        return kind <= GB_DRAW_STROKE || kind == GB_DRAW_CLIP_EO || kind == GB_DRAW_CLIP_NZ;
+    return kind != GB_DRAW_PAINT && kind != GB_DRAW_CLEAR;
+}
 
 /* one edge crossing sample row sy (band row rr): add dir at the last tile
    sample left of the crossing, so that the suffix sum from sample c is the
@@ -245,69 +261,6 @@ __device__ __forceinline__ void acc_row(int32_t x0, int32_t y0, int32_t x1, int3
     flag[p >> 6] = 1;
 }
 
-/* Runs with crossings (counters at cp, slot rotation v), right to left in
-   groups of four samples; a group is skipped when no lane of the warp has a
-   sample to blend in it (about three groups in ten of a mixed warp for
-   scribble-like paths), which the vote decides for the whole warp.  Fills
-   blend where (w & fmask) != 0 (fmask 1: even-odd, ~0: non-zero). */
-template <int M>
-__device__ __forceinline__ void fill_run(uint32_t (&col)[32], const int4 *cp, uint32_t v, int32_t E, int32_t fmask,
-                                         const blend_k &B) {
-    int32_t w = E;
-#pragma unroll
-    for (int q = 7; q >= 0; q--) {
-        const int4    x  = cp[q ^ v];
-        const int32_t w3 = w + x.w, w2 = w3 + x.z, w1 = w2 + x.y, w0 = w1 + x.x;
-        const bool    p3 = (w3 & fmask) != 0, p2 = (w2 & fmask) != 0, p1 = (w1 & fmask) != 0, p0 = (w0 & fmask) != 0;
-        w                = w0;
-        if (__any_sync(0xffffffffu, p0 | p1 | p2 | p3)) {
-            const uint32_t n3 = blend<M>(col[4 * q + 3], B), n2 = blend<M>(col[4 * q + 2], B);
-            const uint32_t n1 = blend<M>(col[4 * q + 1], B), n0 = blend<M>(col[4 * q], B);
-            col[4 * q + 3]    = p3 ? n3 : col[4 * q + 3];
-            col[4 * q + 2]    = p2 ? n2 : col[4 * q + 2];
-            col[4 * q + 1]    = p1 ? n1 : col[4 * q + 1];
-            col[4 * q]        = p0 ? n0 : col[4 * q];
-        }
-    }
-}
-/* strokes: blend w times (w = covering triangles), one pass per blend; the
-   number of passes is the warp's largest w, so that every lane takes part in
-   every vote */
-template <int M>
-__device__ __forceinline__ void stroke_run(uint32_t (&col)[32], const int4 *cp, uint32_t v, int32_t E,
-                                           const blend_k &B) {
-    int32_t kmax = 1, kwarp = 1;
-    for (int32_t rep = 0; rep < kwarp; rep++) {
-        int32_t w = E;
-#pragma unroll
-        for (int q = 7; q >= 0; q--) {
-            const int4    x  = cp[q ^ v];
-            const int32_t w3 = w + x.w, w2 = w3 + x.z, w1 = w2 + x.y, w0 = w1 + x.x;
-            w                = w0;
-            kmax             = max(kmax, max(max(w3, w2), max(w1, w0)));
-            const bool p3 = w3 > rep, p2 = w2 > rep, p1 = w1 > rep, p0 = w0 > rep;
-            if (__any_sync(0xffffffffu, p0 | p1 | p2 | p3)) {
-                const uint32_t n3 = blend<M>(col[4 * q + 3], B), n2 = blend<M>(col[4 * q + 2], B);
-                const uint32_t n1 = blend<M>(col[4 * q + 1], B), n0 = blend<M>(col[4 * q], B);
-                col[4 * q + 3]    = p3 ? n3 : col[4 * q + 3];
-                col[4 * q + 2]    = p2 ? n2 : col[4 * q + 2];
-                col[4 * q + 1]    = p1 ? n1 : col[4 * q + 1];
-                col[4 * q]        = p0 ? n0 : col[4 * q];
-            }
-        }
-        if (rep == 0)
-            kwarp = __reduce_max_sync(0xffffffffu, kmax);
-    }
-}
-/* a run without crossings: blend every sample k times */
-template <int M> __device__ __forceinline__ void uniform_run(uint32_t (&col)[32], int32_t k, const blend_k &B) {
-    for (int32_t rep = 0; rep < k; rep++) {
-#pragma unroll
-        for (int c = 0; c < 32; c++)
-            col[c] = blend<M>(col[c], B);
-    }
-}
-
 /* row y of gradient source image gs - 1, from column x */
 __device__ __forceinline__ const uint32_t *grad_row(const gb_raster_args &A, uint32_t gs, uint32_t y, int32_t x) {
     return A.gsrc + ((size_t)(gs - 1) * A.H + y) * A.W + x;
@@ -320,27 +273,58 @@ __device__ __forceinline__ void load_src4(const uint32_t *row, int c0, int ncols
     for (int k = 0; k < 4; k++)
         s[k] = c0 + k < ncols ? row[c0 + k] : 0u;
 }
-__device__ __forceinline__ void fill_run_grad(uint32_t (&col)[32], const int4 *cp, uint32_t v, int32_t E,
-                                              int32_t fmask, const uint32_t *row, int ncols) {
+/* one sample's blend: the draw's solid source (mode M, constants B) or, for
+   G, the sample's own gradient source word s */
+template <int M, bool G> __device__ __forceinline__ uint32_t blend_any(uint32_t d, const blend_k &B, uint32_t s) {
+    if (G)
+        return blend_src(d, s);
+    return blend<M>(d, B);
+}
+/* blend group q of a run where p_k is set */
+template <int M, bool G>
+__device__ __forceinline__ void blend_group(uint32_t (&col)[32], int q, bool p0, bool p1, bool p2, bool p3,
+                                            const blend_k &B, const uint32_t *row, int ncols) {
+    uint32_t sv[4] = {0u, 0u, 0u, 0u};
+    if (G)
+        load_src4(row, 4 * q, ncols, sv);
+    const uint32_t n3 = blend_any<M, G>(col[4 * q + 3], B, sv[3]), n2 = blend_any<M, G>(col[4 * q + 2], B, sv[2]);
+    const uint32_t n1 = blend_any<M, G>(col[4 * q + 1], B, sv[1]), n0 = blend_any<M, G>(col[4 * q], B, sv[0]);
+    col[4 * q + 3]    = p3 ? n3 : col[4 * q + 3];
+    col[4 * q + 2]    = p2 ? n2 : col[4 * q + 2];
+    col[4 * q + 1]    = p1 ? n1 : col[4 * q + 1];
+    col[4 * q]        = p0 ? n0 : col[4 * q];
+}
+
+/* Runs with crossings (counters at cp, slot rotation v), right to left in
+   groups of four samples; a group is skipped when no lane of the warp has a
+   sample to blend in it (about three groups in ten of a mixed warp for
+   scribble-like paths), which the vote decides for the whole warp.  Fills
+   blend where (w & fmask) != 0 (fmask 1: even-odd, ~0: non-zero); with CL,
+   only samples whose bit of the clip word cm is set. */
+template <int M, bool G, bool CL>
+__device__ __forceinline__ void fill_run(uint32_t (&col)[32], const int4 *cp, uint32_t v, int32_t E, int32_t fmask,
+                                         const blend_k &B, const uint32_t *row, int ncols, uint32_t cm) {
     int32_t w = E;
 #pragma unroll
     for (int q = 7; q >= 0; q--) {
         const int4    x  = cp[q ^ v];
         const int32_t w3 = w + x.w, w2 = w3 + x.z, w1 = w2 + x.y, w0 = w1 + x.x;
-        const bool    p3 = (w3 & fmask) != 0, p2 = (w2 & fmask) != 0, p1 = (w1 & fmask) != 0, p0 = (w0 & fmask) != 0;
-        w                = w0;
-        if (__any_sync(0xffffffffu, p0 | p1 | p2 | p3)) {
-            uint32_t sv[4];
-            load_src4(row, 4 * q, ncols, sv);
-            col[4 * q + 3] = p3 ? blend_src(col[4 * q + 3], sv[3]) : col[4 * q + 3];
-            col[4 * q + 2] = p2 ? blend_src(col[4 * q + 2], sv[2]) : col[4 * q + 2];
-            col[4 * q + 1] = p1 ? blend_src(col[4 * q + 1], sv[1]) : col[4 * q + 1];
-            col[4 * q]     = p0 ? blend_src(col[4 * q], sv[0]) : col[4 * q];
+        bool          p3 = (w3 & fmask) != 0, p2 = (w2 & fmask) != 0, p1 = (w1 & fmask) != 0, p0 = (w0 & fmask) != 0;
+        if (CL) {
+            const uint32_t g = cm >> (4 * q);
+            p0 = p0 && (g & 1u), p1 = p1 && (g & 2u), p2 = p2 && (g & 4u), p3 = p3 && (g & 8u);
         }
+        w = w0;
+        if (__any_sync(0xffffffffu, p0 | p1 | p2 | p3))
+            blend_group<M, G>(col, q, p0, p1, p2, p3, B, row, ncols);
     }
 }
-__device__ __forceinline__ void stroke_run_grad(uint32_t (&col)[32], const int4 *cp, uint32_t v, int32_t E,
-                                                const uint32_t *row, int ncols) {
+/* strokes: blend w times (w = covering triangles), one pass per blend; the
+   number of passes is the warp's largest w, so that every lane takes part in
+   every vote */
+template <int M, bool G, bool CL>
+__device__ __forceinline__ void stroke_run(uint32_t (&col)[32], const int4 *cp, uint32_t v, int32_t E,
+                                           const blend_k &B, const uint32_t *row, int ncols, uint32_t cm) {
     int32_t kmax = 1, kwarp = 1;
     for (int32_t rep = 0; rep < kwarp; rep++) {
         int32_t w = E;
@@ -350,34 +334,55 @@ __device__ __forceinline__ void stroke_run_grad(uint32_t (&col)[32], const int4 
             const int32_t w3 = w + x.w, w2 = w3 + x.z, w1 = w2 + x.y, w0 = w1 + x.x;
             w                = w0;
             kmax             = max(kmax, max(max(w3, w2), max(w1, w0)));
-            const bool p3 = w3 > rep, p2 = w2 > rep, p1 = w1 > rep, p0 = w0 > rep;
-            if (__any_sync(0xffffffffu, p0 | p1 | p2 | p3)) {
-                uint32_t sv[4];
-                load_src4(row, 4 * q, ncols, sv);
-                col[4 * q + 3] = p3 ? blend_src(col[4 * q + 3], sv[3]) : col[4 * q + 3];
-                col[4 * q + 2] = p2 ? blend_src(col[4 * q + 2], sv[2]) : col[4 * q + 2];
-                col[4 * q + 1] = p1 ? blend_src(col[4 * q + 1], sv[1]) : col[4 * q + 1];
-                col[4 * q]     = p0 ? blend_src(col[4 * q], sv[0]) : col[4 * q];
+            bool p3 = w3 > rep, p2 = w2 > rep, p1 = w1 > rep, p0 = w0 > rep;
+            if (CL) {
+                const uint32_t g = cm >> (4 * q);
+                p0 = p0 && (g & 1u), p1 = p1 && (g & 2u), p2 = p2 && (g & 4u), p3 = p3 && (g & 8u);
             }
+            if (__any_sync(0xffffffffu, p0 | p1 | p2 | p3))
+                blend_group<M, G>(col, q, p0, p1, p2, p3, B, row, ncols);
         }
         if (rep == 0)
             kwarp = __reduce_max_sync(0xffffffffu, kmax);
     }
 }
-__device__ __forceinline__ void uniform_run_grad(uint32_t (&col)[32], int32_t k, const uint32_t *row, int ncols) {
+/* a run without crossings: blend every sample (with CL, every sample inside
+   the clip) k times */
+template <int M, bool G, bool CL>
+__device__ __forceinline__ void uniform_run(uint32_t (&col)[32], int32_t k, const blend_k &B, const uint32_t *row,
+                                            int ncols, uint32_t cm) {
     for (int32_t rep = 0; rep < k; rep++) {
 #pragma unroll
         for (int q = 0; q < 8; q++) {
-            uint32_t sv[4];
-            load_src4(row, 4 * q, ncols, sv);
+            uint32_t sv[4] = {0u, 0u, 0u, 0u};
+            if (G)
+                load_src4(row, 4 * q, ncols, sv);
 #pragma unroll
-            for (int e = 0; e < 4; e++)
-                col[4 * q + e] = blend_src(col[4 * q + e], sv[e]);
+            for (int e = 0; e < 4; e++) {
+                const int      c  = 4 * q + e;
+                const uint32_t nb = blend_any<M, G>(col[c], B, sv[e]);
+                col[c]            = (!CL || ((cm >> c) & 1u)) ? nb : col[c];
+            }
         }
     }
 }
+/* a clip draw on a run with crossings: the bits of the samples it covers */
+__device__ __forceinline__ uint32_t clip_bits(const int4 *cp, uint32_t v, int32_t E, int32_t fmask) {
+    int32_t  w    = E;
+    uint32_t bits = 0;
+#pragma unroll
+    for (int q = 7; q >= 0; q--) {
+        const int4    x  = cp[q ^ v];
+        const int32_t w3 = w + x.w, w2 = w3 + x.z, w1 = w2 + x.y, w0 = w1 + x.x;
+        bits |= ((w0 & fmask) ? 1u : 0u) << (4 * q) | ((w1 & fmask) ? 2u : 0u) << (4 * q) |
+                ((w2 & fmask) ? 4u : 0u) << (4 * q) | ((w3 & fmask) ? 8u : 0u) << (4 * q);
+        w = w0;
+    }
+    return bits;
+}
 
-template <bool GRAD> __global__ void __launch_bounds__(XT_THREADS, 1) gb_raster(gb_raster_args A) {
+template <bool GRAD, bool CLIP>
+__global__ void __launch_bounds__(XT_THREADS, 1) gb_raster(gb_raster_args A, gb_clip_args C) {
     extern __shared__ __align__(16) int32_t smem[];
 
     const uint32_t t = threadIdx.x, wi = t >> 5, l = t & 31;
@@ -424,6 +429,16 @@ template <bool GRAD> __global__ void __launch_bounds__(XT_THREADS, 1) gb_raster(
         for (int c = 0; c < 32; c++)
             col[c] = c < ncols ? srow[c] : 0u;
     }
+    /* this lane's clip word: one bit per sample of its run */
+    const size_t cwi = (size_t)(row_ok ? R : 0) * C.clip_wpr + (uint32_t)(X0 + col0) / 32u;
+    uint32_t     cm  = 0xFFFFFFFFu;
+    /* live save planes of this lane's word: plane p at cpl[p * plane_words] */
+    uint32_t *const cpl = CLIP ? C.clip_planes + cwi : nullptr;
+    const bool      cwr = CLIP && row_ok && ncols > 0; /* this lane owns a clip word */
+    if (CLIP && C.clip_load == 1 && ncols > 0)
+        cm = C.clip[cwi];
+    if (CLIP && C.clip_load == 2 && cwr && !dbg)
+        clip_zero_planes(cpl, C.plane_words);
     for (uint32_t i = t; i < SM_WORDS; i += XT_THREADS)
         smem[i] = 0;
     const uint32_t sm_base = (uint32_t)__cvta_generic_to_shared(smem);
@@ -455,14 +470,14 @@ template <bool GRAD> __global__ void __launch_bounds__(XT_THREADS, 1) gb_raster(
     uint32_t   *ct = reinterpret_cast<uint32_t *>(smem + SM_CUR + wi * 192);
     draw_cursor cur;
     cur.d0 = dlo;
-    cur_load(cur, A, cb, dhi, l, ct);
+    cur_load<CLIP>(cur, A, cb, dhi, l, ct);
     uint32_t nx_d = 0, nx_kind = 0, nx_lo = 0, nx_hi = 0, nx_slot = 0;
-    bool     nx_have = cur_next(cur, A, cb, dhi, l, ct, &nx_d, &nx_kind, &nx_lo, &nx_hi, &nx_slot);
+    bool     nx_have = cur_next<CLIP>(cur, A, cb, dhi, l, ct, &nx_d, &nx_kind, &nx_lo, &nx_hi, &nx_slot);
     {
         while (nx_have) {
             const uint32_t d = nx_d, kind = nx_kind, lo = nx_lo, hi = nx_hi;
             const uint32_t src = ct[96 + nx_slot], op = ct[128 + nx_slot], gs = ct[160 + nx_slot];
-            nx_have = cur_next(cur, A, cb, dhi, l, ct, &nx_d, &nx_kind, &nx_lo, &nx_hi, &nx_slot); /* lookahead */
+            nx_have = cur_next<CLIP>(cur, A, cb, dhi, l, ct, &nx_d, &nx_kind, &nx_lo, &nx_hi, &nx_slot); /* lookahead */
             int            bm;
             if (kind == GB_DRAW_PAINT) {
                 const blend_k B = make_blend(src, op, &bm);
@@ -472,19 +487,56 @@ template <bool GRAD> __global__ void __launch_bounds__(XT_THREADS, 1) gb_raster(
                     continue;
                 }
                 if (GRAD && gs)
-                    uniform_run_grad(col, 1, grad_row(A, gs, R / rpp, X0 + col0), ncols);
+                    uniform_run<BM_ADD, GRAD, CLIP>(col, 1, B, grad_row(A, gs, R / rpp, X0 + col0), ncols, cm);
                 else if (bm == BM_ADD)
-                    uniform_run<BM_ADD>(col, 1, B);
+                    uniform_run<BM_ADD, false, CLIP>(col, 1, B, nullptr, ncols, cm);
                 else if (bm == BM_SADD)
-                    uniform_run<BM_SADD>(col, 1, B);
+                    uniform_run<BM_SADD, false, CLIP>(col, 1, B, nullptr, ncols, cm);
                 else
-                    uniform_run<BM_SSUB>(col, 1, B);
+                    uniform_run<BM_SSUB, false, CLIP>(col, 1, B, nullptr, ncols, cm);
                 continue;
             }
-            if (kind == GB_DRAW_CLEAR) {
+            if (kind == GB_DRAW_CLEAR) { /* colour and the whole stencil: clip and save planes */
 #pragma unroll
                 for (int c = 0; c < 32; c++)
                     col[c] = 0u;
+                cm = 0xFFFFFFFFu;
+                if (CLIP && cwr && !dbg)
+                    clip_zero_planes(cpl, C.plane_words);
+                continue;
+            }
+            if (CLIP && kind >= GB_DRAW_CLIP_RESET) { /* stencil plane operations, parameter in src */
+                if (CLIP && cwr && !dbg) {
+                    const size_t pw = C.plane_words;
+                    if (kind == GB_DRAW_CLIP_RESET) {
+                        cm = 0xFFFFFFFFu;
+                        clip_zero_planes(cpl, pw);
+                    } else if (kind == GB_DRAW_CLIP_SAVE) {
+                        cpl[src * pw] = ~cm;
+                    } else if (kind == GB_DRAW_CLIP_RESTORE) {
+                        cm = ~cpl[src * pw];
+                    } else {
+                        uint32_t *img = cpl + (size_t)(GB_CLIP_SAVE_PLANES + GB_CLIP_IMAGE_PLANES * src) * pw;
+                        if (kind == GB_DRAW_CLIP_STORE) {
+                            img[0] = cm;
+#pragma unroll
+                            for (int p = 0; p < GB_CLIP_SAVE_PLANES; p++)
+                                img[(1 + p) * pw] = cpl[p * pw];
+                        } else {
+                            cm = img[0];
+#pragma unroll
+                            for (int p = 0; p < GB_CLIP_SAVE_PLANES; p++)
+                                cpl[p * pw] = img[(1 + p) * pw];
+                        }
+                    }
+                }
+                continue;
+            }
+            /* clip draws reach only the clipping variant */
+            const bool is_clip = CLIP && (kind == GB_DRAW_CLIP_EO || kind == GB_DRAW_CLIP_NZ);
+            if (is_clip && lo == hi) { /* the clip path has nothing in this band */
+                if (CLIP && !dbg)
+                    cm = 0u;
                 continue;
             }
             if (hi > A.nunits || lo > hi) {
@@ -500,7 +552,7 @@ template <bool GRAD> __global__ void __launch_bounds__(XT_THREADS, 1) gb_raster(
             const uint32_t su = min(hi - lo, (uint32_t)STAGE_CAP);
             if ((sb ? stg_d1 : stg_d0) != d)
                 stage_cell(sb, d, lo, su);
-            if (nx_have && is_geom(nx_kind) && nx_lo < nx_hi && nx_hi <= A.nunits)
+            if (nx_have && is_geom<CLIP>(nx_kind) && nx_lo < nx_hi && nx_hi <= A.nunits)
                 stage_cell(sb ^ 1u, nx_d, nx_lo, min(nx_hi - nx_lo, (uint32_t)STAGE_CAP));
             if (mbar_wait(bar0 + 8 * sb, (stg_par >> sb) & 1u)) {
                 stg_pend &= ~(1u << sb);
@@ -562,17 +614,24 @@ template <bool GRAD> __global__ void __launch_bounds__(XT_THREADS, 1) gb_raster(
                 /* no crossing in the strip: every run has the uniform winding Er */
                 int32_t k = 0;
                 if (row_ok)
-                    k = kind == GB_DRAW_STROKE ? max(Er, 0) : kind == GB_DRAW_FILL_EO ? (Er & 1) : (Er != 0);
+                    k = kind == GB_DRAW_STROKE                                             ? max(Er, 0)
+                        : (kind == GB_DRAW_FILL_EO || (CLIP && kind == GB_DRAW_CLIP_EO)) ? (Er & 1)
+                                                                                         : (Er != 0);
+                if (is_clip) { /* the whole run is inside the clip path or outside it */
+                    if (CLIP && !k)
+                        cm = 0u;
+                    continue;
+                }
                 if (!__any_sync(0xffffffffu, k > 0))
                     continue;
                 if (GRAD && gs)
-                    uniform_run_grad(col, k, grad_row(A, gs, R / rpp, X0 + col0), ncols);
+                    uniform_run<BM_ADD, GRAD, CLIP>(col, k, B, grad_row(A, gs, R / rpp, X0 + col0), ncols, cm);
                 else if (bm == BM_ADD)
-                    uniform_run<BM_ADD>(col, k, B);
+                    uniform_run<BM_ADD, false, CLIP>(col, k, B, nullptr, ncols, cm);
                 else if (bm == BM_SADD)
-                    uniform_run<BM_SADD>(col, k, B);
+                    uniform_run<BM_SADD, false, CLIP>(col, k, B, nullptr, ncols, cm);
                 else
-                    uniform_run<BM_SSUB>(col, k, B);
+                    uniform_run<BM_SSUB, false, CLIP>(col, k, B, nullptr, ncols, cm);
                 continue;
             }
             /* this lane's 32 counters: totals first, the blend reads them again;
@@ -589,28 +648,31 @@ template <bool GRAD> __global__ void __launch_bounds__(XT_THREADS, 1) gb_raster(
             const int32_t Lp   = __shfl_xor_sync(0xffffffffu, L, 1);
             const int32_t E    = Er + (hh == 0 ? Lp : 0); /* winding entering this run from the right */
             const bool    work = row_ok && (nzr != 0 || E != 0);
-            if (__any_sync(0xffffffffu, work)) {
+            if (is_clip) { /* the clip region keeps the samples the path covers */
+                if (CLIP)
+                    cm &= clip_bits(cp, v_lane, E, kind == GB_DRAW_CLIP_EO ? 1 : -1);
+            } else if (__any_sync(0xffffffffu, work)) {
+                const int32_t fmask = kind == GB_DRAW_FILL_EO ? 1 : -1;
                 if (GRAD && gs) {
                     const uint32_t *grow = grad_row(A, gs, R / rpp, X0 + col0);
                     if (kind == GB_DRAW_STROKE)
-                        stroke_run_grad(col, cp, v_lane, E, grow, ncols);
+                        stroke_run<BM_ADD, GRAD, CLIP>(col, cp, v_lane, E, B, grow, ncols, cm);
                     else
-                        fill_run_grad(col, cp, v_lane, E, kind == GB_DRAW_FILL_EO ? 1 : -1, grow, ncols);
+                        fill_run<BM_ADD, GRAD, CLIP>(col, cp, v_lane, E, fmask, B, grow, ncols, cm);
                 } else if (kind == GB_DRAW_STROKE) {
                     if (bm == BM_ADD)
-                        stroke_run<BM_ADD>(col, cp, v_lane, E, B);
+                        stroke_run<BM_ADD, false, CLIP>(col, cp, v_lane, E, B, nullptr, ncols, cm);
                     else if (bm == BM_SADD)
-                        stroke_run<BM_SADD>(col, cp, v_lane, E, B);
+                        stroke_run<BM_SADD, false, CLIP>(col, cp, v_lane, E, B, nullptr, ncols, cm);
                     else
-                        stroke_run<BM_SSUB>(col, cp, v_lane, E, B);
+                        stroke_run<BM_SSUB, false, CLIP>(col, cp, v_lane, E, B, nullptr, ncols, cm);
                 } else {
-                    const int32_t fmask = kind == GB_DRAW_FILL_EO ? 1 : -1;
                     if (bm == BM_ADD)
-                        fill_run<BM_ADD>(col, cp, v_lane, E, fmask, B);
+                        fill_run<BM_ADD, false, CLIP>(col, cp, v_lane, E, fmask, B, nullptr, ncols, cm);
                     else if (bm == BM_SADD)
-                        fill_run<BM_SADD>(col, cp, v_lane, E, fmask, B);
+                        fill_run<BM_SADD, false, CLIP>(col, cp, v_lane, E, fmask, B, nullptr, ncols, cm);
                     else
-                        fill_run<BM_SSUB>(col, cp, v_lane, E, fmask, B);
+                        fill_run<BM_SSUB, false, CLIP>(col, cp, v_lane, E, fmask, B, nullptr, ncols, cm);
                 }
             }
 #pragma unroll
@@ -628,6 +690,8 @@ template <bool GRAD> __global__ void __launch_bounds__(XT_THREADS, 1) gb_raster(
             mbar_wait(bar0 + 8 * b, ((stg_par >> b) & 1u) ^ 1u);
     if (dbg)
         return;
+    if (cwr)
+        C.clip[cwi] = cm;
 
     /* write back samples */
     if (ncols == 32) {
@@ -777,12 +841,17 @@ extern "C" cudaError_t gb_launch_unpremultiply(cudaStream_t st, const uint32_t *
     return cudaGetLastError();
 }
 
-extern "C" cudaError_t gb_launch_raster(cudaStream_t st, const gb_raster_args *a, int gradients) {
+extern "C" cudaError_t gb_launch_raster(cudaStream_t st, const gb_raster_args *a, const gb_clip_args *c, int gradients, int clipping) {
     static bool configured = false;
     if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(gb_raster<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, RASTER_SMEM);
+        cudaError_t e = cudaFuncSetAttribute(gb_raster<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             RASTER_SMEM);
         if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(gb_raster<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, RASTER_SMEM);
+            e = cudaFuncSetAttribute(gb_raster<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, RASTER_SMEM);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(gb_raster<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, RASTER_SMEM);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(gb_raster<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, RASTER_SMEM);
         if (e != cudaSuccess)
             return e;
         configured = true;
@@ -790,10 +859,14 @@ extern "C" cudaError_t gb_launch_raster(cudaStream_t st, const gb_raster_args *a
     if (a->nbands == 0)
         return cudaSuccess;
     dim3 grid((a->W + XT_W - 1) / XT_W, a->nbands);
-    /* frames without gradient draws run the variant that has no gradient code */
-    if (gradients)
-        gb_raster<true><<<grid, XT_THREADS, RASTER_SMEM, st>>>(*a);
+    /* frames without gradient draws or clipping run the variants without that code */
+    if (gradients && clipping)
+        gb_raster<true, true><<<grid, XT_THREADS, RASTER_SMEM, st>>>(*a, *c);
+    else if (gradients)
+        gb_raster<true, false><<<grid, XT_THREADS, RASTER_SMEM, st>>>(*a, *c);
+    else if (clipping)
+        gb_raster<false, true><<<grid, XT_THREADS, RASTER_SMEM, st>>>(*a, *c);
     else
-        gb_raster<false><<<grid, XT_THREADS, RASTER_SMEM, st>>>(*a);
+        gb_raster<false, false><<<grid, XT_THREADS, RASTER_SMEM, st>>>(*a, *c);
     return cudaGetLastError();
 }

@@ -197,6 +197,109 @@ def gradient_mix(n_items=14, size=144, seed=9, samples=4):
     return {"name": "gradient_mix", "width": size, "height": size, "samples": samples, "ops": ops, "paths": n_items}
 
 
+def clip_mix(n_items=10, size=128, seed=13, samples=4, flush_every=0):
+    """Clip regions and the state stack: even-odd and non-zero clip paths,
+    clip_preserve then fill, nested save / clip / restore, eight nested
+    saves (the last two past the six stencil save bits), reset_clip, a clear
+    with an active clip, restore re-snapping a gradient under a restored
+    matrix, and the line join that vkvg_restore resets.  flush_every > 0
+    flushes after that many items, so clip state crosses frames."""
+    r = SplitMix64(seed)
+    u = lambda lo, hi: lo + (hi - lo) * r.rnd()
+
+    def blob(n=2):
+        ops = [("move_to", u(0, size), u(0, size))]
+        for _ in range(n):
+            ops.append(("curve_to",) + tuple(u(-0.1 * size, 1.1 * size) for _ in range(6)))
+        return ops + [("close_path",)]
+
+    def rect(lo, hi):
+        x, y = u(lo, hi), u(lo, hi)
+        return [("rectangle", x, y, u(0.2, 0.6) * size, u(0.2, 0.6) * size)]
+
+    def paint_layer():
+        return [("set_source_rgba", r.rnd(), r.rnd(), r.rnd(), u(0.5, 1.0)), ("paint",)]
+
+    def shape_layer(i):
+        return blob(2 + i % 2) + [("set_fill_rule", i % 2), ("set_source_rgba", r.rnd(), r.rnd(), r.rnd(), u(0.4, 1.0)),
+                                  ("fill_preserve",), ("set_line_width", u(1, 6)),
+                                  ("set_source_rgba", r.rnd(), r.rnd(), r.rnd(), u(0.6, 1.0)), ("stroke",)]
+
+    ops = [("set_source_rgb", 1.0, 1.0, 1.0), ("paint",)]
+    for i in range(n_items):
+        mode = i % 5
+        if mode == 0:  # one clip level: even-odd blob, paint and shapes inside
+            ops += [("save",)] + blob(3) + [("set_fill_rule", 0), ("clip",)] + paint_layer() + shape_layer(i)
+            ops += [("restore",)]
+        elif mode == 1:  # nested: non-zero rect, then a blob with clip_preserve + fill
+            ops += [("save",)] + rect(0, size * 0.5) + [("set_fill_rule", 1), ("clip",), ("save",)]
+            ops += blob(2) + [("set_fill_rule", i % 2), ("clip_preserve",),
+                              ("set_source_rgba", r.rnd(), r.rnd(), r.rnd(), 0.8), ("fill",)]
+            ops += paint_layer()[:1] + [("set_line_width", u(2, 8))] + blob(2) + [("stroke",), ("restore",)]
+            ops += shape_layer(i) + [("restore",)] + shape_layer(i + 1)
+        elif mode == 2:  # eight nested saves, each clipping further
+            ops += [("set_line_join", 1)]
+            for k in range(8):
+                ops += [("save",)] + rect(-0.1 * size, 0.7 * size) + [("set_fill_rule", k % 2), ("clip",)]
+                ops += [("set_source_rgba", r.rnd(), r.rnd(), r.rnd(), 0.35), ("paint",)]
+            for k in range(8):
+                ops += [("restore",)] + shape_layer(i + k)[-6:]
+            ops += [("set_line_width", 5.0)] + blob(2) + [("stroke",)]  # miter join after restore
+        elif mode == 3:  # reset_clip inside a saved clip, gradient re-snapped by restore
+            ops += [("identity_matrix",), ("translate", u(-10, 10), u(-10, 10))]
+            ops += [("set_source_linear", 0.0, 0.0, float(size), u(0, size),
+                     [(0.0, r.rnd(), r.rnd(), r.rnd(), 0.9), (1.0, r.rnd(), r.rnd(), r.rnd(), 0.6)], None)]
+            ops += [("save",)] + blob(2) + [("clip",), ("paint",), ("rotate", u(-0.6, 0.6))]
+            ops += [("set_source_rgba", r.rnd(), r.rnd(), r.rnd(), 0.7), ("reset_clip",)] + blob(2) + [("fill",)]
+            ops += [("restore",), ("paint",) if i % 2 else ("fill",), ("identity_matrix",)]
+        else:  # clip without save, then a clear with the clip active, then reset
+            ops += blob(2) + [("set_fill_rule", 0), ("clip",)] + paint_layer() + shape_layer(i)
+            if i == 4:
+                ops += [("clear",)] + paint_layer()
+            ops += [("reset_clip",)] + shape_layer(i + 3)
+        if flush_every and (i + 1) % flush_every == 0:
+            ops.append(("flush",))
+    return {"name": "clip_mix", "width": size, "height": size, "samples": samples, "ops": ops, "paths": n_items}
+
+
+def vkvg_clip_cases(width=1024, height=800, samples=4):
+    """The call sequences of vkvg's clip and save/restore demo programs
+    (tests/clip.c: clipped_paint, clipped_paint2, clipped_transformed,
+    clip_transformed, test_clip, test_clip2 for both fill rules where vkvg
+    has both; tests/save_restore.c: twenty nested save / translate / stroke
+    levels), one scene each on a fresh surface."""
+    red, green, blue = ("set_source_rgb", 1.0, 0.0, 0.0), ("set_source_rgb", 0.0, 1.0, 0.0), \
+        ("set_source_rgb", 0.0, 0.0, 1.0)
+    base = lambda fr: [("set_fill_rule", fr), red, ("paint",)]
+    rect = lambda x, y, w, h: ("rectangle", float(x), float(y), float(w), float(h))
+    out = []
+    for fr, tag in ((1, "nz"), (0, "eo")):
+        out.append(("clipped_paint_" + tag, base(fr) + [green, rect(100, 100, 300, 200), ("clip",), ("paint",)]))
+        out.append(("clipped_paint2_" + tag, base(fr) + [green, rect(100, 100, 300, 200), ("clip",), ("paint",),
+                                                         ("reset_clip",), rect(200, 200, 300, 200), blue, ("paint",)]))
+        out.append(("clipped_transformed_" + tag, base(fr) + [("rotate", 0.2), green, rect(100, 100, 300, 200),
+                                                              ("clip",), ("paint",)]))
+    out.append(("clip_transformed_nz", base(1) + [("rotate", 0.1), green, rect(100, 100, 300, 200), ("clip",),
+                                                  ("paint",), ("translate", 200.0, 100.0), blue, ("paint",)]))
+    star = [("move_to", 10.0, 10.0)] + [("line_to", float(x), float(y)) for x, y in
+                                        ((400, 150), (900, 10), (700, 450), (900, 750), (500, 650), (100, 800),
+                                         (150, 400))]
+    out.append(("test_clip", [("clear",), ("set_fill_rule", 0)] + star +
+                [("clip_preserve",), ("set_operator", 0), ("fill_preserve",), ("clip",), ("set_operator", 2), red,
+                 ("paint",)]))
+    out.append(("test_clip2", [("clear",), ("set_fill_rule", 1), rect(50, 50, 500, 500), ("clip",), red, ("paint",),
+                               ("save",), rect(100, 100, 350, 350), ("clip",), ("save",),
+                               ("set_source_rgb", 1.0, 1.0, 0.0), ("paint",), rect(200, 200, 200, 200), ("clip",),
+                               green, ("paint",), ("restore",), rect(350, 350, 420, 420), blue, ("fill",),
+                               ("restore",)]))
+    rec = []
+    for depth in range(1, 21):
+        rec += [("save",), ("translate", 5.0, 5.0), rect(depth, depth, 200, 200), green, ("stroke",)]
+    out.append(("save_restore", rec + [("restore",)] * 20))
+    return [{"name": n, "width": width, "height": height, "samples": samples, "ops": ops, "paths": 0}
+            for n, ops in out]
+
+
 def play(ctx, ops):
     """Replay a scene's calls on a context object with vkvg method names."""
     for op in ops:
@@ -222,6 +325,7 @@ CMD = {
     "rel_move_to": 0x0504, "rel_line_to": 0x0505, "rel_curve_to": 0x050A, "rel_quadratic_to": 0x050B,
     "paint": 0x0201, "fill": 0x0202, "stroke": 0x0203, "clear": 0x0206, "fill_preserve": 0x0602,
     "stroke_preserve": 0x0603, "set_source_rgb": 0x0801, "set_source_rgba": 0x0802, "set_source_color": 0x0803,
+    "save": 0x0001, "restore": 0x0002, "clip": 0x0204, "reset_clip": 0x0205, "clip_preserve": 0x0604,
 }
 
 
