@@ -257,9 +257,9 @@ vkvg_public void vkvg_transform(VkvgContext ctx, const vkvg_matrix_t *matrix);
 vkvg_public void vkvg_set_matrix(VkvgContext ctx, const vkvg_matrix_t *matrix);
 vkvg_public void vkvg_get_matrix(VkvgContext ctx, vkvg_matrix_t *const matrix);
 
-/* patterns: include/vkvg.h:1749-1900 for linear gradients (up to 16 colour
-   stops; stops beyond that return VKVG_STATUS_INVALID_INDEX where vkvg would
-   write past its array) */
+/* patterns: include/vkvg.h:1749-1900 for linear and radial gradients (up to
+   16 colour stops; stops beyond that return VKVG_STATUS_INVALID_INDEX where
+   vkvg would write past its array) */
 vkvg_public vkvg_status_t       vkvg_pattern_status(VkvgPattern pat);
 vkvg_public VkvgPattern         vkvg_pattern_reference(VkvgPattern pat);
 vkvg_public uint32_t            vkvg_pattern_get_reference_count(VkvgPattern pat);
@@ -268,6 +268,10 @@ vkvg_public VkvgPattern         vkvg_pattern_create_linear(float x0, float y0, f
 vkvg_public vkvg_status_t       vkvg_pattern_edit_linear(VkvgPattern pat, float x0, float y0, float x1, float y1);
 vkvg_public vkvg_status_t       vkvg_pattern_get_linear_points(VkvgPattern pat, float *x0, float *y0, float *x1,
                                                                float *y1);
+vkvg_public VkvgPattern   vkvg_pattern_create_radial(float cx0, float cy0, float radius0, float cx1, float cy1,
+                                                     float radius1);
+vkvg_public vkvg_status_t vkvg_pattern_edit_radial(VkvgPattern pat, float cx0, float cy0, float radius0, float cx1,
+                                                   float cy1, float radius1);
 vkvg_public vkvg_status_t       vkvg_pattern_add_color_stop(VkvgPattern pat, float offset, float r, float g, float b,
                                                             float a);
 vkvg_public vkvg_status_t       vkvg_pattern_get_color_stop_count(VkvgPattern pat, uint32_t *count);

@@ -162,6 +162,8 @@ VKO_API vko_pattern *vko_pattern_reference(vko_pattern *pat);
 VKO_API uint32_t     vko_pattern_get_reference_count(vko_pattern *pat);
 VKO_API void         vko_pattern_destroy(vko_pattern *pat);
 VKO_API int          vko_pattern_edit_linear(vko_pattern *pat, float x0, float y0, float x1, float y1);
+VKO_API vko_pattern *vko_pattern_create_radial(float cx0, float cy0, float r0, float cx1, float cy1, float r1);
+VKO_API int vko_pattern_edit_radial(vko_pattern *pat, float cx0, float cy0, float r0, float cx1, float cy1, float r1);
 VKO_API int          vko_pattern_add_color_stop(vko_pattern *pat, float offset, float r, float g, float b, float a);
 VKO_API int          vko_pattern_get_color_stop_count(vko_pattern *pat, uint32_t *count);
 VKO_API void         vko_pattern_set_matrix(vko_pattern *pat, const vko_matrix *m);

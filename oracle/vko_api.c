@@ -302,9 +302,40 @@ void     vko_pattern_destroy(vko_pattern *pat) {
         return;
     free(pat);
 }
+/* vkvg_pattern_edit_radial / create_radial, src/vkvg_pattern.c:95-134 */
+int vko_pattern_edit_radial(vko_pattern *pat, float cx0, float cy0, float r0, float cx1, float cy1, float r1) {
+    if (vko_pattern_status(pat))
+        return vko_pattern_status(pat);
+    if (pat->type != 3)
+        return VKO_STATUS_PATTERN_TYPE_MISMATCH;
+    v2 c0 = {cx0, cy0}, c1 = {cx1, cy1};
+    if (r0 > r1 - 1.0f)
+        r0 = r1 - 1.0f;
+    v2    u = v2_sub(c0, c1);
+    float l = v2_len(u);
+    if (l + r0 + 1.0f >= r1) {
+        v2 v = v2_div(u, l);
+        c0   = v2_add(c1, v2_mul(v, r1 - r0 - 1.0f));
+    }
+    float cp[8] = {c0.x, c0.y, r0, 0.0f, c1.x, c1.y, r1, 0.0f};
+    memcpy(pat->cp, cp, sizeof(cp));
+    return VKO_STATUS_SUCCESS;
+}
+vko_pattern *vko_pattern_create_radial(float cx0, float cy0, float r0, float cx1, float cy1, float r1) {
+    vko_pattern *p = (vko_pattern *)calloc(1, sizeof(vko_pattern));
+    if (!p)
+        return &s_pattern_no_memory;
+    p->refs = 1;
+    p->type = 3; /* VKVG_PATTERN_TYPE_RADIAL */
+    vko_matrix_init_identity(&p->matrix);
+    vko_pattern_edit_radial(p, cx0, cy0, r0, cx1, cy1, r1);
+    return p;
+}
 int vko_pattern_edit_linear(vko_pattern *pat, float x0, float y0, float x1, float y1) {
     if (vko_pattern_status(pat))
         return vko_pattern_status(pat);
+    if (pat->type != 2)
+        return VKO_STATUS_PATTERN_TYPE_MISMATCH;
     pat->cp[0] = x0;
     pat->cp[1] = y0;
     pat->cp[2] = x1;
@@ -358,26 +389,45 @@ void        vko_set_source(vko_context *ctx, vko_pattern *pat) {
     snap_gradient(ctx, pat);
 }
 static void snap_gradient(vko_context *ctx, vko_pattern *pat) {
+    if (pat->type != 2 && pat->type != 3) {
+        ctx->status = VKO_STATUS_PATTERN_TYPE_MISMATCH;
+        return;
+    }
     if (pat->count < 2) {
         ctx->status = VKO_STATUS_PATTERN_INVALID_GRADIENT;
         return;
     }
     vko_grad *g = &ctx->grad_snap;
     memset(g, 0, sizeof(*g));
-    float x0 = pat->cp[0], y0 = pat->cp[1], x1 = pat->cp[2], y1 = pat->cp[3];
+    /* grad.cp[0] is g->cp[0..3], grad.cp[1] is g->cp[4..7] */
+    memcpy(g->cp, pat->cp, sizeof(g->cp));
+    vko_matrix inv;
+    vko_matrix_init_identity(&inv);
     if (pat->has_matrix) {
-        vko_matrix m = pat->matrix;
-        if (vko_matrix_invert(&m) != VKO_STATUS_SUCCESS)
-            vko_matrix_init_identity(&m);
-        vko_matrix_transform_point(&m, &x0, &y0);
-        vko_matrix_transform_point(&m, &x1, &y1);
+        inv = pat->matrix;
+        if (vko_matrix_invert(&inv) != VKO_STATUS_SUCCESS)
+            vko_matrix_init_identity(&inv);
+        vko_matrix_transform_point(&inv, &g->cp[0], &g->cp[1]);
     }
-    vko_matrix_transform_point(&ctx->mat, &x0, &y0);
-    vko_matrix_transform_point(&ctx->mat, &x1, &y1);
-    g->cp[0] = x0;
-    g->cp[1] = y0;
-    g->cp[2] = x1;
-    g->cp[3] = y1;
+    vko_matrix_transform_point(&ctx->mat, &g->cp[0], &g->cp[1]);
+    if (pat->type == 2) {
+        if (pat->has_matrix)
+            vko_matrix_transform_point(&inv, &g->cp[2], &g->cp[3]);
+        vko_matrix_transform_point(&ctx->mat, &g->cp[2], &g->cp[3]);
+    } else {
+        if (pat->has_matrix)
+            vko_matrix_transform_point(&inv, &g->cp[4], &g->cp[5]);
+        vko_matrix_transform_point(&ctx->mat, &g->cp[4], &g->cp[5]);
+        /* radii: transform_distance with grad.cp[0].w as y for both
+           (src/vkvg_context_internal.c:815-821) */
+        if (pat->has_matrix) {
+            vko_matrix_transform_distance(&inv, &g->cp[2], &g->cp[3]);
+            vko_matrix_transform_distance(&inv, &g->cp[6], &g->cp[3]);
+        }
+        vko_matrix_transform_distance(&ctx->mat, &g->cp[2], &g->cp[3]);
+        vko_matrix_transform_distance(&ctx->mat, &g->cp[6], &g->cp[3]);
+    }
+    g->type  = pat->type;
     g->w     = (float)ctx->surf->width;
     g->h     = (float)ctx->surf->height;
     g->count = pat->count;

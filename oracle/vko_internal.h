@@ -36,7 +36,8 @@ typedef struct {
    stops, premultiplied stop colours, the draw's opacity */
 #define VKO_GRAD_STOPS 16
 typedef struct {
-    float    cp[4];
+    int      type; /* 2 linear, 3 radial (vkvg_pattern_type_t) */
+    float    cp[8];
     float    w, h;
     uint32_t count;
     float    opacity;
@@ -48,7 +49,7 @@ struct vko_pattern_t {
     int        status;
     uint32_t   refs;
     int        type, extend, filter;
-    float      cp[4];
+    float      cp[8];
     uint32_t   count;
     float      stops[VKO_GRAD_STOPS];
     float      colors[VKO_GRAD_STOPS * 4];

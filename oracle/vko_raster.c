@@ -430,14 +430,39 @@ static float g_smoothstep(float e0, float e1, float x) {
     return (t * t) * (3.0f - 2.0f * t);
 }
 static float g_mix(float x, float y, float a) { return x * (1.0f - a) + y * a; }
-static void  grad_src(const vko_grad *g, uint32_t px, uint32_t py, uint8_t s[4]) {
-    float p_x = ((float)px + 0.5f) / g->w, p_y = ((float)py + 0.5f) / g->h;
+/* RADIAL, shaders/vkvg_main.frag:109-144: the ray from centre 0 through p
+   is cut by circle 1; the gradient parameter is (|p - c0| - r0) over the
+   distance of that point from c0 less r0 (1 if the ray misses).
+   normalize(v) is v / length(v). */
+static float radial_t(const vko_grad *g, float p_x, float p_y) {
+    float c0x = g->cp[0] / g->w, c0y = g->cp[1] / g->h;
+    float c1x = g->cp[4] / g->w, c1y = g->cp[5] / g->h;
+    float r0 = g->cp[2] / g->w, r1 = g->cp[6] / g->w;
+    float gradlen = 1.0f;
+    float diffx = c0x - c1x, diffy = c0y - c1y;
+    float vx = p_x - c0x, vy = p_y - c0y;
+    float vlen = sqrtf(vx * vx + vy * vy);
+    float rdx = vx / vlen, rdy = vy / vlen;
+    float a    = rdx * rdx + rdy * rdy;
+    float b    = 2.0f * (rdx * diffx + rdy * diffy);
+    float cc   = (diffx * diffx + diffy * diffy) - r1 * r1;
+    float disc = b * b - 4.0f * a * cc;
+    if (disc >= 0.0f) {
+        float t     = (-b + sqrtf(fabsf(disc))) / (2.0f * a);
+        float projx = c0x + rdx * t, projy = c0y + rdy * t;
+        float qx = projx - c0x, qy = projy - c0y;
+        gradlen = sqrtf(qx * qx + qy * qy) - r0;
+    }
+    return (vlen - r0) / gradlen;
+}
+/* LINEAR: signed distance along the axis in units of its length */
+static float linear_t(const vko_grad *g, float p_x, float p_y) {
+    float dist;
     float p0x = g->cp[0] / g->w, p0y = g->cp[1] / g->h;
     float p1x = g->cp[2] / g->w, p1y = g->cp[3] / g->h;
     float dx = p1x - p0x, dy = p1y - p0y;
     float l  = sqrtf(dx * dx + dy * dy);
     float ux = dx / l, uy = dy / l;
-    float dist;
     if (uy == 0.0f) {
         float t = (p_x - p0x) / l;
         dist    = ux < 0.0f ? -t : t;
@@ -448,6 +473,11 @@ static void  grad_src(const vko_grad *g, uint32_t px, uint32_t py, uint8_t s[4])
         if (uy < 0.0f)
             dist = -dist;
     }
+    return dist;
+}
+static void grad_src(const vko_grad *g, uint32_t px, uint32_t py, uint8_t s[4]) {
+    float p_x  = ((float)px + 0.5f) / g->w, p_y = ((float)py + 0.5f) / g->h;
+    float dist = g->type == 3 ? radial_t(g, p_x, p_y) : linear_t(g, p_x, p_y);
     float c[4];
     float t0 = g_smoothstep(g->stops[0], g->stops[1], dist);
     for (int k = 0; k < 4; k++)

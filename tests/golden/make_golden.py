@@ -37,7 +37,8 @@ def golden_scenes():
             scenes.curve_heavy(n_paths=10, size=128, seed=1, n_min=3, n_max=6),
             scenes.api_mix(n_items=24, size=160, seed=5),
             scenes.gradient_mix(n_items=14, size=144, seed=9),
-            scenes.clip_mix(n_items=10, size=128, seed=13)]
+            scenes.clip_mix(n_items=10, size=128, seed=13),
+            scenes.gradient_mix(n_items=14, size=144, seed=9, radial=True)]
 
 STENCIL_OPS = 7
 FILL_KINDS = (0, 1, 5, 6)

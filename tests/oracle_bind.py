@@ -82,6 +82,8 @@ _SIGS = {
     "vko_pattern_get_reference_count": (_U, [_P]),
     "vko_pattern_destroy": (None, [_P]),
     "vko_pattern_edit_linear": (C.c_int, [_P, _F, _F, _F, _F]),
+    "vko_pattern_create_radial": (_P, [_F, _F, _F, _F, _F, _F]),
+    "vko_pattern_edit_radial": (C.c_int, [_P, _F, _F, _F, _F, _F, _F]),
     "vko_pattern_add_color_stop": (C.c_int, [_P, _F, _F, _F, _F, _F]),
     "vko_pattern_get_color_stop_count": (C.c_int, [_P, _P]),
     "vko_pattern_set_matrix": (None, [_P, _P]),
@@ -171,6 +173,17 @@ class OracleContext:
     def set_source_linear(self, x0, y0, x1, y1, stops, pmat=None):
         """a linear gradient pattern as the source (created, used, released)"""
         p = self.L.vko_pattern_create_linear(x0, y0, x1, y1)
+        for st in stops:
+            self.L.vko_pattern_add_color_stop(p, *st)
+        if pmat is not None:
+            mm = Matrix(*pmat)
+            self.L.vko_pattern_set_matrix(p, C.byref(mm))
+        self.L.vko_set_source(self.h, p)
+        self.L.vko_pattern_destroy(p)
+
+    def set_source_radial(self, cx0, cy0, r0, cx1, cy1, r1, stops, pmat=None):
+        """a radial gradient pattern as the source (created, used, released)"""
+        p = self.L.vko_pattern_create_radial(cx0, cy0, r0, cx1, cy1, r1)
         for st in stops:
             self.L.vko_pattern_add_color_stop(p, *st)
         if pmat is not None:

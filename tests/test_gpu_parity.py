@@ -187,12 +187,12 @@ def test_empty_and_degenerate_paths(gb, vko):
     assert np.array_equal(surf.image(), osurf.image())
 
 
-@pytest.mark.parametrize("samples", [4, 1])
-def test_gradient_sources_bit_exact(gb, vko, samples):
-    """linear gradient sources (more distinct gradients than one frame holds,
-    so the recording is flushed in between): samples and image equal the
-    oracle's"""
-    sc = scenes.gradient_mix(n_items=14, size=144, seed=9, samples=samples)
+@pytest.mark.parametrize("samples,radial", [(4, False), (1, False), (4, True), (1, True)])
+def test_gradient_sources_bit_exact(gb, vko, samples, radial):
+    """linear and radial gradient sources (more distinct gradients than one
+    frame holds, so the recording is flushed in between): samples and image
+    equal the oracle's"""
+    sc = scenes.gradient_mix(n_items=14, size=144, seed=9, samples=samples, radial=radial)
     dev, surf, ctx = pu.run_gpu(gb, sc)
     osurf, octx = pu.run_oracle(vko, sc)
     assert ctx.debug_counts()[5] == 0
@@ -285,3 +285,18 @@ def test_replay_stream_matches_calls(gb, which):
     assert st == 0
     ctx2.flush()
     assert np.array_equal(surf.samples_rgba(), surf2.samples_rgba())
+
+
+def test_radial_gradient_paint_bit_exact(gb, vko):
+    """one radial gradient painted over a non-square surface, focus inside
+    and focus pulled in by edit_radial, with a pattern matrix: the image
+    equals the oracle's"""
+    for args, pmat in (((60.0, 50.0, 5.0, 80.0, 64.0, 60.0), None),
+                       ((140.0, 10.0, 3.0, 70.0, 60.0, 40.0), (1.1, 0.1, -0.2, 0.9, 4.0, -3.0))):
+        stops = [(0.0, 1.0, 1.0, 0.0, 1.0), (0.5, 0.0, 0.5, 1.0, 0.8), (1.0, 0.2, 0.0, 0.4, 1.0)]
+        ops = [("translate", 3.0, 2.0), ("set_source_radial",) + args + (stops, pmat), ("paint",)]
+        sc = {"name": "radial_paint", "width": 160, "height": 128, "samples": 4, "ops": ops, "paths": 0}
+        dev, surf, ctx = pu.run_gpu(gb, sc)
+        osurf, octx = pu.run_oracle(vko, sc)
+        assert ctx.status() == 0 and ctx.debug_counts()[5] == 0
+        assert np.array_equal(surf.samples_rgba(), osurf.samples_rgba())

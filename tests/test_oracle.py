@@ -130,7 +130,8 @@ def small_scenes():
             scenes.curve_heavy(n_paths=10, size=128, seed=1, n_min=3, n_max=6),
             scenes.api_mix(n_items=24, size=160, seed=5),
             scenes.gradient_mix(n_items=14, size=144, seed=9),
-            scenes.clip_mix(n_items=10, size=128, seed=13)]
+            scenes.clip_mix(n_items=10, size=128, seed=13),
+            scenes.gradient_mix(n_items=14, size=144, seed=9, radial=True)]
 
 
 @pytest.mark.parametrize("sc", small_scenes(), ids=lambda s: s["name"])
@@ -285,6 +286,64 @@ def test_linear_gradient_kat():
         assert np.array_equal(got, want)
 
 
+def test_radial_gradient_kat():
+    """a radial gradient painted on a cleared surface equals an independent
+    numpy fp32 evaluation of vkvg's RADIAL fragment expression
+    (shaders/vkvg_main.frag:109-144) after vkvg_pattern_edit_radial's focus
+    adjustment (src/vkvg_pattern.c:95-119): a focus inside the outer circle,
+    and one that edit_radial pulls inside"""
+    f = np.float32
+    W, H = 48, 40
+    stops = [(0.0, 1.0, 1.0, 0.0, 1.0), (0.5, 0.0, 0.5, 1.0, 0.8), (1.0, 0.2, 0.0, 0.4, 1.0)]
+    for (cx0, cy0, r0, cx1, cy1, r1) in ((20.0, 18.0, 3.0, 24.0, 20.0, 30.0), (40.0, 5.0, 2.0, 22.0, 20.0, 16.0)):
+        surf = ob.OracleSurface(W, H, 4)
+        ctx = surf.context()
+        ctx.set_source_radial(cx0, cy0, r0, cx1, cy1, r1, stops)
+        ctx.paint()
+        ctx.flush()
+        got = surf.premult()
+        ctx.destroy()
+        surf.destroy()
+        # edit_radial
+        r0, r1 = f(r0), f(r1)
+        if r0 > r1 - f(1):
+            r0 = r1 - f(1)
+        ux, uy = f(cx0) - f(cx1), f(cy0) - f(cy1)
+        l = np.sqrt(ux * ux + uy * uy)
+        c0x, c0y = f(cx0), f(cy0)
+        if l + r0 + f(1) >= r1:
+            k = r1 - r0 - f(1)
+            c0x, c0y = f(cx1) + (ux / l) * k, f(cy1) + (uy / l) * k
+        # fragment stage, per pixel centre
+        px = np.arange(W, dtype=f)[None, :].repeat(H, 0)
+        py = np.arange(H, dtype=f)[:, None].repeat(W, 1)
+        p_x, p_y = (px + f(0.5)) / f(W), (py + f(0.5)) / f(H)
+        a0x, a0y, a1x, a1y = c0x / f(W), c0y / f(H), f(cx1) / f(W), f(cy1) / f(H)
+        q0, q1 = r0 / f(W), r1 / f(W)
+        dfx, dfy = a0x - a1x, a0y - a1y
+        vx, vy = p_x - a0x, p_y - a0y
+        vlen = np.sqrt(vx * vx + vy * vy)
+        rx, ry = vx / vlen, vy / vlen
+        a = rx * rx + ry * ry
+        b = f(2) * (rx * dfx + ry * dfy)
+        cc = (dfx * dfx + dfy * dfy) - q1 * q1
+        disc = b * b - f(4) * a * cc
+        with np.errstate(invalid="ignore"):
+            t = (-b + np.sqrt(np.abs(disc))) / (f(2) * a)
+            qx, qy = (a0x + rx * t) - a0x, (a0y + ry * t) - a0y
+            glen = np.where(disc >= 0, np.sqrt(qx * qx + qy * qy) - q0, f(1)).astype(f)
+        grad = (vlen - q0) / glen
+        cols = [np.array([al * r, al * g, al * bb, al], f) for (_, r, g, bb, al) in stops]
+        tt = _np_smoothstep(stops[0][0], stops[1][0], grad)
+        c = [_np_mix(cols[0][k], cols[1][k], tt) for k in range(4)]
+        for i in range(2, len(stops)):
+            tt = _np_smoothstep(stops[i - 1][0], stops[i][0], grad)
+            c = [_np_mix(c[k], cols[i][k], tt) for k in range(4)]
+        want = np.stack([np.rint(np.clip(np.nan_to_num(ck * f(255), nan=0.0), 0, 255)).astype(np.uint8)
+                         for ck in c], -1)
+        assert np.array_equal(got, want)
+
+
 def test_pattern_api_semantics():
     """vkvg's pattern object behaviour (src/vkvg_pattern.c) on both libraries:
     reference counts, stop count, type and the 16-stop limit"""
@@ -305,8 +364,17 @@ def test_pattern_api_semantics():
         assert f("pattern_get_color_stop_count")(p, C.byref(n)) == 0 and n.value == 16
         f("pattern_destroy")(p)
         assert f("pattern_get_reference_count")(p) == 1
+        assert f("pattern_edit_radial")(p, 0.0, 0.0, 1.0, 0.0, 0.0, 9.0) == 9  # PATTERN_TYPE_MISMATCH
         f("pattern_destroy")(p)
+        q = f("pattern_create_radial")(1.0, 2.0, 3.0, 4.0, 5.0, 20.0)
+        assert f("pattern_status")(q) == 0 and f("pattern_get_reference_count")(q) == 1
+        assert f("pattern_edit_linear")(q, 0.0, 0.0, 1.0, 1.0) == 9
+        assert f("pattern_edit_radial")(q, 0.0, 0.0, 30.0, 1.0, 1.0, 10.0) == 0  # radius0 clamped, focus moved
+        f("pattern_destroy")(q)
     L = vkvg_gb300.lib()
+    q = L.vkvg_pattern_create_radial(0.0, 0.0, 1.0, 0.0, 0.0, 5.0)
+    assert L.vkvg_pattern_get_type(q) == 3  # VKVG_PATTERN_TYPE_RADIAL
+    L.vkvg_pattern_destroy(q)
     p = L.vkvg_pattern_create_linear(0.0, 0.0, 1.0, 1.0)
     assert L.vkvg_pattern_get_type(p) == 2  # VKVG_PATTERN_TYPE_LINEAR
     L.vkvg_pattern_add_color_stop(p, 0.0, 1.0, 0.5, 0.25, 0.5)

@@ -107,6 +107,8 @@ SIGNATURES = {
     "vkvg_pattern_destroy": (None, [_P]),
     "vkvg_pattern_create_linear": (_P, [_F, _F, _F, _F]),
     "vkvg_pattern_edit_linear": (_I, [_P, _F, _F, _F, _F]),
+    "vkvg_pattern_create_radial": (_P, [_F, _F, _F, _F, _F, _F]),
+    "vkvg_pattern_edit_radial": (_I, [_P, _F, _F, _F, _F, _F, _F]),
     "vkvg_pattern_get_linear_points": (_I, [_P, _P, _P, _P, _P]),
     "vkvg_pattern_add_color_stop": (_I, [_P, _F, _F, _F, _F, _F]),
     "vkvg_pattern_get_color_stop_count": (_I, [_P, _P]),
@@ -279,6 +281,17 @@ class Context:
     def set_source_linear(self, x0, y0, x1, y1, stops, pmat=None):
         """a linear gradient pattern as the source (created, used, released)"""
         p = self.L.vkvg_pattern_create_linear(x0, y0, x1, y1)
+        for st in stops:
+            self.L.vkvg_pattern_add_color_stop(p, *st)
+        if pmat is not None:
+            mm = Matrix(*pmat)
+            self.L.vkvg_pattern_set_matrix(p, C.byref(mm))
+        self.L.vkvg_set_source(self.h, p)
+        self.L.vkvg_pattern_destroy(p)
+
+    def set_source_radial(self, cx0, cy0, r0, cx1, cy1, r1, stops, pmat=None):
+        """a radial gradient pattern as the source (created, used, released)"""
+        p = self.L.vkvg_pattern_create_radial(cx0, cy0, r0, cx1, cy1, r1)
         for st in stops:
             self.L.vkvg_pattern_add_color_stop(p, *st)
         if pmat is not None:

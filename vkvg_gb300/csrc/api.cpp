@@ -1354,6 +1354,42 @@ VkvgPattern vkvg_pattern_create_linear(float x0, float y0, float x1, float y1) {
     p->has_matrix = false;
     return p;
 }
+/* vkvg_pattern_edit_radial, src/vkvg_pattern.c:95-119: radius0 is kept
+   below radius1 - 1 and the focus circle is moved inside circle 1 */
+vkvg_status_t vkvg_pattern_edit_radial(VkvgPattern pat, float cx0, float cy0, float radius0, float cx1, float cy1,
+                                       float radius1) {
+    if (vkvg_pattern_status(pat))
+        return vkvg_pattern_status(pat);
+    if (pat->type != VKVG_PATTERN_TYPE_RADIAL)
+        return VKVG_STATUS_PATTERN_TYPE_MISMATCH;
+    if (radius0 > radius1 - 1.0f)
+        radius0 = radius1 - 1.0f;
+    const float ux = cx0 - cx1, uy = cy0 - cy1;
+    const float l = sqrtf(ux * ux + uy * uy);
+    if (l + radius0 + 1.0f >= radius1) {
+        const float vx = ux / l, vy = uy / l, k = radius1 - radius0 - 1.0f;
+        cx0 = cx1 + vx * k;
+        cy0 = cy1 + vy * k;
+    }
+    const float cp[8] = {cx0, cy0, radius0, 0.0f, cx1, cy1, radius1, 0.0f};
+    memcpy(pat->cp, cp, sizeof(cp));
+    return VKVG_STATUS_SUCCESS;
+}
+VkvgPattern vkvg_pattern_create_radial(float cx0, float cy0, float radius0, float cx1, float cy1, float radius1) {
+    _vkvg_pattern_t *p = new (std::nothrow) _vkvg_pattern_t();
+    if (!p)
+        return (VkvgPattern)&s_no_memory;
+    p->status     = VKVG_STATUS_SUCCESS;
+    p->refs       = 1;
+    p->type       = VKVG_PATTERN_TYPE_RADIAL;
+    p->extend     = VKVG_EXTEND_NONE;
+    p->filter     = VKVG_FILTER_FAST;
+    p->count      = 0;
+    p->matrix     = VKVG_IDENTITY_MATRIX;
+    p->has_matrix = false;
+    vkvg_pattern_edit_radial(p, cx0, cy0, radius0, cx1, cy1, radius1);
+    return p;
+}
 vkvg_status_t vkvg_pattern_status(VkvgPattern pat) { return pat ? pat->status : VKVG_STATUS_NULL_POINTER; }
 VkvgPattern   vkvg_pattern_reference(VkvgPattern pat) {
     if (!vkvg_pattern_status(pat))
@@ -1477,7 +1513,7 @@ void vkvg_set_source(VkvgContext ctx, VkvgPattern pat) {
     snap_gradient(ctx, pat);
 }
 static void snap_gradient(VkvgContext ctx, VkvgPattern pat) {
-    if (pat->type != VKVG_PATTERN_TYPE_LINEAR) {
+    if (pat->type != VKVG_PATTERN_TYPE_LINEAR && pat->type != VKVG_PATTERN_TYPE_RADIAL) {
         ctx->status = VKVG_STATUS_PATTERN_TYPE_MISMATCH;
         return;
     }
@@ -1487,20 +1523,34 @@ static void snap_gradient(VkvgContext ctx, VkvgPattern pat) {
     }
     gb_grad &g = ctx->grad_snap;
     memset(&g, 0, sizeof(g));
-    float x0 = pat->cp[0], y0 = pat->cp[1], x1 = pat->cp[2], y1 = pat->cp[3];
+    float *cp = g.cp; /* vkvg's grad.cp[0] = cp[0..3], grad.cp[1] = cp[4..7] */
+    memcpy(cp, pat->cp, sizeof(g.cp));
+    vkvg_matrix_t m = VKVG_IDENTITY_MATRIX;
     if (pat->has_matrix) {
-        vkvg_matrix_t m = pat->matrix;
+        m = pat->matrix;
         if (vkvg_matrix_invert(&m) != VKVG_STATUS_SUCCESS)
             m = VKVG_IDENTITY_MATRIX;
-        vkvg_matrix_transform_point(&m, &x0, &y0);
-        vkvg_matrix_transform_point(&m, &x1, &y1);
+        vkvg_matrix_transform_point(&m, &cp[0], &cp[1]);
     }
-    vkvg_matrix_transform_point(&ctx->mat, &x0, &y0);
-    vkvg_matrix_transform_point(&ctx->mat, &x1, &y1);
-    g.cp[0] = x0;
-    g.cp[1] = y0;
-    g.cp[2] = x1;
-    g.cp[3] = y1;
+    vkvg_matrix_transform_point(&ctx->mat, &cp[0], &cp[1]);
+    if (pat->type == VKVG_PATTERN_TYPE_LINEAR) {
+        if (pat->has_matrix)
+            vkvg_matrix_transform_point(&m, &cp[2], &cp[3]);
+        vkvg_matrix_transform_point(&ctx->mat, &cp[2], &cp[3]);
+    } else {
+        if (pat->has_matrix)
+            vkvg_matrix_transform_point(&m, &cp[4], &cp[5]);
+        vkvg_matrix_transform_point(&ctx->mat, &cp[4], &cp[5]);
+        /* both radii go through transform_distance with cp[0].w as their y
+           (src/vkvg_context_internal.c:815-821) */
+        if (pat->has_matrix) {
+            vkvg_matrix_transform_distance(&m, &cp[2], &cp[3]);
+            vkvg_matrix_transform_distance(&m, &cp[6], &cp[3]);
+        }
+        vkvg_matrix_transform_distance(&ctx->mat, &cp[2], &cp[3]);
+        vkvg_matrix_transform_distance(&ctx->mat, &cp[6], &cp[3]);
+    }
+    g.type  = (uint32_t)pat->type;
     g.w     = (float)ctx->surf->width;
     g.h     = (float)ctx->surf->height;
     g.count = pat->count;

@@ -79,14 +79,18 @@ typedef struct {
     uint32_t gsrc;     /* 0: the solid colour src; i + 1: gradient source image i of the frame */
 } gb_draw;
 
-/* A linear gradient as vkvg's fragment stage sees it (shaders/vkvg_main.frag
-   LINEAR case, data of _update_cur_pattern): control points transformed by
-   the pattern's inverse matrix and the CTM at vkvg_set_source time, in
-   pixels; surface size; stops; premultiplied stop colours; the draw's
-   opacity.  One per distinct source image of a frame. */
-#define GB_GRAD_STOPS 16
+/* A gradient as vkvg's fragment stage sees it (shaders/vkvg_main.frag LINEAR
+   and RADIAL cases, data of _update_cur_pattern): control points transformed
+   by the pattern's inverse matrix and the CTM at vkvg_set_source time, in
+   pixels, in vkvg's layout of two vec4 (linear: x0 y0 x1 y1; radial:
+   cx0 cy0 r0 - and cx1 cy1 r1 -); surface size; stops; premultiplied stop
+   colours; the draw's opacity.  One per distinct source image of a frame. */
+#define GB_GRAD_STOPS  16
+#define GB_GRAD_LINEAR 2u /* vkvg_pattern_type_t values */
+#define GB_GRAD_RADIAL 3u
 typedef struct {
-    float    cp[4]; /* x0 y0 x1 y1 */
+    uint32_t type;
+    float    cp[8];
     float    w, h;
     uint32_t count;
     float    opacity;

@@ -108,7 +108,7 @@ struct _vkvg_pattern_t {
     vkvg_pattern_type_t type;
     vkvg_extend_t       extend;
     vkvg_filter_t       filter;
-    float               cp[4];
+    float               cp[8]; /* vkvg_gradient_t.cp: two vec4 */
     uint32_t            count;
     float               stops[GB_GRAD_STOPS];
     float               colors[GB_GRAD_STOPS * 4]; /* premultiplied */

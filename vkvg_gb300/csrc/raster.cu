@@ -765,8 +765,46 @@ __device__ __forceinline__ float g_smoothstep(float e0, float e1, float x) {
 __device__ __forceinline__ float g_mix(float x, float y, float a) {
     return __fadd_rn(__fmul_rn(x, __fsub_rn(1.0f, a)), __fmul_rn(y, a));
 }
+/* RADIAL (shaders/vkvg_main.frag:109-144): the focus ray from c0 through p
+   meets circle 1 at the projection; the gradient runs from r0 to that
+   distance (1 where the ray misses).  normalize(v) = v / length(v); dot and
+   distance in GLSL's left-to-right order. */
+__device__ float    gb_linear_t(const gb_grad &g, float p_x, float p_y);
+__device__ uint32_t gb_grad_word(const gb_grad &g, float dist);
+__device__ float gb_radial_t(const gb_grad &g, float p_x, float p_y) {
+    const float c0x = __fdiv_rn(g.cp[0], g.w), c0y = __fdiv_rn(g.cp[1], g.h);
+    const float c1x = __fdiv_rn(g.cp[4], g.w), c1y = __fdiv_rn(g.cp[5], g.h);
+    const float r0 = __fdiv_rn(g.cp[2], g.w), r1 = __fdiv_rn(g.cp[6], g.w);
+    float       grad_len = 1.0f;
+    const float dfx = __fsub_rn(c0x, c1x), dfy = __fsub_rn(c0y, c1y);
+    const float vx = __fsub_rn(p_x, c0x), vy = __fsub_rn(p_y, c0y);
+    const float len = __fsqrt_rn(__fadd_rn(__fmul_rn(vx, vx), __fmul_rn(vy, vy)));
+    const float rx = __fdiv_rn(vx, len), ry = __fdiv_rn(vy, len);
+    const float a    = __fadd_rn(__fmul_rn(rx, rx), __fmul_rn(ry, ry));
+    const float b    = __fmul_rn(2.0f, __fadd_rn(__fmul_rn(rx, dfx), __fmul_rn(ry, dfy)));
+    const float cc   = __fsub_rn(__fadd_rn(__fmul_rn(dfx, dfx), __fmul_rn(dfy, dfy)), __fmul_rn(r1, r1));
+    const float disc = __fsub_rn(__fmul_rn(b, b), __fmul_rn(__fmul_rn(4.0f, a), cc));
+    if (disc >= 0.0f) {
+        const float t  = __fdiv_rn(__fadd_rn(-b, __fsqrt_rn(fabsf(disc))), __fmul_rn(2.0f, a));
+        const float qx = __fsub_rn(__fadd_rn(c0x, __fmul_rn(rx, t)), c0x);
+        const float qy = __fsub_rn(__fadd_rn(c0y, __fmul_rn(ry, t)), c0y);
+        grad_len       = __fsub_rn(__fsqrt_rn(__fadd_rn(__fmul_rn(qx, qx), __fmul_rn(qy, qy))), r0);
+    }
+    return __fdiv_rn(__fsub_rn(len, r0), grad_len);
+}
 __device__ uint32_t gb_grad_pixel(const gb_grad &g, uint32_t px, uint32_t py) {
     const float p_x = __fdiv_rn(__fadd_rn((float)px, 0.5f), g.w), p_y = __fdiv_rn(__fadd_rn((float)py, 0.5f), g.h);
+    float       dist;
+    if (g.type == GB_GRAD_RADIAL) {
+        dist = gb_radial_t(g, p_x, p_y);
+    } else {
+        dist = gb_linear_t(g, p_x, p_y);
+    }
+    return gb_grad_word(g, dist);
+}
+/* LINEAR (shaders/vkvg_main.frag:83-108): signed distance along the axis in
+   units of its length */
+__device__ float gb_linear_t(const gb_grad &g, float p_x, float p_y) {
     const float p0x = __fdiv_rn(g.cp[0], g.w), p0y = __fdiv_rn(g.cp[1], g.h);
     const float p1x = __fdiv_rn(g.cp[2], g.w), p1y = __fdiv_rn(g.cp[3], g.h);
     const float dx = __fsub_rn(p1x, p0x), dy = __fsub_rn(p1y, p0y);
@@ -785,6 +823,10 @@ __device__ uint32_t gb_grad_pixel(const gb_grad &g, uint32_t px, uint32_t py) {
         if (uy < 0.0f)
             dist = -dist;
     }
+    return dist;
+}
+/* the stop colours at gradient parameter dist, times opacity, to UNORM8 */
+__device__ uint32_t gb_grad_word(const gb_grad &g, float dist) {
     float       c[4];
     const float t0 = g_smoothstep(g.stops[0], g.stops[1], dist);
 #pragma unroll

@@ -156,7 +156,11 @@ def api_mix(n_items=24, size=160, seed=5, samples=4):
     return {"name": "api_mix", "width": size, "height": size, "samples": samples, "ops": ops, "paths": n_items}
 
 
-def gradient_mix(n_items=14, size=144, seed=9, samples=4):
+def gradient_mix(n_items=14, size=144, seed=9, samples=4, radial=False):
+    """Filled and stroked curves whose source is a linear gradient (with
+    radial=True, every other one a radial gradient, some with the focus
+    circle pulled inside the outer one by vkvg_pattern_edit_radial), under
+    translated and rotated matrices and pattern matrices."""
     r = SplitMix64(seed)
     u = lambda lo, hi: lo + (hi - lo) * r.rnd()
 
@@ -188,13 +192,20 @@ def gradient_mix(n_items=14, size=144, seed=9, samples=4):
         for _ in range(2):
             ops.append(("curve_to",) + tuple(u(0, size) for _ in range(6)))
         ops.append(("close_path",))
-        ops += [("set_source_linear", x0, y0, x1, y1, stops(), pmat), ("set_fill_rule", i % 2),
+        if radial and i % 2:
+            r1 = u(20, 90)
+            r0 = u(0, r1 - 1) if i % 4 == 1 else u(0, 0.5 * r1)
+            src = ("set_source_radial", x0, y0, r0, x0 + u(-0.4, 0.4) * r1, y0 + u(-0.4, 0.4) * r1, r1, stops(), pmat)
+        else:
+            src = ("set_source_linear", x0, y0, x1, y1, stops(), pmat)
+        ops += [src, ("set_fill_rule", i % 2),
                 ("set_opacity", 1.0 if i % 2 else u(0.4, 1.0)), ("fill_preserve",),
                 ("set_line_width", u(1, 7)), ("set_line_join", i % 3)]
         if i % 3 == 0:
             ops += [("set_source_rgba", r.rnd(), r.rnd(), r.rnd(), u(0.5, 1.0))]
         ops.append(("stroke",))
-    return {"name": "gradient_mix", "width": size, "height": size, "samples": samples, "ops": ops, "paths": n_items}
+    return {"name": "radial_mix" if radial else "gradient_mix", "width": size, "height": size, "samples": samples,
+            "ops": ops, "paths": n_items}
 
 
 def clip_mix(n_items=10, size=128, seed=13, samples=4, flush_every=0):
@@ -308,6 +319,8 @@ def play(ctx, ops):
             ctx.set_dash(args[0], args[1])
         elif name == "set_source_linear":
             ctx.set_source_linear(*args)
+        elif name == "set_source_radial":
+            ctx.set_source_radial(*args)
         elif name == "set_matrix":
             ctx.set_matrix(args[0])
         else:
