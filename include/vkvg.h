@@ -232,6 +232,7 @@ vkvg_public void             vkvg_set_source_rgb(VkvgContext ctx, float r, float
 /* include/vkvg.h:1388-1394, 1531-1536: a pattern as the source (linear
    gradients; other pattern types are outside the path hot path) */
 vkvg_public void        vkvg_set_source(VkvgContext ctx, VkvgPattern pat);
+vkvg_public void        vkvg_set_source_surface(VkvgContext ctx, VkvgSurface surf, float x, float y);
 vkvg_public VkvgPattern vkvg_get_source(VkvgContext ctx);
 vkvg_public void             vkvg_set_line_width(VkvgContext ctx, float width);
 vkvg_public void             vkvg_set_miter_limit(VkvgContext ctx, float limit);
@@ -268,6 +269,7 @@ vkvg_public VkvgPattern         vkvg_pattern_create_linear(float x0, float y0, f
 vkvg_public vkvg_status_t       vkvg_pattern_edit_linear(VkvgPattern pat, float x0, float y0, float x1, float y1);
 vkvg_public vkvg_status_t       vkvg_pattern_get_linear_points(VkvgPattern pat, float *x0, float *y0, float *x1,
                                                                float *y1);
+vkvg_public VkvgPattern   vkvg_pattern_create_for_surface(VkvgSurface surf);
 vkvg_public VkvgPattern   vkvg_pattern_create_radial(float cx0, float cy0, float radius0, float cx1, float cy1,
                                                      float radius1);
 vkvg_public vkvg_status_t vkvg_pattern_edit_radial(VkvgPattern pat, float cx0, float cy0, float radius0, float cx1,

@@ -168,6 +168,10 @@ VKO_API int          vko_pattern_add_color_stop(vko_pattern *pat, float offset, 
 VKO_API int          vko_pattern_get_color_stop_count(vko_pattern *pat, uint32_t *count);
 VKO_API void         vko_pattern_set_matrix(vko_pattern *pat, const vko_matrix *m);
 VKO_API void         vko_set_source(vko_context *ctx, vko_pattern *pat);
+VKO_API vko_pattern *vko_pattern_create_for_surface(vko_surface *surf);
+VKO_API void         vko_pattern_set_extend(vko_pattern *pat, int extend);
+VKO_API void         vko_pattern_set_filter(vko_pattern *pat, int filter);
+VKO_API void         vko_set_source_surface(vko_context *ctx, vko_surface *surf, float x, float y);
 VKO_API bool vko_has_current_point(vko_context *ctx);
 VKO_API void vko_get_current_point(vko_context *ctx, float *x, float *y);
 VKO_API void vko_path_extents(vko_context *ctx, float *x1, float *y1, float *x2, float *y2);

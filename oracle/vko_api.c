@@ -207,6 +207,7 @@ vko_context *vko_create(vko_surface *surf) {
     ctx->cur_color   = 0xff000000u;
     ctx->opacity     = 1.0f;
     vko_matrix_init_identity(&ctx->mat);
+    vko_matrix_init_identity(&ctx->mat_inv);
     vko_ctx_init_geom(ctx);
     /* the context's first render pass clears the stencil
        (renderPass_ClearStencil, src/vkvg_context.c:43-49); recorded only when
@@ -275,6 +276,7 @@ static uint32_t create_rgbaf(float r, float g, float b, float a) {
 /* ---------------------------------------------------------------- patterns */
 /* src/vkvg_pattern.c (linear gradients) */
 static vko_pattern s_pattern_no_memory = {VKO_STATUS_NO_MEMORY};
+static vko_pattern s_pattern_null      = {VKO_STATUS_NULL_POINTER};
 vko_pattern *vko_pattern_create_linear(float x0, float y0, float x1, float y1) {
     vko_pattern *p = (vko_pattern *)calloc(1, sizeof(vko_pattern));
     if (!p)
@@ -300,7 +302,33 @@ void     vko_pattern_destroy(vko_pattern *pat) {
         return;
     if (--pat->refs > 0)
         return;
+    if (pat->surf)
+        surface_release(pat->surf);
     free(pat);
+}
+/* vkvg_pattern_create_for_surface, src/vkvg_pattern.c:28-48 */
+vko_pattern *vko_pattern_create_for_surface(vko_surface *surf) {
+    if (!surf)
+        return &s_pattern_null;
+    vko_pattern *p = (vko_pattern *)calloc(1, sizeof(vko_pattern));
+    if (!p)
+        return &s_pattern_null;
+    p->refs = 1;
+    p->type = 1; /* VKVG_PATTERN_TYPE_SURFACE */
+    p->surf = surf;
+    surf->refs++;
+    vko_matrix_init_identity(&p->matrix);
+    if (vko_surface_status(surf))
+        p->status = VKO_STATUS_INVALID_SURFACE;
+    return p;
+}
+void vko_pattern_set_extend(vko_pattern *pat, int extend) {
+    if (!vko_pattern_status(pat))
+        pat->extend = extend;
+}
+void vko_pattern_set_filter(vko_pattern *pat, int filter) {
+    if (!vko_pattern_status(pat))
+        pat->filter = filter;
 }
 /* vkvg_pattern_edit_radial / create_radial, src/vkvg_pattern.c:95-134 */
 int vko_pattern_edit_radial(vko_pattern *pat, float cx0, float cy0, float r0, float cx1, float cy1, float r1) {
@@ -388,11 +416,49 @@ void        vko_set_source(vko_context *ctx, vko_pattern *pat) {
     ctx->pattern = pat;
     snap_gradient(ctx, pat);
 }
+/* vkvg_set_source_surface, src/vkvg_context.c:1025-1033 */
+void vko_set_source_surface(vko_context *ctx, vko_surface *surf, float x, float y) {
+    if (vko_status(ctx) || vko_surface_status(surf))
+        return;
+    ctx->src_x       = x;
+    ctx->src_y       = y;
+    vko_pattern *pat = vko_pattern_create_for_surface(surf);
+    if (vko_pattern_status(pat)) {
+        ctx->status = vko_pattern_status(pat);
+        return;
+    }
+    set_solid(ctx);
+    ctx->pattern = pat;
+    snap_gradient(ctx, pat);
+}
+/* _update_cur_pattern, src/vkvg_context_internal.c:682-831 */
 static void snap_gradient(vko_context *ctx, vko_pattern *pat) {
+    if (pat->type == 1) {
+        /* sampled through each draw's push constants; the pattern matrix
+           goes into the pushed inverse now */
+        vko_grad *g = &ctx->grad_snap;
+        memset(g, 0, sizeof(*g));
+        g->type     = 1;
+        g->w        = (float)ctx->surf->width;
+        g->h        = (float)ctx->surf->height;
+        g->src      = pat->surf;
+        g->extend   = pat->extend;
+        g->bilinear = pat->filter == 4 || pat->filter == 2; /* VKVG_FILTER_BILINEAR, _BEST */
+        if (pat->has_matrix) {
+            vko_matrix r;
+            vko_matrix_multiply(&r, &ctx->mat_inv, &pat->matrix);
+            ctx->mat_inv = r;
+        }
+        ctx->grad_on = 1;
+        return;
+    }
     if (pat->type != 2 && pat->type != 3) {
         ctx->status = VKO_STATUS_PATTERN_TYPE_MISMATCH;
         return;
     }
+    /* the push constant source becomes the surface bounds */
+    ctx->src_x = (float)ctx->surf->width;
+    ctx->src_y = (float)ctx->surf->height;
     if (pat->count < 2) {
         ctx->status = VKO_STATUS_PATTERN_INVALID_GRADIENT;
         return;
@@ -500,10 +566,18 @@ void vko_set_dash(vko_context *ctx, const float *dashes, uint32_t n, float offse
     }
     memcpy(ctx->dashes, dashes, sizeof(float) * n);
 }
+/* _set_mat_inv_and_vkCmdPush, src/vkvg_context_internal.c:672-676: the
+   pushed inverse follows every matrix change (a failed inversion keeps
+   vkvg_matrix_invert's partial result) */
+static void mat_changed(vko_context *ctx) {
+    ctx->mat_inv = ctx->mat;
+    vko_matrix_invert(&ctx->mat_inv);
+}
 void vko_set_matrix(vko_context *ctx, const vko_matrix *m) {
     if (vko_status(ctx) || !m)
         return;
     ctx->mat = *m;
+    mat_changed(ctx);
 }
 void vko_get_matrix(vko_context *ctx, vko_matrix *m) {
     if (vko_status(ctx) || !m)
@@ -511,8 +585,10 @@ void vko_get_matrix(vko_context *ctx, vko_matrix *m) {
     *m = ctx->mat;
 }
 void vko_identity_matrix(vko_context *ctx) {
-    if (!vko_status(ctx))
-        vko_matrix_init_identity(&ctx->mat);
+    if (vko_status(ctx))
+        return;
+    vko_matrix_init_identity(&ctx->mat);
+    mat_changed(ctx);
 }
 /* vkvg_translate / scale / rotate / transform, src/vkvg_context.c:1513-1559 */
 void vko_transform(vko_context *ctx, const vko_matrix *m) {
@@ -521,18 +597,25 @@ void vko_transform(vko_context *ctx, const vko_matrix *m) {
     vko_matrix r;
     vko_matrix_multiply(&r, &ctx->mat, m);
     ctx->mat = r;
+    mat_changed(ctx);
 }
 void vko_translate(vko_context *ctx, float dx, float dy) {
-    if (!vko_status(ctx))
-        vko_matrix_translate(&ctx->mat, dx, dy);
+    if (vko_status(ctx))
+        return;
+    vko_matrix_translate(&ctx->mat, dx, dy);
+    mat_changed(ctx);
 }
 void vko_scale(vko_context *ctx, float sx, float sy) {
-    if (!vko_status(ctx))
-        vko_matrix_scale(&ctx->mat, sx, sy);
+    if (vko_status(ctx))
+        return;
+    vko_matrix_scale(&ctx->mat, sx, sy);
+    mat_changed(ctx);
 }
 void vko_rotate(vko_context *ctx, float r) {
-    if (!vko_status(ctx))
-        vko_matrix_rotate(&ctx->mat, r);
+    if (vko_status(ctx))
+        return;
+    vko_matrix_rotate(&ctx->mat, r);
+    mat_changed(ctx);
 }
 
 /* ------------------------------------------------------------- draw access */
@@ -673,7 +756,10 @@ void vko_save(vko_context *ctx) {
     sv->line_cap    = ctx->line_cap;
     sv->fill_rule   = ctx->fill_rule;
     /* lineJoint of vkvg_context_save_t is never written: calloc's 0 */
-    sv->mat     = ctx->mat;
+    sv->mat     = ctx->mat; /* pushConsts */
+    sv->mat_inv = ctx->mat_inv;
+    sv->src_x   = ctx->src_x;
+    sv->src_y   = ctx->src_y;
     sv->opacity = ctx->opacity;
     if (ctx->pattern) {
         sv->pattern = ctx->pattern;
@@ -720,6 +806,9 @@ void vko_restore(vko_context *ctx) {
     ctx->line_join   = sv->line_join;
     ctx->fill_rule   = sv->fill_rule;
     ctx->mat         = sv->mat;
+    ctx->mat_inv     = sv->mat_inv;
+    ctx->src_x       = sv->src_x;
+    ctx->src_y       = sv->src_y;
     ctx->opacity     = sv->opacity;
     if (sv->pattern) {
         if (sv->pattern != ctx->pattern) {

@@ -1071,6 +1071,12 @@ static vko_draw *new_draw(vko_context *ctx, int kind) {
         d->grad      = 1;
         d->g         = ctx->grad_snap;
         d->g.opacity = ctx->opacity;
+        if (d->g.type == 1) { /* the push constants of this draw; the draw keeps the source alive */
+            d->g.m  = ctx->mat_inv;
+            d->g.ox = ctx->src_x;
+            d->g.oy = ctx->src_y;
+            ((vko_surface *)d->g.src)->refs++;
+        }
     }
     return d;
 }
@@ -1318,6 +1324,8 @@ void vko_ctx_init_geom(vko_context *ctx) {
     clear_path(ctx);
 }
 void vko_draw_free(vko_draw *d) {
+    if (d->grad && d->g.type == 1 && d->g.src)
+        vko_surface_destroy((vko_surface *)d->g.src);
     free(d->pts);
     free(d->sub_counts);
     free(d->verts);

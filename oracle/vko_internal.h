@@ -43,6 +43,14 @@ typedef struct {
     float    opacity;
     float    stops[VKO_GRAD_STOPS];
     float    colors[VKO_GRAD_STOPS * 4];
+    /* surface sources (type 1): the source surface, sampler state, the
+       draw's pushed inverse matrix and source offset; texels is its resolved
+       image while the draw is rastered */
+    const struct vko_surface_t *src;
+    int            extend, bilinear;
+    vko_matrix     m;
+    float          ox, oy;
+    const uint8_t *texels;
 } vko_grad;
 
 struct vko_pattern_t {
@@ -50,6 +58,7 @@ struct vko_pattern_t {
     uint32_t   refs;
     int        type, extend, filter;
     float      cp[8];
+    vko_surface *surf; /* surface patterns: referenced */
     uint32_t   count;
     float      stops[VKO_GRAD_STOPS];
     float      colors[VKO_GRAD_STOPS * 4];
@@ -107,7 +116,8 @@ typedef struct vko_saved {
     uint32_t          dash_count;
     float            *dashes;
     int               op, line_cap, line_join, fill_rule;
-    vko_matrix        mat;
+    vko_matrix        mat, mat_inv;
+    float             src_x, src_y;
     uint32_t          cur_color;
     vko_pattern      *pattern;
     int               clip_state;
@@ -138,6 +148,8 @@ struct vko_context_t {
     vko_pattern *pattern;
     int          grad_on;
     vko_grad     grad_snap;
+    float        src_x, src_y; /* push constant source.xy */
+    vko_matrix   mat_inv;      /* push constant matInv */
     int          clip_state; /* curClipState */
     uint8_t      sav_bit;    /* curSavBit */
     vko_saved   *saved;      /* pSavedCtxs */

@@ -475,7 +475,78 @@ static float linear_t(const vko_grad *g, float p_x, float p_y) {
     }
     return dist;
 }
+/* SURFACE, shaders/vkvg_main.frag:72-82, sampled as the Vulkan spec's texel
+   filtering defines it for the sampler of src/vkvg_context_internal.c:730-755
+   (nearest, or linear with weights quantised to 8 fractional bits; address
+   modes by vkvg_extend_t; border transparent black: vkh, which sets the
+   border colour, is not in vkvg's tree) */
+static int32_t tex_floor(float x) {
+    float f = floorf(x);
+    if (f != f)
+        return 0;
+    if (f < -1073741824.0f)
+        f = -1073741824.0f;
+    if (f > 1073741824.0f)
+        f = 1073741824.0f;
+    return (int32_t)f;
+}
+static int32_t tex_wrap(int32_t i, int32_t n, int extend) {
+    if (extend == 1) { /* REPEAT */
+        int32_t r = i % n;
+        return r < 0 ? r + n : r;
+    }
+    if (extend == 2) { /* REFLECT: mirrored repeat */
+        int32_t r = i % (2 * n);
+        if (r < 0)
+            r += 2 * n;
+        r -= n;
+        return (n - 1) - (r >= 0 ? r : -(1 + r));
+    }
+    if (extend == 3) /* PAD: clamp to edge */
+        return i < 0 ? 0 : (i >= n ? n - 1 : i);
+    return (i < 0 || i >= n) ? -1 : i; /* NONE: clamp to border */
+}
+static void tex_fetch(const vko_grad *g, int32_t i, int32_t j, float t[4]) {
+    int32_t sw = (int32_t)g->src->width, sh = (int32_t)g->src->height;
+    i = tex_wrap(i, sw, g->extend);
+    j = tex_wrap(j, sh, g->extend);
+    for (int k = 0; k < 4; k++)
+        t[k] = (i < 0 || j < 0) ? 0.0f : (float)g->texels[((size_t)j * sw + i) * 4 + k] / 255.0f;
+}
+static void surface_src(const vko_grad *g, uint32_t px, uint32_t py, uint8_t s[4]) {
+    float sw = (float)g->src->width, sh = (float)g->src->height;
+    float qx = ((float)px + 0.5f) - g->ox, qy = ((float)py + 0.5f) - g->oy;
+    float u  = (g->m.xx * qx + g->m.xy * qy + g->m.x0) / sw;
+    float v  = (g->m.yx * qx + g->m.yy * qy + g->m.y0) / sh;
+    float us = u * sw, vs = v * sh;
+    float c[4];
+    if (!g->bilinear) {
+        tex_fetch(g, tex_floor(us), tex_floor(vs), c);
+    } else {
+        float   a = us - 0.5f, b = vs - 0.5f;
+        float   al = floorf((a - floorf(a)) * 256.0f) * (1.0f / 256.0f);
+        float   be = floorf((b - floorf(b)) * 256.0f) * (1.0f / 256.0f);
+        int32_t i = tex_floor(a), j = tex_floor(b);
+        float   t00[4], t10[4], t01[4], t11[4];
+        tex_fetch(g, i, j, t00);
+        tex_fetch(g, i + 1, j, t10);
+        tex_fetch(g, i, j + 1, t01);
+        tex_fetch(g, i + 1, j + 1, t11);
+        float w00 = (1.0f - al) * (1.0f - be), w10 = al * (1.0f - be), w01 = (1.0f - al) * be, w11 = al * be;
+        for (int k = 0; k < 4; k++)
+            c[k] = w00 * t00[k] + w10 * t10[k] + w01 * t01[k] + w11 * t11[k];
+    }
+    for (int k = 0; k < 4; k++) {
+        float x = (c[k] * g->opacity) * 255.0f;
+        x       = x > 0.0f ? fminf(x, 255.0f) : 0.0f;
+        s[k]    = (uint8_t)lrintf(x);
+    }
+}
 static void grad_src(const vko_grad *g, uint32_t px, uint32_t py, uint8_t s[4]) {
+    if (g->type == 1) {
+        surface_src(g, px, py, s);
+        return;
+    }
     float p_x  = ((float)px + 0.5f) / g->w, p_y = ((float)py + 0.5f) / g->h;
     float dist = g->type == 3 ? radial_t(g, p_x, p_y) : linear_t(g, p_x, p_y);
     float c[4];
@@ -665,8 +736,25 @@ static void stencil_draw(vko_surface *surf, const vko_draw *d) {
     }
 }
 
-/* execute one draw against the surface */
+static void raster_draw(vko_surface *surf, const vko_draw *d);
+/* execute one draw against the surface; a surface source is resolved first
+   (the image vkvg samples is the source surface's resolved attachment) */
 void vko_raster_draw(vko_surface *surf, const vko_draw *d) {
+    if (!(d->grad && d->g.type == 1 && d->g.src)) {
+        raster_draw(surf, d);
+        return;
+    }
+    const vko_surface *src = d->g.src;
+    uint8_t           *tex = (uint8_t *)malloc((size_t)src->width * src->height * 4);
+    if (!tex)
+        return;
+    vko_resolve(src, tex);
+    vko_draw dl   = *d;
+    dl.g.texels   = tex;
+    raster_draw(surf, &dl);
+    free(tex);
+}
+static void raster_draw(vko_surface *surf, const vko_draw *d) {
     uint32_t w = surf->width, h = surf->height, S = surf->samples;
     size_t   ns = (size_t)w * h * S;
     uint8_t  src[4];

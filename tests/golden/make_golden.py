@@ -38,7 +38,8 @@ def golden_scenes():
             scenes.api_mix(n_items=24, size=160, seed=5),
             scenes.gradient_mix(n_items=14, size=144, seed=9),
             scenes.clip_mix(n_items=10, size=128, seed=13),
-            scenes.gradient_mix(n_items=14, size=144, seed=9, radial=True)]
+            scenes.gradient_mix(n_items=14, size=144, seed=9, radial=True),
+            scenes.surface_mix(n_items=12, size=128, seed=23)]
 
 STENCIL_OPS = 7
 FILL_KINDS = (0, 1, 5, 6)

@@ -83,6 +83,10 @@ _SIGS = {
     "vko_pattern_destroy": (None, [_P]),
     "vko_pattern_edit_linear": (C.c_int, [_P, _F, _F, _F, _F]),
     "vko_pattern_create_radial": (_P, [_F, _F, _F, _F, _F, _F]),
+    "vko_pattern_create_for_surface": (_P, [_P]),
+    "vko_pattern_set_extend": (None, [_P, C.c_int]),
+    "vko_pattern_set_filter": (None, [_P, C.c_int]),
+    "vko_set_source_surface": (None, [_P, _P, _F, _F]),
     "vko_pattern_edit_radial": (C.c_int, [_P, _F, _F, _F, _F, _F, _F]),
     "vko_pattern_add_color_stop": (C.c_int, [_P, _F, _F, _F, _F, _F]),
     "vko_pattern_get_color_stop_count": (C.c_int, [_P, _P]),
@@ -175,6 +179,20 @@ class OracleContext:
         p = self.L.vko_pattern_create_linear(x0, y0, x1, y1)
         for st in stops:
             self.L.vko_pattern_add_color_stop(p, *st)
+        if pmat is not None:
+            mm = Matrix(*pmat)
+            self.L.vko_pattern_set_matrix(p, C.byref(mm))
+        self.L.vko_set_source(self.h, p)
+        self.L.vko_pattern_destroy(p)
+
+    def set_source_surface(self, surf, x, y):
+        self.L.vko_set_source_surface(self.h, surf.s, x, y)
+
+    def set_source_surface_pattern(self, surf, extend, filt, pmat=None):
+        """a surface pattern with sampler settings as the source"""
+        p = self.L.vko_pattern_create_for_surface(surf.s)
+        self.L.vko_pattern_set_extend(p, extend)
+        self.L.vko_pattern_set_filter(p, filt)
         if pmat is not None:
             mm = Matrix(*pmat)
             self.L.vko_pattern_set_matrix(p, C.byref(mm))

@@ -5,14 +5,28 @@ import numpy as np
 from vkvg_gb300 import scenes
 
 
+def _gpu_sources(gb, dev, sc):
+    out = []
+    for s in sc.get("sources", ()):
+        surf = gb.Surface(dev, s["width"], s["height"])
+        c = surf.context()
+        scenes.play(c, s["ops"])
+        c.flush()
+        c.destroy()
+        out.append(surf)
+    return out
+
+
 def run_gpu(gb, sc, debug=True):
     dev = gb.Device(samples=sc["samples"])
+    srcs = _gpu_sources(gb, dev, sc)
     surf = gb.Surface(dev, sc["width"], sc["height"])
     ctx = surf.context()
     if debug:
         ctx.debug_capture(True)
-    scenes.play(ctx, sc["ops"])
+    scenes.play(ctx, sc["ops"], srcs)
     ctx.flush()
+    surf.sources = srcs
     return dev, surf, ctx
 
 
@@ -20,11 +34,20 @@ def run_oracle(vko, sc, raster_mode=0, threads=1):
     L = vko.lib()
     L.vko_set_raster_mode(raster_mode)
     L.vko_set_threads(threads)
+    srcs = []
+    for s in sc.get("sources", ()):
+        ss = vko.OracleSurface(s["width"], s["height"], sc["samples"])
+        c = ss.context()
+        scenes.play(c, s["ops"])
+        c.flush()
+        c.destroy()
+        srcs.append(ss)
     surf = vko.OracleSurface(sc["width"], sc["height"], sc["samples"])
     ctx = surf.context()
     ctx.keep_draws(1)
-    scenes.play(ctx, sc["ops"])
+    scenes.play(ctx, sc["ops"], srcs)
     ctx.flush()
+    surf.sources = srcs
     return surf, ctx
 
 

@@ -300,3 +300,45 @@ def test_radial_gradient_paint_bit_exact(gb, vko):
         osurf, octx = pu.run_oracle(vko, sc)
         assert ctx.status() == 0 and ctx.debug_counts()[5] == 0
         assert np.array_equal(surf.samples_rgba(), osurf.samples_rgba())
+
+
+@pytest.mark.parametrize("samples", [4, 1])
+def test_surface_sources_bit_exact(gb, vko, samples):
+    """surface sources (offsets, every extend mode, nearest and bilinear,
+    pattern matrices, opacity, save / restore, the offset a gradient leaves
+    behind): samples and image equal the oracle's"""
+    sc = scenes.surface_mix(n_items=12, size=128, seed=23, samples=samples)
+    dev, surf, ctx = pu.run_gpu(gb, sc)
+    osurf, octx = pu.run_oracle(vko, sc)
+    assert ctx.status() == 0 and ctx.debug_counts()[5] == 0
+    assert np.array_equal(surf.samples_rgba(), osurf.samples_rgba())
+    assert np.array_equal(surf.image(), osurf.image())
+
+
+def test_surface_source_outlives_its_handles(gb, vko):
+    """a surface used as a source and destroyed by the caller before the
+    frame runs stays valid for that frame; the pattern holds a reference"""
+    dev = gb.Device(samples=4)
+    src = gb.Surface(dev, 20, 12)
+    c = src.context()
+    c.set_source_rgba(0.2, 0.6, 0.9, 0.8)
+    c.paint()
+    c.flush()
+    c.destroy()
+    L = gb.lib()
+    before = L.vkvg_surface_get_reference_count(src.h)
+    p = L.vkvg_pattern_create_for_surface(src.h)
+    assert L.vkvg_surface_get_reference_count(src.h) == before + 1
+    L.vkvg_pattern_destroy(p)
+    assert L.vkvg_surface_get_reference_count(src.h) == before
+    dst = gb.Surface(dev, 40, 30)
+    ctx = dst.context()
+    ctx.set_source_surface(src, 3.0, 2.0)
+    ctx.rectangle(0.0, 0.0, 30.0, 20.0)
+    ctx.fill()
+    ctx.set_source_rgb(0.0, 0.0, 0.0)  # releases the pattern
+    src.destroy()  # the caller's reference
+    ctx.flush()
+    assert ctx.status() == 0
+    img = dst.premult()
+    assert tuple(img[5, 10]) != (0, 0, 0, 0) and tuple(img[25, 35]) == (0, 0, 0, 0)

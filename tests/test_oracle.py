@@ -131,7 +131,8 @@ def small_scenes():
             scenes.api_mix(n_items=24, size=160, seed=5),
             scenes.gradient_mix(n_items=14, size=144, seed=9),
             scenes.clip_mix(n_items=10, size=128, seed=13),
-            scenes.gradient_mix(n_items=14, size=144, seed=9, radial=True)]
+            scenes.gradient_mix(n_items=14, size=144, seed=9, radial=True),
+            scenes.surface_mix(n_items=12, size=128, seed=23)]
 
 
 @pytest.mark.parametrize("sc", small_scenes(), ids=lambda s: s["name"])
@@ -342,6 +343,79 @@ def test_radial_gradient_kat():
         want = np.stack([np.rint(np.clip(np.nan_to_num(ck * f(255), nan=0.0), 0, 255)).astype(np.uint8)
                          for ck in c], -1)
         assert np.array_equal(got, want)
+
+
+def _np_wrap(i, n, extend):
+    if extend == 1:
+        return i % n
+    if extend == 2:
+        t = (i % (2 * n)) - n
+        return (n - 1) - np.where(t >= 0, t, -(1 + t))
+    if extend == 3:
+        return np.clip(i, 0, n - 1)
+    return np.where((i < 0) | (i >= n), -1, i)
+
+
+def test_surface_source_kat():
+    """a 5x3 source of solid pixels painted through a surface pattern equals
+    an independent numpy evaluation of the SURFACE fragment case
+    (shaders/vkvg_main.frag:72-82) and Vulkan's texel filtering: nearest and
+    bilinear (8-bit weights), each extend mode, a pattern matrix"""
+    f = np.float32
+    rng = np.random.default_rng(3)
+    sw, sh = 5, 3
+    cols = rng.integers(0, 256, (sh, sw, 3))
+    W, H = 40, 28
+    for extend in range(4):
+        for filt, bil in ((3, False), (4, True)):  # VKVG_FILTER_NEAREST, _BILINEAR
+            src = ob.OracleSurface(sw, sh, 4)
+            c = src.context()
+            for y in range(sh):
+                for x in range(sw):
+                    r, g, b = cols[y, x] / 255.0
+                    c.set_source_rgb(float(r), float(g), float(b))
+                    c.rectangle(float(x), float(y), 1.0, 1.0)
+                    c.fill()
+            c.flush()
+            c.destroy()
+            texels = src.premult()
+            pm = (0.37, 0.05, -0.08, 0.29, 1.3, -0.7)  # pattern matrix, folded into the inverse matrix
+            dst = ob.OracleSurface(W, H, 4)
+            c = dst.context()
+            c.set_source_surface_pattern(src, extend, filt, pm)
+            c.paint()
+            c.flush()
+            got = dst.premult()
+            c.destroy()
+            px = np.arange(W, dtype=f)[None, :].repeat(H, 0) + f(0.5)
+            py = np.arange(H, dtype=f)[:, None].repeat(W, 1) + f(0.5)
+            xx, yx, xy, yy, x0, y0 = [f(v) for v in pm]
+            u = (xx * px + xy * py + x0) / f(sw)
+            v = (yx * px + yy * py + y0) / f(sh)
+            us, vs = u * f(sw), v * f(sh)
+            tex = texels.astype(f) / f(255)
+
+            def fetch(i, j):
+                i, j = _np_wrap(i, sw, extend), _np_wrap(j, sh, extend)
+                ok = (i >= 0) & (j >= 0)
+                return np.where(ok[..., None], tex[np.maximum(j, 0), np.maximum(i, 0)], f(0))
+
+            if not bil:
+                out = fetch(np.floor(us).astype(np.int64), np.floor(vs).astype(np.int64))
+            else:
+                a, b = us - f(0.5), vs - f(0.5)
+                al = np.floor((a - np.floor(a)) * f(256)) * f(1 / 256)
+                be = np.floor((b - np.floor(b)) * f(256)) * f(1 / 256)
+                i, j = np.floor(a).astype(np.int64), np.floor(b).astype(np.int64)
+                w = [((f(1) - al) * (f(1) - be))[..., None], (al * (f(1) - be))[..., None],
+                     ((f(1) - al) * be)[..., None], (al * be)[..., None]]
+                out = w[0] * fetch(i, j) + w[1] * fetch(i + 1, j)
+                out = out + w[2] * fetch(i, j + 1)
+                out = out + w[3] * fetch(i + 1, j + 1)
+            want = np.rint(np.clip(out * f(255), 0, 255)).astype(np.uint8)
+            assert np.array_equal(got, want), (extend, filt, int((got != want).sum()))
+            dst.destroy()
+            src.destroy()
 
 
 def test_pattern_api_semantics():

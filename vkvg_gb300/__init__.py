@@ -108,6 +108,8 @@ SIGNATURES = {
     "vkvg_pattern_create_linear": (_P, [_F, _F, _F, _F]),
     "vkvg_pattern_edit_linear": (_I, [_P, _F, _F, _F, _F]),
     "vkvg_pattern_create_radial": (_P, [_F, _F, _F, _F, _F, _F]),
+    "vkvg_pattern_create_for_surface": (_P, [_P]),
+    "vkvg_set_source_surface": (None, [_P, _P, _F, _F]),
     "vkvg_pattern_edit_radial": (_I, [_P, _F, _F, _F, _F, _F, _F]),
     "vkvg_pattern_get_linear_points": (_I, [_P, _P, _P, _P, _P]),
     "vkvg_pattern_add_color_stop": (_I, [_P, _F, _F, _F, _F, _F]),
@@ -283,6 +285,21 @@ class Context:
         p = self.L.vkvg_pattern_create_linear(x0, y0, x1, y1)
         for st in stops:
             self.L.vkvg_pattern_add_color_stop(p, *st)
+        if pmat is not None:
+            mm = Matrix(*pmat)
+            self.L.vkvg_pattern_set_matrix(p, C.byref(mm))
+        self.L.vkvg_set_source(self.h, p)
+        self.L.vkvg_pattern_destroy(p)
+
+    def set_source_surface(self, surf, x, y):
+        self.L.vkvg_set_source_surface(self.h, surf.h, x, y)
+
+    def set_source_surface_pattern(self, surf, extend, filt, pmat=None):
+        """a surface pattern with sampler settings as the source (created,
+        used, released)"""
+        p = self.L.vkvg_pattern_create_for_surface(surf.h)
+        self.L.vkvg_pattern_set_extend(p, extend)
+        self.L.vkvg_pattern_set_filter(p, filt)
         if pmat is not None:
             mm = Matrix(*pmat)
             self.L.vkvg_pattern_set_matrix(p, C.byref(mm))

@@ -29,6 +29,7 @@
 /* status sentinels returned instead of NULL on creation failure
    (src/vkvg_internal.h:104-109) */
 static vkvg_status_t s_no_memory      = VKVG_STATUS_NO_MEMORY;
+static vkvg_status_t s_null_pattern   = VKVG_STATUS_NULL_POINTER;
 static vkvg_status_t s_invalid_surf   = VKVG_STATUS_INVALID_SURFACE;
 static vkvg_status_t s_device_error   = VKVG_STATUS_DEVICE_ERROR;
 static vkvg_status_t s_invalid_dev_ci = VKVG_STATUS_INVALID_DEVICE_CREATE_INFO;
@@ -758,6 +759,16 @@ static void flush_i(VkvgContext ctx);
 static uint32_t grad_source(VkvgContext ctx) {
     gb_grad g = ctx->grad_snap;
     g.opacity = ctx->opacity;
+    VkvgSurface src = nullptr;
+    if (g.type == GB_SRC_SURFACE) {
+        /* the push constants as this draw pushes them */
+        const vkvg_matrix_t &m = ctx->mat_inv;
+        const float          mv[6] = {m.xx, m.yx, m.xy, m.yy, m.x0, m.y0};
+        memcpy(g.m, mv, sizeof(mv));
+        g.ox = ctx->src_x;
+        g.oy = ctx->src_y;
+        src  = ctx->pattern->surf;
+    }
     std::vector<gb_grad> &v = ctx->frame.grads;
     for (size_t i = 0; i < v.size(); i++)
         if (memcmp(&v[i], &g, sizeof(g)) == 0)
@@ -765,6 +776,8 @@ static uint32_t grad_source(VkvgContext ctx) {
     if (v.size() >= GB_MAX_GRAD_SOURCES)
         flush_i(ctx);
     ctx->frame.grads.push_back(g);
+    if (src)
+        ctx->frame.sources.emplace_back(src);
     return (uint32_t)ctx->frame.grads.size();
 }
 static gb_draw make_draw(VkvgContext ctx, uint32_t kind) {
@@ -1254,6 +1267,9 @@ void vkvg_save(VkvgContext ctx) {
     sv.fill_rule   = ctx->fill_rule;
     sv.op          = ctx->op;
     sv.mat         = ctx->mat;
+    sv.mat_inv     = ctx->mat_inv;
+    sv.src_x       = ctx->src_x;
+    sv.src_y       = ctx->src_y;
     sv.cur_color   = ctx->cur_color;
     sv.pattern     = ctx->pattern;
     if (sv.pattern)
@@ -1295,7 +1311,10 @@ void        vkvg_restore(VkvgContext ctx) {
     ctx->line_cap    = sv.line_cap;
     ctx->line_join   = VKVG_LINE_JOIN_MITER; /* the unsaved lineJoint field */
     ctx->fill_rule   = sv.fill_rule;
-    ctx->mat         = sv.mat;
+    ctx->mat         = sv.mat; /* the push constants: matrices, source.xy, opacity */
+    ctx->mat_inv     = sv.mat_inv;
+    ctx->src_x       = sv.src_x;
+    ctx->src_y       = sv.src_y;
     ctx->opacity     = sv.opacity;
     if (sv.pattern) {
         if (sv.pattern != ctx->pattern) {
@@ -1402,7 +1421,31 @@ void     vkvg_pattern_destroy(VkvgPattern pat) {
         return;
     if (--pat->refs > 0)
         return;
+    if (pat->surf)
+        vkvg_surface_destroy(pat->surf);
     delete pat;
+}
+/* vkvg_pattern_create_for_surface, src/vkvg_pattern.c:28-48: the pattern
+   references the surface */
+VkvgPattern vkvg_pattern_create_for_surface(VkvgSurface surf) {
+    if (!surf)
+        return (VkvgPattern)&s_null_pattern;
+    _vkvg_pattern_t *p = new (std::nothrow) _vkvg_pattern_t();
+    if (!p)
+        return (VkvgPattern)&s_null_pattern;
+    p->status     = VKVG_STATUS_SUCCESS;
+    p->refs       = 1;
+    p->type       = VKVG_PATTERN_TYPE_SURFACE;
+    p->extend     = VKVG_EXTEND_NONE;
+    p->filter     = VKVG_FILTER_FAST;
+    p->count      = 0;
+    p->matrix     = VKVG_IDENTITY_MATRIX;
+    p->has_matrix = false;
+    p->surf       = surf;
+    vkvg_surface_reference(surf);
+    if (vkvg_surface_status(surf))
+        p->status = VKVG_STATUS_INVALID_SURFACE;
+    return p;
 }
 vkvg_status_t vkvg_pattern_edit_linear(VkvgPattern pat, float x0, float y0, float x1, float y1) {
     if (vkvg_pattern_status(pat))
@@ -1512,11 +1555,53 @@ void vkvg_set_source(VkvgContext ctx, VkvgPattern pat) {
     ctx->pattern = pat;
     snap_gradient(ctx, pat);
 }
+/* vkvg_set_source_surface, src/vkvg_context.c:1025-1033: the offset goes to
+   the push constants, the new pattern's only reference to the context */
+void vkvg_set_source_surface(VkvgContext ctx, VkvgSurface surf, float x, float y) {
+    if (vkvg_status(ctx) || vkvg_surface_status(surf))
+        return;
+    ctx->src_x      = x;
+    ctx->src_y      = y;
+    VkvgPattern pat = vkvg_pattern_create_for_surface(surf);
+    if (vkvg_pattern_status(pat)) {
+        ctx->status = vkvg_pattern_status(pat);
+        return;
+    }
+    set_solid(ctx);
+    ctx->pattern = pat;
+    snap_gradient(ctx, pat);
+}
+/* _update_cur_pattern (src/vkvg_context_internal.c:682-831) for a pattern
+   source: a surface samples through the push constants of each draw, with
+   the pattern matrix multiplied into the inverse matrix now; a gradient is
+   captured now and sets source.xy to the surface size */
 static void snap_gradient(VkvgContext ctx, VkvgPattern pat) {
+    if (pat->type == VKVG_PATTERN_TYPE_SURFACE) {
+        VkvgSurface s = pat->surf;
+        gb_grad    &g = ctx->grad_snap;
+        memset(&g, 0, sizeof(g));
+        g.type   = GB_SRC_SURFACE;
+        g.w      = (float)ctx->surf->width;
+        g.h      = (float)ctx->surf->height;
+        g.sw     = s->width;
+        g.sh     = s->height;
+        g.extend = (uint32_t)pat->extend;
+        g.filter = (pat->filter == VKVG_FILTER_BILINEAR || pat->filter == VKVG_FILTER_BEST) ? 1u : 0u;
+        g.texels = s->d_rgba;
+        if (pat->has_matrix) {
+            vkvg_matrix_t r;
+            vkvg_matrix_multiply(&r, &ctx->mat_inv, &pat->matrix);
+            ctx->mat_inv = r;
+        }
+        ctx->grad_on = true;
+        return;
+    }
     if (pat->type != VKVG_PATTERN_TYPE_LINEAR && pat->type != VKVG_PATTERN_TYPE_RADIAL) {
         ctx->status = VKVG_STATUS_PATTERN_TYPE_MISMATCH;
         return;
     }
+    ctx->src_x = (float)ctx->surf->width;
+    ctx->src_y = (float)ctx->surf->height;
     if (pat->count < 2) {
         ctx->status = VKVG_STATUS_PATTERN_INVALID_GRADIENT;
         return;
@@ -1639,17 +1724,30 @@ vkvg_fill_rule_t vkvg_get_fill_rule(VkvgContext ctx) {
     return vkvg_status(ctx) ? VKVG_FILL_RULE_NON_ZERO : ctx->fill_rule;
 }
 VkvgSurface vkvg_get_target(VkvgContext ctx) { return vkvg_status(ctx) ? nullptr : ctx->surf; }
-void        vkvg_translate(VkvgContext ctx, float dx, float dy) {
-    if (!vkvg_status(ctx))
-        vkvg_matrix_translate(&ctx->mat, dx, dy);
+/* _set_mat_inv_and_vkCmdPush, src/vkvg_context_internal.c:672-676: every
+   matrix change recomputes the pushed inverse (a failed inversion leaves
+   vkvg_matrix_invert's partial result) */
+static void mat_changed(VkvgContext ctx) {
+    ctx->mat_inv = ctx->mat;
+    vkvg_matrix_invert(&ctx->mat_inv);
+}
+void vkvg_translate(VkvgContext ctx, float dx, float dy) {
+    if (vkvg_status(ctx))
+        return;
+    vkvg_matrix_translate(&ctx->mat, dx, dy);
+    mat_changed(ctx);
 }
 void vkvg_scale(VkvgContext ctx, float sx, float sy) {
-    if (!vkvg_status(ctx))
-        vkvg_matrix_scale(&ctx->mat, sx, sy);
+    if (vkvg_status(ctx))
+        return;
+    vkvg_matrix_scale(&ctx->mat, sx, sy);
+    mat_changed(ctx);
 }
 void vkvg_rotate(VkvgContext ctx, float radians) {
-    if (!vkvg_status(ctx))
-        vkvg_matrix_rotate(&ctx->mat, radians);
+    if (vkvg_status(ctx))
+        return;
+    vkvg_matrix_rotate(&ctx->mat, radians);
+    mat_changed(ctx);
 }
 void vkvg_transform(VkvgContext ctx, const vkvg_matrix_t *m) {
     if (vkvg_status(ctx) || !m)
@@ -1657,11 +1755,13 @@ void vkvg_transform(VkvgContext ctx, const vkvg_matrix_t *m) {
     vkvg_matrix_t r;
     vkvg_matrix_multiply(&r, &ctx->mat, m);
     ctx->mat = r;
+    mat_changed(ctx);
 }
 void vkvg_set_matrix(VkvgContext ctx, const vkvg_matrix_t *m) {
     if (vkvg_status(ctx) || !m)
         return;
     ctx->mat = *m;
+    mat_changed(ctx);
 }
 void vkvg_get_matrix(VkvgContext ctx, vkvg_matrix_t *const m) {
     if (vkvg_status(ctx) || !m)
@@ -1669,7 +1769,9 @@ void vkvg_get_matrix(VkvgContext ctx, vkvg_matrix_t *const m) {
     *m = ctx->mat;
 }
 void vkvg_identity_matrix(VkvgContext ctx) {
-    if (!vkvg_status(ctx))
-        vkvg_matrix_init_identity(&ctx->mat);
+    if (vkvg_status(ctx))
+        return;
+    vkvg_matrix_init_identity(&ctx->mat);
+    mat_changed(ctx);
 }
 } /* extern "C" */

@@ -79,14 +79,18 @@ typedef struct {
     uint32_t gsrc;     /* 0: the solid colour src; i + 1: gradient source image i of the frame */
 } gb_draw;
 
-/* A gradient as vkvg's fragment stage sees it (shaders/vkvg_main.frag LINEAR
-   and RADIAL cases, data of _update_cur_pattern): control points transformed
-   by the pattern's inverse matrix and the CTM at vkvg_set_source time, in
-   pixels, in vkvg's layout of two vec4 (linear: x0 y0 x1 y1; radial:
-   cx0 cy0 r0 - and cx1 cy1 r1 -); surface size; stops; premultiplied stop
-   colours; the draw's opacity.  One per distinct source image of a frame. */
+/* A pattern source as vkvg's fragment stage sees it (shaders/vkvg_main.frag
+   SURFACE, LINEAR and RADIAL cases).  Gradients (data of _update_cur_pattern):
+   control points transformed by the pattern's inverse matrix and the CTM at
+   vkvg_set_source time, in pixels, in vkvg's layout of two vec4 (linear:
+   x0 y0 x1 y1; radial: cx0 cy0 r0 - and cx1 cy1 r1 -); stops; premultiplied
+   stop colours.  Surfaces (push constants of the draw): the source surface's
+   resolved image, its size, the sampler's extend and filter, the inverse
+   matrix and the source offset.  Both: the target size and the draw's
+   opacity.  One per distinct source image of a frame. */
 #define GB_GRAD_STOPS  16
-#define GB_GRAD_LINEAR 2u /* vkvg_pattern_type_t values */
+#define GB_SRC_SURFACE 1u /* vkvg_pattern_type_t values */
+#define GB_GRAD_LINEAR 2u
 #define GB_GRAD_RADIAL 3u
 typedef struct {
     uint32_t type;
@@ -96,6 +100,12 @@ typedef struct {
     float    opacity;
     float    stops[GB_GRAD_STOPS];
     float    colors[GB_GRAD_STOPS * 4];
+    /* surface sources */
+    uint32_t        sw, sh;         /* source size */
+    uint32_t        extend, filter; /* vkvg_extend_t; 1 bilinear, 0 nearest */
+    float           m[6];           /* inverse matrix xx yx xy yy x0 y0 */
+    float           ox, oy;         /* source offset (push constant source.xy) */
+    const uint32_t *texels;         /* [sh][sw] premultiplied RGBA8 */
 } gb_grad;
 #define GB_MAX_GRAD_SOURCES 8 /* source images per frame; more flush the frame first */
 

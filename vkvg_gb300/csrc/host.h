@@ -15,6 +15,7 @@
 #include <mutex>
 #include <stdint.h>
 #include <string.h>
+#include <utility>
 #include <vector>
 
 struct f4 {
@@ -22,6 +23,29 @@ struct f4 {
 };
 
 /* one frame of recorded work, as host structure-of-arrays */
+/* a counted reference to a surface (a frame's surface sources stay alive
+   until the frame has run) */
+struct SurfRef {
+    VkvgSurface s = nullptr;
+    SurfRef()     = default;
+    explicit SurfRef(VkvgSurface x) : s(x) { vkvg_surface_reference(s); }
+    SurfRef(const SurfRef &o) : s(o.s) {
+        if (s)
+            vkvg_surface_reference(s);
+    }
+    SurfRef &operator=(const SurfRef &o) {
+        if (this != &o) {
+            SurfRef t(o);
+            std::swap(s, t.s);
+        }
+        return *this;
+    }
+    ~SurfRef() {
+        if (s)
+            vkvg_surface_destroy(s);
+    }
+};
+
 struct FrameHost {
     std::vector<uint32_t> seg_info, seg_n, seg_aux;
     std::vector<f4>       seg_a, seg_b, seg_c;
@@ -31,7 +55,8 @@ struct FrameHost {
     std::vector<uint32_t> sdraw_id, sdraw_pair0; /* per stroke draw (+ sentinel in pair0) */
     std::vector<uint32_t> fpair_draw, fpair_sub;
     std::vector<float>    dashes, thetas;
-    std::vector<gb_grad>  grads; /* gradient source images of the frame */
+    std::vector<gb_grad>  grads;   /* pattern source images of the frame */
+    std::vector<SurfRef>  sources; /* surfaces that surface sources read */
     uint32_t              paths = 0; /* fill + stroke draws */
     bool                  any_dash = false;
     bool                  dash_shared = false; /* a subpath belongs to two dashed stroke pairs */
@@ -109,6 +134,7 @@ struct _vkvg_pattern_t {
     vkvg_extend_t       extend;
     vkvg_filter_t       filter;
     float               cp[8]; /* vkvg_gradient_t.cp: two vec4 */
+    VkvgSurface         surf = nullptr; /* surface patterns: referenced */
     uint32_t            count;
     float               stops[GB_GRAD_STOPS];
     float               colors[GB_GRAD_STOPS * 4]; /* premultiplied */
@@ -163,7 +189,8 @@ struct gb_saved_state {
     vkvg_line_cap_t    line_cap;
     vkvg_fill_rule_t   fill_rule;
     vkvg_operator_t    op;
-    vkvg_matrix_t      mat;
+    vkvg_matrix_t      mat, mat_inv;
+    float              src_x, src_y;
     std::vector<float> dashes;
     uint32_t           cur_color;
     VkvgPattern        pattern; /* referenced while saved */
@@ -189,8 +216,12 @@ struct _vkvg_context_t {
     std::vector<float> dashes;
     float              dash_offset = 0;
     VkvgPattern        pattern     = nullptr; /* source pattern, null for the solid colour */
-    bool               grad_on     = false;   /* the source is a gradient snapshot */
-    gb_grad            grad_snap;             /* as of vkvg_set_source (opacity filled per draw) */
+    bool               grad_on     = false;   /* the source is a pattern (gradient snapshot or surface) */
+    gb_grad            grad_snap;             /* gradients: as of vkvg_set_source (opacity filled per draw) */
+    /* push constants the fragment stage reads for surface sources: source.xy
+       and the inverse matrix (src/vkvg_context_internal.h:74-81) */
+    float              src_x = 0, src_y = 0;
+    vkvg_matrix_t      mat_inv     = {1, 0, 0, 1, 0, 0};
 
     /* clip and save/restore (vkvg's curClipState, curSavBit, pSavedCtxs) */
     uint8_t                     clip_state = GB_CLIP_NONE;

@@ -36,6 +36,7 @@ void FrameHost::clear() {
     dashes.clear();
     thetas.clear();
     grads.clear();
+    sources.clear();
     paths       = 0;
     any_dash    = false;
     dash_shared = false;

@@ -792,7 +792,80 @@ __device__ float gb_radial_t(const gb_grad &g, float p_x, float p_y) {
     }
     return __fdiv_rn(__fsub_rn(len, r0), grad_len);
 }
+/* SURFACE (shaders/vkvg_main.frag:72-82) through the sampler vkvg builds
+   (src/vkvg_context_internal.c:730-755): texel coordinates by the Vulkan
+   texel filtering rules, nearest or bilinear with 8-bit weights, the four
+   address modes, a transparent black border */
+__device__ __forceinline__ int32_t gb_wrap(int32_t i, int32_t n, uint32_t extend) {
+    switch (extend) {
+    case 1: /* VKVG_EXTEND_REPEAT: VK_SAMPLER_ADDRESS_MODE_REPEAT */
+        i %= n;
+        return i < 0 ? i + n : i;
+    case 2: { /* REFLECT: MIRRORED_REPEAT, (n - 1) - mirror((i mod 2n) - n) */
+        int32_t t = i % (2 * n);
+        t         = (t < 0 ? t + 2 * n : t) - n;
+        return (n - 1) - (t >= 0 ? t : -(1 + t));
+    }
+    case 3: /* PAD: CLAMP_TO_EDGE */ return min(max(i, 0), n - 1);
+    default: /* NONE: CLAMP_TO_BORDER */ return (i < 0 || i >= n) ? -1 : i;
+    }
+}
+/* floor to an integer texel coordinate: NaN gives 0, magnitudes are held
+   to 2^30 so that the neighbour i + 1 stays representable */
+__device__ __forceinline__ int32_t gb_floor_i(float x) {
+    const float f = floorf(x);
+    if (!(f == f))
+        return 0;
+    return (int32_t)fminf(fmaxf(f, -1073741824.0f), 1073741824.0f);
+}
+__device__ __forceinline__ float4 gb_texel(const gb_grad &g, int32_t i, int32_t j) {
+    i = gb_wrap(i, (int32_t)g.sw, g.extend);
+    j = gb_wrap(j, (int32_t)g.sh, g.extend);
+    if (i < 0 || j < 0)
+        return make_float4(0.f, 0.f, 0.f, 0.f);
+    const uint32_t t = __ldg(g.texels + (size_t)j * g.sw + i);
+    return make_float4(__fdiv_rn((float)(t & 0xFFu), 255.0f), __fdiv_rn((float)((t >> 8) & 0xFFu), 255.0f),
+                       __fdiv_rn((float)((t >> 16) & 0xFFu), 255.0f), __fdiv_rn((float)(t >> 24), 255.0f));
+}
+__device__ uint32_t gb_surface_pixel(const gb_grad &g, uint32_t px, uint32_t py) {
+    const float qx = __fsub_rn(__fadd_rn((float)px, 0.5f), g.ox), qy = __fsub_rn(__fadd_rn((float)py, 0.5f), g.oy);
+    const float u  = __fdiv_rn(__fadd_rn(__fadd_rn(__fmul_rn(g.m[0], qx), __fmul_rn(g.m[2], qy)), g.m[4]), (float)g.sw);
+    const float v  = __fdiv_rn(__fadd_rn(__fadd_rn(__fmul_rn(g.m[1], qx), __fmul_rn(g.m[3], qy)), g.m[5]), (float)g.sh);
+    const float us = __fmul_rn(u, (float)g.sw), vs = __fmul_rn(v, (float)g.sh);
+    float4      c;
+    if (g.filter == 0) {
+        c = gb_texel(g, gb_floor_i(us), gb_floor_i(vs));
+    } else {
+        const float a0 = __fsub_rn(us, 0.5f), b0 = __fsub_rn(vs, 0.5f);
+        const float fi = floorf(a0), fj = floorf(b0);
+        /* weights quantised to 8 fractional bits */
+        const float al = __fmul_rn(floorf(__fmul_rn(__fsub_rn(a0, fi), 256.0f)), 1.0f / 256.0f);
+        const float be = __fmul_rn(floorf(__fmul_rn(__fsub_rn(b0, fj), 256.0f)), 1.0f / 256.0f);
+        const int32_t i = gb_floor_i(a0), j = gb_floor_i(b0);
+        const float4  t00 = gb_texel(g, i, j), t10 = gb_texel(g, i + 1, j);
+        const float4  t01 = gb_texel(g, i, j + 1), t11 = gb_texel(g, i + 1, j + 1);
+        const float   w00 = __fmul_rn(__fsub_rn(1.0f, al), __fsub_rn(1.0f, be)), w10 = __fmul_rn(al, __fsub_rn(1.0f, be));
+        const float   w01 = __fmul_rn(__fsub_rn(1.0f, al), be), w11 = __fmul_rn(al, be);
+        auto mixc = [&](float x00, float x10, float x01, float x11) {
+            return __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(w00, x00), __fmul_rn(w10, x10)), __fmul_rn(w01, x01)),
+                             __fmul_rn(w11, x11));
+        };
+        c = make_float4(mixc(t00.x, t10.x, t01.x, t11.x), mixc(t00.y, t10.y, t01.y, t11.y),
+                        mixc(t00.z, t10.z, t01.z, t11.z), mixc(t00.w, t10.w, t01.w, t11.w));
+    }
+    const float cc[4] = {c.x, c.y, c.z, c.w};
+    uint32_t    word  = 0;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        float x = __fmul_rn(__fmul_rn(cc[k], g.opacity), 255.0f);
+        x       = x > 0.0f ? fminf(x, 255.0f) : 0.0f; /* NaN -> 0 */
+        word |= (uint32_t)__float2int_rn(x) << (8 * k);
+    }
+    return word;
+}
 __device__ uint32_t gb_grad_pixel(const gb_grad &g, uint32_t px, uint32_t py) {
+    if (g.type == GB_SRC_SURFACE)
+        return gb_surface_pixel(g, px, py);
     const float p_x = __fdiv_rn(__fadd_rn((float)px, 0.5f), g.w), p_y = __fdiv_rn(__fadd_rn((float)py, 0.5f), g.h);
     float       dist;
     if (g.type == GB_GRAD_RADIAL) {

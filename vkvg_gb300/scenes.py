@@ -311,11 +311,66 @@ def vkvg_clip_cases(width=1024, height=800, samples=4):
             for n, ops in out]
 
 
-def play(ctx, ops):
-    """Replay a scene's calls on a context object with vkvg method names."""
+def surface_mix(n_items=12, size=128, seed=23, samples=4):
+    """Surface sources: two small drawn surfaces (one of odd size) used as
+    sources with vkvg_set_source_surface offsets and as surface patterns with
+    every extend mode, nearest and bilinear filtering and pattern matrices,
+    under translated, rotated and scaled matrices, with opacity, inside
+    save / restore, and after a gradient source (whose surface-size offset a
+    later pattern source inherits)."""
+    r = SplitMix64(seed)
+    u = lambda lo, hi: lo + (hi - lo) * r.rnd()
+
+    def source(w, h):
+        ops = [("set_source_rgba", r.rnd(), r.rnd(), r.rnd(), 0.6), ("paint",)]
+        for _ in range(4):
+            ops += [("move_to", u(0, w), u(0, h))]
+            ops += [("curve_to",) + tuple(u(-0.2, 1.2) * (w if k % 2 == 0 else h) for k in range(6))]
+            ops += [("close_path",), ("set_source_rgba", r.rnd(), r.rnd(), r.rnd(), u(0.5, 1.0)), ("fill_preserve",),
+                    ("set_line_width", u(1, 4)), ("set_source_rgba", r.rnd(), r.rnd(), r.rnd(), 1.0), ("stroke",)]
+        return {"width": w, "height": h, "ops": ops}
+
+    def shape():
+        ops = [("move_to", u(0, size), u(0, size))]
+        for _ in range(2):
+            ops.append(("curve_to",) + tuple(u(-0.1, 1.1) * size for _ in range(6)))
+        return ops + [("close_path",)]
+
+    ops = [("set_source_rgb", 0.9, 0.9, 0.85), ("paint",)]
+    for i in range(n_items):
+        ops.append(("identity_matrix",))
+        if i % 3 == 1:
+            ops += [("translate", u(-20, 20), u(-20, 20)), ("rotate", u(-0.7, 0.7))]
+        elif i % 3 == 2:
+            ops += [("scale", u(0.6, 1.8), u(0.6, 1.8))]
+        src = i % 2
+        if i % 4 == 0:
+            ops.append(("set_source_surface", src, u(-10, size * 0.7), u(-10, size * 0.7)))
+        else:
+            pmat = (u(0.5, 1.5), u(-0.3, 0.3), u(-0.3, 0.3), u(0.5, 1.5), u(-9, 9), u(-9, 9)) if i % 3 else None
+            ops.append(("set_source_surface_pattern", src, i % 4, 4 if i % 5 < 3 else 0, pmat))
+        ops.append(("set_opacity", 1.0 if i % 3 else u(0.3, 0.9)))
+        if i == 5:
+            ops += [("save",), ("set_source_linear", 0.0, 0.0, float(size), 0.0,
+                                [(0.0, 1.0, 0.0, 0.0, 1.0), (1.0, 0.0, 0.0, 1.0, 1.0)], None),
+                    ("set_source_surface_pattern", 1, 1, 4, None)]
+        ops += shape() + [("set_fill_rule", i % 2), ("fill_preserve",), ("set_line_width", u(2, 9)), ("stroke",)]
+        if i == 5:
+            ops += [("restore",), ("rectangle", 4.0, 4.0, 30.0, 20.0), ("fill",)]
+        if i == n_items - 1:
+            ops += [("set_opacity", 0.5), ("paint",)]
+    return {"name": "surface_mix", "width": size, "height": size, "samples": samples, "ops": ops,
+            "paths": n_items, "sources": [source(48, 40), source(33, 17)]}
+
+
+def play(ctx, ops, sources=()):
+    """Replay a scene's calls on a context object with vkvg method names;
+    surface sources name their surface by its index in `sources`."""
     for op in ops:
         name, args = op[0], op[1:]
-        if name == "set_dash":
+        if name in ("set_source_surface", "set_source_surface_pattern"):
+            getattr(ctx, name)(sources[args[0]], *args[1:])
+        elif name == "set_dash":
             ctx.set_dash(args[0], args[1])
         elif name == "set_source_linear":
             ctx.set_source_linear(*args)
