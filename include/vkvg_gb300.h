@@ -154,6 +154,18 @@ vkvg_public uint64_t vkvg_gb300_kernel_launches(void);
 vkvg_public vkvg_status_t vkvg_gb300_exclusive_scan_noalloc(void *stream, const uint32_t *counts, uint32_t n,
                                                              uint32_t *offsets);
 
+/* ---- parsed SVG documents, read back for the parity tests (no vkvg
+ * counterpart; VkvgSvg is include/vkvg-svg.h's handle).  shape: u = fill
+ * paint type, fill colour, stroke paint type, stroke colour (nanoSVG's ABGR
+ * words; a gradient gives its first stop), visible, path count; f = opacity,
+ * stroke width, bounds[4].  path: its cubic points (x, y pairs), at most
+ * cap_points of them copied, and whether it is closed. */
+typedef struct _vkvg_svg_t *VkvgSvgDoc;
+vkvg_public uint32_t vkvg_gb300_svg_shape_count(VkvgSvgDoc svg);
+vkvg_public int      vkvg_gb300_svg_shape(VkvgSvgDoc svg, uint32_t i, char id[64], uint32_t u[6], float f[6]);
+vkvg_public int      vkvg_gb300_svg_path(VkvgSvgDoc svg, uint32_t shape, uint32_t path, float *pts, uint32_t cap_points,
+                                         uint32_t *npts, uint32_t *closed);
+
 #ifdef __cplusplus
 }
 #endif

@@ -170,7 +170,7 @@ VkvgDevice vkvg_device_create(vkvg_device_create_info_t *info) {
     dev->samples = samples;
     cudaGetDevice(&dev->cuda_dev);
     dev->thread_aware = info->threadAware;
-    dev->hdpi = dev->vdpi = 96;
+    dev->hdpi = dev->vdpi = 72; /* _device_init, src/vkvg_device.c:71-72 */
     const uint8_t *lut = gb_unpremul_table();
     if (cudaMalloc(&dev->d_unpremul, 65536) != cudaSuccess ||
         cudaMemcpy(dev->d_unpremul, lut, 65536, cudaMemcpyHostToDevice) != cudaSuccess) {
