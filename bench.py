@@ -58,6 +58,7 @@ def parse():
     p.add_argument("--size", type=int, default=1024)
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     p.add_argument("--svg-shapes", type=int, default=600, help="shapes of the SVG ingestion workload (0: skip)")
+    p.add_argument("--no-batch", action="store_true", help="skip the uneven-batch comparison")
     return p.parse_args()
 
 
@@ -320,6 +321,66 @@ def main():
         ssurf.destroy()
         doc.destroy()
 
+    # ---- the uneven batch (64 surfaces, Pareto path counts): its frames one
+    # after another (the plain form), then as one batch job
+    batch = None
+    if not a.no_batch and world == 1:
+        bs = scenes.batch_streams(seed=2)
+        bframes, bsurf, bctx, btarget = [], [], [], []
+        for s_ in bs:
+            s1 = gb.Surface(dev, s_["width"], s_["height"])
+            s2 = gb.Surface(dev, s_["width"], s_["height"])
+            c1 = s1.context()
+            assert L.vkvg_gb300_replay_stream(c1.h, s_["cmds"].ctypes.data_as(C.c_void_p), len(s_["cmds"]),
+                                              s_["args"].ctypes.data_as(C.c_void_p), len(s_["args"])) == 0
+            bframes.append(L.vkvg_gb300_frame_capture(c1.h))
+            bsurf.append(s1)
+            bctx.append(c1)
+            btarget.append(s2)
+        bpaths = sum(s_["paths"] for s_ in bs)
+
+        def plain_pass():
+            for fr, s1 in zip(bframes, bsurf):
+                assert L.vkvg_gb300_frame_execute(fr, s1.h) == 0
+
+        plain_pass()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(3):
+            plain_pass()
+        torch.cuda.synchronize()
+        plain_s = (time.perf_counter() - t0) / 3
+        fa = (C.c_void_p * len(bframes))(*bframes)
+        ta = (C.c_void_p * len(btarget))(*[s2.h for s2 in btarget])
+        bt = L.vkvg_gb300_batch_create(fa, ta, len(bframes))
+        assert bt
+        for _ in range(6):  # sizing, four tuning runs, graph capture
+            assert L.vkvg_gb300_batch_execute(bt) == 0
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(5):
+            assert L.vkvg_gb300_batch_execute(bt) == 0
+        batch_s = (time.perf_counter() - t0) / 5
+        bt_info = np.zeros(8, np.float32)
+        L.vkvg_gb300_batch_timing(bt, bt_info.ctypes.data_as(C.c_void_p))
+        same = all(np.array_equal(s1.samples_rgba(), s2.samples_rgba()) for s1, s2 in zip(bsurf[:8], btarget[:8]))
+        batch = {"workload": "64 surfaces, side log-U[256,2048], Pareto(1.2) paths in [100,20000], segments "
+                             "log-U[3,2000] (70%% cubic, 20%% line, 10%% arc), seed 2: %d paths, %.1f Mpx" %
+                             (bpaths, sum(s_["width"] * s_["height"] for s_ in bs) / 1e6),
+                 "plain_ms": plain_s * 1e3, "plain_paths_per_s": bpaths / plain_s, "batch_ms": batch_s * 1e3,
+                 "batch_paths_per_s": bpaths / batch_s, "speedup": plain_s / batch_s,
+                 "graph_replay": bool(bt_info[1]), "tuned_stage_min": int(bt_info[2]),
+                 "tuned_heaviest_first": bool(bt_info[3]), "work_items": int(bt_info[4]),
+                 "first_8_surfaces_equal_to_plain": same,
+                 "note": "host timer, device-resident frames; the plain form executes the 64 captured frames one "
+                         "after another"}
+        L.vkvg_gb300_batch_destroy(bt)
+        for fr, c1, s1, s2 in zip(bframes, bctx, bsurf, btarget):
+            L.vkvg_gb300_frame_destroy(fr)
+            c1.destroy()
+            s1.destroy()
+            s2.destroy()
+
     # ---- roofline of the raster/composite kernel
     peak, peak_kind = hbm_peak()
     nflat, nsv = int(stats[1]), int(stats[2])
@@ -366,6 +427,8 @@ def main():
     }
     if svg:
         line["svg"] = svg
+    if batch:
+        line["batch"] = batch
     if rank == 0 and not a.no_cpu:
         threads = os.cpu_count() or 1
         v, _ = cpu_sample(64, a.size, threads)

@@ -342,3 +342,71 @@ def test_surface_source_outlives_its_handles(gb, vko):
     assert ctx.status() == 0
     img = dst.premult()
     assert tuple(img[5, 10]) != (0, 0, 0, 0) and tuple(img[25, 35]) == (0, 0, 0, 0)
+
+
+def _batch_case(gb, dev, sc):
+    """a surface drawn by its own captured frame (executed once), and a
+    second surface for the same frame in a batch"""
+    import ctypes as C
+
+    L = gb.lib()
+    a = gb.Surface(dev, sc["width"], sc["height"])
+    b = gb.Surface(dev, sc["width"], sc["height"])
+    ctx = a.context()
+    if "cmds" in sc:
+        assert L.vkvg_gb300_replay_stream(ctx.h, sc["cmds"].ctypes.data_as(C.c_void_p), len(sc["cmds"]),
+                                          sc["args"].ctypes.data_as(C.c_void_p), len(sc["args"])) == 0
+    else:
+        scenes.play(ctx, sc["ops"])
+    fr = L.vkvg_gb300_frame_capture(ctx.h)
+    assert fr
+    assert L.vkvg_gb300_frame_execute(fr, a.h) == 0
+    return a, b, ctx, fr
+
+
+def test_batch_matches_frames(gb):
+    """a batch of frames (curves, dashes, elliptic arcs and ellipses, uneven
+    generated surfaces) leaves every surface as its own frame does, on the
+    sizing run, on each tuning run and on graph replays"""
+    import ctypes as C
+
+    L = gb.lib()
+    dev = gb.Device(samples=4)
+    scs = [scenes.api_mix(n_items=24, size=160, seed=5), scenes.curve_heavy(n_paths=30, size=256, seed=4, n_min=3,
+                                                                             n_max=10),
+           scenes.plain_small(n_polys=12, size=96, seed=0)]
+    scs += scenes.batch_streams(seed=2, n_surfaces=4, max_paths=80, min_paths=10, max_segs=40, max_side=1200)
+    cases = [_batch_case(gb, dev, sc) for sc in scs]
+    frames = (C.c_void_p * len(cases))(*[c[3] for c in cases])
+    targets = (C.c_void_p * len(cases))(*[c[1].h for c in cases])
+    bt = L.vkvg_gb300_batch_create(frames, targets, len(cases))
+    assert bt
+    t = np.zeros(8, np.float32)
+    for run in range(7):
+        assert L.vkvg_gb300_batch_execute(bt) == 0, run
+        L.vkvg_gb300_batch_timing(bt, t.ctypes.data_as(C.c_void_p))
+        for k, (a, b, _, _) in enumerate(cases):
+            assert np.array_equal(a.samples_rgba(), b.samples_rgba()), (run, k)
+            assert np.array_equal(a.image(), b.image()), (run, k)
+    assert t[1] == 1 and t[6] == 1 and t[5] == len(cases)  # graph replay, tuned
+    L.vkvg_gb300_batch_destroy(bt)
+    for _, _, ctx, fr in cases:
+        L.vkvg_gb300_frame_destroy(fr)
+        ctx.destroy()
+
+
+def test_batch_rejects_clip_and_duplicates(gb):
+    import ctypes as C
+
+    L = gb.lib()
+    dev = gb.Device(samples=4)
+    sc = {"name": "clipped", "width": 64, "height": 64, "samples": 4, "paths": 1,
+          "ops": [("rectangle", 4.0, 4.0, 30.0, 30.0), ("clip",), ("set_source_rgb", 1.0, 0.0, 0.0), ("paint",)]}
+    a, b, ctx, fr = _batch_case(gb, dev, sc)
+    assert not L.vkvg_gb300_batch_create((C.c_void_p * 1)(fr), (C.c_void_p * 1)(b.h), 1)
+    sc2 = scenes.plain_small(n_polys=4, size=64, seed=1)
+    a2, b2, ctx2, fr2 = _batch_case(gb, dev, sc2)
+    assert not L.vkvg_gb300_batch_create((C.c_void_p * 2)(fr2, fr2), (C.c_void_p * 2)(b2.h, b2.h), 2)
+    for c, f in ((ctx, fr), (ctx2, fr2)):
+        L.vkvg_gb300_frame_destroy(f)
+        c.destroy()

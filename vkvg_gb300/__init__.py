@@ -165,6 +165,10 @@ SIGNATURES = {
     "vkvg_gb300_pmath_eval": (_I, [_I, _P, _P, _P, C.c_uint64, _I]),
     "vkvg_gb300_kernel_launches": (C.c_uint64, []),
     "vkvg_gb300_exclusive_scan_noalloc": (_I, [_P, _P, C.c_uint32, _P]),
+    "vkvg_gb300_batch_create": (_P, [_P, _P, _U]),
+    "vkvg_gb300_batch_execute": (_I, [_P]),
+    "vkvg_gb300_batch_timing": (_I, [_P, _P]),
+    "vkvg_gb300_batch_destroy": (None, [_P]),
     # include/vkvg-svg.h
     "vkvg_svg_load": (_P, [C.c_char_p]),
     "vkvg_svg_load_fragment": (_P, [C.c_char_p]),

@@ -24,7 +24,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_GEOM = ["flatten.cu", "stroke.cu", "setup.cu"]
 CU_FAST = ["raster.cu", "scan.cu"]
-CPP = ["api.cpp", "pipeline.cpp", "extras.cpp", "png.cpp", "svg.cpp"]
+CPP = ["api.cpp", "pipeline.cpp", "extras.cpp", "png.cpp", "svg.cpp", "batch.cpp"]
 HEADERS = ["gb_types.h", "pmath.h", "launch.h", "host.h", "xdiv.cuh"]
 
 NVCC_COMMON = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-fvisibility=hidden",

@@ -77,7 +77,22 @@ typedef struct {
     float    arc_step; /* _get_arc_step(hw) under the draw's CTM */
     float    mat[6];   /* xx yx xy yy x0 y0 */
     uint32_t gsrc;     /* 0: the solid colour src; i + 1: gradient source image i of the frame */
+    uint32_t surf;     /* its surface's entry in the frame's surface table (0 but in a batch) */
 } gb_draw;
+
+/* One target surface of a frame (one entry for a context's frame; one per
+   surface for a batch of frames): its size and sample buffers, its draws
+   [draw0, draw0 + ndraws) of the frame, and its bins, cells
+   [cell0, cell0 + nbands * ndraws) band-major; init_* describe a first draw
+   the raster can apply while loading the tile (a clear or an opaque paint). */
+typedef struct {
+    uint32_t  W, H, nrows, nbands, wpad;
+    uint32_t  draw0, ndraws, draw_first;
+    uint32_t  init_mode, init_color;
+    uint64_t  cell0;
+    uint32_t *samples; /* [nrows][wpad] premultiplied RGBA8 */
+    uint32_t *rgba;    /* [H][W] resolved */
+} gb_surf;
 
 /* A pattern source as vkvg's fragment stage sees it (shaders/vkvg_main.frag
    SURFACE, LINEAR and RADIAL cases).  Gradients (data of _update_cur_pattern):

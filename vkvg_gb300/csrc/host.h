@@ -90,7 +90,9 @@ struct Pipeline {
     DevBuf       cells, cursor, recs, status, dbg;
     DevBuf       dseglen, dseg, dfin;
     DevBuf       tri_idx; /* oriented vertex indices of stroke triangles (edge cancellation) */
-    DevBuf       gsrc;    /* gradient source images of the frame, [n][H][W] */ /* parallel dash walk: per-point lengths / states, per-pair final state */
+    DevBuf       gsrc;    /* gradient source images of the frame, [n][H][W] */
+    DevBuf       surf_tab; /* the frame's surface table (gb_surf) */
+    PinnedBuf    surf_stage; /* parallel dash walk: per-point lengths / states, per-pair final state */
     PinnedBuf    staging, rb;
     cudaEvent_t  evs[8] = {};
     /* offsets of the uploaded arrays inside `in` */
@@ -111,6 +113,8 @@ struct Pipeline {
     cudaError_t upload(const FrameHost &f);
     /* run the uploaded frame on a surface */
     cudaError_t run(const FrameHost &f, struct _vkvg_surface_t *surf, bool timing);
+    cudaError_t geometry(const FrameHost &f, const gb_surf *surfs, uint64_t ncells, uint32_t S, bool timing,
+                         bool sized);
     /* K1 only: flatten the uploaded segments (for vkvg_path_extents) */
     cudaError_t flatten_only();
 };

@@ -20,6 +20,7 @@ struct gb_raster_args {
     int32_t        *cov_out; /* debug coverage output [H][W][S] or null */
     uint32_t        cov_draw;
     const uint32_t *gsrc;   /* gradient source images [n][H][W], premultiplied RGBA8 */
+    uint32_t        stage_min; /* cells of fewer record units are read from global memory, not staged */
 };
 /* the clip planes, a kernel parameter of their own (read by the clipping
    variant only; kept out of gb_raster_args, whose size the register
@@ -97,18 +98,25 @@ cudaError_t gb_launch_fill_pair_edges(cudaStream_t st, uint32_t npairs, const ui
                                       const uint32_t *sub_npts, uint32_t *counts);
 cudaError_t gb_launch_fill_edges(cudaStream_t st, uint32_t nedges, uint32_t npairs, const uint32_t *e_off,
                                  const uint32_t *pair_draw, const uint32_t *pair_sub, const gb_draw *draws,
-                                 const uint32_t *sub_pt0, const uint32_t *sub_npts, const float2 *pts, uint32_t W,
-                                 uint32_t H, int4 *edges, uint32_t *edge_draw);
+                                 const uint32_t *sub_pt0, const uint32_t *sub_npts, const float2 *pts,
+                                 const gb_surf *surfs, int4 *edges, uint32_t *edge_draw);
 cudaError_t gb_launch_stroke_tris(cudaStream_t st, uint32_t ntris, uint32_t ndraw_s, const uint32_t *draw_tri0,
                                   const uint32_t *sdraw_id, const uint32_t *draw_vbase, const gb_draw *draws,
-                                  const float2 *verts, const uint32_t *inds, uint32_t W, uint32_t H, int4 *tri_a,
+                                  const float2 *verts, const uint32_t *inds, const gb_surf *surfs, int4 *tri_a,
                                   int4 *tri_b, uint32_t *tri_draw, uint4 *tri_idx, int4 *edges, uint32_t *edge_draw);
 cudaError_t gb_launch_bin(cudaStream_t st, int scatter, uint32_t nedges, const int4 *edges, const uint32_t *edge_draw,
-                          uint32_t ndraws, uint32_t W, uint32_t samples, uint32_t nrows, uint32_t *cell, int4 *recs,
+                          const gb_draw *draws, const gb_surf *surfs, uint32_t samples, uint32_t *cell, int4 *recs,
                           uint32_t nunits);
 
 cudaError_t gb_launch_raster(cudaStream_t st, const gb_raster_args *a, const gb_clip_args *c, int gradients,
                              int clipping);
+/* out[i] = src[idx[i]] */
+cudaError_t gb_launch_gather_u32(cudaStream_t st, uint32_t n, const uint64_t *idx, const uint32_t *src,
+                                 uint32_t *out);
+/* the persistent batch raster over a work list of (surface, band, tile, -)
+   items (queue: a zeroed counter), nctas CTAs */
+cudaError_t gb_launch_raster_batch(cudaStream_t st, const gb_raster_args *a, const gb_surf *surfs, const uint4 *items,
+                                   uint32_t nitems, uint32_t *queue, uint32_t nctas);
 cudaError_t gb_launch_pmath_eval(cudaStream_t st, int fn, const float *a, const float *b, float *out, uint64_t n);
 }
 

@@ -100,10 +100,11 @@ void Pipeline::destroy() {
     DevBuf *bufs[] = {&in,     &seg_cnt, &seg_off,   &scratch,    &pts,         &pflag,    &sub_pt0, &sub_npts,
                       &ev_cnt, &ev_off,  &events,    &cnt_v,      &cnt_i,       &off_v,    &off_i,   &verts,
                       &inds,   &ev_ret,  &fe_cnt,    &fe_off,     &edges,       &edge_draw, &sdraw_tri0,
-                      &sdraw_vbase, &tri_a, &tri_b, &tri_draw, &cells,   &cursor,   &recs,    &status, &dseglen, &dseg, &dfin, &tri_idx, &gsrc, &dbg};
+                      &sdraw_vbase, &tri_a, &tri_b, &tri_draw, &cells,   &cursor,   &recs,    &status, &dseglen, &dseg, &dfin, &tri_idx, &gsrc, &dbg, &surf_tab};
     for (DevBuf *b : bufs)
         b->release();
     staging.release();
+    surf_stage.release();
     rb.release();
     for (auto &e : evs)
         if (e)
@@ -190,7 +191,12 @@ static cudaError_t scan(Pipeline &pl, const uint32_t *in, uint32_t n, uint32_t *
             return cudaErrorMemoryAllocation;                                                                          \
     } while (0)
 
-cudaError_t Pipeline::run(const FrameHost &f, _vkvg_surface_t *surf, bool timing) {
+/* flattening, stroke expansion, primitive set-up and binning of the uploaded
+   frame into the cells of its surface table (ncells cells in all).  With
+   sized, the sizes of a previous run of the same frame are reused and nothing
+   is read back, so the sequence can be captured in a CUDA graph. */
+cudaError_t Pipeline::geometry(const FrameHost &f, const gb_surf *surfs, uint64_t ncells, uint32_t S, bool timing,
+                               bool sized) {
     const uint8_t *I        = (const uint8_t *)in.p;
     auto           U        = [&](size_t o) { return (const uint32_t *)(I + o); };
     const uint32_t *seg_inf = U(o_seg_info);
@@ -212,8 +218,10 @@ cudaError_t Pipeline::run(const FrameHost &f, _vkvg_surface_t *surf, bool timing
                                status.as<uint32_t>()));
     gb_count_launch(nseg ? 1 : 0);
     CK(scan(*this, seg_cnt.as<uint32_t>(), nseg, seg_off.as<uint32_t>()));
-    CK(readback_u32(*this, seg_off.as<uint32_t>() + nseg, hv, 1));
-    npts = hv[0];
+    if (!sized) {
+        CK(readback_u32(*this, seg_off.as<uint32_t>() + nseg, hv, 1));
+        npts = hv[0];
+    }
     GROW(pts, (size_t)(npts + 1) * 8);
     GROW(pflag, (size_t)(npts + 1));
     GROW(sub_pt0, (size_t)(nsub + 1) * 4);
@@ -249,12 +257,14 @@ cudaError_t Pipeline::run(const FrameHost &f, _vkvg_surface_t *surf, bool timing
     gb_count_launch((nspair ? 1 : 0) + (nfpair ? 1 : 0));
     CK(scan(*this, ev_cnt.as<uint32_t>(), nspair, ev_off.as<uint32_t>()));
     CK(scan(*this, fe_cnt.as<uint32_t>(), nfpair, fe_off.as<uint32_t>()));
-    CK(cudaMemcpyAsync(rb.p, ev_off.as<uint32_t>() + nspair, 4, cudaMemcpyDeviceToHost, st));
-    CK(cudaMemcpyAsync((uint8_t *)rb.p + 4, fe_off.as<uint32_t>() + nfpair, 4, cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
-    memcpy(hv, rb.p, 8);
-    nev    = hv[0];
-    nedges = hv[1];
+    if (!sized) {
+        CK(cudaMemcpyAsync(rb.p, ev_off.as<uint32_t>() + nspair, 4, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync((uint8_t *)rb.p + 4, fe_off.as<uint32_t>() + nfpair, 4, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        memcpy(hv, rb.p, 8);
+        nev    = hv[0];
+        nedges = hv[1];
+    }
     GROW(events, (size_t)(f.any_dash ? nev + 1 : 1) * sizeof(gb_event));
     if (fast_dash) {
         CK(gb_launch_dash_emit(st, nspair, U(o_spd), U(o_sps), draws, sub_pt0.as<uint32_t>(), sub_npts.as<uint32_t>(),
@@ -278,13 +288,15 @@ cudaError_t Pipeline::run(const FrameHost &f, _vkvg_surface_t *surf, bool timing
     gb_count_launch(nev ? 1 : 0);
     CK(scan(*this, cnt_v.as<uint32_t>(), nev, off_v.as<uint32_t>()));
     CK(scan(*this, cnt_i.as<uint32_t>(), nev, off_i.as<uint32_t>()));
-    CK(cudaMemcpyAsync(rb.p, off_v.as<uint32_t>() + nev, 4, cudaMemcpyDeviceToHost, st));
-    CK(cudaMemcpyAsync((uint8_t *)rb.p + 4, off_i.as<uint32_t>() + nev, 4, cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
-    memcpy(hv, rb.p, 8);
-    nverts = hv[0];
-    ninds  = hv[1];
-    ntris  = ninds / 3;
+    if (!sized) {
+        CK(cudaMemcpyAsync(rb.p, off_v.as<uint32_t>() + nev, 4, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync((uint8_t *)rb.p + 4, off_i.as<uint32_t>() + nev, 4, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        memcpy(hv, rb.p, 8);
+        nverts = hv[0];
+        ninds  = hv[1];
+        ntris  = ninds / 3;
+    }
     GROW(verts, (size_t)(nverts + 1) * 8);
     GROW(inds, (size_t)(ninds + 1) * 4);
     GROW(ev_ret, (size_t)(nev + 1));
@@ -306,7 +318,6 @@ cudaError_t Pipeline::run(const FrameHost &f, _vkvg_surface_t *surf, bool timing
         CK(cudaEventRecord(evs[2], st));
 
     /* ---------------- K3 primitive setup + binning */
-    const uint32_t W = surf->width, H = surf->height, S = surf->samples;
     /* edges: fill edges, then three slots per stroke triangle */
     const uint32_t nedge_all = nedges + 3 * ntris;
     GROW(edges, (size_t)(nedge_all + 1) * 16);
@@ -316,32 +327,57 @@ cudaError_t Pipeline::run(const FrameHost &f, _vkvg_surface_t *surf, bool timing
     GROW(tri_draw, (size_t)(ntris + 1) * 4);
     GROW(tri_idx, (size_t)(ntris + 1) * 16);
     CK(gb_launch_fill_edges(st, nedges, nfpair, fe_off.as<uint32_t>(), U(o_fpd), U(o_fps), draws,
-                            sub_pt0.as<uint32_t>(), sub_npts.as<uint32_t>(), pts.as<float2>(), W, H, edges.as<int4>(),
+                            sub_pt0.as<uint32_t>(), sub_npts.as<uint32_t>(), pts.as<float2>(), surfs, edges.as<int4>(),
                             edge_draw.as<uint32_t>()));
     CK(gb_launch_stroke_tris(st, ntris, nsdraw, sdraw_tri0.as<uint32_t>(), U(o_sdid), sdraw_vbase.as<uint32_t>(),
-                             draws, verts.as<float2>(), inds.as<uint32_t>(), W, H, tri_a.as<int4>(), tri_b.as<int4>(),
+                             draws, verts.as<float2>(), inds.as<uint32_t>(), surfs, tri_a.as<int4>(), tri_b.as<int4>(),
                              tri_draw.as<uint32_t>(), tri_idx.as<uint4>(), edges.as<int4>() + nedges,
                              edge_draw.as<uint32_t>() + nedges));
     gb_count_launch((nedges ? 1 : 0) + (ntris ? 2 : 0));
-    nbands          = surf->nbands;
-    size_t ncells   = (size_t)nbands * ndraw;
     GROW(cells, (ncells + 1) * 4);
     GROW(cursor, (ncells + 1) * 4);
     CK(cudaMemsetAsync(cells.p, 0, (ncells + 1) * 4, st));
-    CK(gb_launch_bin(st, 0, nedge_all, edges.as<int4>(), edge_draw.as<uint32_t>(), ndraw, W, S, surf->nrows,
+    CK(gb_launch_bin(st, 0, nedge_all, edges.as<int4>(), edge_draw.as<uint32_t>(), draws, surfs, S,
                      cells.as<uint32_t>(), nullptr, 0u));
     gb_count_launch(nedge_all ? 1 : 0);
     CK(scan(*this, cells.as<uint32_t>(), (uint32_t)ncells, cursor.as<uint32_t>()));
-    CK(readback_u32(*this, cursor.as<uint32_t>() + ncells, hv, 1));
-    nunits = hv[0];
+    if (!sized) {
+        CK(readback_u32(*this, cursor.as<uint32_t>() + ncells, hv, 1));
+        nunits = hv[0];
+    }
     GROW(recs, (size_t)(nunits + 1) * 16);
     /* cells <- offsets (kept for the raster), cursor <- running copy */
     CK(cudaMemcpyAsync(cells.p, cursor.p, (ncells + 1) * 4, cudaMemcpyDeviceToDevice, st));
-    CK(gb_launch_bin(st, 1, nedge_all, edges.as<int4>(), edge_draw.as<uint32_t>(), ndraw, W, S, surf->nrows,
+    CK(gb_launch_bin(st, 1, nedge_all, edges.as<int4>(), edge_draw.as<uint32_t>(), draws, surfs, S,
                      cursor.as<uint32_t>(), recs.as<int4>(), nunits));
     gb_count_launch(nedge_all ? 1 : 0);
     if (timing)
         CK(cudaEventRecord(evs[3], st));
+    return cudaSuccess;
+}
+
+cudaError_t Pipeline::run(const FrameHost &f, _vkvg_surface_t *surf, bool timing) {
+    const uint8_t  *I     = (const uint8_t *)in.p;
+    const gb_draw  *draws = (const gb_draw *)(I + o_draws);
+    const uint32_t  W = surf->width, H = surf->height, S = surf->samples;
+    nbands                = surf->nbands;
+    /* the frame's surface table: its one target */
+    gb_surf sd;
+    memset(&sd, 0, sizeof(sd));
+    sd.W       = W;
+    sd.H       = H;
+    sd.nrows   = surf->nrows;
+    sd.nbands  = nbands;
+    sd.wpad    = surf->wpad;
+    sd.ndraws  = ndraw;
+    sd.samples = surf->d_samples;
+    sd.rgba    = surf->d_rgba;
+    if (!surf_stage.grow(sizeof(gb_surf)))
+        return cudaErrorMemoryAllocation;
+    GROW(surf_tab, sizeof(gb_surf));
+    memcpy(surf_stage.p, &sd, sizeof(sd));
+    CK(cudaMemcpyAsync(surf_tab.p, surf_stage.p, sizeof(sd), cudaMemcpyHostToDevice, st));
+    CK(geometry(f, surf_tab.as<gb_surf>(), (uint64_t)nbands * ndraw, S, timing, false));
 
     /* ---------------- K5 coverage + compositing */
     gb_raster_args A;

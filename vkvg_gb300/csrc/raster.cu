@@ -381,14 +381,15 @@ __device__ __forceinline__ uint32_t clip_bits(const int4 *cp, uint32_t v, int32_
     return bits;
 }
 
+/* One cell of the raster: sample rows [16 band, 16 band + 16) and columns
+   [1024 tile, 1024 tile + 1024) of A's surface, through every draw of the
+   surface in order, then the resolve of its pixels. */
 template <bool GRAD, bool CLIP>
-__global__ void __launch_bounds__(XT_THREADS, 1) gb_raster(gb_raster_args A, gb_clip_args C) {
-    extern __shared__ __align__(16) int32_t smem[];
-
+__device__ __forceinline__ void raster_item(const gb_raster_args &A, const gb_clip_args &C, int32_t *smem,
+                                            uint32_t band, uint32_t tile) {
     const uint32_t t = threadIdx.x, wi = t >> 5, l = t & 31;
     const uint32_t rl = l >> 1, hh = l & 1; /* blend mapping: band row and half-strip */
-    const uint32_t band    = blockIdx.y;
-    const int32_t  X0      = (int32_t)(blockIdx.x * XT_W);
+    const int32_t  X0      = (int32_t)(tile * XT_W);
     const int32_t  TW      = min((int32_t)XT_W, (int32_t)A.W - X0);
     const int32_t  R       = (int32_t)(band * GB_BAND_ROWS + rl);
     const bool     row_ok  = R < (int32_t)A.nrows;
@@ -548,22 +549,29 @@ __global__ void __launch_bounds__(XT_THREADS, 1) gb_raster(gb_raster_args A, gb_
             /* this draw's records: staged now unless prefetched; then prefetch
                the next geometry draw into the other buffer, whose readers all
                passed the previous barrier */
-            const uint32_t sb = nproc & 1;
-            const uint32_t su = min(hi - lo, (uint32_t)STAGE_CAP);
-            if ((sb ? stg_d1 : stg_d0) != d)
+            /* cells below stage_min units are read from global memory by
+               the accumulating threads instead (the same test decides the
+               prefetch, so every copy issued is waited for) */
+            const uint32_t sb  = nproc & 1;
+            const bool     stg = hi - lo >= A.stage_min;
+            const uint32_t su  = stg ? min(hi - lo, (uint32_t)STAGE_CAP) : 0u;
+            if (stg && (sb ? stg_d1 : stg_d0) != d)
                 stage_cell(sb, d, lo, su);
-            if (nx_have && is_geom<CLIP>(nx_kind) && nx_lo < nx_hi && nx_hi <= A.nunits)
+            if (nx_have && is_geom<CLIP>(nx_kind) && nx_lo < nx_hi && nx_hi <= A.nunits &&
+                nx_hi - nx_lo >= A.stage_min)
                 stage_cell(sb ^ 1u, nx_d, nx_lo, min(nx_hi - nx_lo, (uint32_t)STAGE_CAP));
-            if (mbar_wait(bar0 + 8 * sb, (stg_par >> sb) & 1u)) {
-                stg_pend &= ~(1u << sb);
-            } else if (t == 0) {
-                atomicOr(A.status, GB_ERR_RASTER_WAIT);
+            if (stg) {
+                if (mbar_wait(bar0 + 8 * sb, (stg_par >> sb) & 1u)) {
+                    stg_pend &= ~(1u << sb);
+                } else if (t == 0) {
+                    atomicOr(A.status, GB_ERR_RASTER_WAIT);
+                }
+                stg_par ^= 1u << sb;
+                if (sb)
+                    stg_d1 = 0xFFFFFFFFu;
+                else
+                    stg_d0 = 0xFFFFFFFFu;
             }
-            stg_par ^= 1u << sb;
-            if (sb)
-                stg_d1 = 0xFFFFFFFFu;
-            else
-                stg_d0 = 0xFFFFFFFFu;
             const int4 *sg = reinterpret_cast<const int4 *>(smem + SM_STAGE) + sb * STAGE_CAP;
             int32_t *plane = smem + (nproc & 1) * XPLANE;
             int32_t *tot   = smem + SM_TOT + (nproc % 3) * TOT_SET;
@@ -742,6 +750,66 @@ __global__ void __launch_bounds__(XT_THREADS, 1) gb_raster(gb_raster_args A, gb_
             for (int k = 0; k < 4; k++)
                 if ((int32_t)(px + k) < TW)
                     dst[k] = outp[k];
+        }
+    }
+}
+
+template <bool GRAD, bool CLIP>
+__global__ void __launch_bounds__(XT_THREADS, 1) gb_raster(gb_raster_args A, gb_clip_args C) {
+    extern __shared__ __align__(16) int32_t smem[];
+    raster_item<GRAD, CLIP>(A, C, smem, blockIdx.y, blockIdx.x);
+}
+
+__device__ __forceinline__ void mbar_inval(uint32_t bar) {
+    asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(bar) : "memory");
+}
+/* The batch raster: a persistent grid (one CTA per SM) takes (surface, band,
+   tile) items from the work list in queue order until it is exhausted (no
+   wait on other CTAs: each CTA stops at the end of the list).  An item's
+   arguments are its surface's entry of the table over A0's shared fields,
+   staged in shared memory for the whole CTA. */
+__global__ void __launch_bounds__(XT_THREADS, 1)
+    gb_raster_batch(gb_raster_args A0, const gb_surf *__restrict__ surfs, const uint4 *__restrict__ items,
+                    uint32_t nitems, uint32_t *__restrict__ queue) {
+    extern __shared__ __align__(16) int32_t smem[];
+    __shared__ gb_raster_args Ai;
+    __shared__ uint32_t       cur_item, cur_band, cur_tile;
+    const gb_clip_args        C0 = {};
+    for (uint32_t iter = 0; iter < nitems; iter++) {
+        if (threadIdx.x == 0) {
+            const uint32_t it = atomicAdd(queue, 1u);
+            cur_item          = it;
+            if (it < nitems) {
+                const uint4    w  = items[it];
+                const gb_surf &sf = surfs[w.x];
+                gb_raster_args a  = A0;
+                a.W               = sf.W;
+                a.H               = sf.H;
+                a.Wpad            = sf.wpad;
+                a.nrows           = sf.nrows;
+                a.nbands          = sf.nbands;
+                a.ndraws          = sf.ndraws;
+                a.draw_first      = sf.draw_first;
+                a.init_mode       = sf.init_mode;
+                a.init_color      = sf.init_color;
+                a.draws           = A0.draws + sf.draw0;
+                a.cell_off        = A0.cell_off + sf.cell0;
+                a.samples         = sf.samples;
+                a.rgba            = sf.rgba;
+                Ai                = a;
+                cur_band          = w.y;
+                cur_tile          = w.z;
+            }
+        }
+        __syncthreads();
+        if (cur_item >= nitems)
+            break;
+        raster_item<false, false>(Ai, C0, smem, cur_band, cur_tile);
+        __syncthreads();
+        if (threadIdx.x == 0) { /* the next item initialises them again */
+            const uint32_t bar0 = (uint32_t)__cvta_generic_to_shared(smem) + SM_MBAR * 4;
+            mbar_inval(bar0);
+            mbar_inval(bar0 + 8);
         }
     }
 }
@@ -956,7 +1024,22 @@ extern "C" cudaError_t gb_launch_unpremultiply(cudaStream_t st, const uint32_t *
     return cudaGetLastError();
 }
 
-extern "C" cudaError_t gb_launch_raster(cudaStream_t st, const gb_raster_args *a, const gb_clip_args *c, int gradients, int clipping) {
+extern "C" cudaError_t gb_launch_raster_batch(cudaStream_t st, const gb_raster_args *a, const gb_surf *surfs,
+                                             const uint4 *items, uint32_t nitems, uint32_t *queue, uint32_t nctas) {
+    static bool configured = false;
+    if (!configured) {
+        cudaError_t e = cudaFuncSetAttribute(gb_raster_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, RASTER_SMEM);
+        if (e != cudaSuccess)
+            return e;
+        configured = true;
+    }
+    if (!nitems)
+        return cudaSuccess;
+    gb_raster_batch<<<nctas, XT_THREADS, RASTER_SMEM, st>>>(*a, surfs, items, nitems, queue);
+    return cudaGetLastError();
+}
+extern "C" cudaError_t gb_launch_raster(cudaStream_t st, const gb_raster_args *a, const gb_clip_args *c, int gradients,
+                                       int clipping) {
     static bool configured = false;
     if (!configured) {
         cudaError_t e = cudaFuncSetAttribute(gb_raster<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,

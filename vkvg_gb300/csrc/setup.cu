@@ -83,15 +83,17 @@ __global__ void gb_fill_pair_edges(uint32_t npairs, const uint32_t *__restrict__
 __global__ void gb_fill_edges(uint32_t nedges, uint32_t npairs, const uint32_t *__restrict__ e_off,
                               const uint32_t *__restrict__ pair_draw, const uint32_t *__restrict__ pair_sub,
                               const gb_draw *__restrict__ draws, const uint32_t *__restrict__ sub_pt0,
-                              const uint32_t *__restrict__ sub_npts, const float2 *__restrict__ pts, uint32_t W,
-                              uint32_t H, int4 *__restrict__ edges, uint32_t *__restrict__ edge_draw) {
+                              const uint32_t *__restrict__ sub_npts, const float2 *__restrict__ pts,
+                              const gb_surf *__restrict__ surfs, int4 *__restrict__ edges,
+                              uint32_t *__restrict__ edge_draw) {
     uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= nedges)
         return;
     uint32_t p = gb_find(e_off, npairs, e);
     uint32_t s = pair_sub[p], d = pair_draw[p];
     uint32_t j = e - e_off[p], n = sub_npts[s], first = sub_pt0[s];
-    gb_vp    m = make_vp(draws[d], W, H);
+    const gb_surf &sf = surfs[draws[d].surf];
+    gb_vp          m  = make_vp(draws[d], sf.W, sf.H);
     int2     a = gb_snap(m, pts[first + j], nullptr);
     int2     b = gb_snap(m, pts[first + (j + 1 == n ? 0 : j + 1)], nullptr);
     edges[e]     = make_int4(a.x, a.y, b.x, b.y);
@@ -102,7 +104,8 @@ __global__ void gb_fill_edges(uint32_t nedges, uint32_t npairs, const uint32_t *
 __global__ void gb_stroke_tris(uint32_t ntris, uint32_t ndraw_s, const uint32_t *__restrict__ draw_tri0,
                                const uint32_t *__restrict__ sdraw_id, const uint32_t *__restrict__ draw_vbase,
                                const gb_draw *__restrict__ draws, const float2 *__restrict__ verts,
-                               const uint32_t *__restrict__ inds, uint32_t W, uint32_t H, int4 *__restrict__ tri_a,
+                               const uint32_t *__restrict__ inds, const gb_surf *__restrict__ surfs,
+                               int4 *__restrict__ tri_a,
                                int4 *__restrict__ tri_b, uint32_t *__restrict__ tri_draw,
                                uint4 *__restrict__ tri_idx) {
     uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -110,7 +113,8 @@ __global__ void gb_stroke_tris(uint32_t ntris, uint32_t ndraw_s, const uint32_t 
         return;
     uint32_t k  = gb_find(draw_tri0, ndraw_s, t);
     uint32_t d  = sdraw_id[k];
-    gb_vp    m  = make_vp(draws[d], W, H);
+    const gb_surf &sf = surfs[draws[d].surf];
+    gb_vp          m  = make_vp(draws[d], sf.W, sf.H);
     uint32_t vb = draw_vbase[k], nv = draw_vbase[k + 1] - vb;
     uint32_t i0 = inds[3 * t], i1 = inds[3 * t + 1], i2 = inds[3 * t + 2];
     bool     inb = i0 < nv && i1 < nv && i2 < nv;
@@ -224,29 +228,45 @@ __device__ __forceinline__ bool gb_prim_bands(int32_t ylo, int32_t yhi, int32_t 
 }
 
 /* Binning: count (SCATTER false) or write (SCATTER true) each edge's record
-   (x0, y0, x1, y1) into every (band, draw) cell it touches, so that a cell is
-   one contiguous block of 16-byte records the raster can stage with a single
-   bulk copy. */
+   (x0, y0, x1, y1) into every (band, draw) cell of its surface it touches,
+   so that a cell is one contiguous block of 16-byte records the raster can
+   stage with a single bulk copy. */
 template <bool SCATTER>
 __global__ void gb_bin_edges(uint32_t nedges, const int4 *__restrict__ edges, const uint32_t *__restrict__ edge_draw,
-                             uint32_t ndraws, uint32_t W, uint32_t samples, uint32_t nrows,
+                             const gb_draw *__restrict__ draws, const gb_surf *__restrict__ surfs, uint32_t samples,
                              uint32_t *__restrict__ cell, int4 *__restrict__ recs, uint32_t nunits) {
     uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= nedges)
         return;
-    int4     ed = edges[e];
-    uint32_t b0, b1;
-    int32_t  ylo = min(ed.y, ed.w), yhi = max(ed.y, ed.w);
-    if (!gb_prim_bands(ylo, yhi, max(ed.x, ed.z), samples, nrows, &b0, &b1))
+    int4           ed = edges[e];
+    const uint32_t d  = edge_draw[e];
+    const gb_surf &sf = surfs[draws[d].surf];
+    uint32_t       b0, b1;
+    int32_t        ylo = min(ed.y, ed.w), yhi = max(ed.y, ed.w);
+    if (!gb_prim_bands(ylo, yhi, max(ed.x, ed.z), samples, sf.nrows, &b0, &b1))
         return;
-    uint32_t d = edge_draw[e];
+    uint32_t *c = cell + sf.cell0 + (d - sf.draw0);
     for (uint32_t b = b0; b <= b1; b++) {
-        uint32_t slot = atomicAdd(&cell[(size_t)b * ndraws + d], 1u);
+        uint32_t slot = atomicAdd(&c[(size_t)b * sf.ndraws], 1u);
         if (SCATTER && slot < nunits)
             recs[slot] = ed;
     }
 }
+/* out[i] = src[idx[i]] */
+__global__ void gb_gather_u32(uint32_t n, const uint64_t *__restrict__ idx, const uint32_t *__restrict__ src,
+                              uint32_t *__restrict__ out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n)
+        out[i] = src[idx[i]];
+}
 extern "C" {
+cudaError_t gb_launch_gather_u32(cudaStream_t st, uint32_t n, const uint64_t *idx, const uint32_t *src,
+                                 uint32_t *out) {
+    if (!n)
+        return cudaSuccess;
+    gb_gather_u32<<<(n + 255) / 256, 256, 0, st>>>(n, idx, src, out);
+    return cudaGetLastError();
+}
 cudaError_t gb_launch_fill_pair_edges(cudaStream_t st, uint32_t npairs, const uint32_t *pair_sub,
                                       const uint32_t *sub_npts, uint32_t *counts) {
     if (!npairs)
@@ -256,35 +276,35 @@ cudaError_t gb_launch_fill_pair_edges(cudaStream_t st, uint32_t npairs, const ui
 }
 cudaError_t gb_launch_fill_edges(cudaStream_t st, uint32_t nedges, uint32_t npairs, const uint32_t *e_off,
                                  const uint32_t *pair_draw, const uint32_t *pair_sub, const gb_draw *draws,
-                                 const uint32_t *sub_pt0, const uint32_t *sub_npts, const float2 *pts, uint32_t W,
-                                 uint32_t H, int4 *edges, uint32_t *edge_draw) {
+                                 const uint32_t *sub_pt0, const uint32_t *sub_npts, const float2 *pts,
+                                 const gb_surf *surfs, int4 *edges, uint32_t *edge_draw) {
     if (!nedges)
         return cudaSuccess;
     gb_fill_edges<<<(nedges + 255) / 256, 256, 0, st>>>(nedges, npairs, e_off, pair_draw, pair_sub, draws, sub_pt0,
-                                                         sub_npts, pts, W, H, edges, edge_draw);
+                                                         sub_npts, pts, surfs, edges, edge_draw);
     return cudaGetLastError();
 }
 cudaError_t gb_launch_stroke_tris(cudaStream_t st, uint32_t ntris, uint32_t ndraw_s, const uint32_t *draw_tri0,
                                   const uint32_t *sdraw_id, const uint32_t *draw_vbase, const gb_draw *draws,
-                                  const float2 *verts, const uint32_t *inds, uint32_t W, uint32_t H, int4 *tri_a,
+                                  const float2 *verts, const uint32_t *inds, const gb_surf *surfs, int4 *tri_a,
                                   int4 *tri_b, uint32_t *tri_draw, uint4 *tri_idx, int4 *edges, uint32_t *edge_draw) {
     if (!ntris)
         return cudaSuccess;
     gb_stroke_tris<<<(ntris + 255) / 256, 256, 0, st>>>(ntris, ndraw_s, draw_tri0, sdraw_id, draw_vbase, draws, verts,
-                                                         inds, W, H, tri_a, tri_b, tri_draw, tri_idx);
+                                                         inds, surfs, tri_a, tri_b, tri_draw, tri_idx);
     gb_stroke_edges<<<(ntris + 255) / 256, 256, 0, st>>>(ntris, tri_a, tri_b, tri_idx, tri_draw, edges, edge_draw);
     return cudaGetLastError();
 }
 cudaError_t gb_launch_bin(cudaStream_t st, int scatter, uint32_t nedges, const int4 *edges, const uint32_t *edge_draw,
-                          uint32_t ndraws, uint32_t W, uint32_t samples, uint32_t nrows, uint32_t *cell, int4 *recs,
+                          const gb_draw *draws, const gb_surf *surfs, uint32_t samples, uint32_t *cell, int4 *recs,
                           uint32_t nunits) {
     if (nedges) {
         if (scatter)
-            gb_bin_edges<true><<<(nedges + 255) / 256, 256, 0, st>>>(nedges, edges, edge_draw, ndraws, W, samples,
-                                                                      nrows, cell, recs, nunits);
+            gb_bin_edges<true><<<(nedges + 255) / 256, 256, 0, st>>>(nedges, edges, edge_draw, draws, surfs, samples,
+                                                                      cell, recs, nunits);
         else
-            gb_bin_edges<false><<<(nedges + 255) / 256, 256, 0, st>>>(nedges, edges, edge_draw, ndraws, W, samples,
-                                                                       nrows, cell, nullptr, 0u);
+            gb_bin_edges<false><<<(nedges + 255) / 256, 256, 0, st>>>(nedges, edges, edge_draw, draws, surfs,
+                                                                       samples, cell, nullptr, 0u);
     }
     return cudaGetLastError();
 }

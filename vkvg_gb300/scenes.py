@@ -603,3 +603,163 @@ def svg_document(seed=31, n_shapes=40, size=240, quirks=False):
             q.append(part)
         text = "\n".join(q)
     return text.encode()
+
+
+def batch_scenes(seed=2, n_surfaces=64, max_paths=20000, min_paths=100, max_segs=2000, max_side=2048,
+                 samples=4):
+    """The uneven batch: n_surfaces independent surfaces, side log-uniform in
+    [256, max_side] rounded to a multiple of 16; paths per surface
+    Pareto(alpha 1.2) clipped to [min_paths, max_paths]; segments per path
+    log-uniform in [3, max_segs], 70% cubics, 20% lines, 10% arcs of radius
+    U[2, 200] px; path bounding boxes log-uniform from 4 px to the surface;
+    60% filled, 30% filled then stroked, 10% stroked, width U[0.5, 12].
+    Returns a list of scenes (one per surface)."""
+    import math
+
+    r = SplitMix64(seed)
+    u = lambda lo, hi: lo + (hi - lo) * r.rnd()
+    logu = lambda lo, hi: math.exp(u(math.log(lo), math.log(hi)))
+    out = []
+    for k in range(n_surfaces):
+        side = max(16, int(round(logu(256, max_side) / 16.0)) * 16)
+        n_paths = int(min(max_paths, max(min_paths, min_paths * (1.0 - r.rnd()) ** (-1.0 / 1.2))))
+        ops = [("set_source_rgb", 1.0, 1.0, 1.0), ("paint",)]
+        for i in range(n_paths):
+            bw = logu(4, side)
+            bx, by = u(0, side - bw), u(0, side - bw)
+            pt = lambda: (bx + u(0, bw), by + u(0, bw))
+            nseg = int(logu(3, max_segs))
+            ops.append(("move_to",) + pt())
+            for _ in range(nseg):
+                t = r.rnd()
+                if t < 0.7:
+                    ops.append(("curve_to",) + pt() + pt() + pt())
+                elif t < 0.9:
+                    ops.append(("line_to",) + pt())
+                else:
+                    rad = min(u(2, 200), bw)
+                    cx, cy = pt()
+                    a0 = u(0, 2 * math.pi)
+                    ops.append(("arc", cx, cy, rad, a0, a0 + u(0.3, 2 * math.pi)))
+            ops.append(("close_path",))
+            kind = r.rnd()
+            ops.append(("set_source_rgba", r.rnd(), r.rnd(), r.rnd(), u(0.3, 1.0)))
+            if kind < 0.6:
+                ops.append(("fill",))
+            else:
+                if kind < 0.9:
+                    ops.append(("fill_preserve",))
+                    ops.append(("set_source_rgba", r.rnd(), r.rnd(), r.rnd(), u(0.5, 1.0)))
+                ops += [("set_line_width", u(0.5, 12)), ("stroke",)]
+        out.append({"name": "batch%d" % k, "width": side, "height": side, "samples": samples, "ops": ops,
+                    "paths": n_paths})
+    return out
+
+
+def np_rnd(seed, start, n):
+    """outputs start+1 .. start+n of SplitMix64(seed) as floats in [0, 1)
+    (SplitMix64's i-th output is mix(seed + i * gamma), so a block is one
+    vector operation)"""
+    import numpy as np
+
+    with np.errstate(over="ignore"):
+        z = np.uint64(seed & MASK64) + (np.arange(start + 1, start + n + 1, dtype=np.uint64) *
+                                        np.uint64(0x9E3779B97F4A7C15))
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        z = z ^ (z >> np.uint64(31))
+    return (z >> np.uint64(40)).astype(np.float64) * (1.0 / 16777216.0)
+
+
+def batch_streams(seed=2, n_surfaces=64, max_paths=20000, min_paths=100, max_segs=2000, max_side=2048,
+                  paths_scale=1.0):
+    """The uneven batch (64 independent surfaces in one job), generated as
+    vkvg command streams for vkvg_gb300_replay_stream: side log-uniform in
+    [256, max_side] rounded to a multiple of 16; paths per surface
+    Pareto(alpha 1.2) clipped to [min_paths, max_paths] (times paths_scale);
+    segments per path log-uniform in [3, max_segs], 70% cubics, 20% lines and
+    10% arcs of radius U[2, 200] px (at most the box); path bounding boxes
+    log-uniform from 4 px to the surface; 60% of paths filled, 30% filled
+    then stroked, 10% stroked, width U[0.5, 12], colours uniform with alpha
+    U[0.3, 1].  Each surface is cleared to opaque white.  Returns one dict
+    per surface: width, height, cmds (uint32), args (float32), paths."""
+    import math
+
+    import numpy as np
+
+    top = SplitMix64(seed)
+    C_ = CMD
+    out = []
+    for k in range(n_surfaces):
+        s = top.next()
+        a = np_rnd(s, 0, 2)
+        side = max(16, int(round(math.exp(math.log(256) + (math.log(max_side) - math.log(256)) * a[0]) / 16.0)) * 16)
+        n_paths = int(min(max_paths, max(min_paths, min_paths * (1.0 - a[1]) ** (-1.0 / 1.2))))
+        n_paths = max(1, int(n_paths * paths_scale))
+        P = np_rnd(s, 2, n_paths * 12).reshape(n_paths, 12)
+        bw = np.exp(math.log(4) + (math.log(side) - math.log(4)) * P[:, 0])
+        bx, by = P[:, 1] * (side - bw), P[:, 2] * (side - bw)
+        nseg = np.exp(math.log(3) + (math.log(max_segs) - math.log(3)) * P[:, 3]).astype(np.int64)
+        kind = P[:, 4]
+        total = int(nseg.sum())
+        S = np_rnd(s, 2 + n_paths * 12, total * 8).reshape(total, 8)
+        pb = np.repeat(np.arange(n_paths), nseg)
+        sbw, sbx, sby = bw[pb], bx[pb], by[pb]
+        t = S[:, 0]
+        cub, lin = t < 0.7, (t >= 0.7) & (t < 0.9)
+        arc = ~(cub | lin)
+        seg_args = np.zeros((total, 6))
+        seg_args[:, 0::2] = sbx[:, None] + S[:, 1:7:2] * sbw[:, None]
+        seg_args[:, 1::2] = sby[:, None] + S[:, 2:7:2] * sbw[:, None]
+        rad = np.minimum(2.0 + 198.0 * S[:, 3], sbw)
+        a0 = 2 * math.pi * S[:, 4]
+        arc_args = np.stack([seg_args[:, 0], seg_args[:, 1], rad, a0, a0 + 0.3 + (2 * math.pi - 0.3) * S[:, 5],
+                             np.zeros(total)], 1)
+        seg_args = np.where(arc[:, None], arc_args, seg_args)
+        nargs = np.where(cub, 6, np.where(lin, 2, 5))
+        mask = np.arange(6)[None, :] < nargs[:, None]
+        seg_cmd = np.where(cub, C_["curve_to"], np.where(lin, C_["line_to"], C_["arc"])).astype(np.uint32)
+        seg_flat = seg_args[mask]
+        seg_off = np.concatenate([[0], np.cumsum(nargs)])
+        seg0 = np.concatenate([[0], np.cumsum(nseg)])
+        cmds, args = [np.array([C_["set_source_rgb"], C_["paint"]], np.uint32)], [np.array([1.0, 1.0, 1.0])]
+        for i in range(n_paths):
+            c = [C_["move_to"]]
+            x0, y0 = bx[i] + P[i, 5] * bw[i], by[i] + P[i, 6] * bw[i]
+            cmds.append(np.array([C_["move_to"]], np.uint32))
+            args.append(np.array([x0, y0]))
+            cmds.append(seg_cmd[seg0[i]:seg0[i + 1]])
+            args.append(seg_flat[seg_off[seg0[i]]:seg_off[seg0[i + 1]]])
+            rgba = P[i, 7:11].copy()
+            rgba[3] = 0.3 + 0.7 * rgba[3]
+            c = [C_["close_path"], C_["set_source_rgba"]]
+            g = list(rgba)
+            width = 0.5 + 11.5 * P[i, 11]
+            if kind[i] < 0.6:
+                c.append(C_["fill"])
+            elif kind[i] < 0.9:
+                c += [C_["fill_preserve"], C_["set_source_rgba"], C_["set_line_width"], C_["stroke"]]
+                g += [rgba[2], rgba[0], rgba[1], 0.5 + 0.5 * P[i, 9], width]
+            else:
+                c += [C_["set_line_width"], C_["stroke"]]
+                g += [width]
+            cmds.append(np.array(c, np.uint32))
+            args.append(np.array(g))
+        out.append({"name": "batch%d" % k, "width": side, "height": side, "paths": n_paths,
+                    "cmds": np.concatenate(cmds).astype(np.uint32), "args": np.concatenate(args).astype(np.float32)})
+    return out
+
+
+def decode(cmds, args):
+    """command stream -> scene calls (the inverse of encode for the codes
+    batch_streams emits)"""
+    names = {v: k for k, v in CMD.items()}
+    nargs = {"move_to": 2, "line_to": 2, "curve_to": 6, "arc": 5, "close_path": 0, "set_source_rgb": 3,
+             "set_source_rgba": 4, "paint": 0, "fill": 0, "fill_preserve": 0, "stroke": 0, "set_line_width": 1}
+    ops, a = [], 0
+    for c in cmds:
+        name = names[int(c)]
+        n = nargs[name]
+        ops.append((name,) + tuple(float(v) for v in args[a:a + n]))
+        a += n
+    return ops
