@@ -184,6 +184,70 @@ vkvg_public int      vkvg_gb300_svg_shape(VkvgSvgDoc svg, uint32_t i, char id[64
 vkvg_public int      vkvg_gb300_svg_path(VkvgSvgDoc svg, uint32_t shape, uint32_t path, float *pts, uint32_t cap_points,
                                          uint32_t *npts, uint32_t *closed);
 
+/* ---- differentiable analytic coverage (no vkvg counterpart) ----
+ *
+ * A scene of paths, each a list of closed contours of line and cubic
+ * segments over one array of control points: a segment of kind k consumes k
+ * control points (its start point, then a cubic's two inner control points)
+ * and ends at the next segment's start, the last segment of a contour at
+ * the contour's first point.  Cubics are flattened by vkvg's
+ * _recursive_bezier at vkvg's default tolerance.  Every path draws, in path
+ * order, a fill layer (VKVG_GB300_ANALYTIC_FILL: NON_ZERO, coverage
+ * min(1, |A|) with A the exact area integral of the winding number over the
+ * pixel) and a stroke layer (VKVG_GB300_ANALYTIC_STROKE: one rectangle of
+ * half-width w/2 per flattened segment and one bevel triangle on the outer
+ * side of every joint, coverage min(1, the sum of their areas in the
+ * pixel)), both in the path's premultiplied RGBA colour, composited with
+ * source-over onto the background into a W x H fp32 RGBA canvas.
+ *
+ * Parameters are device pointers (CUDA memory): ctrl [control points][2],
+ * colors [paths][4] premultiplied RGBA, widths [paths]; canvas and target
+ * [H][W][4].  Calls are queued on the scene's stream (set_stream, default: a
+ * stream of its own) and return at once; sync waits and returns the first
+ * error of the calls since the last sync.  VKVG_STATUS_NO_MEMORY from sync
+ * means a flattening outgrew the point buffer: the results since the last
+ * sync are zero, the buffer has been grown, and the calls must be repeated.
+ *
+ * forward renders the canvas (copied to canvas when it is not null) and,
+ * when target is not null, the loss mean((canvas - target)^2) into loss[0].
+ * backward returns the gradients of the last forward's parameters: of its
+ * loss when d_canvas is null (that forward must have had a target), else of
+ * sum(d_canvas * canvas).  d_ctrl, d_colors and d_widths are overwritten.
+ * The flattening is walked again in the backward pass, not stored; the
+ * parameters must not change between forward and backward.
+ * adam applies one Adam step (bias-corrected, step >= 1) to n parameters
+ * and clamps them to [lo, hi]. */
+#define VKVG_GB300_SEG_LINE        1
+#define VKVG_GB300_SEG_CUBIC       3
+#define VKVG_GB300_ANALYTIC_FILL   1u
+#define VKVG_GB300_ANALYTIC_STROKE 2u
+typedef struct _vkvg_gb300_analytic_t *VkvgAnalytic;
+vkvg_public VkvgAnalytic  vkvg_gb300_analytic_create(uint32_t width, uint32_t height, const float background[4],
+                                                     uint32_t npaths, const uint32_t *path_ncontours,
+                                                     const uint32_t *path_flags, uint32_t ncontours,
+                                                     const uint32_t *contour_nseg, uint32_t nseg,
+                                                     const uint8_t *seg_kind);
+vkvg_public void          vkvg_gb300_analytic_destroy(VkvgAnalytic a);
+vkvg_public vkvg_status_t vkvg_gb300_analytic_status(VkvgAnalytic a);
+vkvg_public uint32_t      vkvg_gb300_analytic_control_point_count(VkvgAnalytic a);
+vkvg_public uint32_t      vkvg_gb300_analytic_layer_count(VkvgAnalytic a);
+vkvg_public vkvg_status_t vkvg_gb300_analytic_set_stream(VkvgAnalytic a, void *stream);
+vkvg_public vkvg_status_t vkvg_gb300_analytic_forward(VkvgAnalytic a, const float *ctrl, const float *colors,
+                                                      const float *widths, const float *target, float *canvas,
+                                                      float *loss);
+vkvg_public vkvg_status_t vkvg_gb300_analytic_backward(VkvgAnalytic a, const float *d_canvas, float *d_ctrl,
+                                                       float *d_colors, float *d_widths);
+vkvg_public vkvg_status_t vkvg_gb300_analytic_adam(VkvgAnalytic a, float *param, const float *grad, float *m,
+                                                   float *v, uint32_t n, float lr, float beta1, float beta2,
+                                                   float eps, uint32_t step, float lo, float hi);
+vkvg_public vkvg_status_t vkvg_gb300_analytic_sync(VkvgAnalytic a);
+/* the last forward's flattened points (host copy, at most cap points; syncs):
+   returns their count; seg_offsets, if not null, gets nseg+1 offsets */
+vkvg_public uint32_t      vkvg_gb300_analytic_points(VkvgAnalytic a, float *pts, uint32_t cap, uint32_t *seg_offsets);
+/* the last backward's gradient with respect to each flattened point (host
+   copy of at most cap points, x and y; syncs): returns the point count */
+vkvg_public uint32_t      vkvg_gb300_analytic_point_grads(VkvgAnalytic a, float *grads, uint32_t cap);
+
 #ifdef __cplusplus
 }
 #endif

@@ -12,7 +12,7 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libvko.so")
-SOURCES = ["vko_geom.c", "vko_raster.c", "vko_api.c", "vko_png.c"]
+SOURCES = ["vko_geom.c", "vko_raster.c", "vko_api.c", "vko_png.c", "vko_analytic.c"]
 HEADERS = ["vko.h", "vko_internal.h", "vko_pmath.h"]
 CFLAGS = ["-std=gnu11", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math",
           "-fvisibility=hidden", "-Wall", "-Wno-unused-function", "-pthread"]

@@ -233,6 +233,30 @@ VKO_API void vko_snap(vko_context *ctx, uint32_t i, float x, float y, int32_t *f
 VKO_API void vko_coverage_edges(uint32_t w, uint32_t h, uint32_t samples, const int32_t *edges, uint64_t nedges,
                                 int32_t *out);
 
+/* ---- analytic-coverage mode, FP64 reference (vko_analytic.c) ---- */
+#define VKO_AN_LINE   1 /* segment kinds = control points a segment consumes */
+#define VKO_AN_CUBIC  3
+#define VKO_AN_FILL   1u
+#define VKO_AN_STROKE 2u
+typedef struct vko_an_t vko_an;
+VKO_API vko_an  *vko_an_create(uint32_t width, uint32_t height, const float *background, uint32_t npaths,
+                               const uint32_t *path_ncontours, const uint32_t *path_flags, uint32_t ncontours,
+                               const uint32_t *contour_nseg, uint32_t nseg, const uint8_t *seg_kind);
+VKO_API void     vko_an_destroy(vko_an *a);
+VKO_API void     vko_an_set_points_mode(int f32);
+VKO_API uint32_t vko_an_nctrl(const vko_an *a);
+VKO_API uint32_t vko_an_nlayers(const vko_an *a);
+VKO_API uint32_t vko_an_flatten(const vko_an *a, const double *ctrl, float *pts_f32, double *pts_f64, uint32_t cap,
+                                uint32_t *seg_off);
+VKO_API double   vko_an_forward(const vko_an *a, const double *ctrl, const double *colors, const double *widths,
+                                const double *target, double *canvas, double *area);
+VKO_API double   vko_an_backward(const vko_an *a, const double *ctrl, const double *colors, const double *widths,
+                                 const double *target, const double *d_canvas, double *d_ctrl, double *d_colors,
+                                 double *d_widths, double *d_pts);
+VKO_API void     vko_an_fd(const vko_an *a, const double *ctrl, const double *colors, const double *widths,
+                           const double *target, uint32_t n, const uint32_t *group, const uint32_t *index, double h,
+                           double h2, int full, int threads, double *fd, double *fd2, int32_t *valid);
+
 #ifdef __cplusplus
 }
 #endif

@@ -192,9 +192,12 @@ static float get_arc_step(const vko_context *ctx, float radius) {
 
 /* _recursive_bezier, :1313-1461 (AGG adaptive subdivision).  The branch
    "M_ANGLE_TOLERANCE < CURVE_ANGLE_TOLERANCE_EPSILON" is constant-false and
-   omitted.  "da = M_2_PIF - da" (2/pi, not 2*pi) is kept as in vkvg. */
-static void recursive_bezier(vko_context *ctx, float distanceTolerance, float x1, float y1, float x2, float y2,
-                             float x3, float y3, float x4, float y4, unsigned level) {
+   omitted.  "da = M_2_PIF - da" (2/pi, not 2*pi) is kept as in vkvg.
+   Every added point is reported to emit() with which sub-curve point it is
+   (VKO_BEZ_MID = x1234, VKO_BEZ_C2 = x2, VKO_BEZ_C3 = x3) and the sub-curve's
+   parameter interval [ta, tb] on the original cubic. */
+void vko_bezier_walk(vko_bez_emit emit, void *u, float distanceTolerance, float x1, float y1, float x2, float y2,
+                     float x3, float y3, float x4, float y4, unsigned level, double ta, double tb) {
     if (level > CURVE_RECURSION_LIMIT)
         return;
     float x12   = (x1 + x2) / 2;
@@ -226,15 +229,15 @@ static void recursive_bezier(vko_context *ctx, float distanceTolerance, float x1
                 if (da2 >= VKO_PIF)
                     da2 = VKO_2_PIF - da2;
                 if (da1 + da2 < (float)M_ANGLE_TOLERANCE) {
-                    add_point(ctx, x1234, y1234);
+                    emit(u, x1234, y1234, VKO_BEZ_MID, ta, tb);
                     return;
                 }
                 if (da1 > M_CUSP_LIMIT) {
-                    add_point(ctx, x2, y2);
+                    emit(u, x2, y2, VKO_BEZ_C2, ta, tb);
                     return;
                 }
                 if (da2 > M_CUSP_LIMIT) {
-                    add_point(ctx, x3, y3);
+                    emit(u, x3, y3, VKO_BEZ_C3, ta, tb);
                     return;
                 }
             }
@@ -245,12 +248,12 @@ static void recursive_bezier(vko_context *ctx, float distanceTolerance, float x1
                     if (da1 >= VKO_PIF)
                         da1 = VKO_2_PIF - da1;
                     if (da1 < M_ANGLE_TOLERANCE) {
-                        add_point(ctx, x2, y2);
-                        add_point(ctx, x3, y3);
+                        emit(u, x2, y2, VKO_BEZ_C2, ta, tb);
+                        emit(u, x3, y3, VKO_BEZ_C3, ta, tb);
                         return;
                     }
                     if (da1 > M_CUSP_LIMIT) {
-                        add_point(ctx, x2, y2);
+                        emit(u, x2, y2, VKO_BEZ_C2, ta, tb);
                         return;
                     }
                 }
@@ -260,12 +263,12 @@ static void recursive_bezier(vko_context *ctx, float distanceTolerance, float x1
                     if (da1 >= VKO_PIF)
                         da1 = VKO_2_PIF - da1;
                     if (da1 < M_ANGLE_TOLERANCE) {
-                        add_point(ctx, x2, y2);
-                        add_point(ctx, x3, y3);
+                        emit(u, x2, y2, VKO_BEZ_C2, ta, tb);
+                        emit(u, x3, y3, VKO_BEZ_C3, ta, tb);
                         return;
                     }
                     if (da1 > M_CUSP_LIMIT) {
-                        add_point(ctx, x3, y3);
+                        emit(u, x3, y3, VKO_BEZ_C3, ta, tb);
                         return;
                     }
                 }
@@ -273,14 +276,24 @@ static void recursive_bezier(vko_context *ctx, float distanceTolerance, float x1
                 dx = x1234 - (x1 + x4) / 2;
                 dy = y1234 - (y1 + y4) / 2;
                 if (dx * dx + dy * dy <= distanceTolerance) {
-                    add_point(ctx, x1234, y1234);
+                    emit(u, x1234, y1234, VKO_BEZ_MID, ta, tb);
                     return;
                 }
             }
         }
     }
-    recursive_bezier(ctx, distanceTolerance, x1, y1, x12, y12, x123, y123, x1234, y1234, level + 1);
-    recursive_bezier(ctx, distanceTolerance, x1234, y1234, x234, y234, x34, y34, x4, y4, level + 1);
+    double tm = (ta + tb) * 0.5;
+    vko_bezier_walk(emit, u, distanceTolerance, x1, y1, x12, y12, x123, y123, x1234, y1234, level + 1, ta, tm);
+    vko_bezier_walk(emit, u, distanceTolerance, x1234, y1234, x234, y234, x34, y34, x4, y4, level + 1, tm, tb);
+}
+
+static void ctx_emit(void *u, float x, float y, int which, double ta, double tb) {
+    (void)which, (void)ta, (void)tb;
+    add_point((vko_context *)u, x, y);
+}
+static void recursive_bezier(vko_context *ctx, float distanceTolerance, float x1, float y1, float x2, float y2,
+                             float x3, float y3, float x4, float y4, unsigned level) {
+    vko_bezier_walk(ctx_emit, ctx, distanceTolerance, x1, y1, x2, y2, x3, y3, x4, y4, level, 0.0, 1.0);
 }
 
 static int finite8(float a, float b, float c, float d, float e, float f, float g, float h) {

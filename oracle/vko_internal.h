@@ -211,4 +211,12 @@ void vko_resolve(const vko_surface *surf, uint8_t *rgba);
 /* png (vko_png.c) */
 int vko_png_write(const char *path, uint32_t w, uint32_t h, const uint8_t *rgba);
 
+/* _recursive_bezier with a point callback (vko_geom.c); which is one of: */
+#define VKO_BEZ_MID 0 /* the sub-curve's midpoint x1234 */
+#define VKO_BEZ_C2  1 /* its second control point x2 */
+#define VKO_BEZ_C3  2 /* its third control point x3 */
+typedef void (*vko_bez_emit)(void *u, float x, float y, int which, double ta, double tb);
+void vko_bezier_walk(vko_bez_emit emit, void *u, float distanceTolerance, float x1, float y1, float x2, float y2,
+                     float x3, float y3, float x4, float y4, unsigned level, double ta, double tb);
+
 #endif

@@ -180,6 +180,18 @@ SIGNATURES = {
     "vkvg_gb300_svg_shape_count": (_U, [_P]),
     "vkvg_gb300_svg_shape": (_I, [_P, _U, _P, _P, _P]),
     "vkvg_gb300_svg_path": (_I, [_P, _U, _U, _P, _U, _P, _P]),
+    "vkvg_gb300_analytic_create": (_P, [_U, _U, _P, _U, _P, _P, _U, _P, _U, _P]),
+    "vkvg_gb300_analytic_destroy": (None, [_P]),
+    "vkvg_gb300_analytic_status": (_I, [_P]),
+    "vkvg_gb300_analytic_control_point_count": (_U, [_P]),
+    "vkvg_gb300_analytic_layer_count": (_U, [_P]),
+    "vkvg_gb300_analytic_set_stream": (_I, [_P, _P]),
+    "vkvg_gb300_analytic_forward": (_I, [_P, _P, _P, _P, _P, _P, _P]),
+    "vkvg_gb300_analytic_backward": (_I, [_P, _P, _P, _P, _P]),
+    "vkvg_gb300_analytic_adam": (_I, [_P, _P, _P, _P, _P, _U, _F, _F, _F, _F, _U, _F, _F]),
+    "vkvg_gb300_analytic_sync": (_I, [_P]),
+    "vkvg_gb300_analytic_points": (_U, [_P, _P, _U, _P]),
+    "vkvg_gb300_analytic_point_grads": (_U, [_P, _P, _U]),
 }
 
 
@@ -458,4 +470,91 @@ class Svg:
     def destroy(self):
         if self.h:
             self.L.vkvg_svg_destroy(self.h)
+            self.h = None
+
+
+class Analytic:
+    """Differentiable analytic-coverage scene (vkvg_gb300_analytic_* of
+    include/vkvg_gb300.h) for a scene description of
+    vkvg_gb300.scenes.analytic_scene.  Parameters and results are CUDA
+    tensors (float32, contiguous); the calls are queued on the tensors'
+    current stream."""
+
+    def __init__(self, scene):
+        import torch
+
+        self.L = lib()
+        self.torch = torch
+        s = {k: np.ascontiguousarray(v) for k, v in scene.items() if isinstance(v, np.ndarray)}
+        self._keep = s
+        self.W, self.H = int(scene["width"]), int(scene["height"])
+        self.npaths = len(s["path_ncontours"])
+        self.h = self.L.vkvg_gb300_analytic_create(
+            self.W, self.H, _ptr(s["background"].astype(np.float32)), self.npaths, _ptr(s["path_ncontours"]),
+            _ptr(s["path_flags"]), len(s["contour_nseg"]), _ptr(s["contour_nseg"]), len(s["seg_kind"]),
+            _ptr(s["seg_kind"]))
+        if not self.h:
+            raise VkvgError("vkvg_gb300_analytic_create failed")
+        self.nctrl = self.L.vkvg_gb300_analytic_control_point_count(self.h)
+        self.nlayers = self.L.vkvg_gb300_analytic_layer_count(self.h)
+        self.L.vkvg_gb300_analytic_set_stream(self.h, C.c_void_p(torch.cuda.current_stream().cuda_stream))
+        self.canvas = torch.empty((self.H, self.W, 4), dtype=torch.float32, device="cuda")
+        self.loss = torch.zeros(1, dtype=torch.float32, device="cuda")
+
+    @staticmethod
+    def _p(t):
+        return C.c_void_p(t.data_ptr()) if t is not None else None
+
+    def _check(self, st, what):
+        if st:
+            raise VkvgError("%s: status %d" % (what, st))
+
+    def forward(self, ctrl, colors, widths, target=None):
+        """renders into self.canvas (and the loss into self.loss when a target
+        is given); returns (canvas, loss or None)"""
+        p = self._p
+        st = self.L.vkvg_gb300_analytic_forward(self.h, p(ctrl), p(colors), p(widths), p(target), p(self.canvas),
+                                                p(self.loss) if target is not None else None)
+        self._check(st, "analytic_forward")
+        self._keep_fwd = (ctrl, colors, widths, target)
+        return self.canvas, (self.loss if target is not None else None)
+
+    def backward(self, d_canvas=None, grads=None):
+        """gradients of the last forward's loss (d_canvas None) or of
+        sum(d_canvas * canvas): (d_ctrl, d_colors, d_widths)"""
+        t = self.torch
+        if grads is None:
+            grads = (t.empty((self.nctrl, 2), dtype=t.float32, device="cuda"),
+                     t.empty((self.npaths, 4), dtype=t.float32, device="cuda"),
+                     t.empty(self.npaths, dtype=t.float32, device="cuda"))
+        p = self._p
+        st = self.L.vkvg_gb300_analytic_backward(self.h, p(d_canvas), p(grads[0]), p(grads[1]), p(grads[2]))
+        self._check(st, "analytic_backward")
+        return grads
+
+    def adam(self, param, grad, m, v, step, lr, lo, hi, beta1=0.9, beta2=0.999, eps=1e-8):
+        st = self.L.vkvg_gb300_analytic_adam(self.h, self._p(param), self._p(grad), self._p(m), self._p(v),
+                                             param.numel(), lr, beta1, beta2, eps, step, lo, hi)
+        self._check(st, "analytic_adam")
+
+    def sync(self):
+        return int(self.L.vkvg_gb300_analytic_sync(self.h))
+
+    def points(self):
+        n = self.L.vkvg_gb300_analytic_points(self.h, None, 0, None)
+        pts = np.zeros((max(n, 1), 2), np.float32)
+        off = np.zeros(len(self._keep["seg_kind"]) + 1, np.uint32)
+        self.L.vkvg_gb300_analytic_points(self.h, _ptr(pts), n, _ptr(off))
+        return pts[:n], off
+
+    def point_grads(self):
+        """dL/dpoint of the last backward, float32 [points, 2]"""
+        n = self.L.vkvg_gb300_analytic_point_grads(self.h, None, 0)
+        g = np.zeros((max(n, 1), 2), np.float32)
+        self.L.vkvg_gb300_analytic_point_grads(self.h, _ptr(g), n)
+        return g[:n]
+
+    def destroy(self):
+        if self.h:
+            self.L.vkvg_gb300_analytic_destroy(self.h)
             self.h = None

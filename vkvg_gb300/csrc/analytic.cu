@@ -1,0 +1,749 @@
+/*
+ * K7/K8 - analytic area coverage, compositing and their adjoints, sm_103a.
+ *
+ * Forward (K7):
+ *   ak_cover      grid (bands of AK_BAND rows) x (layers).  Every thread takes
+ *                 flattened points of the layer's path and builds the
+ *                 polygons of that point - the fill edge to the next point,
+ *                 or the stroke's rectangle of the segment to the next point
+ *                 and the bevel triangle on the outer side of its joint - and
+ *                 walks each polygon edge through the pixel cells of the band
+ *                 (ak_walk).  Each piece of edge in a cell deposits its signed
+ *                 area into two shared-memory cells of the row (the cell, and
+ *                 the one right of it for the rest of the row); a row prefix
+ *                 sum then gives every pixel's exact winding-area integral A,
+ *                 written to area[layer][y][x].  Edges left of the canvas
+ *                 cover the whole row (deposit in column 0).
+ *   ak_composite  one thread per pixel: coverage min(1, |A|) per layer,
+ *                 premultiplied source-over in layer order onto the
+ *                 background, the colour under every AK_CHUNK-th layer kept
+ *                 as a checkpoint, canvas and per-block loss partials.
+ * Backward (K8):
+ *   ak_composite_bwd  one thread per pixel, chunks of AK_CHUNK layers from the
+ *                 top: the chunk's under-colours are recomputed from its
+ *                 checkpoint, then the layers are walked downwards with the
+ *                 transmittance of the layers above; writes dL/dA in place of
+ *                 A and per-block colour-gradient partials.
+ *   ak_cover_bwd  the same grid and polygons as ak_cover; every edge
+ *                 integrates the pixel gradients along itself against its two
+ *                 endpoint hat functions (the derivative of a polygon's area
+ *                 in a pixel is the integral of the normal motion of its
+ *                 boundary inside the pixel), which gives dL/dvertex, then
+ *                 chains through the rectangle and bevel construction to the
+ *                 points and the stroke width.
+ * The flattening and its adjoint are in analytic_flat.cu.
+ */
+#include "analytic.h"
+
+#include <cuda_runtime.h>
+#include <math_constants.h>
+
+#define AK_THREADS 256
+
+__device__ __forceinline__ float2 v2(float x, float y) { return make_float2(x, y); }
+__device__ __forceinline__ float2 operator+(float2 a, float2 b) { return v2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 operator-(float2 a, float2 b) { return v2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 operator*(float2 a, float s) { return v2(a.x * s, a.y * s); }
+__device__ __forceinline__ float  dot2(float2 a, float2 b) { return a.x * b.x + a.y * b.y; }
+__device__ __forceinline__ float  crs2(float2 a, float2 b) { return a.x * b.y - a.y * b.x; }
+__device__ __forceinline__ float2 perp(float2 a) { return v2(-a.y, a.x); }
+__device__ __forceinline__ float2 perpT(float2 a) { return v2(a.y, -a.x); }
+__device__ __forceinline__ bool   fin2(float2 a) {
+    return ((__float_as_uint(a.x) & 0x7f800000u) != 0x7f800000u) &&
+           ((__float_as_uint(a.y) & 0x7f800000u) != 0x7f800000u);
+}
+
+/* ------------------------------------------------------------ cell walk */
+
+/* Liang-Barsky: restrict [t0, t1] to p t <= q; id names the boundary that
+   set t0 (in id0) or t1 (in id1) */
+__device__ __forceinline__ bool lb_clip(float p, float q, float &t0, float &t1, int id, int &id0, int &id1) {
+    if (p == 0.f)
+        return q >= 0.f;
+    float r = q / p;
+    if (p < 0.f) {
+        if (r > t1)
+            return false;
+        if (r > t0)
+            t0 = r, id0 = id;
+    } else {
+        if (r < t0)
+            return false;
+        if (r < t1)
+            t1 = r, id1 = id;
+    }
+    return true;
+}
+
+/* Visit, in order of t, the pieces [ta, tb] of edge a->b inside the box
+   [bx0,bx1] x [by0,by1] that lie in one pixel cell (i, j), with the piece's
+   end points (pa, pb); without xlines only rows split the edge and i = -1.
+   Coordinates are those of a local frame whose origin is an integer pixel
+   corner (box and cells included), so positions near the origin keep their
+   full fp32 precision.  A piece ends where the next one starts, at the same
+   float values, and a point on a grid line or box side has that line's exact
+   coordinate: sums over consecutive pieces telescope.  At most lim steps;
+   false if the bound was hit (it cannot be for a finite edge: lim covers
+   every crossing of the box). */
+template <class V>
+__device__ __forceinline__ bool ak_walk(float2 a, float2 b, float bx0, float bx1, float by0, float by1, bool xlines,
+                                        int lim, V &v) {
+    float dx = b.x - a.x, dy = b.y - a.y, t0 = 0.f, t1 = 1.f;
+    int   id0 = -1, id1 = -1;
+    if (!lb_clip(-dx, a.x - bx0, t0, t1, 0, id0, id1) || !lb_clip(dx, bx1 - a.x, t0, t1, 1, id0, id1) ||
+        !lb_clip(-dy, a.y - by0, t0, t1, 2, id0, id1) || !lb_clip(dy, by1 - a.y, t0, t1, 3, id0, id1) || !(t0 < t1))
+        return true;
+    const float bnd[4] = {bx0, bx1, by0, by1};
+    float2      pa = a, pend = b;
+    if (id0 >= 0)
+        pa = id0 < 2 ? v2(bnd[id0], a.y + dy * t0) : v2(a.x + dx * t0, bnd[id0]);
+    if (id1 >= 0)
+        pend = id1 < 2 ? v2(bnd[id1], a.y + dy * t1) : v2(a.x + dx * t1, bnd[id1]);
+    float tx = CUDART_INF_F, ty = CUDART_INF_F, kx = 0.f, ky = 0.f, sx = 0.f, sy = 0.f;
+    if (xlines && dx != 0.f) {
+        sx = dx > 0.f ? 1.f : -1.f;
+        kx = dx > 0.f ? floorf(pa.x) + 1.f : ceilf(pa.x) - 1.f;
+        tx = (kx - a.x) / dx;
+    }
+    if (dy != 0.f) {
+        sy = dy > 0.f ? 1.f : -1.f;
+        ky = dy > 0.f ? floorf(pa.y) + 1.f : ceilf(pa.y) - 1.f;
+        ty = (ky - a.y) / dy;
+    }
+    float ta  = t0;
+    int   ix0 = xlines ? (int)bx0 : 0, ix1 = xlines ? (int)bx1 - 1 : 0;
+    int   jy0 = (int)by0, jy1 = (int)by1 - 1;
+    for (int it = 0; it < lim; it++) {
+        bool   xs = tx <= ty;
+        float  tn = xs ? tx : ty;
+        bool   last = tn >= t1;
+        float  tb   = last ? t1 : tn;
+        float2 pb   = last ? pend : xs ? v2(kx, a.y + dy * tn) : v2(a.x + dx * tn, ky);
+        if (tb > ta) {
+            float tm = 0.5f * (ta + tb);
+            int   i  = -1;
+            if (xlines) {
+                i = (int)floorf(a.x + dx * tm);
+                i = i < ix0 ? ix0 : i > ix1 ? ix1 : i;
+            }
+            int j = (int)floorf(a.y + dy * tm);
+            j     = j < jy0 ? jy0 : j > jy1 ? jy1 : j;
+            v(i, j, ta, tb, pa, pb);
+            ta = tb;
+        }
+        pa = pb;
+        if (last)
+            return true;
+        if (xs)
+            kx += sx, tx = (kx - a.x) / dx;
+        else
+            ky += sy, ty = (ky - a.y) / dy;
+    }
+    return false;
+}
+
+/* Areas accumulate in fixed point (AK_FIX units per px^2) with integer
+   shared-memory atomics: the sums are exact and order-independent.  A piece
+   deposits the fixed-point difference of its end points' y, so the deposits
+   of consecutive pieces, of consecutive edges and of the two walks of an
+   edge telescope: past a closed polygon a row holds its exact integer
+   winding, and rounding stays in the pixels the edges cross. */
+#define AK_FIX     1048576.f /* 2^20 */
+#define AK_FIX_INV (1.f / 1048576.f)
+
+/* the visitors get cells of the local frame whose origin is (ox, oy) */
+struct ak_acc_v {
+    int *acc;
+    int  ox, oy, y0, W1, sgn;
+    __device__ void operator()(int i, int j, float ta, float tb, float2 pa, float2 pb) {
+        int dys = (int)(__float2ll_rn(pb.y * AK_FIX) - __float2ll_rn(pa.y * AK_FIX)) * sgn;
+        int *row = acc + (j + oy - y0) * W1;
+        if (i < 0 && ox == 0) { /* left of the canvas: covers the whole row */
+            atomicAdd(row, dys);
+            return;
+        }
+        /* mean x of the piece relative to its cell's left side */
+        float f  = fminf(fmaxf(0.5f * ((pa.x - (float)i) + (pb.x - (float)i)), 0.f), 1.f);
+        int   d1 = __float2int_rn((float)dys * f);
+        atomicAdd(row + i + ox, dys - d1);
+        atomicAdd(row + i + ox + 1, d1);
+    }
+};
+
+struct ak_grad_v {
+    const float *g;
+    int          ox, oy, y0, W;
+    float        w0, w1;
+    __device__ void operator()(int i, int j, float ta, float tb, float2, float2) {
+        float gv = g[(j + oy - y0) * W + i + ox];
+        float d  = (tb - ta) * gv;
+        float tm = 0.5f * (ta + tb);
+        w0 += d * (1.f - tm);
+        w1 += d * tm;
+    }
+};
+
+struct ak_band {
+    int       y0, y1, W;
+    uint32_t *status;
+};
+
+/* An edge a->b of a polygon given in the local frame with integer origin o. */
+__device__ __forceinline__ bool edge_in_band(const ak_band &bd, float2 a, float2 b, float2 o) {
+    return fmaxf(a.y, b.y) + o.y >= (float)bd.y0 && fminf(a.y, b.y) + o.y <= (float)bd.y1 && fin2(a) && fin2(b);
+}
+
+/* Positions along an edge are evaluated from the endpoint nearer the band:
+   from the far one, a + t (b - a) would lose the fp32 bits of the far
+   coordinate's magnitude exactly where the edge crosses the canvas. */
+__device__ __forceinline__ bool far_first(const ak_band &bd, float2 a, float2 b, float2 o) {
+    float cx = 0.5f * (float)bd.W - o.x, cy = 0.5f * (float)(bd.y0 + bd.y1) - o.y;
+    return fmaxf(fabsf(a.x - cx), fabsf(a.y - cy)) > fmaxf(fabsf(b.x - cx), fabsf(b.y - cy));
+}
+
+__device__ __forceinline__ void edge_fwd(int *acc, const ak_band &bd, float2 a, float2 b, float2 o) {
+    if (a.y == b.y || !edge_in_band(bd, a, b, o))
+        return;
+    int sgn = 1;
+    if (far_first(bd, a, b, o)) { /* walk b->a: the deposits change sign */
+        float2 t = a;
+        a = b, b = t, sgn = -1;
+    }
+    ak_acc_v v{acc, (int)o.x, (int)o.y, bd.y0, bd.W + 1, sgn};
+    float    bx1 = (float)bd.W - o.x, by0 = (float)bd.y0 - o.y, by1 = (float)bd.y1 - o.y;
+    int      lim = bd.W + (bd.y1 - bd.y0) + 8;
+    bool     ok  = ak_walk(a, b, -o.x, bx1, by0, by1, true, lim, v);
+    if (!(b.x == a.x && a.x + o.x >= 0.f) && fminf(a.x, b.x) + o.x < 0.f) { /* the part left of x = 0 */
+        v.ox = 0;
+        ok   = ak_walk(a, b, -CUDART_INF_F, -o.x, by0, by1, false, lim, v) && ok;
+    }
+    if (!ok)
+        atomicOr(bd.status, AK_ERR_WALK);
+}
+
+/* dL/da += N*w0, dL/db += N*w1 for edge a->b, N = perp(b - a); walked from
+   the nearer endpoint, whose hat function is then the walk's first */
+__device__ __forceinline__ void edge_bwd(const float *g, const ak_band &bd, float2 a, float2 b, float2 o,
+                                         float2 &ga, float2 &gb) {
+    if (!edge_in_band(bd, a, b, o))
+        return;
+    bool      rev = far_first(bd, a, b, o);
+    ak_grad_v v{g, (int)o.x, (int)o.y, bd.y0, bd.W, 0.f, 0.f};
+    if (!ak_walk(rev ? b : a, rev ? a : b, -o.x, (float)bd.W - o.x, (float)bd.y0 - o.y, (float)bd.y1 - o.y, true,
+                 bd.W + (bd.y1 - bd.y0) + 8, v))
+        atomicOr(bd.status, AK_ERR_WALK);
+    float2 N = perp(b - a);
+    ga       = ga + N * (rev ? v.w1 : v.w0);
+    gb       = gb + N * (rev ? v.w0 : v.w1);
+}
+
+/* ------------------------------------------------------- stroke pieces */
+
+__device__ __forceinline__ bool quad_verts(float2 a, float2 b, float h, float2 q[4]) {
+    float2 d  = b - a;
+    float  L2 = dot2(d, d);
+    if (L2 == 0.f)
+        return false;
+    float2 n = perp(d) * (h / sqrtf(L2));
+    q[0] = a + n, q[1] = b + n, q[2] = b - n, q[3] = a - n;
+    return true;
+}
+
+__device__ __forceinline__ int bevel_verts(float2 pa, float2 p, float2 pb, float h, float2 v[3]) {
+    float2 da = p - pa, db = pb - p;
+    float  La = dot2(da, da), Lb = dot2(db, db);
+    if (La == 0.f || Lb == 0.f)
+        return 0;
+    float c = crs2(da, db);
+    if (c == 0.f)
+        return 0;
+    float2 na = perp(da) * (h / sqrtf(La)), nb = perp(db) * (h / sqrtf(Lb));
+    v[0] = p;
+    if (c > 0.f) {
+        v[1] = p - nb, v[2] = p - na;
+        return 1;
+    }
+    v[1] = p + na, v[2] = p + nb;
+    return -1;
+}
+
+__device__ __forceinline__ float2 dnormal(float2 d, float2 gn) {
+    float  iL = rsqrtf(dot2(d, d));
+    float2 u = d * iL, m = perpT(gn);
+    return (m - u * dot2(u, m)) * iL;
+}
+
+__device__ __forceinline__ bool pieces_in_band(const ak_band &bd, float2 pp, float2 p, float2 pn, float h) {
+    float lo = fminf(fminf(pp.y, p.y), pn.y) - h, hi = fmaxf(fmaxf(pp.y, p.y), pn.y) + h;
+    return hi >= (float)bd.y0 && lo <= (float)bd.y1;
+}
+
+/* the point's neighbours in its contour */
+__device__ __forceinline__ void neighbours(const ak_scene &S, const ak_bufs &B, uint32_t k, uint32_t &kp,
+                                           uint32_t &kn) {
+    uint32_t c  = B.pt_cont[k];
+    uint32_t c0 = B.off[S.cont_s0[c]], c1 = B.off[S.cont_s0[c + 1]];
+    kn          = k + 1 == c1 ? c0 : k + 1;
+    kp          = k == c0 ? c1 - 1 : k - 1;
+}
+
+/* ------------------------------------------------- band work compaction */
+
+/* one flattened point whose polygons reach the band: its neighbours and the
+   vertices of its polygons - the fill edge (v0, v1), or the stroke's
+   rectangle (v0..v3) and bevel triangle (v4..v6) - relative to the integer
+   pixel corner o at or below the point (exact, and small near the point) */
+struct ak_slot {
+    uint32_t k, kp, kn, flags; /* flags: 1 rectangle, 2 bevel, 4 bevel on the -n side */
+    float2   o;
+    float2   v[7];
+};
+#define AK_SLOT_RECT  1u
+#define AK_SLOT_BEVEL 2u
+#define AK_SLOT_NEG   4u
+
+/* Phase 1 of a round: threads test the points [base, base + AK_THREADS) of
+   the layer and append those reaching the band to the slot list. */
+__device__ __forceinline__ void gather_slots(const ak_scene &S, const ak_bufs &B, const ak_band &bd, bool stroke,
+                                             bool fwd, float h, uint32_t k, uint32_t p1, ak_slot *slots,
+                                             int *nslot) {
+    if (k >= p1)
+        return;
+    uint32_t kp, kn;
+    neighbours(S, B, k, kp, kn);
+    float2 P = B.pts[k], Pn = B.pts[kn];
+    float2 O = v2(floorf(P.x), floorf(P.y));
+    if (!fin2(O))
+        O = v2(0.f, 0.f);
+    if (!stroke) {
+        /* a horizontal edge adds no area but moves it: the backward keeps it */
+        if ((fwd && P.y == Pn.y) || !edge_in_band(bd, P, Pn, v2(0.f, 0.f)))
+            return;
+        int      n = atomicAdd(nslot, 1);
+        ak_slot &o = slots[n];
+        o.k = k, o.kp = kp, o.kn = kn, o.flags = 0, o.o = O, o.v[0] = P - O, o.v[1] = Pn - O;
+        return;
+    }
+    float2 Pp = B.pts[kp];
+    if (!pieces_in_band(bd, Pp, P, Pn, h))
+        return;
+    float2   q[4], v[3];
+    uint32_t fl   = quad_verts(P - O, Pn - O, h, q) ? AK_SLOT_RECT : 0u;
+    int      side = bevel_verts(Pp - O, P - O, Pn - O, h, v);
+    fl |= side ? AK_SLOT_BEVEL : 0u;
+    fl |= side > 0 ? AK_SLOT_NEG : 0u;
+    if (!fl)
+        return;
+    int      n = atomicAdd(nslot, 1);
+    ak_slot &o = slots[n];
+    o.k = k, o.kp = kp, o.kn = kn, o.flags = fl, o.o = O;
+#pragma unroll
+    for (int e = 0; e < 4; e++)
+        o.v[e] = q[e];
+#pragma unroll
+    for (int e = 0; e < 3; e++)
+        o.v[4 + e] = v[e];
+}
+
+/* edge e of a slot: (a, b); false if that polygon is absent */
+__device__ __forceinline__ bool slot_edge(const ak_slot &o, bool stroke, int e, float2 &a, float2 &b) {
+    if (!stroke) {
+        a = o.v[0], b = o.v[1];
+        return true;
+    }
+    if (e < 4) {
+        a = o.v[e], b = o.v[(e + 1) & 3];
+        return (o.flags & AK_SLOT_RECT) != 0;
+    }
+    a = o.v[e], b = o.v[e == 6 ? 4 : e + 1];
+    return (o.flags & AK_SLOT_BEVEL) != 0;
+}
+
+/* ------------------------------------------------------------- forward */
+
+__global__ void __launch_bounds__(AK_THREADS) ak_cover(ak_scene S, ak_bufs B, const float *__restrict__ widths) {
+    extern __shared__ __align__(16) unsigned char ak_smem[];
+    ak_slot *slots = reinterpret_cast<ak_slot *>(ak_smem);
+    int     *acc   = reinterpret_cast<int *>(slots + AK_THREADS);
+    __shared__ int nslot;
+    uint32_t l = blockIdx.y;
+    ak_band  bd{(int)(blockIdx.x * AK_BAND), 0, (int)S.W, B.status};
+    bd.y1    = min((int)S.H, bd.y0 + AK_BAND);
+    int rows = bd.y1 - bd.y0, W1 = S.W + 1;
+    for (int i = threadIdx.x; i < rows * W1; i += AK_THREADS)
+        acc[i] = 0;
+    if (B.off[S.nseg] <= B.cap) {
+        uint32_t p = S.layer_path[l];
+        bool     stroke = S.layer_stroke[l] != 0;
+        int      E      = stroke ? 7 : 1;
+        float    h      = 0.5f * widths[p];
+        uint32_t p1     = B.off[S.path_s0[p + 1]];
+        for (uint32_t base = B.off[S.path_s0[p]]; base < p1; base += AK_THREADS) {
+            if (threadIdx.x == 0)
+                nslot = 0;
+            __syncthreads();
+            gather_slots(S, B, bd, stroke, true, h, base + threadIdx.x, p1, slots, &nslot);
+            __syncthreads();
+            int ne = nslot * E;
+            for (int t = threadIdx.x; t < ne; t += AK_THREADS) {
+                float2 a, b;
+                const ak_slot &sl = slots[t / E];
+                if (slot_edge(sl, stroke, t % E, a, b))
+                    edge_fwd(acc, bd, a, b, sl.o);
+            }
+            __syncthreads();
+        }
+    }
+    __syncthreads();
+    /* row prefix sums, one warp per row, 32 cells per step */
+    uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    float   *out  = B.area + ((size_t)l * S.H + bd.y0) * S.W;
+    for (int r = warp; r < rows; r += AK_THREADS / 32) {
+        int carry = 0;
+        for (uint32_t c = 0; c < S.W; c += 32) {
+            uint32_t i = c + lane;
+            int      x = i < S.W ? acc[r * W1 + i] : 0;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                int t = __shfl_up_sync(0xffffffffu, x, o);
+                if (lane >= (uint32_t)o)
+                    x += t;
+            }
+            if (i < S.W)
+                out[(size_t)r * S.W + i] = (float)(carry + x) * AK_FIX_INV;
+            carry += __shfl_sync(0xffffffffu, x, 31);
+        }
+    }
+}
+
+__device__ __forceinline__ float4 blend(float al, float4 c, float4 d) {
+    float keep = 1.f - al * c.w;
+    return make_float4(fmaf(al, c.x, keep * d.x), fmaf(al, c.y, keep * d.y), fmaf(al, c.z, keep * d.z),
+                       fmaf(al, c.w, keep * d.w));
+}
+__device__ __forceinline__ float cover(float A) { return fminf(fabsf(A), 1.f); }
+
+template <int N>
+__device__ __forceinline__ float block_sum(float v, float *red) {
+    for (int o = 16; o > 0; o >>= 1)
+        v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0)
+        red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    float s = 0.f;
+    if (threadIdx.x == 0)
+        for (int w = 0; w < N / 32; w++)
+            s += red[w];
+    return s;
+}
+
+__global__ void __launch_bounds__(AK_THREADS)
+    ak_composite(ak_scene S, ak_bufs B, const float4 *__restrict__ colors, const float4 *__restrict__ target,
+                 float *__restrict__ loss_part) {
+    __shared__ float4 col[AK_CHUNK];
+    __shared__ float  red[AK_THREADS / 32];
+    size_t            np = (size_t)S.W * S.H, px = (size_t)blockIdx.x * AK_THREADS + threadIdx.x;
+    bool              valid = px < np;
+    float4            C     = S.bg;
+    for (uint32_t lb = 0; lb < S.nlayers; lb += AK_CHUNK) {
+        uint32_t n = min((uint32_t)AK_CHUNK, S.nlayers - lb);
+        __syncthreads();
+        if (threadIdx.x < n)
+            col[threadIdx.x] = colors[S.layer_path[lb + threadIdx.x]];
+        __syncthreads();
+        if (!valid)
+            continue;
+        B.ckpt[(size_t)(lb / AK_CHUNK) * np + px] = C;
+        float A[AK_CHUNK];
+#pragma unroll
+        for (int q = 0; q < AK_CHUNK; q++)
+            A[q] = q < (int)n ? B.area[(size_t)(lb + q) * np + px] : 0.f;
+#pragma unroll
+        for (int q = 0; q < AK_CHUNK; q++)
+            if (q < (int)n)
+                C = blend(cover(A[q]), col[q], C);
+    }
+    float s = 0.f;
+    if (valid) {
+        B.canvas[px] = C;
+        if (target) {
+            float4 t = target[px];
+            float  a = C.x - t.x, b = C.y - t.y, c = C.z - t.z, d = C.w - t.w;
+            s        = a * a + b * b + c * c + d * d;
+        }
+    }
+    if (target) {
+        s = block_sum<AK_THREADS>(s, red);
+        if (threadIdx.x == 0)
+            loss_part[blockIdx.x] = s;
+    }
+}
+
+/* ------------------------------------------------------------ backward */
+
+__device__ __forceinline__ float4 warp_sum4(float4 v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+        v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+        v.z += __shfl_xor_sync(0xffffffffu, v.z, o);
+        v.w += __shfl_xor_sync(0xffffffffu, v.w, o);
+    }
+    return v;
+}
+
+__global__ void __launch_bounds__(AK_THREADS)
+    ak_composite_bwd(ak_scene S, ak_bufs B, const float4 *__restrict__ colors, const float4 *__restrict__ target,
+                     const float4 *__restrict__ d_canvas, float4 *__restrict__ color_part) {
+    __shared__ float4 col[AK_CHUNK];
+    __shared__ float4 red[AK_THREADS / 32][AK_CHUNK];
+    size_t            np = (size_t)S.W * S.H, px = (size_t)blockIdx.x * AK_THREADS + threadIdx.x;
+    bool              valid = px < np;
+    float4            g     = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (valid) {
+        if (d_canvas) {
+            g = d_canvas[px];
+        } else {
+            float  s = 2.f / (float)(np * 4);
+            float4 c = B.canvas[px], t = target[px];
+            g        = make_float4((c.x - t.x) * s, (c.y - t.y) * s, (c.z - t.z) * s, (c.w - t.w) * s);
+        }
+    }
+    float    T    = 1.f; /* transmittance of the layers above */
+    uint32_t nch  = (S.nlayers + AK_CHUNK - 1) / AK_CHUNK;
+    uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (uint32_t ch = nch; ch-- > 0;) {
+        uint32_t lb = ch * AK_CHUNK, n = min((uint32_t)AK_CHUNK, S.nlayers - lb);
+        __syncthreads();
+        if (threadIdx.x < n)
+            col[threadIdx.x] = colors[S.layer_path[lb + threadIdx.x]];
+        __syncthreads();
+        float4 Bq[AK_CHUNK];
+        float  A[AK_CHUNK];
+        float4 Bc = valid ? B.ckpt[(size_t)ch * np + px] : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int q = 0; q < AK_CHUNK; q++) {
+            A[q]  = (valid && q < (int)n) ? B.area[(size_t)(lb + q) * np + px] : 0.f;
+            Bq[q] = Bc;
+            if (q < (int)n)
+                Bc = blend(cover(A[q]), col[q], Bc);
+        }
+#pragma unroll
+        for (int q = AK_CHUNK - 1; q >= 0; q--) {
+            if (q >= (int)n)
+                continue;
+            float4 c  = col[q];
+            float  al = cover(A[q]);
+            float  gB = g.x * Bq[q].x + g.y * Bq[q].y + g.z * Bq[q].z + g.w * Bq[q].w;
+            float  gc = g.x * c.x + g.y * c.y + g.z * c.z + g.w * c.w;
+            float  da = T * (gc - c.w * gB);
+            float  gA = fabsf(A[q]) < 1.f ? (A[q] > 0.f ? da : A[q] < 0.f ? -da : 0.f) : 0.f;
+            if (valid)
+                B.area[(size_t)(lb + q) * np + px] = gA;
+            float  ta = T * al;
+            float4 dc = make_float4(ta * g.x, ta * g.y, ta * g.z, ta * (g.w - gB));
+            dc        = warp_sum4(dc);
+            if (lane == 0)
+                red[warp][q] = dc;
+            T *= 1.f - al * c.w;
+        }
+        __syncthreads();
+        if (threadIdx.x < n * 4) {
+            uint32_t q = threadIdx.x >> 2, k = threadIdx.x & 3;
+            float    s = 0.f;
+            for (int w = 0; w < AK_THREADS / 32; w++)
+                s += reinterpret_cast<const float *>(&red[w][q])[k];
+            reinterpret_cast<float *>(color_part)[((size_t)blockIdx.x * S.nlayers + lb + q) * 4 + k] = s;
+        }
+    }
+}
+
+__device__ __forceinline__ void add_grad(float2 *g, float2 v) {
+    if (v.x != 0.f || v.y != 0.f) {
+        atomicAdd(&g->x, v.x);
+        atomicAdd(&g->y, v.y);
+    }
+}
+
+__global__ void __launch_bounds__(AK_THREADS)
+    ak_cover_bwd(ak_scene S, ak_bufs B, const float *__restrict__ widths, float2 *__restrict__ gpts,
+                 float *__restrict__ gwidth) {
+    extern __shared__ __align__(16) unsigned char ak_smem[];
+    ak_slot *slots = reinterpret_cast<ak_slot *>(ak_smem);
+    float4  *eg    = reinterpret_cast<float4 *>(slots + AK_THREADS); /* per slot edge: dL/da, dL/db */
+    float   *gs    = reinterpret_cast<float *>(eg + AK_THREADS * 7);
+    __shared__ float red[AK_THREADS / 32];
+    __shared__ int   nslot;
+    uint32_t         l = blockIdx.y;
+    ak_band          bd{(int)(blockIdx.x * AK_BAND), 0, (int)S.W, B.status};
+    bd.y1             = min((int)S.H, bd.y0 + AK_BAND);
+    int          rows = bd.y1 - bd.y0;
+    const float *src  = B.area + ((size_t)l * S.H + bd.y0) * S.W;
+    for (int i = threadIdx.x; i < rows * (int)S.W; i += AK_THREADS)
+        gs[i] = src[i];
+    if (B.off[S.nseg] > B.cap)
+        return;
+    uint32_t p      = S.layer_path[l];
+    bool     stroke = S.layer_stroke[l] != 0;
+    int      E      = stroke ? 7 : 1;
+    float    h      = 0.5f * widths[p], gh = 0.f;
+    uint32_t p1     = B.off[S.path_s0[p + 1]];
+    for (uint32_t base = B.off[S.path_s0[p]]; base < p1; base += AK_THREADS) {
+        if (threadIdx.x == 0)
+            nslot = 0;
+        __syncthreads();
+        gather_slots(S, B, bd, stroke, false, h, base + threadIdx.x, p1, slots, &nslot);
+        __syncthreads();
+        int ns = nslot, ne = ns * E;
+        for (int t = threadIdx.x; t < ne; t += AK_THREADS) {
+            float2 a, b, ga = v2(0.f, 0.f), gb = v2(0.f, 0.f);
+            const ak_slot &sl = slots[t / E];
+            if (slot_edge(sl, stroke, t % E, a, b))
+                edge_bwd(gs, bd, a, b, sl.o, ga, gb);
+            eg[t] = make_float4(ga.x, ga.y, gb.x, gb.y);
+        }
+        __syncthreads();
+        if ((int)threadIdx.x < ns) {
+            const ak_slot &o = slots[threadIdx.x];
+            const float4  *g = eg + threadIdx.x * E;
+            if (!stroke) {
+                add_grad(&gpts[o.k], v2(g[0].x, g[0].y));
+                add_grad(&gpts[o.kn], v2(g[0].z, g[0].w));
+            } else {
+                float2 P = B.pts[o.k], Pn = B.pts[o.kn], Pp = B.pts[o.kp];
+                float2 gP = v2(0.f, 0.f), gPn = v2(0.f, 0.f), gPp = v2(0.f, 0.f);
+                if (o.flags & AK_SLOT_RECT) {
+                    float2 gq[4];
+#pragma unroll
+                    for (int e = 0; e < 4; e++) /* vertex e starts edge e and ends edge e-1 */
+                        gq[e] = v2(g[e].x + g[(e + 3) & 3].z, g[e].y + g[(e + 3) & 3].w);
+                    float2 d  = Pn - P;
+                    float2 n  = perp(d) * rsqrtf(dot2(d, d));
+                    float2 Sg = (gq[0] + gq[1]) - (gq[2] + gq[3]);
+                    gh += dot2(n, Sg);
+                    float2 dd = dnormal(d, Sg * h);
+                    gP        = gP + (gq[0] + gq[3]) - dd;
+                    gPn       = gPn + (gq[1] + gq[2]) + dd;
+                }
+                if (o.flags & AK_SLOT_BEVEL) {
+                    float2 gv[3];
+#pragma unroll
+                    for (int e = 0; e < 3; e++)
+                        gv[e] = v2(g[4 + e].x + g[4 + (e + 2) % 3].z, g[4 + e].y + g[4 + (e + 2) % 3].w);
+                    float2 da = P - Pp, db = Pn - P;
+                    float2 na = perp(da) * rsqrtf(dot2(da, da)), nb = perp(db) * rsqrtf(dot2(db, db));
+                    float2 gna, gnb;
+                    if (o.flags & AK_SLOT_NEG) { /* v1 = p - h nb, v2 = p - h na */
+                        gnb = gv[1] * -h, gna = gv[2] * -h;
+                        gh -= dot2(nb, gv[1]) + dot2(na, gv[2]);
+                    } else { /* v1 = p + h na, v2 = p + h nb */
+                        gna = gv[1] * h, gnb = gv[2] * h;
+                        gh += dot2(na, gv[1]) + dot2(nb, gv[2]);
+                    }
+                    float2 gda = dnormal(da, gna), gdb = dnormal(db, gnb);
+                    gP         = gP + (gv[0] + gv[1] + gv[2]) + (gda - gdb);
+                    gPp        = gPp - gda;
+                    gPn        = gPn + gdb;
+                }
+                add_grad(&gpts[o.kp], gPp);
+                add_grad(&gpts[o.k], gP);
+                add_grad(&gpts[o.kn], gPn);
+            }
+        }
+        __syncthreads();
+    }
+    if (stroke) {
+        float s = block_sum<AK_THREADS>(gh, red);
+        if (threadIdx.x == 0 && s != 0.f)
+            atomicAdd(&gwidth[p], 0.5f * s);
+    }
+}
+
+/* dL/dcolour of every path: sum of its layers' per-block partials */
+__global__ void ak_reduce_colors(ak_scene S, uint32_t nblocks, const float *__restrict__ part,
+                                 float *__restrict__ d_colors) {
+    uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= S.nlayers * 4)
+        return;
+    float s = 0.f;
+    for (uint32_t b = 0; b < nblocks; b++)
+        s += part[(size_t)b * S.nlayers * 4 + t];
+    atomicAdd(&d_colors[S.layer_path[t >> 2] * 4 + (t & 3)], s);
+}
+
+__global__ void ak_reduce_loss(uint32_t nblocks, float scale, const float *__restrict__ part, float *__restrict__ loss) {
+    __shared__ float red[AK_THREADS / 32];
+    float            s = 0.f;
+    for (uint32_t b = threadIdx.x; b < nblocks; b += AK_THREADS)
+        s += part[b];
+    s = block_sum<AK_THREADS>(s, red);
+    if (threadIdx.x == 0)
+        *loss = s * scale;
+}
+
+__global__ void ak_adam(float *__restrict__ p, const float *__restrict__ g, float *__restrict__ m,
+                        float *__restrict__ v, uint32_t n, float lr, float b1, float b2, float eps, float c1, float c2,
+                        float lo, float hi) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    float gi = g[i];
+    float mi = b1 * m[i] + (1.f - b1) * gi;
+    float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+    m[i] = mi, v[i] = vi;
+    float x = p[i] - lr * (mi * c1) / (sqrtf(vi * c2) + eps);
+    p[i]    = fminf(fmaxf(x, lo), hi);
+}
+
+/* ------------------------------------------------------------ launchers */
+
+uint32_t ak_pixel_blocks(const ak_scene &S) { return (uint32_t)(((size_t)S.W * S.H + AK_THREADS - 1) / AK_THREADS); }
+size_t   ak_cover_smem(uint32_t W) {
+    size_t fwd = sizeof(ak_slot) * AK_THREADS + sizeof(int) * AK_BAND * (W + 1);
+    size_t bwd = sizeof(ak_slot) * AK_THREADS + sizeof(float4) * AK_THREADS * 7 + sizeof(float) * AK_BAND * W;
+    return fwd > bwd ? fwd : bwd;
+}
+
+cudaError_t ak_launch_cover(cudaStream_t st, const ak_scene &S, const ak_bufs &B, const float *widths) {
+    size_t smem = sizeof(ak_slot) * AK_THREADS + sizeof(int) * AK_BAND * (S.W + 1);
+    if (smem > 48 * 1024)
+        cudaFuncSetAttribute(ak_cover, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (S.nlayers)
+        ak_cover<<<dim3(S.nbands, S.nlayers), AK_THREADS, smem, st>>>(S, B, widths);
+    return cudaGetLastError();
+}
+cudaError_t ak_launch_composite(cudaStream_t st, const ak_scene &S, const ak_bufs &B, const float4 *colors,
+                                const float4 *target, float *loss_part) {
+    ak_composite<<<ak_pixel_blocks(S), AK_THREADS, 0, st>>>(S, B, colors, target, loss_part);
+    return cudaGetLastError();
+}
+cudaError_t ak_launch_composite_bwd(cudaStream_t st, const ak_scene &S, const ak_bufs &B, const float4 *colors,
+                                    const float4 *target, const float4 *d_canvas, float4 *color_part) {
+    ak_composite_bwd<<<ak_pixel_blocks(S), AK_THREADS, 0, st>>>(S, B, colors, target, d_canvas, color_part);
+    return cudaGetLastError();
+}
+cudaError_t ak_launch_cover_bwd(cudaStream_t st, const ak_scene &S, const ak_bufs &B, const float *widths,
+                                float2 *gpts, float *gwidth) {
+    size_t smem = sizeof(ak_slot) * AK_THREADS + sizeof(float4) * AK_THREADS * 7 + sizeof(float) * AK_BAND * S.W;
+    if (smem > 48 * 1024)
+        cudaFuncSetAttribute(ak_cover_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (S.nlayers)
+        ak_cover_bwd<<<dim3(S.nbands, S.nlayers), AK_THREADS, smem, st>>>(S, B, widths, gpts, gwidth);
+    return cudaGetLastError();
+}
+cudaError_t ak_launch_reduce(cudaStream_t st, const ak_scene &S, uint32_t nblocks, const float4 *color_part,
+                             float4 *d_colors, const float *loss_part, float *loss) {
+    if (color_part && S.nlayers)
+        ak_reduce_colors<<<(S.nlayers * 4 + 255) / 256, 256, 0, st>>>(
+            S, nblocks, reinterpret_cast<const float *>(color_part), reinterpret_cast<float *>(d_colors));
+    if (loss_part)
+        ak_reduce_loss<<<1, AK_THREADS, 0, st>>>(nblocks, 1.f / (float)((size_t)S.W * S.H * 4), loss_part, loss);
+    return cudaGetLastError();
+}
+cudaError_t ak_launch_adam(cudaStream_t st, float *param, const float *grad, float *m, float *v, uint32_t n, float lr,
+                           float beta1, float beta2, float eps, uint32_t step, float lo, float hi) {
+    float c1 = 1.f / (1.f - powf(beta1, (float)step)), c2 = 1.f / (1.f - powf(beta2, (float)step));
+    if (n)
+        ak_adam<<<(n + 255) / 256, 256, 0, st>>>(param, grad, m, v, n, lr, beta1, beta2, eps, c1, c2, lo, hi);
+    return cudaGetLastError();
+}

@@ -1,0 +1,64 @@
+/*
+ * Device-side description of an analytic-coverage scene and the launchers of
+ * its kernels (analytic_flat.cu: flattening and its adjoint; analytic.cu:
+ * coverage, compositing, their adjoints, reductions, Adam).
+ */
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#define AK_SEG_LINE  1 /* segment kinds = the control points a segment consumes */
+#define AK_SEG_CUBIC 3
+#define AK_FILL      1u
+#define AK_STROKE    2u
+
+#define AK_ERR_POINTS 1u /* flattened points exceeded the point buffer */
+#define AK_ERR_WALK   2u /* an edge walk hit its iteration bound */
+
+#define AK_BAND  16 /* pixel rows per coverage block */
+#define AK_CHUNK 16 /* layers per compositing checkpoint */
+
+struct ak_scene {
+    uint32_t        W, H, npaths, ncontours, nseg, ncp, nlayers, nbands;
+    float4          bg;
+    const uint8_t  *seg_kind;     /* nseg */
+    const uint32_t *seg_cp;       /* nseg: first control point */
+    const uint32_t *seg_end;      /* nseg: control point the segment ends at */
+    const uint32_t *seg_contour;  /* nseg */
+    const uint32_t *cont_s0;      /* ncontours+1: first segment */
+    const uint32_t *path_s0;      /* npaths+1: first segment */
+    const uint32_t *layer_path;   /* nlayers */
+    const uint8_t  *layer_stroke; /* nlayers */
+};
+
+/* per-evaluation buffers */
+struct ak_bufs {
+    const uint32_t *off;     /* nseg+1 point offsets of the segments */
+    const float2   *pts;     /* flattened points */
+    const uint32_t *pt_cont; /* contour of each point */
+    uint32_t        cap;     /* capacity of pts */
+    float          *area;    /* nlayers * W * H: signed areas, then their gradients */
+    float4         *ckpt;    /* ceil(nlayers / AK_CHUNK) * W * H: colour under every chunk */
+    float4         *canvas;  /* W * H */
+    uint32_t       *status;
+};
+
+cudaError_t ak_launch_flat_count(cudaStream_t st, const ak_scene &S, const float2 *ctrl, uint32_t *cnt);
+cudaError_t ak_launch_flat_emit(cudaStream_t st, const ak_scene &S, const float2 *ctrl, const uint32_t *off,
+                                float2 *pts, uint32_t *pt_cont, uint32_t cap, uint32_t *status);
+cudaError_t ak_launch_flat_bwd(cudaStream_t st, const ak_scene &S, const float2 *ctrl, const uint32_t *off,
+                               uint32_t cap, const float2 *gpts, float2 *gctrl);
+
+size_t      ak_cover_smem(uint32_t W);
+cudaError_t ak_launch_cover(cudaStream_t st, const ak_scene &S, const ak_bufs &B, const float *widths);
+cudaError_t ak_launch_composite(cudaStream_t st, const ak_scene &S, const ak_bufs &B, const float4 *colors,
+                                const float4 *target, float *loss_part);
+cudaError_t ak_launch_composite_bwd(cudaStream_t st, const ak_scene &S, const ak_bufs &B, const float4 *colors,
+                                    const float4 *target, const float4 *d_canvas, float4 *color_part);
+cudaError_t ak_launch_cover_bwd(cudaStream_t st, const ak_scene &S, const ak_bufs &B, const float *widths,
+                                float2 *gpts, float *gwidth);
+cudaError_t ak_launch_reduce(cudaStream_t st, const ak_scene &S, uint32_t nblocks, const float4 *color_part,
+                             float4 *d_colors, const float *loss_part, float *loss);
+cudaError_t ak_launch_adam(cudaStream_t st, float *param, const float *grad, float *m, float *v, uint32_t n, float lr,
+                           float beta1, float beta2, float eps, uint32_t step, float lo, float hi);
+uint32_t    ak_pixel_blocks(const ak_scene &S);

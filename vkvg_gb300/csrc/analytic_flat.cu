@@ -1,0 +1,151 @@
+/*
+ * K7/K8 (flattening part) - the analytic-coverage mode's flattening and its
+ * adjoint, sm_103a.
+ *
+ * One thread per segment.  A segment starts at its first control point and
+ * ends at the next segment's start (the contour's first for the last one);
+ * it adds its start point, then, for a cubic, the interior points of vkvg's
+ * _recursive_bezier walk (src/vkvg_context_internal.c:1313-1461) at vkvg's
+ * default tolerance 0.25 (src/vkvg_context.c:558).  Concatenated, the
+ * segments of a contour give exactly the points vkvg's move_to / curve_to /
+ * close_path sequence leaves in its path.
+ *
+ * The backward pass walks the same subdivision again instead of storing it:
+ * every emitted point is the blossom of its sub-curve interval, a fixed
+ * linear combination of the four control points (gb_bez_weights), so
+ * dL/dcontrol = sum over the segment's points of weight * dL/dpoint.
+ *
+ * Built with -fmad=false and IEEE division (geometry unit), so the decisions
+ * and the points are those of the plain flatten kernels and of the oracle.
+ */
+#include "analytic.h"
+#include "bezier.cuh"
+
+#include <cuda_runtime.h>
+
+#define AK_TOL 0.25f
+
+__device__ __forceinline__ bool ak_fin(float v) { return (__float_as_uint(v) & 0x7f800000u) != 0x7f800000u; }
+
+struct ak_cnt_emit {
+    uint32_t n;
+    __device__ void operator()(float x, float y, int, float, float) {
+        if (!(x != x || y != y))
+            n++;
+    }
+};
+struct ak_pt_emit {
+    float2   *pts;
+    uint32_t *pc;
+    uint32_t  o, cont;
+    __device__ void operator()(float x, float y, int, float, float) {
+        if (x != x || y != y)
+            return;
+        pts[o] = make_float2(x, y);
+        pc[o]  = cont;
+        o++;
+    }
+};
+struct ak_grad_emit {
+    const float2 *g;
+    uint32_t      o;
+    float2        gc[4];
+    __device__ void operator()(float x, float y, int which, float ta, float tb) {
+        if (x != x || y != y)
+            return;
+        float  w[4];
+        float2 d = g[o++];
+        gb_bez_weights(which, ta, tb, w);
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+            gc[k].x += w[k] * d.x, gc[k].y += w[k] * d.y;
+    }
+};
+
+__device__ __forceinline__ bool ak_cubic_cp(const ak_scene &S, const float2 *ctrl, uint32_t s, float2 c[4]) {
+    uint32_t c0 = S.seg_cp[s];
+    c[0] = ctrl[c0], c[1] = ctrl[c0 + 1], c[2] = ctrl[c0 + 2], c[3] = ctrl[S.seg_end[s]];
+    bool fin = true;
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+        fin = fin && ak_fin(c[k].x) && ak_fin(c[k].y);
+    return fin;
+}
+
+__global__ void ak_flat_count(ak_scene S, const float2 *__restrict__ ctrl, uint32_t *__restrict__ cnt) {
+    uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= S.nseg)
+        return;
+    float2      p = ctrl[S.seg_cp[s]];
+    ak_cnt_emit e{0};
+    e(p.x, p.y, 0, 0.f, 0.f);
+    float2 c[4];
+    if (S.seg_kind[s] == AK_SEG_CUBIC && ak_cubic_cp(S, ctrl, s, c))
+        gb_bezier_walk<false>(AK_TOL, c[0].x, c[0].y, c[1].x, c[1].y, c[2].x, c[2].y, c[3].x, c[3].y, e);
+    cnt[s] = e.n;
+}
+
+__global__ void ak_flat_emit(ak_scene S, const float2 *__restrict__ ctrl, const uint32_t *__restrict__ off,
+                             float2 *__restrict__ pts, uint32_t *__restrict__ pt_cont, uint32_t cap,
+                             uint32_t *__restrict__ status) {
+    uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (off[S.nseg] > cap) {
+        if (s == 0)
+            atomicOr(status, AK_ERR_POINTS);
+        return;
+    }
+    if (s >= S.nseg)
+        return;
+    float2     p = ctrl[S.seg_cp[s]];
+    ak_pt_emit e{pts, pt_cont, off[s], S.seg_contour[s]};
+    e(p.x, p.y, 0, 0.f, 0.f);
+    float2 c[4];
+    if (S.seg_kind[s] == AK_SEG_CUBIC && ak_cubic_cp(S, ctrl, s, c))
+        gb_bezier_walk<false>(AK_TOL, c[0].x, c[0].y, c[1].x, c[1].y, c[2].x, c[2].y, c[3].x, c[3].y, e);
+}
+
+__global__ void ak_flat_bwd(ak_scene S, const float2 *__restrict__ ctrl, const uint32_t *__restrict__ off,
+                            uint32_t cap, const float2 *__restrict__ gpts, float2 *__restrict__ gctrl) {
+    uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= S.nseg || off[S.nseg] > cap)
+        return;
+    uint32_t     c0 = S.seg_cp[s];
+    float2       p  = ctrl[c0];
+    ak_grad_emit e;
+    e.g = gpts, e.o = off[s];
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+        e.gc[k] = make_float2(0.f, 0.f);
+    if (!(p.x != p.x || p.y != p.y)) {
+        e.gc[0] = gpts[e.o];
+        e.o++;
+    }
+    float2 c[4];
+    bool   cubic = S.seg_kind[s] == AK_SEG_CUBIC;
+    if (cubic && ak_cubic_cp(S, ctrl, s, c))
+        gb_bezier_walk<true>(AK_TOL, c[0].x, c[0].y, c[1].x, c[1].y, c[2].x, c[2].y, c[3].x, c[3].y, e);
+    atomicAdd(&gctrl[c0].x, e.gc[0].x), atomicAdd(&gctrl[c0].y, e.gc[0].y);
+    if (cubic) {
+        atomicAdd(&gctrl[c0 + 1].x, e.gc[1].x), atomicAdd(&gctrl[c0 + 1].y, e.gc[1].y);
+        atomicAdd(&gctrl[c0 + 2].x, e.gc[2].x), atomicAdd(&gctrl[c0 + 2].y, e.gc[2].y);
+        uint32_t ce = S.seg_end[s];
+        atomicAdd(&gctrl[ce].x, e.gc[3].x), atomicAdd(&gctrl[ce].y, e.gc[3].y);
+    }
+}
+
+cudaError_t ak_launch_flat_count(cudaStream_t st, const ak_scene &S, const float2 *ctrl, uint32_t *cnt) {
+    if (S.nseg)
+        ak_flat_count<<<(S.nseg + 127) / 128, 128, 0, st>>>(S, ctrl, cnt);
+    return cudaGetLastError();
+}
+cudaError_t ak_launch_flat_emit(cudaStream_t st, const ak_scene &S, const float2 *ctrl, const uint32_t *off,
+                                float2 *pts, uint32_t *pt_cont, uint32_t cap, uint32_t *status) {
+    ak_flat_emit<<<(S.nseg + 127) / 128 + 1, 128, 0, st>>>(S, ctrl, off, pts, pt_cont, cap, status);
+    return cudaGetLastError();
+}
+cudaError_t ak_launch_flat_bwd(cudaStream_t st, const ak_scene &S, const float2 *ctrl, const uint32_t *off,
+                               uint32_t cap, const float2 *gpts, float2 *gctrl) {
+    if (S.nseg)
+        ak_flat_bwd<<<(S.nseg + 127) / 128, 128, 0, st>>>(S, ctrl, off, cap, gpts, gctrl);
+    return cudaGetLastError();
+}

@@ -5,141 +5,23 @@
  * output, an exclusive scan turns counts into offsets, and an emit pass
  * writes the points (float2) and their per-point flags in path order.
  *
- * Cubic segments restate vkvg's _recursive_bezier
- * (src/vkvg_context_internal.c:1313-1461, AGG adaptive subdivision) as an
- * explicit-stack depth-first walk, so points come out in exactly the order of
- * the recursive host code.  The translation unit is built with -fmad=false and
- * IEEE division, and the trigonometry comes from pmath.h, so every decision
- * and every coordinate matches the CPU restatement bit for bit.
- *
- * vkvg compares float values against the double constants 1.7 and 0.01; the
- * float forms below are the exact equivalents:
- *     d > 1.7 (double)   <=>  d >= 1.7f        (1.7f > 1.7 > prev(1.7f))
- *     d < 0.01 (double)  <=>  d <= 0.01f       (0.01f < 0.01 < next(0.01f))
- *     d > 0.01 (double)  <=>  d >  0.01f
+ * Cubic segments follow vkvg's _recursive_bezier
+ * (src/vkvg_context_internal.c:1313-1461) through the explicit-stack walk of
+ * bezier.cuh, so points come out in exactly the order of the recursive host
+ * code.  The translation unit is built with -fmad=false and IEEE division,
+ * and the trigonometry comes from pmath.h, so every decision and every
+ * coordinate matches the CPU restatement bit for bit.
  */
 #include "gb_types.h"
 #include "pmath.h"
 
 #include <cuda_runtime.h>
 
-#define GB_PIF  3.14159265358979323846f
-#define GB_2PIF 0.63661977236758134308f /* vkvg's M_2_PIF = 2/pi (src/vkvg_internal.h:45) */
-
-/* work cap per cubic: far above any finite curve's subdivision tree */
-#define GB_CURVE_NODE_CAP (1u << 22)
-
-struct gb_bez_frame {
-    float x1, y1, x2, y2, x3, y3, x4, y4;
-    unsigned level;
-};
-
-/* Walk the subdivision tree of one cubic, calling emit(x, y) for every point
-   _recursive_bezier would add.  Returns false if the node cap was hit. */
-template <class Emit>
-__device__ __forceinline__ bool gb_bezier_walk(float tol, float x1, float y1, float x2, float y2, float x3, float y3,
-                                               float x4, float y4, Emit &emit) {
-    gb_bez_frame st[102];
-    int          sp = 0;
-    st[sp++]        = {x1, y1, x2, y2, x3, y3, x4, y4, 0u};
-    unsigned nodes  = 0;
-    while (sp > 0) {
-        gb_bez_frame f = st[--sp];
-        if (++nodes > GB_CURVE_NODE_CAP)
-            return false;
-        if (f.level > 100u)
-            continue;
-        float x12   = (f.x1 + f.x2) / 2;
-        float y12   = (f.y1 + f.y2) / 2;
-        float x23   = (f.x2 + f.x3) / 2;
-        float y23   = (f.y2 + f.y3) / 2;
-        float x34   = (f.x3 + f.x4) / 2;
-        float y34   = (f.y3 + f.y4) / 2;
-        float x123  = (x12 + x23) / 2;
-        float y123  = (y12 + y23) / 2;
-        float x234  = (x23 + x34) / 2;
-        float y234  = (y23 + y34) / 2;
-        float x1234 = (x123 + x234) / 2;
-        float y1234 = (y123 + y234) / 2;
-        if (f.level > 0u) {
-            float dx = f.x4 - f.x1;
-            float dy = f.y4 - f.y1;
-            float d2 = fabsf(((f.x2 - f.x4) * dy - (f.y2 - f.y4) * dx));
-            float d3 = fabsf(((f.x3 - f.x4) * dy - (f.y3 - f.y4) * dx));
-            float da1, da2;
-            if (d2 >= 1.7f && d3 >= 1.7f) {
-                if ((d2 + d3) * (d2 + d3) <= (dx * dx + dy * dy) * tol) {
-                    float a23 = pm_atan2f(f.y3 - f.y2, f.x3 - f.x2);
-                    da1       = fabsf(a23 - pm_atan2f(f.y2 - f.y1, f.x2 - f.x1));
-                    da2       = fabsf(pm_atan2f(f.y4 - f.y3, f.x4 - f.x3) - a23);
-                    if (da1 >= GB_PIF)
-                        da1 = GB_2PIF - da1;
-                    if (da2 >= GB_PIF)
-                        da2 = GB_2PIF - da2;
-                    if (da1 + da2 < 0.01f) {
-                        emit(x1234, y1234);
-                        continue;
-                    }
-                    if (da1 > 0.01f) {
-                        emit(f.x2, f.y2);
-                        continue;
-                    }
-                    if (da2 > 0.01f) {
-                        emit(f.x3, f.y3);
-                        continue;
-                    }
-                }
-            } else {
-                if (d2 >= 1.7f) {
-                    if (d2 * d2 <= tol * (dx * dx + dy * dy)) {
-                        da1 = fabsf(pm_atan2f(f.y3 - f.y2, f.x3 - f.x2) - pm_atan2f(f.y2 - f.y1, f.x2 - f.x1));
-                        if (da1 >= GB_PIF)
-                            da1 = GB_2PIF - da1;
-                        if (da1 <= 0.01f) {
-                            emit(f.x2, f.y2);
-                            emit(f.x3, f.y3);
-                            continue;
-                        }
-                        if (da1 > 0.01f) {
-                            emit(f.x2, f.y2);
-                            continue;
-                        }
-                    }
-                } else if (d3 >= 1.7f) {
-                    if (d3 * d3 <= tol * (dx * dx + dy * dy)) {
-                        da1 = fabsf(pm_atan2f(f.y4 - f.y3, f.x4 - f.x3) - pm_atan2f(f.y3 - f.y2, f.x3 - f.x2));
-                        if (da1 >= GB_PIF)
-                            da1 = GB_2PIF - da1;
-                        if (da1 <= 0.01f) {
-                            emit(f.x2, f.y2);
-                            emit(f.x3, f.y3);
-                            continue;
-                        }
-                        if (da1 > 0.01f) {
-                            emit(f.x3, f.y3);
-                            continue;
-                        }
-                    }
-                } else {
-                    float ex = x1234 - (f.x1 + f.x4) / 2;
-                    float ey = y1234 - (f.y1 + f.y4) / 2;
-                    if (ex * ex + ey * ey <= tol) {
-                        emit(x1234, y1234);
-                        continue;
-                    }
-                }
-            }
-        }
-        /* subdivide: left half first, so push the right half below it */
-        st[sp++] = {x1234, y1234, x234, y234, x34, y34, f.x4, f.y4, f.level + 1u};
-        st[sp++] = {f.x1, f.y1, x12, y12, x123, y123, x1234, y1234, f.level + 1u};
-    }
-    return true;
-}
+#include "bezier.cuh"
 
 struct gb_count_emit {
     uint32_t n;
-    __device__ void operator()(float x, float y) {
+    __device__ void operator()(float x, float y, int = 0, float = 0.f, float = 0.f) {
         if (!(x != x || y != y))
             n++;
     }
@@ -149,7 +31,7 @@ struct gb_write_emit {
     uint8_t *flg;
     uint32_t o, end;
     uint8_t  flag;
-    __device__ void operator()(float x, float y) {
+    __device__ void operator()(float x, float y, int = 0, float = 0.f, float = 0.f) {
         if (x != x || y != y)
             return;
         if (o < end) {
@@ -174,7 +56,7 @@ __device__ __forceinline__ bool gb_segment_points(uint32_t info, float4 a, float
         bool fin = gb_finite(a.x) && gb_finite(a.y) && gb_finite(a.z) && gb_finite(a.w) && gb_finite(b.x) &&
                    gb_finite(b.y) && gb_finite(b.z) && gb_finite(b.w);
         if (fin)
-            ok = gb_bezier_walk(c.x, a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, emit);
+            ok = gb_bezier_walk<false>(c.x, a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, emit);
         emit(b.z, b.w);
     } else if (kind == GB_SEG_ARC) {
         /* vkvg_arc / vkvg_arc_negative loop, src/vkvg_context.c:424-430 */

@@ -763,3 +763,40 @@ def decode(cmds, args):
         ops.append((name,) + tuple(float(v) for v in args[a:a + n]))
         a += n
     return ops
+
+
+# ------------------------------------------------------------------ analytic
+
+AN_LINE, AN_CUBIC = 1, 3
+AN_FILL, AN_STROKE = 1, 2
+
+
+def analytic_scene(seed=3, n_paths=128, n_cubics=8, size=256, w_min=0.5, w_max=4.0):
+    """Scene of the differentiable analytic-coverage mode: a size x size fp32
+    RGBA canvas on an opaque white background; n_paths closed paths of
+    n_cubics cubic Beziers each, control points uniform in [0,size)^2; per
+    path a colour with straight RGBA U[0,1) premultiplied by its alpha, a
+    NON_ZERO fill and a stroke of width U[w_min, w_max) in the same colour.
+    The differentiable benchmark uses seed 3 for the optimised paths and
+    seed 4 for the target image.  Returns the scene description and its
+    parameters (float32 arrays)."""
+    import numpy as np
+
+    r = SplitMix64(seed)
+    ncp = n_paths * n_cubics * 3
+    ctrl = np.array([r.rnd() * size for _ in range(2 * ncp)], np.float32).reshape(ncp, 2)
+    colors = np.zeros((n_paths, 4), np.float32)
+    widths = np.zeros(n_paths, np.float32)
+    for p in range(n_paths):
+        rgb = [r.rnd() for _ in range(3)]
+        a = r.rnd()
+        colors[p] = [rgb[0] * a, rgb[1] * a, rgb[2] * a, a]
+        widths[p] = w_min + r.rnd() * (w_max - w_min)
+    scene = {
+        "width": size, "height": size, "background": np.ones(4, np.float32),
+        "path_ncontours": np.ones(n_paths, np.uint32),
+        "path_flags": np.full(n_paths, AN_FILL | AN_STROKE, np.uint32),
+        "contour_nseg": np.full(n_paths, n_cubics, np.uint32),
+        "seg_kind": np.full(n_paths * n_cubics, AN_CUBIC, np.uint8),
+    }
+    return scene, {"ctrl": ctrl, "colors": colors, "widths": widths}
