@@ -59,6 +59,8 @@ def parse():
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     p.add_argument("--svg-shapes", type=int, default=600, help="shapes of the SVG ingestion workload (0: skip)")
     p.add_argument("--no-batch", action="store_true", help="skip the uneven-batch comparison")
+    p.add_argument("--no-analytic", action="store_true", help="skip the differentiable analytic-coverage workload")
+    p.add_argument("--adam-steps", type=int, default=200, help="Adam steps of the differentiable workload")
     return p.parse_args()
 
 
@@ -160,6 +162,162 @@ def cpu_sample(n_paths, size, threads, reps=1):
         ctx.destroy()
         surf.destroy()
     return n_paths / min(times), min(times)
+
+
+def analytic_bench(a, gb, torch, np, flush, cpu):
+    """The differentiable analytic-coverage workload: a 256x256 fp32 canvas on
+    white, 128 closed paths of 8 cubics (seed 3), NON_ZERO fill + stroke in a
+    premultiplied colour, MSE against the same render of an independent
+    seed-4 path set.  Times the forward, forward + backward, and Adam steps
+    (lr 0.5 px for control points), all through the C ABI on device memory;
+    e2e adds the host copies of parameters and gradients.  With cpu, also
+    times the FP64 CPU reference's forward + backward and checks the GPU
+    gradient against it and against FP64 central differences."""
+    import ctypes as C
+
+    from vkvg_gb300 import scenes
+
+    scene, par = scenes.analytic_scene(seed=3)
+    _, tpar = scenes.analytic_scene(seed=4)
+    A = gb.Analytic(scene)
+    dev = {k: torch.tensor(v, device="cuda") for k, v in par.items()}
+    tdev = {k: torch.tensor(v, device="cuda") for k, v in tpar.items()}
+    canvas, _ = A.forward(tdev["ctrl"], tdev["colors"], tdev["widths"])
+    target = canvas.clone()
+    st = torch.cuda.current_stream()
+    A.forward(dev["ctrl"], dev["colors"], dev["widths"], target)
+    grads = A.backward()
+
+    def fwd():
+        A.forward(dev["ctrl"], dev["colors"], dev["widths"], target)
+
+    def fwd_bwd():
+        fwd()
+        A.backward(grads=grads)
+
+    def timed(fn, n):
+        for _ in range(max(3, a.warmup)):
+            fn()
+        ts = []
+        for _ in range(n):
+            flush()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            fn()
+            e1.record(st)
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        return statistics.median(ts)
+
+    n = max(10, a.steps)
+    t_f = timed(fwd, n)
+    t_fb = timed(fwd_bwd, n)
+    A.set_timing(True)
+    fwd_bwd()
+    phases = [float(x) for x in A.timing()]
+    A.set_timing(False)
+    assert A.sync() == 0
+    # Adam on all parameters: lr 0.5 px (control points), 0.01 (colours,
+    # clamped to [0,1]), 0.05 px (widths, clamped to [0.1,16])
+    p = {k: v.clone() for k, v in dev.items()}
+    m = {k: torch.zeros_like(v) for k, v in p.items()}
+    v_ = {k: torch.zeros_like(v) for k, v in p.items()}
+    lr = {"ctrl": (0.5, -1e4, 1e4), "colors": (0.01, 0.0, 1.0), "widths": (0.05, 0.1, 16.0)}
+    losses = torch.zeros(a.adam_steps, device="cuda")
+    torch.cuda.synchronize()
+    l0 = gb.kernel_launches()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for i in range(1, a.adam_steps + 1):
+        A.forward(p["ctrl"], p["colors"], p["widths"], target)
+        losses[i - 1].copy_(A.loss[0])
+        g = A.backward(grads=grads)
+        for k, gk in zip(("ctrl", "colors", "widths"), g):
+            A.adam(p[k], gk, m[k], v_[k], i, *lr[k])
+    e1.record(st)
+    e1.synchronize()
+    adam_ms = e0.elapsed_time(e1) / a.adam_steps
+    launches = (gb.kernel_launches() - l0) / a.adam_steps
+    assert A.sync() == 0
+    ls = losses.cpu().numpy()
+    # end to end: host parameters in, host gradients out, every step
+    hp = {k: torch.tensor(v).pin_memory() for k, v in par.items()}
+    hg = [torch.empty(t.shape, dtype=torch.float32).pin_memory() for t in grads]
+    hl = torch.empty(1, dtype=torch.float32).pin_memory()
+
+    def e2e_step():
+        for k in dev:
+            dev[k].copy_(hp[k], non_blocking=True)
+        A.forward(dev["ctrl"], dev["colors"], dev["widths"], target)
+        hl.copy_(A.loss, non_blocking=True)
+        gg = A.backward(grads=grads)
+        for h, d in zip(hg, gg):
+            h.copy_(d, non_blocking=True)
+        st.synchronize()
+
+    for _ in range(3):
+        e2e_step()
+    t0 = time.perf_counter()
+    for _ in range(n):
+        e2e_step()
+    e2e_ms = (time.perf_counter() - t0) / n * 1e3
+    h2d = sum(t.numel() * 4 for t in hp.values())
+    d2h = sum(t.numel() * 4 for t in hg) + 4
+    pts, _ = A.points()
+    npx, nl = 256 * 256, A.nlayers
+    nchunk = (nl + 15) // 16
+    # algorithmic bytes of the compositing adjoint: areas read and their
+    # gradients written (4 B per layer-pixel each), chunk checkpoints read
+    # (16 B per chunk-pixel), canvas and target read (32 B per pixel)
+    cb_bytes = npx * (8 * nl + 16 * nchunk + 32)
+    out = {"workload": "analytic fp32 256x256, 128 closed paths x 8 cubics (seed 3), NON_ZERO fill + stroke w U[0.5,4), "
+                       "MSE vs the seed-4 render", "layers": nl, "flattened_points": int(len(pts)),
+           "fwd_ms": t_f, "fwd_bwd_ms": t_fb, "fwd_bwd_over_fwd": t_fb / t_f,
+           "phase_ms": {"flatten": phases[0], "cover": phases[1], "composite": phases[2],
+                        "composite_adjoint": phases[3], "cover_adjoint": phases[4], "flatten_adjoint": phases[5]},
+           "adam_steps": a.adam_steps, "adam_ms_per_step": adam_ms, "loss_first": float(ls[0]),
+           "loss_last": float(ls[-1]), "gpu_launches_per_step": launches,
+           "e2e": {"ms_per_step": e2e_ms, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+           "roofline": {"kernel": "ak_composite_bwd", "bound": "hbm", "algorithmic_bytes": cb_bytes,
+                        "achieved": cb_bytes / (phases[3] / 1e3) / 1e9, "unit": "GB/s"},
+           "timing": "CUDA events on the scene's stream, L2 flushed (256 MiB write) before each fwd / fwd+bwd "
+                     "iteration; the Adam loop runs unflushed, as a training loop does"}
+    if cpu:
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        import analytic_ref as ar
+
+        R = ar.Reference(scene)
+        tgt = target.cpu().numpy().astype(np.float64)
+        t0 = time.perf_counter()
+        _, rc, rcol, rw = R.backward(par["ctrl"], par["colors"], par["widths"], tgt)
+        cpu_s = time.perf_counter() - t0
+        A.forward(dev["ctrl"], dev["colors"], dev["widths"], target)
+        gg = [x.cpu().numpy().astype(np.float64) for x in A.backward()]
+        assert A.sync() == 0
+        rel = {k: float(np.linalg.norm(a_ - b_) / np.linalg.norm(b_))
+               for k, a_, b_ in zip(("ctrl", "colors", "widths"), gg, (rc, rcol, rw))}
+        rng = np.random.default_rng(3)
+        grp = np.concatenate([np.zeros(160), np.ones(80), 2 * np.ones(80)]).astype(np.uint32)
+        idx = np.concatenate([rng.choice(2 * R.nctrl, 160, replace=False), rng.choice(4 * R.npaths, 80, replace=False),
+                              rng.choice(R.npaths, 80, replace=False)]).astype(np.uint32)
+        fd, fd2, ok = R.fd(par["ctrl"], par["colors"], par["widths"], tgt, grp, idx, h=1e-3, h2=1e-4)
+        floor = 1e-3 * np.abs(fd).max()
+        ok &= np.abs(fd2 - fd) / np.maximum(np.abs(fd), floor) < 2e-4
+        keep = np.zeros(len(grp), bool)
+        for gq, want in ((0, 128), (1, 64), (2, 64)):
+            keep[np.nonzero((grp == gq) & ok)[0][:want]] = True
+        an = np.array([gg[0].reshape(-1)[i] if k == 0 else gg[1].reshape(-1)[i] if k == 1 else gg[2][i]
+                       for k, i in zip(grp, idx)])
+        err = np.abs(an[keep] - fd[keep]) / np.maximum(np.abs(fd[keep]), floor)
+        out["cpu_baseline"] = {"fwd_bwd_ms": cpu_s * 1e3, "cores": 1, "kind": "port",
+                               "sample": "one forward + backward of the same scene, FP64 CPU reference"}
+        out["grad_error"] = {"vs_fp64_reference_rel_l2": rel, "vs_fp64_fd_h1e-3_max_rel": float(err.max()),
+                             "vs_fp64_fd_median_rel": float(np.median(err)), "fd_params": int(keep.sum()),
+                             "fd_not_smooth_replaced": int((~ok[:np.nonzero(keep)[0].max() + 1]).sum()),
+                             "rel": "|g - fd| / max(|fd|, 1e-3 max|fd|)"}
+        R.close()
+    A.destroy()
+    return out
 
 
 def run_reference(a, rank):
@@ -381,6 +539,11 @@ def main():
             s1.destroy()
             s2.destroy()
 
+    # ---- the differentiable analytic-coverage workload
+    analytic = None
+    if not a.no_analytic and world == 1:
+        analytic = analytic_bench(a, gb, torch, np, l2_flush, cpu=rank == 0 and not a.no_cpu)
+
     # ---- roofline of the raster/composite kernel
     peak, peak_kind = hbm_peak()
     nflat, nsv = int(stats[1]), int(stats[2])
@@ -429,6 +592,10 @@ def main():
         line["svg"] = svg
     if batch:
         line["batch"] = batch
+    if analytic:
+        analytic["roofline"]["peak"] = peak
+        analytic["roofline"]["frac"] = analytic["roofline"]["achieved"] / peak
+        line["analytic"] = analytic
     if rank == 0 and not a.no_cpu:
         threads = os.cpu_count() or 1
         v, _ = cpu_sample(64, a.size, threads)

@@ -244,6 +244,12 @@ vkvg_public vkvg_status_t vkvg_gb300_analytic_sync(VkvgAnalytic a);
 /* the last forward's flattened points (host copy, at most cap points; syncs):
    returns their count; seg_offsets, if not null, gets nseg+1 offsets */
 vkvg_public uint32_t      vkvg_gb300_analytic_points(VkvgAnalytic a, float *pts, uint32_t cap, uint32_t *seg_offsets);
+/* phase times of the last forward and backward, ms (set_timing(a, 1) first;
+   syncs): [0] flattening, [1] coverage, [2] compositing and loss, [3]
+   compositing adjoint and colour reduction, [4] coverage adjoint, [5]
+   flattening adjoint */
+vkvg_public vkvg_status_t vkvg_gb300_analytic_set_timing(VkvgAnalytic a, int on);
+vkvg_public vkvg_status_t vkvg_gb300_analytic_timing(VkvgAnalytic a, float out[6]);
 /* the last backward's gradient with respect to each flattened point (host
    copy of at most cap points, x and y; syncs): returns the point count */
 vkvg_public uint32_t      vkvg_gb300_analytic_point_grads(VkvgAnalytic a, float *grads, uint32_t cap);

@@ -192,6 +192,8 @@ SIGNATURES = {
     "vkvg_gb300_analytic_sync": (_I, [_P]),
     "vkvg_gb300_analytic_points": (_U, [_P, _P, _U, _P]),
     "vkvg_gb300_analytic_point_grads": (_U, [_P, _P, _U]),
+    "vkvg_gb300_analytic_set_timing": (_I, [_P, _I]),
+    "vkvg_gb300_analytic_timing": (_I, [_P, _P]),
 }
 
 
@@ -546,6 +548,16 @@ class Analytic:
         off = np.zeros(len(self._keep["seg_kind"]) + 1, np.uint32)
         self.L.vkvg_gb300_analytic_points(self.h, _ptr(pts), n, _ptr(off))
         return pts[:n], off
+
+    def set_timing(self, on=True):
+        self._check(self.L.vkvg_gb300_analytic_set_timing(self.h, 1 if on else 0), "analytic_set_timing")
+
+    def timing(self):
+        """ms of the last forward's flattening, coverage, compositing and the
+        last backward's compositing, coverage and flattening adjoints"""
+        t = np.zeros(6, np.float32)
+        self._check(self.L.vkvg_gb300_analytic_timing(self.h, _ptr(t)), "analytic_timing")
+        return t
 
     def point_grads(self):
         """dL/dpoint of the last backward, float32 [points, 2]"""

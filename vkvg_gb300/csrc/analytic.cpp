@@ -36,6 +36,10 @@ struct _vkvg_gb300_analytic_t {
     bool        mon_pending = false;
     uint32_t    cap = 0;
     vkvg_status_t pending = VKVG_STATUS_SUCCESS; /* first error since the last sync */
+    /* phase timing (set_timing): events around flatten, cover, composite of
+       the forward and composite, cover, flatten adjoints of the backward */
+    bool        timing = false;
+    cudaEvent_t ev[8]  = {};
     /* the last forward */
     bool         have_fwd = false, sized = false;
     const float *f_ctrl = nullptr, *f_colors = nullptr, *f_widths = nullptr, *f_target = nullptr;
@@ -165,7 +169,7 @@ VkvgAnalytic vkvg_gb300_analytic_create(uint32_t width, uint32_t height, const f
          a->d_area.grow(sizeof(float) * np * std::max<uint32_t>(a->nlayers, 1)) &&
          a->d_ckpt.grow(sizeof(float4) * np * std::max<size_t>(nchk, 1)) && a->d_canvas.grow(sizeof(float4) * np) &&
          a->d_loss_part.grow(sizeof(float) * nbk) && a->d_loss.grow(sizeof(float)) &&
-         a->d_color_part.grow(sizeof(float4) * (size_t)nbk * std::max<uint32_t>(a->nlayers, 1)) &&
+         a->d_color_part.grow(sizeof(float4) * (size_t)(np + 127) / 128 * std::max<uint32_t>(a->nlayers, 1)) &&
          a->d_status.grow(4) && a->h_mon.grow(8) && size_points(a, std::max<uint32_t>(64 * nseg, 65536));
     ok = ok && cudaMemset(a->d_status.p, 0, 4) == cudaSuccess;
     if (!ok) {
@@ -202,6 +206,9 @@ void vkvg_gb300_analytic_destroy(VkvgAnalytic a) {
     a->h_mon.release();
     if (a->ev_mon)
         cudaEventDestroy(a->ev_mon);
+    for (cudaEvent_t ev : a->ev)
+        if (ev)
+            cudaEventDestroy(ev);
     if (a->own_stream)
         cudaStreamDestroy(a->stream);
     delete a;
@@ -233,7 +240,9 @@ vkvg_status_t vkvg_gb300_analytic_forward(VkvgAnalytic a, const float *ctrl, con
     poll(a, false);
     cudaStream_t st = a->stream;
     const float2 *c2 = (const float2 *)ctrl;
-    cudaError_t   e  = ak_launch_flat_count(st, a->S, c2, a->d_cnt.as<uint32_t>());
+    if (a->timing)
+        cudaEventRecord(a->ev[0], st);
+    cudaError_t e = ak_launch_flat_count(st, a->S, c2, a->d_cnt.as<uint32_t>());
     if (e == cudaSuccess)
         e = gb_exclusive_scan(st, a->d_cnt.as<uint32_t>(), a->nseg, a->d_off.as<uint32_t>(), a->d_scan.as<uint32_t>());
     gb_count_launch(4);
@@ -251,8 +260,12 @@ vkvg_status_t vkvg_gb300_analytic_forward(VkvgAnalytic a, const float *ctrl, con
     ak_bufs B = bufs(a);
     e         = ak_launch_flat_emit(st, a->S, c2, B.off, a->d_pts.as<float2>(), a->d_pt_cont.as<uint32_t>(), a->cap,
                                     B.status);
+    if (a->timing)
+        cudaEventRecord(a->ev[1], st);
     if (e == cudaSuccess)
         e = ak_launch_cover(st, a->S, B, widths);
+    if (a->timing)
+        cudaEventRecord(a->ev[2], st);
     if (e == cudaSuccess)
         e = ak_launch_composite(st, a->S, B, (const float4 *)colors, (const float4 *)target,
                                 target ? a->d_loss_part.as<float>() : nullptr);
@@ -261,6 +274,8 @@ vkvg_status_t vkvg_gb300_analytic_forward(VkvgAnalytic a, const float *ctrl, con
         e = ak_launch_reduce(st, a->S, ak_pixel_blocks(a->S), nullptr, nullptr, a->d_loss_part.as<float>(), loss);
         gb_count_launch(1);
     }
+    if (a->timing)
+        cudaEventRecord(a->ev[3], st);
     if (e == cudaSuccess && canvas)
         e = cudaMemcpyAsync(canvas, a->d_canvas.p, sizeof(float4) * a->W * a->H, cudaMemcpyDeviceToDevice, st);
     if (e == cudaSuccess && !a->mon_pending) {
@@ -290,7 +305,7 @@ vkvg_status_t vkvg_gb300_analytic_backward(VkvgAnalytic a, const float *d_canvas
         return VKVG_STATUS_NULL_POINTER;
     cudaStream_t st = a->stream;
     ak_bufs      B  = bufs(a);
-    uint32_t     nb = ak_pixel_blocks(a->S);
+    uint32_t     nb = ak_composite_bwd_blocks(a->S);
     cudaError_t  e  = cudaMemsetAsync(d_ctrl, 0, sizeof(float) * 2 * a->ncp, st);
     if (e == cudaSuccess)
         e = cudaMemsetAsync(d_colors, 0, sizeof(float) * 4 * a->npaths, st);
@@ -298,16 +313,24 @@ vkvg_status_t vkvg_gb300_analytic_backward(VkvgAnalytic a, const float *d_canvas
         e = cudaMemsetAsync(d_widths, 0, sizeof(float) * a->npaths, st);
     if (e == cudaSuccess)
         e = cudaMemsetAsync(a->d_gpts.p, 0, sizeof(float2) * a->cap, st);
+    if (a->timing)
+        cudaEventRecord(a->ev[4], st);
     if (e == cudaSuccess)
         e = ak_launch_composite_bwd(st, a->S, B, (const float4 *)a->f_colors, (const float4 *)a->f_target,
                                     (const float4 *)d_canvas, a->d_color_part.as<float4>());
     if (e == cudaSuccess)
         e = ak_launch_reduce(st, a->S, nb, a->d_color_part.as<float4>(), (float4 *)d_colors, nullptr, nullptr);
+    if (a->timing)
+        cudaEventRecord(a->ev[5], st);
     if (e == cudaSuccess)
         e = ak_launch_cover_bwd(st, a->S, B, a->f_widths, a->d_gpts.as<float2>(), d_widths);
+    if (a->timing)
+        cudaEventRecord(a->ev[6], st);
     if (e == cudaSuccess)
         e = ak_launch_flat_bwd(st, a->S, (const float2 *)a->f_ctrl, B.off, a->cap, a->d_gpts.as<float2>(),
                                (float2 *)d_ctrl);
+    if (a->timing)
+        cudaEventRecord(a->ev[7], st);
     gb_count_launch(4);
     a->have_fwd = false; /* the areas now hold their gradients */
     return fail(a, e);
@@ -356,6 +379,30 @@ uint32_t vkvg_gb300_analytic_points(VkvgAnalytic a, float *pts, uint32_t cap, ui
     if (seg_offsets)
         memcpy(seg_offsets, off.data(), 4 * off.size());
     return n;
+}
+
+vkvg_status_t vkvg_gb300_analytic_set_timing(VkvgAnalytic a, int on) {
+    if (!a)
+        return VKVG_STATUS_NULL_POINTER;
+    if (on && !a->ev[0])
+        for (cudaEvent_t &ev : a->ev)
+            if (cudaEventCreate(&ev) != cudaSuccess)
+                return VKVG_STATUS_DEVICE_ERROR;
+    a->timing = on != 0;
+    return VKVG_STATUS_SUCCESS;
+}
+
+vkvg_status_t vkvg_gb300_analytic_timing(VkvgAnalytic a, float out[6]) {
+    if (!a || !out)
+        return VKVG_STATUS_NULL_POINTER;
+    if (!a->timing || cudaStreamSynchronize(a->stream) != cudaSuccess)
+        return VKVG_STATUS_INVALID_STATUS;
+    for (int k = 0; k < 6; k++) {
+        int i0 = k < 3 ? k : k + 1;
+        if (cudaEventElapsedTime(&out[k], a->ev[i0], a->ev[i0 + 1]) != cudaSuccess)
+            out[k] = -1.f;
+    }
+    return VKVG_STATUS_SUCCESS;
 }
 
 uint32_t vkvg_gb300_analytic_point_grads(VkvgAnalytic a, float *grads, uint32_t cap) {

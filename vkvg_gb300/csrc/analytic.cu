@@ -492,12 +492,32 @@ __device__ __forceinline__ float4 warp_sum4(float4 v) {
     return v;
 }
 
-__global__ void __launch_bounds__(AK_THREADS)
+/* Sum of v[0..31] over the warp, scattered: lane l returns the warp's sum of
+   v[l] (recursive halving, 31 shuffles for 32 sums). */
+__device__ __forceinline__ float warp_reduce_scatter32(float (&v)[32]) {
+    const unsigned lane = threadIdx.x & 31u;
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) {
+        bool up = (lane & (unsigned)o) != 0;
+#pragma unroll
+        for (int k = 0; k < o; k++) {
+            float send = up ? v[k] : v[k + o];
+            float keep = up ? v[k + o] : v[k];
+            v[k]       = keep + __shfl_xor_sync(0xffffffffu, send, o);
+        }
+    }
+    return v[0];
+}
+
+#define AK_CB_THREADS 128 /* pixels per compositing-adjoint block */
+
+__global__ void __launch_bounds__(AK_CB_THREADS)
     ak_composite_bwd(ak_scene S, ak_bufs B, const float4 *__restrict__ colors, const float4 *__restrict__ target,
-                     const float4 *__restrict__ d_canvas, float4 *__restrict__ color_part) {
+                     const float4 *__restrict__ d_canvas, float *__restrict__ color_part) {
     __shared__ float4 col[AK_CHUNK];
-    __shared__ float4 red[AK_THREADS / 32][AK_CHUNK];
-    size_t            np = (size_t)S.W * S.H, px = (size_t)blockIdx.x * AK_THREADS + threadIdx.x;
+    __shared__ float4 sB[AK_CHUNK][AK_CB_THREADS]; /* colour under each layer of the chunk */
+    __shared__ float  red[AK_CB_THREADS / 32][AK_CHUNK * 4];
+    size_t            np = (size_t)S.W * S.H, px = (size_t)blockIdx.x * AK_CB_THREADS + threadIdx.x;
     bool              valid = px < np;
     float4            g     = make_float4(0.f, 0.f, 0.f, 0.f);
     if (valid) {
@@ -518,42 +538,48 @@ __global__ void __launch_bounds__(AK_THREADS)
         if (threadIdx.x < n)
             col[threadIdx.x] = colors[S.layer_path[lb + threadIdx.x]];
         __syncthreads();
-        float4 Bq[AK_CHUNK];
         float  A[AK_CHUNK];
         float4 Bc = valid ? B.ckpt[(size_t)ch * np + px] : make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
+        for (int q = 0; q < AK_CHUNK; q++)
+            A[q] = (valid && q < (int)n) ? B.area[(size_t)(lb + q) * np + px] : 0.f;
+#pragma unroll
         for (int q = 0; q < AK_CHUNK; q++) {
-            A[q]  = (valid && q < (int)n) ? B.area[(size_t)(lb + q) * np + px] : 0.f;
-            Bq[q] = Bc;
+            sB[q][threadIdx.x] = Bc;
             if (q < (int)n)
                 Bc = blend(cover(A[q]), col[q], Bc);
         }
+        /* two halves of 8 layers, top half first; colour partials per half */
 #pragma unroll
-        for (int q = AK_CHUNK - 1; q >= 0; q--) {
-            if (q >= (int)n)
-                continue;
-            float4 c  = col[q];
-            float  al = cover(A[q]);
-            float  gB = g.x * Bq[q].x + g.y * Bq[q].y + g.z * Bq[q].z + g.w * Bq[q].w;
-            float  gc = g.x * c.x + g.y * c.y + g.z * c.z + g.w * c.w;
-            float  da = T * (gc - c.w * gB);
-            float  gA = fabsf(A[q]) < 1.f ? (A[q] > 0.f ? da : A[q] < 0.f ? -da : 0.f) : 0.f;
-            if (valid)
-                B.area[(size_t)(lb + q) * np + px] = gA;
-            float  ta = T * al;
-            float4 dc = make_float4(ta * g.x, ta * g.y, ta * g.z, ta * (g.w - gB));
-            dc        = warp_sum4(dc);
-            if (lane == 0)
-                red[warp][q] = dc;
-            T *= 1.f - al * c.w;
+        for (int hf = 1; hf >= 0; hf--) {
+            float dc[32];
+#pragma unroll
+            for (int q8 = 7; q8 >= 0; q8--) {
+                int q = hf * 8 + q8;
+                dc[4 * q8] = dc[4 * q8 + 1] = dc[4 * q8 + 2] = dc[4 * q8 + 3] = 0.f;
+                if (q >= (int)n)
+                    continue;
+                float4 c  = col[q], Bq = sB[q][threadIdx.x];
+                float  al = cover(A[q]);
+                float  gB = g.x * Bq.x + g.y * Bq.y + g.z * Bq.z + g.w * Bq.w;
+                float  gc = g.x * c.x + g.y * c.y + g.z * c.z + g.w * c.w;
+                float  da = T * (gc - c.w * gB);
+                float  gA = fabsf(A[q]) < 1.f ? (A[q] > 0.f ? da : A[q] < 0.f ? -da : 0.f) : 0.f;
+                if (valid)
+                    B.area[(size_t)(lb + q) * np + px] = gA;
+                float ta = T * al;
+                dc[4 * q8] = ta * g.x, dc[4 * q8 + 1] = ta * g.y, dc[4 * q8 + 2] = ta * g.z;
+                dc[4 * q8 + 3] = ta * (g.w - gB);
+                T *= 1.f - al * c.w;
+            }
+            red[warp][hf * 32 + lane] = warp_reduce_scatter32(dc);
         }
         __syncthreads();
         if (threadIdx.x < n * 4) {
-            uint32_t q = threadIdx.x >> 2, k = threadIdx.x & 3;
-            float    s = 0.f;
-            for (int w = 0; w < AK_THREADS / 32; w++)
-                s += reinterpret_cast<const float *>(&red[w][q])[k];
-            reinterpret_cast<float *>(color_part)[((size_t)blockIdx.x * S.nlayers + lb + q) * 4 + k] = s;
+            float s = 0.f;
+            for (int w = 0; w < AK_CB_THREADS / 32; w++)
+                s += red[w][threadIdx.x];
+            color_part[((size_t)blockIdx.x * S.nlayers + lb) * 4 + threadIdx.x] = s;
         }
     }
 }
@@ -717,9 +743,13 @@ cudaError_t ak_launch_composite(cudaStream_t st, const ak_scene &S, const ak_buf
     ak_composite<<<ak_pixel_blocks(S), AK_THREADS, 0, st>>>(S, B, colors, target, loss_part);
     return cudaGetLastError();
 }
+uint32_t ak_composite_bwd_blocks(const ak_scene &S) {
+    return (uint32_t)(((size_t)S.W * S.H + AK_CB_THREADS - 1) / AK_CB_THREADS);
+}
 cudaError_t ak_launch_composite_bwd(cudaStream_t st, const ak_scene &S, const ak_bufs &B, const float4 *colors,
                                     const float4 *target, const float4 *d_canvas, float4 *color_part) {
-    ak_composite_bwd<<<ak_pixel_blocks(S), AK_THREADS, 0, st>>>(S, B, colors, target, d_canvas, color_part);
+    ak_composite_bwd<<<ak_composite_bwd_blocks(S), AK_CB_THREADS, 0, st>>>(S, B, colors, target, d_canvas,
+                                                                           reinterpret_cast<float *>(color_part));
     return cudaGetLastError();
 }
 cudaError_t ak_launch_cover_bwd(cudaStream_t st, const ak_scene &S, const ak_bufs &B, const float *widths,

@@ -62,3 +62,4 @@ cudaError_t ak_launch_reduce(cudaStream_t st, const ak_scene &S, uint32_t nblock
 cudaError_t ak_launch_adam(cudaStream_t st, float *param, const float *grad, float *m, float *v, uint32_t n, float lr,
                            float beta1, float beta2, float eps, uint32_t step, float lo, float hi);
 uint32_t    ak_pixel_blocks(const ak_scene &S);
+uint32_t    ak_composite_bwd_blocks(const ak_scene &S); /* blocks of ak_composite_bwd's colour partials */
