@@ -60,6 +60,7 @@ def parse():
     p.add_argument("--svg-shapes", type=int, default=600, help="shapes of the SVG ingestion workload (0: skip)")
     p.add_argument("--no-batch", action="store_true", help="skip the uneven-batch comparison")
     p.add_argument("--no-analytic", action="store_true", help="skip the differentiable analytic-coverage workload")
+    p.add_argument("--no-glyphs", action="store_true", help="skip the 4096x4096 glyph workload")
     p.add_argument("--adam-steps", type=int, default=200, help="Adam steps of the differentiable workload")
     return p.parse_args()
 
@@ -320,6 +321,80 @@ def analytic_bench(a, gb, torch, np, flush, cpu):
     return out
 
 
+def glyph_bench(a, gb, L, np, flush):
+    """The large glyph scene (4096x4096, MSAA 4, seed 5): 200,000 quadratic
+    glyph outlines with holes (NON_ZERO) and 20,000 round-join strokes under
+    one linear gradient, recorded through vkvg's API (command-stream replay),
+    then timed as device-resident frames and end to end."""
+    import ctypes as C
+
+    from vkvg_gb300 import scenes
+
+    t0 = time.perf_counter()
+    g = scenes.glyph_streams(seed=5)
+    gen_s = time.perf_counter() - t0
+    cm, ar = g["cmds"], g["args"]
+    size = g["width"]
+    x0, y0, x1, y1, stops = g["gradient"]
+    dev = gb.Device(samples=4)
+    surf = gb.Surface(dev, size, size)
+    ctx = surf.context()
+
+    def record(c):
+        c.set_source_rgb(1.0, 1.0, 1.0)
+        c.paint()
+        c.set_source_linear(float(x0), float(y0), float(x1), float(y1), [tuple(float(v) for v in st) for st in stops])
+        st = L.vkvg_gb300_replay_stream(c.h, cm.ctypes.data_as(C.c_void_p), len(cm), ar.ctypes.data_as(C.c_void_p),
+                                        len(ar))
+        assert st == 0, st
+
+    record(ctx)
+    frame = L.vkvg_gb300_frame_capture(ctx.h)
+    assert frame
+    timing = np.zeros(8, np.float32)
+    for _ in range(2):
+        flush()
+        assert L.vkvg_gb300_frame_execute(frame, surf.h) == 0
+    n = 3
+    tot = np.zeros(5)
+    for _ in range(n):
+        flush()
+        assert L.vkvg_gb300_frame_execute(frame, surf.h) == 0
+        L.vkvg_gb300_frame_timing(frame, timing.ctypes.data_as(C.c_void_p))
+        tot += timing[:5]
+    ms = tot[4] / n
+    stats = np.zeros(16, np.uint64)
+    L.vkvg_gb300_frame_stats(frame, stats.ctypes.data_as(C.c_void_p))
+    img = np.zeros((size, size, 4), np.uint8)
+    ectx = surf.context()
+
+    def e2e():
+        record(ectx)
+        L.vkvg_flush(ectx.h)
+        assert L.vkvg_surface_write_to_memory(surf.h, img.ctypes.data_as(C.c_void_p)) == 0
+
+    e2e()
+    t0 = time.perf_counter()
+    for _ in range(2):
+        e2e()
+    e_ms = (time.perf_counter() - t0) / 2 * 1e3
+    paths = g["outlines"] + g["strokes"]
+    out = {"workload": "glyphs 4096x4096 msaa4 (seed 5): %d quadratic outlines with holes (NON_ZERO), %d round-join "
+                       "strokes, %d quads, one linear gradient" % (g["outlines"], g["strokes"], g["quads"]),
+           "paths_per_s": paths / (ms / 1e3), "ms_per_frame": ms, "mpx_per_s": size * size / (ms / 1e3) / 1e6,
+           "stage_ms": {"flatten": tot[0] / n, "stroke": tot[1] / n, "setup_bin": tot[2] / n, "raster": tot[3] / n},
+           "flattened_points": int(stats[1]), "stroke_vertices": int(stats[2]), "bin_units": int(stats[5]),
+           "e2e": {"ms_per_step": e_ms, "paths_per_s": paths / (e_ms / 1e3),
+                   "note": "replay of the recorded calls + vkvg_flush + write_to_memory, host timer"},
+           "scene_build_s": gen_s, "timing": "CUDA events on the library's stream, L2 flushed before each frame"}
+    L.vkvg_gb300_frame_destroy(frame)
+    ectx.destroy()
+    ctx.destroy()
+    surf.destroy()
+    dev.destroy()
+    return out
+
+
 def run_reference(a, rank):
     """CPU implementation of the path (the oracle port), all host threads."""
     if rank != 0:
@@ -544,6 +619,11 @@ def main():
     if not a.no_analytic and world == 1:
         analytic = analytic_bench(a, gb, torch, np, l2_flush, cpu=rank == 0 and not a.no_cpu)
 
+    # ---- the large glyph scene (4096x4096, 200k quadratic outlines + 20k strokes)
+    glyphs = None
+    if not a.no_glyphs and world == 1:
+        glyphs = glyph_bench(a, gb, L, np, l2_flush)
+
     # ---- roofline of the raster/composite kernel
     peak, peak_kind = hbm_peak()
     nflat, nsv = int(stats[1]), int(stats[2])
@@ -592,6 +672,8 @@ def main():
         line["svg"] = svg
     if batch:
         line["batch"] = batch
+    if glyphs:
+        line["glyphs"] = glyphs
     if analytic:
         analytic["roofline"]["peak"] = peak
         analytic["roofline"]["frac"] = analytic["roofline"]["achieved"] / peak

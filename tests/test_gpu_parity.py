@@ -410,3 +410,17 @@ def test_batch_rejects_clip_and_duplicates(gb):
     for c, f in ((ctx, fr), (ctx2, fr2)):
         L.vkvg_gb300_frame_destroy(f)
         c.destroy()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("size,n,m", [(192, 300, 30), (256, 600, 60)])
+def test_glyph_scene_bit_exact(gb, vko, size, n, m):
+    """the large glyph scene's construction on a crop: quadratic outlines with
+    holes (NON_ZERO), round-join strokes, one linear gradient source; samples
+    bit-exact against the oracle"""
+    sc = scenes.glyph_scene(n_outlines=n, n_strokes=m, size=size)
+    dev, surf, ctx = pu.run_gpu(gb, sc, debug=False)
+    osurf, octx = pu.run_oracle(vko, sc)
+    assert ctx.status() == 0
+    assert np.array_equal(surf.samples_rgba(), osurf.samples_rgba())
+    assert np.array_equal(surf.image(), osurf.image())

@@ -752,15 +752,17 @@ def batch_streams(seed=2, n_surfaces=64, max_paths=20000, min_paths=100, max_seg
 
 def decode(cmds, args):
     """command stream -> scene calls (the inverse of encode for the codes
-    batch_streams emits)"""
+    batch_streams and glyph_streams emit)"""
     names = {v: k for k, v in CMD.items()}
-    nargs = {"move_to": 2, "line_to": 2, "curve_to": 6, "arc": 5, "close_path": 0, "set_source_rgb": 3,
-             "set_source_rgba": 4, "paint": 0, "fill": 0, "fill_preserve": 0, "stroke": 0, "set_line_width": 1}
+    nargs = {"move_to": 2, "line_to": 2, "curve_to": 6, "quadratic_to": 4, "arc": 5, "close_path": 0,
+             "set_source_rgb": 3, "set_source_rgba": 4, "paint": 0, "fill": 0, "fill_preserve": 0, "stroke": 0,
+             "set_line_width": 1, "set_line_join": 1, "set_fill_rule": 1}
     ops, a = [], 0
+    ints = ("set_line_join", "set_fill_rule")
     for c in cmds:
         name = names[int(c)]
         n = nargs[name]
-        ops.append((name,) + tuple(float(v) for v in args[a:a + n]))
+        ops.append((name,) + tuple(int(v) if name in ints else float(v) for v in args[a:a + n]))
         a += n
     return ops
 
@@ -800,3 +802,162 @@ def analytic_scene(seed=3, n_paths=128, n_cubics=8, size=256, w_min=0.5, w_max=4
         "seg_kind": np.full(n_paths * n_cubics, AN_CUBIC, np.uint8),
     }
     return scene, {"ctrl": ctrl, "colors": colors, "widths": widths}
+
+
+def glyph_streams(seed=5, n_outlines=200000, n_strokes=20000, size=4096, size_min=8.0, size_max=48.0):
+    """The large glyph scene as a command stream: a size x size surface, MSAA
+    4, which the caller paints white and then sets the gradient source on
+    before replaying the stream; n_outlines glyph-like closed outlines of quadratic
+    Beziers - outline size U[size_min, size_max) px, 1-3 contours, 6-40 quads
+    per contour; the first contour runs counter-clockwise on screen and the
+    others (holes, inside it) clockwise - filled NON_ZERO; then n_strokes
+    open strokes of 3-8 quads, width U[1,3), round joins.  Every draw uses
+    one linear gradient between two random RGBA stops along a random axis,
+    which the caller sets as the source before replaying ("gradient": x0,
+    y0, x1, y1 and two (offset, r, g, b, a) stops).  Random values are
+    splitmix64 outputs (np_rnd), drawn in blocks so that the scene builds in
+    seconds.  Returns cmds, args, the gradient and the counts."""
+    import numpy as np
+
+    C = CMD
+    pos = [0]
+
+    def take(n):
+        v = np_rnd(seed, pos[0], n)
+        pos[0] += n
+        return v
+
+    g = take(12)
+    grad = (g[0] * size, g[1] * size, g[2] * size, g[3] * size,
+            [(0.0, g[4], g[5], g[6], 0.5 + 0.5 * g[7]), (1.0, g[8], g[9], g[10], 0.5 + 0.5 * g[11])])
+    # per outline: centre, size, contour count; per contour: quad count
+    o = take(4 * n_outlines).reshape(n_outlines, 4)
+    cx, cy = o[:, 0] * size, o[:, 1] * size
+    osz = size_min + (size_max - size_min) * o[:, 2]
+    ncont = 1 + np.minimum((o[:, 3] * 3).astype(np.int64), 2)
+    nc = int(ncont.sum())
+    cont_out = np.repeat(np.arange(n_outlines), ncont)
+    first = np.zeros(nc, bool)
+    first[np.concatenate([[0], np.cumsum(ncont)[:-1]])] = True
+    c = take(4 * nc).reshape(nc, 4)
+    nq = 6 + np.minimum((c[:, 0] * 35).astype(np.int64), 34)
+    # contour frame: outer contours span the outline, holes a fifth to two
+    # fifths of it, placed inside it
+    half = osz[cont_out] / 2
+    rad = np.where(first, half, half * (0.2 + 0.2 * c[:, 1]))
+    off = np.where(first, 0.0, half * 0.35)
+    ang = c[:, 2] * 2 * np.pi
+    ccx = cx[cont_out] + off * np.cos(ang)
+    ccy = cy[cont_out] + off * np.sin(ang)
+    sgn = np.where(first, -1.0, 1.0)  # y down: decreasing screen angle is counter-clockwise
+    nqt = int(nq.sum())
+    qc = np.repeat(np.arange(nc), nq)
+    k = np.arange(nqt) - np.repeat(np.cumsum(nq) - nq, nq)
+    q = take(3 * nqt).reshape(nqt, 3)
+    th = (k + 0.3 * (q[:, 0] - 0.5)) * (2 * np.pi / nq[qc])
+    th_c = (k + 0.5) * (2 * np.pi / nq[qc])
+    r_on = rad[qc] * (0.7 + 0.3 * q[:, 1])
+    r_off = rad[qc] * (0.7 + 0.45 * q[:, 2])
+    px = ccx[qc] + r_on * np.cos(sgn[qc] * th)
+    py = ccy[qc] + r_on * np.sin(sgn[qc] * th)
+    ox = ccx[qc] + r_off * np.cos(sgn[qc] * th_c)
+    oy = ccy[qc] + r_off * np.sin(sgn[qc] * th_c)
+    # stream: per contour move_to(p0), quads to p1 .. p_{n-1}, p0, close_path;
+    # per outline one fill after its contours
+    nxt = np.arange(nqt) + 1
+    last = np.cumsum(nq) - 1
+    nxt[last] = last - nq + 1
+    cmd_list, arg_list = [], []
+    head = [(C["set_fill_rule"], [0.0])]
+    for cm, a in head:
+        cmd_list.append(np.array([cm], np.uint32))
+        arg_list.append(np.array(a, np.float32))
+    # cmds per contour: move_to, nq quads, close_path; fill after the last contour of an outline
+    ncmd = nq + 2 + np.where(np.r_[first[1:], True], 1, 0)
+    cbase = np.concatenate([[0], np.cumsum(ncmd)[:-1]])
+    cm = np.empty(int(ncmd.sum()), np.uint32)
+    cm[cbase] = C["move_to"]
+    qi = np.repeat(cbase + 1, nq) + k
+    cm[qi] = C["quadratic_to"]
+    cm[cbase + 1 + nq] = C["close_path"]
+    has_fill = np.r_[first[1:], True]
+    cm[(cbase + 2 + nq)[has_fill]] = C["fill"]
+    nargs = np.zeros(len(cm), np.int64)
+    nargs[cbase] = 2
+    nargs[qi] = 4
+    abase = np.concatenate([[0], np.cumsum(nargs)[:-1]])
+    ar = np.empty(int(nargs.sum()), np.float32)
+    s0 = np.repeat(np.cumsum(nq) - nq, 1)
+    ar[abase[cbase]] = px[s0]
+    ar[abase[cbase] + 1] = py[s0]
+    ar[abase[qi]] = ox
+    ar[abase[qi] + 1] = oy
+    ar[abase[qi] + 2] = px[nxt]
+    ar[abase[qi] + 3] = py[nxt]
+    cmd_list.append(cm)
+    arg_list.append(ar)
+    # strokes: open chains of 3-8 quads, width U[1,3), round joins
+    if n_strokes:
+        st = take(5 * n_strokes).reshape(n_strokes, 5)
+        ns = 3 + np.minimum((st[:, 0] * 6).astype(np.int64), 5)
+        nst = int(ns.sum())
+        sk = np.arange(nst) - np.repeat(np.cumsum(ns) - ns, ns)
+        si = np.repeat(np.arange(n_strokes), ns)
+        w = take(4 * nst).reshape(nst, 4)
+        step = 6.0 + 12.0 * st[:, 3]
+        hd = st[:, 4] * 2 * np.pi
+        sx0, sy0 = st[:, 1] * size, st[:, 2] * size
+        hh = hd[si] + np.cumsum(0.8 * (w[:, 0] - 0.5))
+        ex = sx0[si] + np.cumsum(step[si] * np.cos(hh))
+        ey = sy0[si] + np.cumsum(step[si] * np.sin(hh))
+        # restart the running sums at every stroke
+        b0 = np.cumsum(ns) - ns
+        ex = ex - np.repeat(ex[b0] - sx0 - step * np.cos(hh[b0]), ns)
+        ey = ey - np.repeat(ey[b0] - sy0 - step * np.sin(hh[b0]), ns)
+        prx = np.where(sk == 0, np.repeat(sx0, ns), np.roll(ex, 1))
+        pry = np.where(sk == 0, np.repeat(sy0, ns), np.roll(ey, 1))
+        qx = 0.5 * (prx + ex) + 0.4 * step[si] * (w[:, 1] - 0.5)
+        qy = 0.5 * (pry + ey) + 0.4 * step[si] * (w[:, 2] - 0.5)
+        width = 1.0 + 2.0 * w[b0, 3]
+        per = ns + 4  # set_line_width, set_line_join, move_to, quads, stroke
+        sb = np.concatenate([[0], np.cumsum(per)[:-1]])
+        scm = np.empty(int(per.sum()), np.uint32)
+        scm[sb] = C["set_line_width"]
+        scm[sb + 1] = C["set_line_join"]
+        scm[sb + 2] = C["move_to"]
+        sq = np.repeat(sb + 3, ns) + sk
+        scm[sq] = C["quadratic_to"]
+        scm[sb + 3 + ns] = C["stroke"]
+        sna = np.zeros(len(scm), np.int64)
+        sna[sb] = 1
+        sna[sb + 1] = 1
+        sna[sb + 2] = 2
+        sna[sq] = 4
+        sab = np.concatenate([[0], np.cumsum(sna)[:-1]])
+        sar = np.empty(int(sna.sum()), np.float32)
+        sar[sab[sb]] = width
+        sar[sab[sb + 1]] = 1.0  # VKVG_LINE_JOIN_ROUND
+        sar[sab[sb + 2]] = sx0
+        sar[sab[sb + 2] + 1] = sy0
+        sar[sab[sq]] = qx
+        sar[sab[sq] + 1] = qy
+        sar[sab[sq] + 2] = ex
+        sar[sab[sq] + 3] = ey
+        cmd_list.append(scm)
+        arg_list.append(sar)
+    return {"width": size, "height": size, "samples": 4, "cmds": np.concatenate(cmd_list),
+            "args": np.concatenate(arg_list), "gradient": grad, "outlines": n_outlines, "strokes": n_strokes,
+            "contours": nc, "quads": nqt + (int(ns.sum()) if n_strokes else 0)}
+
+
+def glyph_scene(**kw):
+    """glyph_streams as a scene of calls: white paint, the gradient source,
+    then the stream's calls"""
+    s = glyph_streams(**kw)
+    x0, y0, x1, y1, stops = s["gradient"]
+    ops = [("set_source_rgb", 1.0, 1.0, 1.0), ("paint",),
+           ("set_source_linear", float(x0), float(y0), float(x1), float(y1),
+            [tuple(float(v) for v in st) for st in stops])]
+    ops += decode(s["cmds"], s["args"])
+    return {"name": "glyphs", "width": s["width"], "height": s["height"], "samples": 4, "ops": ops,
+            "paths": s["outlines"] + s["strokes"]}
