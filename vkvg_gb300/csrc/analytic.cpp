@@ -29,7 +29,7 @@ struct _vkvg_gb300_analytic_t {
     DevBuf d_seg_kind, d_seg_cp, d_seg_end, d_seg_contour, d_cont_s0, d_path_s0, d_layer_path, d_layer_stroke;
     ak_scene S{};
     /* per evaluation */
-    DevBuf    d_cnt, d_off, d_scan, d_pts, d_pt_cont, d_area, d_ckpt, d_canvas, d_loss_part, d_loss, d_color_part,
+    DevBuf    d_cnt, d_off, d_scan, d_pts, d_pt_nb, d_area, d_ckpt, d_canvas, d_loss_part, d_loss, d_color_part,
               d_gpts, d_status;
     PinnedBuf h_mon; /* [0] status word, [1] point total of the last forward */
     cudaEvent_t ev_mon = nullptr;
@@ -66,7 +66,7 @@ bool size_points(VkvgAnalytic a, uint32_t need) {
     if (need <= a->cap)
         return true;
     uint32_t cap = std::max<uint32_t>(need + need / 4, 1024);
-    if (!a->d_pts.grow((size_t)cap * sizeof(float2)) || !a->d_pt_cont.grow((size_t)cap * 4) ||
+    if (!a->d_pts.grow((size_t)cap * sizeof(float2)) || !a->d_pt_nb.grow((size_t)cap * 8) ||
         !a->d_gpts.grow((size_t)cap * sizeof(float2)))
         return false;
     a->cap = cap;
@@ -77,7 +77,7 @@ ak_bufs bufs(VkvgAnalytic a) {
     ak_bufs B;
     B.off     = a->d_off.as<uint32_t>();
     B.pts     = a->d_pts.as<float2>();
-    B.pt_cont = a->d_pt_cont.as<uint32_t>();
+    B.pt_nb   = a->d_pt_nb.as<uint2>();
     B.cap     = a->cap;
     B.area    = a->d_area.as<float>();
     B.ckpt    = a->d_ckpt.as<float4>();
@@ -179,7 +179,8 @@ VkvgAnalytic vkvg_gb300_analytic_create(uint32_t width, uint32_t height, const f
     ak_scene &S    = a->S;
     S.W = width, S.H = height, S.npaths = npaths, S.ncontours = ncontours, S.nseg = nseg, S.ncp = cp;
     S.nlayers      = a->nlayers;
-    S.nbands       = (height + AK_BAND - 1) / AK_BAND;
+    S.band         = ak_band_rows(width);
+    S.nbands       = (height + S.band - 1) / S.band;
     S.bg           = make_float4(a->bg[0], a->bg[1], a->bg[2], a->bg[3]);
     S.seg_kind     = a->d_seg_kind.as<uint8_t>();
     S.seg_cp       = a->d_seg_cp.as<uint32_t>();
@@ -199,7 +200,7 @@ void vkvg_gb300_analytic_destroy(VkvgAnalytic a) {
         cudaStreamSynchronize(a->stream);
     DevBuf *bs[] = {&a->d_seg_kind, &a->d_seg_cp,  &a->d_seg_end, &a->d_seg_contour, &a->d_cont_s0,
                     &a->d_path_s0,  &a->d_layer_path, &a->d_layer_stroke, &a->d_cnt, &a->d_off, &a->d_scan,
-                    &a->d_pts, &a->d_pt_cont, &a->d_area, &a->d_ckpt, &a->d_canvas, &a->d_loss_part, &a->d_loss,
+                    &a->d_pts, &a->d_pt_nb, &a->d_area, &a->d_ckpt, &a->d_canvas, &a->d_loss_part, &a->d_loss,
                     &a->d_color_part, &a->d_gpts, &a->d_status};
     for (DevBuf *b : bs)
         b->release();
@@ -258,7 +259,7 @@ vkvg_status_t vkvg_gb300_analytic_forward(VkvgAnalytic a, const float *ctrl, con
         a->sized = true;
     }
     ak_bufs B = bufs(a);
-    e         = ak_launch_flat_emit(st, a->S, c2, B.off, a->d_pts.as<float2>(), a->d_pt_cont.as<uint32_t>(), a->cap,
+    e         = ak_launch_flat_emit(st, a->S, c2, B.off, a->d_pts.as<float2>(), a->d_pt_nb.as<uint2>(), a->cap,
                                     B.status);
     if (a->timing)
         cudaEventRecord(a->ev[1], st);

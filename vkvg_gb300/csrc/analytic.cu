@@ -2,7 +2,7 @@
  * K7/K8 - analytic area coverage, compositing and their adjoints, sm_103a.
  *
  * Forward (K7):
- *   ak_cover      grid (bands of AK_BAND rows) x (layers).  Every thread takes
+ *   ak_cover      grid (bands of 16 or 32 rows) x (layers).  Every thread takes
  *                 flattened points of the layer's path and builds the
  *                 polygons of that point - the fill edge to the next point,
  *                 or the stroke's rectangle of the segment to the next point
@@ -279,12 +279,10 @@ __device__ __forceinline__ bool pieces_in_band(const ak_band &bd, float2 pp, flo
 }
 
 /* the point's neighbours in its contour */
-__device__ __forceinline__ void neighbours(const ak_scene &S, const ak_bufs &B, uint32_t k, uint32_t &kp,
+__device__ __forceinline__ void neighbours(const ak_scene &, const ak_bufs &B, uint32_t k, uint32_t &kp,
                                            uint32_t &kn) {
-    uint32_t c  = B.pt_cont[k];
-    uint32_t c0 = B.off[S.cont_s0[c]], c1 = B.off[S.cont_s0[c + 1]];
-    kn          = k + 1 == c1 ? c0 : k + 1;
-    kp          = k == c0 ? c1 - 1 : k - 1;
+    const uint2 nb = B.pt_nb[k];
+    kp = nb.x, kn = nb.y;
 }
 
 /* ------------------------------------------------- band work compaction */
@@ -367,8 +365,8 @@ __global__ void __launch_bounds__(AK_THREADS) ak_cover(ak_scene S, ak_bufs B, co
     int     *acc   = reinterpret_cast<int *>(slots + AK_THREADS);
     __shared__ int nslot;
     uint32_t l = blockIdx.y;
-    ak_band  bd{(int)(blockIdx.x * AK_BAND), 0, (int)S.W, B.status};
-    bd.y1    = min((int)S.H, bd.y0 + AK_BAND);
+    ak_band  bd{(int)(blockIdx.x * S.band), 0, (int)S.W, B.status};
+    bd.y1    = min((int)S.H, bd.y0 + (int)S.band);
     int rows = bd.y1 - bd.y0, W1 = S.W + 1;
     for (int i = threadIdx.x; i < rows * W1; i += AK_THREADS)
         acc[i] = 0;
@@ -516,6 +514,7 @@ __global__ void __launch_bounds__(AK_CB_THREADS)
                      const float4 *__restrict__ d_canvas, float *__restrict__ color_part) {
     __shared__ float4 col[AK_CHUNK];
     __shared__ float4 sB[AK_CHUNK][AK_CB_THREADS]; /* colour under each layer of the chunk */
+    __shared__ float  sA[AK_CHUNK][AK_CB_THREADS]; /* the chunk's areas */
     __shared__ float  red[AK_CB_THREADS / 32][AK_CHUNK * 4];
     size_t            np = (size_t)S.W * S.H, px = (size_t)blockIdx.x * AK_CB_THREADS + threadIdx.x;
     bool              valid = px < np;
@@ -538,16 +537,20 @@ __global__ void __launch_bounds__(AK_CB_THREADS)
         if (threadIdx.x < n)
             col[threadIdx.x] = colors[S.layer_path[lb + threadIdx.x]];
         __syncthreads();
-        float  A[AK_CHUNK];
-        float4 Bc = valid ? B.ckpt[(size_t)ch * np + px] : make_float4(0.f, 0.f, 0.f, 0.f);
+        float4       Bc = valid ? B.ckpt[(size_t)ch * np + px] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float *ap = B.area + (size_t)lb * np + px;
+        {
+            float A[AK_CHUNK];
 #pragma unroll
-        for (int q = 0; q < AK_CHUNK; q++)
-            A[q] = (valid && q < (int)n) ? B.area[(size_t)(lb + q) * np + px] : 0.f;
+            for (int q = 0; q < AK_CHUNK; q++)
+                A[q] = (valid && q < (int)n) ? ap[(size_t)q * np] : 0.f;
 #pragma unroll
-        for (int q = 0; q < AK_CHUNK; q++) {
-            sB[q][threadIdx.x] = Bc;
-            if (q < (int)n)
-                Bc = blend(cover(A[q]), col[q], Bc);
+            for (int q = 0; q < AK_CHUNK; q++) {
+                sB[q][threadIdx.x] = Bc;
+                sA[q][threadIdx.x] = A[q];
+                if (q < (int)n)
+                    Bc = blend(cover(A[q]), col[q], Bc);
+            }
         }
         /* two halves of 8 layers, top half first; colour partials per half */
 #pragma unroll
@@ -560,11 +563,12 @@ __global__ void __launch_bounds__(AK_CB_THREADS)
                 if (q >= (int)n)
                     continue;
                 float4 c  = col[q], Bq = sB[q][threadIdx.x];
-                float  al = cover(A[q]);
+                float  Aq = sA[q][threadIdx.x];
+                float  al = cover(Aq);
                 float  gB = g.x * Bq.x + g.y * Bq.y + g.z * Bq.z + g.w * Bq.w;
                 float  gc = g.x * c.x + g.y * c.y + g.z * c.z + g.w * c.w;
                 float  da = T * (gc - c.w * gB);
-                float  gA = fabsf(A[q]) < 1.f ? (A[q] > 0.f ? da : A[q] < 0.f ? -da : 0.f) : 0.f;
+                float  gA = fabsf(Aq) < 1.f ? (Aq > 0.f ? da : Aq < 0.f ? -da : 0.f) : 0.f;
                 if (valid)
                     B.area[(size_t)(lb + q) * np + px] = gA;
                 float ta = T * al;
@@ -601,8 +605,8 @@ __global__ void __launch_bounds__(AK_THREADS)
     __shared__ float red[AK_THREADS / 32];
     __shared__ int   nslot;
     uint32_t         l = blockIdx.y;
-    ak_band          bd{(int)(blockIdx.x * AK_BAND), 0, (int)S.W, B.status};
-    bd.y1             = min((int)S.H, bd.y0 + AK_BAND);
+    ak_band          bd{(int)(blockIdx.x * S.band), 0, (int)S.W, B.status};
+    bd.y1             = min((int)S.H, bd.y0 + (int)S.band);
     int          rows = bd.y1 - bd.y0;
     const float *src  = B.area + ((size_t)l * S.H + bd.y0) * S.W;
     for (int i = threadIdx.x; i < rows * (int)S.W; i += AK_THREADS)
@@ -724,14 +728,21 @@ __global__ void ak_adam(float *__restrict__ p, const float *__restrict__ g, floa
 /* ------------------------------------------------------------ launchers */
 
 uint32_t ak_pixel_blocks(const ak_scene &S) { return (uint32_t)(((size_t)S.W * S.H + AK_THREADS - 1) / AK_THREADS); }
-size_t   ak_cover_smem(uint32_t W) {
-    size_t fwd = sizeof(ak_slot) * AK_THREADS + sizeof(int) * AK_BAND * (W + 1);
-    size_t bwd = sizeof(ak_slot) * AK_THREADS + sizeof(float4) * AK_THREADS * 7 + sizeof(float) * AK_BAND * W;
+uint32_t ak_band_rows(uint32_t W) { return W <= AK_BAND_WIDE_MAX ? 32u : 16u; }
+static size_t cover_fwd_smem(uint32_t W, uint32_t band) {
+    return sizeof(ak_slot) * AK_THREADS + sizeof(int) * band * (W + 1);
+}
+static size_t cover_bwd_smem(uint32_t W, uint32_t band) {
+    return sizeof(ak_slot) * AK_THREADS + sizeof(float4) * AK_THREADS * 7 + sizeof(float) * band * W;
+}
+size_t ak_cover_smem(uint32_t W) {
+    uint32_t band = ak_band_rows(W);
+    size_t   fwd = cover_fwd_smem(W, band), bwd = cover_bwd_smem(W, band);
     return fwd > bwd ? fwd : bwd;
 }
 
 cudaError_t ak_launch_cover(cudaStream_t st, const ak_scene &S, const ak_bufs &B, const float *widths) {
-    size_t smem = sizeof(ak_slot) * AK_THREADS + sizeof(int) * AK_BAND * (S.W + 1);
+    size_t smem = cover_fwd_smem(S.W, S.band);
     if (smem > 48 * 1024)
         cudaFuncSetAttribute(ak_cover, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (S.nlayers)
@@ -754,7 +765,7 @@ cudaError_t ak_launch_composite_bwd(cudaStream_t st, const ak_scene &S, const ak
 }
 cudaError_t ak_launch_cover_bwd(cudaStream_t st, const ak_scene &S, const ak_bufs &B, const float *widths,
                                 float2 *gpts, float *gwidth) {
-    size_t smem = sizeof(ak_slot) * AK_THREADS + sizeof(float4) * AK_THREADS * 7 + sizeof(float) * AK_BAND * S.W;
+    size_t smem = cover_bwd_smem(S.W, S.band);
     if (smem > 48 * 1024)
         cudaFuncSetAttribute(ak_cover_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (S.nlayers)

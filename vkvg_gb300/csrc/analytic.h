@@ -15,11 +15,13 @@
 #define AK_ERR_POINTS 1u /* flattened points exceeded the point buffer */
 #define AK_ERR_WALK   2u /* an edge walk hit its iteration bound */
 
-#define AK_BAND  16 /* pixel rows per coverage block */
+/* pixel rows per coverage block: 32 where a band of 32 rows fits the blocks'
+   shared memory (canvases up to AK_BAND_WIDE_MAX wide), else 16 */
+#define AK_BAND_WIDE_MAX 1024
 #define AK_CHUNK 16 /* layers per compositing checkpoint */
 
 struct ak_scene {
-    uint32_t        W, H, npaths, ncontours, nseg, ncp, nlayers, nbands;
+    uint32_t        W, H, npaths, ncontours, nseg, ncp, nlayers, nbands, band;
     float4          bg;
     const uint8_t  *seg_kind;     /* nseg */
     const uint32_t *seg_cp;       /* nseg: first control point */
@@ -35,7 +37,7 @@ struct ak_scene {
 struct ak_bufs {
     const uint32_t *off;     /* nseg+1 point offsets of the segments */
     const float2   *pts;     /* flattened points */
-    const uint32_t *pt_cont; /* contour of each point */
+    const uint2    *pt_nb;   /* each point's previous and next point in its contour */
     uint32_t        cap;     /* capacity of pts */
     float          *area;    /* nlayers * W * H: signed areas, then their gradients */
     float4         *ckpt;    /* ceil(nlayers / AK_CHUNK) * W * H: colour under every chunk */
@@ -45,10 +47,11 @@ struct ak_bufs {
 
 cudaError_t ak_launch_flat_count(cudaStream_t st, const ak_scene &S, const float2 *ctrl, uint32_t *cnt);
 cudaError_t ak_launch_flat_emit(cudaStream_t st, const ak_scene &S, const float2 *ctrl, const uint32_t *off,
-                                float2 *pts, uint32_t *pt_cont, uint32_t cap, uint32_t *status);
+                                float2 *pts, uint2 *pt_nb, uint32_t cap, uint32_t *status);
 cudaError_t ak_launch_flat_bwd(cudaStream_t st, const ak_scene &S, const float2 *ctrl, const uint32_t *off,
                                uint32_t cap, const float2 *gpts, float2 *gctrl);
 
+uint32_t    ak_band_rows(uint32_t W);
 size_t      ak_cover_smem(uint32_t W);
 cudaError_t ak_launch_cover(cudaStream_t st, const ak_scene &S, const ak_bufs &B, const float *widths);
 cudaError_t ak_launch_composite(cudaStream_t st, const ak_scene &S, const ak_bufs &B, const float4 *colors,

@@ -38,15 +38,19 @@ struct ak_cnt_emit {
             n++;
     }
 };
+/* a point's neighbours in its closed contour [c0, c1) */
+__device__ __forceinline__ uint2 ak_nb(uint32_t o, uint32_t c0, uint32_t c1) {
+    return make_uint2(o == c0 ? c1 - 1 : o - 1, o + 1 == c1 ? c0 : o + 1);
+}
 struct ak_pt_emit {
     float2   *pts;
-    uint32_t *pc;
-    uint32_t  o, cont;
+    uint2    *nb;
+    uint32_t  o, c0, c1;
     __device__ void operator()(float x, float y, int, float, float) {
         if (x != x || y != y)
             return;
         pts[o] = make_float2(x, y);
-        pc[o]  = cont;
+        nb[o]  = ak_nb(o, c0, c1);
         o++;
     }
 };
@@ -109,7 +113,7 @@ __global__ void __launch_bounds__(32 * AK_FW) ak_flat_count(ak_scene S, const fl
 
 __global__ void __launch_bounds__(32 * AK_FW) ak_flat_emit(ak_scene S, const float2 *__restrict__ ctrl,
                                                           const uint32_t *__restrict__ off, float2 *__restrict__ pts,
-                                                          uint32_t *__restrict__ pt_cont, uint32_t cap,
+                                                          uint2 *__restrict__ pt_nb, uint32_t cap,
                                                           uint32_t *__restrict__ status) {
     __shared__ gb_bw_smem sm[AK_FW];
     uint32_t              w = threadIdx.x >> 5, lane = threadIdx.x & 31, s = blockIdx.x * AK_FW + w;
@@ -120,18 +124,20 @@ __global__ void __launch_bounds__(32 * AK_FW) ak_flat_emit(ak_scene S, const flo
     }
     if (s >= S.nseg)
         return;
-    float2   p, c[4];
-    uint32_t o = off[s], cont = S.seg_contour[s];
+    float2         p, c[4];
+    const uint32_t cont = S.seg_contour[s];
+    const uint32_t c0 = off[S.cont_s0[cont]], c1 = off[S.cont_s0[cont + 1]];
+    uint32_t       o  = off[s];
     if (seg_start(S, ctrl, s, p)) {
         if (lane == 0)
-            pts[o] = p, pt_cont[o] = cont;
+            pts[o] = p, pt_nb[o] = ak_nb(o, c0, c1);
         o++;
     }
     if (S.seg_kind[s] == AK_SEG_CUBIC && ak_cubic_cp(S, ctrl, s, c)) {
         int m = gb_bezier_warp(AK_TOL, c[0].x, c[0].y, c[1].x, c[1].y, c[2].x, c[2].y, c[3].x, c[3].y, sm[w]);
         if (m < 0) {
             if (lane == 0) {
-                ak_pt_emit e{pts, pt_cont, o, cont};
+                ak_pt_emit e{pts, pt_nb, o, c0, c1};
                 gb_bezier_walk<false>(AK_TOL, c[0].x, c[0].y, c[1].x, c[1].y, c[2].x, c[2].y, c[3].x, c[3].y, e);
             }
             return;
@@ -139,7 +145,7 @@ __global__ void __launch_bounds__(32 * AK_FW) ak_flat_emit(ak_scene S, const flo
         for (int i = (int)lane; i < m; i += 32) {
             int r        = gb_bw_rank(sm[w], m, i);
             pts[o + r]   = sm[w].pt[i].p;
-            pt_cont[o + r] = cont;
+            pt_nb[o + r] = ak_nb(o + r, c0, c1);
         }
     }
 }
@@ -212,8 +218,8 @@ cudaError_t ak_launch_flat_count(cudaStream_t st, const ak_scene &S, const float
     return cudaGetLastError();
 }
 cudaError_t ak_launch_flat_emit(cudaStream_t st, const ak_scene &S, const float2 *ctrl, const uint32_t *off,
-                                float2 *pts, uint32_t *pt_cont, uint32_t cap, uint32_t *status) {
-    ak_flat_emit<<<(S.nseg + AK_FW - 1) / AK_FW + 1, 32 * AK_FW, 0, st>>>(S, ctrl, off, pts, pt_cont, cap, status);
+                                float2 *pts, uint2 *pt_nb, uint32_t cap, uint32_t *status) {
+    ak_flat_emit<<<(S.nseg + AK_FW - 1) / AK_FW + 1, 32 * AK_FW, 0, st>>>(S, ctrl, off, pts, pt_nb, cap, status);
     return cudaGetLastError();
 }
 cudaError_t ak_launch_flat_bwd(cudaStream_t st, const ak_scene &S, const float2 *ctrl, const uint32_t *off,
