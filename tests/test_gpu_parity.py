@@ -168,6 +168,41 @@ def test_ragged_and_wide_surfaces_bit_exact(gb, vko, w, h, samples):
     assert np.array_equal(surf.image(), osurf.image())
 
 
+def test_wide_surface_small_shapes_bit_exact(gb, vko):
+    """a surface three raster tiles wide with shapes that lie inside one tile,
+    straddle a tile boundary, or cover a whole tile with edges only outside
+    it (left of the surface and right of the tile): the raster passes over
+    the draws whose edges all lie left or all right of a tile"""
+    w, h = 3000, 40
+    r = scenes.SplitMix64(91)
+    ops = [("set_source_rgb", 1.0, 1.0, 1.0), ("paint",),
+           ("rectangle", -50.0, 4.0, 2950.0, 10.0), ("set_source_rgba", 0.2, 0.6, 0.3, 0.7), ("fill",),
+           ("move_to", 900.0, 20.0), ("line_to", 2200.0, 22.0), ("line_to", 2150.0, 36.0), ("line_to", 950.0, 33.0),
+           ("close_path",), ("set_source_rgba", 0.7, 0.2, 0.5, 0.6), ("fill_preserve",),
+           ("set_line_width", 3.0), ("set_source_rgba", 0.1, 0.1, 0.1, 0.9), ("stroke",)]
+    centres = [1024.0, 2048.0, 3.0, 2996.0] + [r.rnd() * w for _ in range(40)]
+    for i, cx in enumerate(centres):
+        cy = r.rnd() * h
+        rad = 2.0 + 14.0 * r.rnd()
+        ops.append(("move_to", cx + rad, cy))
+        for k in range(1, 7):
+            a = k * 2.0 * np.pi / 7
+            ops.append(("line_to", cx + rad * np.cos(a) * (0.6 + 0.4 * r.rnd()), cy + rad * np.sin(a)))
+        ops.append(("close_path",))
+        ops += [("set_fill_rule", i % 2), ("set_source_rgba", r.rnd(), r.rnd(), r.rnd(), 0.4 + 0.6 * r.rnd()),
+                ("fill_preserve",), ("set_line_width", 1 + 4 * r.rnd()), ("set_line_join", i % 3),
+                ("set_line_cap", i % 3), ("set_dash", [5.0, 3.0] if i % 4 == 0 else [], 0.0),
+                ("set_source_rgba", r.rnd(), r.rnd(), r.rnd(), 0.5 + 0.5 * r.rnd()), ("stroke",)]
+    sc = {"name": "wide_small", "width": w, "height": h, "samples": 4, "ops": ops, "paths": len(centres) + 2}
+    dev, surf, ctx = pu.run_gpu(gb, sc)
+    osurf, octx = pu.run_oracle(vko, sc)
+    assert ctx.debug_counts()[5] == 0
+    errs = pu.compare_geometry(ctx, octx)
+    assert not errs, errs[:10]
+    assert np.array_equal(surf.samples_rgba(), osurf.samples_rgba())
+    assert np.array_equal(surf.image(), osurf.image())
+
+
 def test_empty_and_degenerate_paths(gb, vko):
     """fills and strokes of empty, single-point, zero-length and NaN paths
     draw nothing and leave no error; a degenerate-only frame still resolves"""

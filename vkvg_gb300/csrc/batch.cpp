@@ -53,6 +53,7 @@ struct _vkvg_gb300_batch_t {
     PinnedBuf            h_stage;
     std::vector<uint4>   items_cost, items_plain; /* the work list in both orders */
     uint64_t             ncells  = 0;
+    uint64_t             every   = 0; /* cells of the draws that act on every band */
     uint32_t             samples = 0;
     uint32_t             nctas   = 1; /* persistent raster CTAs: one per SM */
     int                  runs    = 0; /* executions so far */
@@ -205,7 +206,10 @@ cudaError_t build_items(VkvgBatch b) {
    unless sized), the batch raster with settings p, the status read back */
 cudaError_t run_batch(VkvgBatch b, bool sized, const RasterParams &p) {
     Pipeline &pl = b->pl;
-    BCK(pl.geometry(b->merged, b->d_tab.as<gb_surf>(), b->ncells, b->samples, false, sized));
+    bool wide = false;
+    for (const gb_surf &s : b->tab)
+        wide |= s.W > GB_RASTER_TILE_W;
+    BCK(pl.geometry(b->merged, b->d_tab.as<gb_surf>(), b->ncells, b->every, wide, b->samples, false, sized));
     if (!sized)
         BCK(build_items(b));
     const uint32_t ni = (uint32_t)b->items_plain.size();
@@ -214,6 +218,9 @@ cudaError_t run_batch(VkvgBatch b, bool sized, const RasterParams &p) {
     A0.S         = b->samples;
     A0.draws     = (const gb_draw *)((const uint8_t *)pl.in.p + pl.o_draws);
     A0.cell_off  = pl.cells.as<uint32_t>();
+    A0.apos      = pl.apos.as<uint32_t>();
+    A0.alist     = pl.alist.as<uint32_t>();
+    A0.dbox      = pl.dbox.as<int2>();
     A0.recs      = pl.recs.as<int4>();
     A0.nunits    = pl.nunits;
     A0.status    = pl.status.as<uint32_t>();
@@ -265,6 +272,8 @@ VkvgBatch vkvg_gb300_batch_create(VkvgFrame *frames, VkvgSurface *targets, uint3
         e.rgba    = s->d_rgba;
         first_draw_init(b->merged.draws.data() + d0, e.ndraws, e);
         b->ncells += (uint64_t)e.nbands * e.ndraws;
+        for (uint32_t j = d0; j < d0 + e.ndraws; j++)
+            b->every += b->merged.draws[j].kind > GB_DRAW_STROKE ? e.nbands : 0u;
         b->tab.push_back(e);
         b->targets.emplace_back(s);
     }

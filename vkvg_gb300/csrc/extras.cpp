@@ -150,6 +150,10 @@ vkvg_status_t vkvg_gb300_debug_coverage(VkvgContext ctx, uint32_t i, int32_t *ou
     A.ndraws   = p.ndraw;
     A.draws    = (const gb_draw *)((const uint8_t *)p.in.p + p.o_draws);
     A.cell_off = p.cells.as<uint32_t>();
+    A.apos     = p.apos.as<uint32_t>();
+    A.alist    = p.alist.as<uint32_t>();
+    A.dbox     = p.dbox.as<int2>();
+    A.cell0    = 0;
     A.recs     = p.recs.as<int4>();
     A.nunits   = p.nunits;
     A.status   = p.status.as<uint32_t>();

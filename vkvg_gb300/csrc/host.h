@@ -88,6 +88,8 @@ struct Pipeline {
     DevBuf       fe_cnt, fe_off, edges, edge_draw;
     DevBuf       sdraw_tri0, sdraw_vbase, tri_a, tri_b, tri_draw;
     DevBuf       cells, cursor, recs, status, dbg;
+    DevBuf       dbox;        /* per draw: x extent of its binned edges (min x, -max x) */
+    DevBuf       apos, alist; /* the raster's per-band draw lists: cell -> list position, active cells */
     DevBuf       dseglen, dseg, dfin;
     DevBuf       tri_idx; /* oriented vertex indices of stroke triangles (edge cancellation) */
     DevBuf       gsrc;    /* gradient source images of the frame, [n][H][W] */
@@ -113,8 +115,12 @@ struct Pipeline {
     cudaError_t upload(const FrameHost &f);
     /* run the uploaded frame on a surface */
     cudaError_t run(const FrameHost &f, struct _vkvg_surface_t *surf, bool timing);
-    cudaError_t geometry(const FrameHost &f, const gb_surf *surfs, uint64_t ncells, uint32_t S, bool timing,
-                         bool sized);
+    /* every_cells: the cells of the draws that act on every band of their
+       surface (kinds after STROKE), a bound the draw lists are sized by;
+       wide: a surface is wider than one raster tile (the raster then reads
+       the draws' x extents) */
+    cudaError_t geometry(const FrameHost &f, const gb_surf *surfs, uint64_t ncells, uint64_t every_cells, bool wide,
+                         uint32_t S, bool timing, bool sized);
     /* K1 only: flatten the uploaded segments (for vkvg_path_extents) */
     cudaError_t flatten_only();
 };

@@ -12,6 +12,10 @@ struct gb_raster_args {
     uint32_t        init_mode, init_color;
     const gb_draw  *draws;
     const uint32_t *cell_off; /* band-major (band * ndraws + draw) offsets, nbands*ndraws + 1 */
+    const uint32_t *apos;     /* per cell: position of its entry in alist (exclusive scan of active cells) */
+    const uint32_t *alist;    /* active cells (global cell indices), band-major and in draw order */
+    const int2     *dbox;     /* per draw: (min x, -max x) of its edges, 24.8 fixed point */
+    uint32_t        cell0;    /* global index of this surface's first cell */
     const int4     *recs;   /* per-cell primitive records: an edge is one 16-byte unit, a triangle two */
     uint32_t        nunits; /* record units in recs */
     uint32_t       *status; /* device status word (GB_ERR_*) */
@@ -106,7 +110,13 @@ cudaError_t gb_launch_stroke_tris(cudaStream_t st, uint32_t ntris, uint32_t ndra
                                   int4 *tri_b, uint32_t *tri_draw, uint4 *tri_idx, int4 *edges, uint32_t *edge_draw);
 cudaError_t gb_launch_bin(cudaStream_t st, int scatter, uint32_t nedges, const int4 *edges, const uint32_t *edge_draw,
                           const gb_draw *draws, const gb_surf *surfs, uint32_t samples, uint32_t *cell, int4 *recs,
-                          uint32_t nunits);
+                          uint32_t nunits, int2 *dbox);
+/* flags[c] = 1 for the cells the raster visits: cells with records, and every
+   band's cell of the draws that act on all bands (kinds after STROKE) */
+cudaError_t gb_launch_cell_flags(cudaStream_t st, uint32_t ncells, const uint32_t *off, uint32_t ndraws,
+                                 const gb_draw *draws, const gb_surf *surfs, uint32_t *flags);
+/* alist[pos[c]] = c for the cells whose pos[c + 1] != pos[c] */
+cudaError_t gb_launch_cell_compact(cudaStream_t st, uint32_t ncells, const uint32_t *pos, uint32_t *alist);
 
 cudaError_t gb_launch_raster(cudaStream_t st, const gb_raster_args *a, const gb_clip_args *c, int gradients,
                              int clipping);

@@ -100,7 +100,7 @@ void Pipeline::destroy() {
     DevBuf *bufs[] = {&in,     &seg_cnt, &seg_off,   &scratch,    &pts,         &pflag,    &sub_pt0, &sub_npts,
                       &ev_cnt, &ev_off,  &events,    &cnt_v,      &cnt_i,       &off_v,    &off_i,   &verts,
                       &inds,   &ev_ret,  &fe_cnt,    &fe_off,     &edges,       &edge_draw, &sdraw_tri0,
-                      &sdraw_vbase, &tri_a, &tri_b, &tri_draw, &cells,   &cursor,   &recs,    &status, &dseglen, &dseg, &dfin, &tri_idx, &gsrc, &dbg, &surf_tab};
+                      &sdraw_vbase, &tri_a, &tri_b, &tri_draw, &cells,   &cursor,   &recs,    &status, &dbox, &apos, &alist, &dseglen, &dseg, &dfin, &tri_idx, &gsrc, &dbg, &surf_tab};
     for (DevBuf *b : bufs)
         b->release();
     staging.release();
@@ -195,8 +195,8 @@ static cudaError_t scan(Pipeline &pl, const uint32_t *in, uint32_t n, uint32_t *
    frame into the cells of its surface table (ncells cells in all).  With
    sized, the sizes of a previous run of the same frame are reused and nothing
    is read back, so the sequence can be captured in a CUDA graph. */
-cudaError_t Pipeline::geometry(const FrameHost &f, const gb_surf *surfs, uint64_t ncells, uint32_t S, bool timing,
-                               bool sized) {
+cudaError_t Pipeline::geometry(const FrameHost &f, const gb_surf *surfs, uint64_t ncells, uint64_t every_cells,
+                               bool wide, uint32_t S, bool timing, bool sized) {
     const uint8_t *I        = (const uint8_t *)in.p;
     auto           U        = [&](size_t o) { return (const uint32_t *)(I + o); };
     const uint32_t *seg_inf = U(o_seg_info);
@@ -337,8 +337,12 @@ cudaError_t Pipeline::geometry(const FrameHost &f, const gb_surf *surfs, uint64_
     GROW(cells, (ncells + 1) * 4);
     GROW(cursor, (ncells + 1) * 4);
     CK(cudaMemsetAsync(cells.p, 0, (ncells + 1) * 4, st));
+    if (wide) {
+        GROW(dbox, (size_t)(ndraw + 1) * 8);
+        CK(cudaMemsetAsync(dbox.p, 0x7F, (size_t)(ndraw + 1) * 8, st)); /* (min x, -max x) start at 0x7F7F7F7F */
+    }
     CK(gb_launch_bin(st, 0, nedge_all, edges.as<int4>(), edge_draw.as<uint32_t>(), draws, surfs, S,
-                     cells.as<uint32_t>(), nullptr, 0u));
+                     cells.as<uint32_t>(), nullptr, 0u, wide ? dbox.as<int2>() : nullptr));
     gb_count_launch(nedge_all ? 1 : 0);
     CK(scan(*this, cells.as<uint32_t>(), (uint32_t)ncells, cursor.as<uint32_t>()));
     if (!sized) {
@@ -349,8 +353,18 @@ cudaError_t Pipeline::geometry(const FrameHost &f, const gb_surf *surfs, uint64_
     /* cells <- offsets (kept for the raster), cursor <- running copy */
     CK(cudaMemcpyAsync(cells.p, cursor.p, (ncells + 1) * 4, cudaMemcpyDeviceToDevice, st));
     CK(gb_launch_bin(st, 1, nedge_all, edges.as<int4>(), edge_draw.as<uint32_t>(), draws, surfs, S,
-                     cursor.as<uint32_t>(), recs.as<int4>(), nunits));
+                     cursor.as<uint32_t>(), recs.as<int4>(), nunits, nullptr));
     gb_count_launch(nedge_all ? 1 : 0);
+    /* the raster's per-band draw lists: the active cells, band-major, in
+       draw order (the cursor copy is free again and holds the flags) */
+    GROW(apos, (ncells + 1) * 4);
+    CK(gb_launch_cell_flags(st, (uint32_t)ncells, cells.as<uint32_t>(), ndraw, draws, surfs, cursor.as<uint32_t>()));
+    CK(scan(*this, cursor.as<uint32_t>(), (uint32_t)ncells, apos.as<uint32_t>()));
+    /* an active cell holds a record unit or belongs to an every-band draw */
+    GROW(alist, (size_t)(nunits + every_cells + 1) * 4);
+    CK(gb_launch_cell_compact(st, (uint32_t)ncells, apos.as<uint32_t>(), alist.as<uint32_t>()));
+    gb_count_launch(ncells ? 2 : 0);
+    gb_count_launch(ndraw ? 1 : 0);
     if (timing)
         CK(cudaEventRecord(evs[3], st));
     return cudaSuccess;
@@ -377,7 +391,10 @@ cudaError_t Pipeline::run(const FrameHost &f, _vkvg_surface_t *surf, bool timing
     GROW(surf_tab, sizeof(gb_surf));
     memcpy(surf_stage.p, &sd, sizeof(sd));
     CK(cudaMemcpyAsync(surf_tab.p, surf_stage.p, sizeof(sd), cudaMemcpyHostToDevice, st));
-    CK(geometry(f, surf_tab.as<gb_surf>(), (uint64_t)nbands * ndraw, S, timing, false));
+    uint64_t every = 0;
+    for (const gb_draw &d : f.draws)
+        every += d.kind > GB_DRAW_STROKE ? nbands : 0u;
+    CK(geometry(f, surf_tab.as<gb_surf>(), (uint64_t)nbands * ndraw, every, W > GB_RASTER_TILE_W, S, timing, false));
 
     /* ---------------- K5 coverage + compositing */
     gb_raster_args A;
@@ -476,6 +493,10 @@ cudaError_t Pipeline::run(const FrameHost &f, _vkvg_surface_t *surf, bool timing
     }
     A.draws    = draws;
     A.cell_off = cells.as<uint32_t>();
+    A.apos     = apos.as<uint32_t>();
+    A.alist    = alist.as<uint32_t>();
+    A.dbox     = dbox.as<int2>();
+    A.cell0    = 0;
     A.recs     = recs.as<int4>();
     A.nunits   = nunits;
     A.status   = status.as<uint32_t>();

@@ -52,7 +52,7 @@
 
 #include <cuda_runtime.h>
 
-#define XT_W       1024 /* tile width in pixels */
+#define XT_W       GB_RASTER_TILE_W /* tile width in pixels */
 #define XT_THREADS 512  /* 16 warps, one per 64-pixel strip */
 #define XT_STRIPS  16
 #define XPLANE     (GB_BAND_ROWS * XT_W) /* one crossing counter per tile sample */
@@ -67,7 +67,8 @@
 #define SM_STAGE    SM_WORDS
 #define SM_CUR      (SM_STAGE + 2 * STAGE_CAP * 4) /* per-warp draw-chunk tables: 16 x 192 words */
 #define SM_MBAR     (SM_CUR + XT_STRIPS * 192)
-#define RASTER_SMEM (SM_MBAR * 4 + 16)
+#define SM_RG       (SM_MBAR + 4) /* the walk's bounds (draw_range), CTA-uniform */
+#define RASTER_SMEM ((SM_RG + 8) * 4)
 #define WAIT_LIMIT  (1u << 20) /* mbarrier polls before a staged copy counts as lost */
 
 #define BM_ADD  0 /* valid premultiplied source: exact on the FMA pipe */
@@ -162,30 +163,52 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
     return false;
 }
 
-/* The band's active draws (with geometry in the band, or paint / clear), 32
-   at a time: each warp keeps the chunk's (kind, lo, hi, src, op, gsrc) in its own
-   table in shared memory (ct), amask the active ones not yet taken.  All
-   warps walk the same sequence. */
+/* The band's active draws, 32 at a time, from its list of active cells
+   (positions [i0, iend) of A.alist: cells with records, and the draws that
+   act on every band).  Draws before dlo or from dhi on are passed over, and
+   so are fill and stroke draws whose edges all lie left of the tile (they
+   cross no sample) or all right of it (their closed contours add a net zero
+   to every row; tested on surfaces wider than one tile).  Each warp keeps
+   the chunk's (kind, lo, hi, src, op, gsrc) in its own table in shared
+   memory (ct), amask the active ones not yet taken.  A band whose list
+   holds more than half of the draws walks the draws themselves instead
+   (dense: positions are draw indices), which saves the list's dependent
+   load.  The walk's bounds are CTA-uniform and live in shared memory
+   (smem + SM_RG), out of the registers the blend needs.  All warps walk the
+   same sequence. */
 struct draw_cursor {
-    uint32_t d0, amask;
+    uint32_t i0, amask;
+};
+struct draw_range {
+    uint32_t iend, dlo, dhi;
+    int32_t  tx_lo, tx_hi;
+    uint32_t tiles, dense;
 };
 template <bool CLIP>
-__device__ __forceinline__ void cur_load(draw_cursor &c, const gb_raster_args &A, size_t cb, uint32_t dhi, uint32_t l,
-                                         uint32_t *ct) {
-    const uint32_t dl  = c.d0 + l;
-    bool           act = false;
-    uint32_t       kind = 0, lo = 0, hi = 0, src = 0, op = 0, gs = 0;
-    if (dl < dhi) {
-        const gb_draw &D = A.draws[dl];
-        kind             = D.kind;
-        src              = D.src;
-        op               = D.op;
-        gs               = D.gsrc;
-        lo               = A.cell_off[cb + dl];
-        hi               = A.cell_off[cb + dl + 1];
-        /* paint, clear and the clip kinds act on every band; the others only
-           where they have geometry */
-        act = kind == GB_DRAW_PAINT || (CLIP ? kind >= GB_DRAW_CLEAR : kind == GB_DRAW_CLEAR) || lo != hi;
+__device__ __forceinline__ void cur_load(draw_cursor &c, const gb_raster_args &A, size_t cb, const int32_t *smem,
+                                         uint32_t l, uint32_t *ct) {
+    const draw_range &rg  = *reinterpret_cast<const draw_range *>(smem + SM_RG);
+    const uint32_t    il  = c.i0 + l;
+    bool              act = false;
+    uint32_t          kind = 0, lo = 0, hi = 0, src = 0, op = 0, gs = 0;
+    if (il < rg.iend) {
+        const uint32_t dl = rg.dense ? il : A.alist[il] - A.cell0 - (uint32_t)cb;
+        if (dl >= rg.dlo && dl < rg.dhi) {
+            const gb_draw &D = A.draws[dl];
+            kind             = D.kind;
+            src              = D.src;
+            op               = D.op;
+            gs               = D.gsrc;
+            lo               = A.cell_off[cb + dl];
+            hi               = A.cell_off[cb + dl + 1];
+            /* paint, clear and the clip kinds act on every band; the others only
+               where they have geometry */
+            act = kind == GB_DRAW_PAINT || (CLIP ? kind >= GB_DRAW_CLEAR : kind == GB_DRAW_CLEAR) || lo != hi;
+            if (rg.tiles && act && kind <= GB_DRAW_STROKE) {
+                const int2 bx = A.dbox[dl];
+                act           = bx.x <= rg.tx_hi && -bx.y >= rg.tx_lo;
+            }
+        }
     }
     __syncwarp();
     ct[l]       = kind;
@@ -196,19 +219,21 @@ __device__ __forceinline__ void cur_load(draw_cursor &c, const gb_raster_args &A
     ct[160 + l] = gs;
     c.amask    = __ballot_sync(0xffffffffu, act);
 }
+/* the next active draw: its list position (the identity the staging
+   buffers use), kind, record range and table slot */
 template <bool CLIP>
-__device__ __forceinline__ bool cur_next(draw_cursor &c, const gb_raster_args &A, size_t cb, uint32_t dhi, uint32_t l,
-                                         uint32_t *ct, uint32_t *d, uint32_t *kind, uint32_t *lo, uint32_t *hi,
-                                         uint32_t *slot) {
+__device__ __forceinline__ bool cur_next(draw_cursor &c, const gb_raster_args &A, size_t cb, const int32_t *smem,
+                                         uint32_t l, uint32_t *ct, uint32_t *d, uint32_t *kind, uint32_t *lo,
+                                         uint32_t *hi, uint32_t *slot) {
     while (c.amask == 0) {
-        c.d0 += 32;
-        if (c.d0 >= dhi)
+        c.i0 += 32;
+        if (c.i0 >= reinterpret_cast<const draw_range *>(smem + SM_RG)->iend)
             return false;
-        cur_load<CLIP>(c, A, cb, dhi, l, ct);
+        cur_load<CLIP>(c, A, cb, smem, l, ct);
     }
     const int j = __ffs(c.amask) - 1;
     c.amask &= c.amask - 1;
-    *d    = c.d0 + (uint32_t)j;
+    *d    = c.i0 + (uint32_t)j;
     *slot = (uint32_t)j;
     *kind = ct[j];
     *lo   = ct[32 + j];
@@ -448,6 +473,16 @@ __device__ __forceinline__ void raster_item(const gb_raster_args &A, const gb_cl
         mbar_init(bar0);
         mbar_init(bar0 + 8);
         mbar_init_fence();
+        draw_range &rg = *reinterpret_cast<draw_range *>(smem + SM_RG);
+        const uint32_t ib = A.apos[cb], ie = A.apos[cb + nd];
+        rg.dlo            = dbg ? A.cov_draw : A.draw_first;
+        rg.dhi            = dbg ? A.cov_draw + 1 : nd;
+        rg.dense          = 2u * (ie - ib) > nd ? 1u : 0u;
+        rg.iend           = rg.dense ? rg.dhi : ie;
+        rg.tx_lo          = tx_lo;
+        rg.tx_hi          = tx_hi;
+        rg.tiles          = A.W > XT_W ? 1u : 0u;
+        smem[SM_RG + 7]   = rg.dense ? rg.dlo : ib; /* the walk's first position */
     }
     __syncthreads();
     /* staging state, identical in every thread: the draw each buffer holds
@@ -465,20 +500,18 @@ __device__ __forceinline__ void raster_item(const gb_raster_args &A, const gb_cl
         stg_pend |= 1u << b;
     };
 
-    const uint32_t dlo   = dbg ? A.cov_draw : A.draw_first;
-    const uint32_t dhi   = dbg ? A.cov_draw + 1 : nd;
-    uint32_t       nproc = 0; /* draws with geometry in this band so far */
-    uint32_t   *ct = reinterpret_cast<uint32_t *>(smem + SM_CUR + wi * 192);
+    uint32_t    nproc = 0; /* draws with geometry in this band so far */
+    uint32_t   *ct    = reinterpret_cast<uint32_t *>(smem + SM_CUR + wi * 192);
     draw_cursor cur;
-    cur.d0 = dlo;
-    cur_load<CLIP>(cur, A, cb, dhi, l, ct);
+    cur.i0 = (uint32_t)smem[SM_RG + 7];
+    cur_load<CLIP>(cur, A, cb, smem, l, ct);
     uint32_t nx_d = 0, nx_kind = 0, nx_lo = 0, nx_hi = 0, nx_slot = 0;
-    bool     nx_have = cur_next<CLIP>(cur, A, cb, dhi, l, ct, &nx_d, &nx_kind, &nx_lo, &nx_hi, &nx_slot);
+    bool     nx_have = cur_next<CLIP>(cur, A, cb, smem, l, ct, &nx_d, &nx_kind, &nx_lo, &nx_hi, &nx_slot);
     {
         while (nx_have) {
             const uint32_t d = nx_d, kind = nx_kind, lo = nx_lo, hi = nx_hi;
             const uint32_t src = ct[96 + nx_slot], op = ct[128 + nx_slot], gs = ct[160 + nx_slot];
-            nx_have = cur_next<CLIP>(cur, A, cb, dhi, l, ct, &nx_d, &nx_kind, &nx_lo, &nx_hi, &nx_slot); /* lookahead */
+            nx_have = cur_next<CLIP>(cur, A, cb, smem, l, ct, &nx_d, &nx_kind, &nx_lo, &nx_hi, &nx_slot); /* lookahead */
             int            bm;
             if (kind == GB_DRAW_PAINT) {
                 const blend_k B = make_blend(src, op, &bm);
@@ -794,6 +827,9 @@ __global__ void __launch_bounds__(XT_THREADS, 1)
                 a.init_color      = sf.init_color;
                 a.draws           = A0.draws + sf.draw0;
                 a.cell_off        = A0.cell_off + sf.cell0;
+                a.apos            = A0.apos + sf.cell0;
+                a.cell0           = (uint32_t)sf.cell0;
+                a.dbox            = A0.dbox + sf.draw0;
                 a.samples         = sf.samples;
                 a.rgba            = sf.rgba;
                 Ai                = a;

@@ -230,26 +230,79 @@ __device__ __forceinline__ bool gb_prim_bands(int32_t ylo, int32_t yhi, int32_t 
 /* Binning: count (SCATTER false) or write (SCATTER true) each edge's record
    (x0, y0, x1, y1) into every (band, draw) cell of its surface it touches,
    so that a cell is one contiguous block of 16-byte records the raster can
-   stage with a single bulk copy. */
+   stage with a single bulk copy.  The counting pass also folds every edge's
+   x extent into its draw's box (min x, -max x), one atomic per warp where
+   the warp's edges belong to one draw.  Every edge that is not horizontal
+   counts, binned or not: a draw is passed over in a tile only when all of
+   the edges that can cross a row lie right of the tile (a net zero on every
+   row) or all left of it. */
 template <bool SCATTER>
 __global__ void gb_bin_edges(uint32_t nedges, const int4 *__restrict__ edges, const uint32_t *__restrict__ edge_draw,
                              const gb_draw *__restrict__ draws, const gb_surf *__restrict__ surfs, uint32_t samples,
-                             uint32_t *__restrict__ cell, int4 *__restrict__ recs, uint32_t nunits) {
-    uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= nedges)
+                             uint32_t *__restrict__ cell, int4 *__restrict__ recs, uint32_t nunits,
+                             int2 *__restrict__ dbox) {
+    const uint32_t e     = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool     valid = e < nedges;
+    bool           ok    = valid;
+    int4           ed    = make_int4(0, 0, 0, 0);
+    uint32_t       d = 0xFFFFFFFFu, b0 = 0, b1 = 0;
+    const gb_surf *sf = nullptr;
+    if (ok) {
+        ed = edges[e];
+        d  = edge_draw[e];
+        sf = &surfs[draws[d].surf];
+        ok = gb_prim_bands(min(ed.y, ed.w), max(ed.y, ed.w), max(ed.x, ed.z), samples, sf->nrows, &b0, &b1);
+    }
+    if (!SCATTER && dbox) { /* every lane of the (full) warp reaches the vote */
+        const bool     xb = valid && ed.y != ed.w;
+        const int32_t  mn = xb ? min(ed.x, ed.z) : 0x7FFFFFFF, nmx = xb ? -max(ed.x, ed.z) : 0x7FFFFFFF;
+        const uint32_t dk = xb ? d : 0xFFFFFFFFu;
+        const uint32_t d0 = __reduce_min_sync(0xFFFFFFFFu, dk);
+        if (__all_sync(0xFFFFFFFFu, dk == d0 || dk == 0xFFFFFFFFu)) {
+            const int32_t wmn = __reduce_min_sync(0xFFFFFFFFu, mn), wnmx = __reduce_min_sync(0xFFFFFFFFu, nmx);
+            if ((threadIdx.x & 31u) == 0 && d0 != 0xFFFFFFFFu) {
+                atomicMin(&dbox[d0].x, wmn);
+                atomicMin(&dbox[d0].y, wnmx);
+            }
+        } else if (xb) {
+            atomicMin(&dbox[d].x, mn);
+            atomicMin(&dbox[d].y, nmx);
+        }
+    }
+    if (!ok)
         return;
-    int4           ed = edges[e];
-    const uint32_t d  = edge_draw[e];
-    const gb_surf &sf = surfs[draws[d].surf];
-    uint32_t       b0, b1;
-    int32_t        ylo = min(ed.y, ed.w), yhi = max(ed.y, ed.w);
-    if (!gb_prim_bands(ylo, yhi, max(ed.x, ed.z), samples, sf.nrows, &b0, &b1))
-        return;
-    uint32_t *c = cell + sf.cell0 + (d - sf.draw0);
+    uint32_t *c = cell + sf->cell0 + (d - sf->draw0);
     for (uint32_t b = b0; b <= b1; b++) {
-        uint32_t slot = atomicAdd(&c[(size_t)b * sf.ndraws], 1u);
+        uint32_t slot = atomicAdd(&c[(size_t)b * sf->ndraws], 1u);
         if (SCATTER && slot < nunits)
             recs[slot] = ed;
+    }
+}
+
+/* Active cells, for the raster's per-band draw lists: a cell is active when
+   it holds records; the draws that act on every band (paint, clear, the clip
+   kinds) are active in every band of their surface. */
+__global__ void gb_cell_flags(uint32_t ncells, const uint32_t *__restrict__ off, uint32_t *__restrict__ flags) {
+    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c < ncells)
+        flags[c] = off[c + 1] != off[c] ? 1u : 0u;
+}
+__global__ void gb_cell_flags_every_band(uint32_t ndraws, const gb_draw *__restrict__ draws,
+                                         const gb_surf *__restrict__ surfs, uint32_t *__restrict__ flags) {
+    const uint32_t d = blockIdx.x * blockDim.x + threadIdx.x;
+    if (d >= ndraws || draws[d].kind <= GB_DRAW_STROKE)
+        return;
+    const gb_surf &sf = surfs[draws[d].surf];
+    for (uint32_t b = 0; b < sf.nbands; b++)
+        flags[sf.cell0 + (uint64_t)b * sf.ndraws + (d - sf.draw0)] = 1u;
+}
+/* alist[pos[c]] = c for every active cell c (pos: exclusive scan of the flags) */
+__global__ void gb_cell_compact(uint32_t ncells, const uint32_t *__restrict__ pos, uint32_t *__restrict__ alist) {
+    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c < ncells) {
+        const uint32_t p = pos[c];
+        if (pos[c + 1] != p)
+            alist[p] = c;
     }
 }
 /* out[i] = src[idx[i]] */
@@ -297,15 +350,28 @@ cudaError_t gb_launch_stroke_tris(cudaStream_t st, uint32_t ntris, uint32_t ndra
 }
 cudaError_t gb_launch_bin(cudaStream_t st, int scatter, uint32_t nedges, const int4 *edges, const uint32_t *edge_draw,
                           const gb_draw *draws, const gb_surf *surfs, uint32_t samples, uint32_t *cell, int4 *recs,
-                          uint32_t nunits) {
+                          uint32_t nunits, int2 *dbox) {
     if (nedges) {
         if (scatter)
             gb_bin_edges<true><<<(nedges + 255) / 256, 256, 0, st>>>(nedges, edges, edge_draw, draws, surfs, samples,
-                                                                      cell, recs, nunits);
+                                                                      cell, recs, nunits, nullptr);
         else
             gb_bin_edges<false><<<(nedges + 255) / 256, 256, 0, st>>>(nedges, edges, edge_draw, draws, surfs,
-                                                                       samples, cell, nullptr, 0u);
+                                                                       samples, cell, nullptr, 0u, dbox);
     }
+    return cudaGetLastError();
+}
+cudaError_t gb_launch_cell_flags(cudaStream_t st, uint32_t ncells, const uint32_t *off, uint32_t ndraws,
+                                 const gb_draw *draws, const gb_surf *surfs, uint32_t *flags) {
+    if (ncells)
+        gb_cell_flags<<<(ncells + 255) / 256, 256, 0, st>>>(ncells, off, flags);
+    if (ndraws)
+        gb_cell_flags_every_band<<<(ndraws + 255) / 256, 256, 0, st>>>(ndraws, draws, surfs, flags);
+    return cudaGetLastError();
+}
+cudaError_t gb_launch_cell_compact(cudaStream_t st, uint32_t ncells, const uint32_t *pos, uint32_t *alist) {
+    if (ncells)
+        gb_cell_compact<<<(ncells + 255) / 256, 256, 0, st>>>(ncells, pos, alist);
     return cudaGetLastError();
 }
 }
