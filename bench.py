@@ -587,14 +587,14 @@ def main():
         ta = (C.c_void_p * len(btarget))(*[s2.h for s2 in btarget])
         bt = L.vkvg_gb300_batch_create(fa, ta, len(bframes))
         assert bt
-        for _ in range(6):  # sizing, four tuning runs, graph capture
+        for _ in range(10):  # sizing, eight tuning runs, graph capture
             assert L.vkvg_gb300_batch_execute(bt) == 0
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for _ in range(5):
             assert L.vkvg_gb300_batch_execute(bt) == 0
         batch_s = (time.perf_counter() - t0) / 5
-        bt_info = np.zeros(8, np.float32)
+        bt_info = np.zeros(9, np.float32)
         L.vkvg_gb300_batch_timing(bt, bt_info.ctypes.data_as(C.c_void_p))
         same = all(np.array_equal(s1.samples_rgba(), s2.samples_rgba()) for s1, s2 in zip(bsurf[:8], btarget[:8]))
         batch = {"workload": "64 surfaces, side log-U[256,2048], Pareto(1.2) paths in [100,20000], segments "
@@ -603,7 +603,8 @@ def main():
                  "plain_ms": plain_s * 1e3, "plain_paths_per_s": bpaths / plain_s, "batch_ms": batch_s * 1e3,
                  "batch_paths_per_s": bpaths / batch_s, "speedup": plain_s / batch_s,
                  "graph_replay": bool(bt_info[1]), "tuned_stage_min": int(bt_info[2]),
-                 "tuned_heaviest_first": bool(bt_info[3]), "work_items": int(bt_info[4]),
+                 "tuned_heaviest_first": bool(bt_info[3]), "tuned_tile_px": 256 if bt_info[8] else 1024,
+                 "work_items": int(bt_info[4]),
                  "first_8_surfaces_equal_to_plain": same,
                  "note": "host timer, device-resident frames; the plain form executes the 64 captured frames one "
                          "after another"}

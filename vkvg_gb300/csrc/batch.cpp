@@ -25,8 +25,10 @@ namespace {
 struct RasterParams {
     uint32_t stage_min;  /* cells of fewer record units skip the shared-memory stage */
     bool     cost_order; /* work list heaviest first (else surface, band, tile order) */
+    bool     narrow;     /* 256-pixel tiles, four CTAs per SM (else 1024-pixel tiles, one per SM) */
 };
-const RasterParams CANDIDATES[] = {{0, true}, {8, true}, {32, true}, {0, false}};
+const RasterParams CANDIDATES[] = {{0, true, false}, {8, true, false}, {32, true, false}, {0, false, false},
+                                   {0, true, true},  {8, true, true},  {32, true, true},  {0, false, true}};
 constexpr int      NCAND        = sizeof(CANDIDATES) / sizeof(CANDIDATES[0]);
 
 /* the tuner's choice per class of scene: surfaces, draws and record units,
@@ -51,7 +53,7 @@ struct _vkvg_gb300_batch_t {
     std::vector<gb_surf> tab;
     DevBuf               d_tab, d_items, d_queue, d_idx, d_units;
     PinnedBuf            h_stage;
-    std::vector<uint4>   items_cost, items_plain; /* the work list in both orders */
+    std::vector<uint4>   items_cost[2], items_plain[2]; /* the work lists (wide, narrow tiles) in both orders */
     uint64_t             ncells  = 0;
     uint64_t             every   = 0; /* cells of the draws that act on every band */
     uint32_t             samples = 0;
@@ -151,8 +153,9 @@ void first_draw_init(const gb_draw *d, uint32_t n, gb_surf &s) {
 
 namespace {
 
-/* the work list: every (surface, band, tile), in surface order and sorted by
-   the band's record units (heaviest first); both kept on the device */
+/* the work lists: every (surface, band, tile) for either tile width, in
+   surface order and sorted by the band's record units (heaviest first); all
+   four kept on the device, one after another */
 cudaError_t build_items(VkvgBatch b) {
     Pipeline            &pl = b->pl;
     std::vector<uint64_t> idx;
@@ -170,35 +173,44 @@ cudaError_t build_items(VkvgBatch b) {
     BCK(cudaMemcpyAsync(b->h_stage.p, b->d_units.p, n * 4, cudaMemcpyDeviceToHost, pl.st));
     BCK(cudaStreamSynchronize(pl.st));
     memcpy(off.data(), b->h_stage.p, n * 4);
-    std::vector<std::pair<uint32_t, uint4>> costed;
-    b->items_plain.clear();
-    size_t j = 0;
-    for (uint32_t si = 0; si < b->tab.size(); si++) {
-        const gb_surf &s     = b->tab[si];
-        const uint32_t tiles = (s.W + 1023) / 1024;
-        for (uint32_t band = 0; band < s.nbands; band++, j++) {
-            const uint32_t units = off[j + 1] - off[j];
-            for (uint32_t t = 0; t < tiles; t++) {
-                const uint4 it = make_uint4(si, band, t, units);
-                b->items_plain.push_back(it);
-                costed.push_back({units, it});
+    size_t tot = 0;
+    for (int nw = 0; nw < 2; nw++) {
+        const uint32_t                          tw = gb_raster_tile_width(nw);
+        std::vector<std::pair<uint32_t, uint4>> costed;
+        b->items_plain[nw].clear();
+        size_t j = 0;
+        for (uint32_t si = 0; si < b->tab.size(); si++) {
+            const gb_surf &s     = b->tab[si];
+            const uint32_t tiles = (s.W + tw - 1) / tw;
+            for (uint32_t band = 0; band < s.nbands; band++, j++) {
+                const uint32_t units = off[j + 1] - off[j];
+                for (uint32_t t = 0; t < tiles; t++) {
+                    const uint4 it = make_uint4(si, band, t, units);
+                    b->items_plain[nw].push_back(it);
+                    costed.push_back({units, it});
+                }
             }
+            j++; /* the surface's end boundary */
         }
-        j++; /* the surface's end boundary */
+        std::stable_sort(costed.begin(), costed.end(),
+                         [](const std::pair<uint32_t, uint4> &x, const std::pair<uint32_t, uint4> &y) {
+                             return x.first > y.first;
+                         });
+        b->items_cost[nw].clear();
+        for (auto &c : costed)
+            b->items_cost[nw].push_back(c.second);
+        tot += 2 * b->items_plain[nw].size();
     }
-    std::stable_sort(costed.begin(), costed.end(),
-                     [](const std::pair<uint32_t, uint4> &x, const std::pair<uint32_t, uint4> &y) {
-                         return x.first > y.first;
-                     });
-    b->items_cost.clear();
-    for (auto &c : costed)
-        b->items_cost.push_back(c.second);
-    const size_t ni = b->items_plain.size();
-    if (!b->d_items.grow(std::max<size_t>(2 * ni * 16, 16)) || !b->h_stage.grow(std::max<size_t>(2 * ni * 16, 64)))
+    if (!b->d_items.grow(std::max<size_t>(tot * 16, 16)) || !b->h_stage.grow(std::max<size_t>(tot * 16, 64)))
         return cudaErrorMemoryAllocation;
-    memcpy(b->h_stage.p, b->items_plain.data(), ni * 16);
-    memcpy((uint8_t *)b->h_stage.p + ni * 16, b->items_cost.data(), ni * 16);
-    BCK(cudaMemcpyAsync(b->d_items.p, b->h_stage.p, 2 * ni * 16, cudaMemcpyHostToDevice, pl.st));
+    uint8_t *h = (uint8_t *)b->h_stage.p;
+    for (int nw = 0; nw < 2; nw++) {
+        memcpy(h, b->items_plain[nw].data(), b->items_plain[nw].size() * 16);
+        h += b->items_plain[nw].size() * 16;
+        memcpy(h, b->items_cost[nw].data(), b->items_cost[nw].size() * 16);
+        h += b->items_cost[nw].size() * 16;
+    }
+    BCK(cudaMemcpyAsync(b->d_items.p, b->h_stage.p, tot * 16, cudaMemcpyHostToDevice, pl.st));
     return cudaStreamSynchronize(pl.st);
 }
 
@@ -206,13 +218,15 @@ cudaError_t build_items(VkvgBatch b) {
    unless sized), the batch raster with settings p, the status read back */
 cudaError_t run_batch(VkvgBatch b, bool sized, const RasterParams &p) {
     Pipeline &pl = b->pl;
-    bool wide = false;
+    bool wide = false; /* the x extents serve the narrow tiles' candidates too */
     for (const gb_surf &s : b->tab)
-        wide |= s.W > GB_RASTER_TILE_W;
+        wide |= s.W > gb_raster_tile_width(1);
     BCK(pl.geometry(b->merged, b->d_tab.as<gb_surf>(), b->ncells, b->every, wide, b->samples, false, sized));
     if (!sized)
         BCK(build_items(b));
-    const uint32_t ni = (uint32_t)b->items_plain.size();
+    const int      nw   = p.narrow ? 1 : 0;
+    const uint32_t ni   = (uint32_t)b->items_plain[nw].size();
+    const size_t   base = nw ? 2 * b->items_plain[0].size() : 0; /* this width's lists on the device */
     gb_raster_args A0;
     memset(&A0, 0, sizeof(A0));
     A0.S         = b->samples;
@@ -226,8 +240,9 @@ cudaError_t run_batch(VkvgBatch b, bool sized, const RasterParams &p) {
     A0.status    = pl.status.as<uint32_t>();
     A0.stage_min = p.stage_min;
     BCK(cudaMemsetAsync(b->d_queue.p, 0, 4, pl.st));
-    BCK(gb_launch_raster_batch(pl.st, &A0, b->d_tab.as<gb_surf>(), b->d_items.as<uint4>() + (p.cost_order ? ni : 0),
-                               ni, b->d_queue.as<uint32_t>(), b->nctas));
+    BCK(gb_launch_raster_batch(pl.st, &A0, b->d_tab.as<gb_surf>(),
+                               b->d_items.as<uint4>() + base + (p.cost_order ? ni : 0),
+                               ni, b->d_queue.as<uint32_t>(), b->nctas, p.narrow ? 1 : 0));
     gb_count_launch(ni ? 1 : 0);
     return cudaMemcpyAsync(pl.rb.p, pl.status.p, 4, cudaMemcpyDeviceToHost, pl.st);
 }
@@ -384,17 +399,18 @@ vkvg_status_t vkvg_gb300_batch_execute(VkvgBatch b) {
     return VKVG_STATUS_SUCCESS;
 }
 
-vkvg_status_t vkvg_gb300_batch_timing(VkvgBatch b, float out[8]) {
+vkvg_status_t vkvg_gb300_batch_timing(VkvgBatch b, float out[9]) {
     if (!b || !out)
         return VKVG_STATUS_NULL_POINTER;
     out[0] = b->last_ms;
     out[1] = b->last_graph ? 1.f : 0.f;
     out[2] = (float)b->params.stage_min;
     out[3] = b->params.cost_order ? 1.f : 0.f;
-    out[4] = (float)b->items_plain.size();
+    out[4] = (float)b->items_plain[b->params.narrow ? 1 : 0].size();
     out[5] = (float)b->tab.size();
     out[6] = b->tuned ? 1.f : 0.f;
     out[7] = (float)b->pl.nunits;
+    out[8] = b->params.narrow ? 1.f : 0.f;
     return VKVG_STATUS_SUCCESS;
 }
 

@@ -163,7 +163,7 @@ vkvg_status_t vkvg_gb300_debug_coverage(VkvgContext ctx, uint32_t i, int32_t *ou
     A.cov_draw = i;
     gb_clip_args CA;
     memset(&CA, 0, sizeof(CA));
-    if (gb_launch_raster(p.st, &A, &CA, 0, 0) != cudaSuccess)
+    if (gb_launch_raster(p.st, &A, &CA, 0, 0, 0) != cudaSuccess)
         return VKVG_STATUS_DEVICE_ERROR;
     gb_count_launch(1);
     if (cudaStreamSynchronize(p.st) != cudaSuccess)

@@ -105,6 +105,8 @@ struct Pipeline {
     uint32_t nseg = 0, nsub = 0, ndraw = 0, nspair = 0, nsdraw = 0, nfpair = 0;
     uint32_t npts = 0, nev = 0, nverts = 0, ninds = 0, nedges = 0, ntris = 0, nunits = 0, nbands = 0;
     uint32_t dev_status = 0;
+    uint32_t stats_w    = 0;     /* surface width of a one-surface frame: geometry measures its draws' widths */
+    bool     narrow     = false; /* the last frame's raster form (256-pixel tiles) */
     uint64_t launches   = 0;
     uint64_t upload_bytes = 0;
     float    ms[5]      = {0, 0, 0, 0, 0};

@@ -110,23 +110,33 @@ cudaError_t gb_launch_stroke_tris(cudaStream_t st, uint32_t ntris, uint32_t ndra
                                   int4 *tri_b, uint32_t *tri_draw, uint4 *tri_idx, int4 *edges, uint32_t *edge_draw);
 cudaError_t gb_launch_bin(cudaStream_t st, int scatter, uint32_t nedges, const int4 *edges, const uint32_t *edge_draw,
                           const gb_draw *draws, const gb_surf *surfs, uint32_t samples, uint32_t *cell, int4 *recs,
-                          uint32_t nunits, int2 *dbox);
+                          uint32_t nunits, int2 *dbox, uint32_t *dcnt);
 /* flags[c] = 1 for the cells the raster visits: cells with records, and every
    band's cell of the draws that act on all bands (kinds after STROKE) */
 cudaError_t gb_launch_cell_flags(cudaStream_t st, uint32_t ncells, const uint32_t *off, uint32_t ndraws,
                                  const gb_draw *draws, const gb_surf *surfs, uint32_t *flags);
+/* stats[0] += clipped pixel width x edges of each fill and stroke draw, stats[1] += its edges */
+cudaError_t gb_launch_draw_width_stats(cudaStream_t st, uint32_t ndraws, const gb_draw *draws, const int2 *dbox,
+                                       const uint32_t *dcnt, uint32_t W, unsigned long long *stats);
+/* *mx = max(*mx, cnt[0 .. ncells)) */
+cudaError_t gb_launch_cells_max(cudaStream_t st, uint32_t ncells, const uint32_t *cnt, uint32_t *mx);
 /* alist[pos[c]] = c for the cells whose pos[c + 1] != pos[c] */
 cudaError_t gb_launch_cell_compact(cudaStream_t st, uint32_t ncells, const uint32_t *pos, uint32_t *alist);
 
+/* narrow: the 256-pixel raster form (4 warps, 4 CTAs per SM) instead of the
+   1024-pixel one (16 warps, one CTA per SM); clipping frames run the latter */
 cudaError_t gb_launch_raster(cudaStream_t st, const gb_raster_args *a, const gb_clip_args *c, int gradients,
-                             int clipping);
+                             int clipping, int narrow);
+/* pixels per raster tile of either form */
+uint32_t gb_raster_tile_width(int narrow);
 /* out[i] = src[idx[i]] */
 cudaError_t gb_launch_gather_u32(cudaStream_t st, uint32_t n, const uint64_t *idx, const uint32_t *src,
                                  uint32_t *out);
 /* the persistent batch raster over a work list of (surface, band, tile, -)
-   items (queue: a zeroed counter), nctas CTAs */
+   items (queue: a zeroed counter), nctas SMs' worth of CTAs, tiles of the
+   form narrow selects */
 cudaError_t gb_launch_raster_batch(cudaStream_t st, const gb_raster_args *a, const gb_surf *surfs, const uint4 *items,
-                                   uint32_t nitems, uint32_t *queue, uint32_t nctas);
+                                   uint32_t nitems, uint32_t *queue, uint32_t nctas, int narrow);
 cudaError_t gb_launch_pmath_eval(cudaStream_t st, int fn, const float *a, const float *b, float *out, uint64_t n);
 }
 

@@ -337,23 +337,52 @@ cudaError_t Pipeline::geometry(const FrameHost &f, const gb_surf *surfs, uint64_
     GROW(cells, (ncells + 1) * 4);
     GROW(cursor, (ncells + 1) * 4);
     CK(cudaMemsetAsync(cells.p, 0, (ncells + 1) * 4, st));
+    /* per draw: (min x, -max x) from 0x7F7F7F7F, then its edge count from 0 */
+    uint32_t *dcnt = nullptr;
     if (wide) {
-        GROW(dbox, (size_t)(ndraw + 1) * 8);
-        CK(cudaMemsetAsync(dbox.p, 0x7F, (size_t)(ndraw + 1) * 8, st)); /* (min x, -max x) start at 0x7F7F7F7F */
+        GROW(dbox, (size_t)(ndraw + 1) * 12);
+        dcnt = (uint32_t *)(dbox.as<int2>() + ndraw + 1);
+        CK(cudaMemsetAsync(dbox.p, 0x7F, (size_t)(ndraw + 1) * 8, st));
+        CK(cudaMemsetAsync(dcnt, 0, (size_t)(ndraw + 1) * 4, st));
     }
     CK(gb_launch_bin(st, 0, nedge_all, edges.as<int4>(), edge_draw.as<uint32_t>(), draws, surfs, S,
-                     cells.as<uint32_t>(), nullptr, 0u, wide ? dbox.as<int2>() : nullptr));
+                     cells.as<uint32_t>(), nullptr, 0u, wide ? dbox.as<int2>() : nullptr, dcnt));
     gb_count_launch(nedge_all ? 1 : 0);
+    /* a one-surface frame's edge-weighted mean draw width (status words 4..7)
+       and heaviest cell (word 8) pick the raster form */
+    const bool stats = stats_w && !sized;
+    if (stats) {
+        CK(cudaMemsetAsync(status.as<uint32_t>() + 4, 0, 20, st));
+        if (wide)
+            CK(gb_launch_draw_width_stats(st, ndraw, draws, dbox.as<int2>(), dcnt, stats_w,
+                                          (unsigned long long *)(status.as<uint32_t>() + 4)));
+        CK(gb_launch_cells_max(st, (uint32_t)ncells, cells.as<uint32_t>(), status.as<uint32_t>() + 8));
+        gb_count_launch((wide && ndraw ? 1 : 0) + (ncells ? 1 : 0));
+    }
     CK(scan(*this, cells.as<uint32_t>(), (uint32_t)ncells, cursor.as<uint32_t>()));
     if (!sized) {
-        CK(readback_u32(*this, cursor.as<uint32_t>() + ncells, hv, 1));
+        CK(cudaMemcpyAsync(rb.p, cursor.as<uint32_t>() + ncells, 4, cudaMemcpyDeviceToHost, st));
+        if (stats)
+            CK(cudaMemcpyAsync((uint8_t *)rb.p + 8, status.as<uint32_t>() + 4, 20, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        uint64_t ws[2] = {0, 0};
+        uint32_t mxc   = 0;
+        memcpy(hv, rb.p, 4);
+        memcpy(ws, (uint8_t *)rb.p + 8, 16);
+        memcpy(&mxc, (uint8_t *)rb.p + 24, 4);
         nunits = hv[0];
+        /* narrow tiles when every cell fits the narrow form's staging buffer
+           (a heavy cell is one CTA's serial work: the wide form's 512 threads
+           finish it sooner) and the draws that carry the edges are small next
+           to a wide tile, or the surface is no wider than a narrow one */
+        const bool small = !wide || (ws[1] && ws[0] <= 384u * ws[1]);
+        narrow           = stats && mxc <= 512u && small;
     }
     GROW(recs, (size_t)(nunits + 1) * 16);
     /* cells <- offsets (kept for the raster), cursor <- running copy */
     CK(cudaMemcpyAsync(cells.p, cursor.p, (ncells + 1) * 4, cudaMemcpyDeviceToDevice, st));
     CK(gb_launch_bin(st, 1, nedge_all, edges.as<int4>(), edge_draw.as<uint32_t>(), draws, surfs, S,
-                     cursor.as<uint32_t>(), recs.as<int4>(), nunits, nullptr));
+                     cursor.as<uint32_t>(), recs.as<int4>(), nunits, nullptr, nullptr));
     gb_count_launch(nedge_all ? 1 : 0);
     /* the raster's per-band draw lists: the active cells, band-major, in
        draw order (the cursor copy is free again and holds the flags) */
@@ -394,7 +423,10 @@ cudaError_t Pipeline::run(const FrameHost &f, _vkvg_surface_t *surf, bool timing
     uint64_t every = 0;
     for (const gb_draw &d : f.draws)
         every += d.kind > GB_DRAW_STROKE ? nbands : 0u;
-    CK(geometry(f, surf_tab.as<gb_surf>(), (uint64_t)nbands * ndraw, every, W > GB_RASTER_TILE_W, S, timing, false));
+    stats_w = W;
+    CK(geometry(f, surf_tab.as<gb_surf>(), (uint64_t)nbands * ndraw, every, W > gb_raster_tile_width(1), S, timing,
+                false));
+    stats_w = 0;
 
     /* ---------------- K5 coverage + compositing */
     gb_raster_args A;
@@ -512,7 +544,7 @@ cudaError_t Pipeline::run(const FrameHost &f, _vkvg_surface_t *surf, bool timing
         gb_count_launch(ngrad);
         A.gsrc = gsrc.as<uint32_t>();
     }
-    CK(gb_launch_raster(st, &A, &CA, ngrad > 0, clip_use));
+    CK(gb_launch_raster(st, &A, &CA, ngrad > 0, clip_use, narrow && !clip_use));
     surf->clip_active = act;
     surf->save_nz     = snz;
     gb_count_launch(1);

@@ -52,23 +52,36 @@
 
 #include <cuda_runtime.h>
 
-#define XT_W       GB_RASTER_TILE_W /* tile width in pixels */
-#define XT_THREADS 512  /* 16 warps, one per 64-pixel strip */
-#define XT_STRIPS  16
-#define XPLANE     (GB_BAND_ROWS * XT_W) /* one crossing counter per tile sample */
-#define TOT_ROW    20                    /* strip totals per row, padded against bank conflicts */
-#define TOT_SET    (GB_BAND_ROWS * TOT_ROW)
-/* shared memory: 2 counter planes, 3 strip-total sets, 2 flag sets */
-#define SM_TOT      (2 * XPLANE)
-#define SM_FLAG     (SM_TOT + 3 * TOT_SET)
-#define SM_WORDS    (SM_FLAG + 2 * XT_STRIPS)
-/* then 2 staging buffers for a cell's records (16-byte units), 2 mbarriers */
-#define STAGE_CAP   2048 /* units per staging buffer: 32 KB */
-#define SM_STAGE    SM_WORDS
-#define SM_CUR      (SM_STAGE + 2 * STAGE_CAP * 4) /* per-warp draw-chunk tables: 16 x 192 words */
-#define SM_MBAR     (SM_CUR + XT_STRIPS * 192)
-#define SM_RG       (SM_MBAR + 4) /* the walk's bounds (draw_range), CTA-uniform */
-#define RASTER_SMEM ((SM_RG + 8) * 4)
+/* Tile geometry of a raster CTA of NW warps: NW strips of 64 pixels, 16
+   sample rows.  Shared memory: 2 counter planes, 3 strip-total sets, 2 flag
+   sets; then 2 staging buffers for a cell's records (16-byte units), the
+   per-warp draw-chunk tables (192 words each), 2 mbarriers and the walk's
+   bounds.  The wide form (16 warps, 1024 pixels, one CTA per SM) suits
+   surfaces whose draws span most of a tile; the narrow form (4 warps, 256
+   pixels, four CTAs per SM) suits small draws and narrow surfaces, where
+   the wide form's warps would wait at each draw's barrier with nothing to
+   blend. */
+template <int NW> struct XT {
+    static constexpr int W         = 64 * NW;
+    static constexpr int THREADS   = 32 * NW;
+    static constexpr int MINB      = NW >= 16 ? 1 : 4; /* CTAs per SM */
+    static constexpr int PLANE     = GB_BAND_ROWS * W; /* one crossing counter per tile sample */
+    static constexpr int TOT_ROW   = NW + 4;           /* strip totals per row, padded against bank conflicts */
+    static constexpr int TOT_SET   = GB_BAND_ROWS * TOT_ROW;
+    static constexpr int S_TOT     = 2 * PLANE;
+    static constexpr int S_FLAG    = S_TOT + 3 * TOT_SET;
+    static constexpr int S_WORDS   = S_FLAG + 2 * NW;
+    static constexpr int STAGE_CAP = NW >= 16 ? 2048 : 512; /* units per staging buffer */
+    static constexpr int S_STAGE   = S_WORDS;
+    static constexpr int S_CUR     = S_STAGE + 2 * STAGE_CAP * 4;
+    static constexpr int S_MBAR    = S_CUR + NW * 192;
+    static constexpr int S_RG      = S_MBAR + 4;
+    static constexpr int SMEM      = (S_RG + 8) * 4;
+    static_assert(S_STAGE % 4 == 0 && S_MBAR % 2 == 0, "staging buffers 16-byte, mbarriers 8-byte aligned");
+    static_assert(MINB * (SMEM + 1024) <= 232448, "shared memory of the CTAs an SM holds");
+};
+#define XT_WIDE   16
+#define XT_NARROW 4
 #define WAIT_LIMIT  (1u << 20) /* mbarrier polls before a staged copy counts as lost */
 
 #define BM_ADD  0 /* valid premultiplied source: exact on the FMA pipe */
@@ -128,9 +141,9 @@ __device__ __forceinline__ blend_k make_blend(uint32_t src, uint32_t op, int *mo
 /* counter (or staged sample) of tile sample p in band row rr: each lane run
    of 32 samples is eight 16-byte slots, rotated by the row and the run's
    half-strip so that the eight lanes of one 128-byte phase hit distinct banks */
-__device__ __forceinline__ uint32_t swz(uint32_t rr, uint32_t p) {
+template <int NW> __device__ __forceinline__ uint32_t swz(uint32_t rr, uint32_t p) {
     const uint32_t v = ((rr & 3u) << 1) | ((p >> 5) & 1u);
-    return rr * XT_W + (((p >> 2) ^ v) << 2) + (p & 3u);
+    return rr * XT<NW>::W + (((p >> 2) ^ v) << 2) + (p & 3u);
 }
 
 /* ---- bulk-copy staging (cp.async.bulk + mbarrier transaction counts) */
@@ -174,7 +187,7 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
    holds more than half of the draws walks the draws themselves instead
    (dense: positions are draw indices), which saves the list's dependent
    load.  The walk's bounds are CTA-uniform and live in shared memory
-   (smem + SM_RG), out of the registers the blend needs.  All warps walk the
+   (smem + S_RG), out of the registers the blend needs.  All warps walk the
    same sequence. */
 struct draw_cursor {
     uint32_t i0, amask;
@@ -184,10 +197,10 @@ struct draw_range {
     int32_t  tx_lo, tx_hi;
     uint32_t tiles, dense;
 };
-template <bool CLIP>
+template <int NW, bool CLIP>
 __device__ __forceinline__ void cur_load(draw_cursor &c, const gb_raster_args &A, size_t cb, const int32_t *smem,
                                          uint32_t l, uint32_t *ct) {
-    const draw_range &rg  = *reinterpret_cast<const draw_range *>(smem + SM_RG);
+    const draw_range &rg  = *reinterpret_cast<const draw_range *>(smem + XT<NW>::S_RG);
     const uint32_t    il  = c.i0 + l;
     bool              act = false;
     uint32_t          kind = 0, lo = 0, hi = 0, src = 0, op = 0, gs = 0;
@@ -221,15 +234,15 @@ __device__ __forceinline__ void cur_load(draw_cursor &c, const gb_raster_args &A
 }
 /* the next active draw: its list position (the identity the staging
    buffers use), kind, record range and table slot */
-template <bool CLIP>
+template <int NW, bool CLIP>
 __device__ __forceinline__ bool cur_next(draw_cursor &c, const gb_raster_args &A, size_t cb, const int32_t *smem,
                                          uint32_t l, uint32_t *ct, uint32_t *d, uint32_t *kind, uint32_t *lo,
                                          uint32_t *hi, uint32_t *slot) {
     while (c.amask == 0) {
         c.i0 += 32;
-        if (c.i0 >= reinterpret_cast<const draw_range *>(smem + SM_RG)->iend)
+        if (c.i0 >= reinterpret_cast<const draw_range *>(smem + XT<NW>::S_RG)->iend)
             return false;
-        cur_load<CLIP>(c, A, cb, smem, l, ct);
+        cur_load<NW, CLIP>(c, A, cb, smem, l, ct);
     }
     const int j = __ffs(c.amask) - 1;
     c.amask &= c.amask - 1;
@@ -257,6 +270,7 @@ template <bool CLIP> __device__ __forceinline__ bool is_geom(uint32_t kind) {
 /* one edge crossing sample row sy (band row rr): add dir at the last tile
    sample left of the crossing, so that the suffix sum from sample c is the
    winding contribution at c */
+template <int NW>
 __device__ __forceinline__ void acc_row(int32_t x0, int32_t y0, int32_t x1, int32_t y1, int32_t sy, uint32_t rr,
                                         int32_t ox, int32_t X0, int32_t TW, int32_t tx_lo, int32_t tx_hi,
                                         int32_t *__restrict__ plane, int32_t *__restrict__ tot,
@@ -281,8 +295,8 @@ __device__ __forceinline__ void acc_row(int32_t x0, int32_t y0, int32_t x1, int3
         k = kt > TW ? TW : (int32_t)kt;
     }
     const uint32_t p = (uint32_t)(k - 1);
-    atomicAdd(&plane[swz(rr, p)], dir);
-    atomicAdd(&tot[rr * TOT_ROW + (p >> 6)], dir);
+    atomicAdd(&plane[swz<NW>(rr, p)], dir);
+    atomicAdd(&tot[rr * XT<NW>::TOT_ROW + (p >> 6)], dir);
     flag[p >> 6] = 1;
 }
 
@@ -407,15 +421,16 @@ __device__ __forceinline__ uint32_t clip_bits(const int4 *cp, uint32_t v, int32_
 }
 
 /* One cell of the raster: sample rows [16 band, 16 band + 16) and columns
-   [1024 tile, 1024 tile + 1024) of A's surface, through every draw of the
+   [W tile, W tile + W) of A's surface (W = 64 NW), through every draw of the
    surface in order, then the resolve of its pixels. */
-template <bool GRAD, bool CLIP>
+template <int NW, bool GRAD, bool CLIP>
 __device__ __forceinline__ void raster_item(const gb_raster_args &A, const gb_clip_args &C, int32_t *smem,
                                             uint32_t band, uint32_t tile) {
+    using X          = XT<NW>;
     const uint32_t t = threadIdx.x, wi = t >> 5, l = t & 31;
     const uint32_t rl = l >> 1, hh = l & 1; /* blend mapping: band row and half-strip */
-    const int32_t  X0      = (int32_t)(tile * XT_W);
-    const int32_t  TW      = min((int32_t)XT_W, (int32_t)A.W - X0);
+    const int32_t  X0      = (int32_t)(tile * X::W);
+    const int32_t  TW      = min((int32_t)X::W, (int32_t)A.W - X0);
     const int32_t  R       = (int32_t)(band * GB_BAND_ROWS + rl);
     const bool     row_ok  = R < (int32_t)A.nrows;
     const int32_t  col0    = (int32_t)(64 * wi + 32 * hh);
@@ -465,15 +480,15 @@ __device__ __forceinline__ void raster_item(const gb_raster_args &A, const gb_cl
         cm = C.clip[cwi];
     if (CLIP && C.clip_load == 2 && cwr && !dbg)
         clip_zero_planes(cpl, C.plane_words);
-    for (uint32_t i = t; i < SM_WORDS; i += XT_THREADS)
+    for (uint32_t i = t; i < X::S_WORDS; i += X::THREADS)
         smem[i] = 0;
     const uint32_t sm_base = (uint32_t)__cvta_generic_to_shared(smem);
-    const uint32_t bar0    = sm_base + SM_MBAR * 4;
+    const uint32_t bar0    = sm_base + X::S_MBAR * 4;
     if (t == 0) {
         mbar_init(bar0);
         mbar_init(bar0 + 8);
         mbar_init_fence();
-        draw_range &rg = *reinterpret_cast<draw_range *>(smem + SM_RG);
+        draw_range &rg = *reinterpret_cast<draw_range *>(smem + X::S_RG);
         const uint32_t ib = A.apos[cb], ie = A.apos[cb + nd];
         rg.dlo            = dbg ? A.cov_draw : A.draw_first;
         rg.dhi            = dbg ? A.cov_draw + 1 : nd;
@@ -481,8 +496,8 @@ __device__ __forceinline__ void raster_item(const gb_raster_args &A, const gb_cl
         rg.iend           = rg.dense ? rg.dhi : ie;
         rg.tx_lo          = tx_lo;
         rg.tx_hi          = tx_hi;
-        rg.tiles          = A.W > XT_W ? 1u : 0u;
-        smem[SM_RG + 7]   = rg.dense ? rg.dlo : ib; /* the walk's first position */
+        rg.tiles          = A.W > X::W ? 1u : 0u;
+        smem[X::S_RG + 7] = rg.dense ? rg.dlo : ib; /* the walk's first position */
     }
     __syncthreads();
     /* staging state, identical in every thread: the draw each buffer holds
@@ -492,7 +507,7 @@ __device__ __forceinline__ void raster_item(const gb_raster_args &A, const gb_cl
     uint32_t stg_par = 0, stg_pend = 0;
     auto     stage_cell = [&](uint32_t b, uint32_t d, uint32_t lo, uint32_t units) {
         if (t == 0)
-            stage_copy(sm_base + (SM_STAGE + b * STAGE_CAP * 4) * 4, A.recs + lo, units * 16u, bar0 + 8 * b);
+            stage_copy(sm_base + (X::S_STAGE + b * X::STAGE_CAP * 4) * 4, A.recs + lo, units * 16u, bar0 + 8 * b);
         if (b)
             stg_d1 = d;
         else
@@ -501,17 +516,17 @@ __device__ __forceinline__ void raster_item(const gb_raster_args &A, const gb_cl
     };
 
     uint32_t    nproc = 0; /* draws with geometry in this band so far */
-    uint32_t   *ct    = reinterpret_cast<uint32_t *>(smem + SM_CUR + wi * 192);
+    uint32_t   *ct    = reinterpret_cast<uint32_t *>(smem + X::S_CUR + wi * 192);
     draw_cursor cur;
-    cur.i0 = (uint32_t)smem[SM_RG + 7];
-    cur_load<CLIP>(cur, A, cb, smem, l, ct);
+    cur.i0 = (uint32_t)smem[X::S_RG + 7];
+    cur_load<NW, CLIP>(cur, A, cb, smem, l, ct);
     uint32_t nx_d = 0, nx_kind = 0, nx_lo = 0, nx_hi = 0, nx_slot = 0;
-    bool     nx_have = cur_next<CLIP>(cur, A, cb, smem, l, ct, &nx_d, &nx_kind, &nx_lo, &nx_hi, &nx_slot);
+    bool     nx_have = cur_next<NW, CLIP>(cur, A, cb, smem, l, ct, &nx_d, &nx_kind, &nx_lo, &nx_hi, &nx_slot);
     {
         while (nx_have) {
             const uint32_t d = nx_d, kind = nx_kind, lo = nx_lo, hi = nx_hi;
             const uint32_t src = ct[96 + nx_slot], op = ct[128 + nx_slot], gs = ct[160 + nx_slot];
-            nx_have = cur_next<CLIP>(cur, A, cb, smem, l, ct, &nx_d, &nx_kind, &nx_lo, &nx_hi, &nx_slot); /* lookahead */
+            nx_have = cur_next<NW, CLIP>(cur, A, cb, smem, l, ct, &nx_d, &nx_kind, &nx_lo, &nx_hi, &nx_slot); /* lookahead */
             int            bm;
             if (kind == GB_DRAW_PAINT) {
                 const blend_k B = make_blend(src, op, &bm);
@@ -587,12 +602,12 @@ __device__ __forceinline__ void raster_item(const gb_raster_args &A, const gb_cl
                prefetch, so every copy issued is waited for) */
             const uint32_t sb  = nproc & 1;
             const bool     stg = hi - lo >= A.stage_min;
-            const uint32_t su  = stg ? min(hi - lo, (uint32_t)STAGE_CAP) : 0u;
+            const uint32_t su  = stg ? min(hi - lo, (uint32_t)X::STAGE_CAP) : 0u;
             if (stg && (sb ? stg_d1 : stg_d0) != d)
                 stage_cell(sb, d, lo, su);
             if (nx_have && is_geom<CLIP>(nx_kind) && nx_lo < nx_hi && nx_hi <= A.nunits &&
                 nx_hi - nx_lo >= A.stage_min)
-                stage_cell(sb ^ 1u, nx_d, nx_lo, min(nx_hi - nx_lo, (uint32_t)STAGE_CAP));
+                stage_cell(sb ^ 1u, nx_d, nx_lo, min(nx_hi - nx_lo, (uint32_t)X::STAGE_CAP));
             if (stg) {
                 if (mbar_wait(bar0 + 8 * sb, (stg_par >> sb) & 1u)) {
                     stg_pend &= ~(1u << sb);
@@ -605,31 +620,31 @@ __device__ __forceinline__ void raster_item(const gb_raster_args &A, const gb_cl
                 else
                     stg_d0 = 0xFFFFFFFFu;
             }
-            const int4 *sg = reinterpret_cast<const int4 *>(smem + SM_STAGE) + sb * STAGE_CAP;
-            int32_t *plane = smem + (nproc & 1) * XPLANE;
-            int32_t *tot   = smem + SM_TOT + (nproc % 3) * TOT_SET;
-            int32_t *flag  = smem + SM_FLAG + (nproc & 1) * XT_STRIPS;
+            const int4 *sg = reinterpret_cast<const int4 *>(smem + X::S_STAGE) + sb * X::STAGE_CAP;
+            int32_t *plane = smem + (nproc & 1) * X::PLANE;
+            int32_t *tot   = smem + X::S_TOT + (nproc % 3) * X::TOT_SET;
+            int32_t *flag  = smem + X::S_FLAG + (nproc & 1) * NW;
 
             /* ---- accumulate: one item per (primitive, band row) */
             if (iok) {
                 const uint32_t n = (hi - lo) * 16u;
-                for (uint32_t it = t; it < n; it += XT_THREADS) {
+                for (uint32_t it = t; it < n; it += X::THREADS) {
                     const uint32_t u  = it >> 4;
                     const int4     ed = u < su ? sg[u] : A.recs[lo + u];
-                    acc_row(ed.x, ed.y, ed.z, ed.w, isy, irr, iox, X0, TW, tx_lo, tx_hi, plane, tot, flag);
+                    acc_row<NW>(ed.x, ed.y, ed.z, ed.w, isy, irr, iox, X0, TW, tx_lo, tx_hi, plane, tot, flag);
                 }
             }
             __syncthreads();
 
             /* ---- blend.  The previous draw's totals are no longer read by anyone. */
             if (hh == 0)
-                smem[SM_TOT + ((nproc + 2) % 3) * TOT_SET + rl * TOT_ROW + wi] = 0;
+                smem[X::S_TOT + ((nproc + 2) % 3) * X::TOT_SET + rl * X::TOT_ROW + wi] = 0;
             nproc++;
             int32_t Er = 0; /* winding from strips to the right */
             {
-                const int4 *tr4 = reinterpret_cast<const int4 *>(tot + rl * TOT_ROW);
+                const int4 *tr4 = reinterpret_cast<const int4 *>(tot + rl * X::TOT_ROW);
 #pragma unroll
-                for (int q = 0; q < 4; q++) {
+                for (int q = 0; q < NW / 4; q++) {
                     const int4 v = tr4[q];
                     Er += (4 * q > (int)wi ? v.x : 0) + (4 * q + 1 > (int)wi ? v.y : 0) +
                           (4 * q + 2 > (int)wi ? v.z : 0) + (4 * q + 3 > (int)wi ? v.w : 0);
@@ -641,11 +656,11 @@ __device__ __forceinline__ void raster_item(const gb_raster_args &A, const gb_cl
                 /* coverage of a single draw: read the counters in place */
                 int32_t L = 0;
                 for (int c = 0; c < 32; c++)
-                    L += plane[swz(rl, col0 + c)];
+                    L += plane[swz<NW>(rl, col0 + c)];
                 const int32_t Lp = __shfl_xor_sync(0xffffffffu, L, 1);
                 int32_t       w  = Er + (hh == 0 ? Lp : 0);
                 for (int c = 31; c >= 0; c--) {
-                    w += plane[swz(rl, col0 + c)];
+                    w += plane[swz<NW>(rl, col0 + c)];
                     if (c < ncols)
                         A.cov_out[((size_t)(R / rpp) * A.W + X0 + col0 + c) * A.S + R % rpp] = w;
                 }
@@ -677,7 +692,7 @@ __device__ __forceinline__ void raster_item(const gb_raster_args &A, const gb_cl
             }
             /* this lane's 32 counters: totals first, the blend reads them again;
                then they are cleared for the draw after next */
-            int4   *cp  = reinterpret_cast<int4 *>(plane + rl * XT_W + col0);
+            int4   *cp  = reinterpret_cast<int4 *>(plane + rl * X::W + col0);
             int     nzr = 0;
             int32_t L   = 0;
 #pragma unroll
@@ -749,16 +764,16 @@ __device__ __forceinline__ void raster_item(const gb_raster_args &A, const gb_cl
     /* resolve through shared memory (aliases the counter planes); lanes
        stage their runs in the counters' rotated slot order */
     __syncthreads();
-    uint4 *stage4 = reinterpret_cast<uint4 *>(smem + rl * XT_W + col0);
+    uint4 *stage4 = reinterpret_cast<uint4 *>(smem + rl * X::W + col0);
 #pragma unroll
     for (int q = 0; q < 8; q++)
         stage4[q ^ v_lane] = make_uint4(col[4 * q], col[4 * q + 1], col[4 * q + 2], col[4 * q + 3]);
     __syncthreads();
     const uint32_t *stage = reinterpret_cast<const uint32_t *>(smem);
     const uint32_t  prows = GB_BAND_ROWS / rpp;
-    const uint32_t  npx   = prows * XT_W;
-    for (uint32_t q = t * 4; q < npx; q += XT_THREADS * 4) {
-        uint32_t pr = q / XT_W, px = q % XT_W; /* 4 consecutive pixels px..px+3 */
+    const uint32_t  npx   = prows * X::W;
+    for (uint32_t q = t * 4; q < npx; q += X::THREADS * 4) {
+        uint32_t pr = q / X::W, px = q % X::W; /* 4 consecutive pixels px..px+3 */
         uint32_t py = band * prows + pr;
         if (py >= A.H || (int32_t)px >= TW)
             continue;
@@ -767,7 +782,7 @@ __device__ __forceinline__ void raster_item(const gb_raster_args &A, const gb_cl
         for (int k = 0; k < 4; k++) {
             uint32_t s0 = 0, s1 = 0, s2 = 0, s3 = 0;
             for (uint32_t s = 0; s < rpp; s++) {
-                uint32_t v = stage[swz(pr * rpp + s, px + k)];
+                uint32_t v = stage[swz<NW>(pr * rpp + s, px + k)];
                 s0 += v & 0xFFu;
                 s1 += (v >> 8) & 0xFFu;
                 s2 += (v >> 16) & 0xFFu;
@@ -787,10 +802,10 @@ __device__ __forceinline__ void raster_item(const gb_raster_args &A, const gb_cl
     }
 }
 
-template <bool GRAD, bool CLIP>
-__global__ void __launch_bounds__(XT_THREADS, 1) gb_raster(gb_raster_args A, gb_clip_args C) {
+template <int NW, bool GRAD, bool CLIP>
+__global__ void __launch_bounds__(XT<NW>::THREADS, XT<NW>::MINB) gb_raster(gb_raster_args A, gb_clip_args C) {
     extern __shared__ __align__(16) int32_t smem[];
-    raster_item<GRAD, CLIP>(A, C, smem, blockIdx.y, blockIdx.x);
+    raster_item<NW, GRAD, CLIP>(A, C, smem, blockIdx.y, blockIdx.x);
 }
 
 __device__ __forceinline__ void mbar_inval(uint32_t bar) {
@@ -801,7 +816,8 @@ __device__ __forceinline__ void mbar_inval(uint32_t bar) {
    wait on other CTAs: each CTA stops at the end of the list).  An item's
    arguments are its surface's entry of the table over A0's shared fields,
    staged in shared memory for the whole CTA. */
-__global__ void __launch_bounds__(XT_THREADS, 1)
+template <int NW>
+__global__ void __launch_bounds__(XT<NW>::THREADS, XT<NW>::MINB)
     gb_raster_batch(gb_raster_args A0, const gb_surf *__restrict__ surfs, const uint4 *__restrict__ items,
                     uint32_t nitems, uint32_t *__restrict__ queue) {
     extern __shared__ __align__(16) int32_t smem[];
@@ -840,10 +856,10 @@ __global__ void __launch_bounds__(XT_THREADS, 1)
         __syncthreads();
         if (cur_item >= nitems)
             break;
-        raster_item<false, false>(Ai, C0, smem, cur_band, cur_tile);
+        raster_item<NW, false, false>(Ai, C0, smem, cur_band, cur_tile);
         __syncthreads();
         if (threadIdx.x == 0) { /* the next item initialises them again */
-            const uint32_t bar0 = (uint32_t)__cvta_generic_to_shared(smem) + SM_MBAR * 4;
+            const uint32_t bar0 = (uint32_t)__cvta_generic_to_shared(smem) + XT<NW>::S_MBAR * 4;
             mbar_inval(bar0);
             mbar_inval(bar0 + 8);
         }
@@ -1060,47 +1076,52 @@ extern "C" cudaError_t gb_launch_unpremultiply(cudaStream_t st, const uint32_t *
     return cudaGetLastError();
 }
 
-extern "C" cudaError_t gb_launch_raster_batch(cudaStream_t st, const gb_raster_args *a, const gb_surf *surfs,
-                                             const uint4 *items, uint32_t nitems, uint32_t *queue, uint32_t nctas) {
+template <int NW> cudaError_t raster_batch_nw(cudaStream_t st, const gb_raster_args *a, const gb_surf *surfs,
+                                               const uint4 *items, uint32_t nitems, uint32_t *queue, uint32_t nctas) {
     static bool configured = false;
     if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(gb_raster_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, RASTER_SMEM);
+        cudaError_t e =
+            cudaFuncSetAttribute(gb_raster_batch<NW>, cudaFuncAttributeMaxDynamicSharedMemorySize, XT<NW>::SMEM);
         if (e != cudaSuccess)
             return e;
         configured = true;
     }
-    if (!nitems)
-        return cudaSuccess;
-    gb_raster_batch<<<nctas, XT_THREADS, RASTER_SMEM, st>>>(*a, surfs, items, nitems, queue);
+    gb_raster_batch<NW><<<nctas * XT<NW>::MINB, XT<NW>::THREADS, XT<NW>::SMEM, st>>>(*a, surfs, items, nitems, queue);
     return cudaGetLastError();
 }
-extern "C" cudaError_t gb_launch_raster(cudaStream_t st, const gb_raster_args *a, const gb_clip_args *c, int gradients,
-                                       int clipping) {
+template <int NW, bool GRAD, bool CLIP> cudaError_t raster_nw(cudaStream_t st, const gb_raster_args *a,
+                                                              const gb_clip_args *c) {
     static bool configured = false;
     if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(gb_raster<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             RASTER_SMEM);
-        if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(gb_raster<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, RASTER_SMEM);
-        if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(gb_raster<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, RASTER_SMEM);
-        if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(gb_raster<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, RASTER_SMEM);
+        cudaError_t e = cudaFuncSetAttribute(gb_raster<NW, GRAD, CLIP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             XT<NW>::SMEM);
         if (e != cudaSuccess)
             return e;
         configured = true;
     }
+    dim3 grid((a->W + XT<NW>::W - 1) / XT<NW>::W, a->nbands);
+    gb_raster<NW, GRAD, CLIP><<<grid, XT<NW>::THREADS, XT<NW>::SMEM, st>>>(*a, *c);
+    return cudaGetLastError();
+}
+
+extern "C" uint32_t gb_raster_tile_width(int narrow) { return narrow ? XT<XT_NARROW>::W : XT<XT_WIDE>::W; }
+extern "C" cudaError_t gb_launch_raster_batch(cudaStream_t st, const gb_raster_args *a, const gb_surf *surfs,
+                                             const uint4 *items, uint32_t nitems, uint32_t *queue, uint32_t nctas,
+                                             int narrow) {
+    if (!nitems)
+        return cudaSuccess;
+    return narrow ? raster_batch_nw<XT_NARROW>(st, a, surfs, items, nitems, queue, nctas)
+                  : raster_batch_nw<XT_WIDE>(st, a, surfs, items, nitems, queue, nctas);
+}
+/* frames without gradient draws or clipping run the variants without that
+   code; frames with clipping run the wide form */
+extern "C" cudaError_t gb_launch_raster(cudaStream_t st, const gb_raster_args *a, const gb_clip_args *c, int gradients,
+                                       int clipping, int narrow) {
     if (a->nbands == 0)
         return cudaSuccess;
-    dim3 grid((a->W + XT_W - 1) / XT_W, a->nbands);
-    /* frames without gradient draws or clipping run the variants without that code */
-    if (gradients && clipping)
-        gb_raster<true, true><<<grid, XT_THREADS, RASTER_SMEM, st>>>(*a, *c);
-    else if (gradients)
-        gb_raster<true, false><<<grid, XT_THREADS, RASTER_SMEM, st>>>(*a, *c);
-    else if (clipping)
-        gb_raster<false, true><<<grid, XT_THREADS, RASTER_SMEM, st>>>(*a, *c);
-    else
-        gb_raster<false, false><<<grid, XT_THREADS, RASTER_SMEM, st>>>(*a, *c);
-    return cudaGetLastError();
+    if (clipping)
+        return gradients ? raster_nw<XT_WIDE, true, true>(st, a, c) : raster_nw<XT_WIDE, false, true>(st, a, c);
+    if (narrow)
+        return gradients ? raster_nw<XT_NARROW, true, false>(st, a, c) : raster_nw<XT_NARROW, false, false>(st, a, c);
+    return gradients ? raster_nw<XT_WIDE, true, false>(st, a, c) : raster_nw<XT_WIDE, false, false>(st, a, c);
 }

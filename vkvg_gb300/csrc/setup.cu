@@ -19,6 +19,8 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #define GB_FIX_LIMIT 268435456.0f /* 2^28 units = 2^20 px */
 
 __device__ __forceinline__ int32_t gb_to_fixed(float v) {
@@ -240,7 +242,7 @@ template <bool SCATTER>
 __global__ void gb_bin_edges(uint32_t nedges, const int4 *__restrict__ edges, const uint32_t *__restrict__ edge_draw,
                              const gb_draw *__restrict__ draws, const gb_surf *__restrict__ surfs, uint32_t samples,
                              uint32_t *__restrict__ cell, int4 *__restrict__ recs, uint32_t nunits,
-                             int2 *__restrict__ dbox) {
+                             int2 *__restrict__ dbox, uint32_t *__restrict__ dcnt) {
     const uint32_t e     = blockIdx.x * blockDim.x + threadIdx.x;
     const bool     valid = e < nedges;
     bool           ok    = valid;
@@ -253,20 +255,48 @@ __global__ void gb_bin_edges(uint32_t nedges, const int4 *__restrict__ edges, co
         sf = &surfs[draws[d].surf];
         ok = gb_prim_bands(min(ed.y, ed.w), max(ed.y, ed.w), max(ed.x, ed.z), samples, sf->nrows, &b0, &b1);
     }
-    if (!SCATTER && dbox) { /* every lane of the (full) warp reaches the vote */
-        const bool     xb = valid && ed.y != ed.w;
-        const int32_t  mn = xb ? min(ed.x, ed.z) : 0x7FFFFFFF, nmx = xb ? -max(ed.x, ed.z) : 0x7FFFFFFF;
-        const uint32_t dk = xb ? d : 0xFFFFFFFFu;
-        const uint32_t d0 = __reduce_min_sync(0xFFFFFFFFu, dk);
-        if (__all_sync(0xFFFFFFFFu, dk == d0 || dk == 0xFFFFFFFFu)) {
-            const int32_t wmn = __reduce_min_sync(0xFFFFFFFFu, mn), wnmx = __reduce_min_sync(0xFFFFFFFFu, nmx);
-            if ((threadIdx.x & 31u) == 0 && d0 != 0xFFFFFFFFu) {
-                atomicMin(&dbox[d0].x, wmn);
-                atomicMin(&dbox[d0].y, wnmx);
-            }
-        } else if (xb) {
+    if (!SCATTER && dbox) { /* every thread of the (full) block reaches the votes */
+        __shared__ uint32_t s_d[8], s_n[8];
+        __shared__ int32_t  s_mn[8], s_nmx[8];
+        const bool          xb = valid && ed.y != ed.w;
+        const int32_t       mn = xb ? min(ed.x, ed.z) : 0x7FFFFFFF, nmx = xb ? -max(ed.x, ed.z) : 0x7FFFFFFF;
+        const uint32_t      dk = xb ? d : 0xFFFFFFFFu;
+        const uint32_t      d0 = __reduce_min_sync(0xFFFFFFFFu, dk);
+        const bool          wu = __all_sync(0xFFFFFFFFu, dk == d0 || dk == 0xFFFFFFFFu);
+        const int32_t wmn = __reduce_min_sync(0xFFFFFFFFu, mn), wnmx = __reduce_min_sync(0xFFFFFFFFu, nmx);
+        const uint32_t wn = __reduce_add_sync(0xFFFFFFFFu, xb ? 1u : 0u);
+        const uint32_t w  = threadIdx.x >> 5;
+        if ((threadIdx.x & 31u) == 0) { /* a warp of one draw hands its box to the block */
+            s_d[w]   = wu ? d0 : 0xFFFFFFFEu;
+            s_mn[w]  = wmn;
+            s_nmx[w] = wnmx;
+            s_n[w]   = wn;
+        }
+        if (!wu && xb) {
             atomicMin(&dbox[d].x, mn);
             atomicMin(&dbox[d].y, nmx);
+            atomicAdd(&dcnt[d], 1u);
+        }
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            const uint32_t nw  = blockDim.x >> 5, l = threadIdx.x;
+            const uint32_t bd  = l < nw ? s_d[l] : 0xFFFFFFFFu;
+            const int32_t  bmn = l < nw ? s_mn[l] : 0x7FFFFFFF, bnmx = l < nw ? s_nmx[l] : 0x7FFFFFFF;
+            const uint32_t bn  = l < nw && bd < 0xFFFFFFFEu ? s_n[l] : 0u;
+            const uint32_t b0d = __reduce_min_sync(0xFFFFFFFFu, bd);
+            if (__all_sync(0xFFFFFFFFu, bd == b0d || bd == 0xFFFFFFFFu)) { /* the block's edges: one draw */
+                const int32_t  m = __reduce_min_sync(0xFFFFFFFFu, bmn), n = __reduce_min_sync(0xFFFFFFFFu, bnmx);
+                const uint32_t c = __reduce_add_sync(0xFFFFFFFFu, bn);
+                if (l == 0 && b0d < 0xFFFFFFFEu) {
+                    atomicMin(&dbox[b0d].x, m);
+                    atomicMin(&dbox[b0d].y, n);
+                    atomicAdd(&dcnt[b0d], c);
+                }
+            } else if (bd < 0xFFFFFFFEu) {
+                atomicMin(&dbox[bd].x, bmn);
+                atomicMin(&dbox[bd].y, bnmx);
+                atomicAdd(&dcnt[bd], bn);
+            }
         }
     }
     if (!ok)
@@ -276,6 +306,56 @@ __global__ void gb_bin_edges(uint32_t nedges, const int4 *__restrict__ edges, co
         uint32_t slot = atomicAdd(&c[(size_t)b * sf->ndraws], 1u);
         if (SCATTER && slot < nunits)
             recs[slot] = ed;
+    }
+}
+
+/* The mean width of a frame's fill and stroke draws, clipped to the surface
+   (W pixels), weighted by their edges (the draws that carry the raster's
+   work decide): stats[0] += width x edges, stats[1] += edges.  It picks the
+   raster's tile form. */
+__device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        v += __shfl_xor_sync(0xFFFFFFFFu, v, o);
+    return v;
+}
+__global__ void gb_draw_width_stats(uint32_t ndraws, const gb_draw *__restrict__ draws, const int2 *__restrict__ dbox,
+                                    const uint32_t *__restrict__ dcnt, int32_t W,
+                                    unsigned long long *__restrict__ stats) {
+    const uint32_t     d = blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned long long w = 0, n = 0;
+    if (d < ndraws && draws[d].kind <= GB_DRAW_STROKE) {
+        const int2    b  = dbox[d];
+        const int32_t lo = max(0, min(W, b.x >> 8)), hi = max(0, min(W, ((-b.y) >> 8) + 1));
+        if (b.x <= -b.y) {
+            n = dcnt[d];
+            w = (unsigned long long)max(0, hi - lo) * n;
+        }
+    }
+    w = warp_sum_u64(w);
+    n = warp_sum_u64(n);
+    if ((threadIdx.x & 31u) == 0 && n) {
+        atomicAdd(&stats[0], w);
+        atomicAdd(&stats[1], n);
+    }
+}
+
+/* *mx = max(*mx, the largest cell count): the heaviest (band, draw) cell,
+   which one raster CTA works through on its own */
+__global__ void gb_cells_max(uint32_t ncells, const uint32_t *__restrict__ cnt, uint32_t *__restrict__ mx) {
+    __shared__ uint32_t s_m[32];
+    uint32_t            m = 0;
+    for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < ncells; c += (size_t)gridDim.x * blockDim.x)
+        m = max(m, cnt[c]);
+    m = __reduce_max_sync(0xFFFFFFFFu, m);
+    if ((threadIdx.x & 31u) == 0)
+        s_m[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        m = threadIdx.x < (blockDim.x >> 5) ? s_m[threadIdx.x] : 0u;
+        m = __reduce_max_sync(0xFFFFFFFFu, m);
+        if (threadIdx.x == 0 && m)
+            atomicMax(mx, m);
     }
 }
 
@@ -350,14 +430,14 @@ cudaError_t gb_launch_stroke_tris(cudaStream_t st, uint32_t ntris, uint32_t ndra
 }
 cudaError_t gb_launch_bin(cudaStream_t st, int scatter, uint32_t nedges, const int4 *edges, const uint32_t *edge_draw,
                           const gb_draw *draws, const gb_surf *surfs, uint32_t samples, uint32_t *cell, int4 *recs,
-                          uint32_t nunits, int2 *dbox) {
+                          uint32_t nunits, int2 *dbox, uint32_t *dcnt) {
     if (nedges) {
         if (scatter)
             gb_bin_edges<true><<<(nedges + 255) / 256, 256, 0, st>>>(nedges, edges, edge_draw, draws, surfs, samples,
-                                                                      cell, recs, nunits, nullptr);
+                                                                      cell, recs, nunits, nullptr, nullptr);
         else
             gb_bin_edges<false><<<(nedges + 255) / 256, 256, 0, st>>>(nedges, edges, edge_draw, draws, surfs,
-                                                                       samples, cell, nullptr, 0u, dbox);
+                                                                       samples, cell, nullptr, 0u, dbox, dcnt);
     }
     return cudaGetLastError();
 }
@@ -367,6 +447,19 @@ cudaError_t gb_launch_cell_flags(cudaStream_t st, uint32_t ncells, const uint32_
         gb_cell_flags<<<(ncells + 255) / 256, 256, 0, st>>>(ncells, off, flags);
     if (ndraws)
         gb_cell_flags_every_band<<<(ndraws + 255) / 256, 256, 0, st>>>(ndraws, draws, surfs, flags);
+    return cudaGetLastError();
+}
+cudaError_t gb_launch_draw_width_stats(cudaStream_t st, uint32_t ndraws, const gb_draw *draws, const int2 *dbox,
+                                       const uint32_t *dcnt, uint32_t W, unsigned long long *stats) {
+    if (ndraws)
+        gb_draw_width_stats<<<(ndraws + 255) / 256, 256, 0, st>>>(ndraws, draws, dbox, dcnt, (int32_t)W, stats);
+    return cudaGetLastError();
+}
+cudaError_t gb_launch_cells_max(cudaStream_t st, uint32_t ncells, const uint32_t *cnt, uint32_t *mx) {
+    if (ncells) {
+        const uint32_t nb = std::min<uint32_t>((ncells + 255) / 256, 2048u);
+        gb_cells_max<<<nb, 256, 0, st>>>(ncells, cnt, mx);
+    }
     return cudaGetLastError();
 }
 cudaError_t gb_launch_cell_compact(cudaStream_t st, uint32_t ncells, const uint32_t *pos, uint32_t *alist) {
