@@ -587,7 +587,7 @@ def main():
         ta = (C.c_void_p * len(btarget))(*[s2.h for s2 in btarget])
         bt = L.vkvg_gb300_batch_create(fa, ta, len(bframes))
         assert bt
-        for _ in range(10):  # sizing, eight tuning runs, graph capture
+        for _ in range(12):  # sizing, ten tuning runs, graph capture
             assert L.vkvg_gb300_batch_execute(bt) == 0
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -603,7 +603,7 @@ def main():
                  "plain_ms": plain_s * 1e3, "plain_paths_per_s": bpaths / plain_s, "batch_ms": batch_s * 1e3,
                  "batch_paths_per_s": bpaths / batch_s, "speedup": plain_s / batch_s,
                  "graph_replay": bool(bt_info[1]), "tuned_stage_min": int(bt_info[2]),
-                 "tuned_heaviest_first": bool(bt_info[3]), "tuned_tile_px": 256 if bt_info[8] else 1024,
+                 "tuned_heaviest_first": bool(bt_info[3]), "tuned_tile_px": int(bt_info[8]),
                  "work_items": int(bt_info[4]),
                  "first_8_surfaces_equal_to_plain": same,
                  "note": "host timer, device-resident frames; the plain form executes the 64 captured frames one "

@@ -158,7 +158,7 @@ vkvg_public vkvg_status_t vkvg_gb300_exclusive_scan_noalloc(void *stream, const 
  * (vkvg_gb300_frame_capture), each for its own surface, rendered as one job:
  * one pass of the geometry kernels over all of them and one persistent
  * raster launch over every surface's bands, heaviest first.  The first
- * execution sizes the job, the next eight time candidate raster settings
+ * execution sizes the job, the next ten time candidate raster settings
  * (tile width, stage threshold, work-list order; kept per class of scene
  * for later batches), later ones replay a CUDA
  * graph of the whole job.  Frames with clip or pattern sources, or a surface
@@ -166,7 +166,7 @@ vkvg_public vkvg_status_t vkvg_gb300_exclusive_scan_noalloc(void *stream, const 
  * ends as vkvg_gb300_frame_execute of its frame would leave it.
  * timing out: [0] last execution ms, [1] it was a graph replay, [2] stage
  * threshold, [3] heaviest-first order, [4] work items, [5] surfaces,
- * [6] settings tuned, [7] bin record units, [8] 256-pixel tiles. */
+ * [6] settings tuned, [7] bin record units, [8] tile width in pixels. */
 typedef struct _vkvg_gb300_batch_t *VkvgBatch;
 vkvg_public VkvgBatch     vkvg_gb300_batch_create(VkvgFrame *frames, VkvgSurface *targets, uint32_t count);
 vkvg_public vkvg_status_t vkvg_gb300_batch_execute(VkvgBatch batch);

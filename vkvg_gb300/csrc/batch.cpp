@@ -25,10 +25,10 @@ namespace {
 struct RasterParams {
     uint32_t stage_min;  /* cells of fewer record units skip the shared-memory stage */
     bool     cost_order; /* work list heaviest first (else surface, band, tile order) */
-    bool     narrow;     /* 256-pixel tiles, four CTAs per SM (else 1024-pixel tiles, one per SM) */
+    int      form;       /* tiles: 0 1024 pixels (one CTA per SM), 1 256 (four), 2 512 (two) */
 };
-const RasterParams CANDIDATES[] = {{0, true, false}, {8, true, false}, {32, true, false}, {0, false, false},
-                                   {0, true, true},  {8, true, true},  {32, true, true},  {0, false, true}};
+const RasterParams CANDIDATES[] = {{0, true, 0}, {8, true, 0}, {32, true, 0}, {0, false, 0}, {0, true, 2},
+                                   {8, true, 2}, {32, true, 2}, {0, true, 1}, {8, true, 1}, {32, true, 1}};
 constexpr int      NCAND        = sizeof(CANDIDATES) / sizeof(CANDIDATES[0]);
 
 /* the tuner's choice per class of scene: surfaces, draws and record units,
@@ -53,7 +53,7 @@ struct _vkvg_gb300_batch_t {
     std::vector<gb_surf> tab;
     DevBuf               d_tab, d_items, d_queue, d_idx, d_units;
     PinnedBuf            h_stage;
-    std::vector<uint4>   items_cost[2], items_plain[2]; /* the work lists (wide, narrow tiles) in both orders */
+    std::vector<uint4>   items_cost[3], items_plain[3]; /* the work lists (per tile form) in both orders */
     uint64_t             ncells  = 0;
     uint64_t             every   = 0; /* cells of the draws that act on every band */
     uint32_t             samples = 0;
@@ -153,9 +153,9 @@ void first_draw_init(const gb_draw *d, uint32_t n, gb_surf &s) {
 
 namespace {
 
-/* the work lists: every (surface, band, tile) for either tile width, in
+/* the work lists: every (surface, band, tile) for each tile form, in
    surface order and sorted by the band's record units (heaviest first); all
-   four kept on the device, one after another */
+   six kept on the device, one after another */
 cudaError_t build_items(VkvgBatch b) {
     Pipeline            &pl = b->pl;
     std::vector<uint64_t> idx;
@@ -174,7 +174,7 @@ cudaError_t build_items(VkvgBatch b) {
     BCK(cudaStreamSynchronize(pl.st));
     memcpy(off.data(), b->h_stage.p, n * 4);
     size_t tot = 0;
-    for (int nw = 0; nw < 2; nw++) {
+    for (int nw = 0; nw < 3; nw++) {
         const uint32_t                          tw = gb_raster_tile_width(nw);
         std::vector<std::pair<uint32_t, uint4>> costed;
         b->items_plain[nw].clear();
@@ -204,7 +204,7 @@ cudaError_t build_items(VkvgBatch b) {
     if (!b->d_items.grow(std::max<size_t>(tot * 16, 16)) || !b->h_stage.grow(std::max<size_t>(tot * 16, 64)))
         return cudaErrorMemoryAllocation;
     uint8_t *h = (uint8_t *)b->h_stage.p;
-    for (int nw = 0; nw < 2; nw++) {
+    for (int nw = 0; nw < 3; nw++) {
         memcpy(h, b->items_plain[nw].data(), b->items_plain[nw].size() * 16);
         h += b->items_plain[nw].size() * 16;
         memcpy(h, b->items_cost[nw].data(), b->items_cost[nw].size() * 16);
@@ -224,9 +224,11 @@ cudaError_t run_batch(VkvgBatch b, bool sized, const RasterParams &p) {
     BCK(pl.geometry(b->merged, b->d_tab.as<gb_surf>(), b->ncells, b->every, wide, b->samples, false, sized));
     if (!sized)
         BCK(build_items(b));
-    const int      nw   = p.narrow ? 1 : 0;
+    const int      nw   = p.form;
     const uint32_t ni   = (uint32_t)b->items_plain[nw].size();
-    const size_t   base = nw ? 2 * b->items_plain[0].size() : 0; /* this width's lists on the device */
+    size_t         base = 0; /* this form's lists on the device */
+    for (int k = 0; k < nw; k++)
+        base += 2 * b->items_plain[k].size();
     gb_raster_args A0;
     memset(&A0, 0, sizeof(A0));
     A0.S         = b->samples;
@@ -242,7 +244,7 @@ cudaError_t run_batch(VkvgBatch b, bool sized, const RasterParams &p) {
     BCK(cudaMemsetAsync(b->d_queue.p, 0, 4, pl.st));
     BCK(gb_launch_raster_batch(pl.st, &A0, b->d_tab.as<gb_surf>(),
                                b->d_items.as<uint4>() + base + (p.cost_order ? ni : 0),
-                               ni, b->d_queue.as<uint32_t>(), b->nctas, p.narrow ? 1 : 0));
+                               ni, b->d_queue.as<uint32_t>(), b->nctas, p.form));
     gb_count_launch(ni ? 1 : 0);
     return cudaMemcpyAsync(pl.rb.p, pl.status.p, 4, cudaMemcpyDeviceToHost, pl.st);
 }
@@ -406,11 +408,11 @@ vkvg_status_t vkvg_gb300_batch_timing(VkvgBatch b, float out[9]) {
     out[1] = b->last_graph ? 1.f : 0.f;
     out[2] = (float)b->params.stage_min;
     out[3] = b->params.cost_order ? 1.f : 0.f;
-    out[4] = (float)b->items_plain[b->params.narrow ? 1 : 0].size();
+    out[4] = (float)b->items_plain[b->params.form].size();
     out[5] = (float)b->tab.size();
     out[6] = b->tuned ? 1.f : 0.f;
     out[7] = (float)b->pl.nunits;
-    out[8] = b->params.narrow ? 1.f : 0.f;
+    out[8] = (float)gb_raster_tile_width(b->params.form);
     return VKVG_STATUS_SUCCESS;
 }
 

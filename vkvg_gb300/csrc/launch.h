@@ -127,16 +127,16 @@ cudaError_t gb_launch_cell_compact(cudaStream_t st, uint32_t ncells, const uint3
    1024-pixel one (16 warps, one CTA per SM); clipping frames run the latter */
 cudaError_t gb_launch_raster(cudaStream_t st, const gb_raster_args *a, const gb_clip_args *c, int gradients,
                              int clipping, int narrow);
-/* pixels per raster tile of either form */
-uint32_t gb_raster_tile_width(int narrow);
+/* pixels per raster tile of a form: 0 wide (1024), 1 narrow (256), 2 middle (512) */
+uint32_t gb_raster_tile_width(int form);
 /* out[i] = src[idx[i]] */
 cudaError_t gb_launch_gather_u32(cudaStream_t st, uint32_t n, const uint64_t *idx, const uint32_t *src,
                                  uint32_t *out);
 /* the persistent batch raster over a work list of (surface, band, tile, -)
    items (queue: a zeroed counter), nctas SMs' worth of CTAs, tiles of the
-   form narrow selects */
+   given form (as gb_raster_tile_width) */
 cudaError_t gb_launch_raster_batch(cudaStream_t st, const gb_raster_args *a, const gb_surf *surfs, const uint4 *items,
-                                   uint32_t nitems, uint32_t *queue, uint32_t nctas, int narrow);
+                                   uint32_t nitems, uint32_t *queue, uint32_t nctas, int form);
 cudaError_t gb_launch_pmath_eval(cudaStream_t st, int fn, const float *a, const float *b, float *out, uint64_t n);
 }
 

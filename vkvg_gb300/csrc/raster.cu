@@ -60,18 +60,19 @@
    surfaces whose draws span most of a tile; the narrow form (4 warps, 256
    pixels, four CTAs per SM) suits small draws and narrow surfaces, where
    the wide form's warps would wait at each draw's barrier with nothing to
-   blend. */
+   blend; the middle form (8 warps, 512 pixels, two CTAs per SM) sits
+   between them for the batch tuner. */
 template <int NW> struct XT {
     static constexpr int W         = 64 * NW;
     static constexpr int THREADS   = 32 * NW;
-    static constexpr int MINB      = NW >= 16 ? 1 : 4; /* CTAs per SM */
+    static constexpr int MINB      = NW >= 16 ? 1 : NW >= 8 ? 2 : 4; /* CTAs per SM */
     static constexpr int PLANE     = GB_BAND_ROWS * W; /* one crossing counter per tile sample */
     static constexpr int TOT_ROW   = NW + 4;           /* strip totals per row, padded against bank conflicts */
     static constexpr int TOT_SET   = GB_BAND_ROWS * TOT_ROW;
     static constexpr int S_TOT     = 2 * PLANE;
     static constexpr int S_FLAG    = S_TOT + 3 * TOT_SET;
     static constexpr int S_WORDS   = S_FLAG + 2 * NW;
-    static constexpr int STAGE_CAP = NW >= 16 ? 2048 : 512; /* units per staging buffer */
+    static constexpr int STAGE_CAP = 128 * NW; /* units per staging buffer */
     static constexpr int S_STAGE   = S_WORDS;
     static constexpr int S_CUR     = S_STAGE + 2 * STAGE_CAP * 4;
     static constexpr int S_MBAR    = S_CUR + NW * 192;
@@ -81,6 +82,7 @@ template <int NW> struct XT {
     static_assert(MINB * (SMEM + 1024) <= 232448, "shared memory of the CTAs an SM holds");
 };
 #define XT_WIDE   16
+#define XT_MID    8
 #define XT_NARROW 4
 #define WAIT_LIMIT  (1u << 20) /* mbarrier polls before a staged copy counts as lost */
 
@@ -1104,14 +1106,19 @@ template <int NW, bool GRAD, bool CLIP> cudaError_t raster_nw(cudaStream_t st, c
     return cudaGetLastError();
 }
 
-extern "C" uint32_t gb_raster_tile_width(int narrow) { return narrow ? XT<XT_NARROW>::W : XT<XT_WIDE>::W; }
+extern "C" uint32_t gb_raster_tile_width(int form) {
+    return form == 1 ? XT<XT_NARROW>::W : form == 2 ? XT<XT_MID>::W : XT<XT_WIDE>::W;
+}
 extern "C" cudaError_t gb_launch_raster_batch(cudaStream_t st, const gb_raster_args *a, const gb_surf *surfs,
                                              const uint4 *items, uint32_t nitems, uint32_t *queue, uint32_t nctas,
-                                             int narrow) {
+                                             int form) {
     if (!nitems)
         return cudaSuccess;
-    return narrow ? raster_batch_nw<XT_NARROW>(st, a, surfs, items, nitems, queue, nctas)
-                  : raster_batch_nw<XT_WIDE>(st, a, surfs, items, nitems, queue, nctas);
+    if (form == 1)
+        return raster_batch_nw<XT_NARROW>(st, a, surfs, items, nitems, queue, nctas);
+    if (form == 2)
+        return raster_batch_nw<XT_MID>(st, a, surfs, items, nitems, queue, nctas);
+    return raster_batch_nw<XT_WIDE>(st, a, surfs, items, nitems, queue, nctas);
 }
 /* frames without gradient draws or clipping run the variants without that
    code; frames with clipping run the wide form */
