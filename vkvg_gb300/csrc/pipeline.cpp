@@ -371,12 +371,12 @@ cudaError_t Pipeline::geometry(const FrameHost &f, const gb_surf *surfs, uint64_
         memcpy(ws, (uint8_t *)rb.p + 8, 16);
         memcpy(&mxc, (uint8_t *)rb.p + 24, 4);
         nunits = hv[0];
-        /* narrow tiles when every cell fits the narrow form's staging buffer
+        /* narrow tiles when every cell fits the narrow form's staging buffer (480 units)
            (a heavy cell is one CTA's serial work: the wide form's 512 threads
            finish it sooner) and the draws that carry the edges are small next
            to a wide tile, or the surface is no wider than a narrow one */
         const bool small = !wide || (ws[1] && ws[0] <= 384u * ws[1]);
-        narrow           = stats && mxc <= 512u && small;
+        narrow           = stats && mxc <= 480u && small;
     }
     GROW(recs, (size_t)(nunits + 1) * 16);
     /* cells <- offsets (kept for the raster), cursor <- running copy */

@@ -72,12 +72,16 @@ template <int NW> struct XT {
     static constexpr int S_TOT     = 2 * PLANE;
     static constexpr int S_FLAG    = S_TOT + 3 * TOT_SET;
     static constexpr int S_WORDS   = S_FLAG + 2 * NW;
-    static constexpr int STAGE_CAP = 128 * NW; /* units per staging buffer */
+    static constexpr int STAGE_CAP = NW >= 8 ? 128 * NW : 480; /* units per staging buffer */
     static constexpr int S_STAGE   = S_WORDS;
     static constexpr int S_CUR     = S_STAGE + 2 * STAGE_CAP * 4;
     static constexpr int S_MBAR    = S_CUR + NW * 192;
     static constexpr int S_RG      = S_MBAR + 4;
-    static constexpr int SMEM      = (S_RG + 8) * 4;
+    /* narrow form: the band's 4 pixel rows of the current gradient source
+       image (4x MSAA), staged once per source instead of loaded per sample */
+    static constexpr int GC        = NW == 4 ? 4 * W : 0;
+    static constexpr int S_GC      = S_RG + 8;
+    static constexpr int SMEM      = (S_GC + GC) * 4;
     static_assert(S_STAGE % 4 == 0 && S_MBAR % 2 == 0, "staging buffers 16-byte, mbarriers 8-byte aligned");
     static_assert(MINB * (SMEM + 1024) <= 232448, "shared memory of the CTAs an SM holds");
 };
@@ -518,6 +522,11 @@ __device__ __forceinline__ void raster_item(const gb_raster_args &A, const gb_cl
     };
 
     uint32_t    nproc = 0; /* draws with geometry in this band so far */
+    /* gradient rows staged in shared memory (narrow form, 4x MSAA): which
+       source they hold, and this lane's row of them */
+    const bool      gc_on  = GRAD && X::GC > 0 && A.S == 4 && !dbg;
+    uint32_t        gc_gs  = 0;
+    const uint32_t *gc_row = reinterpret_cast<const uint32_t *>(smem + X::S_GC) + (rl >> 2) * X::W + col0;
     uint32_t   *ct    = reinterpret_cast<uint32_t *>(smem + X::S_CUR + wi * 192);
     draw_cursor cur;
     cur.i0 = (uint32_t)smem[X::S_RG + 7];
@@ -529,6 +538,18 @@ __device__ __forceinline__ void raster_item(const gb_raster_args &A, const gb_cl
             const uint32_t d = nx_d, kind = nx_kind, lo = nx_lo, hi = nx_hi;
             const uint32_t src = ct[96 + nx_slot], op = ct[128 + nx_slot], gs = ct[160 + nx_slot];
             nx_have = cur_next<NW, CLIP>(cur, A, cb, smem, l, ct, &nx_d, &nx_kind, &nx_lo, &nx_hi, &nx_slot); /* lookahead */
+            if (gc_on && gs && gs != gc_gs) {
+                /* a new gradient source: once every warp is done with the
+                   old rows, the tile's pixel rows of this one */
+                __syncthreads();
+                uint32_t *gc = reinterpret_cast<uint32_t *>(smem + X::S_GC);
+                for (uint32_t i = t; i < (uint32_t)X::GC; i += X::THREADS) {
+                    const uint32_t pr = i / X::W, px = i % X::W, py = band * 4 + pr;
+                    gc[i] = ((int32_t)px < TW && py < A.H) ? grad_row(A, gs, py, X0 + (int32_t)px)[0] : 0u;
+                }
+                __syncthreads();
+                gc_gs = gs;
+            }
             int            bm;
             if (kind == GB_DRAW_PAINT) {
                 const blend_k B = make_blend(src, op, &bm);
@@ -538,7 +559,8 @@ __device__ __forceinline__ void raster_item(const gb_raster_args &A, const gb_cl
                     continue;
                 }
                 if (GRAD && gs)
-                    uniform_run<BM_ADD, GRAD, CLIP>(col, 1, B, grad_row(A, gs, R / rpp, X0 + col0), ncols, cm);
+                    uniform_run<BM_ADD, GRAD, CLIP>(col, 1, B, gc_on ? gc_row : grad_row(A, gs, R / rpp, X0 + col0),
+                                                    ncols, cm);
                 else if (bm == BM_ADD)
                     uniform_run<BM_ADD, false, CLIP>(col, 1, B, nullptr, ncols, cm);
                 else if (bm == BM_SADD)
@@ -683,7 +705,8 @@ __device__ __forceinline__ void raster_item(const gb_raster_args &A, const gb_cl
                 if (!__any_sync(0xffffffffu, k > 0))
                     continue;
                 if (GRAD && gs)
-                    uniform_run<BM_ADD, GRAD, CLIP>(col, k, B, grad_row(A, gs, R / rpp, X0 + col0), ncols, cm);
+                    uniform_run<BM_ADD, GRAD, CLIP>(col, k, B, gc_on ? gc_row : grad_row(A, gs, R / rpp, X0 + col0),
+                                                    ncols, cm);
                 else if (bm == BM_ADD)
                     uniform_run<BM_ADD, false, CLIP>(col, k, B, nullptr, ncols, cm);
                 else if (bm == BM_SADD)
@@ -712,7 +735,7 @@ __device__ __forceinline__ void raster_item(const gb_raster_args &A, const gb_cl
             } else if (__any_sync(0xffffffffu, work)) {
                 const int32_t fmask = kind == GB_DRAW_FILL_EO ? 1 : -1;
                 if (GRAD && gs) {
-                    const uint32_t *grow = grad_row(A, gs, R / rpp, X0 + col0);
+                    const uint32_t *grow = gc_on ? gc_row : grad_row(A, gs, R / rpp, X0 + col0);
                     if (kind == GB_DRAW_STROKE)
                         stroke_run<BM_ADD, GRAD, CLIP>(col, cp, v_lane, E, B, grow, ncols, cm);
                     else
