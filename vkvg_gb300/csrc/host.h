@@ -106,7 +106,7 @@ struct Pipeline {
     uint32_t npts = 0, nev = 0, nverts = 0, ninds = 0, nedges = 0, ntris = 0, nunits = 0, nbands = 0;
     uint32_t dev_status = 0;
     uint32_t stats_w    = 0;     /* surface width of a one-surface frame: geometry measures its draws' widths */
-    bool     narrow     = false; /* the last frame's raster form (256-pixel tiles) */
+    int      narrow     = 0; /* the last frame's raster form: 0 1024-pixel, 1 256-pixel, 2 128-pixel tiles */
     uint64_t launches   = 0;
     uint64_t upload_bytes = 0;
     float    ms[5]      = {0, 0, 0, 0, 0};

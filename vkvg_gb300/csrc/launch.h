@@ -123,11 +123,12 @@ cudaError_t gb_launch_cells_max(cudaStream_t st, uint32_t ncells, const uint32_t
 /* alist[pos[c]] = c for the cells whose pos[c + 1] != pos[c] */
 cudaError_t gb_launch_cell_compact(cudaStream_t st, uint32_t ncells, const uint32_t *pos, uint32_t *alist);
 
-/* narrow: the 256-pixel raster form (4 warps, 4 CTAs per SM) instead of the
-   1024-pixel one (16 warps, one CTA per SM); clipping frames run the latter */
+/* narrow: 1 the 256-pixel raster form (4 warps, 4 CTAs per SM), 2 the
+   128-pixel one (2 warps, 8 CTAs per SM), 0 the 1024-pixel one (16 warps,
+   one CTA per SM); clipping frames run the last */
 cudaError_t gb_launch_raster(cudaStream_t st, const gb_raster_args *a, const gb_clip_args *c, int gradients,
                              int clipping, int narrow);
-/* pixels per raster tile of a form: 0 wide (1024), 1 narrow (256), 2 middle (512) */
+/* pixels per raster tile of a form: 0 wide (1024), 1 narrow (256), 2 middle (512), 3 tiny (128) */
 uint32_t gb_raster_tile_width(int form);
 /* out[i] = src[idx[i]] */
 cudaError_t gb_launch_gather_u32(cudaStream_t st, uint32_t n, const uint64_t *idx, const uint32_t *src,

@@ -371,12 +371,13 @@ cudaError_t Pipeline::geometry(const FrameHost &f, const gb_surf *surfs, uint64_
         memcpy(ws, (uint8_t *)rb.p + 8, 16);
         memcpy(&mxc, (uint8_t *)rb.p + 24, 4);
         nunits = hv[0];
-        /* narrow tiles when every cell fits the narrow form's staging buffer (480 units)
+        /* narrow tiles (256 pixels; 128 when every cell fits 128 units) when
+           every cell fits the narrow form's staging buffer (480 units)
            (a heavy cell is one CTA's serial work: the wide form's 512 threads
            finish it sooner) and the draws that carry the edges are small next
            to a wide tile, or the surface is no wider than a narrow one */
         const bool small = !wide || (ws[1] && ws[0] <= 384u * ws[1]);
-        narrow           = stats && mxc <= 480u && small;
+        narrow           = !(stats && small) ? 0 : mxc <= 128u ? 2 : mxc <= 480u ? 1 : 0;
     }
     GROW(recs, (size_t)(nunits + 1) * 16);
     /* cells <- offsets (kept for the raster), cursor <- running copy */
@@ -424,7 +425,7 @@ cudaError_t Pipeline::run(const FrameHost &f, _vkvg_surface_t *surf, bool timing
     for (const gb_draw &d : f.draws)
         every += d.kind > GB_DRAW_STROKE ? nbands : 0u;
     stats_w = W;
-    CK(geometry(f, surf_tab.as<gb_surf>(), (uint64_t)nbands * ndraw, every, W > gb_raster_tile_width(1), S, timing,
+    CK(geometry(f, surf_tab.as<gb_surf>(), (uint64_t)nbands * ndraw, every, W > gb_raster_tile_width(3), S, timing,
                 false));
     stats_w = 0;
 
@@ -544,7 +545,7 @@ cudaError_t Pipeline::run(const FrameHost &f, _vkvg_surface_t *surf, bool timing
         gb_count_launch(ngrad);
         A.gsrc = gsrc.as<uint32_t>();
     }
-    CK(gb_launch_raster(st, &A, &CA, ngrad > 0, clip_use, narrow && !clip_use));
+    CK(gb_launch_raster(st, &A, &CA, ngrad > 0, clip_use, clip_use ? 0 : narrow));
     surf->clip_active = act;
     surf->save_nz     = snz;
     gb_count_launch(1);

@@ -65,21 +65,21 @@
 template <int NW> struct XT {
     static constexpr int W         = 64 * NW;
     static constexpr int THREADS   = 32 * NW;
-    static constexpr int MINB      = NW >= 16 ? 1 : NW >= 8 ? 2 : 4; /* CTAs per SM */
+    static constexpr int MINB      = NW >= 16 ? 1 : NW >= 8 ? 2 : NW >= 4 ? 4 : 8; /* CTAs per SM */
     static constexpr int PLANE     = GB_BAND_ROWS * W; /* one crossing counter per tile sample */
-    static constexpr int TOT_ROW   = NW + 4;           /* strip totals per row, padded against bank conflicts */
+    static constexpr int TOT_ROW   = (NW + 7) / 4 * 4; /* strip totals per row, padded (int4 rows, bank spread) */
     static constexpr int TOT_SET   = GB_BAND_ROWS * TOT_ROW;
     static constexpr int S_TOT     = 2 * PLANE;
     static constexpr int S_FLAG    = S_TOT + 3 * TOT_SET;
     static constexpr int S_WORDS   = S_FLAG + 2 * NW;
-    static constexpr int STAGE_CAP = NW >= 8 ? 128 * NW : 480; /* units per staging buffer */
+    static constexpr int STAGE_CAP = NW >= 8 ? 128 * NW : NW >= 4 ? 480 : 128; /* units per staging buffer */
     static constexpr int S_STAGE   = S_WORDS;
     static constexpr int S_CUR     = S_STAGE + 2 * STAGE_CAP * 4;
     static constexpr int S_MBAR    = S_CUR + NW * 192;
     static constexpr int S_RG      = S_MBAR + 4;
     /* narrow form: the band's 4 pixel rows of the current gradient source
        image (4x MSAA), staged once per source instead of loaded per sample */
-    static constexpr int GC        = NW == 4 ? 4 * W : 0;
+    static constexpr int GC        = NW <= 4 ? 4 * W : 0;
     static constexpr int S_GC      = S_RG + 8;
     static constexpr int SMEM      = (S_GC + GC) * 4;
     static_assert(S_STAGE % 4 == 0 && S_MBAR % 2 == 0, "staging buffers 16-byte, mbarriers 8-byte aligned");
@@ -88,6 +88,7 @@ template <int NW> struct XT {
 #define XT_WIDE   16
 #define XT_MID    8
 #define XT_NARROW 4
+#define XT_TINY   2
 #define WAIT_LIMIT  (1u << 20) /* mbarrier polls before a staged copy counts as lost */
 
 #define BM_ADD  0 /* valid premultiplied source: exact on the FMA pipe */
@@ -668,7 +669,7 @@ __device__ __forceinline__ void raster_item(const gb_raster_args &A, const gb_cl
             {
                 const int4 *tr4 = reinterpret_cast<const int4 *>(tot + rl * X::TOT_ROW);
 #pragma unroll
-                for (int q = 0; q < NW / 4; q++) {
+                for (int q = 0; q < (NW + 3) / 4; q++) {
                     const int4 v = tr4[q];
                     Er += (4 * q > (int)wi ? v.x : 0) + (4 * q + 1 > (int)wi ? v.y : 0) +
                           (4 * q + 2 > (int)wi ? v.z : 0) + (4 * q + 3 > (int)wi ? v.w : 0);
@@ -1130,7 +1131,7 @@ template <int NW, bool GRAD, bool CLIP> cudaError_t raster_nw(cudaStream_t st, c
 }
 
 extern "C" uint32_t gb_raster_tile_width(int form) {
-    return form == 1 ? XT<XT_NARROW>::W : form == 2 ? XT<XT_MID>::W : XT<XT_WIDE>::W;
+    return form == 1 ? XT<XT_NARROW>::W : form == 2 ? XT<XT_MID>::W : form == 3 ? XT<XT_TINY>::W : XT<XT_WIDE>::W;
 }
 extern "C" cudaError_t gb_launch_raster_batch(cudaStream_t st, const gb_raster_args *a, const gb_surf *surfs,
                                              const uint4 *items, uint32_t nitems, uint32_t *queue, uint32_t nctas,
@@ -1151,6 +1152,8 @@ extern "C" cudaError_t gb_launch_raster(cudaStream_t st, const gb_raster_args *a
         return cudaSuccess;
     if (clipping)
         return gradients ? raster_nw<XT_WIDE, true, true>(st, a, c) : raster_nw<XT_WIDE, false, true>(st, a, c);
+    if (narrow == 2)
+        return gradients ? raster_nw<XT_TINY, true, false>(st, a, c) : raster_nw<XT_TINY, false, false>(st, a, c);
     if (narrow)
         return gradients ? raster_nw<XT_NARROW, true, false>(st, a, c) : raster_nw<XT_NARROW, false, false>(st, a, c);
     return gradients ? raster_nw<XT_WIDE, true, false>(st, a, c) : raster_nw<XT_WIDE, false, false>(st, a, c);
