@@ -9,6 +9,7 @@
 #include "launch.h"
 
 #include <algorithm>
+#include <utility>
 #include <cstdio>
 
 static std::atomic<uint64_t> g_launches{0};
@@ -334,9 +335,14 @@ cudaError_t Pipeline::geometry(const FrameHost &f, const gb_surf *surfs, uint64_
                              tri_draw.as<uint32_t>(), tri_idx.as<uint4>(), edges.as<int4>() + nedges,
                              edge_draw.as<uint32_t>() + nedges));
     gb_count_launch((nedges ? 1 : 0) + (ntris ? 2 : 0));
-    GROW(cells, (ncells + 1) * 4);
-    GROW(cursor, (ncells + 1) * 4);
+    /* cells: the counts; cursor: one zero, then their exclusive scan, which
+       the scatter pass advances in place, so that afterwards cursor[c] is
+       the first record of cell c (the scatter leaves slot c + 1 at the end
+       of cell c); the two buffers then swap names */
+    GROW(cells, (ncells + 2) * 4);
+    GROW(cursor, (ncells + 2) * 4);
     CK(cudaMemsetAsync(cells.p, 0, (ncells + 1) * 4, st));
+    CK(cudaMemsetAsync(cursor.p, 0, 4, st));
     /* per draw: (min x, -max x) from 0x7F7F7F7F, then its edge count from 0 */
     uint32_t *dcnt = nullptr;
     if (wide) {
@@ -359,9 +365,9 @@ cudaError_t Pipeline::geometry(const FrameHost &f, const gb_surf *surfs, uint64_
         CK(gb_launch_cells_max(st, (uint32_t)ncells, cells.as<uint32_t>(), status.as<uint32_t>() + 8));
         gb_count_launch((wide && ndraw ? 1 : 0) + (ncells ? 1 : 0));
     }
-    CK(scan(*this, cells.as<uint32_t>(), (uint32_t)ncells, cursor.as<uint32_t>()));
+    CK(scan(*this, cells.as<uint32_t>(), (uint32_t)ncells, cursor.as<uint32_t>() + 1));
     if (!sized) {
-        CK(cudaMemcpyAsync(rb.p, cursor.as<uint32_t>() + ncells, 4, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(rb.p, cursor.as<uint32_t>() + 1 + ncells, 4, cudaMemcpyDeviceToHost, st));
         if (stats)
             CK(cudaMemcpyAsync((uint8_t *)rb.p + 8, status.as<uint32_t>() + 4, 20, cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
@@ -380,11 +386,10 @@ cudaError_t Pipeline::geometry(const FrameHost &f, const gb_surf *surfs, uint64_
         narrow           = !(stats && small) ? 0 : mxc <= 128u ? 2 : mxc <= 480u ? 1 : 0;
     }
     GROW(recs, (size_t)(nunits + 1) * 16);
-    /* cells <- offsets (kept for the raster), cursor <- running copy */
-    CK(cudaMemcpyAsync(cells.p, cursor.p, (ncells + 1) * 4, cudaMemcpyDeviceToDevice, st));
     CK(gb_launch_bin(st, 1, nedge_all, edges.as<int4>(), edge_draw.as<uint32_t>(), draws, surfs, S,
-                     cursor.as<uint32_t>(), recs.as<int4>(), nunits, nullptr, nullptr));
+                     cursor.as<uint32_t>() + 1, recs.as<int4>(), nunits, nullptr, nullptr));
     gb_count_launch(nedge_all ? 1 : 0);
+    std::swap(cells, cursor); /* cells <- the offsets (kept for the raster); cursor is free */
     /* the raster's per-band draw lists: the active cells, band-major, in
        draw order (the cursor copy is free again and holds the flags) */
     GROW(apos, (ncells + 1) * 4);
