@@ -46,6 +46,9 @@ cudaError_t gb_launch_unpremultiply(cudaStream_t st, const uint32_t *in, size_t 
                                     uint32_t *out);
 size_t      gb_scan_scratch_words(uint32_t n);
 cudaError_t gb_exclusive_scan(cudaStream_t st, const uint32_t *in, uint32_t n, uint32_t *out, uint32_t *scratch);
+/* exclusive scan of (in != 0): positions of the nonzero entries, out[n] their count */
+cudaError_t gb_exclusive_scan_flags(cudaStream_t st, const uint32_t *in, uint32_t n, uint32_t *out,
+                                    uint32_t *scratch);
 
 cudaError_t gb_launch_flatten_count(cudaStream_t st, uint32_t nseg, const uint32_t *info, const float4 *a,
                                     const float4 *b, const float4 *c, const uint32_t *n, const uint32_t *aux,
@@ -111,8 +114,10 @@ cudaError_t gb_launch_stroke_tris(cudaStream_t st, uint32_t ntris, uint32_t ndra
 cudaError_t gb_launch_bin(cudaStream_t st, int scatter, uint32_t nedges, const int4 *edges, const uint32_t *edge_draw,
                           const gb_draw *draws, const gb_surf *surfs, uint32_t samples, uint32_t *cell, int4 *recs,
                           uint32_t nunits, int2 *dbox, uint32_t *dcnt);
-/* flags[c] = 1 for the cells the raster visits: cells with records, and every
-   band's cell of the draws that act on all bands (kinds after STROKE) */
+/* flags[c] = 1 for the cells the raster visits: cells with records (from the
+   offsets off, skipped when null: flags then already holds the cells'
+   record counts), and every band's cell of the draws that act on all bands
+   (kinds after STROKE) */
 cudaError_t gb_launch_cell_flags(cudaStream_t st, uint32_t ncells, const uint32_t *off, uint32_t ndraws,
                                  const gb_draw *draws, const gb_surf *surfs, uint32_t *flags);
 /* stats[0] += clipped pixel width x edges of each fill and stroke draw, stats[1] += its edges */

@@ -391,14 +391,19 @@ cudaError_t Pipeline::geometry(const FrameHost &f, const gb_surf *surfs, uint64_
     gb_count_launch(nedge_all ? 1 : 0);
     std::swap(cells, cursor); /* cells <- the offsets (kept for the raster); cursor is free */
     /* the raster's per-band draw lists: the active cells, band-major, in
-       draw order (the cursor copy is free again and holds the flags) */
+       draw order, from the cells' record counts (now in cursor, a nonzero
+       count marks an active cell) and the every-band draws' cells */
     GROW(apos, (ncells + 1) * 4);
-    CK(gb_launch_cell_flags(st, (uint32_t)ncells, cells.as<uint32_t>(), ndraw, draws, surfs, cursor.as<uint32_t>()));
-    CK(scan(*this, cursor.as<uint32_t>(), (uint32_t)ncells, apos.as<uint32_t>()));
+    CK(gb_launch_cell_flags(st, (uint32_t)ncells, nullptr, ndraw, draws, surfs, cursor.as<uint32_t>()));
+    if (!scratch.grow(gb_scan_scratch_words((uint32_t)ncells) * 4 + 64))
+        return cudaErrorMemoryAllocation;
+    CK(gb_exclusive_scan_flags(st, cursor.as<uint32_t>(), (uint32_t)ncells, apos.as<uint32_t>(),
+                               scratch.as<uint32_t>()));
+    gb_count_launch(ncells ? 3 : 0);
     /* an active cell holds a record unit or belongs to an every-band draw */
     GROW(alist, (size_t)(nunits + every_cells + 1) * 4);
     CK(gb_launch_cell_compact(st, (uint32_t)ncells, apos.as<uint32_t>(), alist.as<uint32_t>()));
-    gb_count_launch(ncells ? 2 : 0);
+    gb_count_launch(ncells ? 1 : 0);
     gb_count_launch(ndraw ? 1 : 0);
     if (timing)
         CK(cudaEventRecord(evs[3], st));

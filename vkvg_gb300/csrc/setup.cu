@@ -443,7 +443,7 @@ cudaError_t gb_launch_bin(cudaStream_t st, int scatter, uint32_t nedges, const i
 }
 cudaError_t gb_launch_cell_flags(cudaStream_t st, uint32_t ncells, const uint32_t *off, uint32_t ndraws,
                                  const gb_draw *draws, const gb_surf *surfs, uint32_t *flags) {
-    if (ncells)
+    if (ncells && off)
         gb_cell_flags<<<(ncells + 255) / 256, 256, 0, st>>>(ncells, off, flags);
     if (ndraws)
         gb_cell_flags_every_band<<<(ndraws + 255) / 256, 256, 0, st>>>(ndraws, draws, surfs, flags);
