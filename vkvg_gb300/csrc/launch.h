@@ -114,12 +114,11 @@ cudaError_t gb_launch_stroke_tris(cudaStream_t st, uint32_t ntris, uint32_t ndra
 cudaError_t gb_launch_bin(cudaStream_t st, int scatter, uint32_t nedges, const int4 *edges, const uint32_t *edge_draw,
                           const gb_draw *draws, const gb_surf *surfs, uint32_t samples, uint32_t *cell, int4 *recs,
                           uint32_t nunits, int2 *dbox, uint32_t *dcnt);
-/* flags[c] = 1 for the cells the raster visits: cells with records (from the
-   offsets off, skipped when null: flags then already holds the cells'
-   record counts), and every band's cell of the draws that act on all bands
-   (kinds after STROKE) */
-cudaError_t gb_launch_cell_flags(cudaStream_t st, uint32_t ncells, const uint32_t *off, uint32_t ndraws,
-                                 const gb_draw *draws, const gb_surf *surfs, uint32_t *flags);
+/* counts[c] = 1 in every band's cell of the draws that act on all bands
+   (kinds after STROKE): with the cells' record counts, the cells the raster
+   visits are then the nonzero entries */
+cudaError_t gb_launch_cell_flags(cudaStream_t st, uint32_t ndraws, const gb_draw *draws, const gb_surf *surfs,
+                                 uint32_t *counts);
 /* stats[0] += clipped pixel width x edges of each fill and stroke draw, stats[1] += its edges */
 cudaError_t gb_launch_draw_width_stats(cudaStream_t st, uint32_t ndraws, const gb_draw *draws, const int2 *dbox,
                                        const uint32_t *dcnt, uint32_t W, unsigned long long *stats);

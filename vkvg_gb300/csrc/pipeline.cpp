@@ -394,7 +394,7 @@ cudaError_t Pipeline::geometry(const FrameHost &f, const gb_surf *surfs, uint64_
        draw order, from the cells' record counts (now in cursor, a nonzero
        count marks an active cell) and the every-band draws' cells */
     GROW(apos, (ncells + 1) * 4);
-    CK(gb_launch_cell_flags(st, (uint32_t)ncells, nullptr, ndraw, draws, surfs, cursor.as<uint32_t>()));
+    CK(gb_launch_cell_flags(st, ndraw, draws, surfs, cursor.as<uint32_t>()));
     if (!scratch.grow(gb_scan_scratch_words((uint32_t)ncells) * 4 + 64))
         return cudaErrorMemoryAllocation;
     CK(gb_exclusive_scan_flags(st, cursor.as<uint32_t>(), (uint32_t)ncells, apos.as<uint32_t>(),

@@ -360,13 +360,9 @@ __global__ void gb_cells_max(uint32_t ncells, const uint32_t *__restrict__ cnt, 
 }
 
 /* Active cells, for the raster's per-band draw lists: a cell is active when
-   it holds records; the draws that act on every band (paint, clear, the clip
-   kinds) are active in every band of their surface. */
-__global__ void gb_cell_flags(uint32_t ncells, const uint32_t *__restrict__ off, uint32_t *__restrict__ flags) {
-    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c < ncells)
-        flags[c] = off[c + 1] != off[c] ? 1u : 0u;
-}
+   it holds records (its record count, scanned as a flag); the draws that act
+   on every band (paint, clear, the clip kinds) are active in every band of
+   their surface: their cells' counts are set to 1. */
 __global__ void gb_cell_flags_every_band(uint32_t ndraws, const gb_draw *__restrict__ draws,
                                          const gb_surf *__restrict__ surfs, uint32_t *__restrict__ flags) {
     const uint32_t d = blockIdx.x * blockDim.x + threadIdx.x;
@@ -441,12 +437,10 @@ cudaError_t gb_launch_bin(cudaStream_t st, int scatter, uint32_t nedges, const i
     }
     return cudaGetLastError();
 }
-cudaError_t gb_launch_cell_flags(cudaStream_t st, uint32_t ncells, const uint32_t *off, uint32_t ndraws,
-                                 const gb_draw *draws, const gb_surf *surfs, uint32_t *flags) {
-    if (ncells && off)
-        gb_cell_flags<<<(ncells + 255) / 256, 256, 0, st>>>(ncells, off, flags);
+cudaError_t gb_launch_cell_flags(cudaStream_t st, uint32_t ndraws, const gb_draw *draws, const gb_surf *surfs,
+                                 uint32_t *counts) {
     if (ndraws)
-        gb_cell_flags_every_band<<<(ndraws + 255) / 256, 256, 0, st>>>(ndraws, draws, surfs, flags);
+        gb_cell_flags_every_band<<<(ndraws + 255) / 256, 256, 0, st>>>(ndraws, draws, surfs, counts);
     return cudaGetLastError();
 }
 cudaError_t gb_launch_draw_width_stats(cudaStream_t st, uint32_t ndraws, const gb_draw *draws, const int2 *dbox,
