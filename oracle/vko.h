@@ -96,6 +96,10 @@ VKO_API void vko_set_threads(int n);        /* raster worker threads (CPU baseli
 
 /* portable math, exported for the bit-identity test against the product copy */
 VKO_API void vko_pmath_eval(int fn, const float *a, const float *b, float *out, uint64_t n);
+/* the interior points of one cubic (x0,y0 .. x3,y3 in p[8]) by the
+   subdivision walk at the given squared distance tolerance, in the current
+   math mode; returns the count, storing at most cap points in xy */
+VKO_API uint32_t vko_flatten_cubic(float distanceTolerance, const float *p, float *xy, uint32_t cap);
 
 /* matrices (src/vkvg_matrix.c of vkvg) */
 VKO_API void vko_matrix_init_identity(vko_matrix *m);

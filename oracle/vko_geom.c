@@ -296,6 +296,29 @@ static void recursive_bezier(vko_context *ctx, float distanceTolerance, float x1
     vko_bezier_walk(ctx_emit, ctx, distanceTolerance, x1, y1, x2, y2, x3, y3, x4, y4, level, 0.0, 1.0);
 }
 
+/* one cubic through the walk alone (the interior points _recursive_bezier
+   adds between the start and the end point), for measuring how often the
+   math mode changes a subdivision; returns the point count, storing at most
+   cap points */
+typedef struct {
+    float   *xy;
+    uint32_t n, cap;
+} cubic_sink;
+static void cubic_emit(void *u, float x, float y, int which, double ta, double tb) {
+    (void)which, (void)ta, (void)tb;
+    cubic_sink *s = (cubic_sink *)u;
+    if (s->n < s->cap) {
+        s->xy[2 * s->n]     = x;
+        s->xy[2 * s->n + 1] = y;
+    }
+    s->n++;
+}
+uint32_t vko_flatten_cubic(float distanceTolerance, const float *p, float *xy, uint32_t cap) {
+    cubic_sink s = {xy, 0, cap};
+    vko_bezier_walk(cubic_emit, &s, distanceTolerance, p[0], p[1], p[2], p[3], p[4], p[5], p[6], p[7], 0, 0.0, 1.0);
+    return s.n;
+}
+
 static int finite8(float a, float b, float c, float d, float e, float f, float g, float h) {
     return isfinite(a) && isfinite(b) && isfinite(c) && isfinite(d) && isfinite(e) && isfinite(f) && isfinite(g) &&
            isfinite(h);

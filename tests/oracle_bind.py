@@ -28,6 +28,7 @@ _SIGS = {
     "vko_set_raster_mode": (None, [C.c_int]),
     "vko_set_threads": (None, [C.c_int]),
     "vko_pmath_eval": (None, [C.c_int, _P, _P, _P, C.c_uint64]),
+    "vko_flatten_cubic": (_U, [_F, _P, _P, _U]),
     "vko_surface_create": (_P, [_U, _U, _U]),
     "vko_surface_destroy": (None, [_P]),
     "vko_surface_status": (C.c_int, [_P]),

@@ -231,7 +231,7 @@ def test_portable_math_vs_libm():
     a, b = s0.image().astype(np.int32), s1.image().astype(np.int32)
     diff = np.abs(a - b)
     assert (diff <= 1).mean() >= 0.999, (diff > 1).mean()
-    assert diff.max() <= 2 or (diff > 2).mean() < 1e-3
+    assert diff.max() <= 2, diff.max()
 
 
 def _np_smoothstep(e0, e1, x):
