@@ -302,9 +302,11 @@ def test_clip_state_on_gpu(gb):
 
 
 @pytest.mark.parametrize("which", ["api_mix", "clip_mix"])
-def test_replay_stream_matches_calls(gb, which):
+def test_replay_stream_matches_calls(gb, vko, which):
     """vkvg_gb300_replay_stream of a scene's command codes gives the same
-    samples as the scene's calls"""
+    samples as the scene's calls, and both equal the oracle's samples for
+    those calls (vkvg's replay, src/recording/vkvg_record_internal.c:249,
+    dispatches each code to the public call it records)"""
     import ctypes as C
 
     sc = scenes.api_mix(n_items=24, size=160, seed=5) if which == "api_mix" else \
@@ -320,6 +322,9 @@ def test_replay_stream_matches_calls(gb, which):
     assert st == 0
     ctx2.flush()
     assert np.array_equal(surf.samples_rgba(), surf2.samples_rgba())
+    osurf, octx = pu.run_oracle(vko, sc)
+    assert np.array_equal(surf2.samples_rgba(), osurf.samples_rgba())
+    assert np.array_equal(surf2.image(), osurf.image())
 
 
 def test_radial_gradient_paint_bit_exact(gb, vko):
@@ -459,3 +464,64 @@ def test_glyph_scene_bit_exact(gb, vko, size, n, m):
     assert ctx.status() == 0
     assert np.array_equal(surf.samples_rgba(), osurf.samples_rgba())
     assert np.array_equal(surf.image(), osurf.image())
+
+
+def test_small_polygon_config_bit_exact(gb, vko):
+    """The small polygon configuration as stated: 512x512 at 4x MSAA, 64
+    closed polygons of 3-32 vertices uniform over the surface (seed 0,
+    self-intersecting), each filled NON_ZERO in an opaque random colour and
+    stroked in black at width 4, miter join (limit 10), butt cap.  Flattened
+    points, stroke buffers, every draw's per-sample winding / covering counts,
+    the samples and the image equal the oracle's."""
+    sc = scenes.plain_small()
+    assert (sc["width"], sc["height"], sc["paths"]) == (512, 512, 64)
+    dev, surf, ctx = pu.run_gpu(gb, sc)
+    osurf, octx = pu.run_oracle(vko, sc, threads=8)
+    assert ctx.debug_counts()[5] == 0 and ctx.status() == 0
+    errs = pu.compare_geometry(ctx, octx)
+    assert not errs, errs[:10]
+    gi, oi = pu.geometry_draws(ctx), _oracle_geometry_draws(octx)
+    assert len(gi) == len(oi) == 129  # the paint, 64 fills, 64 strokes
+    for i, j in zip(gi, oi):
+        g = ctx.debug_coverage(i)
+        o = octx.coverage(j, sc["width"], sc["height"], sc["samples"], mode=0)
+        assert np.array_equal(g, o), "draw %d: %d samples differ" % (i, int((g != o).sum()))
+    assert np.array_equal(surf.samples_rgba(), osurf.samples_rgba())
+    assert np.array_equal(surf.image(), osurf.image())
+
+
+def test_batch_streams_match_oracle(gb, vko):
+    """The uneven batch's own content through the batch: four generated
+    surfaces (sides up to 512 so the oracle stays quick; cubics, lines and
+    arcs of radius up to 200 px, path boxes log-uniform from 4 px, fill only,
+    fill then stroke and stroke only, widths up to 12 px) rendered by one
+    batch execution and by its graph replays; every surface's samples and
+    image equal the oracle's rendering of the same command stream."""
+    import ctypes as C
+
+    L = gb.lib()
+    dev = gb.Device(samples=4)
+    scs = scenes.batch_streams(seed=2, n_surfaces=4, max_paths=240, min_paths=60, max_segs=400, max_side=512)
+    ops_all = []
+    for sc in scs:
+        sc["samples"] = 4
+        sc["ops"] = scenes.decode(sc["cmds"], sc["args"])
+        ops_all += [op[0] for op in sc["ops"]]
+    for name in ("curve_to", "line_to", "arc", "fill", "fill_preserve", "stroke"):
+        assert name in ops_all, name
+    cases = [_batch_case(gb, dev, sc) for sc in scs]
+    frames = (C.c_void_p * len(cases))(*[c[3] for c in cases])
+    targets = (C.c_void_p * len(cases))(*[c[1].h for c in cases])
+    bt = L.vkvg_gb300_batch_create(frames, targets, len(cases))
+    assert bt
+    oracle = [pu.run_oracle(vko, sc, threads=8)[0] for sc in scs]
+    for run in range(13):  # sizing, tuning runs, graph capture and a replay
+        assert L.vkvg_gb300_batch_execute(bt) == 0, run
+        if run in (0, 5, 12):
+            for k, (a, b, _, _) in enumerate(cases):
+                assert np.array_equal(b.samples_rgba(), oracle[k].samples_rgba()), (run, k)
+                assert np.array_equal(b.image(), oracle[k].image()), (run, k)
+    L.vkvg_gb300_batch_destroy(bt)
+    for _, _, ctx, fr in cases:
+        L.vkvg_gb300_frame_destroy(fr)
+        ctx.destroy()

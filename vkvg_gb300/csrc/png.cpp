@@ -6,21 +6,24 @@
 
 #include <stdio.h>
 
-static uint32_t crc32_table[256];
-static bool     crc32_ready = false;
+/* the CRC-32 table (reflected polynomial 0xEDB88320), built at compile
+   time so that concurrent writers share it without initialisation races */
+struct Crc32Table {
+    uint32_t v[256];
+    constexpr Crc32Table() : v() {
+        for (uint32_t i = 0; i < 256; i++) {
+            uint32_t c = i;
+            for (int k = 0; k < 8; k++)
+                c = (c & 1) ? 0xEDB88320u ^ (c >> 1) : c >> 1;
+            v[i] = c;
+        }
+    }
+};
+static constexpr Crc32Table crc32_table{};
 
 static uint32_t crc32_update(uint32_t c, const uint8_t *b, size_t n) {
-    if (!crc32_ready) {
-        for (uint32_t i = 0; i < 256; i++) {
-            uint32_t v = i;
-            for (int k = 0; k < 8; k++)
-                v = (v & 1) ? 0xEDB88320u ^ (v >> 1) : v >> 1;
-            crc32_table[i] = v;
-        }
-        crc32_ready = true;
-    }
     for (size_t i = 0; i < n; i++)
-        c = crc32_table[(c ^ b[i]) & 0xFF] ^ (c >> 8);
+        c = crc32_table.v[(c ^ b[i]) & 0xFF] ^ (c >> 8);
     return c;
 }
 static void put_be32(uint8_t *p, uint32_t v) {
