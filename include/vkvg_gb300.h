@@ -147,7 +147,8 @@ vkvg_public uint64_t vkvg_gb300_kernel_launches(void);
  *
  * The first call on each device (with that device current) looks the array's
  * address up, which may load the library's device code; make that first call
- * before any stream capture begins.  All calls on one device share the one
+ * before any stream capture begins.  A device context created anew (after
+ * cudaDeviceReset) gets the lookup again on its first call.  All calls on one device share the one
  * array, so calls that overlap in time - on different streams or host
  * threads - race and corrupt each other's results: order them. */
 #define VKVG_GB300_SCAN_NOALLOC_MAX (1u << 26)

@@ -113,7 +113,7 @@ cudaError_t gb_launch_stroke_tris(cudaStream_t st, uint32_t ntris, uint32_t ndra
                                   int4 *tri_b, uint32_t *tri_draw, uint4 *tri_idx, int4 *edges, uint32_t *edge_draw);
 cudaError_t gb_launch_bin(cudaStream_t st, int scatter, uint32_t nedges, const int4 *edges, const uint32_t *edge_draw,
                           const gb_draw *draws, const gb_surf *surfs, uint32_t samples, uint32_t *cell, int4 *recs,
-                          uint32_t nunits, int2 *dbox, uint32_t *dcnt);
+                          uint32_t nunits, int2 *dbox, uint32_t *dcnt, unsigned long long *total);
 /* counts[c] = 1 in every band's cell of the draws that act on all bands
    (kinds after STROKE): with the cells' record counts, the cells the raster
    visits are then the nonzero entries */

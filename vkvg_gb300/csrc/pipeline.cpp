@@ -207,6 +207,9 @@ cudaError_t Pipeline::geometry(const FrameHost &f, const gb_surf *surfs, uint64_
     const float   *dsh   = (const float *)(I + o_dashes);
     const float   *th    = (const float *)(I + o_thetas);
     uint32_t       hv[4];
+    /* cell indices, their scans and the active-cell lists are 32-bit */
+    if (ncells + every_cells + 2 >= (1ull << 32))
+        return cudaErrorMemoryAllocation;
 
     CK(cudaMemsetAsync(status.p, 0, 16, st));
     if (timing)
@@ -351,8 +354,13 @@ cudaError_t Pipeline::geometry(const FrameHost &f, const gb_surf *surfs, uint64_
         CK(cudaMemsetAsync(dbox.p, 0x7F, (size_t)(ndraw + 1) * 8, st));
         CK(cudaMemsetAsync(dcnt, 0, (size_t)(ndraw + 1) * 4, st));
     }
+    /* status words 12-13: the record total in 64 bits, against the scan's wrap */
+    unsigned long long *total64 = (unsigned long long *)(status.as<uint32_t>() + 12);
+    if (!sized)
+        CK(cudaMemsetAsync(total64, 0, 8, st));
     CK(gb_launch_bin(st, 0, nedge_all, edges.as<int4>(), edge_draw.as<uint32_t>(), draws, surfs, S,
-                     cells.as<uint32_t>(), nullptr, 0u, wide ? dbox.as<int2>() : nullptr, dcnt));
+                     cells.as<uint32_t>(), nullptr, 0u, wide ? dbox.as<int2>() : nullptr, dcnt,
+                     sized ? nullptr : total64));
     gb_count_launch(nedge_all ? 1 : 0);
     /* a one-surface frame's edge-weighted mean draw width (status words 4..7)
        and heaviest cell (word 8) pick the raster form */
@@ -368,6 +376,7 @@ cudaError_t Pipeline::geometry(const FrameHost &f, const gb_surf *surfs, uint64_
     CK(scan(*this, cells.as<uint32_t>(), (uint32_t)ncells, cursor.as<uint32_t>() + 1));
     if (!sized) {
         CK(cudaMemcpyAsync(rb.p, cursor.as<uint32_t>() + 1 + ncells, 4, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync((uint8_t *)rb.p + 32, total64, 8, cudaMemcpyDeviceToHost, st));
         if (stats)
             CK(cudaMemcpyAsync((uint8_t *)rb.p + 8, status.as<uint32_t>() + 4, 20, cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
@@ -376,6 +385,10 @@ cudaError_t Pipeline::geometry(const FrameHost &f, const gb_surf *surfs, uint64_
         memcpy(hv, rb.p, 4);
         memcpy(ws, (uint8_t *)rb.p + 8, 16);
         memcpy(&mxc, (uint8_t *)rb.p + 24, 4);
+        uint64_t tot = 0;
+        memcpy(&tot, (uint8_t *)rb.p + 32, 8);
+        if (tot != (uint64_t)hv[0]) /* more than 2^32 - 1 bin records: beyond the 32-bit offsets */
+            return cudaErrorMemoryAllocation;
         nunits = hv[0];
         /* narrow tiles (256 pixels; 128 when every cell fits 128 units) when
            every cell fits the narrow form's staging buffer (480 units)
@@ -387,7 +400,7 @@ cudaError_t Pipeline::geometry(const FrameHost &f, const gb_surf *surfs, uint64_
     }
     GROW(recs, (size_t)(nunits + 1) * 16);
     CK(gb_launch_bin(st, 1, nedge_all, edges.as<int4>(), edge_draw.as<uint32_t>(), draws, surfs, S,
-                     cursor.as<uint32_t>() + 1, recs.as<int4>(), nunits, nullptr, nullptr));
+                     cursor.as<uint32_t>() + 1, recs.as<int4>(), nunits, nullptr, nullptr, nullptr));
     gb_count_launch(nedge_all ? 1 : 0);
     std::swap(cells, cursor); /* cells <- the offsets (kept for the raster); cursor is free */
     /* the raster's per-band draw lists: the active cells, band-major, in
@@ -604,7 +617,10 @@ vkvg_status_t gb_run_frame(Pipeline &pl, const FrameHost &f, VkvgSurface surf, b
         return VKVG_STATUS_SUCCESS;
     std::lock_guard<std::mutex> lk(surf->mtx);
     if (do_upload || !pl.uploaded) {
-        if (pl.upload(f) != cudaSuccess)
+        const cudaError_t ue = pl.upload(f);
+        if (ue == cudaErrorMemoryAllocation)
+            return VKVG_STATUS_NO_MEMORY;
+        if (ue != cudaSuccess)
             return VKVG_STATUS_DEVICE_ERROR;
     }
     cudaError_t e = pl.run(f, surf, timing);
@@ -616,6 +632,14 @@ vkvg_status_t gb_run_frame(Pipeline &pl, const FrameHost &f, VkvgSurface surf, b
     }
     if (pl.dev_status & GB_ERR_RASTER_WAIT) {
         fprintf(stderr, "vkvg_gb300: raster staging wait exceeded its limit\n");
+        return VKVG_STATUS_DEVICE_ERROR;
+    }
+    if (pl.dev_status & GB_ERR_OVERFLOW) {
+        fprintf(stderr, "vkvg_gb300: a raster cell's records lay beyond the binned total\n");
+        return VKVG_STATUS_DEVICE_ERROR;
+    }
+    if (pl.dev_status & GB_ERR_CURVE_LIMIT) {
+        fprintf(stderr, "vkvg_gb300: a curve exceeded the subdivision work cap and was cut short\n");
         return VKVG_STATUS_DEVICE_ERROR;
     }
     return VKVG_STATUS_SUCCESS;

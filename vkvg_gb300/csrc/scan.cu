@@ -6,6 +6,7 @@
  */
 #include "vkvg_gb300.h"
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <mutex>
 #include <stdint.h>
@@ -132,8 +133,11 @@ cudaError_t gb_exclusive_scan_flags(cudaStream_t st, const uint32_t *in, uint32_
  * part of the module's device image instead of a buffer allocated by the
  * pipeline.  Block sums are fully written by the first kernel before the
  * others read them, so the array needs no initial contents.  Its device
- * address is looked up once per device, by the first call made with that
- * device current.  All calls on one device share the array. */
+ * address is looked up once per device context, by the first call made with
+ * that device current: the cache is keyed by the context's unique id, so a
+ * context created anew after cudaDeviceReset (which reloads the module,
+ * possibly elsewhere) gets a fresh lookup instead of a stale address.  All
+ * calls on one device share the array. */
 #define SCAN_NOALLOC_WORDS ((VKVG_GB300_SCAN_NOALLOC_MAX + SCAN_TILE - 1) / SCAN_TILE + 1)
 #define SCAN_NOALLOC_DEVS  64
 
@@ -141,10 +145,35 @@ static __device__ __align__(256) uint32_t g_scan_noalloc_scratch[SCAN_NOALLOC_WO
 
 void gb_count_launch(uint64_t n);
 
+/* the current context's unique id through the driver entry points the
+   runtime hands out (nothing linked against libcuda); 0 when unavailable */
+typedef CUresult (*pfn_ctx_current)(CUcontext *);
+typedef CUresult (*pfn_ctx_id)(CUcontext, unsigned long long *);
+static unsigned long long current_ctx_id() {
+    static pfn_ctx_current get_cur = nullptr;
+    static pfn_ctx_id      get_id  = nullptr;
+    static std::once_flag  once;
+    std::call_once(once, [] {
+        void *f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, nullptr) ==
+                cudaSuccess)
+            get_cur = (pfn_ctx_current)f;
+        f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, nullptr) == cudaSuccess)
+            get_id = (pfn_ctx_id)f;
+    });
+    CUcontext          c  = nullptr;
+    unsigned long long id = 0;
+    if (!get_cur || !get_id || get_cur(&c) != CUDA_SUCCESS || !c || get_id(c, &id) != CUDA_SUCCESS)
+        return 0;
+    return id;
+}
+
 extern "C" vkvg_status_t vkvg_gb300_exclusive_scan_noalloc(void *stream, const uint32_t *counts, uint32_t n,
                                                             uint32_t *offsets) {
-    static std::mutex lock;
-    static uint32_t  *scratch[SCAN_NOALLOC_DEVS];
+    static std::mutex         lock;
+    static uint32_t          *scratch[SCAN_NOALLOC_DEVS];
+    static unsigned long long scratch_ctx[SCAN_NOALLOC_DEVS];
     if (!offsets || (n && !counts))
         return VKVG_STATUS_NULL_POINTER;
     if (n > VKVG_GB300_SCAN_NOALLOC_MAX) {
@@ -158,7 +187,9 @@ extern "C" vkvg_status_t vkvg_gb300_exclusive_scan_noalloc(void *stream, const u
     uint32_t *sp;
     {
         std::lock_guard<std::mutex> g(lock);
-        if (!scratch[dev]) {
+        const unsigned long long    id = current_ctx_id();
+        if (!scratch[dev] || !id || scratch_ctx[dev] != id) {
+            /* the lookup also makes the device's primary context current */
             void       *p = nullptr;
             cudaError_t e = cudaGetSymbolAddress(&p, g_scan_noalloc_scratch);
             if (e != cudaSuccess || !p) {
@@ -166,7 +197,8 @@ extern "C" vkvg_status_t vkvg_gb300_exclusive_scan_noalloc(void *stream, const u
                         cudaGetErrorString(e));
                 return VKVG_STATUS_DEVICE_ERROR;
             }
-            scratch[dev] = (uint32_t *)p;
+            scratch[dev]     = (uint32_t *)p;
+            scratch_ctx[dev] = current_ctx_id();
         }
         sp = scratch[dev];
     }

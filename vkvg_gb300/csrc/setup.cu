@@ -242,7 +242,8 @@ template <bool SCATTER>
 __global__ void gb_bin_edges(uint32_t nedges, const int4 *__restrict__ edges, const uint32_t *__restrict__ edge_draw,
                              const gb_draw *__restrict__ draws, const gb_surf *__restrict__ surfs, uint32_t samples,
                              uint32_t *__restrict__ cell, int4 *__restrict__ recs, uint32_t nunits,
-                             int2 *__restrict__ dbox, uint32_t *__restrict__ dcnt) {
+                             int2 *__restrict__ dbox, uint32_t *__restrict__ dcnt,
+                             unsigned long long *__restrict__ total) {
     const uint32_t e     = blockIdx.x * blockDim.x + threadIdx.x;
     const bool     valid = e < nedges;
     bool           ok    = valid;
@@ -298,6 +299,12 @@ __global__ void gb_bin_edges(uint32_t nedges, const int4 *__restrict__ edges, co
                 atomicAdd(&dcnt[bd], bn);
             }
         }
+    }
+    if (!SCATTER && total) {
+        /* the record total in 64 bits (the cells' scan wraps at 2^32) */
+        const uint32_t wn = __reduce_add_sync(0xFFFFFFFFu, ok ? b1 - b0 + 1u : 0u);
+        if ((threadIdx.x & 31u) == 0 && wn)
+            atomicAdd(total, (unsigned long long)wn);
     }
     if (!ok)
         return;
@@ -426,14 +433,14 @@ cudaError_t gb_launch_stroke_tris(cudaStream_t st, uint32_t ntris, uint32_t ndra
 }
 cudaError_t gb_launch_bin(cudaStream_t st, int scatter, uint32_t nedges, const int4 *edges, const uint32_t *edge_draw,
                           const gb_draw *draws, const gb_surf *surfs, uint32_t samples, uint32_t *cell, int4 *recs,
-                          uint32_t nunits, int2 *dbox, uint32_t *dcnt) {
+                          uint32_t nunits, int2 *dbox, uint32_t *dcnt, unsigned long long *total) {
     if (nedges) {
         if (scatter)
             gb_bin_edges<true><<<(nedges + 255) / 256, 256, 0, st>>>(nedges, edges, edge_draw, draws, surfs, samples,
-                                                                      cell, recs, nunits, nullptr, nullptr);
+                                                                      cell, recs, nunits, nullptr, nullptr, nullptr);
         else
             gb_bin_edges<false><<<(nedges + 255) / 256, 256, 0, st>>>(nedges, edges, edge_draw, draws, surfs,
-                                                                       samples, cell, nullptr, 0u, dbox, dcnt);
+                                                                       samples, cell, nullptr, 0u, dbox, dcnt, total);
     }
     return cudaGetLastError();
 }
