@@ -116,6 +116,23 @@ vkvg_public vkvg_status_t vkvg_gb300_debug_stroke(VkvgContext ctx, uint32_t i, f
 /* per-sample winding (fills) or covering-triangle count (strokes) of draw i,
    int32 [height][width][samples] */
 vkvg_public vkvg_status_t vkvg_gb300_debug_coverage(VkvgContext ctx, uint32_t i, int32_t *out);
+/* The raster form frames use, for the whole process: -1 automatic (the
+   default), 0 the register tile of 1024 pixels, 1 of 256 pixels, 2 of 128
+   pixels, 3 the row form.  Frames with clipping always run the first.  And
+   the form the context's last flush ran (-1 before any). */
+vkvg_public void vkvg_gb300_debug_set_raster_form(int form);
+vkvg_public int  vkvg_gb300_debug_raster_form(VkvgContext ctx);
+/* Failure injection for the tests, process-wide (no vkvg counterpart; vkvg's
+   own failure paths are a fence timeout, src/vkvg_context_internal.c:407-419,
+   and allocation failures reported through the status sentinels):
+     what 0: the value-th device buffer growth from now fails as an
+             allocation failure would (1 the next one, 0 disarms);
+     what 1: the row form's staging waits give up after value polls instead
+             of 2^20 (0 restores), which sets the device status bit the host
+             reports as VKVG_STATUS_DEVICE_ERROR;
+     what 2: the subdivision work cap per cubic, in nodes (0 restores 2^22),
+             beyond which a curve is cut short and reported the same way. */
+vkvg_public void vkvg_gb300_debug_inject(int what, uint32_t value);
 /* raw per-sample premultiplied RGBA8 of a surface, [height][width][samples][4] */
 vkvg_public vkvg_status_t vkvg_gb300_surface_read_samples(VkvgSurface surf, uint8_t *out);
 /* resolved premultiplied RGBA8 of a surface (before unpremultiplication) */

@@ -525,3 +525,59 @@ def test_batch_streams_match_oracle(gb, vko):
     for _, _, ctx, fr in cases:
         L.vkvg_gb300_frame_destroy(fr)
         ctx.destroy()
+
+
+@pytest.fixture
+def raster_form(gb):
+    """sets the process-wide raster form for one test, then restores automatic"""
+    L = gb.lib()
+    yield lambda f: L.vkvg_gb300_debug_set_raster_form(f)
+    L.vkvg_gb300_debug_set_raster_form(-1)
+
+
+def _form_scenes():
+    out = [scenes.curve_heavy(n_paths=12, size=200, seed=3, n_min=3, n_max=8),
+           scenes.api_mix(n_items=24, size=160, seed=5),
+           scenes.gradient_mix(n_items=14, size=144, seed=9, samples=4),
+           scenes.gradient_mix(n_items=6, size=96, seed=2, samples=1, radial=True),
+           scenes.surface_mix(n_items=8, size=112, seed=23, samples=4),
+           scenes.glyph_scene(n_outlines=60, n_strokes=8, size=128)]
+    for o in out:
+        o.setdefault("samples", 4)
+    wide = scenes.curve_heavy(n_paths=8, size=100, seed=6, n_min=3, n_max=6)
+    wide["width"], wide["name"] = 1300, "wide1300"  # two tiles, the second ragged
+    out.append(wide)
+    return out
+
+
+@pytest.mark.parametrize("form", [0, 1, 2, 3])
+def test_each_raster_form_bit_exact(gb, vko, raster_form, form):
+    """every raster form (the register tiles of 1024, 256 and 128 pixels and
+    the row form) on solid, gradient (one source image and several), radial,
+    surface-source and glyph scenes, one and four samples, a surface two
+    tiles wide: the form asked for is the one that ran, and its samples and
+    image equal the oracle's"""
+    raster_form(form)
+    for sc in _form_scenes():
+        dev, surf, ctx = pu.run_gpu(gb, sc, debug=False)
+        assert ctx.raster_form() == form, sc["name"]
+        assert ctx.status() == 0 and ctx.debug_counts()[5] == 0, sc["name"]
+        osurf, octx = pu.run_oracle(vko, sc)
+        assert np.array_equal(surf.samples_rgba(), osurf.samples_rgba()), sc["name"]
+        assert np.array_equal(surf.image(), osurf.image()), sc["name"]
+
+
+@pytest.mark.parametrize("form", [0, 3])
+def test_coverage_each_form_bit_exact(gb, vko, raster_form, form):
+    """per-draw winding and covering counts read back through the row form and
+    the wide register tile equal the oracle's"""
+    raster_form(form)
+    sc = scenes.curve_heavy(n_paths=10, size=128, seed=1, n_min=3, n_max=6)
+    dev, surf, ctx = pu.run_gpu(gb, sc)
+    osurf, octx = pu.run_oracle(vko, sc)
+    assert ctx.raster_form() == form
+    gi, oi = pu.geometry_draws(ctx), _oracle_geometry_draws(octx)
+    for i, j in zip(gi, oi):
+        g = ctx.debug_coverage(i)
+        o = octx.coverage(j, sc["width"], sc["height"], sc["samples"], mode=0)
+        assert np.array_equal(g, o), "draw %d: %d samples differ" % (i, int((g != o).sum()))

@@ -160,6 +160,9 @@ SIGNATURES = {
     "vkvg_gb300_debug_draw": (_I, [_P, _U, _P]),
     "vkvg_gb300_debug_stroke": (_I, [_P, _U, _P, _P]),
     "vkvg_gb300_debug_coverage": (_I, [_P, _U, _P]),
+    "vkvg_gb300_debug_set_raster_form": (None, [_I]),
+    "vkvg_gb300_debug_raster_form": (_I, [_P]),
+    "vkvg_gb300_debug_inject": (None, [_I, _U]),
     "vkvg_gb300_surface_read_samples": (_I, [_P, _P]),
     "vkvg_gb300_surface_read_premult": (_I, [_P, _P]),
     "vkvg_gb300_pmath_eval": (_I, [_I, _P, _P, _P, C.c_uint64, _I]),
@@ -390,6 +393,11 @@ class Context:
         if st:
             raise VkvgError("debug_stroke %d: %d" % (i, st))
         return v[:nv], ix[:ni]
+
+    def raster_form(self):
+        """the raster form the last flush ran (0 1024-pixel register tile,
+        1 256-pixel, 2 128-pixel, 3 row form)"""
+        return int(self.L.vkvg_gb300_debug_raster_form(self.h))
 
     def debug_coverage(self, i):
         s = self.surf

@@ -231,7 +231,8 @@ static VkvgSurface surface_alloc(VkvgDevice dev, uint32_t width, uint32_t height
     s->clip_wpr = (s->wpad + 31) / 32;
     s->plane_words = (size_t)s->nbands * GB_BAND_ROWS * s->clip_wpr;
     size_t cb      = s->plane_words * 4;
-    if (cudaMalloc(&s->d_samples, sb) != cudaSuccess || cudaMalloc(&s->d_rgba, rb) != cudaSuccess ||
+    if (gb_inject_alloc_fail() || cudaMalloc(&s->d_samples, sb) != cudaSuccess ||
+        cudaMalloc(&s->d_rgba, rb) != cudaSuccess ||
         cudaMalloc(&s->d_out, rb) != cudaSuccess || cudaMalloc(&s->d_clip, cb) != cudaSuccess) {
         if (s->d_samples)
             cudaFree(s->d_samples);
@@ -377,8 +378,10 @@ VkvgContext vkvg_create(VkvgSurface surf) {
     ctx->surf   = surf;
     ctx->dev    = surf->dev;
     if (!ctx->pl.init()) {
+        const bool oom = ctx->pl.init_oom;
+        ctx->pl.destroy();
         delete ctx;
-        return (VkvgContext)&s_device_error;
+        return (VkvgContext)(oom ? &s_no_memory : &s_device_error);
     }
     vkvg_surface_reference(surf);
     /* a context's first render pass clears the stencil (renderPass_ClearStencil,

@@ -131,10 +131,10 @@ __device__ __forceinline__ void gb_bez_eval(float tol, const gb_bez_frame &f, gb
 
 /* Walk the subdivision tree of one cubic, calling emit(x, y, which, ta, tb)
    for every point _recursive_bezier would add.  Returns false if the node cap
-   was hit. */
+   (cap nodes visited) was hit. */
 template <bool TRACK, class Emit>
 __device__ __forceinline__ bool gb_bezier_walk(float tol, float x1, float y1, float x2, float y2, float x3, float y3,
-                                               float x4, float y4, Emit &emit) {
+                                               float x4, float y4, Emit &emit, unsigned cap = GB_CURVE_NODE_CAP) {
     gb_bez_frame st[102];
     float2       tt[TRACK ? 102 : 1];
     int          sp = 0;
@@ -146,7 +146,7 @@ __device__ __forceinline__ bool gb_bezier_walk(float tol, float x1, float y1, fl
         --sp;
         gb_bez_frame f  = st[sp];
         float2       ti = TRACK ? tt[sp] : make_float2(0.f, 0.f);
-        if (++nodes > GB_CURVE_NODE_CAP)
+        if (++nodes > cap)
             return false;
         if (f.level > 100u)
             continue;

@@ -128,6 +128,17 @@ vkvg_status_t vkvg_gb300_debug_stroke(VkvgContext ctx, uint32_t i, float *xy, ui
     return r;
 }
 
+void vkvg_gb300_debug_set_raster_form(int form) { gb_form_override.store(form >= 0 && form <= 3 ? form : -1); }
+int  vkvg_gb300_debug_raster_form(VkvgContext ctx) { return vkvg_status(ctx) ? -1 : ctx->pl.form_run; }
+void vkvg_gb300_debug_inject(int what, uint32_t value) {
+    if (what == 0)
+        gb_fail_alloc.store(value);
+    else if (what == 1)
+        gb_wait_limit.store(value);
+    else if (what == 2)
+        gb_set_flatten_node_cap(value);
+}
+
 vkvg_status_t vkvg_gb300_debug_coverage(VkvgContext ctx, uint32_t i, int32_t *out) {
     if (vkvg_status(ctx))
         return vkvg_status(ctx);
@@ -161,9 +172,13 @@ vkvg_status_t vkvg_gb300_debug_coverage(VkvgContext ctx, uint32_t i, int32_t *ou
     A.rgba     = s->d_rgba;
     A.cov_out  = p.dbg.as<int32_t>();
     A.cov_draw = i;
+    A.wait_limit = WAIT_LIMIT_POLLS;
     gb_clip_args CA;
     memset(&CA, 0, sizeof(CA));
-    if (gb_launch_raster(p.st, &A, &CA, 0, 0, 0) != cudaSuccess)
+    /* the form the frame itself ran (the register tile after a clipping frame) */
+    const cudaError_t e =
+        p.form_run == 3 ? gb_launch_raster_rows(p.st, &A, 0) : gb_launch_raster(p.st, &A, &CA, 0, 0, 0);
+    if (e != cudaSuccess)
         return VKVG_STATUS_DEVICE_ERROR;
     gb_count_launch(1);
     if (cudaStreamSynchronize(p.st) != cudaSuccess)

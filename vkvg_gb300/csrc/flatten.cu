@@ -42,6 +42,9 @@ struct gb_write_emit {
     }
 };
 
+/* the subdivision work cap per cubic (a test hook can lower it) */
+__device__ uint32_t g_flatten_node_cap = GB_CURVE_NODE_CAP;
+
 __device__ __forceinline__ bool gb_finite(float v) { return (__float_as_uint(v) & 0x7f800000u) != 0x7f800000u; }
 
 /* Visit every point one segment adds, in order. */
@@ -56,7 +59,7 @@ __device__ __forceinline__ bool gb_segment_points(uint32_t info, float4 a, float
         bool fin = gb_finite(a.x) && gb_finite(a.y) && gb_finite(a.z) && gb_finite(a.w) && gb_finite(b.x) &&
                    gb_finite(b.y) && gb_finite(b.z) && gb_finite(b.w);
         if (fin)
-            ok = gb_bezier_walk<false>(c.x, a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, emit);
+            ok = gb_bezier_walk<false>(c.x, a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, emit, g_flatten_node_cap);
         emit(b.z, b.w);
     } else if (kind == GB_SEG_ARC) {
         /* vkvg_arc / vkvg_arc_negative loop, src/vkvg_context.c:424-430 */
@@ -145,6 +148,11 @@ __global__ void gb_pmath_eval(int fn, const float *__restrict__ a, const float *
 }
 
 extern "C" {
+/* set the flattening kernels' work cap per cubic (0: the default) */
+cudaError_t gb_set_flatten_node_cap(uint32_t cap) {
+    const uint32_t v = cap ? cap : GB_CURVE_NODE_CAP;
+    return cudaMemcpyToSymbol(g_flatten_node_cap, &v, sizeof(v));
+}
 cudaError_t gb_launch_pmath_eval(cudaStream_t st, int fn, const float *a, const float *b, float *out, uint64_t n) {
     if (!n)
         return cudaSuccess;

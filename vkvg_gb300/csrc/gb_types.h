@@ -146,5 +146,6 @@ typedef struct {
 #define GB_ERR_CURVE_LIMIT 0x1u /* a cubic exceeded the subdivision work cap */
 #define GB_ERR_OVERFLOW    0x2u
 #define GB_ERR_RASTER_WAIT 0x4u /* a staged copy in the raster did not arrive within its wait limit */
+#define WAIT_LIMIT_POLLS   (1u << 20) /* mbarrier polls before a staged copy counts as lost */
 
 #endif

@@ -106,9 +106,11 @@ struct Pipeline {
     uint32_t npts = 0, nev = 0, nverts = 0, ninds = 0, nedges = 0, ntris = 0, nunits = 0, nbands = 0;
     uint32_t dev_status = 0;
     uint32_t stats_w    = 0;     /* surface width of a one-surface frame: geometry measures its draws' widths */
-    int      narrow     = 0; /* the last frame's raster form: 0 1024-pixel, 1 256-pixel, 2 128-pixel tiles */
+    int      narrow     = 0; /* the register-tile form geometry picked: 0 1024-pixel, 1 256-pixel, 2 128-pixel tiles */
+    int      form_run   = -1; /* the raster form the last frame ran (as vkvg_gb300_debug_set_raster_form) */
     uint64_t launches   = 0;
     uint64_t upload_bytes = 0;
+    bool     init_oom     = false; /* init failed growing a buffer */
     float    ms[5]      = {0, 0, 0, 0, 0};
 
     bool init();
@@ -126,6 +128,13 @@ struct Pipeline {
     /* K1 only: flatten the uploaded segments (for vkvg_path_extents) */
     cudaError_t flatten_only();
 };
+
+/* process-wide test settings (vkvg_gb300_debug_set_raster_form, _inject) */
+extern std::atomic<int>      gb_form_override; /* -1 automatic */
+extern std::atomic<uint32_t> gb_fail_alloc;    /* growths until one fails, 0 off */
+extern std::atomic<uint32_t> gb_wait_limit;    /* row-form staging wait polls, 0 default */
+/* true when an armed allocation failure falls on this allocation */
+bool gb_inject_alloc_fail();
 
 struct _vkvg_device_t {
     vkvg_status_t status;

@@ -25,6 +25,8 @@ struct gb_raster_args {
     uint32_t        cov_draw;
     const uint32_t *gsrc;   /* gradient source images [n][H][W], premultiplied RGBA8 */
     uint32_t        stage_min; /* cells of fewer record units are read from global memory, not staged */
+    uint32_t        gc_src;    /* row form, 4x MSAA: source image (index + 1) whose band rows are staged, or 0 */
+    uint32_t        wait_limit; /* row form: mbarrier polls before a slot counts as lost */
 };
 /* the clip planes, a kernel parameter of their own (read by the clipping
    variant only; kept out of gb_raster_args, whose size the register
@@ -142,6 +144,16 @@ cudaError_t gb_launch_gather_u32(cudaStream_t st, uint32_t n, const uint64_t *id
    given form (as gb_raster_tile_width) */
 cudaError_t gb_launch_raster_batch(cudaStream_t st, const gb_raster_args *a, const gb_surf *surfs, const uint4 *items,
                                    uint32_t nitems, uint32_t *queue, uint32_t nctas, int form);
+/* the row form of the raster (one warp per sample row, samples in shared
+   memory, a producer warp staging each draw's records through a ring of
+   slots): one CTA per (1024-pixel tile, band); frames without clipping */
+cudaError_t gb_launch_raster_rows(cudaStream_t st, const gb_raster_args *a, int gradients);
+/* the row form as the persistent batch raster (one CTA per SM, nctas CTAs) */
+cudaError_t gb_launch_raster_rows_batch(cudaStream_t st, const gb_raster_args *a, const gb_surf *surfs,
+                                        const uint4 *items, uint32_t nitems, uint32_t *queue, uint32_t nctas);
+uint32_t    gb_raster_rows_tile_width(void);
+/* the flattening kernels' subdivision work cap per cubic, in nodes (0: 2^22) */
+cudaError_t gb_set_flatten_node_cap(uint32_t cap);
 cudaError_t gb_launch_pmath_eval(cudaStream_t st, int fn, const float *a, const float *b, float *out, uint64_t n);
 }
 

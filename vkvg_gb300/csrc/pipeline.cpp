@@ -44,9 +44,26 @@ void FrameHost::clear() {
     dash_sub_hi = 0;
 }
 
+std::atomic<int>      gb_form_override{-1};
+std::atomic<uint32_t> gb_fail_alloc{0};
+std::atomic<uint32_t> gb_wait_limit{0};
+
+/* true when a test armed an allocation failure and this growth is the one */
+static bool injected_alloc_failure() {
+    uint32_t v = gb_fail_alloc.load();
+    while (v) {
+        if (gb_fail_alloc.compare_exchange_weak(v, v - 1))
+            return v == 1;
+    }
+    return false;
+}
+bool gb_inject_alloc_fail() { return injected_alloc_failure(); }
+
 bool DevBuf::grow(size_t bytes) {
     if (bytes <= cap)
         return true;
+    if (injected_alloc_failure())
+        return false;
     size_t nc = std::max(bytes + bytes / 4, (size_t)4096);
     if (p)
         cudaFree(p);
@@ -93,7 +110,8 @@ bool Pipeline::init() {
     for (auto &e : evs)
         if (cudaEventCreate(&e) != cudaSuccess)
             return false;
-    return rb.grow(256) && status.grow(64);
+    init_oom = !(rb.grow(256) && status.grow(64));
+    return !init_oom;
 }
 void Pipeline::destroy() {
     if (st)
@@ -568,7 +586,19 @@ cudaError_t Pipeline::run(const FrameHost &f, _vkvg_surface_t *surf, bool timing
         gb_count_launch(ngrad);
         A.gsrc = gsrc.as<uint32_t>();
     }
-    CK(gb_launch_raster(st, &A, &CA, ngrad > 0, clip_use, clip_use ? 0 : narrow));
+    /* the band rows of a frame's only source image are staged by the row form */
+    A.gc_src     = ngrad == 1 && S == 4 ? 1u : 0u;
+    A.wait_limit = gb_wait_limit.load() ? gb_wait_limit.load() : WAIT_LIMIT_POLLS;
+    int form     = gb_form_override.load();
+    if (clip_use)
+        form = 0; /* only the register tile carries the clip planes */
+    else if (form < 0 || form > 3)
+        form = narrow ? narrow : 3; /* small draws: the narrow register tiles; otherwise the row form */
+    form_run = form;
+    if (form == 3)
+        CK(gb_launch_raster_rows(st, &A, ngrad > 0));
+    else
+        CK(gb_launch_raster(st, &A, &CA, ngrad > 0, clip_use, form));
     surf->clip_active = act;
     surf->save_nz     = snz;
     gb_count_launch(1);
