@@ -85,9 +85,9 @@ def test_allocation_failure_at_flush(gb, vko, inject):
     _still_renders(gb, vko)
 
 
-@pytest.mark.parametrize("limit", [1, 4])
-def test_raster_wait_limit_reports_device_error(gb, vko, inject, limit):
-    gb.lib().vkvg_gb300_debug_set_raster_form(3)
+@pytest.mark.parametrize("form,limit", [(3, 1), (4, 1), (4, 4)])
+def test_raster_wait_limit_reports_device_error(gb, vko, inject, form, limit):
+    gb.lib().vkvg_gb300_debug_set_raster_form(form)
     dev = gb.Device(samples=4)
     surf = gb.Surface(dev, 300, 200)
     ctx = surf.context()

@@ -550,10 +550,10 @@ def _form_scenes():
     return out
 
 
-@pytest.mark.parametrize("form", [0, 1, 2, 3])
+@pytest.mark.parametrize("form", [0, 1, 2, 3, 4])
 def test_each_raster_form_bit_exact(gb, vko, raster_form, form):
     """every raster form (the register tiles of 1024, 256 and 128 pixels and
-    the row form) on solid, gradient (one source image and several), radial,
+    the row form in half and whole bands) on solid, gradient (one source image and several), radial,
     surface-source and glyph scenes, one and four samples, a surface two
     tiles wide: the form asked for is the one that ran, and its samples and
     image equal the oracle's"""
@@ -567,7 +567,7 @@ def test_each_raster_form_bit_exact(gb, vko, raster_form, form):
         assert np.array_equal(surf.image(), osurf.image()), sc["name"]
 
 
-@pytest.mark.parametrize("form", [0, 3])
+@pytest.mark.parametrize("form", [0, 3, 4])
 def test_coverage_each_form_bit_exact(gb, vko, raster_form, form):
     """per-draw winding and covering counts read back through the row form and
     the wide register tile equal the oracle's"""

@@ -396,7 +396,7 @@ class Context:
 
     def raster_form(self):
         """the raster form the last flush ran (0 1024-pixel register tile,
-        1 256-pixel, 2 128-pixel, 3 row form)"""
+        1 256-pixel, 2 128-pixel, 3 row form in half bands, 4 in whole bands)"""
         return int(self.L.vkvg_gb300_debug_raster_form(self.h))
 
     def debug_coverage(self, i):

@@ -108,6 +108,9 @@ struct Pipeline {
     uint32_t stats_w    = 0;     /* surface width of a one-surface frame: geometry measures its draws' widths */
     int      narrow     = 0; /* the register-tile form geometry picked: 0 1024-pixel, 1 256-pixel, 2 128-pixel tiles */
     int      form_run   = -1; /* the raster form the last frame ran (as vkvg_gb300_debug_set_raster_form) */
+    int      form_half  = 0;  /* the row form ran in half bands with 16-bit counters */
+    bool     small_draws = false; /* the frame's draws are narrow next to a 1024-pixel tile */
+    uint32_t max_cell   = 0xFFFFFFFFu; /* record units of the heaviest cell (one-surface frames; else unknown) */
     uint64_t launches   = 0;
     uint64_t upload_bytes = 0;
     bool     init_oom     = false; /* init failed growing a buffer */

@@ -146,8 +146,10 @@ cudaError_t gb_launch_raster_batch(cudaStream_t st, const gb_raster_args *a, con
                                    uint32_t nitems, uint32_t *queue, uint32_t nctas, int form);
 /* the row form of the raster (one warp per sample row, samples in shared
    memory, a producer warp staging each draw's records through a ring of
-   slots): one CTA per (1024-pixel tile, band); frames without clipping */
-cudaError_t gb_launch_raster_rows(cudaStream_t st, const gb_raster_args *a, int gradients);
+   slots): one CTA per (1024-pixel tile, band), or with half per (tile, half
+   band) with 16-bit counters, three CTAs per SM (every cell under 2^15
+   record units); frames without clipping */
+cudaError_t gb_launch_raster_rows(cudaStream_t st, const gb_raster_args *a, int gradients, int half);
 /* the row form as the persistent batch raster (one CTA per SM, nctas CTAs) */
 cudaError_t gb_launch_raster_rows_batch(cudaStream_t st, const gb_raster_args *a, const gb_surf *surfs,
                                         const uint4 *items, uint32_t nitems, uint32_t *queue, uint32_t nctas);

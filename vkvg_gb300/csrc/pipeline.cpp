@@ -407,7 +407,8 @@ cudaError_t Pipeline::geometry(const FrameHost &f, const gb_surf *surfs, uint64_
         memcpy(&tot, (uint8_t *)rb.p + 32, 8);
         if (tot != (uint64_t)hv[0]) /* more than 2^32 - 1 bin records: beyond the 32-bit offsets */
             return cudaErrorMemoryAllocation;
-        nunits = hv[0];
+        nunits   = hv[0];
+        max_cell = stats ? mxc : 0xFFFFFFFFu;
         /* narrow tiles (256 pixels; 128 when every cell fits 128 units) when
            every cell fits the narrow form's staging buffer (480 units)
            (a heavy cell is one CTA's serial work: the wide form's 512 threads
@@ -415,6 +416,7 @@ cudaError_t Pipeline::geometry(const FrameHost &f, const gb_surf *surfs, uint64_
            to a wide tile, or the surface is no wider than a narrow one */
         const bool small = !wide || (ws[1] && ws[0] <= 384u * ws[1]);
         narrow           = !(stats && small) ? 0 : mxc <= 128u ? 2 : mxc <= 480u ? 1 : 0;
+        small_draws      = stats && small;
     }
     GROW(recs, (size_t)(nunits + 1) * 16);
     CK(gb_launch_bin(st, 1, nedge_all, edges.as<int4>(), edge_draw.as<uint32_t>(), draws, surfs, S,
@@ -592,11 +594,14 @@ cudaError_t Pipeline::run(const FrameHost &f, _vkvg_surface_t *surf, bool timing
     int form     = gb_form_override.load();
     if (clip_use)
         form = 0; /* only the register tile carries the clip planes */
-    else if (form < 0 || form > 3)
-        form = narrow ? narrow : 3; /* small draws: the narrow register tiles; otherwise the row form */
-    form_run = form;
-    if (form == 3)
-        CK(gb_launch_raster_rows(st, &A, ngrad > 0));
+    else if (form < 0 || form > 4)
+        form = narrow ? narrow : small_draws ? 0 : 3; /* small draws: the register tiles; wide ones: the row form */
+    if (form == 3 && max_cell >= 32768u)
+        form = 4; /* 16-bit counters would not hold a cell's crossings: whole bands */
+    form_run  = form;
+    form_half = form == 3 ? 1 : 0;
+    if (form >= 3)
+        CK(gb_launch_raster_rows(st, &A, ngrad > 0, form_half));
     else
         CK(gb_launch_raster(st, &A, &CA, ngrad > 0, clip_use, form));
     surf->clip_active = act;

@@ -49,31 +49,49 @@
 #include <cuda_runtime.h>
 
 namespace rw {
-constexpr int ROWS    = GB_BAND_ROWS; /* consumer warps, one per sample row */
-constexpr int TW      = 1024;         /* tile width in pixels (samples per row) */
-constexpr int THREADS = (ROWS + 1) * 32;
-constexpr int PROD    = ROWS;         /* the producer's warp index */
-constexpr int NSLOT   = 4;            /* ring depth */
-constexpr int CAP     = 1024;         /* record units (16 bytes) per slot */
-constexpr int HDR     = 16;           /* header words per slot */
-/* shared memory, in 32-bit words */
-constexpr int S_SMP  = 0;                    /* samples [ROWS][TW] */
-constexpr int S_CNT  = S_SMP + ROWS * TW;    /* crossing counters [ROWS][TW] */
-constexpr int S_OCC  = S_CNT + ROWS * TW;    /* bit planes [ROWS][TW / 32] */
-constexpr int S_GC   = S_OCC + ROWS * 32;    /* the band's 4 pixel rows of one source image (4x MSAA) */
-constexpr int S_HDR  = S_GC + 4 * TW;        /* slot headers */
-constexpr int S_BAR  = S_HDR + NSLOT * HDR;  /* full[NSLOT], empty[NSLOT] mbarriers (8 bytes each) */
-constexpr int S_MISC = S_BAR + 4 * NSLOT;    /* abort flag, walk bounds */
-constexpr int S_STG  = (S_MISC + 16 + 3) / 4 * 4;
-constexpr int SMEM   = (S_STG + NSLOT * CAP * 4) * 4;
-static_assert(S_HDR % 4 == 0 && S_BAR % 2 == 0 && S_STG % 4 == 0, "headers and staging 16-byte aligned");
-static_assert(SMEM <= 232448, "one CTA per SM");
+constexpr int TW  = 1024; /* tile width in pixels (samples per row) */
+constexpr int HDR = 16;   /* header words per slot */
 /* header words (read as four 16-byte vectors) */
 enum { H_KIND, H_OP, H_SRC, H_GS, H_LO, H_UNITS, H_STAGED, H_MODE, H_K, H_C0, H_C1, H_C2, H_C3, H_INV };
 constexpr uint32_t KIND_END = 0xFFFFFFFFu;
 /* misc words */
 enum { M_ABORT, M_IEND, M_DLO, M_DHI, M_TILES, M_DENSE, M_I0 };
 } // namespace rw
+
+/* A row-form configuration: ROWS consumer warps (sample rows per CTA, 16 or
+   8: a CTA then covers a half band), the ring's depth and slot capacity,
+   and 32- or 16-bit crossing counters.  16-bit counters hold a position's
+   net crossings exactly while the draw's cell has fewer than 2^15 records
+   (the host checks the heaviest cell). */
+template <int ROWS_, int NSLOT_, int CAP_, bool C16_> struct RWT {
+    static constexpr int  ROWS    = ROWS_;
+    static constexpr int  NSLOT   = NSLOT_;
+    static constexpr int  CAP     = CAP_;
+    static constexpr bool C16     = C16_;
+    static constexpr int  TW      = rw::TW;
+    static constexpr int  HDR     = rw::HDR;
+    static constexpr int  THREADS = (ROWS + 1) * 32;
+    static constexpr int  PROD    = ROWS;            /* the producer's warp index */
+    static constexpr int  CW      = C16 ? TW / 2 : TW; /* counter words per row */
+    static constexpr int  GCR     = ROWS / 4;        /* pixel rows of the CTA at 4x MSAA */
+    /* shared memory, in 32-bit words */
+    static constexpr int S_SMP  = 0;                    /* samples [ROWS][TW] */
+    static constexpr int S_CNT  = S_SMP + ROWS * TW;    /* crossing counters [ROWS][CW] */
+    static constexpr int S_OCC  = S_CNT + ROWS * CW;    /* bit planes [ROWS][TW / 32] */
+    static constexpr int S_GC   = S_OCC + ROWS * 32;    /* the CTA's pixel rows of one source image (4x MSAA) */
+    static constexpr int S_HDR  = S_GC + GCR * TW;      /* slot headers */
+    static constexpr int S_BAR  = S_HDR + NSLOT * HDR;  /* full[NSLOT], empty[NSLOT] mbarriers (8 bytes each) */
+    static constexpr int S_MISC = S_BAR + 4 * NSLOT;    /* abort flag, walk bounds */
+    static constexpr int S_STG  = (S_MISC + 16 + 3) / 4 * 4;
+    static constexpr int SMEM   = (S_STG + NSLOT * CAP * 4) * 4;
+    static constexpr int MINB   = SMEM + 1024 <= 233472 / 3 ? 3 : SMEM + 1024 <= 233472 / 2 ? 2 : 1; /* CTAs per SM */
+    static_assert(S_HDR % 4 == 0 && S_BAR % 2 == 0 && S_STG % 4 == 0, "headers and staging 16-byte aligned");
+    static_assert(SMEM <= 232448, "shared memory of one CTA");
+};
+/* the band-sized configuration (also the batch's) and the half-band one
+   that fits three CTAs per SM */
+using RW16 = RWT<16, 4, 1024, false>;
+using RW8  = RWT<8, 4, 256, true>;
 
 /* the bits [a, b] of a word, a <= b <= 31 */
 __device__ __forceinline__ uint32_t bit_range(uint32_t a, uint32_t b) { return ((0xFFFFFFFFu >> (31u - b)) >> a) << a; }
@@ -146,10 +164,13 @@ __device__ __forceinline__ void blend_any(uint32_t *smp, uint32_t t, uint32_t l,
    coverage read-back variant, which writes one draw's per-sample counts to
    A.cov_out and leaves the surface alone.  Returns false when a staging wait
    ran out (the tile keeps its previous samples). */
-template <bool GRAD, bool DBG>
-__device__ __forceinline__ bool rows_item(const gb_raster_args &A, int32_t *smem, uint32_t band, uint32_t tile,
-                                          uint32_t &seq) {
+template <class T, bool GRAD, bool DBG>
+__device__ __forceinline__ bool rows_item(const gb_raster_args &A, int32_t *smem, uint32_t band, uint32_t part,
+                                          uint32_t tile, uint32_t &seq) {
     using namespace rw;
+    constexpr int ROWS = T::ROWS, NSLOT = T::NSLOT, CAP = T::CAP, THREADS = T::THREADS, PROD = T::PROD;
+    constexpr int S_SMP = T::S_SMP, S_CNT = T::S_CNT, S_OCC = T::S_OCC, S_GC = T::S_GC, S_HDR = T::S_HDR;
+    constexpr int S_BAR = T::S_BAR, S_MISC = T::S_MISC, S_STG = T::S_STG, CW = T::CW;
     const uint32_t t = threadIdx.x, wi = t >> 5, l = t & 31;
     const int32_t  X0  = (int32_t)(tile * TW);
     const int32_t  TWr = min(TW, (int32_t)A.W - X0);
@@ -164,7 +185,7 @@ __device__ __forceinline__ bool rows_item(const gb_raster_args &A, int32_t *smem
 
     /* ---- load the tile's samples (or the first draw's uniform colour), the
        staged source rows and the walk bounds */
-    const uint32_t band_r0 = band * ROWS;
+    const uint32_t band_r0 = band * GB_BAND_ROWS + part * ROWS; /* the CTA's first sample row */
     for (uint32_t i = t; i < (uint32_t)(ROWS * TW / 4); i += THREADS) {
         const uint32_t r = i / (TW / 4), c4 = (i % (TW / 4)) * 4;
         uint4          v = make_uint4(0, 0, 0, 0);
@@ -178,12 +199,12 @@ __device__ __forceinline__ bool rows_item(const gb_raster_args &A, int32_t *smem
         }
         *reinterpret_cast<uint4 *>(smem + S_SMP + r * TW + c4) = v;
     }
-    for (uint32_t i = t; i < (uint32_t)(ROWS * TW + ROWS * 32) / 4; i += THREADS)
+    for (uint32_t i = t; i < (uint32_t)(ROWS * CW + ROWS * 32) / 4; i += THREADS)
         reinterpret_cast<int4 *>(smem + S_CNT)[i] = make_int4(0, 0, 0, 0);
     const uint32_t gc_gs = GRAD && A.S == 4 && !dbg ? A.gc_src : 0u;
     if (gc_gs) {
-        for (uint32_t i = t; i < (uint32_t)(4 * TW); i += THREADS) {
-            const uint32_t pr = i / TW, px = i % TW, py = band * 4 + pr;
+        for (uint32_t i = t; i < (uint32_t)(T::GCR * TW); i += THREADS) {
+            const uint32_t pr = i / TW, px = i % TW, py = band_r0 / 4 + pr;
             smem[S_GC + i]    = ((int32_t)px < TWr && py < A.H)
                                     ? A.gsrc[((size_t)(gc_gs - 1) * A.H + py) * A.W + X0 + px]
                                     : 0u;
@@ -307,8 +328,29 @@ __device__ __forceinline__ bool rows_item(const gb_raster_args &A, int32_t *smem
         const int32_t  sy     = A.S == 4 ? 32 + 64 * R : 128 + 256 * R;
         const int32_t  ox     = A.S == 4 ? ((R & 3) == 0 ? 96 : (R & 3) == 1 ? 224 : (R & 3) == 2 ? 32 : 160) : 128;
         uint32_t      *smp    = reinterpret_cast<uint32_t *>(smem + S_SMP + rr * TW);
-        int32_t       *cnt    = smem + S_CNT + rr * TW;
+        int32_t       *cnt    = smem + S_CNT + rr * CW;
         uint32_t      *occ    = reinterpret_cast<uint32_t *>(smem + S_OCC + rr * 32);
+        /* the crossing counters of position p (16-bit ones two to a word:
+           the word is lo + 65536 hi with both halves signed) */
+        auto cadd = [&](uint32_t p, int32_t dir) {
+            if (T::C16)
+                atomicAdd(&cnt[p >> 1], (int32_t)((uint32_t)dir << (16u * (p & 1u))));
+            else
+                atomicAdd(&cnt[p], dir);
+        };
+        auto cget = [&](uint32_t p) -> int32_t {
+            if (!T::C16)
+                return cnt[p];
+            const int32_t w = cnt[p >> 1], lo = (int16_t)(w & 0xFFFF);
+            return (p & 1u) ? (int32_t)((uint32_t)w - (uint32_t)lo) >> 16 : lo;
+        };
+        /* lane l's run of counters back to zero (16-byte stores) */
+        auto cclear = [&]() {
+            int4 *q = reinterpret_cast<int4 *>(cnt + (T::C16 ? 16u : 32u) * l);
+#pragma unroll
+            for (int i = 0; i < (T::C16 ? 4 : 8); i++)
+                q[i] = make_int4(0, 0, 0, 0);
+        };
         /* this lane's run of the row [32 l, 32 l + 32): the samples inside the tile */
         const int32_t  nrun  = TWr - 32 * (int32_t)l;
         const uint32_t vmask = !row_ok || nrun <= 0 ? 0u : nrun >= 32 ? 0xFFFFFFFFu : (1u << nrun) - 1u;
@@ -378,7 +420,7 @@ __device__ __forceinline__ bool rows_item(const gb_raster_args &A, int32_t *smem
                     if (eo) {
                         atomicXor(&occ[p >> 5], 1u << (p & 31u));
                     } else {
-                        atomicAdd(&cnt[p], ed.y < ed.w ? 1 : -1);
+                        cadd(p, ed.y < ed.w ? 1 : -1);
                         atomicOr(&occ[p >> 5], 1u << (p & 31u));
                     }
                 }
@@ -444,7 +486,7 @@ __device__ __forceinline__ bool rows_item(const gb_raster_args &A, int32_t *smem
                winding entering the run from the right */
             int32_t rs = 0;
             for (uint32_t b = m; b; b &= b - 1)
-                rs += cnt[(l << 5) + __ffs(b) - 1];
+                rs += cget((l << 5) + __ffs(b) - 1);
             int32_t incl = rs; /* sum over this lane's run and the runs right of it */
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
@@ -455,16 +497,15 @@ __device__ __forceinline__ bool rows_item(const gb_raster_args &A, int32_t *smem
             if (dbg) {
                 int32_t w = incl - rs;
                 for (int j = 31; j >= 0; j--) {
-                    w += cnt[(l << 5) + j];
+                    w += cget((l << 5) + j);
                     if ((vmask >> j) & 1u)
                         A.cov_out[((size_t)(R / rpp) * A.W + X0 + 32 * l + j) * A.S + R % rpp] = w;
                 }
             }
             /* walk the occupied positions left to right (the winding left of
-               position p includes its count): non-zero fills cover w != 0 and
-               clear the counts as they go; strokes blend once per covering
-               triangle, so pass k covers w > k, the first four passes' masks
-               in this walk */
+               position p includes its count): non-zero fills cover w != 0;
+               strokes blend once per covering triangle, so pass k covers
+               w > k, the first four passes' masks in this walk */
             const bool stroke = kind == GB_DRAW_STROKE;
             uint32_t   c1 = 0, c2 = 0, c3 = 0, c4 = 0, start = 0;
             int32_t    w = incl, kmax = 0;
@@ -476,9 +517,7 @@ __device__ __forceinline__ bool rows_item(const gb_raster_args &A, int32_t *smem
                 c3 |= w > 2 ? r : 0u;
                 c4 |= w > 3 ? r : 0u;
                 kmax = max(kmax, w);
-                w -= cnt[(l << 5) + p];
-                if (!stroke)
-                    cnt[(l << 5) + p] = 0;
+                w -= cget((l << 5) + p);
                 start = p + 1;
             }
             if (start < 32) {
@@ -500,7 +539,7 @@ __device__ __forceinline__ bool rows_item(const gb_raster_args &A, int32_t *smem
                         for (uint32_t b = m; b; b &= b - 1) {
                             const uint32_t p = __ffs(b) - 1;
                             cv |= ww > rep ? bit_range(st, p) : 0u;
-                            ww -= cnt[(l << 5) + p];
+                            ww -= cget((l << 5) + p);
                             st = p + 1;
                         }
                         cv |= st < 32 && ww > rep ? bit_range(st, 31) : 0u;
@@ -512,9 +551,8 @@ __device__ __forceinline__ bool rows_item(const gb_raster_args &A, int32_t *smem
                         blend_any<false>(smp, tb, l, mode, B, S);
                 }
             }
-            if (stroke)
-                for (uint32_t b = m; b; b &= b - 1)
-                    cnt[(l << 5) + __ffs(b) - 1] = 0;
+            if (m)
+                cclear();
             __syncwarp();
         }
     }
@@ -533,7 +571,7 @@ __device__ __forceinline__ bool rows_item(const gb_raster_args &A, int32_t *smem
     const uint32_t *stage = reinterpret_cast<const uint32_t *>(smem + S_SMP);
     const uint32_t  prows = ROWS / rpp;
     for (uint32_t q = t * 4; q < prows * TW; q += THREADS * 4) {
-        const uint32_t pr = q / TW, px = q % TW, py = band * prows + pr;
+        const uint32_t pr = q / TW, px = q % TW, py = band_r0 / rpp + pr;
         if (py >= A.H || (int32_t)px >= TWr)
             continue;
         uint32_t outp[4];
@@ -564,39 +602,40 @@ __device__ __forceinline__ bool rows_item(const gb_raster_args &A, int32_t *smem
     return true;
 }
 
-__device__ __forceinline__ void rows_init_barriers(int32_t *smem) {
-    using namespace rw;
+template <class T> __device__ __forceinline__ void rows_init_barriers(int32_t *smem) {
     if (threadIdx.x == 0) {
-        const uint32_t full0 = (uint32_t)__cvta_generic_to_shared(smem) + S_BAR * 4, empty0 = full0 + NSLOT * 8;
-        for (uint32_t s = 0; s < (uint32_t)NSLOT; s++) {
+        const uint32_t full0 = (uint32_t)__cvta_generic_to_shared(smem) + T::S_BAR * 4, empty0 = full0 + T::NSLOT * 8;
+        for (uint32_t s = 0; s < (uint32_t)T::NSLOT; s++) {
             mbar_init_n(full0 + 8 * s, 1);
-            mbar_init_n(empty0 + 8 * s, ROWS);
+            mbar_init_n(empty0 + 8 * s, T::ROWS);
         }
         mbar_init_fence();
     }
     __syncthreads();
 }
 
-/* 17 warps: the register file's four partitions hold five warps each at
-   most, so a thread gets at most 96 registers */
-template <bool GRAD, bool DBG>
-__global__ void __launch_bounds__(rw::THREADS, 1) gb_raster_rows(gb_raster_args A) {
+/* grid: x tiles, y bands times the parts of a band (16 / ROWS).  The
+   register file's four partitions hold whole warps: 17 warps leave 96
+   registers a thread, three CTAs of 9 warps 72 */
+template <class T, bool GRAD, bool DBG>
+__global__ void __launch_bounds__(T::THREADS, T::MINB) gb_raster_rows(gb_raster_args A) {
     extern __shared__ __align__(16) int32_t smem[];
-    rows_init_barriers(smem);
-    uint32_t seq = 0;
-    rows_item<GRAD, DBG>(A, smem, blockIdx.y, blockIdx.x, seq);
+    rows_init_barriers<T>(smem);
+    uint32_t           seq   = 0;
+    constexpr uint32_t parts = GB_BAND_ROWS / T::ROWS;
+    rows_item<T, GRAD, DBG>(A, smem, blockIdx.y / parts, blockIdx.y % parts, blockIdx.x, seq);
 }
 
 /* The batch raster in the row form: a persistent grid (one CTA per SM)
    takes (surface, band, tile) items from the work list until it is
    exhausted; no CTA waits on another. */
-__global__ void __launch_bounds__(rw::THREADS, 1)
+__global__ void __launch_bounds__(RW16::THREADS, 1)
     gb_raster_rows_batch(gb_raster_args A0, const gb_surf *__restrict__ surfs, const uint4 *__restrict__ items,
                          uint32_t nitems, uint32_t *__restrict__ queue) {
     extern __shared__ __align__(16) int32_t smem[];
     __shared__ gb_raster_args Ai;
     __shared__ uint32_t       cur_item, cur_band, cur_tile;
-    rows_init_barriers(smem);
+    rows_init_barriers<RW16>(smem);
     uint32_t seq = 0;
     for (uint32_t iter = 0; iter < nitems; iter++) {
         if (threadIdx.x == 0) {
@@ -630,32 +669,35 @@ __global__ void __launch_bounds__(rw::THREADS, 1)
         __syncthreads();
         if (cur_item >= nitems)
             break;
-        if (!rows_item<false, false>(Ai, smem, cur_band, cur_tile, seq))
+        if (!rows_item<RW16, false, false>(Ai, smem, cur_band, 0, cur_tile, seq))
             break; /* mbarrier phases no longer in step: stop this CTA */
     }
 }
 
 extern "C" uint32_t gb_raster_rows_tile_width() { return rw::TW; }
 
-template <bool GRAD, bool DBG> static cudaError_t rows_launch(cudaStream_t st, const gb_raster_args *a) {
+template <class T, bool GRAD, bool DBG> static cudaError_t rows_launch(cudaStream_t st, const gb_raster_args *a) {
     static bool configured = false;
     if (!configured) {
         const cudaError_t e =
-            cudaFuncSetAttribute(gb_raster_rows<GRAD, DBG>, cudaFuncAttributeMaxDynamicSharedMemorySize, rw::SMEM);
+            cudaFuncSetAttribute(gb_raster_rows<T, GRAD, DBG>, cudaFuncAttributeMaxDynamicSharedMemorySize, T::SMEM);
         if (e != cudaSuccess)
             return e;
         configured = true;
     }
-    const dim3 grid((a->W + rw::TW - 1) / rw::TW, a->nbands);
-    gb_raster_rows<GRAD, DBG><<<grid, rw::THREADS, rw::SMEM, st>>>(*a);
+    const dim3 grid((a->W + rw::TW - 1) / rw::TW, a->nbands * (GB_BAND_ROWS / T::ROWS));
+    gb_raster_rows<T, GRAD, DBG><<<grid, T::THREADS, T::SMEM, st>>>(*a);
     return cudaGetLastError();
 }
-extern "C" cudaError_t gb_launch_raster_rows(cudaStream_t st, const gb_raster_args *a, int gradients) {
+template <class T> static cudaError_t rows_pick(cudaStream_t st, const gb_raster_args *a, int gradients) {
+    if (a->cov_out)
+        return gradients ? rows_launch<T, true, true>(st, a) : rows_launch<T, false, true>(st, a);
+    return gradients ? rows_launch<T, true, false>(st, a) : rows_launch<T, false, false>(st, a);
+}
+extern "C" cudaError_t gb_launch_raster_rows(cudaStream_t st, const gb_raster_args *a, int gradients, int half) {
     if (a->nbands == 0)
         return cudaSuccess;
-    if (a->cov_out)
-        return gradients ? rows_launch<true, true>(st, a) : rows_launch<false, true>(st, a);
-    return gradients ? rows_launch<true, false>(st, a) : rows_launch<false, false>(st, a);
+    return half ? rows_pick<RW8>(st, a, gradients) : rows_pick<RW16>(st, a, gradients);
 }
 
 extern "C" cudaError_t gb_launch_raster_rows_batch(cudaStream_t st, const gb_raster_args *a, const gb_surf *surfs,
@@ -666,11 +708,11 @@ extern "C" cudaError_t gb_launch_raster_rows_batch(cudaStream_t st, const gb_ras
         return cudaSuccess;
     if (!configured) {
         cudaError_t e =
-            cudaFuncSetAttribute(gb_raster_rows_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, rw::SMEM);
+            cudaFuncSetAttribute(gb_raster_rows_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, RW16::SMEM);
         if (e != cudaSuccess)
             return e;
         configured = true;
     }
-    gb_raster_rows_batch<<<nctas, rw::THREADS, rw::SMEM, st>>>(*a, surfs, items, nitems, queue);
+    gb_raster_rows_batch<<<nctas, RW16::THREADS, RW16::SMEM, st>>>(*a, surfs, items, nitems, queue);
     return cudaGetLastError();
 }
