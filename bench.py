@@ -16,17 +16,23 @@ e2e    - paths/s through the public C API from host memory: each step replays
          the scene's vkvg_* calls (vkvg_gb300_replay_stream), flushes (H2D copy
          + kernels) and reads the image back (vkvg_surface_write_to_memory);
          wall-clock time.
-roofline - the raster/composite kernel (dominant) against the measured HBM
-         copy bandwidth; algorithmic bytes = 8 B per flattened point and per
-         stroke vertex read once, plus the RGBA8 surface read and written.
-         frame_frac applies the whole-frame count (8 B per input control
-         point, 4 B per command word, 16 B per flattened point and per stroke
-         vertex - written once, read once - and 8 B per pixel) to the whole
-         frame time.  The raster kernel is instruction-issue bound, not HBM
-         bound; its ncu issue and pipe figures are read from the committed
-         profile summary (profiles/raster_curve_heavy_1024.md).
-cpu_baseline - the CPU restatement of vkvg's path code (oracle/) on a bounded
-         sample (the first 64 paths of the same scene), all host threads.
+roofline - the raster/composite kernel (dominant; the row form in half
+         bands) against the measured HBM copy bandwidth; algorithmic bytes =
+         8 B per flattened point and per stroke vertex read once, plus the
+         RGBA8 surface read and written.  frame_frac applies the whole-frame
+         count (8 B per input control point, 4 B per command word, 16 B per
+         flattened point and per stroke vertex - written once, read once - and
+         8 B per pixel) to the whole frame time.  The raster kernel is
+         instruction-issue bound, not HBM bound: roofline.issue sets its warp
+         instructions per launch (ncu, full-size launch, from the committed
+         summary profiles/raster_rows_curve_heavy_1024.md) over its CUDA-event
+         time against the SM issue peak (SMs x 4 schedulers x the SM clock
+         sampled during the run).
+cpu_baseline - the CPU restatement of vkvg's path code (oracle/): the
+         headline figure on a bounded sample of the same scene (the first 256
+         paths on the full surface, all host threads, median of 3), plus
+         one-core and all-core medians on bounded samples of the other
+         configurations (cpu_baseline.configs).
 
 `--impl reference` times that CPU implementation alone (vkvg itself cannot be
 built or run here: no Vulkan stack and its vkh / glutess submodules are empty).
@@ -63,6 +69,14 @@ def parse():
     p.add_argument("--no-glyphs", action="store_true", help="skip the 4096x4096 glyph workload")
     p.add_argument("--adam-steps", type=int, default=200, help="Adam steps of the differentiable workload")
     return p.parse_args()
+
+
+def sm_max_mhz():
+    try:
+        with open(PEAKS_FILE) as f:
+            return float(json.load(f)["sm_max_mhz"])
+    except Exception:
+        return 2070.0
 
 
 def hbm_peak():
@@ -163,6 +177,53 @@ def cpu_sample(n_paths, size, threads, reps=1):
         ctx.destroy()
         surf.destroy()
     return n_paths / min(times), min(times)
+
+
+def cpu_scene_time(sc, threads, reps=3):
+    """median wall time of the CPU restatement rendering one scene (its
+    sources included) with the given raster worker threads"""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_bind as ob
+    import parity_util as pu
+
+    L = ob.lib()
+    L.vko_set_math_mode(0)
+    times = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        surf, ctx = pu.run_oracle(ob, sc, raster_mode=0, threads=threads)
+        times.append(time.perf_counter() - t0)
+        ctx.destroy()
+        surf.destroy()
+    return statistics.median(times)
+
+
+def cpu_configs(threads):
+    """one-core and all-core medians (3 repetitions) of the CPU restatement on
+    bounded samples of every single-GPU configuration"""
+    from vkvg_gb300 import scenes
+
+    cases = []
+    cases.append(("small_polygons", scenes.plain_small(), "the whole configuration: 512x512, 64 polygons"))
+    cases.append(("curve_heavy", scenes.curve_heavy(n_paths=32), "first 32 of 2048 paths, full 1024x1024 surface"))
+    bs = scenes.batch_streams(seed=2, n_surfaces=2, max_paths=240, min_paths=60, max_segs=400, max_side=512)
+    for b in bs:
+        b["samples"] = 4
+        b["ops"] = scenes.decode(b["cmds"], b["args"])
+    cases.append(("batch_uneven", bs, "2 generated surfaces of the batch's construction, sides <= 512"))
+    g = scenes.glyph_scene(n_outlines=3125, n_strokes=312, size=512)
+    cases.append(("glyphs", g, "512x512 crop of the glyph construction at the same density (3,125 outlines, "
+                               "312 strokes)"))
+    out = {}
+    for name, sc, sample in cases:
+        scs = sc if isinstance(sc, list) else [sc]
+        paths = sum(x["paths"] for x in scs)
+        e = {"sample": sample, "paths": paths}
+        for label, th in (("one_core", 1), ("all_cores", threads)):
+            t = sum(cpu_scene_time(x, th) for x in scs)
+            e[label + "_paths_per_s"] = paths / t
+        out[name] = e
+    return out
 
 
 def analytic_bench(a, gb, torch, np, flush, cpu):
@@ -396,11 +457,17 @@ def glyph_bench(a, gb, L, np, flush):
 
 
 def run_reference(a, rank):
-    """CPU implementation of the path (the oracle port), all host threads."""
+    """CPU implementation of the path (the oracle port), all host threads.
+    Each step renders the whole frame (all paths of the scene on the full
+    surface) when the run's steps fit in about five minutes at the speed a
+    64-path probe shows; otherwise the first n paths, n as large as fits."""
     if rank != 0:
         return
     threads = os.cpu_count() or 1
-    n_paths = 64
+    _, t64 = cpu_sample(64, a.size, threads)
+    per_path = t64 / 64
+    budget = 300.0 / max(1, a.steps + a.warmup)
+    n_paths = a.paths if per_path * a.paths <= budget else max(64, int(budget / per_path))
     for _ in range(a.warmup):
         cpu_sample(n_paths, a.size, threads)
     t = 0.0
@@ -413,7 +480,7 @@ def run_reference(a, rank):
         "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1000.0 * t / a.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "fp32/int64/u8", "data": "synthetic",
         "config": {"workload": "curve_heavy_%dx%d_msaa4" % (a.size, a.size), "paths_per_frame": a.paths,
-                   "sample": "first %d paths of the scene per step" % n_paths},
+                   "sample": "first %d paths of the scene per step" % n_paths, "same_config": n_paths == a.paths},
         "cpu_baseline": {"value": value, "unit": "paths/s", "cores": threads, "kind": "port",
                          "sample": "first %d of %d paths, full %dx%d surface" % (n_paths, a.paths, a.size, a.size)},
         "e2e": {"value": value, "unit": "paths/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -634,16 +701,28 @@ def main():
     n_ctrl = len(args) // 2
     frame_bytes = 8 * n_ctrl + 4 * len(cmds) + 16 * nflat + 16 * nsv + 8 * a.size * a.size
     prof = {}
-    tfile = os.path.join(ROOT, "profiles", "raster_curve_heavy_1024.md")
+    tfile = os.path.join(ROOT, "profiles", "raster_rows_curve_heavy_1024.md")
     if os.path.exists(tfile):
         for ln in open(tfile):
             k, _, v = ln.partition(":")
-            if k.strip() in ("dram_bytes_per_launch", "issue_slots_busy_pct", "alu_pipe_active_pct"):
+            if k.strip() in ("dram_bytes_per_launch", "issue_slots_busy_pct", "alu_pipe_active_pct",
+                             "warp_inst_per_launch"):
                 try:
                     prof[k.strip()] = float(v.split()[0])
                 except (ValueError, IndexError):
                     pass
     traffic = int(prof["dram_bytes_per_launch"]) if "dram_bytes_per_launch" in prof else None
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
+    sm_mhz = clk["sm_mhz"] if clk else sm_max_mhz()
+    issue_peak = sms * 4 * sm_mhz * 1e6  # warp instructions per second, one per scheduler per cycle
+    issue = {"bound": "sm issue", "unit": "warp inst/s", "peak": issue_peak, "sms": sms, "sm_mhz": sm_mhz,
+             "issue_slots_busy_pct": prof.get("issue_slots_busy_pct"),
+             "alu_pipe_active_pct": prof.get("alu_pipe_active_pct"),
+             "source": "ncu summary in profiles/raster_rows_curve_heavy_1024.md"}
+    if "warp_inst_per_launch" in prof:
+        issue["warp_inst_per_launch"] = prof["warp_inst_per_launch"]
+        issue["achieved"] = prof["warp_inst_per_launch"] / (raster_ms / 1000.0)
+        issue["frac"] = issue["achieved"] / issue_peak
 
     line = {
         "metric": "paths/s", "value": value, "unit": "paths/s", "n_gpus": world, "steps": a.steps,
@@ -660,13 +739,10 @@ def main():
         "e2e": {"value": e2e_value, "unit": "paths/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": e_t * 1000.0},
         "gpu_launches": int(launches),
-        "roofline": {"bound": "hbm", "kernel": "gb_raster", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
-                     "algorithmic_bytes": raster_bytes, "frame_bytes": frame_bytes,
-                     "frame_frac": frame_bytes / (ms / 1000.0) / 1e9 / peak,
-                     "issue": {"bound": "sm issue", "issue_slots_busy_pct": prof.get("issue_slots_busy_pct"),
-                               "alu_pipe_active_pct": prof.get("alu_pipe_active_pct"),
-                               "source": "ncu summary in profiles/raster_curve_heavy_1024.md"}},
+        "roofline": {"bound": "hbm", "kernel": "gb_raster_rows (row form, half bands)", "achieved": achieved,
+                     "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
+                     "traffic": traffic, "algorithmic_bytes": raster_bytes, "frame_bytes": frame_bytes,
+                     "frame_frac": frame_bytes / (ms / 1000.0) / 1e9 / peak, "issue": issue},
         "clocks": clk,
     }
     if svg:
@@ -681,10 +757,12 @@ def main():
         line["analytic"] = analytic
     if rank == 0 and not a.no_cpu:
         threads = os.cpu_count() or 1
-        v, _ = cpu_sample(64, a.size, threads)
+        ts = [cpu_sample(256, a.size, threads)[1] for _ in range(3)]
+        v = 256 / statistics.median(ts)
         line["cpu_baseline"] = {"value": v, "unit": "paths/s", "cores": threads, "kind": "port",
-                                "sample": "first 64 of %d paths, full %dx%d surface, 4x MSAA" % (paths, a.size,
-                                                                                                  a.size)}
+                                "sample": "first 256 of %d paths, full %dx%d surface, 4x MSAA, median of 3" %
+                                          (paths, a.size, a.size),
+                                "configs": cpu_configs(threads)}
     L.vkvg_gb300_frame_destroy(frame)
     ectx.destroy()
     ctx.destroy()

@@ -110,7 +110,7 @@ bool Pipeline::init() {
     for (auto &e : evs)
         if (cudaEventCreate(&e) != cudaSuccess)
             return false;
-    init_oom = !(rb.grow(256) && status.grow(64));
+    init_oom = !(rb.grow(512) && status.grow(512));
     return !init_oom;
 }
 void Pipeline::destroy() {
@@ -372,10 +372,11 @@ cudaError_t Pipeline::geometry(const FrameHost &f, const gb_surf *surfs, uint64_
         CK(cudaMemsetAsync(dbox.p, 0x7F, (size_t)(ndraw + 1) * 8, st));
         CK(cudaMemsetAsync(dcnt, 0, (size_t)(ndraw + 1) * 4, st));
     }
-    /* status words 12-13: the record total in 64 bits, against the scan's wrap */
-    unsigned long long *total64 = (unsigned long long *)(status.as<uint32_t>() + 12);
+    /* status bytes 256-511: the record total in 64 bits, as 32 partial sums,
+       against the scan's wrap */
+    unsigned long long *total64 = (unsigned long long *)(status.as<uint8_t>() + 256);
     if (!sized)
-        CK(cudaMemsetAsync(total64, 0, 8, st));
+        CK(cudaMemsetAsync(total64, 0, 256, st));
     CK(gb_launch_bin(st, 0, nedge_all, edges.as<int4>(), edge_draw.as<uint32_t>(), draws, surfs, S,
                      cells.as<uint32_t>(), nullptr, 0u, wide ? dbox.as<int2>() : nullptr, dcnt,
                      sized ? nullptr : total64));
@@ -394,7 +395,7 @@ cudaError_t Pipeline::geometry(const FrameHost &f, const gb_surf *surfs, uint64_
     CK(scan(*this, cells.as<uint32_t>(), (uint32_t)ncells, cursor.as<uint32_t>() + 1));
     if (!sized) {
         CK(cudaMemcpyAsync(rb.p, cursor.as<uint32_t>() + 1 + ncells, 4, cudaMemcpyDeviceToHost, st));
-        CK(cudaMemcpyAsync((uint8_t *)rb.p + 32, total64, 8, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync((uint8_t *)rb.p + 256, total64, 256, cudaMemcpyDeviceToHost, st));
         if (stats)
             CK(cudaMemcpyAsync((uint8_t *)rb.p + 8, status.as<uint32_t>() + 4, 20, cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
@@ -403,8 +404,10 @@ cudaError_t Pipeline::geometry(const FrameHost &f, const gb_surf *surfs, uint64_
         memcpy(hv, rb.p, 4);
         memcpy(ws, (uint8_t *)rb.p + 8, 16);
         memcpy(&mxc, (uint8_t *)rb.p + 24, 4);
-        uint64_t tot = 0;
-        memcpy(&tot, (uint8_t *)rb.p + 32, 8);
+        uint64_t tot = 0, part[32];
+        memcpy(part, (uint8_t *)rb.p + 256, 256);
+        for (uint64_t v : part)
+            tot += v;
         if (tot != (uint64_t)hv[0]) /* more than 2^32 - 1 bin records: beyond the 32-bit offsets */
             return cudaErrorMemoryAllocation;
         nunits   = hv[0];

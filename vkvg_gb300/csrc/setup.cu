@@ -301,10 +301,19 @@ __global__ void gb_bin_edges(uint32_t nedges, const int4 *__restrict__ edges, co
         }
     }
     if (!SCATTER && total) {
-        /* the record total in 64 bits (the cells' scan wraps at 2^32) */
+        /* the record total in 64 bits (the cells' scan wraps at 2^32): the
+           block's sum into one of 32 counters (every thread of the block
+           reaches the barriers) */
+        __shared__ unsigned long long s_tot;
+        if (threadIdx.x == 0)
+            s_tot = 0;
+        __syncthreads();
         const uint32_t wn = __reduce_add_sync(0xFFFFFFFFu, ok ? b1 - b0 + 1u : 0u);
         if ((threadIdx.x & 31u) == 0 && wn)
-            atomicAdd(total, (unsigned long long)wn);
+            atomicAdd(&s_tot, (unsigned long long)wn);
+        __syncthreads();
+        if (threadIdx.x == 0 && s_tot)
+            atomicAdd(&total[blockIdx.x & 31u], s_tot);
     }
     if (!ok)
         return;
