@@ -109,7 +109,7 @@ struct Pipeline {
     int      narrow     = 0; /* the register-tile form geometry picked: 0 1024-pixel, 1 256-pixel, 2 128-pixel tiles */
     int      form_run   = -1; /* the raster form the last frame ran (as vkvg_gb300_debug_set_raster_form) */
     int      form_half  = 0;  /* the row form ran in half bands with 16-bit counters */
-    bool     small_draws = false; /* the frame's draws are narrow next to a 1024-pixel tile */
+    bool     row_draws  = false; /* the frame's draws span most of a 1024-pixel tile (the row form's case) */
     uint32_t max_cell   = 0xFFFFFFFFu; /* record units of the heaviest cell (one-surface frames; else unknown) */
     uint64_t launches   = 0;
     uint64_t upload_bytes = 0;

@@ -419,7 +419,11 @@ cudaError_t Pipeline::geometry(const FrameHost &f, const gb_surf *surfs, uint64_
            to a wide tile, or the surface is no wider than a narrow one */
         const bool small = !wide || (ws[1] && ws[0] <= 384u * ws[1]);
         narrow           = !(stats && small) ? 0 : mxc <= 128u ? 2 : mxc <= 480u ? 1 : 0;
-        small_draws      = stats && small;
+        /* the row form pays per row and draw, and per crossing in a lane's
+           run: it wins when the draws span most of a tile with crossings
+           spread thin (mean width over 640 pixels, weighted by edges); on
+           denser, smaller geometry the register tiles do */
+        row_draws = stats && wide && ws[1] && ws[0] > 640u * ws[1];
     }
     GROW(recs, (size_t)(nunits + 1) * 16);
     CK(gb_launch_bin(st, 1, nedge_all, edges.as<int4>(), edge_draw.as<uint32_t>(), draws, surfs, S,
@@ -598,7 +602,7 @@ cudaError_t Pipeline::run(const FrameHost &f, _vkvg_surface_t *surf, bool timing
     if (clip_use)
         form = 0; /* only the register tile carries the clip planes */
     else if (form < 0 || form > 4)
-        form = narrow ? narrow : small_draws ? 0 : 3; /* small draws: the register tiles; wide ones: the row form */
+        form = narrow ? narrow : row_draws ? 3 : 0;
     if (form == 3 && max_cell >= 32768u)
         form = 4; /* 16-bit counters would not hold a cell's crossings: whole bands */
     form_run  = form;
