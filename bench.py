@@ -63,7 +63,6 @@ def parse():
     p.add_argument("--paths", type=int, default=2048)
     p.add_argument("--size", type=int, default=1024)
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
-    p.add_argument("--svg-shapes", type=int, default=600, help="shapes of the SVG ingestion workload (0: skip)")
     p.add_argument("--no-batch", action="store_true", help="skip the uneven-batch comparison")
     p.add_argument("--no-analytic", action="store_true", help="skip the differentiable analytic-coverage workload")
     p.add_argument("--no-glyphs", action="store_true", help="skip the 4096x4096 glyph workload")
@@ -585,42 +584,6 @@ def main():
     h2d = int(stats[12])
     d2h = a.size * a.size * 4
 
-    # ---- SVG ingestion through vkvg's SVG API (include/vkvg-svg.h): parse a
-    # seeded tiger-scale document, then render it on a surface of its size and
-    # read the image back, every step
-    svg = None
-    if a.svg_shapes > 0:
-        text = scenes.svg_document(seed=7, n_shapes=a.svg_shapes, size=a.size)
-        t0 = time.perf_counter()
-        doc = gb.Svg(text)
-        parse_ms = (time.perf_counter() - t0) * 1000.0
-        sw, sh = doc.dimensions()
-        nshapes = int(L.vkvg_gb300_svg_shape_count(doc.h))
-        ssurf = gb.Surface(dev, sw, sh)
-        sctx = ssurf.context()
-        simg = np.zeros((sh, sw, 4), np.uint8)
-
-        def svg_step():
-            doc.render(sctx)
-            L.vkvg_flush(sctx.h)
-            assert L.vkvg_surface_write_to_memory(ssurf.h, simg.ctypes.data_as(C.c_void_p)) == 0
-
-        for _ in range(2):
-            svg_step()
-        torch.cuda.synchronize()
-        s_steps = 5
-        t0 = time.perf_counter()
-        for _ in range(s_steps):
-            svg_step()
-        s_t = (time.perf_counter() - t0) / s_steps
-        svg = {"workload": "seeded SVG document (svg_document seed 7), %d shapes, %dx%d, 4x MSAA" % (nshapes, sw, sh),
-               "bytes": len(text), "parse_ms": parse_ms, "render_e2e_ms": s_t * 1000.0,
-               "shapes_per_s": nshapes / s_t, "note": "host timer around vkvg_svg_render + vkvg_flush + "
-                                                      "write_to_memory; not the headline metric"}
-        sctx.destroy()
-        ssurf.destroy()
-        doc.destroy()
-
     # ---- the uneven batch (64 surfaces, Pareto path counts): its frames one
     # after another (the plain form), then as one batch job
     batch = None
@@ -745,8 +708,6 @@ def main():
                      "frame_frac": frame_bytes / (ms / 1000.0) / 1e9 / peak, "issue": issue},
         "clocks": clk,
     }
-    if svg:
-        line["svg"] = svg
     if batch:
         line["batch"] = batch
     if glyphs:

@@ -193,18 +193,6 @@ vkvg_public vkvg_status_t vkvg_gb300_batch_execute(VkvgBatch batch);
 vkvg_public vkvg_status_t vkvg_gb300_batch_timing(VkvgBatch batch, float out[9]);
 vkvg_public void          vkvg_gb300_batch_destroy(VkvgBatch batch);
 
-/* ---- parsed SVG documents, read back for the parity tests (no vkvg
- * counterpart; VkvgSvg is include/vkvg-svg.h's handle).  shape: u = fill
- * paint type, fill colour, stroke paint type, stroke colour (nanoSVG's ABGR
- * words; a gradient gives its first stop), visible, path count; f = opacity,
- * stroke width, bounds[4].  path: its cubic points (x, y pairs), at most
- * cap_points of them copied, and whether it is closed. */
-typedef struct _vkvg_svg_t *VkvgSvgDoc;
-vkvg_public uint32_t vkvg_gb300_svg_shape_count(VkvgSvgDoc svg);
-vkvg_public int      vkvg_gb300_svg_shape(VkvgSvgDoc svg, uint32_t i, char id[64], uint32_t u[6], float f[6]);
-vkvg_public int      vkvg_gb300_svg_path(VkvgSvgDoc svg, uint32_t shape, uint32_t path, float *pts, uint32_t cap_points,
-                                         uint32_t *npts, uint32_t *closed);
-
 /* ---- differentiable analytic coverage (no vkvg counterpart) ----
  *
  * A scene of paths, each a list of closed contours of line and cubic
