@@ -419,11 +419,11 @@ cudaError_t Pipeline::geometry(const FrameHost &f, const gb_surf *surfs, uint64_
            to a wide tile, or the surface is no wider than a narrow one */
         const bool small = !wide || (ws[1] && ws[0] <= 384u * ws[1]);
         narrow           = !(stats && small) ? 0 : mxc <= 128u ? 2 : mxc <= 480u ? 1 : 0;
-        /* the row form pays per row and draw, and per crossing in a lane's
-           run: it wins when the draws span most of a tile with crossings
-           spread thin (mean width over 640 pixels, weighted by edges); on
-           denser, smaller geometry the register tiles do */
-        row_draws = stats && wide && ws[1] && ws[0] > 640u * ws[1];
+        /* the row form wins when many draws (a thousand or more, which
+           amortise its per-tile set-up) span most of a tile (mean width over
+           640 pixels, weighted by edges); measured on the uneven batch's
+           surfaces, the register tiles win everywhere else */
+        row_draws = stats && wide && ndraw >= 1024u && ws[1] && ws[0] > 640u * ws[1];
     }
     GROW(recs, (size_t)(nunits + 1) * 16);
     CK(gb_launch_bin(st, 1, nedge_all, edges.as<int4>(), edge_draw.as<uint32_t>(), draws, surfs, S,
