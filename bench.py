@@ -381,6 +381,64 @@ def analytic_bench(a, gb, torch, np, flush, cpu):
     return out
 
 
+def small_polygon_bench(a, gb, L, np, flush):
+    """The small polygon configuration as stated (512x512, MSAA 4, seed 0):
+    64 closed self-intersecting polygons of 3-32 vertices, each filled
+    NON_ZERO in an opaque colour then stroked black, width 4, miter (10),
+    butt.  Device-resident frames (median of 20, L2 flushed before each) and
+    end to end through the API (replay + flush + write_to_memory)."""
+    import ctypes as C
+
+    from vkvg_gb300 import scenes
+
+    sc = scenes.plain_small()
+    cm, ar = scenes.encode(sc["ops"])
+    dev = gb.Device(samples=4)
+    surf = gb.Surface(dev, sc["width"], sc["height"])
+    ctx = surf.context()
+    assert L.vkvg_gb300_replay_stream(ctx.h, cm.ctypes.data_as(C.c_void_p), len(cm), ar.ctypes.data_as(C.c_void_p),
+                                      len(ar)) == 0
+    frame = L.vkvg_gb300_frame_capture(ctx.h)
+    timing = np.zeros(8, np.float32)
+    for _ in range(3):
+        flush()
+        assert L.vkvg_gb300_frame_execute(frame, surf.h) == 0
+    ms, stages = [], []
+    for _ in range(20):
+        flush()
+        assert L.vkvg_gb300_frame_execute(frame, surf.h) == 0
+        L.vkvg_gb300_frame_timing(frame, timing.ctypes.data_as(C.c_void_p))
+        ms.append(float(timing[4]))
+        stages.append(timing[:4].copy())
+    med = statistics.median(ms)
+    img = np.zeros((sc["height"], sc["width"], 4), np.uint8)
+    ectx = surf.context()
+    e = []
+    for _ in range(10):
+        t0 = time.perf_counter()
+        L.vkvg_gb300_replay_stream(ectx.h, cm.ctypes.data_as(C.c_void_p), len(cm), ar.ctypes.data_as(C.c_void_p),
+                                   len(ar))
+        ectx.flush()
+        L.vkvg_surface_write_to_memory(surf.h, img.ctypes.data_as(C.c_void_p))
+        e.append(time.perf_counter() - t0)
+    e_ms = statistics.median(e) * 1e3
+    st = np.median(np.array(stages), axis=0)
+    out = {"workload": "small polygons 512x512 msaa4 (seed 0): 64 self-intersecting polygons, NON_ZERO fill + "
+                       "black width-4 miter stroke", "paths_per_s": 64 / (med / 1e3), "ms_per_frame": med,
+           "mpx_per_s": 512 * 512 / (med / 1e3) / 1e6,
+           "stage_ms": {"flatten": float(st[0]), "stroke": float(st[1]), "setup_bin": float(st[2]),
+                        "raster": float(st[3])},
+           "e2e": {"ms_per_step": e_ms, "paths_per_s": 64 / (e_ms / 1e3),
+                   "note": "replay of the recorded calls + vkvg_flush + write_to_memory, host timer, median of 10"},
+           "timing": "CUDA events on the library's stream, L2 flushed before each frame, median of 20"}
+    L.vkvg_gb300_frame_destroy(frame)
+    ectx.destroy()
+    ctx.destroy()
+    surf.destroy()
+    dev.destroy()
+    return out
+
+
 def glyph_bench(a, gb, L, np, flush):
     """The large glyph scene (4096x4096, MSAA 4, seed 5): 200,000 quadratic
     glyph outlines with holes (NON_ZERO) and 20,000 round-join strokes under
@@ -650,6 +708,9 @@ def main():
     if not a.no_analytic and world == 1:
         analytic = analytic_bench(a, gb, torch, np, l2_flush, cpu=rank == 0 and not a.no_cpu)
 
+    # ---- the small polygon configuration as stated
+    small = small_polygon_bench(a, gb, L, np, l2_flush) if world == 1 else None
+
     # ---- the large glyph scene (4096x4096, 200k quadratic outlines + 20k strokes)
     glyphs = None
     if not a.no_glyphs and world == 1:
@@ -708,6 +769,8 @@ def main():
                      "frame_frac": frame_bytes / (ms / 1000.0) / 1e9 / peak, "issue": issue},
         "clocks": clk,
     }
+    if small:
+        line["small_polygons"] = small
     if batch:
         line["batch"] = batch
     if glyphs:

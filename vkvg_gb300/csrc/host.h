@@ -110,6 +110,8 @@ struct Pipeline {
     int      form_run   = -1; /* the raster form the last frame ran (as vkvg_gb300_debug_set_raster_form) */
     int      form_half  = 0;  /* the row form ran in half bands with 16-bit counters */
     bool     row_draws  = false; /* the frame's draws span most of a 1024-pixel tile (the row form's case) */
+    double   mean_width = 0.0;   /* edge-weighted mean draw width of a one-surface frame, pixels */
+    bool     sparse_crossings(uint64_t ncells_run); /* records per active cell thin enough for the row form */
     uint32_t max_cell   = 0xFFFFFFFFu; /* record units of the heaviest cell (one-surface frames; else unknown) */
     uint64_t launches   = 0;
     uint64_t upload_bytes = 0;

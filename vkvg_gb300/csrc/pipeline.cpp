@@ -419,11 +419,11 @@ cudaError_t Pipeline::geometry(const FrameHost &f, const gb_surf *surfs, uint64_
            to a wide tile, or the surface is no wider than a narrow one */
         const bool small = !wide || (ws[1] && ws[0] <= 384u * ws[1]);
         narrow           = !(stats && small) ? 0 : mxc <= 128u ? 2 : mxc <= 480u ? 1 : 0;
-        /* the row form wins when many draws (a thousand or more, which
-           amortise its per-tile set-up) span most of a tile (mean width over
-           640 pixels, weighted by edges); measured on the uneven batch's
-           surfaces, the register tiles win everywhere else */
-        row_draws = stats && wide && ndraw >= 1024u && ws[1] && ws[0] > 640u * ws[1];
+        /* candidates for the row form: draws that span most of a tile (mean
+           width over 640 pixels, weighted by edges); the raster launch then
+           checks how thinly their crossings spread */
+        row_draws  = stats && wide && ws[1] && ws[0] > 640u * ws[1];
+        mean_width = ws[1] ? (double)ws[0] / (double)ws[1] : 0.0;
     }
     GROW(recs, (size_t)(nunits + 1) * 16);
     CK(gb_launch_bin(st, 1, nedge_all, edges.as<int4>(), edge_draw.as<uint32_t>(), draws, surfs, S,
@@ -448,6 +448,21 @@ cudaError_t Pipeline::geometry(const FrameHost &f, const gb_surf *surfs, uint64_
     if (timing)
         CK(cudaEventRecord(evs[3], st));
     return cudaSuccess;
+}
+
+/* The row form spends per crossing in a lane's run of 32 samples (a walk
+   over the run's flagged positions), the register tiles per sample: the
+   row form wins (the curve-heavy scene) when a draw's records per band,
+   spread over its width in runs, stay near one per run, and loses two- to
+   fourfold on denser geometry (the uneven batch's surfaces: hundreds of
+   segments in one bounding box).  Records per active cell over the mean
+   draw width in runs below 3 picks it. */
+bool Pipeline::sparse_crossings(uint64_t ncells_run) {
+    uint32_t active = 0;
+    if (readback_u32(*this, apos.as<uint32_t>() + ncells_run, &active, 1) != cudaSuccess || !active)
+        return false;
+    const double runs = mean_width / 32.0;
+    return runs > 0.0 && (double)nunits / (double)active < 3.0 * runs;
 }
 
 cudaError_t Pipeline::run(const FrameHost &f, _vkvg_surface_t *surf, bool timing) {
@@ -602,7 +617,7 @@ cudaError_t Pipeline::run(const FrameHost &f, _vkvg_surface_t *surf, bool timing
     if (clip_use)
         form = 0; /* only the register tile carries the clip planes */
     else if (form < 0 || form > 4)
-        form = narrow ? narrow : row_draws ? 3 : 0;
+        form = narrow ? narrow : row_draws && sparse_crossings((uint64_t)nbands * ndraw) ? 3 : 0;
     if (form == 3 && max_cell >= 32768u)
         form = 4; /* 16-bit counters would not hold a cell's crossings: whole bands */
     form_run  = form;
