@@ -505,6 +505,27 @@ def glyph_bench(a, gb, L, np, flush):
            "e2e": {"ms_per_step": e_ms, "paths_per_s": paths / (e_ms / 1e3),
                    "note": "replay of the recorded calls + vkvg_flush + write_to_memory, host timer"},
            "scene_build_s": gen_s, "timing": "CUDA events on the library's stream, L2 flushed before each frame"}
+    # the same frame as a batch of one surface: sizing, tuning, then timed
+    # replays of its CUDA graph
+    tgt = gb.Surface(dev, size, size)
+    bt = L.vkvg_gb300_batch_create((C.c_void_p * 1)(frame), (C.c_void_p * 1)(tgt.h), 1)
+    if bt:
+        for _ in range(14):
+            flush()
+            assert L.vkvg_gb300_batch_execute(bt) == 0
+        bms = []
+        bi = np.zeros(9, np.float32)
+        for _ in range(3):
+            flush()
+            assert L.vkvg_gb300_batch_execute(bt) == 0
+            L.vkvg_gb300_batch_timing(bt, bi.ctypes.data_as(C.c_void_p))
+            bms.append(float(bi[0]))
+        out["batch"] = {"ms_per_frame": statistics.median(bms), "graph_replay": bool(bi[1]),
+                        "tile_px": int(bi[8]), "equal_to_frame": bool(np.array_equal(tgt.samples_rgba(),
+                                                                                       surf.samples_rgba())),
+                        "timing": "CUDA events around the graph launch, L2 flushed before each, median of 3"}
+        L.vkvg_gb300_batch_destroy(bt)
+    tgt.destroy()
     L.vkvg_gb300_frame_destroy(frame)
     ectx.destroy()
     ctx.destroy()
@@ -675,7 +696,7 @@ def main():
         ta = (C.c_void_p * len(btarget))(*[s2.h for s2 in btarget])
         bt = L.vkvg_gb300_batch_create(fa, ta, len(bframes))
         assert bt
-        for _ in range(12):  # sizing, ten tuning runs, graph capture
+        for _ in range(14):  # sizing, twelve tuning runs, graph capture
             assert L.vkvg_gb300_batch_execute(bt) == 0
         torch.cuda.synchronize()
         t0 = time.perf_counter()

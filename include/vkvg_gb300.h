@@ -178,11 +178,13 @@ vkvg_public vkvg_status_t vkvg_gb300_exclusive_scan_noalloc(void *stream, const 
  * (vkvg_gb300_frame_capture), each for its own surface, rendered as one job:
  * one pass of the geometry kernels over all of them and one persistent
  * raster launch over every surface's bands, heaviest first.  The first
- * execution sizes the job, the next ten time candidate raster settings
+ * execution sizes the job, the next twelve time candidate raster settings
  * (tile width, stage threshold, work-list order; kept per class of scene
- * for later batches), later ones replay a CUDA
- * graph of the whole job.  Frames with clip or pattern sources, or a surface
- * with an active clip, are not batched (create returns null).  Each surface
+ * for later batches), later ones replay a CUDA graph of the whole job.
+ * Pattern sources (gradients, surface sources) are batched: each surface's
+ * source images are filled into a block of their own every execution.
+ * Frames with clip, or a surface with an active clip, are not batched
+ * (create returns null).  Each surface
  * ends as vkvg_gb300_frame_execute of its frame would leave it.
  * timing out: [0] last execution ms, [1] it was a graph replay, [2] stage
  * threshold, [3] heaviest-first order, [4] work items, [5] surfaces,

@@ -422,13 +422,48 @@ def test_batch_matches_frames(gb):
     bt = L.vkvg_gb300_batch_create(frames, targets, len(cases))
     assert bt
     t = np.zeros(9, np.float32)
-    for run in range(13):  # sizing, ten tuning runs, graph capture and a replay
+    for run in range(15):  # sizing, twelve tuning runs, graph capture and a replay
         assert L.vkvg_gb300_batch_execute(bt) == 0, run
         L.vkvg_gb300_batch_timing(bt, t.ctypes.data_as(C.c_void_p))
         for k, (a, b, _, _) in enumerate(cases):
             assert np.array_equal(a.samples_rgba(), b.samples_rgba()), (run, k)
             assert np.array_equal(a.image(), b.image()), (run, k)
     assert t[1] == 1 and t[6] == 1 and t[5] == len(cases)  # graph replay, tuned
+    L.vkvg_gb300_batch_destroy(bt)
+    for _, _, ctx, fr in cases:
+        L.vkvg_gb300_frame_destroy(fr)
+        ctx.destroy()
+
+
+def test_batch_gradient_sources(gb, vko):
+    """frames with pattern sources in a batch (linear and radial gradients,
+    several per frame, a glyph crop under one gradient, and a frame without
+    any): every surface equals its own frame's result and the oracle's, on
+    the sizing run, tuning runs over every tile form and graph replays"""
+    import ctypes as C
+
+    L = gb.lib()
+    dev = gb.Device(samples=4)
+    scs = [scenes.gradient_mix(n_items=6, size=144, seed=9, samples=4),
+           scenes.gradient_mix(n_items=5, size=200, seed=3, samples=4, radial=True),
+           scenes.glyph_scene(n_outlines=200, n_strokes=20, size=160),
+           scenes.curve_heavy(n_paths=8, size=120, seed=4, n_min=3, n_max=6)]
+    cases = [_batch_case(gb, dev, sc) for sc in scs]
+    frames = (C.c_void_p * len(cases))(*[c[3] for c in cases])
+    targets = (C.c_void_p * len(cases))(*[c[1].h for c in cases])
+    bt = L.vkvg_gb300_batch_create(frames, targets, len(cases))
+    assert bt
+    oracle = [pu.run_oracle(vko, sc)[0] for sc in scs]
+    t = np.zeros(9, np.float32)
+    for run in range(15):
+        assert L.vkvg_gb300_batch_execute(bt) == 0, run
+        L.vkvg_gb300_batch_timing(bt, t.ctypes.data_as(C.c_void_p))
+        for k, (a, b, _, _) in enumerate(cases):
+            assert np.array_equal(a.samples_rgba(), b.samples_rgba()), (run, k)
+            if run in (0, 14):
+                assert np.array_equal(b.samples_rgba(), oracle[k].samples_rgba()), (run, k)
+                assert np.array_equal(b.image(), oracle[k].image()), (run, k)
+    assert t[1] == 1 and t[6] == 1
     L.vkvg_gb300_batch_destroy(bt)
     for _, _, ctx, fr in cases:
         L.vkvg_gb300_frame_destroy(fr)
@@ -515,9 +550,9 @@ def test_batch_streams_match_oracle(gb, vko):
     bt = L.vkvg_gb300_batch_create(frames, targets, len(cases))
     assert bt
     oracle = [pu.run_oracle(vko, sc, threads=8)[0] for sc in scs]
-    for run in range(13):  # sizing, tuning runs, graph capture and a replay
+    for run in range(15):  # sizing, tuning runs, graph capture and a replay
         assert L.vkvg_gb300_batch_execute(bt) == 0, run
-        if run in (0, 5, 12):
+        if run in (0, 5, 11, 14):
             for k, (a, b, _, _) in enumerate(cases):
                 assert np.array_equal(b.samples_rgba(), oracle[k].samples_rgba()), (run, k)
                 assert np.array_equal(b.image(), oracle[k].image()), (run, k)

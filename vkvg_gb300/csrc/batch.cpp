@@ -25,10 +25,12 @@ namespace {
 struct RasterParams {
     uint32_t stage_min;  /* cells of fewer record units skip the shared-memory stage */
     bool     cost_order; /* work list heaviest first (else surface, band, tile order) */
-    int      form;       /* tiles: 0 1024 pixels (one CTA per SM), 1 256 (four), 2 512 (two) */
+    int      form;       /* tiles: 0 1024 pixels (one CTA per SM), 1 256 (four), 2 512 (two), 3 128 (eight) */
 };
 const RasterParams CANDIDATES[] = {{0, true, 0}, {8, true, 0}, {32, true, 0}, {0, false, 0}, {0, true, 2},
-                                   {8, true, 2}, {32, true, 2}, {0, true, 1}, {8, true, 1}, {32, true, 1}};
+                                   {8, true, 2}, {32, true, 2}, {0, true, 1}, {8, true, 1}, {32, true, 1},
+                                   {0, true, 3}, {32, true, 3}};
+constexpr int NFORMS = 4;
 constexpr int      NCAND        = sizeof(CANDIDATES) / sizeof(CANDIDATES[0]);
 
 /* the tuner's choice per class of scene: surfaces, draws and record units,
@@ -53,7 +55,12 @@ struct _vkvg_gb300_batch_t {
     std::vector<gb_surf> tab;
     DevBuf               d_tab, d_items, d_queue, d_idx, d_units;
     PinnedBuf            h_stage;
-    std::vector<uint4>   items_cost[3], items_plain[3]; /* the work lists (per tile form) in both orders */
+    std::vector<uint4>   items_cost[NFORMS], items_plain[NFORMS]; /* the work lists (per tile form) in both orders */
+    /* pattern source images: per surface, its frame's images [n][H][W] in
+       one buffer; the merged frame's gradient records in the same order */
+    DevBuf                d_grad;
+    std::vector<uint32_t> grad_surf; /* per merged gradient record: its surface */
+    std::vector<size_t>   grad_off;  /* per merged gradient record: its image's offset in d_grad, words */
     uint64_t             ncells  = 0;
     uint64_t             every   = 0; /* cells of the draws that act on every band */
     uint32_t             samples = 0;
@@ -73,14 +80,16 @@ namespace {
 
 /* append frame k's arrays to the merged frame, indices rebased */
 bool merge_frame(FrameHost &m, const FrameHost &f, uint32_t k) {
-    if (!f.grads.empty())
-        return false; /* pattern sources are not batched */
     const uint32_t seg0 = (uint32_t)m.seg_info.size(), sub0 = (uint32_t)m.sub_seg0.size();
     const uint32_t draw0 = (uint32_t)m.draws.size(), sp0 = (uint32_t)m.spair_draw.size();
     const uint32_t dash0 = (uint32_t)m.dashes.size(), th0 = (uint32_t)m.thetas.size();
     for (const gb_draw &d : f.draws)
-        if (d.kind >= GB_DRAW_CLIP_EO || d.gsrc)
-            return false; /* nor clip */
+        if (d.kind >= GB_DRAW_CLIP_EO)
+            return false; /* clip is not batched */
+    /* pattern sources: a draw's gsrc stays an index into its own frame's
+       images, which its surface's table entry points at */
+    m.grads.insert(m.grads.end(), f.grads.begin(), f.grads.end());
+    m.sources.insert(m.sources.end(), f.sources.begin(), f.sources.end());
     for (size_t i = 0; i < f.seg_info.size(); i++) {
         m.seg_info.push_back(f.seg_info[i]);
         m.seg_n.push_back(f.seg_n[i]);
@@ -174,7 +183,7 @@ cudaError_t build_items(VkvgBatch b) {
     BCK(cudaStreamSynchronize(pl.st));
     memcpy(off.data(), b->h_stage.p, n * 4);
     size_t tot = 0;
-    for (int nw = 0; nw < 3; nw++) {
+    for (int nw = 0; nw < NFORMS; nw++) {
         const uint32_t                          tw = gb_raster_tile_width(nw);
         std::vector<std::pair<uint32_t, uint4>> costed;
         b->items_plain[nw].clear();
@@ -204,7 +213,7 @@ cudaError_t build_items(VkvgBatch b) {
     if (!b->d_items.grow(std::max<size_t>(tot * 16, 16)) || !b->h_stage.grow(std::max<size_t>(tot * 16, 64)))
         return cudaErrorMemoryAllocation;
     uint8_t *h = (uint8_t *)b->h_stage.p;
-    for (int nw = 0; nw < 3; nw++) {
+    for (int nw = 0; nw < NFORMS; nw++) {
         memcpy(h, b->items_plain[nw].data(), b->items_plain[nw].size() * 16);
         h += b->items_plain[nw].size() * 16;
         memcpy(h, b->items_cost[nw].data(), b->items_cost[nw].size() * 16);
@@ -218,9 +227,9 @@ cudaError_t build_items(VkvgBatch b) {
    unless sized), the batch raster with settings p, the status read back */
 cudaError_t run_batch(VkvgBatch b, bool sized, const RasterParams &p) {
     Pipeline &pl = b->pl;
-    bool wide = false; /* the x extents serve the narrow tiles' candidates too */
+    bool wide = false; /* the draws' x extents, for every tile width a candidate uses (down to 128 pixels) */
     for (const gb_surf &s : b->tab)
-        wide |= s.W > gb_raster_tile_width(1);
+        wide |= s.W > gb_raster_tile_width(3);
     BCK(pl.geometry(b->merged, b->d_tab.as<gb_surf>(), b->ncells, b->every, wide, b->samples, false, sized));
     if (!sized)
         BCK(build_items(b));
@@ -241,10 +250,17 @@ cudaError_t run_batch(VkvgBatch b, bool sized, const RasterParams &p) {
     A0.nunits    = pl.nunits;
     A0.status    = pl.status.as<uint32_t>();
     A0.stage_min = p.stage_min;
+    /* every surface's pattern source images (its frame's gradients and surface sources) */
+    const gb_grad *g = (const gb_grad *)((const uint8_t *)pl.in.p + pl.o_grads);
+    for (size_t i = 0; i < b->grad_surf.size(); i++) {
+        const gb_surf &s = b->tab[b->grad_surf[i]];
+        BCK(gb_launch_gradient_fill(pl.st, s.W, s.H, g + i, b->d_grad.as<uint32_t>() + b->grad_off[i]));
+    }
+    gb_count_launch(b->grad_surf.size());
     BCK(cudaMemsetAsync(b->d_queue.p, 0, 4, pl.st));
     BCK(gb_launch_raster_batch(pl.st, &A0, b->d_tab.as<gb_surf>(),
                                b->d_items.as<uint4>() + base + (p.cost_order ? ni : 0),
-                               ni, b->d_queue.as<uint32_t>(), b->nctas, p.form));
+                               ni, b->d_queue.as<uint32_t>(), b->nctas, p.form, b->grad_surf.empty() ? 0 : 1));
     gb_count_launch(ni ? 1 : 0);
     return cudaMemcpyAsync(pl.rb.p, pl.status.p, 4, cudaMemcpyDeviceToHost, pl.st);
 }
@@ -274,7 +290,15 @@ VkvgBatch vkvg_gb300_batch_create(VkvgFrame *frames, VkvgSurface *targets, uint3
             break;
         b->samples          = s->samples;
         const uint32_t d0   = (uint32_t)b->merged.draws.size();
+        const size_t   g0   = b->merged.grads.size();
         ok                  = merge_frame(b->merged, fr->frame, k);
+        size_t gwords = 0; /* the images before this surface's */
+        for (size_t gi = 0; gi < b->grad_off.size(); gi++)
+            gwords = std::max(gwords, b->grad_off[gi] + (size_t)b->tab[b->grad_surf[gi]].W * b->tab[b->grad_surf[gi]].H);
+        for (size_t gi = g0; ok && gi < b->merged.grads.size(); gi++) {
+            b->grad_surf.push_back(k);
+            b->grad_off.push_back(gwords + (gi - g0) * (size_t)s->width * s->height);
+        }
         gb_surf e;
         memset(&e, 0, sizeof(e));
         e.W       = s->width;
@@ -296,6 +320,16 @@ VkvgBatch vkvg_gb300_batch_create(VkvgFrame *frames, VkvgSurface *targets, uint3
     }
     if (ok && !b->merged.sdraw_id.empty())
         b->merged.sdraw_pair0.push_back((uint32_t)b->merged.spair_draw.size());
+    if (ok && !b->grad_surf.empty()) {
+        /* one buffer for every surface's source images; each surface's entry
+           points at its first */
+        size_t words = 0;
+        for (size_t gi = 0; gi < b->grad_off.size(); gi++)
+            words = std::max(words, b->grad_off[gi] + (size_t)b->tab[b->grad_surf[gi]].W * b->tab[b->grad_surf[gi]].H);
+        ok = b->d_grad.grow(words * 4);
+        for (size_t gi = b->grad_off.size(); ok && gi-- > 0;)
+            b->tab[b->grad_surf[gi]].gsrc = b->d_grad.as<uint32_t>() + b->grad_off[gi];
+    }
     const size_t tb = b->tab.size() * sizeof(gb_surf);
     ok = ok && b->pl.upload(b->merged) == cudaSuccess && b->d_tab.grow(tb) && b->h_stage.grow(tb);
     if (ok) {
@@ -422,7 +456,7 @@ void vkvg_gb300_batch_destroy(VkvgBatch b) {
     if (b->exec)
         cudaGraphExecDestroy(b->exec);
     b->pl.destroy();
-    DevBuf *bufs[] = {&b->d_tab, &b->d_items, &b->d_queue, &b->d_idx, &b->d_units};
+    DevBuf *bufs[] = {&b->d_tab, &b->d_items, &b->d_queue, &b->d_idx, &b->d_units, &b->d_grad};
     for (DevBuf *d : bufs)
         d->release();
     b->h_stage.release();

@@ -92,6 +92,7 @@ typedef struct {
     uint64_t  cell0;
     uint32_t *samples; /* [nrows][wpad] premultiplied RGBA8 */
     uint32_t *rgba;    /* [H][W] resolved */
+    const uint32_t *gsrc; /* the surface's pattern source images [n][H][W] (batches; else null) */
 } gb_surf;
 
 /* A pattern source as vkvg's fragment stage sees it (shaders/vkvg_main.frag

@@ -143,7 +143,7 @@ cudaError_t gb_launch_gather_u32(cudaStream_t st, uint32_t n, const uint64_t *id
    items (queue: a zeroed counter), nctas SMs' worth of CTAs, tiles of the
    given form (as gb_raster_tile_width) */
 cudaError_t gb_launch_raster_batch(cudaStream_t st, const gb_raster_args *a, const gb_surf *surfs, const uint4 *items,
-                                   uint32_t nitems, uint32_t *queue, uint32_t nctas, int form);
+                                   uint32_t nitems, uint32_t *queue, uint32_t nctas, int form, int gradients);
 /* the row form of the raster (one warp per sample row, samples in shared
    memory, a producer warp staging each draw's records through a ring of
    slots): one CTA per (1024-pixel tile, band), or with half per (tile, half

@@ -140,7 +140,7 @@ __device__ __forceinline__ void cur_load(draw_cursor &c, const gb_raster_args &A
             /* paint, clear and the clip kinds act on every band; the others only
                where they have geometry */
             act = kind == GB_DRAW_PAINT || (CLIP ? kind >= GB_DRAW_CLEAR : kind == GB_DRAW_CLEAR) || lo != hi;
-            if (rg.tiles && act && kind <= GB_DRAW_STROKE) {
+            if (rg.tiles && act && kind <= GB_DRAW_STROKE && A.dbox) {
                 const int2 bx = A.dbox[dl];
                 act           = bx.x <= rg.tx_hi && -bx.y >= rg.tx_lo;
             }
@@ -755,7 +755,7 @@ __device__ __forceinline__ void mbar_inval(uint32_t bar) {
    wait on other CTAs: each CTA stops at the end of the list).  An item's
    arguments are its surface's entry of the table over A0's shared fields,
    staged in shared memory for the whole CTA. */
-template <int NW>
+template <int NW, bool GRAD>
 __global__ void __launch_bounds__(XT<NW>::THREADS, XT<NW>::MINB)
     gb_raster_batch(gb_raster_args A0, const gb_surf *__restrict__ surfs, const uint4 *__restrict__ items,
                     uint32_t nitems, uint32_t *__restrict__ queue) {
@@ -784,9 +784,10 @@ __global__ void __launch_bounds__(XT<NW>::THREADS, XT<NW>::MINB)
                 a.cell_off        = A0.cell_off + sf.cell0;
                 a.apos            = A0.apos + sf.cell0;
                 a.cell0           = (uint32_t)sf.cell0;
-                a.dbox            = A0.dbox + sf.draw0;
+                a.dbox            = A0.dbox ? A0.dbox + sf.draw0 : nullptr;
                 a.samples         = sf.samples;
                 a.rgba            = sf.rgba;
+                a.gsrc            = sf.gsrc;
                 Ai                = a;
                 cur_band          = w.y;
                 cur_tile          = w.z;
@@ -795,7 +796,7 @@ __global__ void __launch_bounds__(XT<NW>::THREADS, XT<NW>::MINB)
         __syncthreads();
         if (cur_item >= nitems)
             break;
-        raster_item<NW, false, false>(Ai, C0, smem, cur_band, cur_tile);
+        raster_item<NW, GRAD, false>(Ai, C0, smem, cur_band, cur_tile);
         __syncthreads();
         if (threadIdx.x == 0) { /* the next item initialises them again */
             const uint32_t bar0 = (uint32_t)__cvta_generic_to_shared(smem) + XT<NW>::S_MBAR * 4;
@@ -1015,18 +1016,31 @@ extern "C" cudaError_t gb_launch_unpremultiply(cudaStream_t st, const uint32_t *
     return cudaGetLastError();
 }
 
-template <int NW> cudaError_t raster_batch_nw(cudaStream_t st, const gb_raster_args *a, const gb_surf *surfs,
-                                               const uint4 *items, uint32_t nitems, uint32_t *queue, uint32_t nctas) {
+template <int NW, bool GRAD>
+cudaError_t raster_batch_nw(cudaStream_t st, const gb_raster_args *a, const gb_surf *surfs, const uint4 *items,
+                            uint32_t nitems, uint32_t *queue, uint32_t nctas) {
     static bool configured = false;
     if (!configured) {
-        cudaError_t e =
-            cudaFuncSetAttribute(gb_raster_batch<NW>, cudaFuncAttributeMaxDynamicSharedMemorySize, XT<NW>::SMEM);
+        cudaError_t e = cudaFuncSetAttribute(gb_raster_batch<NW, GRAD>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             XT<NW>::SMEM);
         if (e != cudaSuccess)
             return e;
         configured = true;
     }
-    gb_raster_batch<NW><<<nctas * XT<NW>::MINB, XT<NW>::THREADS, XT<NW>::SMEM, st>>>(*a, surfs, items, nitems, queue);
+    gb_raster_batch<NW, GRAD>
+        <<<nctas * XT<NW>::MINB, XT<NW>::THREADS, XT<NW>::SMEM, st>>>(*a, surfs, items, nitems, queue);
     return cudaGetLastError();
+}
+template <bool GRAD>
+static cudaError_t raster_batch_form(cudaStream_t st, const gb_raster_args *a, const gb_surf *surfs,
+                                     const uint4 *items, uint32_t nitems, uint32_t *queue, uint32_t nctas, int form) {
+    if (form == 1)
+        return raster_batch_nw<XT_NARROW, GRAD>(st, a, surfs, items, nitems, queue, nctas);
+    if (form == 2)
+        return raster_batch_nw<XT_MID, GRAD>(st, a, surfs, items, nitems, queue, nctas);
+    if (form == 3)
+        return raster_batch_nw<XT_TINY, GRAD>(st, a, surfs, items, nitems, queue, nctas);
+    return raster_batch_nw<XT_WIDE, GRAD>(st, a, surfs, items, nitems, queue, nctas);
 }
 template <int NW, bool GRAD, bool CLIP> cudaError_t raster_nw(cudaStream_t st, const gb_raster_args *a,
                                                               const gb_clip_args *c) {
@@ -1048,14 +1062,11 @@ extern "C" uint32_t gb_raster_tile_width(int form) {
 }
 extern "C" cudaError_t gb_launch_raster_batch(cudaStream_t st, const gb_raster_args *a, const gb_surf *surfs,
                                              const uint4 *items, uint32_t nitems, uint32_t *queue, uint32_t nctas,
-                                             int form) {
+                                             int form, int gradients) {
     if (!nitems)
         return cudaSuccess;
-    if (form == 1)
-        return raster_batch_nw<XT_NARROW>(st, a, surfs, items, nitems, queue, nctas);
-    if (form == 2)
-        return raster_batch_nw<XT_MID>(st, a, surfs, items, nitems, queue, nctas);
-    return raster_batch_nw<XT_WIDE>(st, a, surfs, items, nitems, queue, nctas);
+    return gradients ? raster_batch_form<true>(st, a, surfs, items, nitems, queue, nctas, form)
+                     : raster_batch_form<false>(st, a, surfs, items, nitems, queue, nctas, form);
 }
 /* frames without gradient draws or clipping run the variants without that
    code; frames with clipping run the wide form */

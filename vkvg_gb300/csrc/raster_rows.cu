@@ -291,7 +291,7 @@ __device__ __forceinline__ bool rows_item(const gb_raster_args &A, int32_t *smem
                         atomicOr(A.status, GB_ERR_OVERFLOW);
                         act = false;
                     }
-                    if (tiles && act && kind <= GB_DRAW_STROKE) {
+                    if (tiles && act && kind <= GB_DRAW_STROKE && A.dbox) {
                         const int2 bx = A.dbox[dl];
                         act           = bx.x <= tx_hi && -bx.y >= tx_lo;
                     }
@@ -658,7 +658,7 @@ __global__ void __launch_bounds__(RW16::THREADS, 1)
                 a.cell_off        = A0.cell_off + sf.cell0;
                 a.apos            = A0.apos + sf.cell0;
                 a.cell0           = (uint32_t)sf.cell0;
-                a.dbox            = A0.dbox + sf.draw0;
+                a.dbox            = A0.dbox ? A0.dbox + sf.draw0 : nullptr;
                 a.samples         = sf.samples;
                 a.rgba            = sf.rgba;
                 Ai                = a;
