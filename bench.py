@@ -178,6 +178,77 @@ def cpu_sample(n_paths, size, threads, reps=1):
     return n_paths / min(times), min(times)
 
 
+def analytic_glyph_bench(a, gb, torch, np, flush, tile=128):
+    """The large glyph configuration in the differentiable analytic mode
+    (4096x4096 fp32 canvas, 200,000 quadratic outlines elevated to cubics,
+    20,000 closed strokes, seed 5; the target is the same construction from
+    seed 6): the tiled evaluation (tiles of `tile` pixels, every tile's area
+    planes resident), forward and forward + backward timed with CUDA events
+    (median of 3 after 2 warm-ups, L2 flushed), the device memory the scene
+    holds, and the gradient of the outline control points (on-curve and
+    off-curve points, through the elevation's transpose)."""
+    from vkvg_gb300 import scenes
+
+    t0 = time.perf_counter()
+    scene, par, quad = scenes.analytic_glyph_scene(seed=5)
+    tscene, tpar, _ = scenes.analytic_glyph_scene(seed=6)
+    gen_s = time.perf_counter() - t0
+    # the target: the seed-6 draw of the construction, rendered by its own scene
+    T = gb.Analytic(tscene, tile=tile)
+    td = {k: torch.tensor(v, device="cuda") for k, v in tpar.items()}
+    canvas, _ = T.forward(td["ctrl"], td["colors"], td["widths"])
+    target = canvas.clone()
+    assert T.sync() == 0
+    T.destroy()
+    del td, canvas, T
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    A = gb.Analytic(scene, tile=tile)
+    d = {k: torch.tensor(v, device="cuda") for k, v in par.items()}
+    A.forward(d["ctrl"], d["colors"], d["widths"], target)
+    grads = A.backward()
+    assert A.sync() == 0
+    free1, _ = torch.cuda.mem_get_info()
+    st = torch.cuda.current_stream()
+
+    def timed(fn):
+        for _ in range(2):
+            flush()
+            fn()
+        ts = []
+        for _ in range(3):
+            flush()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            fn()
+            e1.record(st)
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        return statistics.median(ts)
+
+    fwd_ms = timed(lambda: A.forward(d["ctrl"], d["colors"], d["widths"], target))
+
+    def fb():
+        A.forward(d["ctrl"], d["colors"], d["widths"], target)
+        A.backward(grads=grads)
+
+    fb_ms = timed(fb)
+    assert A.sync() == 0
+    loss = float(A.loss.item())
+    gP, gQ = scenes.elevate_adjoint(quad, grads[0].cpu().numpy())
+    out = {"workload": "analytic fp32 4096x4096 (seed 5; target seed 6): 200000 quadratic outlines with holes "
+                       "(fill), 20000 closed strokes, %d cubic segments after elevation, tiles of %d px" %
+                       (len(scene["seg_kind"]), tile),
+           "fwd_ms": fwd_ms, "fwd_bwd_ms": fb_ms, "fwd_bwd_over_fwd": fb_ms / fwd_ms, "loss": loss,
+           "layers": int(A.nlayers), "device_bytes": int(free0 - free1), "scene_build_s": gen_s,
+           "outline_grad_norm": {"on_curve": float(np.linalg.norm(gP)), "off_curve": float(np.linalg.norm(gQ))},
+           "timing": "CUDA events on the scene's stream, L2 flushed before each, median of 3",
+           "checked": "tests/test_analytic.py: tiled == whole canvas; the construction on a 192x192 crop against the "
+                      "FP64 reference"}
+    A.destroy()
+    return out
+
+
 def cpu_scene_time(sc, threads, reps=3):
     """median wall time of the CPU restatement rendering one scene (its
     sources included) with the given raster worker threads"""
@@ -728,6 +799,8 @@ def main():
     analytic = None
     if not a.no_analytic and world == 1:
         analytic = analytic_bench(a, gb, torch, np, l2_flush, cpu=rank == 0 and not a.no_cpu)
+        if not a.no_glyphs:
+            analytic["glyphs"] = analytic_glyph_bench(a, gb, torch, np, l2_flush)
 
     # ---- the small polygon configuration as stated
     small = small_polygon_bench(a, gb, L, np, l2_flush) if world == 1 else None

@@ -238,6 +238,20 @@ vkvg_public VkvgAnalytic  vkvg_gb300_analytic_create(uint32_t width, uint32_t he
                                                      const uint32_t *path_flags, uint32_t ncontours,
                                                      const uint32_t *contour_nseg, uint32_t nseg,
                                                      const uint8_t *seg_kind);
+/* The same scene evaluated in square tiles of `tile` pixels (16 to 4096):
+   after the flattening, each layer's box gives the tiles it reaches (a layer
+   is zero outside its box), and every tile runs the coverage and compositing
+   of its own layers, its area planes kept resident for the backward (memory:
+   the sum over tiles of tile pixels x layers reaching the tile, four bytes
+   each, plus a sixteenth of that in checkpoints of sixteen bytes).  For
+   canvases whose whole-canvas planes would not fit (a 4096 x 4096 canvas of
+   200,000 glyph outlines); results equal the whole-canvas scene's.  A tiled
+   forward waits once for the per-tile layer counts. */
+vkvg_public VkvgAnalytic  vkvg_gb300_analytic_create_tiled(uint32_t width, uint32_t height, uint32_t tile,
+                                                           const float background[4], uint32_t npaths,
+                                                           const uint32_t *path_ncontours, const uint32_t *path_flags,
+                                                           uint32_t ncontours, const uint32_t *contour_nseg,
+                                                           uint32_t nseg, const uint8_t *seg_kind);
 vkvg_public void          vkvg_gb300_analytic_destroy(VkvgAnalytic a);
 vkvg_public vkvg_status_t vkvg_gb300_analytic_status(VkvgAnalytic a);
 vkvg_public uint32_t      vkvg_gb300_analytic_control_point_count(VkvgAnalytic a);

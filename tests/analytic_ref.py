@@ -36,8 +36,13 @@ def _p(a):
     return a.ctypes.data_as(C.c_void_p) if a is not None else None
 
 
-def _f64(a):
-    return np.ascontiguousarray(a, np.float64)
+def _f64(a, n=None):
+    """a as contiguous float64; n: the number of values it must hold (the C
+    reference indexes it by the scene's structure)"""
+    a = np.ascontiguousarray(a, np.float64)
+    if n is not None and a.size != n:
+        raise ValueError("want %d values, got %d" % (n, a.size))
+    return a
 
 
 class Reference:
@@ -65,8 +70,11 @@ class Reference:
     def __del__(self):
         self.close()
 
+    def _ctrl(self, ctrl):
+        return _f64(ctrl, 2 * self.nctrl)
+
     def flatten(self, ctrl):
-        ctrl = _f64(ctrl)
+        ctrl = self._ctrl(ctrl)
         seg = np.zeros(len(self.s["seg_kind"]) + 1, np.uint32)
         n = lib().vko_an_flatten(self.h, _p(ctrl), None, None, 0, _p(seg))
         f32 = np.zeros((max(n, 1), 2), np.float32)
@@ -77,8 +85,9 @@ class Reference:
     def forward(self, ctrl, colors, widths, target=None, area=False):
         canvas = np.zeros((self.H, self.W, 4), np.float64)
         A = np.zeros((self.nlayers, self.H, self.W), np.float64) if area else None
-        t = _f64(target) if target is not None else None
-        loss = lib().vko_an_forward(self.h, _p(_f64(ctrl)), _p(_f64(colors)), _p(_f64(widths)), _p(t),
+        t = _f64(target, 4 * self.W * self.H) if target is not None else None
+        loss = lib().vko_an_forward(self.h, _p(self._ctrl(ctrl)), _p(_f64(colors, 4 * self.npaths)),
+                                    _p(_f64(widths, self.npaths)), _p(t),
                                     _p(canvas), _p(A))
         return (canvas, loss, A) if area else (canvas, loss)
 
@@ -88,9 +97,10 @@ class Reference:
         d_col = np.zeros((self.npaths, 4), np.float64)
         d_w = np.zeros(self.npaths, np.float64)
         d_pts = np.zeros((max(len(self.flatten(ctrl)[0]), 1), 2), np.float64) if points else None
-        t = _f64(target) if target is not None else None
-        g = _f64(d_canvas) if d_canvas is not None else None
-        loss = lib().vko_an_backward(self.h, _p(_f64(ctrl)), _p(_f64(colors)), _p(_f64(widths)), _p(t), _p(g),
+        t = _f64(target, 4 * self.W * self.H) if target is not None else None
+        g = _f64(d_canvas, 4 * self.W * self.H) if d_canvas is not None else None
+        loss = lib().vko_an_backward(self.h, _p(self._ctrl(ctrl)), _p(_f64(colors, 4 * self.npaths)),
+                                     _p(_f64(widths, self.npaths)), _p(t), _p(g),
                                      _p(d_ctrl), _p(d_col), _p(d_w), _p(d_pts))
         return (loss, d_ctrl, d_col, d_w, d_pts) if points else (loss, d_ctrl, d_col, d_w)
 
@@ -107,6 +117,7 @@ class Reference:
         out2 = np.zeros(len(group), np.float64)
         ok = np.zeros(len(group), np.int32)
         threads = threads or min(16, os.cpu_count() or 1)
-        lib().vko_an_fd(self.h, _p(_f64(ctrl)), _p(_f64(colors)), _p(_f64(widths)), _p(_f64(target)), len(group),
+        lib().vko_an_fd(self.h, _p(self._ctrl(ctrl)), _p(_f64(colors, 4 * self.npaths)), _p(_f64(widths, self.npaths)),
+                        _p(_f64(target, 4 * self.W * self.H)), len(group),
                         _p(group), _p(index), h, h2, int(full), threads, _p(out), _p(out2), _p(ok))
         return (out, ok.astype(bool)) if h2 <= 0 else (out, out2, ok.astype(bool))

@@ -429,3 +429,74 @@ def test_gpu_point_buffer_growth(gb):
     assert len(pts) > 65536 and np.array_equal(off, seg)
     assert np.array_equal(pts.view(np.uint32), f32.view(np.uint32))
     A.destroy()
+
+
+# ----------------------------------------------------- tiled evaluation
+
+
+def test_quadratic_elevation_adjoint():
+    """the glyph scene's quadratic outlines reach the analytic mode as exact
+    cubic elevations; elevate_adjoint is elevate's transpose"""
+    _, _, quad = scenes.analytic_glyph_scene(n_outlines=60, n_strokes=8, size=96)
+    rng = np.random.default_rng(4)
+    P, Q = rng.normal(size=quad["P"].shape), rng.normal(size=quad["Q"].shape)
+    y = rng.normal(size=(3 * len(P), 2))
+    lhs = np.sum(scenes.elevate(quad, P, Q).astype(np.float64) * y)
+    gP, gQ = scenes.elevate_adjoint(quad, y)
+    assert abs(lhs - (np.sum(P * gP) + np.sum(Q * gQ))) <= 1e-5 * abs(lhs)
+
+
+def _gpu_eval_tiled(gb, scene, par, target, tile):
+    A = gb.Analytic(scene, tile=tile)
+    p = {k: _dev(v) for k, v in par.items()}
+    canvas, loss = A.forward(p["ctrl"], p["colors"], p["widths"], _dev(target))
+    canvas, loss = _host(canvas), float(loss.item())
+    grads = tuple(_host(g) for g in A.backward())
+    assert A.sync() == 0
+    A.destroy()
+    return canvas, loss, grads
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("tile", [48, 128])
+def test_gpu_tiled_matches_whole_canvas(gb, tile):
+    """the tiled evaluation (tiles of 48 and 128 pixels, ragged at the canvas
+    edge, paths crossing tiles and leaving the canvas) equals the
+    whole-canvas one: canvas, loss and every gradient"""
+    scene, par = scenes.analytic_scene(seed=3, n_paths=40, n_cubics=6, size=300, w_min=1.0, w_max=9.0)
+    _, tpar = scenes.analytic_scene(seed=4, n_paths=40, n_cubics=6, size=300)
+    par["ctrl"] = par["ctrl"] * np.float32(1.1) - np.float32(15.0)  # some control points off the canvas
+    R = ar.Reference(scene)
+    target, _ = R.forward(tpar["ctrl"], tpar["colors"], tpar["widths"])
+    c0, l0, g0, A = _gpu_eval(gb, scene, par, target)
+    A.destroy()
+    c1, l1, g1 = _gpu_eval_tiled(gb, scene, par, target, tile)
+    assert np.abs(c1 - c0).max() < 1e-5
+    assert abs(l1 - l0) <= 1e-5 * l0
+    for name, a, b in zip(("ctrl", "colors", "widths"), g1, g0):
+        err = np.linalg.norm(a - b) / np.linalg.norm(b)
+        assert err < 1e-4, (name, err)
+
+
+@pytest.mark.gpu
+def test_gpu_tiled_glyph_crop_matches_fp64(gb):
+    """the large glyph configuration's analytic construction on a 192 x 192
+    crop at its density (440 quadratic outlines with holes, 44 closed
+    strokes), tiled: canvas and loss against the FP64 reference, and the
+    gradients of the outline control points (chained through the quadratic
+    elevation) within the analytic mode's bar"""
+    scene, par, quad = scenes.analytic_glyph_scene(n_outlines=440, n_strokes=44, size=192)
+    # the target: another draw of the construction (its own structure)
+    tscene, tpar, _ = scenes.analytic_glyph_scene(seed=6, n_outlines=440, n_strokes=44, size=192)
+    target, _ = ar.Reference(tscene).forward(tpar["ctrl"], tpar["colors"], tpar["widths"])
+    R = ar.Reference(scene)
+    ref_canvas, ref_loss = R.forward(par["ctrl"], par["colors"], par["widths"], target)
+    _, rc, rcol, rw = R.backward(par["ctrl"], par["colors"], par["widths"], target)
+    canvas, loss, (gc, gcol, gw) = _gpu_eval_tiled(gb, scene, par, target, 64)
+    assert np.abs(canvas - ref_canvas).max() < CANVAS_TOL
+    assert abs(loss - ref_loss) <= 1e-4 * ref_loss
+    gP, gQ = scenes.elevate_adjoint(quad, gc)
+    rP, rQ = scenes.elevate_adjoint(quad, rc)
+    for name, a, b in (("on-curve", gP, rP), ("off-curve", gQ, rQ), ("colors", gcol, rcol), ("widths", gw, rw)):
+        err = np.linalg.norm(a - b) / np.linalg.norm(b)
+        assert err < GRAD_TOL, (name, err)

@@ -173,6 +173,7 @@ SIGNATURES = {
     "vkvg_gb300_batch_timing": (_I, [_P, _P]),
     "vkvg_gb300_batch_destroy": (None, [_P]),
     "vkvg_gb300_analytic_create": (_P, [_U, _U, _P, _U, _P, _P, _U, _P, _U, _P]),
+    "vkvg_gb300_analytic_create_tiled": (_P, [_U, _U, _U, _P, _U, _P, _P, _U, _P, _U, _P]),
     "vkvg_gb300_analytic_destroy": (None, [_P]),
     "vkvg_gb300_analytic_status": (_I, [_P]),
     "vkvg_gb300_analytic_control_point_count": (_U, [_P]),
@@ -433,7 +434,8 @@ class Analytic:
     tensors (float32, contiguous); the calls are queued on the tensors'
     current stream."""
 
-    def __init__(self, scene):
+    def __init__(self, scene, tile=0):
+        """tile > 0: the tiled evaluation (vkvg_gb300_analytic_create_tiled)"""
         import torch
 
         self.L = lib()
@@ -442,10 +444,13 @@ class Analytic:
         self._keep = s
         self.W, self.H = int(scene["width"]), int(scene["height"])
         self.npaths = len(s["path_ncontours"])
-        self.h = self.L.vkvg_gb300_analytic_create(
-            self.W, self.H, _ptr(s["background"].astype(np.float32)), self.npaths, _ptr(s["path_ncontours"]),
-            _ptr(s["path_flags"]), len(s["contour_nseg"]), _ptr(s["contour_nseg"]), len(s["seg_kind"]),
-            _ptr(s["seg_kind"]))
+        args = (_ptr(s["background"].astype(np.float32)), self.npaths, _ptr(s["path_ncontours"]),
+                _ptr(s["path_flags"]), len(s["contour_nseg"]), _ptr(s["contour_nseg"]), len(s["seg_kind"]),
+                _ptr(s["seg_kind"]))
+        if tile:
+            self.h = self.L.vkvg_gb300_analytic_create_tiled(self.W, self.H, tile, *args)
+        else:
+            self.h = self.L.vkvg_gb300_analytic_create(self.W, self.H, *args)
         if not self.h:
             raise VkvgError("vkvg_gb300_analytic_create failed")
         self.nctrl = self.L.vkvg_gb300_analytic_control_point_count(self.h)
@@ -458,13 +463,28 @@ class Analytic:
     def _p(t):
         return C.c_void_p(t.data_ptr()) if t is not None else None
 
+    def _shape(self, name, t, n):
+        t_ = self.torch
+        if t.dtype != t_.float32 or not t.is_contiguous() or t.numel() != n or t.device.type != "cuda":
+            raise VkvgError("%s: want %d contiguous float32 values on the GPU, got %s %s of %d on %s"
+                            % (name, n, t.dtype, "contiguous" if t.is_contiguous() else "strided", t.numel(),
+                               t.device))
+
     def _check(self, st, what):
         if st:
             raise VkvgError("%s: status %d" % (what, st))
 
     def forward(self, ctrl, colors, widths, target=None):
         """renders into self.canvas (and the loss into self.loss when a target
-        is given); returns (canvas, loss or None)"""
+        is given); returns (canvas, loss or None).  The tensors must be this
+        scene's: float32, contiguous, on the GPU, ctrl of its control points,
+        colors and widths of its paths, target of its canvas (the kernels
+        index them by the scene's structure)."""
+        self._shape("ctrl", ctrl, 2 * self.nctrl)
+        self._shape("colors", colors, 4 * self.npaths)
+        self._shape("widths", widths, self.npaths)
+        if target is not None:
+            self._shape("target", target, 4 * self.W * self.H)
         p = self._p
         st = self.L.vkvg_gb300_analytic_forward(self.h, p(ctrl), p(colors), p(widths), p(target), p(self.canvas),
                                                 p(self.loss) if target is not None else None)
@@ -480,6 +500,10 @@ class Analytic:
             grads = (t.empty((self.nctrl, 2), dtype=t.float32, device="cuda"),
                      t.empty((self.npaths, 4), dtype=t.float32, device="cuda"),
                      t.empty(self.npaths, dtype=t.float32, device="cuda"))
+        if d_canvas is not None:
+            self._shape("d_canvas", d_canvas, 4 * self.W * self.H)
+        for name, g, n in zip(("d_ctrl", "d_colors", "d_widths"), grads, (2 * self.nctrl, 4 * self.npaths, self.npaths)):
+            self._shape(name, g, n)
         p = self._p
         st = self.L.vkvg_gb300_analytic_backward(self.h, p(d_canvas), p(grads[0]), p(grads[1]), p(grads[2]))
         self._check(st, "analytic_backward")

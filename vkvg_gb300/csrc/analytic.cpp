@@ -10,6 +10,16 @@
  * (dL/dcontrol).  Nothing is read back in steady state: the point total is
  * copied to pinned memory after each forward and checked when it has landed;
  * only the first forward waits for it, to size the point buffer.
+ *
+ * A tiled scene (create_tiled) keeps the same kernels but runs them per
+ * square tile of the canvas: after the flattening, every layer's box in
+ * tiles (from its points, strokes widened by half their width), a flag per
+ * (tile, layer), one exclusive scan of the flags and a compaction give every
+ * tile its layers in scene order; the per-tile counts are read back (the one
+ * synchronisation of a tiled forward) to place every tile's area planes and
+ * checkpoints in one buffer, all kept resident for the backward.  A layer is
+ * zero outside its box, so a tile's composite over its own layers equals the
+ * whole canvas's there; the adjoints accumulate over tiles.
  */
 #include "analytic.h"
 #include "host.h"
@@ -40,6 +50,15 @@ struct _vkvg_gb300_analytic_t {
        the forward and composite, cover, flatten adjoints of the backward */
     bool        timing = false;
     cudaEvent_t ev[8]  = {};
+    /* tiled scenes: tile side (0: one window, the whole canvas), tiles
+       across and down, per-layer boxes, flags and their scan, the tiles'
+       layer lists, and per tile its list start, layer count and the offsets
+       of its area planes and checkpoints */
+    uint32_t              tile = 0, ntx = 1, nty = 1;
+    DevBuf                d_box, d_flags, d_fpos, d_fscan, d_list;
+    PinnedBuf             h_tiles;
+    std::vector<uint32_t> t_first, t_count;
+    std::vector<size_t>   t_area, t_ckpt;
     /* the last forward */
     bool         have_fwd = false, sized = false;
     const float *f_ctrl = nullptr, *f_colors = nullptr, *f_widths = nullptr, *f_target = nullptr;
@@ -112,13 +131,17 @@ void poll(VkvgAnalytic a, bool wait) {
 
 extern "C" {
 
-VkvgAnalytic vkvg_gb300_analytic_create(uint32_t width, uint32_t height, const float background[4], uint32_t npaths,
-                                        const uint32_t *path_ncontours, const uint32_t *path_flags,
-                                        uint32_t ncontours, const uint32_t *contour_nseg, uint32_t nseg,
-                                        const uint8_t *seg_kind) {
-    /* a band of the canvas must fit in one block's shared memory */
+} /* extern "C" */
+
+namespace {
+VkvgAnalytic create_scene(uint32_t width, uint32_t height, uint32_t tile, const float background[4], uint32_t npaths,
+                          const uint32_t *path_ncontours, const uint32_t *path_flags, uint32_t ncontours,
+                          const uint32_t *contour_nseg, uint32_t nseg, const uint8_t *seg_kind) {
+    /* a band of a window (the canvas, or a tile) must fit in one block's
+       shared memory */
+    const uint32_t win = tile ? std::min(tile, width) : width;
     if (!width || !height || !npaths || !path_ncontours || !path_flags || !contour_nseg || !seg_kind ||
-        ak_cover_smem(width) > 227 * 1024 || height > 65536)
+        ak_cover_smem(win) > 227 * 1024 || height > 65536 || (tile && (tile < 16 || tile > 4096)))
         return nullptr;
     std::vector<uint8_t>  kind(nseg), lstroke;
     std::vector<uint32_t> seg_cp(nseg), seg_end(nseg), seg_cont(nseg), cont_s0(ncontours + 1), path_s0(npaths + 1),
@@ -153,6 +176,9 @@ VkvgAnalytic vkvg_gb300_analytic_create(uint32_t width, uint32_t height, const f
         return nullptr;
     a->W = width, a->H = height, a->npaths = npaths, a->ncontours = ncontours, a->nseg = nseg, a->ncp = cp;
     a->nlayers = (uint32_t)lpath.size();
+    a->tile    = tile;
+    a->ntx     = tile ? (width + tile - 1) / tile : 1;
+    a->nty     = tile ? (height + tile - 1) / tile : 1;
     if (background)
         memcpy(a->bg, background, sizeof a->bg);
     size_t np    = (size_t)width * height;
@@ -165,12 +191,15 @@ VkvgAnalytic vkvg_gb300_analytic_create(uint32_t width, uint32_t height, const f
          upload(a->d_seg_contour, seg_cont) && upload(a->d_cont_s0, cont_s0) && upload(a->d_path_s0, path_s0) &&
          upload(a->d_layer_path, lpath) && upload(a->d_layer_stroke, lstroke);
     ok = ok && a->d_cnt.grow(4 * ((size_t)nseg + 1)) && a->d_off.grow(4 * ((size_t)nseg + 1)) &&
-         a->d_scan.grow(4 * gb_scan_scratch_words(nseg + 1)) &&
-         a->d_area.grow(sizeof(float) * np * std::max<uint32_t>(a->nlayers, 1)) &&
-         a->d_ckpt.grow(sizeof(float4) * np * std::max<size_t>(nchk, 1)) && a->d_canvas.grow(sizeof(float4) * np) &&
-         a->d_loss_part.grow(sizeof(float) * nbk) && a->d_loss.grow(sizeof(float)) &&
-         a->d_color_part.grow(sizeof(float4) * (size_t)(np + 127) / 128 * std::max<uint32_t>(a->nlayers, 1)) &&
-         a->d_status.grow(4) && a->h_mon.grow(8) && size_points(a, std::max<uint32_t>(64 * nseg, 65536));
+         a->d_scan.grow(4 * gb_scan_scratch_words(nseg + 1)) && a->d_canvas.grow(sizeof(float4) * np) &&
+         a->d_loss.grow(sizeof(float)) && a->d_status.grow(4) && a->h_mon.grow(8) &&
+         size_points(a, std::max<uint32_t>(64 * nseg, 65536));
+    if (!tile) /* one window: its planes are sized now */
+        ok = ok && a->d_area.grow(sizeof(float) * np * std::max<uint32_t>(a->nlayers, 1)) &&
+             a->d_ckpt.grow(sizeof(float4) * np * std::max<size_t>(nchk, 1)) && a->d_loss_part.grow(sizeof(float) * nbk) &&
+             a->d_color_part.grow(sizeof(float4) * (size_t)(np + 127) / 128 * std::max<uint32_t>(a->nlayers, 1));
+    else
+        ok = ok && a->d_box.grow(sizeof(int4) * std::max<uint32_t>(a->nlayers, 1));
     ok = ok && cudaMemset(a->d_status.p, 0, 4) == cudaSuccess;
     if (!ok) {
         vkvg_gb300_analytic_destroy(a);
@@ -178,6 +207,7 @@ VkvgAnalytic vkvg_gb300_analytic_create(uint32_t width, uint32_t height, const f
     }
     ak_scene &S    = a->S;
     S.W = width, S.H = height, S.npaths = npaths, S.ncontours = ncontours, S.nseg = nseg, S.ncp = cp;
+    S.x0 = S.y0 = 0, S.CW = width, S.CH = height, S.layer_map = nullptr;
     S.nlayers      = a->nlayers;
     S.band         = ak_band_rows(width);
     S.nbands       = (height + S.band - 1) / S.band;
@@ -192,6 +222,25 @@ VkvgAnalytic vkvg_gb300_analytic_create(uint32_t width, uint32_t height, const f
     S.layer_stroke = a->d_layer_stroke.as<uint8_t>();
     return a;
 }
+} /* namespace */
+
+extern "C" {
+VkvgAnalytic vkvg_gb300_analytic_create(uint32_t width, uint32_t height, const float background[4], uint32_t npaths,
+                                        const uint32_t *path_ncontours, const uint32_t *path_flags,
+                                        uint32_t ncontours, const uint32_t *contour_nseg, uint32_t nseg,
+                                        const uint8_t *seg_kind) {
+    return create_scene(width, height, 0, background, npaths, path_ncontours, path_flags, ncontours, contour_nseg,
+                        nseg, seg_kind);
+}
+VkvgAnalytic vkvg_gb300_analytic_create_tiled(uint32_t width, uint32_t height, uint32_t tile, const float background[4],
+                                              uint32_t npaths, const uint32_t *path_ncontours,
+                                              const uint32_t *path_flags, uint32_t ncontours,
+                                              const uint32_t *contour_nseg, uint32_t nseg, const uint8_t *seg_kind) {
+    if (!tile)
+        return nullptr;
+    return create_scene(width, height, tile, background, npaths, path_ncontours, path_flags, ncontours, contour_nseg,
+                        nseg, seg_kind);
+}
 
 void vkvg_gb300_analytic_destroy(VkvgAnalytic a) {
     if (!a)
@@ -201,10 +250,12 @@ void vkvg_gb300_analytic_destroy(VkvgAnalytic a) {
     DevBuf *bs[] = {&a->d_seg_kind, &a->d_seg_cp,  &a->d_seg_end, &a->d_seg_contour, &a->d_cont_s0,
                     &a->d_path_s0,  &a->d_layer_path, &a->d_layer_stroke, &a->d_cnt, &a->d_off, &a->d_scan,
                     &a->d_pts, &a->d_pt_nb, &a->d_area, &a->d_ckpt, &a->d_canvas, &a->d_loss_part, &a->d_loss,
-                    &a->d_color_part, &a->d_gpts, &a->d_status};
+                    &a->d_color_part, &a->d_gpts, &a->d_status, &a->d_box, &a->d_flags, &a->d_fpos, &a->d_fscan,
+                    &a->d_list};
     for (DevBuf *b : bs)
         b->release();
     a->h_mon.release();
+    a->h_tiles.release();
     if (a->ev_mon)
         cudaEventDestroy(a->ev_mon);
     for (cudaEvent_t ev : a->ev)
@@ -230,6 +281,78 @@ vkvg_status_t vkvg_gb300_analytic_set_stream(VkvgAnalytic a, void *stream) {
     return VKVG_STATUS_SUCCESS;
 }
 
+} /* extern "C" */
+
+namespace {
+/* tiled scenes: the layers of every tile, their planes' places, and the
+   buffers sized for them (after the flattening of this forward) */
+cudaError_t tile_setup(VkvgAnalytic a, const float *widths) {
+    cudaStream_t   st = a->stream;
+    const uint32_t nt = a->ntx * a->nty, nl = a->nlayers;
+    const uint64_t n  = (uint64_t)nt * nl;
+    if (n >= 0xFFFFFFFFull)
+        return cudaErrorMemoryAllocation; /* positions are 32-bit */
+    if (!a->d_flags.grow(4 * std::max<uint64_t>(n, 1)) || !a->d_fpos.grow(4 * (n + 1)) ||
+        !a->d_fscan.grow(4 * gb_scan_scratch_words((uint32_t)n) + 64) || !a->h_tiles.grow(4 * ((size_t)nt + 2)))
+        return cudaErrorMemoryAllocation;
+    ak_bufs     B = bufs(a);
+    cudaError_t e = ak_launch_layer_boxes(st, a->S, B, widths, a->tile, a->ntx, a->nty, a->d_box.as<int4>());
+    if (e == cudaSuccess)
+        e = ak_launch_tile_flags(st, nl, nt, a->ntx, a->d_box.as<int4>(), a->d_flags.as<uint32_t>());
+    if (e == cudaSuccess)
+        e = gb_exclusive_scan_flags(st, a->d_flags.as<uint32_t>(), (uint32_t)n, a->d_fpos.as<uint32_t>(),
+                                    a->d_fscan.as<uint32_t>());
+    uint32_t *h = (uint32_t *)a->h_tiles.p;
+    if (e == cudaSuccess) /* the position of every tile's first (tile, layer) entry, and the total */
+        e = cudaMemcpy2DAsync(h, 4, a->d_fpos.p, (size_t)nl * 4, 4, nt, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(h + nt, a->d_fpos.as<uint32_t>() + n, 4, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(st);
+    gb_count_launch(5);
+    if (e != cudaSuccess)
+        return e;
+    const uint32_t total = h[nt];
+    if (!a->d_list.grow(4 * (size_t)std::max<uint32_t>(total, 1)))
+        return cudaErrorMemoryAllocation;
+    e = ak_launch_tile_lists(st, n, nl, a->d_flags.as<uint32_t>(), a->d_fpos.as<uint32_t>(), a->d_list.as<uint32_t>());
+    gb_count_launch(1);
+    a->t_first.assign(nt, 0), a->t_count.assign(nt, 0), a->t_area.assign(nt, 0), a->t_ckpt.assign(nt, 0);
+    size_t area = 0, ckpt = 0, lossb = 1, colb = 1;
+    for (uint32_t t = 0; t < nt; t++) {
+        const uint32_t tw = std::min(a->tile, a->W - (t % a->ntx) * a->tile);
+        const uint32_t th = std::min(a->tile, a->H - (t / a->ntx) * a->tile);
+        const size_t   px = (size_t)tw * th, cnt = (t + 1 < nt ? h[t + 1] : total) - h[t];
+        a->t_first[t] = h[t], a->t_count[t] = (uint32_t)cnt, a->t_area[t] = area, a->t_ckpt[t] = ckpt;
+        area += px * cnt;
+        ckpt += px * ((cnt + AK_CHUNK - 1) / AK_CHUNK);
+        lossb = std::max<size_t>(lossb, (px + 255) / 256);
+        colb  = std::max<size_t>(colb, (px + 127) / 128 * cnt);
+    }
+    if (!a->d_area.grow(sizeof(float) * std::max<size_t>(area, 1)) ||
+        !a->d_ckpt.grow(sizeof(float4) * std::max<size_t>(ckpt, 1)) || !a->d_loss_part.grow(sizeof(float) * lossb) ||
+        !a->d_color_part.grow(sizeof(float4) * colb))
+        return cudaErrorMemoryAllocation;
+    return e;
+}
+/* the window and buffers of tile t */
+void tile_window(VkvgAnalytic a, uint32_t t, ak_scene &S, ak_bufs &B) {
+    S           = a->S;
+    S.x0        = (t % a->ntx) * a->tile;
+    S.y0        = (t / a->ntx) * a->tile;
+    S.W         = std::min(a->tile, a->W - S.x0);
+    S.H         = std::min(a->tile, a->H - S.y0);
+    S.nlayers   = a->t_count[t];
+    S.layer_map = a->d_list.as<uint32_t>() + a->t_first[t];
+    S.band      = ak_band_rows(S.W);
+    S.nbands    = (S.H + S.band - 1) / S.band;
+    B           = bufs(a);
+    B.area      = a->d_area.as<float>() + a->t_area[t];
+    B.ckpt      = a->d_ckpt.as<float4>() + a->t_ckpt[t];
+}
+} /* namespace */
+
+extern "C" {
 vkvg_status_t vkvg_gb300_analytic_forward(VkvgAnalytic a, const float *ctrl, const float *colors,
                                           const float *widths, const float *target, float *canvas, float *loss) {
     if (!a)
@@ -261,22 +384,50 @@ vkvg_status_t vkvg_gb300_analytic_forward(VkvgAnalytic a, const float *ctrl, con
     ak_bufs B = bufs(a);
     e         = ak_launch_flat_emit(st, a->S, c2, B.off, a->d_pts.as<float2>(), a->d_pt_nb.as<uint2>(), a->cap,
                                     B.status);
-    if (a->timing)
-        cudaEventRecord(a->ev[1], st);
-    if (e == cudaSuccess)
-        e = ak_launch_cover(st, a->S, B, widths);
-    if (a->timing)
-        cudaEventRecord(a->ev[2], st);
-    if (e == cudaSuccess)
-        e = ak_launch_composite(st, a->S, B, (const float4 *)colors, (const float4 *)target,
-                                target ? a->d_loss_part.as<float>() : nullptr);
-    gb_count_launch(3);
-    if (e == cudaSuccess && loss) {
-        e = ak_launch_reduce(st, a->S, ak_pixel_blocks(a->S), nullptr, nullptr, a->d_loss_part.as<float>(), loss);
-        gb_count_launch(1);
+    if (a->tile) {
+        /* tiled: the layers of every tile, then each tile's coverage and
+           composite in turn (the loss summed over the tiles) */
+        if (e == cudaSuccess)
+            e = tile_setup(a, widths);
+        if (a->timing)
+            cudaEventRecord(a->ev[1], st);
+        if (e == cudaSuccess && loss)
+            e = cudaMemsetAsync(loss, 0, sizeof(float), st);
+        for (uint32_t t = 0; e == cudaSuccess && t < a->ntx * a->nty; t++) {
+            ak_scene S;
+            ak_bufs  Bt;
+            tile_window(a, t, S, Bt);
+            e = ak_launch_cover(st, S, Bt, widths);
+            if (e == cudaSuccess)
+                e = ak_launch_composite(st, S, Bt, (const float4 *)colors, (const float4 *)target,
+                                        target ? a->d_loss_part.as<float>() : nullptr);
+            if (e == cudaSuccess && loss)
+                e = ak_launch_reduce(st, S, ak_pixel_blocks(S), nullptr, nullptr, a->d_loss_part.as<float>(), loss,
+                                     true);
+            gb_count_launch((S.nlayers ? 1 : 0) + 1 + (loss ? 1 : 0));
+        }
+        if (a->timing) {
+            cudaEventRecord(a->ev[2], st);
+            cudaEventRecord(a->ev[3], st);
+        }
+    } else {
+        if (a->timing)
+            cudaEventRecord(a->ev[1], st);
+        if (e == cudaSuccess)
+            e = ak_launch_cover(st, a->S, B, widths);
+        if (a->timing)
+            cudaEventRecord(a->ev[2], st);
+        if (e == cudaSuccess)
+            e = ak_launch_composite(st, a->S, B, (const float4 *)colors, (const float4 *)target,
+                                    target ? a->d_loss_part.as<float>() : nullptr);
+        gb_count_launch(3);
+        if (e == cudaSuccess && loss) {
+            e = ak_launch_reduce(st, a->S, ak_pixel_blocks(a->S), nullptr, nullptr, a->d_loss_part.as<float>(), loss);
+            gb_count_launch(1);
+        }
+        if (a->timing)
+            cudaEventRecord(a->ev[3], st);
     }
-    if (a->timing)
-        cudaEventRecord(a->ev[3], st);
     if (e == cudaSuccess && canvas)
         e = cudaMemcpyAsync(canvas, a->d_canvas.p, sizeof(float4) * a->W * a->H, cudaMemcpyDeviceToDevice, st);
     if (e == cudaSuccess && !a->mon_pending) {
@@ -316,17 +467,41 @@ vkvg_status_t vkvg_gb300_analytic_backward(VkvgAnalytic a, const float *d_canvas
         e = cudaMemsetAsync(a->d_gpts.p, 0, sizeof(float2) * a->cap, st);
     if (a->timing)
         cudaEventRecord(a->ev[4], st);
-    if (e == cudaSuccess)
-        e = ak_launch_composite_bwd(st, a->S, B, (const float4 *)a->f_colors, (const float4 *)a->f_target,
-                                    (const float4 *)d_canvas, a->d_color_part.as<float4>());
-    if (e == cudaSuccess)
-        e = ak_launch_reduce(st, a->S, nb, a->d_color_part.as<float4>(), (float4 *)d_colors, nullptr, nullptr);
-    if (a->timing)
-        cudaEventRecord(a->ev[5], st);
-    if (e == cudaSuccess)
-        e = ak_launch_cover_bwd(st, a->S, B, a->f_widths, a->d_gpts.as<float2>(), d_widths);
-    if (a->timing)
-        cudaEventRecord(a->ev[6], st);
+    if (a->tile) {
+        /* tiled: per tile its compositing adjoint, colour reduction and
+           coverage adjoint (gradients accumulate over the tiles) */
+        for (uint32_t t = 0; e == cudaSuccess && t < a->ntx * a->nty; t++) {
+            ak_scene S;
+            ak_bufs  Bt;
+            tile_window(a, t, S, Bt);
+            if (!S.nlayers)
+                continue;
+            e = ak_launch_composite_bwd(st, S, Bt, (const float4 *)a->f_colors, (const float4 *)a->f_target,
+                                        (const float4 *)d_canvas, a->d_color_part.as<float4>());
+            if (e == cudaSuccess)
+                e = ak_launch_reduce(st, S, ak_composite_bwd_blocks(S), a->d_color_part.as<float4>(),
+                                     (float4 *)d_colors, nullptr, nullptr);
+            if (e == cudaSuccess)
+                e = ak_launch_cover_bwd(st, S, Bt, a->f_widths, a->d_gpts.as<float2>(), d_widths);
+            gb_count_launch(3);
+        }
+        if (a->timing) {
+            cudaEventRecord(a->ev[5], st);
+            cudaEventRecord(a->ev[6], st);
+        }
+    } else {
+        if (e == cudaSuccess)
+            e = ak_launch_composite_bwd(st, a->S, B, (const float4 *)a->f_colors, (const float4 *)a->f_target,
+                                        (const float4 *)d_canvas, a->d_color_part.as<float4>());
+        if (e == cudaSuccess)
+            e = ak_launch_reduce(st, a->S, nb, a->d_color_part.as<float4>(), (float4 *)d_colors, nullptr, nullptr);
+        if (a->timing)
+            cudaEventRecord(a->ev[5], st);
+        if (e == cudaSuccess)
+            e = ak_launch_cover_bwd(st, a->S, B, a->f_widths, a->d_gpts.as<float2>(), d_widths);
+        if (a->timing)
+            cudaEventRecord(a->ev[6], st);
+    }
     if (e == cudaSuccess)
         e = ak_launch_flat_bwd(st, a->S, (const float2 *)a->f_ctrl, B.off, a->cap, a->d_gpts.as<float2>(),
                                (float2 *)d_ctrl);

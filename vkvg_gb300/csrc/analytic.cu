@@ -2,7 +2,7 @@
  * K7/K8 - analytic area coverage, compositing and their adjoints, sm_103a.
  *
  * Forward (K7):
- *   ak_cover      grid (bands of 16 or 32 rows) x (layers).  Every thread takes
+ *   ak_cover      grid (layers) x (bands of 16 or 32 rows).  Every thread takes
  *                 flattened points of the layer's path and builds the
  *                 polygons of that point - the fill edge to the next point,
  *                 or the stroke's rectangle of the segment to the next point
@@ -309,7 +309,8 @@ __device__ __forceinline__ void gather_slots(const ak_scene &S, const ak_bufs &B
         return;
     uint32_t kp, kn;
     neighbours(S, B, k, kp, kn);
-    float2 P = B.pts[k], Pn = B.pts[kn];
+    const float2 org = v2((float)S.x0, (float)S.y0); /* the window's origin: an integer, exact */
+    float2       P = B.pts[k] - org, Pn = B.pts[kn] - org;
     float2 O = v2(floorf(P.x), floorf(P.y));
     if (!fin2(O))
         O = v2(0.f, 0.f);
@@ -322,7 +323,7 @@ __device__ __forceinline__ void gather_slots(const ak_scene &S, const ak_bufs &B
         o.k = k, o.kp = kp, o.kn = kn, o.flags = 0, o.o = O, o.v[0] = P - O, o.v[1] = Pn - O;
         return;
     }
-    float2 Pp = B.pts[kp];
+    float2 Pp = B.pts[kp] - org;
     if (!pieces_in_band(bd, Pp, P, Pn, h))
         return;
     float2   q[4], v[3];
@@ -364,15 +365,16 @@ __global__ void __launch_bounds__(AK_THREADS) ak_cover(ak_scene S, ak_bufs B, co
     ak_slot *slots = reinterpret_cast<ak_slot *>(ak_smem);
     int     *acc   = reinterpret_cast<int *>(slots + AK_THREADS);
     __shared__ int nslot;
-    uint32_t l = blockIdx.y;
-    ak_band  bd{(int)(blockIdx.x * S.band), 0, (int)S.W, B.status};
+    uint32_t l = blockIdx.x; /* grid: layers (x, up to 2^31) by bands (y) */
+    ak_band  bd{(int)(blockIdx.y * S.band), 0, (int)S.W, B.status};
     bd.y1    = min((int)S.H, bd.y0 + (int)S.band);
     int rows = bd.y1 - bd.y0, W1 = S.W + 1;
     for (int i = threadIdx.x; i < rows * W1; i += AK_THREADS)
         acc[i] = 0;
     if (B.off[S.nseg] <= B.cap) {
-        uint32_t p = S.layer_path[l];
-        bool     stroke = S.layer_stroke[l] != 0;
+        const uint32_t lg = S.layer_map ? S.layer_map[l] : l;
+        uint32_t p = S.layer_path[lg];
+        bool     stroke = S.layer_stroke[lg] != 0;
         int      E      = stroke ? 7 : 1;
         float    h      = 0.5f * widths[p];
         uint32_t p1     = B.off[S.path_s0[p + 1]];
@@ -447,7 +449,7 @@ __global__ void __launch_bounds__(AK_THREADS)
         uint32_t n = min((uint32_t)AK_CHUNK, S.nlayers - lb);
         __syncthreads();
         if (threadIdx.x < n)
-            col[threadIdx.x] = colors[S.layer_path[lb + threadIdx.x]];
+            col[threadIdx.x] = colors[S.layer_path[S.layer_map ? S.layer_map[lb + threadIdx.x] : lb + threadIdx.x]];
         __syncthreads();
         if (!valid)
             continue;
@@ -461,11 +463,12 @@ __global__ void __launch_bounds__(AK_THREADS)
             if (q < (int)n)
                 C = blend(cover(A[q]), col[q], C);
     }
-    float s = 0.f;
+    float        s  = 0.f;
+    const size_t cp = valid ? ((size_t)S.y0 + px / S.W) * S.CW + S.x0 + px % S.W : 0; /* on the canvas */
     if (valid) {
-        B.canvas[px] = C;
+        B.canvas[cp] = C;
         if (target) {
-            float4 t = target[px];
+            float4 t = target[cp];
             float  a = C.x - t.x, b = C.y - t.y, c = C.z - t.z, d = C.w - t.w;
             s        = a * a + b * b + c * c + d * d;
         }
@@ -520,11 +523,12 @@ __global__ void __launch_bounds__(AK_CB_THREADS)
     bool              valid = px < np;
     float4            g     = make_float4(0.f, 0.f, 0.f, 0.f);
     if (valid) {
+        const size_t cp = ((size_t)S.y0 + px / S.W) * S.CW + S.x0 + px % S.W; /* on the canvas */
         if (d_canvas) {
-            g = d_canvas[px];
+            g = d_canvas[cp];
         } else {
-            float  s = 2.f / (float)(np * 4);
-            float4 c = B.canvas[px], t = target[px];
+            float  s = 2.f / (float)((size_t)S.CW * S.CH * 4);
+            float4 c = B.canvas[cp], t = target[cp];
             g        = make_float4((c.x - t.x) * s, (c.y - t.y) * s, (c.z - t.z) * s, (c.w - t.w) * s);
         }
     }
@@ -535,7 +539,7 @@ __global__ void __launch_bounds__(AK_CB_THREADS)
         uint32_t lb = ch * AK_CHUNK, n = min((uint32_t)AK_CHUNK, S.nlayers - lb);
         __syncthreads();
         if (threadIdx.x < n)
-            col[threadIdx.x] = colors[S.layer_path[lb + threadIdx.x]];
+            col[threadIdx.x] = colors[S.layer_path[S.layer_map ? S.layer_map[lb + threadIdx.x] : lb + threadIdx.x]];
         __syncthreads();
         float4       Bc = valid ? B.ckpt[(size_t)ch * np + px] : make_float4(0.f, 0.f, 0.f, 0.f);
         const float *ap = B.area + (size_t)lb * np + px;
@@ -604,8 +608,8 @@ __global__ void __launch_bounds__(AK_THREADS)
     float   *gs    = reinterpret_cast<float *>(eg + AK_THREADS * 7);
     __shared__ float red[AK_THREADS / 32];
     __shared__ int   nslot;
-    uint32_t         l = blockIdx.y;
-    ak_band          bd{(int)(blockIdx.x * S.band), 0, (int)S.W, B.status};
+    uint32_t         l = blockIdx.x;
+    ak_band          bd{(int)(blockIdx.y * S.band), 0, (int)S.W, B.status};
     bd.y1             = min((int)S.H, bd.y0 + (int)S.band);
     int          rows = bd.y1 - bd.y0;
     const float *src  = B.area + ((size_t)l * S.H + bd.y0) * S.W;
@@ -613,8 +617,9 @@ __global__ void __launch_bounds__(AK_THREADS)
         gs[i] = src[i];
     if (B.off[S.nseg] > B.cap)
         return;
-    uint32_t p      = S.layer_path[l];
-    bool     stroke = S.layer_stroke[l] != 0;
+    const uint32_t lg = S.layer_map ? S.layer_map[l] : l;
+    uint32_t p      = S.layer_path[lg];
+    bool     stroke = S.layer_stroke[lg] != 0;
     int      E      = stroke ? 7 : 1;
     float    h      = 0.5f * widths[p], gh = 0.f;
     uint32_t p1     = B.off[S.path_s0[p + 1]];
@@ -698,17 +703,83 @@ __global__ void ak_reduce_colors(ak_scene S, uint32_t nblocks, const float *__re
     float s = 0.f;
     for (uint32_t b = 0; b < nblocks; b++)
         s += part[(size_t)b * S.nlayers * 4 + t];
-    atomicAdd(&d_colors[S.layer_path[t >> 2] * 4 + (t & 3)], s);
+    const uint32_t l = t >> 2;
+    atomicAdd(&d_colors[S.layer_path[S.layer_map ? S.layer_map[l] : l] * 4 + (t & 3)], s);
 }
 
-__global__ void ak_reduce_loss(uint32_t nblocks, float scale, const float *__restrict__ part, float *__restrict__ loss) {
+__global__ void ak_reduce_loss(uint32_t nblocks, float scale, const float *__restrict__ part, float *__restrict__ loss,
+                               bool accumulate) {
     __shared__ float red[AK_THREADS / 32];
     float            s = 0.f;
     for (uint32_t b = threadIdx.x; b < nblocks; b += AK_THREADS)
         s += part[b];
     s = block_sum<AK_THREADS>(s, red);
     if (threadIdx.x == 0)
-        *loss = s * scale;
+        *loss = accumulate ? *loss + s * scale : s * scale;
+}
+
+/* ------------------------------------------------------------- tiling */
+
+/* one warp per scene layer: the box of its path's flattened points in
+   tiles, a stroke's widened by half its width and one pixel (its rectangles
+   and bevels reach at most half the width from a point) */
+__global__ void ak_layer_boxes(ak_scene S, ak_bufs B, const float *__restrict__ widths, uint32_t tile, uint32_t ntx,
+                               uint32_t nty, int4 *__restrict__ box) {
+    const uint32_t l = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (l >= S.nlayers)
+        return;
+    const uint32_t p  = S.layer_path[l];
+    const uint32_t q0 = B.off[S.path_s0[p]], q1 = B.off[S.path_s0[p + 1]];
+    float          x0 = CUDART_INF_F, y0 = CUDART_INF_F, x1 = -CUDART_INF_F, y1 = -CUDART_INF_F;
+    if (B.off[S.nseg] <= B.cap)
+        for (uint32_t k = q0 + lane; k < q1; k += 32) {
+            const float2 P = B.pts[k];
+            if (!fin2(P))
+                continue;
+            x0 = fminf(x0, P.x), y0 = fminf(y0, P.y), x1 = fmaxf(x1, P.x), y1 = fmaxf(y1, P.y);
+        }
+    for (int o = 16; o > 0; o >>= 1) {
+        x0 = fminf(x0, __shfl_xor_sync(0xffffffffu, x0, o));
+        y0 = fminf(y0, __shfl_xor_sync(0xffffffffu, y0, o));
+        x1 = fmaxf(x1, __shfl_xor_sync(0xffffffffu, x1, o));
+        y1 = fmaxf(y1, __shfl_xor_sync(0xffffffffu, y1, o));
+    }
+    if (lane)
+        return;
+    /* the winding of a closed contour is zero outside its points' box, so a
+       fill's areas stay inside it (a pixel of margin) */
+    const bool  stroke = S.layer_stroke[l] != 0;
+    const float pad    = stroke ? 0.5f * fabsf(widths[p]) + 1.f : 1.f;
+    int4        b      = make_int4(1, 1, 0, 0); /* empty */
+    if (x0 <= x1 && isfinite(pad)) {
+        const float fx0 = x0 - pad, fx1 = x1 + pad, fy0 = y0 - pad, fy1 = y1 + pad;
+        const float lim = (float)max(ntx, nty) * (float)tile;
+        const int   tx0 = (int)floorf(fminf(fmaxf(fx0, 0.f), lim) / (float)tile);
+        const int   tx1 = (int)floorf(fminf(fmaxf(fx1, 0.f), lim) / (float)tile);
+        const int   ty0 = (int)floorf(fminf(fmaxf(fy0, 0.f), lim) / (float)tile);
+        const int   ty1 = (int)floorf(fminf(fmaxf(fy1, 0.f), lim) / (float)tile);
+        if (fx1 >= 0.f && fy1 >= 0.f && fy0 < (float)(nty * tile) && fx0 < (float)(ntx * tile))
+            b = make_int4(tx0, ty0, min(tx1, (int)ntx - 1), min(ty1, (int)nty - 1));
+    }
+    box[l] = b;
+}
+
+__global__ void ak_tile_flags(uint32_t nlayers, uint64_t n, uint32_t ntx, const int4 *__restrict__ box,
+                              uint32_t *__restrict__ flags) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    const uint32_t t = (uint32_t)(i / nlayers), l = (uint32_t)(i % nlayers);
+    const int      tx = (int)(t % ntx), ty = (int)(t / ntx);
+    const int4     b  = box[l];
+    flags[i]          = tx >= b.x && tx <= b.z && ty >= b.y && ty <= b.w ? 1u : 0u;
+}
+
+__global__ void ak_tile_lists(uint64_t n, uint32_t nlayers, const uint32_t *__restrict__ flags,
+                              const uint32_t *__restrict__ pos, uint32_t *__restrict__ list) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n && flags[i])
+        list[pos[i]] = (uint32_t)(i % nlayers);
 }
 
 __global__ void ak_adam(float *__restrict__ p, const float *__restrict__ g, float *__restrict__ m,
@@ -746,7 +817,7 @@ cudaError_t ak_launch_cover(cudaStream_t st, const ak_scene &S, const ak_bufs &B
     if (smem > 48 * 1024)
         cudaFuncSetAttribute(ak_cover, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (S.nlayers)
-        ak_cover<<<dim3(S.nbands, S.nlayers), AK_THREADS, smem, st>>>(S, B, widths);
+        ak_cover<<<dim3(S.nlayers, S.nbands), AK_THREADS, smem, st>>>(S, B, widths);
     return cudaGetLastError();
 }
 cudaError_t ak_launch_composite(cudaStream_t st, const ak_scene &S, const ak_bufs &B, const float4 *colors,
@@ -769,16 +840,36 @@ cudaError_t ak_launch_cover_bwd(cudaStream_t st, const ak_scene &S, const ak_buf
     if (smem > 48 * 1024)
         cudaFuncSetAttribute(ak_cover_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (S.nlayers)
-        ak_cover_bwd<<<dim3(S.nbands, S.nlayers), AK_THREADS, smem, st>>>(S, B, widths, gpts, gwidth);
+        ak_cover_bwd<<<dim3(S.nlayers, S.nbands), AK_THREADS, smem, st>>>(S, B, widths, gpts, gwidth);
     return cudaGetLastError();
 }
 cudaError_t ak_launch_reduce(cudaStream_t st, const ak_scene &S, uint32_t nblocks, const float4 *color_part,
-                             float4 *d_colors, const float *loss_part, float *loss) {
+                             float4 *d_colors, const float *loss_part, float *loss, bool accumulate) {
     if (color_part && S.nlayers)
         ak_reduce_colors<<<(S.nlayers * 4 + 255) / 256, 256, 0, st>>>(
             S, nblocks, reinterpret_cast<const float *>(color_part), reinterpret_cast<float *>(d_colors));
     if (loss_part)
-        ak_reduce_loss<<<1, AK_THREADS, 0, st>>>(nblocks, 1.f / (float)((size_t)S.W * S.H * 4), loss_part, loss);
+        ak_reduce_loss<<<1, AK_THREADS, 0, st>>>(nblocks, 1.f / (float)((size_t)S.CW * S.CH * 4), loss_part, loss,
+                                                 accumulate);
+    return cudaGetLastError();
+}
+cudaError_t ak_launch_layer_boxes(cudaStream_t st, const ak_scene &S, const ak_bufs &B, const float *widths,
+                                  uint32_t tile, uint32_t ntx, uint32_t nty, int4 *box) {
+    if (S.nlayers)
+        ak_layer_boxes<<<(S.nlayers * 32 + 255) / 256, 256, 0, st>>>(S, B, widths, tile, ntx, nty, box);
+    return cudaGetLastError();
+}
+cudaError_t ak_launch_tile_flags(cudaStream_t st, uint32_t nlayers, uint32_t ntiles, uint32_t ntx, const int4 *box,
+                                 uint32_t *flags) {
+    const uint64_t n = (uint64_t)nlayers * ntiles;
+    if (n)
+        ak_tile_flags<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(nlayers, n, ntx, box, flags);
+    return cudaGetLastError();
+}
+cudaError_t ak_launch_tile_lists(cudaStream_t st, uint64_t n, uint32_t nlayers, const uint32_t *flags,
+                                 const uint32_t *pos, uint32_t *list) {
+    if (n)
+        ak_tile_lists<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, nlayers, flags, pos, list);
     return cudaGetLastError();
 }
 cudaError_t ak_launch_adam(cudaStream_t st, float *param, const float *grad, float *m, float *v, uint32_t n, float lr,

@@ -23,6 +23,12 @@
 struct ak_scene {
     uint32_t        W, H, npaths, ncontours, nseg, ncp, nlayers, nbands, band;
     float4          bg;
+    /* the window of the canvas the kernels cover: W x H pixels from
+       (x0, y0) of a CW x CH canvas (the whole canvas, or one tile of a tiled
+       scene); nlayers are the window's layers, layer_map[i] the scene layer of
+       window layer i (null: the identity) */
+    uint32_t        x0, y0, CW, CH;
+    const uint32_t *layer_map;
     const uint8_t  *seg_kind;     /* nseg */
     const uint32_t *seg_cp;       /* nseg: first control point */
     const uint32_t *seg_end;      /* nseg: control point the segment ends at */
@@ -61,7 +67,18 @@ cudaError_t ak_launch_composite_bwd(cudaStream_t st, const ak_scene &S, const ak
 cudaError_t ak_launch_cover_bwd(cudaStream_t st, const ak_scene &S, const ak_bufs &B, const float *widths,
                                 float2 *gpts, float *gwidth);
 cudaError_t ak_launch_reduce(cudaStream_t st, const ak_scene &S, uint32_t nblocks, const float4 *color_part,
-                             float4 *d_colors, const float *loss_part, float *loss);
+                             float4 *d_colors, const float *loss_part, float *loss, bool accumulate = false);
+/* tiled scenes: per scene layer its box in tiles (x0, y0, x1, y1 inclusive;
+   x0 > x1 when empty), from its flattened points (strokes widened by half
+   their width plus a pixel) */
+cudaError_t ak_launch_layer_boxes(cudaStream_t st, const ak_scene &S, const ak_bufs &B, const float *widths,
+                                  uint32_t tile, uint32_t ntx, uint32_t nty, int4 *box);
+/* flags[t * nlayers + l] = 1 when layer l's box holds tile t */
+cudaError_t ak_launch_tile_flags(cudaStream_t st, uint32_t nlayers, uint32_t ntiles, uint32_t ntx, const int4 *box,
+                                 uint32_t *flags);
+/* list[pos[i]] = i % nlayers where flags[i] (pos: exclusive scan of the flags) */
+cudaError_t ak_launch_tile_lists(cudaStream_t st, uint64_t n, uint32_t nlayers, const uint32_t *flags,
+                                 const uint32_t *pos, uint32_t *list);
 cudaError_t ak_launch_adam(cudaStream_t st, float *param, const float *grad, float *m, float *v, uint32_t n, float lr,
                            float beta1, float beta2, float eps, uint32_t step, float lo, float hi);
 uint32_t    ak_pixel_blocks(const ak_scene &S);

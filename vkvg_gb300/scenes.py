@@ -617,6 +617,155 @@ def analytic_scene(seed=3, n_paths=128, n_cubics=8, size=256, w_min=0.5, w_max=4
     return scene, {"ctrl": ctrl, "colors": colors, "widths": widths}
 
 
+def analytic_glyph_scene(seed=5, n_outlines=200000, n_strokes=20000, size=4096, size_min=8.0, size_max=48.0):
+    """The large glyph configuration in the analytic mode's terms: a size x
+    size fp32 canvas on white; n_outlines glyph-like outlines of quadratic
+    Beziers (outline size U[size_min, size_max) px, 1-3 contours of 6-40
+    quads, the outer contour counter-clockwise on screen and the holes inside
+    it clockwise), each a fill layer (NON_ZERO); then n_strokes closed chains
+    of 3-8 quads as stroke layers of width U[1, 3) (the analytic mode strokes
+    closed contours with bevel joints).  Each path's colour is the scene's
+    linear gradient (two random RGBA stops along a random axis) at the path's
+    first point, premultiplied.  Every quadratic is degree-elevated to the
+    cubic with the same curve (control points p, p + 2/3 (q - p),
+    p' + 2/3 (q - p'), exact), so the mode's cubic segments carry it; quad
+    holds the outline control points (on-curve P, off-curve Q, next on-curve
+    index) and elevate / elevate_adjoint map them to the cubic control
+    points and gradients back.  Random values are splitmix64 outputs drawn in
+    blocks (np_rnd).  Returns (scene, params, quad)."""
+    import numpy as np
+
+    pos = [0]
+
+    def take(n):
+        v = np_rnd(seed, pos[0], n)
+        pos[0] += n
+        return v
+
+    g = take(12)
+    gx0, gy0, gx1, gy1 = g[0] * size, g[1] * size, g[2] * size, g[3] * size
+    c0 = np.array([g[4], g[5], g[6], 0.5 + 0.5 * g[7]])
+    c1 = np.array([g[8], g[9], g[10], 0.5 + 0.5 * g[11]])
+    o = take(4 * n_outlines).reshape(n_outlines, 4)
+    cx, cy = o[:, 0] * size, o[:, 1] * size
+    osz = size_min + (size_max - size_min) * o[:, 2]
+    ncont = 1 + np.minimum((o[:, 3] * 3).astype(np.int64), 2)
+    nc = int(ncont.sum())
+    cont_out = np.repeat(np.arange(n_outlines), ncont)
+    first = np.zeros(nc, bool)
+    first[np.concatenate([[0], np.cumsum(ncont)[:-1]])] = True
+    c = take(4 * nc).reshape(nc, 4)
+    nq = 6 + np.minimum((c[:, 0] * 35).astype(np.int64), 34)
+    half = osz[cont_out] / 2
+    rad = np.where(first, half, half * (0.2 + 0.2 * c[:, 1]))
+    off = np.where(first, 0.0, half * 0.35)
+    ang = c[:, 2] * 2 * np.pi
+    ccx, ccy = cx[cont_out] + off * np.cos(ang), cy[cont_out] + off * np.sin(ang)
+    sgn = np.where(first, -1.0, 1.0)
+    nqt = int(nq.sum())
+    qc = np.repeat(np.arange(nc), nq)
+    k = np.arange(nqt) - np.repeat(np.cumsum(nq) - nq, nq)
+    q = take(3 * nqt).reshape(nqt, 3)
+    th = (k + 0.3 * (q[:, 0] - 0.5)) * (2 * np.pi / nq[qc])
+    th_c = (k + 0.5) * (2 * np.pi / nq[qc])
+    r_on, r_off = rad[qc] * (0.7 + 0.3 * q[:, 1]), rad[qc] * (0.7 + 0.45 * q[:, 2])
+    P = np.stack([ccx[qc] + r_on * np.cos(sgn[qc] * th), ccy[qc] + r_on * np.sin(sgn[qc] * th)], 1)
+    Q = np.stack([ccx[qc] + r_off * np.cos(sgn[qc] * th_c), ccy[qc] + r_off * np.sin(sgn[qc] * th_c)], 1)
+    nxt = np.arange(nqt) + 1
+    last = np.cumsum(nq) - 1
+    nxt[last] = last - nq + 1
+    path_ncont = list(ncont)
+    cont_nseg = list(nq)
+    flags = [AN_FILL] * n_outlines
+    widths = np.ones(n_outlines + n_strokes, np.float32)
+    path_start = np.concatenate([[0], np.cumsum(np.add.reduceat(nq, np.concatenate([[0], np.cumsum(ncont)[:-1]])))[:-1]])
+    starts = [P[path_start]]
+    if n_strokes:
+        st = take(5 * n_strokes).reshape(n_strokes, 5)
+        ns = 3 + np.minimum((st[:, 0] * 6).astype(np.int64), 5)
+        nst = int(ns.sum())
+        sk = np.arange(nst) - np.repeat(np.cumsum(ns) - ns, ns)
+        si = np.repeat(np.arange(n_strokes), ns)
+        w = take(4 * nst).reshape(nst, 4)
+        step = 6.0 + 12.0 * st[:, 3]
+        hd = st[:, 4] * 2 * np.pi
+        sx0, sy0 = st[:, 1] * size, st[:, 2] * size
+        hh = hd[si] + np.cumsum(0.8 * (w[:, 0] - 0.5))
+        ex = sx0[si] + np.cumsum(step[si] * np.cos(hh))
+        ey = sy0[si] + np.cumsum(step[si] * np.sin(hh))
+        b0 = np.cumsum(ns) - ns
+        ex = ex - np.repeat(ex[b0] - sx0 - step * np.cos(hh[b0]), ns)
+        ey = ey - np.repeat(ey[b0] - sy0 - step * np.sin(hh[b0]), ns)
+        # on-curve points: the chain's start then its joints; the last quad
+        # closes the contour back to the start
+        SP = np.stack([np.where(sk == 0, np.repeat(sx0, ns), np.roll(ex, 1)),
+                       np.where(sk == 0, np.repeat(sy0, ns), np.roll(ey, 1))], 1)
+        SN = np.stack([np.where(sk == ns[si] - 1, np.repeat(sx0, ns), ex), np.where(sk == ns[si] - 1, np.repeat(sy0, ns), ey)], 1)
+        SQ = 0.5 * (SP + SN) + np.stack([0.4 * step[si] * (w[:, 1] - 0.5), 0.4 * step[si] * (w[:, 2] - 0.5)], 1)
+        snxt = nqt + np.arange(nst) + 1
+        slast = nqt + np.cumsum(ns) - 1
+        snxt[slast - nqt] = slast - ns + 1
+        P = np.concatenate([P, SP])
+        Q = np.concatenate([Q, SQ])
+        nxt = np.concatenate([nxt, snxt])
+        path_ncont += [1] * n_strokes
+        cont_nseg += list(ns)
+        flags += [AN_STROKE] * n_strokes
+        widths[n_outlines:] = 1.0 + 2.0 * w[b0, 3]
+        starts.append(SP[b0])
+    starts = np.concatenate(starts)
+    # colour: the gradient at the path's first point (smoothstep between the stops)
+    dx, dy = gx1 - gx0, gy1 - gy0
+    t = np.clip(((starts[:, 0] - gx0) * dx + (starts[:, 1] - gy0) * dy) / max(dx * dx + dy * dy, 1e-9), 0.0, 1.0)
+    t = t * t * (3 - 2 * t)
+    col = c0[None, :] * (1 - t[:, None]) + c1[None, :] * t[:, None]
+    colors = np.concatenate([col[:, :3] * col[:, 3:], col[:, 3:]], 1).astype(np.float32)
+    nseg = len(P)
+    scene = {
+        "width": size, "height": size, "background": np.ones(4, np.float32),
+        "path_ncontours": np.array(path_ncont, np.uint32), "path_flags": np.array(flags, np.uint32),
+        "contour_nseg": np.array(cont_nseg, np.uint32), "seg_kind": np.full(nseg, AN_CUBIC, np.uint8),
+    }
+    quad = {"P": P.astype(np.float32), "Q": Q.astype(np.float32), "nxt": nxt.astype(np.int64)}
+    return scene, {"ctrl": elevate(quad), "colors": colors, "widths": widths}, quad
+
+
+def elevate(quad, P=None, Q=None):
+    """cubic control points [segments * 3][2] of the quadratic segments
+    (start p, p + 2/3 (q - p), p' + 2/3 (q - p') with p' the next on-curve
+    point), in float32"""
+    import numpy as np
+
+    P = np.asarray(quad["P"] if P is None else P, np.float32)
+    Q = np.asarray(quad["Q"] if Q is None else Q, np.float32)
+    t = np.float32(2.0 / 3.0)
+    out = np.empty((len(P), 3, 2), np.float32)
+    out[:, 0] = P
+    np.subtract(Q, P, out=out[:, 1])
+    out[:, 1] *= t
+    out[:, 1] += P
+    Pn = P[quad["nxt"]]
+    np.subtract(Q, Pn, out=out[:, 2])
+    out[:, 2] *= t
+    out[:, 2] += Pn
+    return out.reshape(-1, 2)
+
+
+def elevate_adjoint(quad, g):
+    """gradients of the on-curve and off-curve points from the gradients of
+    the cubic control points (the transpose of elevate)"""
+    import numpy as np
+
+    g = np.asarray(g, np.float64).reshape(-1, 3, 2)
+    n = len(g)
+    gP = g[:, 0] + g[:, 1] / 3.0
+    nxt = quad["nxt"]
+    gP[:, 0] += np.bincount(nxt, g[:, 2, 0], n) / 3.0
+    gP[:, 1] += np.bincount(nxt, g[:, 2, 1], n) / 3.0
+    gQ = (2.0 / 3.0) * (g[:, 1] + g[:, 2])
+    return gP, gQ
+
+
 def glyph_streams(seed=5, n_outlines=200000, n_strokes=20000, size=4096, size_min=8.0, size_max=48.0):
     """The large glyph scene as a command stream: a size x size surface, MSAA
     4, which the caller paints white and then sets the gradient source on
