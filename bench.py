@@ -34,6 +34,12 @@ cpu_baseline - the CPU restatement of vkvg's path code (oracle/): the
          one-core and all-core medians on bounded samples of the other
          configurations (cpu_baseline.configs).
 
+svg    - SVG ingestion through vkvg's SVG API (include/vkvg-svg.h): a seeded
+         600-shape document parsed once, then rendered, flushed and read back
+         per step (host timer); reported beside the headline.
+analytic.glyphs - the 4096x4096 glyph construction in the differentiable
+         analytic mode (tiled), forward and forward + backward (CUDA events).
+
 `--impl reference` times that CPU implementation alone (vkvg itself cannot be
 built or run here: no Vulkan stack and its vkh / glutess submodules are empty).
 Multi-GPU: replicas only (one independent frame per GPU).
@@ -66,6 +72,7 @@ def parse():
     p.add_argument("--no-batch", action="store_true", help="skip the uneven-batch comparison")
     p.add_argument("--no-analytic", action="store_true", help="skip the differentiable analytic-coverage workload")
     p.add_argument("--no-glyphs", action="store_true", help="skip the 4096x4096 glyph workload")
+    p.add_argument("--svg-shapes", type=int, default=600, help="shapes of the SVG ingestion workload (0: skip)")
     p.add_argument("--adam-steps", type=int, default=200, help="Adam steps of the differentiable workload")
     return p.parse_args()
 
@@ -734,6 +741,42 @@ def main():
     h2d = int(stats[12])
     d2h = a.size * a.size * 4
 
+    # ---- SVG ingestion through vkvg's SVG API (include/vkvg-svg.h): parse a
+    # seeded tiger-scale document, then render it on a surface of its size and
+    # read the image back, every step
+    svg = None
+    if a.svg_shapes > 0:
+        text = scenes.svg_document(seed=7, n_shapes=a.svg_shapes, size=a.size)
+        t0 = time.perf_counter()
+        doc = gb.Svg(text)
+        parse_ms = (time.perf_counter() - t0) * 1000.0
+        sw, sh = doc.dimensions()
+        nshapes = int(L.vkvg_gb300_svg_shape_count(doc.h))
+        ssurf = gb.Surface(dev, sw, sh)
+        sctx = ssurf.context()
+        simg = np.zeros((sh, sw, 4), np.uint8)
+
+        def svg_step():
+            doc.render(sctx)
+            L.vkvg_flush(sctx.h)
+            assert L.vkvg_surface_write_to_memory(ssurf.h, simg.ctypes.data_as(C.c_void_p)) == 0
+
+        for _ in range(2):
+            svg_step()
+        torch.cuda.synchronize()
+        s_steps = 5
+        t0 = time.perf_counter()
+        for _ in range(s_steps):
+            svg_step()
+        s_t = (time.perf_counter() - t0) / s_steps
+        svg = {"workload": "seeded SVG document (svg_document seed 7), %d shapes, %dx%d, 4x MSAA" % (nshapes, sw, sh),
+               "bytes": len(text), "parse_ms": parse_ms, "render_e2e_ms": s_t * 1000.0,
+               "shapes_per_s": nshapes / s_t, "note": "host timer around vkvg_svg_render + vkvg_flush + "
+                                                      "write_to_memory; not the headline metric"}
+        sctx.destroy()
+        ssurf.destroy()
+        doc.destroy()
+
     # ---- the uneven batch (64 surfaces, Pareto path counts): its frames one
     # after another (the plain form), then as one batch job
     batch = None
@@ -869,6 +912,8 @@ def main():
         line["batch"] = batch
     if glyphs:
         line["glyphs"] = glyphs
+    if svg:
+        line["svg"] = svg
     if analytic:
         analytic["roofline"]["peak"] = peak
         analytic["roofline"]["frac"] = analytic["roofline"]["achieved"] / peak

@@ -195,6 +195,20 @@ vkvg_public vkvg_status_t vkvg_gb300_batch_execute(VkvgBatch batch);
 vkvg_public vkvg_status_t vkvg_gb300_batch_timing(VkvgBatch batch, float out[9]);
 vkvg_public void          vkvg_gb300_batch_destroy(VkvgBatch batch);
 
+/* ---- parsed SVG documents, read back for the parity tests (no vkvg
+ * counterpart; the handle is include/vkvg-svg.h's VkvgSvg).  shape: u = fill
+ * paint type (0 none, 1 colour, 2 linear gradient, 3 radial gradient), fill
+ * colour, stroke paint type, stroke colour (ABGR words, r in the low byte; a
+ * gradient gives its first stop's), visible, subpath count; f = opacity,
+ * stroke width, box[4] (x0, y0, x1, y1).  path: its cubic points (x, y
+ * pairs; 1 + 3n of them), at most cap_points copied, and whether it is
+ * closed.  Both return 0, or -1 for an index out of range. */
+typedef struct _vkvg_svg_t *VkvgSvgDoc;
+vkvg_public uint32_t vkvg_gb300_svg_shape_count(VkvgSvgDoc svg);
+vkvg_public int      vkvg_gb300_svg_shape(VkvgSvgDoc svg, uint32_t i, char id[64], uint32_t u[6], float f[6]);
+vkvg_public int      vkvg_gb300_svg_path(VkvgSvgDoc svg, uint32_t shape, uint32_t path, float *pts, uint32_t cap_points,
+                                         uint32_t *npts, uint32_t *closed);
+
 /* ---- differentiable analytic coverage (no vkvg counterpart) ----
  *
  * A scene of paths, each a list of closed contours of line and cubic

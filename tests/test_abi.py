@@ -1,5 +1,6 @@
 """The C-ABI library builds for sm_103a, loads, and exports every function
-that include/vkvg.h and include/vkvg_gb300.h declare (no GPU needed)."""
+that include/vkvg.h, include/vkvg-svg.h and include/vkvg_gb300.h declare
+(no GPU needed)."""
 import ctypes
 import os
 import re
@@ -12,7 +13,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 def declared_functions():
     names = []
-    for h in ("vkvg.h", "vkvg_gb300.h"):
+    for h in ("vkvg.h", "vkvg-svg.h", "vkvg_gb300.h"):
         src = open(os.path.join(ROOT, "include", h)).read()
         src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
         names += re.findall(r"vkvg_public\s+[\w\s\*]+?\b(vkvg_\w+)\s*\(", src)
@@ -22,7 +23,8 @@ def declared_functions():
 def test_headers_declare_api():
     names = declared_functions()
     for n in ("vkvg_move_to", "vkvg_curve_to", "vkvg_arc", "vkvg_fill", "vkvg_stroke", "vkvg_set_dash",
-              "vkvg_set_fill_rule", "vkvg_surface_write_to_png", "vkvg_gb300_frame_execute"):
+              "vkvg_set_fill_rule", "vkvg_surface_write_to_png", "vkvg_gb300_frame_execute", "vkvg_svg_render",
+              "vkvg_surface_create_from_svg"):
         assert n in names
     assert len(names) > 100
 

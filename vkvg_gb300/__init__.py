@@ -172,6 +172,17 @@ SIGNATURES = {
     "vkvg_gb300_batch_execute": (_I, [_P]),
     "vkvg_gb300_batch_timing": (_I, [_P, _P]),
     "vkvg_gb300_batch_destroy": (None, [_P]),
+    # include/vkvg-svg.h
+    "vkvg_svg_load": (_P, [C.c_char_p]),
+    "vkvg_svg_load_fragment": (_P, [C.c_char_p]),
+    "vkvg_svg_destroy": (None, [_P]),
+    "vkvg_svg_get_dimensions": (None, [_P, _P, _P]),
+    "vkvg_svg_render": (None, [_P, _P, C.c_char_p]),
+    "vkvg_surface_create_from_svg": (_P, [_P, _U, _U, C.c_char_p]),
+    "vkvg_surface_create_from_svg_fragment": (_P, [_P, _U, _U, C.c_char_p]),
+    "vkvg_gb300_svg_shape_count": (_U, [_P]),
+    "vkvg_gb300_svg_shape": (_I, [_P, _U, _P, _P, _P]),
+    "vkvg_gb300_svg_path": (_I, [_P, _U, _U, _P, _U, _P, _P]),
     "vkvg_gb300_analytic_create": (_P, [_U, _U, _P, _U, _P, _P, _U, _P, _U, _P]),
     "vkvg_gb300_analytic_create_tiled": (_P, [_U, _U, _U, _P, _U, _P, _P, _U, _P, _U, _P]),
     "vkvg_gb300_analytic_destroy": (None, [_P]),
@@ -425,6 +436,52 @@ def pmath(fn, a, b=None, device=False):
     if st:
         raise VkvgError("pmath_eval: %d" % st)
     return out
+
+
+class Svg:
+    """A parsed SVG document (include/vkvg-svg.h): vkvg_svg_load_fragment of
+    `text` (bytes), rendered with render(ctx, id)."""
+
+    def __init__(self, text):
+        self.L = lib()
+        self.h = self.L.vkvg_svg_load_fragment(text)
+        if not self.h:
+            raise VkvgError("vkvg_svg_load_fragment failed")
+
+    def dimensions(self):
+        w, h = C.c_uint32(), C.c_uint32()
+        self.L.vkvg_svg_get_dimensions(self.h, C.byref(w), C.byref(h))
+        return w.value, h.value
+
+    def render(self, ctx, sub_id=None):
+        self.L.vkvg_svg_render(self.h, ctx.h, sub_id)
+
+    def shapes(self):
+        """what vkvg's SVG walk reads, per shape: id, fill / stroke paint type
+        and colour, visibility, opacity, stroke width, bounds, and the paths
+        as (float32 points [n, 2], closed)"""
+        out = []
+        for i in range(self.L.vkvg_gb300_svg_shape_count(self.h)):
+            idb = C.create_string_buffer(64)
+            u = np.zeros(6, np.uint32)
+            f = np.zeros(6, np.float32)
+            self.L.vkvg_gb300_svg_shape(self.h, i, idb, _ptr(u), _ptr(f))
+            paths = []
+            for p in range(int(u[5])):
+                n, closed = C.c_uint32(), C.c_uint32()
+                self.L.vkvg_gb300_svg_path(self.h, i, p, None, 0, C.byref(n), C.byref(closed))
+                pts = np.zeros((max(n.value, 1), 2), np.float32)
+                self.L.vkvg_gb300_svg_path(self.h, i, p, _ptr(pts), n.value, C.byref(n), C.byref(closed))
+                paths.append((pts[:n.value], bool(closed.value)))
+            out.append({"id": idb.value, "fill_type": int(u[0]), "fill_color": int(u[1]), "stroke_type": int(u[2]),
+                        "stroke_color": int(u[3]), "visible": bool(u[4]), "opacity": f[0], "stroke_width": f[1],
+                        "bounds": f[2:6].copy(), "paths": paths})
+        return out
+
+    def destroy(self):
+        if self.h:
+            self.L.vkvg_svg_destroy(self.h)
+            self.h = None
 
 
 class Analytic:

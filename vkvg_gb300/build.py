@@ -24,7 +24,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_GEOM = ["flatten.cu", "stroke.cu", "setup.cu", "analytic_flat.cu"]
 CU_FAST = ["raster.cu", "raster_rows.cu", "scan.cu", "analytic.cu"]
-CPP = ["api.cpp", "pipeline.cpp", "extras.cpp", "png.cpp", "batch.cpp", "analytic.cpp"]
+CPP = ["api.cpp", "pipeline.cpp", "extras.cpp", "png.cpp", "svg.cpp", "batch.cpp", "analytic.cpp"]
 HEADERS = ["gb_types.h", "pmath.h", "launch.h", "host.h", "xdiv.cuh", "bezier.cuh", "analytic.h", "raster_common.cuh"]
 
 NVCC_COMMON = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-fvisibility=hidden",
@@ -50,7 +50,7 @@ def _stale():
         return True
     t = os.path.getmtime(LIB)
     deps = [os.path.join(CSRC, f) for f in CU_GEOM + CU_FAST + CPP + HEADERS]
-    deps += [os.path.join(INC, f) for f in ("vkvg.h", "vkvg_gb300.h")] + [os.path.abspath(__file__)]
+    deps += [os.path.join(INC, f) for f in ("vkvg.h", "vkvg_gb300.h", "vkvg-svg.h")] + [os.path.abspath(__file__)]
     return any(os.path.getmtime(d) > t for d in deps)
 
 

@@ -418,6 +418,195 @@ def encode(ops):
     return np.array(cmds, np.uint32), np.array(args, np.float32)
 
 
+def svg_document(seed=31, n_shapes=40, size=240, quirks=False):
+    """A seeded SVG document exercising what vkvg's SVG path reads: every
+    path command (absolute and relative, implicit repeats, arcs with packed
+    flags), rect / rounded rect / circle / ellipse / line / polyline /
+    polygon, nested groups with transform lists (matrix, translate, scale,
+    rotate about a point, skewX, skewY), style attributes and style="...",
+    colours as #rgb, #rrggbb, rgb(), rgb(%) and names (known and unknown),
+    opacities, stroke widths with units, linear and radial gradients with
+    stops (one reached through xlink:href), display:none, and a viewBox with
+    preserveAspectRatio.  With quirks, some empty-element tags get a space
+    before their closing '/>', some values trailing spaces, and some path
+    data a trailing newline.  (Whitespace before the '>' of a start tag is
+    not generated: vkvg's parser takes the string terminator for whitespace
+    there and reads on into the following tags.)  Returns the document text
+    (bytes)."""
+    r = SplitMix64(seed)
+    u = lambda lo, hi: lo + (hi - lo) * r.rnd()
+    pick = lambda seq: seq[r.randint(0, len(seq) - 1)]
+
+    def num(v):
+        k = r.randint(0, 5)
+        if k == 0:
+            return "%.0f" % v
+        if k == 1:
+            return ("%.3e" % v)
+        if k == 2 and abs(v) < 1:
+            return ("%.3f" % v).replace("0.", ".", 1)
+        return "%.2f" % v
+
+    def color():
+        k = r.randint(0, 6)
+        if k == 0:
+            return "#%x%x%x" % (r.randint(0, 15), r.randint(0, 15), r.randint(0, 15))
+        if k == 1:
+            return "rgb(%d,%d,%d)" % (r.randint(0, 255), r.randint(0, 255), r.randint(0, 255))
+        if k == 2:
+            return "rgb(%d%%, %d%%, %d%%)" % (r.randint(0, 100), r.randint(0, 100), r.randint(0, 100))
+        if k == 3:
+            return pick(["red", "green", "blue", "yellow", "cyan", "magenta", "black", "grey", "white", "orange"])
+        return "#%02x%02x%02x" % (r.randint(0, 255), r.randint(0, 255), r.randint(0, 255))
+
+    def paint():
+        k = r.randint(0, 9)
+        if k == 0:
+            return "none"
+        if k == 1:
+            return "url(#lg%d)" % r.randint(0, 2)
+        if k == 2:
+            return "url(#rg0)"
+        return color()
+
+    def transform():
+        fs = []
+        for _ in range(r.randint(1, 3)):
+            k = r.randint(0, 5)
+            if k == 0:
+                fs.append("translate(%s,%s)" % (num(u(-30, 30)), num(u(-30, 30))))
+            elif k == 1:
+                fs.append("scale(%s)" % num(u(0.6, 1.4)) if r.randint(0, 1) else
+                          "scale(%s %s)" % (num(u(0.6, 1.4)), num(u(0.6, 1.4))))
+            elif k == 2:
+                fs.append("rotate(%s)" % num(u(-40, 40)) if r.randint(0, 1) else
+                          "rotate(%s %s %s)" % (num(u(-40, 40)), num(u(0, size)), num(u(0, size))))
+            elif k == 3:
+                fs.append("skewX(%s)" % num(u(-20, 20)))
+            elif k == 4:
+                fs.append("skewY(%s)" % num(u(-20, 20)))
+            else:
+                fs.append("matrix(%s)" % " ".join(num(v) for v in (u(0.7, 1.2), u(-0.3, 0.3), u(-0.3, 0.3),
+                                                                     u(0.7, 1.2), u(-20, 20), u(-20, 20))))
+        return " ".join(fs)
+
+    def style_attrs():
+        out = []
+        if r.randint(0, 2) == 0:
+            decl = ["fill:%s" % paint(), "stroke:%s" % paint(), "stroke-width:%s" % num(u(0.5, 6))]
+            if r.randint(0, 1):
+                decl.append("fill-opacity: %s" % num(u(0.2, 1)))
+            out.append('style="%s"' % "; ".join(decl[:r.randint(1, len(decl))]))
+        else:
+            if r.randint(0, 3):
+                out.append('fill="%s"' % paint())
+            if r.randint(0, 1):
+                out.append('stroke="%s"' % paint())
+                out.append('stroke-width="%s%s"' % (num(u(0.5, 5)), pick(["", "px", "pt", "mm", "%"])))
+            if r.randint(0, 3) == 0:
+                out.append('stroke-opacity="%s"' % num(u(0.2, 1)))
+        if r.randint(0, 4) == 0:
+            out.append('opacity="%s"' % num(u(0.3, 1)))
+        if r.randint(0, 4) == 0:
+            out.append('transform="%s"' % transform())
+        if r.randint(0, 25) == 0:
+            out.append('display="none"')
+        return " ".join(out)
+
+    def path_data():
+        d = ["M%s %s" % (num(u(0, size)), num(u(0, size)))]
+        for _ in range(r.randint(2, 7)):
+            c = pick("LlHhVvCcSsQqTtAa")
+            k = {"L": 2, "H": 1, "V": 1, "C": 6, "S": 4, "Q": 4, "T": 2, "A": 7}[c.upper()]
+            reps = r.randint(1, 2)
+            args = []
+            for _ in range(reps):
+                if c.upper() == "A":
+                    args += [num(u(5, 60)), num(u(5, 60)), num(u(-90, 90))]
+                    flags = "%d%d" % (r.randint(0, 1), r.randint(0, 1))
+                    args.append(flags if r.randint(0, 1) else " ".join(flags))
+                    args += [num(u(-40, 40) if c == "a" else u(0, size)), num(u(-40, 40) if c == "a" else u(0, size))]
+                else:
+                    args += [num(u(-40, 40) if c.islower() else u(0, size)) for _ in range(k)]
+            sep = pick([" ", ","])
+            d.append(c + sep.join(args))
+        if r.randint(0, 1):
+            d.append(pick(["Z", "z"]))
+        if r.randint(0, 3) == 0:
+            d.append("m%s %s l%s %s %s %s z" % tuple(num(u(-30, 30)) for _ in range(6)))
+        return "".join(x + pick([" ", "", "\n"]) for x in d)
+
+    def shape():
+        k = r.randint(0, 7)
+        a = style_attrs()
+        if k <= 1:
+            return '<path id="p%d" d="%s" %s/>' % (r.randint(0, 999), path_data(), a)
+        if k == 2:
+            rr = ' rx="%s"' % num(u(0, 15)) if r.randint(0, 1) else ""
+            rr += ' ry="%s"' % num(u(0, 15)) if r.randint(0, 2) == 0 else ""
+            return '<rect x="%s" y="%s" width="%s" height="%s"%s %s/>' % (
+                num(u(0, size)), num(u(0, size)), num(u(5, 90)), num(u(5, 90)), rr, a)
+        if k == 3:
+            return '<circle cx="%s" cy="%s" r="%s" %s/>' % (num(u(0, size)), num(u(0, size)), num(u(3, 50)), a)
+        if k == 4:
+            return '<ellipse cx="%s" cy="%s" rx="%s" ry="%s" %s/>' % (
+                num(u(0, size)), num(u(0, size)), num(u(3, 60)), num(u(3, 40)), a)
+        if k == 5:
+            return '<line x1="%s" y1="%s" x2="%s" y2="%s" %s/>' % tuple(
+                [num(u(0, size)) for _ in range(4)] + [a])
+        pts = " ".join("%s,%s" % (num(u(0, size)), num(u(0, size))) for _ in range(r.randint(3, 7)))
+        return '<%s points="%s" %s/>' % ("polyline" if k == 6 else "polygon", pts, a)
+
+    vb = r.randint(0, 3)
+    root = ['width="%d" height="%d"' % (size, size)]
+    if vb:
+        root.append('viewBox="%s %s %s %s"' % (num(u(-20, 20)), num(u(-20, 20)), num(u(size * 0.8, size * 1.3)),
+                                               num(u(size * 0.8, size * 1.3))))
+        root.append('preserveAspectRatio="%s"' % pick(["xMidYMid meet", "xMinYMax slice", "none", "xMaxYMin"]))
+    out = ['<?xml version="1.0" encoding="UTF-8"?>', "<!-- seeded test document -->",
+           '<svg xmlns="http://www.w3.org/2000/svg" xmlns:xlink="http://www.w3.org/1999/xlink" %s>' % " ".join(root),
+           "<defs>"]
+    for g in range(3):
+        if g == 2:
+            out.append('<linearGradient id="lg2" xlink:href="#lg0" x1="0" y1="0" x2="1" y2="1"/>')
+            continue
+        out.append('<linearGradient id="lg%d" x1="%s" y1="0" x2="1" y2="%s">' % (g, num(u(0, 0.5)), num(u(0, 1))))
+        for _ in range(r.randint(2, 4)):
+            off = u(0, 1)
+            if r.randint(0, 1):
+                out.append('<stop offset="%s" stop-color="%s" stop-opacity="%s"/>' % (num(off), color(), num(u(0.3, 1))))
+            else:
+                out.append('<stop offset="%d%%" style="stop-color:%s"/>' % (int(off * 100), color()))
+        out.append("</linearGradient>")
+    out.append('<radialGradient id="rg0" cx="50%" cy="50%" r="50%">')
+    out.append('<stop offset="0" stop-color="%s"/><stop offset="1" stop-color="%s"/>' % (color(), color()))
+    out.append("</radialGradient></defs>")
+    depth = 0
+    for i in range(n_shapes):
+        if r.randint(0, 5) == 0 and depth < 3:
+            out.append(('<g id="g%d" %s' % (i, style_attrs())).rstrip() + ">")
+            depth += 1
+        out.append(shape())
+        if depth and r.randint(0, 4) == 0:
+            out.append("</g>")
+            depth -= 1
+    out += ["</g>"] * depth + ["</svg>"]
+    text = "\n".join(out)
+    if quirks:
+        q = []
+        for part in text.split("\n"):
+            k = r.randint(0, 5)
+            if k == 0 and part.endswith('"/>'):
+                part = part[:-3] + '" />'
+            elif k == 1 and part.startswith('" '):
+                part = "\n" + part
+            elif k == 2 and ' d="' in part:
+                part = part.replace('" ', '  " ', 1)
+            q.append(part)
+        text = "\n".join(q)
+    return text.encode()
+
+
 def batch_scenes(seed=2, n_surfaces=64, max_paths=20000, min_paths=100, max_segs=2000, max_side=2048,
                  samples=4):
     """The uneven batch: n_surfaces independent surfaces, side log-uniform in
