@@ -11,15 +11,17 @@
  * copied to pinned memory after each forward and checked when it has landed;
  * only the first forward waits for it, to size the point buffer.
  *
- * A tiled scene (create_tiled) keeps the same kernels but runs them per
- * square tile of the canvas: after the flattening, every layer's box in
- * tiles (from its points, strokes widened by half their width), a flag per
- * (tile, layer), one exclusive scan of the flags and a compaction give every
- * tile its layers in scene order; the per-tile counts are read back (the one
- * synchronisation of a tiled forward) to place every tile's area planes and
- * checkpoints in one buffer, all kept resident for the backward.  A layer is
- * zero outside its box, so a tile's composite over its own layers equals the
- * whole canvas's there; the adjoints accumulate over tiles.
+ * A tiled scene (create_tiled) keeps the same kernels and runs each of them
+ * once over every square tile of the canvas: after the flattening, every
+ * layer's box in tiles (from its points, strokes widened by half their
+ * width), a flag per (tile, layer), one exclusive scan of the flags and a
+ * compaction give the (tile, layer) pairs, tile by tile in scene order; the
+ * per-tile counts are read back (the one synchronisation of a tiled
+ * forward) to place every tile's area planes and checkpoints in one
+ * buffer, all kept resident for the backward.  A coverage block takes its
+ * pair's tile and plane from the pair index, a compositing block its tile
+ * from its block index.  A layer is zero outside its box, so a tile's
+ * composite over its own layers equals the whole canvas's there.
  */
 #include "analytic.h"
 #include "host.h"
@@ -51,14 +53,14 @@ struct _vkvg_gb300_analytic_t {
     bool        timing = false;
     cudaEvent_t ev[8]  = {};
     /* tiled scenes: tile side (0: one window, the whole canvas), tiles
-       across and down, per-layer boxes, flags and their scan, the tiles'
-       layer lists, and per tile its list start, layer count and the offsets
-       of its area planes and checkpoints */
-    uint32_t              tile = 0, ntx = 1, nty = 1;
-    DevBuf                d_box, d_flags, d_fpos, d_fscan, d_list;
-    PinnedBuf             h_tiles;
-    std::vector<uint32_t> t_first, t_count;
-    std::vector<size_t>   t_area, t_ckpt;
+       across and down, per-layer boxes, flags and their scan, the (tile,
+       layer) pairs' scene layers and tiles, per tile its pairs and plane
+       offsets (pinned, then on the device), and the scene the tiled launches
+       take (TS: every tile at once) */
+    uint32_t  tile = 0, ntx = 1, nty = 1;
+    DevBuf    d_box, d_flags, d_fpos, d_fscan, d_list, d_ptile, d_tinfo;
+    PinnedBuf h_tiles, h_tinfo;
+    ak_scene  TS{};
     /* the last forward */
     bool         have_fwd = false, sized = false;
     const float *f_ctrl = nullptr, *f_colors = nullptr, *f_widths = nullptr, *f_target = nullptr;
@@ -207,7 +209,8 @@ VkvgAnalytic create_scene(uint32_t width, uint32_t height, uint32_t tile, const 
     }
     ak_scene &S    = a->S;
     S.W = width, S.H = height, S.npaths = npaths, S.ncontours = ncontours, S.nseg = nseg, S.ncp = cp;
-    S.x0 = S.y0 = 0, S.CW = width, S.CH = height, S.layer_map = nullptr;
+    S.CW = width, S.CH = height, S.tiles = 0, S.ntx = 1, S.ntiles = 1;
+    S.layer_map = nullptr, S.pair_tile = nullptr, S.tinfo = nullptr;
     S.nlayers      = a->nlayers;
     S.band         = ak_band_rows(width);
     S.nbands       = (height + S.band - 1) / S.band;
@@ -251,11 +254,12 @@ void vkvg_gb300_analytic_destroy(VkvgAnalytic a) {
                     &a->d_path_s0,  &a->d_layer_path, &a->d_layer_stroke, &a->d_cnt, &a->d_off, &a->d_scan,
                     &a->d_pts, &a->d_pt_nb, &a->d_area, &a->d_ckpt, &a->d_canvas, &a->d_loss_part, &a->d_loss,
                     &a->d_color_part, &a->d_gpts, &a->d_status, &a->d_box, &a->d_flags, &a->d_fpos, &a->d_fscan,
-                    &a->d_list};
+                    &a->d_list, &a->d_ptile, &a->d_tinfo};
     for (DevBuf *b : bs)
         b->release();
     a->h_mon.release();
     a->h_tiles.release();
+    a->h_tinfo.release();
     if (a->ev_mon)
         cudaEventDestroy(a->ev_mon);
     for (cudaEvent_t ev : a->ev)
@@ -284,8 +288,9 @@ vkvg_status_t vkvg_gb300_analytic_set_stream(VkvgAnalytic a, void *stream) {
 } /* extern "C" */
 
 namespace {
-/* tiled scenes: the layers of every tile, their planes' places, and the
-   buffers sized for them (after the flattening of this forward) */
+/* tiled scenes: the (tile, layer) pairs, every tile's pairs and planes, the
+   buffers sized for them and the scene of the tiled launches (after the
+   flattening of this forward) */
 cudaError_t tile_setup(VkvgAnalytic a, const float *widths) {
     cudaStream_t   st = a->stream;
     const uint32_t nt = a->ntx * a->nty, nl = a->nlayers;
@@ -293,7 +298,8 @@ cudaError_t tile_setup(VkvgAnalytic a, const float *widths) {
     if (n >= 0xFFFFFFFFull)
         return cudaErrorMemoryAllocation; /* positions are 32-bit */
     if (!a->d_flags.grow(4 * std::max<uint64_t>(n, 1)) || !a->d_fpos.grow(4 * (n + 1)) ||
-        !a->d_fscan.grow(4 * gb_scan_scratch_words((uint32_t)n) + 64) || !a->h_tiles.grow(4 * ((size_t)nt + 2)))
+        !a->d_fscan.grow(4 * gb_scan_scratch_words((uint32_t)n) + 64) || !a->h_tiles.grow(4 * ((size_t)nt + 2)) ||
+        !a->h_tinfo.grow(sizeof(ak_tile_info) * nt) || !a->d_tinfo.grow(sizeof(ak_tile_info) * nt))
         return cudaErrorMemoryAllocation;
     ak_bufs     B = bufs(a);
     cudaError_t e = ak_launch_layer_boxes(st, a->S, B, widths, a->tile, a->ntx, a->nty, a->d_box.as<int4>());
@@ -313,42 +319,42 @@ cudaError_t tile_setup(VkvgAnalytic a, const float *widths) {
     if (e != cudaSuccess)
         return e;
     const uint32_t total = h[nt];
-    if (!a->d_list.grow(4 * (size_t)std::max<uint32_t>(total, 1)))
+    if (!a->d_list.grow(4 * (size_t)std::max<uint32_t>(total, 1)) ||
+        !a->d_ptile.grow(4 * (size_t)std::max<uint32_t>(total, 1)))
         return cudaErrorMemoryAllocation;
-    e = ak_launch_tile_lists(st, n, nl, a->d_flags.as<uint32_t>(), a->d_fpos.as<uint32_t>(), a->d_list.as<uint32_t>());
+    e = ak_launch_tile_lists(st, n, nl, a->d_flags.as<uint32_t>(), a->d_fpos.as<uint32_t>(), a->d_list.as<uint32_t>(),
+                             a->d_ptile.as<uint32_t>());
     gb_count_launch(1);
-    a->t_first.assign(nt, 0), a->t_count.assign(nt, 0), a->t_area.assign(nt, 0), a->t_ckpt.assign(nt, 0);
-    size_t area = 0, ckpt = 0, lossb = 1, colb = 1;
+    /* every tile's planes: a tile of tw x th pixels and c layers holds c
+       area planes and ceil(c / AK_CHUNK) checkpoint planes of tw x th */
+    ak_tile_info *ti   = (ak_tile_info *)a->h_tinfo.p;
+    size_t        area = 0, ckpt = 0;
     for (uint32_t t = 0; t < nt; t++) {
         const uint32_t tw = std::min(a->tile, a->W - (t % a->ntx) * a->tile);
         const uint32_t th = std::min(a->tile, a->H - (t / a->ntx) * a->tile);
         const size_t   px = (size_t)tw * th, cnt = (t + 1 < nt ? h[t + 1] : total) - h[t];
-        a->t_first[t] = h[t], a->t_count[t] = (uint32_t)cnt, a->t_area[t] = area, a->t_ckpt[t] = ckpt;
+        ti[t].first = h[t], ti[t].count = (uint32_t)cnt, ti[t].area = area, ti[t].ckpt = ckpt;
         area += px * cnt;
         ckpt += px * ((cnt + AK_CHUNK - 1) / AK_CHUNK);
-        lossb = std::max<size_t>(lossb, (px + 255) / 256);
-        colb  = std::max<size_t>(colb, (px + 127) / 128 * cnt);
     }
+    ak_scene &T = a->TS;
+    T           = a->S;
+    T.tiles = a->tile, T.ntx = a->ntx, T.ntiles = nt;
+    T.W = T.H    = a->tile;
+    T.band       = ak_band_rows(a->tile);
+    T.nbands     = (a->tile + T.band - 1) / T.band;
+    T.nlayers    = total;
+    T.layer_map  = a->d_list.as<uint32_t>();
+    T.pair_tile  = a->d_ptile.as<uint32_t>();
+    T.tinfo      = a->d_tinfo.as<ak_tile_info>();
     if (!a->d_area.grow(sizeof(float) * std::max<size_t>(area, 1)) ||
-        !a->d_ckpt.grow(sizeof(float4) * std::max<size_t>(ckpt, 1)) || !a->d_loss_part.grow(sizeof(float) * lossb) ||
-        !a->d_color_part.grow(sizeof(float4) * colb))
+        !a->d_ckpt.grow(sizeof(float4) * std::max<size_t>(ckpt, 1)) ||
+        !a->d_loss_part.grow(sizeof(float) * ak_pixel_blocks_all(T)) ||
+        !a->d_color_part.grow(sizeof(float4) * std::max<size_t>(ak_color_partials(T), 1)))
         return cudaErrorMemoryAllocation;
+    if (e == cudaSuccess) /* pinned, copied in stream order before the launches that read it */
+        e = cudaMemcpyAsync(a->d_tinfo.p, ti, sizeof(ak_tile_info) * nt, cudaMemcpyHostToDevice, st);
     return e;
-}
-/* the window and buffers of tile t */
-void tile_window(VkvgAnalytic a, uint32_t t, ak_scene &S, ak_bufs &B) {
-    S           = a->S;
-    S.x0        = (t % a->ntx) * a->tile;
-    S.y0        = (t / a->ntx) * a->tile;
-    S.W         = std::min(a->tile, a->W - S.x0);
-    S.H         = std::min(a->tile, a->H - S.y0);
-    S.nlayers   = a->t_count[t];
-    S.layer_map = a->d_list.as<uint32_t>() + a->t_first[t];
-    S.band      = ak_band_rows(S.W);
-    S.nbands    = (S.H + S.band - 1) / S.band;
-    B           = bufs(a);
-    B.area      = a->d_area.as<float>() + a->t_area[t];
-    B.ckpt      = a->d_ckpt.as<float4>() + a->t_ckpt[t];
 }
 } /* namespace */
 
@@ -384,45 +390,24 @@ vkvg_status_t vkvg_gb300_analytic_forward(VkvgAnalytic a, const float *ctrl, con
     ak_bufs B = bufs(a);
     e         = ak_launch_flat_emit(st, a->S, c2, B.off, a->d_pts.as<float2>(), a->d_pt_nb.as<uint2>(), a->cap,
                                     B.status);
-    if (a->tile) {
-        /* tiled: the layers of every tile, then each tile's coverage and
-           composite in turn (the loss summed over the tiles) */
-        if (e == cudaSuccess)
-            e = tile_setup(a, widths);
-        if (a->timing)
-            cudaEventRecord(a->ev[1], st);
-        if (e == cudaSuccess && loss)
-            e = cudaMemsetAsync(loss, 0, sizeof(float), st);
-        for (uint32_t t = 0; e == cudaSuccess && t < a->ntx * a->nty; t++) {
-            ak_scene S;
-            ak_bufs  Bt;
-            tile_window(a, t, S, Bt);
-            e = ak_launch_cover(st, S, Bt, widths);
-            if (e == cudaSuccess)
-                e = ak_launch_composite(st, S, Bt, (const float4 *)colors, (const float4 *)target,
-                                        target ? a->d_loss_part.as<float>() : nullptr);
-            if (e == cudaSuccess && loss)
-                e = ak_launch_reduce(st, S, ak_pixel_blocks(S), nullptr, nullptr, a->d_loss_part.as<float>(), loss,
-                                     true);
-            gb_count_launch((S.nlayers ? 1 : 0) + 1 + (loss ? 1 : 0));
-        }
-        if (a->timing) {
-            cudaEventRecord(a->ev[2], st);
-            cudaEventRecord(a->ev[3], st);
-        }
-    } else {
+    if (a->tile && e == cudaSuccess) { /* tiled: the (tile, layer) pairs, then one launch for all tiles */
+        e = tile_setup(a, widths);
+        B = bufs(a); /* the planes were sized (and may have moved) for this forward's pairs */
+    }
+    {
+        const ak_scene &S = a->tile ? a->TS : a->S;
         if (a->timing)
             cudaEventRecord(a->ev[1], st);
         if (e == cudaSuccess)
-            e = ak_launch_cover(st, a->S, B, widths);
+            e = ak_launch_cover(st, S, B, widths);
         if (a->timing)
             cudaEventRecord(a->ev[2], st);
         if (e == cudaSuccess)
-            e = ak_launch_composite(st, a->S, B, (const float4 *)colors, (const float4 *)target,
+            e = ak_launch_composite(st, S, B, (const float4 *)colors, (const float4 *)target,
                                     target ? a->d_loss_part.as<float>() : nullptr);
         gb_count_launch(3);
         if (e == cudaSuccess && loss) {
-            e = ak_launch_reduce(st, a->S, ak_pixel_blocks(a->S), nullptr, nullptr, a->d_loss_part.as<float>(), loss);
+            e = ak_launch_reduce(st, S, ak_pixel_blocks_all(S), nullptr, nullptr, a->d_loss_part.as<float>(), loss);
             gb_count_launch(1);
         }
         if (a->timing)
@@ -467,38 +452,18 @@ vkvg_status_t vkvg_gb300_analytic_backward(VkvgAnalytic a, const float *d_canvas
         e = cudaMemsetAsync(a->d_gpts.p, 0, sizeof(float2) * a->cap, st);
     if (a->timing)
         cudaEventRecord(a->ev[4], st);
-    if (a->tile) {
-        /* tiled: per tile its compositing adjoint, colour reduction and
-           coverage adjoint (gradients accumulate over the tiles) */
-        for (uint32_t t = 0; e == cudaSuccess && t < a->ntx * a->nty; t++) {
-            ak_scene S;
-            ak_bufs  Bt;
-            tile_window(a, t, S, Bt);
-            if (!S.nlayers)
-                continue;
-            e = ak_launch_composite_bwd(st, S, Bt, (const float4 *)a->f_colors, (const float4 *)a->f_target,
-                                        (const float4 *)d_canvas, a->d_color_part.as<float4>());
-            if (e == cudaSuccess)
-                e = ak_launch_reduce(st, S, ak_composite_bwd_blocks(S), a->d_color_part.as<float4>(),
-                                     (float4 *)d_colors, nullptr, nullptr);
-            if (e == cudaSuccess)
-                e = ak_launch_cover_bwd(st, S, Bt, a->f_widths, a->d_gpts.as<float2>(), d_widths);
-            gb_count_launch(3);
-        }
-        if (a->timing) {
-            cudaEventRecord(a->ev[5], st);
-            cudaEventRecord(a->ev[6], st);
-        }
-    } else {
+    {
+        const ak_scene &S = a->tile ? a->TS : a->S; /* tiled: every tile in one launch */
         if (e == cudaSuccess)
-            e = ak_launch_composite_bwd(st, a->S, B, (const float4 *)a->f_colors, (const float4 *)a->f_target,
+            e = ak_launch_composite_bwd(st, S, B, (const float4 *)a->f_colors, (const float4 *)a->f_target,
                                         (const float4 *)d_canvas, a->d_color_part.as<float4>());
         if (e == cudaSuccess)
-            e = ak_launch_reduce(st, a->S, nb, a->d_color_part.as<float4>(), (float4 *)d_colors, nullptr, nullptr);
+            e = ak_launch_reduce(st, S, a->tile ? ak_composite_bwd_blocks(S) : nb, a->d_color_part.as<float4>(),
+                                 (float4 *)d_colors, nullptr, nullptr);
         if (a->timing)
             cudaEventRecord(a->ev[5], st);
         if (e == cudaSuccess)
-            e = ak_launch_cover_bwd(st, a->S, B, a->f_widths, a->d_gpts.as<float2>(), d_widths);
+            e = ak_launch_cover_bwd(st, S, B, a->f_widths, a->d_gpts.as<float2>(), d_widths);
         if (a->timing)
             cudaEventRecord(a->ev[6], st);
     }

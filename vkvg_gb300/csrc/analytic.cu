@@ -285,6 +285,52 @@ __device__ __forceinline__ void neighbours(const ak_scene &, const ak_bufs &B, u
     kp = nb.x, kn = nb.y;
 }
 
+/* ---------------------------------------------------------- windows */
+
+/* the part of the canvas a block covers: the canvas, or one tile (its
+   origin, size, layers and plane offsets) */
+struct ak_win {
+    uint32_t x0, y0, W, H, nl, first;
+    size_t   area, ckpt;
+};
+__device__ __forceinline__ ak_win ak_window(const ak_scene &S, uint32_t t) {
+    ak_win w;
+    if (!S.tiles) {
+        w.x0 = w.y0 = 0, w.W = S.W, w.H = S.H, w.nl = S.nlayers, w.first = 0, w.area = w.ckpt = 0;
+        return w;
+    }
+    const ak_tile_info ti = S.tinfo[t];
+    w.x0    = (t % S.ntx) * S.tiles;
+    w.y0    = (t / S.ntx) * S.tiles;
+    w.W     = min(S.tiles, S.CW - w.x0);
+    w.H     = min(S.tiles, S.CH - w.y0);
+    w.nl    = ti.count;
+    w.first = ti.first;
+    w.area  = (size_t)ti.area;
+    w.ckpt  = (size_t)ti.ckpt;
+    return w;
+}
+/* blocks of n pixels per window (the canvas, or a tile) */
+__host__ __device__ __forceinline__ uint32_t window_blocks(const ak_scene &S, uint32_t n) {
+    return (uint32_t)(((size_t)S.W * S.H + n - 1) / n);
+}
+/* the scene layer of window layer l */
+__device__ __forceinline__ uint32_t ak_layer(const ak_scene &S, const ak_win &w, uint32_t l) {
+    return S.layer_map ? S.layer_map[w.first + l] : l;
+}
+/* a coverage block's window and window layer: blockIdx.x is the layer, or
+   the (tile, layer) pair of a tiled scene */
+__device__ __forceinline__ ak_win ak_cover_window(const ak_scene &S, uint32_t &l) {
+    const uint32_t j = blockIdx.x;
+    if (!S.tiles) {
+        l = j;
+        return ak_window(S, 0);
+    }
+    const ak_win w = ak_window(S, S.pair_tile[j]);
+    l              = j - w.first;
+    return w;
+}
+
 /* ------------------------------------------------- band work compaction */
 
 /* one flattened point whose polygons reach the band: its neighbours and the
@@ -302,15 +348,15 @@ struct ak_slot {
 
 /* Phase 1 of a round: threads test the points [base, base + AK_THREADS) of
    the layer and append those reaching the band to the slot list. */
-__device__ __forceinline__ void gather_slots(const ak_scene &S, const ak_bufs &B, const ak_band &bd, bool stroke,
-                                             bool fwd, float h, uint32_t k, uint32_t p1, ak_slot *slots,
+__device__ __forceinline__ void gather_slots(const ak_scene &S, const ak_bufs &B, const ak_band &bd, float2 org,
+                                             bool stroke, bool fwd, float h, uint32_t k, uint32_t p1, ak_slot *slots,
                                              int *nslot) {
     if (k >= p1)
         return;
     uint32_t kp, kn;
     neighbours(S, B, k, kp, kn);
-    const float2 org = v2((float)S.x0, (float)S.y0); /* the window's origin: an integer, exact */
-    float2       P = B.pts[k] - org, Pn = B.pts[kn] - org;
+    /* org: the window's origin, an integer (exact in the subtraction) */
+    float2 P = B.pts[k] - org, Pn = B.pts[kn] - org;
     float2 O = v2(floorf(P.x), floorf(P.y));
     if (!fin2(O))
         O = v2(0.f, 0.f);
@@ -365,14 +411,19 @@ __global__ void __launch_bounds__(AK_THREADS) ak_cover(ak_scene S, ak_bufs B, co
     ak_slot *slots = reinterpret_cast<ak_slot *>(ak_smem);
     int     *acc   = reinterpret_cast<int *>(slots + AK_THREADS);
     __shared__ int nslot;
-    uint32_t l = blockIdx.x; /* grid: layers (x, up to 2^31) by bands (y) */
-    ak_band  bd{(int)(blockIdx.y * S.band), 0, (int)S.W, B.status};
-    bd.y1    = min((int)S.H, bd.y0 + (int)S.band);
-    int rows = bd.y1 - bd.y0, W1 = S.W + 1;
+    /* grid: layers or (tile, layer) pairs (x, up to 2^31) by bands (y) */
+    uint32_t     l;
+    const ak_win w = ak_cover_window(S, l);
+    if (blockIdx.y * S.band >= w.H)
+        return; /* a band below a tile at the canvas's bottom edge */
+    ak_band bd{(int)(blockIdx.y * S.band), 0, (int)w.W, B.status};
+    bd.y1    = min((int)w.H, bd.y0 + (int)S.band);
+    int rows = bd.y1 - bd.y0, W1 = w.W + 1;
     for (int i = threadIdx.x; i < rows * W1; i += AK_THREADS)
         acc[i] = 0;
+    const float2 org = v2((float)w.x0, (float)w.y0);
     if (B.off[S.nseg] <= B.cap) {
-        const uint32_t lg = S.layer_map ? S.layer_map[l] : l;
+        const uint32_t lg = ak_layer(S, w, l);
         uint32_t p = S.layer_path[lg];
         bool     stroke = S.layer_stroke[lg] != 0;
         int      E      = stroke ? 7 : 1;
@@ -382,7 +433,7 @@ __global__ void __launch_bounds__(AK_THREADS) ak_cover(ak_scene S, ak_bufs B, co
             if (threadIdx.x == 0)
                 nslot = 0;
             __syncthreads();
-            gather_slots(S, B, bd, stroke, true, h, base + threadIdx.x, p1, slots, &nslot);
+            gather_slots(S, B, bd, org, stroke, true, h, base + threadIdx.x, p1, slots, &nslot);
             __syncthreads();
             int ne = nslot * E;
             for (int t = threadIdx.x; t < ne; t += AK_THREADS) {
@@ -397,20 +448,20 @@ __global__ void __launch_bounds__(AK_THREADS) ak_cover(ak_scene S, ak_bufs B, co
     __syncthreads();
     /* row prefix sums, one warp per row, 32 cells per step */
     uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    float   *out  = B.area + ((size_t)l * S.H + bd.y0) * S.W;
+    float   *out  = B.area + w.area + ((size_t)l * w.H + bd.y0) * w.W;
     for (int r = warp; r < rows; r += AK_THREADS / 32) {
         int carry = 0;
-        for (uint32_t c = 0; c < S.W; c += 32) {
+        for (uint32_t c = 0; c < w.W; c += 32) {
             uint32_t i = c + lane;
-            int      x = i < S.W ? acc[r * W1 + i] : 0;
+            int      x = i < w.W ? acc[r * W1 + i] : 0;
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
                 int t = __shfl_up_sync(0xffffffffu, x, o);
                 if (lane >= (uint32_t)o)
                     x += t;
             }
-            if (i < S.W)
-                out[(size_t)r * S.W + i] = (float)(carry + x) * AK_FIX_INV;
+            if (i < w.W)
+                out[(size_t)r * w.W + i] = (float)(carry + x) * AK_FIX_INV;
             carry += __shfl_sync(0xffffffffu, x, 31);
         }
     }
@@ -442,29 +493,34 @@ __global__ void __launch_bounds__(AK_THREADS)
                  float *__restrict__ loss_part) {
     __shared__ float4 col[AK_CHUNK];
     __shared__ float  red[AK_THREADS / 32];
-    size_t            np = (size_t)S.W * S.H, px = (size_t)blockIdx.x * AK_THREADS + threadIdx.x;
-    bool              valid = px < np;
-    float4            C     = S.bg;
-    for (uint32_t lb = 0; lb < S.nlayers; lb += AK_CHUNK) {
-        uint32_t n = min((uint32_t)AK_CHUNK, S.nlayers - lb);
+    /* grid: the window's pixel blocks, window after window */
+    const uint32_t bpw = window_blocks(S, AK_THREADS), b = blockIdx.x % bpw;
+    const ak_win   w   = ak_window(S, blockIdx.x / bpw);
+    size_t         np = (size_t)w.W * w.H, px = (size_t)b * AK_THREADS + threadIdx.x;
+    bool           valid = px < np;
+    float4         C     = S.bg;
+    float4        *ckpt  = B.ckpt + w.ckpt;
+    const float   *area  = B.area + w.area;
+    for (uint32_t lb = 0; lb < w.nl; lb += AK_CHUNK) {
+        uint32_t n = min((uint32_t)AK_CHUNK, w.nl - lb);
         __syncthreads();
         if (threadIdx.x < n)
-            col[threadIdx.x] = colors[S.layer_path[S.layer_map ? S.layer_map[lb + threadIdx.x] : lb + threadIdx.x]];
+            col[threadIdx.x] = colors[S.layer_path[ak_layer(S, w, lb + threadIdx.x)]];
         __syncthreads();
         if (!valid)
             continue;
-        B.ckpt[(size_t)(lb / AK_CHUNK) * np + px] = C;
+        ckpt[(size_t)(lb / AK_CHUNK) * np + px] = C;
         float A[AK_CHUNK];
 #pragma unroll
         for (int q = 0; q < AK_CHUNK; q++)
-            A[q] = q < (int)n ? B.area[(size_t)(lb + q) * np + px] : 0.f;
+            A[q] = q < (int)n ? area[(size_t)(lb + q) * np + px] : 0.f;
 #pragma unroll
         for (int q = 0; q < AK_CHUNK; q++)
             if (q < (int)n)
                 C = blend(cover(A[q]), col[q], C);
     }
     float        s  = 0.f;
-    const size_t cp = valid ? ((size_t)S.y0 + px / S.W) * S.CW + S.x0 + px % S.W : 0; /* on the canvas */
+    const size_t cp = valid ? ((size_t)w.y0 + px / w.W) * S.CW + w.x0 + px % w.W : 0; /* on the canvas */
     if (valid) {
         B.canvas[cp] = C;
         if (target) {
@@ -519,11 +575,16 @@ __global__ void __launch_bounds__(AK_CB_THREADS)
     __shared__ float4 sB[AK_CHUNK][AK_CB_THREADS]; /* colour under each layer of the chunk */
     __shared__ float  sA[AK_CHUNK][AK_CB_THREADS]; /* the chunk's areas */
     __shared__ float  red[AK_CB_THREADS / 32][AK_CHUNK * 4];
-    size_t            np = (size_t)S.W * S.H, px = (size_t)blockIdx.x * AK_CB_THREADS + threadIdx.x;
-    bool              valid = px < np;
-    float4            g     = make_float4(0.f, 0.f, 0.f, 0.f);
+    /* grid: the window's pixel blocks, window after window */
+    const uint32_t bpw = window_blocks(S, AK_CB_THREADS), b = blockIdx.x % bpw;
+    const ak_win   w   = ak_window(S, blockIdx.x / bpw);
+    size_t         np = (size_t)w.W * w.H, px = (size_t)b * AK_CB_THREADS + threadIdx.x;
+    bool           valid = px < np;
+    float4         g     = make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4  *ckpt  = B.ckpt + w.ckpt;
+    float         *area  = B.area + w.area;
     if (valid) {
-        const size_t cp = ((size_t)S.y0 + px / S.W) * S.CW + S.x0 + px % S.W; /* on the canvas */
+        const size_t cp = ((size_t)w.y0 + px / w.W) * S.CW + w.x0 + px % w.W; /* on the canvas */
         if (d_canvas) {
             g = d_canvas[cp];
         } else {
@@ -533,16 +594,16 @@ __global__ void __launch_bounds__(AK_CB_THREADS)
         }
     }
     float    T    = 1.f; /* transmittance of the layers above */
-    uint32_t nch  = (S.nlayers + AK_CHUNK - 1) / AK_CHUNK;
+    uint32_t nch  = (w.nl + AK_CHUNK - 1) / AK_CHUNK;
     uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (uint32_t ch = nch; ch-- > 0;) {
-        uint32_t lb = ch * AK_CHUNK, n = min((uint32_t)AK_CHUNK, S.nlayers - lb);
+        uint32_t lb = ch * AK_CHUNK, n = min((uint32_t)AK_CHUNK, w.nl - lb);
         __syncthreads();
         if (threadIdx.x < n)
-            col[threadIdx.x] = colors[S.layer_path[S.layer_map ? S.layer_map[lb + threadIdx.x] : lb + threadIdx.x]];
+            col[threadIdx.x] = colors[S.layer_path[ak_layer(S, w, lb + threadIdx.x)]];
         __syncthreads();
-        float4       Bc = valid ? B.ckpt[(size_t)ch * np + px] : make_float4(0.f, 0.f, 0.f, 0.f);
-        const float *ap = B.area + (size_t)lb * np + px;
+        float4       Bc = valid ? ckpt[(size_t)ch * np + px] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float *ap = area + (size_t)lb * np + px;
         {
             float A[AK_CHUNK];
 #pragma unroll
@@ -574,7 +635,7 @@ __global__ void __launch_bounds__(AK_CB_THREADS)
                 float  da = T * (gc - c.w * gB);
                 float  gA = fabsf(Aq) < 1.f ? (Aq > 0.f ? da : Aq < 0.f ? -da : 0.f) : 0.f;
                 if (valid)
-                    B.area[(size_t)(lb + q) * np + px] = gA;
+                    area[(size_t)(lb + q) * np + px] = gA;
                 float ta = T * al;
                 dc[4 * q8] = ta * g.x, dc[4 * q8 + 1] = ta * g.y, dc[4 * q8 + 2] = ta * g.z;
                 dc[4 * q8 + 3] = ta * (g.w - gB);
@@ -585,9 +646,13 @@ __global__ void __launch_bounds__(AK_CB_THREADS)
         __syncthreads();
         if (threadIdx.x < n * 4) {
             float s = 0.f;
-            for (int w = 0; w < AK_CB_THREADS / 32; w++)
-                s += red[w][threadIdx.x];
-            color_part[((size_t)blockIdx.x * S.nlayers + lb) * 4 + threadIdx.x] = s;
+            for (int k = 0; k < AK_CB_THREADS / 32; k++)
+                s += red[k][threadIdx.x];
+            /* one window: [block][layer][channel]; tiled: [pair][block of the tile][channel] */
+            const uint32_t q = threadIdx.x >> 2, c = threadIdx.x & 3;
+            const size_t   i = S.tiles ? ((size_t)(w.first + lb + q) * bpw + b) * 4 + c
+                                       : ((size_t)b * S.nlayers + lb) * 4 + threadIdx.x;
+            color_part[i] = s;
         }
     }
 }
@@ -608,16 +673,20 @@ __global__ void __launch_bounds__(AK_THREADS)
     float   *gs    = reinterpret_cast<float *>(eg + AK_THREADS * 7);
     __shared__ float red[AK_THREADS / 32];
     __shared__ int   nslot;
-    uint32_t         l = blockIdx.x;
-    ak_band          bd{(int)(blockIdx.y * S.band), 0, (int)S.W, B.status};
-    bd.y1             = min((int)S.H, bd.y0 + (int)S.band);
+    uint32_t         l;
+    const ak_win     w = ak_cover_window(S, l);
+    if (blockIdx.y * S.band >= w.H)
+        return; /* a band below a tile at the canvas's bottom edge */
+    ak_band bd{(int)(blockIdx.y * S.band), 0, (int)w.W, B.status};
+    bd.y1             = min((int)w.H, bd.y0 + (int)S.band);
     int          rows = bd.y1 - bd.y0;
-    const float *src  = B.area + ((size_t)l * S.H + bd.y0) * S.W;
-    for (int i = threadIdx.x; i < rows * (int)S.W; i += AK_THREADS)
+    const float *src  = B.area + w.area + ((size_t)l * w.H + bd.y0) * w.W;
+    for (int i = threadIdx.x; i < rows * (int)w.W; i += AK_THREADS)
         gs[i] = src[i];
     if (B.off[S.nseg] > B.cap)
         return;
-    const uint32_t lg = S.layer_map ? S.layer_map[l] : l;
+    const float2   org = v2((float)w.x0, (float)w.y0);
+    const uint32_t lg  = ak_layer(S, w, l);
     uint32_t p      = S.layer_path[lg];
     bool     stroke = S.layer_stroke[lg] != 0;
     int      E      = stroke ? 7 : 1;
@@ -627,7 +696,7 @@ __global__ void __launch_bounds__(AK_THREADS)
         if (threadIdx.x == 0)
             nslot = 0;
         __syncthreads();
-        gather_slots(S, B, bd, stroke, false, h, base + threadIdx.x, p1, slots, &nslot);
+        gather_slots(S, B, bd, org, stroke, false, h, base + threadIdx.x, p1, slots, &nslot);
         __syncthreads();
         int ns = nslot, ne = ns * E;
         for (int t = threadIdx.x; t < ne; t += AK_THREADS) {
@@ -701,21 +770,24 @@ __global__ void ak_reduce_colors(ak_scene S, uint32_t nblocks, const float *__re
     if (t >= S.nlayers * 4)
         return;
     float s = 0.f;
-    for (uint32_t b = 0; b < nblocks; b++)
-        s += part[(size_t)b * S.nlayers * 4 + t];
+    if (S.tiles) /* t: (pair, channel); the pair's partials are contiguous */
+        for (uint32_t b = 0; b < nblocks; b++)
+            s += part[((size_t)(t >> 2) * nblocks + b) * 4 + (t & 3)];
+    else
+        for (uint32_t b = 0; b < nblocks; b++)
+            s += part[(size_t)b * S.nlayers * 4 + t];
     const uint32_t l = t >> 2;
     atomicAdd(&d_colors[S.layer_path[S.layer_map ? S.layer_map[l] : l] * 4 + (t & 3)], s);
 }
 
-__global__ void ak_reduce_loss(uint32_t nblocks, float scale, const float *__restrict__ part, float *__restrict__ loss,
-                               bool accumulate) {
+__global__ void ak_reduce_loss(uint32_t nblocks, float scale, const float *__restrict__ part, float *__restrict__ loss) {
     __shared__ float red[AK_THREADS / 32];
     float            s = 0.f;
     for (uint32_t b = threadIdx.x; b < nblocks; b += AK_THREADS)
         s += part[b];
     s = block_sum<AK_THREADS>(s, red);
     if (threadIdx.x == 0)
-        *loss = accumulate ? *loss + s * scale : s * scale;
+        *loss = s * scale;
 }
 
 /* ------------------------------------------------------------- tiling */
@@ -776,10 +848,13 @@ __global__ void ak_tile_flags(uint32_t nlayers, uint64_t n, uint32_t ntx, const 
 }
 
 __global__ void ak_tile_lists(uint64_t n, uint32_t nlayers, const uint32_t *__restrict__ flags,
-                              const uint32_t *__restrict__ pos, uint32_t *__restrict__ list) {
+                              const uint32_t *__restrict__ pos, uint32_t *__restrict__ list,
+                              uint32_t *__restrict__ tile) {
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n && flags[i])
+    if (i < n && flags[i]) {
         list[pos[i]] = (uint32_t)(i % nlayers);
+        tile[pos[i]] = (uint32_t)(i / nlayers);
+    }
 }
 
 __global__ void ak_adam(float *__restrict__ p, const float *__restrict__ g, float *__restrict__ m,
@@ -820,18 +895,21 @@ cudaError_t ak_launch_cover(cudaStream_t st, const ak_scene &S, const ak_bufs &B
         ak_cover<<<dim3(S.nlayers, S.nbands), AK_THREADS, smem, st>>>(S, B, widths);
     return cudaGetLastError();
 }
+static uint32_t windows(const ak_scene &S) { return S.tiles ? S.ntiles : 1u; }
+uint32_t ak_pixel_blocks_all(const ak_scene &S) { return ak_pixel_blocks(S) * windows(S); }
 cudaError_t ak_launch_composite(cudaStream_t st, const ak_scene &S, const ak_bufs &B, const float4 *colors,
                                 const float4 *target, float *loss_part) {
-    ak_composite<<<ak_pixel_blocks(S), AK_THREADS, 0, st>>>(S, B, colors, target, loss_part);
+    ak_composite<<<ak_pixel_blocks_all(S), AK_THREADS, 0, st>>>(S, B, colors, target, loss_part);
     return cudaGetLastError();
 }
 uint32_t ak_composite_bwd_blocks(const ak_scene &S) {
     return (uint32_t)(((size_t)S.W * S.H + AK_CB_THREADS - 1) / AK_CB_THREADS);
 }
+size_t ak_color_partials(const ak_scene &S) { return (size_t)ak_composite_bwd_blocks(S) * S.nlayers; }
 cudaError_t ak_launch_composite_bwd(cudaStream_t st, const ak_scene &S, const ak_bufs &B, const float4 *colors,
                                     const float4 *target, const float4 *d_canvas, float4 *color_part) {
-    ak_composite_bwd<<<ak_composite_bwd_blocks(S), AK_CB_THREADS, 0, st>>>(S, B, colors, target, d_canvas,
-                                                                           reinterpret_cast<float *>(color_part));
+    ak_composite_bwd<<<ak_composite_bwd_blocks(S) * windows(S), AK_CB_THREADS, 0, st>>>(
+        S, B, colors, target, d_canvas, reinterpret_cast<float *>(color_part));
     return cudaGetLastError();
 }
 cudaError_t ak_launch_cover_bwd(cudaStream_t st, const ak_scene &S, const ak_bufs &B, const float *widths,
@@ -844,13 +922,12 @@ cudaError_t ak_launch_cover_bwd(cudaStream_t st, const ak_scene &S, const ak_buf
     return cudaGetLastError();
 }
 cudaError_t ak_launch_reduce(cudaStream_t st, const ak_scene &S, uint32_t nblocks, const float4 *color_part,
-                             float4 *d_colors, const float *loss_part, float *loss, bool accumulate) {
+                             float4 *d_colors, const float *loss_part, float *loss) {
     if (color_part && S.nlayers)
         ak_reduce_colors<<<(S.nlayers * 4 + 255) / 256, 256, 0, st>>>(
             S, nblocks, reinterpret_cast<const float *>(color_part), reinterpret_cast<float *>(d_colors));
     if (loss_part)
-        ak_reduce_loss<<<1, AK_THREADS, 0, st>>>(nblocks, 1.f / (float)((size_t)S.CW * S.CH * 4), loss_part, loss,
-                                                 accumulate);
+        ak_reduce_loss<<<1, AK_THREADS, 0, st>>>(nblocks, 1.f / (float)((size_t)S.CW * S.CH * 4), loss_part, loss);
     return cudaGetLastError();
 }
 cudaError_t ak_launch_layer_boxes(cudaStream_t st, const ak_scene &S, const ak_bufs &B, const float *widths,
@@ -867,9 +944,9 @@ cudaError_t ak_launch_tile_flags(cudaStream_t st, uint32_t nlayers, uint32_t nti
     return cudaGetLastError();
 }
 cudaError_t ak_launch_tile_lists(cudaStream_t st, uint64_t n, uint32_t nlayers, const uint32_t *flags,
-                                 const uint32_t *pos, uint32_t *list) {
+                                 const uint32_t *pos, uint32_t *list, uint32_t *tile) {
     if (n)
-        ak_tile_lists<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, nlayers, flags, pos, list);
+        ak_tile_lists<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, nlayers, flags, pos, list, tile);
     return cudaGetLastError();
 }
 cudaError_t ak_launch_adam(cudaStream_t st, float *param, const float *grad, float *m, float *v, uint32_t n, float lr,

@@ -20,15 +20,27 @@
 #define AK_BAND_WIDE_MAX 1024
 #define AK_CHUNK 16 /* layers per compositing checkpoint */
 
+/* a tile of a tiled scene: its first (tile, layer) pair, the number of its
+   layers, and the offsets (in elements) of its area planes and checkpoints */
+struct ak_tile_info {
+    uint32_t           first, count;
+    unsigned long long area, ckpt;
+};
+
 struct ak_scene {
     uint32_t        W, H, npaths, ncontours, nseg, ncp, nlayers, nbands, band;
     float4          bg;
-    /* the window of the canvas the kernels cover: W x H pixels from
-       (x0, y0) of a CW x CH canvas (the whole canvas, or one tile of a tiled
-       scene); nlayers are the window's layers, layer_map[i] the scene layer of
-       window layer i (null: the identity) */
-    uint32_t        x0, y0, CW, CH;
-    const uint32_t *layer_map;
+    /* CW x CH: the canvas.  One window (tiles == 0): the kernels cover the
+       canvas, W x H = CW x CH, over its nlayers layers.  Tiled (tiles: the
+       tile side): every launch covers all tiles at once; W = H = tiles, nbands
+       the bands of a tile, nlayers the number of (tile, layer) pairs (tile
+       by tile, each tile's layers in scene order), layer_map[j] the scene
+       layer of pair j, pair_tile[j] its tile, tinfo[t] tile t's pairs and
+       planes, ntx the tiles across, ntiles the tiles in all */
+    uint32_t            CW, CH, tiles, ntx, ntiles;
+    const uint32_t     *layer_map;
+    const uint32_t     *pair_tile;
+    const ak_tile_info *tinfo;
     const uint8_t  *seg_kind;     /* nseg */
     const uint32_t *seg_cp;       /* nseg: first control point */
     const uint32_t *seg_end;      /* nseg: control point the segment ends at */
@@ -67,7 +79,7 @@ cudaError_t ak_launch_composite_bwd(cudaStream_t st, const ak_scene &S, const ak
 cudaError_t ak_launch_cover_bwd(cudaStream_t st, const ak_scene &S, const ak_bufs &B, const float *widths,
                                 float2 *gpts, float *gwidth);
 cudaError_t ak_launch_reduce(cudaStream_t st, const ak_scene &S, uint32_t nblocks, const float4 *color_part,
-                             float4 *d_colors, const float *loss_part, float *loss, bool accumulate = false);
+                             float4 *d_colors, const float *loss_part, float *loss);
 /* tiled scenes: per scene layer its box in tiles (x0, y0, x1, y1 inclusive;
    x0 > x1 when empty), from its flattened points (strokes widened by half
    their width plus a pixel) */
@@ -76,10 +88,15 @@ cudaError_t ak_launch_layer_boxes(cudaStream_t st, const ak_scene &S, const ak_b
 /* flags[t * nlayers + l] = 1 when layer l's box holds tile t */
 cudaError_t ak_launch_tile_flags(cudaStream_t st, uint32_t nlayers, uint32_t ntiles, uint32_t ntx, const int4 *box,
                                  uint32_t *flags);
-/* list[pos[i]] = i % nlayers where flags[i] (pos: exclusive scan of the flags) */
+/* list[pos[i]] = i % nlayers and tile[pos[i]] = i / nlayers where flags[i]
+   (pos: exclusive scan of the flags) */
 cudaError_t ak_launch_tile_lists(cudaStream_t st, uint64_t n, uint32_t nlayers, const uint32_t *flags,
-                                 const uint32_t *pos, uint32_t *list);
+                                 const uint32_t *pos, uint32_t *list, uint32_t *tile);
 cudaError_t ak_launch_adam(cudaStream_t st, float *param, const float *grad, float *m, float *v, uint32_t n, float lr,
                            float beta1, float beta2, float eps, uint32_t step, float lo, float hi);
+/* pixel blocks of ak_composite (loss partials) and of ak_composite_bwd per
+   window (the canvas, or one tile), and in all */
 uint32_t    ak_pixel_blocks(const ak_scene &S);
-uint32_t    ak_composite_bwd_blocks(const ak_scene &S); /* blocks of ak_composite_bwd's colour partials */
+uint32_t    ak_composite_bwd_blocks(const ak_scene &S);
+uint32_t    ak_pixel_blocks_all(const ak_scene &S);
+size_t      ak_color_partials(const ak_scene &S); /* float4 colour partials of ak_composite_bwd */
