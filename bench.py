@@ -240,6 +240,10 @@ def analytic_glyph_bench(a, gb, torch, np, flush, tile=128):
         A.backward(grads=grads)
 
     fb_ms = timed(fb)
+    A.set_timing(True)
+    fb()
+    phases = [float(x) for x in A.timing()]
+    A.set_timing(False)
     assert A.sync() == 0
     loss = float(A.loss.item())
     gP, gQ = scenes.elevate_adjoint(quad, grads[0].cpu().numpy())
@@ -247,6 +251,8 @@ def analytic_glyph_bench(a, gb, torch, np, flush, tile=128):
                        "(fill), 20000 closed strokes, %d cubic segments after elevation, tiles of %d px" %
                        (len(scene["seg_kind"]), tile),
            "fwd_ms": fwd_ms, "fwd_bwd_ms": fb_ms, "fwd_bwd_over_fwd": fb_ms / fwd_ms, "loss": loss,
+           "phase_ms": {"flatten_and_tiles": phases[0], "cover": phases[1], "composite": phases[2],
+                        "composite_adjoint": phases[3], "cover_adjoint": phases[4], "flatten_adjoint": phases[5]},
            "layers": int(A.nlayers), "device_bytes": int(free0 - free1), "scene_build_s": gen_s,
            "outline_grad_norm": {"on_curve": float(np.linalg.norm(gP)), "off_curve": float(np.linalg.norm(gQ))},
            "timing": "CUDA events on the scene's stream, L2 flushed before each, median of 3",

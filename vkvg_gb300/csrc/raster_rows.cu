@@ -60,9 +60,12 @@ enum { M_ABORT, M_IEND, M_DLO, M_DHI, M_TILES, M_DENSE, M_I0 };
 
 /* A row-form configuration: ROWS consumer warps (sample rows per CTA, 16 or
    8: a CTA then covers a half band), the ring's depth and slot capacity,
-   and 32- or 16-bit crossing counters.  16-bit counters hold a position's
-   net crossings exactly while the draw's cell has fewer than 2^15 records
-   (the host checks the heaviest cell). */
+   and 32- or 16-bit crossing counters.  16-bit counters are kept biased by
+   2^15 (an empty counter holds 0x8000), two to a word, so that a word-wide
+   atomic add of +-1 or +-2^16 never carries between the halves and each
+   half reads back with one 16-bit load; they hold a position's net crossings
+   exactly while the draw's cell has fewer than 2^15 records (the host checks
+   the heaviest cell). */
 template <int ROWS_, int NSLOT_, int CAP_, bool C16_> struct RWT {
     static constexpr int  ROWS    = ROWS_;
     static constexpr int  NSLOT   = NSLOT_;
@@ -199,8 +202,11 @@ __device__ __forceinline__ bool rows_item(const gb_raster_args &A, int32_t *smem
         }
         *reinterpret_cast<uint4 *>(smem + S_SMP + r * TW + c4) = v;
     }
-    for (uint32_t i = t; i < (uint32_t)(ROWS * CW + ROWS * 32) / 4; i += THREADS)
-        reinterpret_cast<int4 *>(smem + S_CNT)[i] = make_int4(0, 0, 0, 0);
+    constexpr int32_t CZERO = T::C16 ? (int32_t)0x80008000u : 0; /* an empty counter word */
+    for (uint32_t i = t; i < (uint32_t)(ROWS * CW) / 4; i += THREADS)
+        reinterpret_cast<int4 *>(smem + S_CNT)[i] = make_int4(CZERO, CZERO, CZERO, CZERO);
+    for (uint32_t i = t; i < (uint32_t)(ROWS * 32) / 4; i += THREADS)
+        reinterpret_cast<int4 *>(smem + S_OCC)[i] = make_int4(0, 0, 0, 0);
     const uint32_t gc_gs = GRAD && A.S == 4 && !dbg ? A.gc_src : 0u;
     if (gc_gs) {
         for (uint32_t i = t; i < (uint32_t)(T::GCR * TW); i += THREADS) {
@@ -330,8 +336,8 @@ __device__ __forceinline__ bool rows_item(const gb_raster_args &A, int32_t *smem
         uint32_t      *smp    = reinterpret_cast<uint32_t *>(smem + S_SMP + rr * TW);
         int32_t       *cnt    = smem + S_CNT + rr * CW;
         uint32_t      *occ    = reinterpret_cast<uint32_t *>(smem + S_OCC + rr * 32);
-        /* the crossing counters of position p (16-bit ones two to a word:
-           the word is lo + 65536 hi with both halves signed) */
+        /* the crossing counter of position p (16-bit ones: half p & 1 of
+           word p >> 1, biased by 2^15) */
         auto cadd = [&](uint32_t p, int32_t dir) {
             if (T::C16)
                 atomicAdd(&cnt[p >> 1], (int32_t)((uint32_t)dir << (16u * (p & 1u))));
@@ -341,15 +347,14 @@ __device__ __forceinline__ bool rows_item(const gb_raster_args &A, int32_t *smem
         auto cget = [&](uint32_t p) -> int32_t {
             if (!T::C16)
                 return cnt[p];
-            const int32_t w = cnt[p >> 1], lo = (int16_t)(w & 0xFFFF);
-            return (p & 1u) ? (int32_t)((uint32_t)w - (uint32_t)lo) >> 16 : lo;
+            return (int32_t)reinterpret_cast<const uint16_t *>(cnt)[p] - 32768;
         };
-        /* lane l's run of counters back to zero (16-byte stores) */
+        /* lane l's run of counters back to empty (16-byte stores) */
         auto cclear = [&]() {
             int4 *q = reinterpret_cast<int4 *>(cnt + (T::C16 ? 16u : 32u) * l);
 #pragma unroll
             for (int i = 0; i < (T::C16 ? 4 : 8); i++)
-                q[i] = make_int4(0, 0, 0, 0);
+                q[i] = make_int4(CZERO, CZERO, CZERO, CZERO);
         };
         /* this lane's run of the row [32 l, 32 l + 32): the samples inside the tile */
         const int32_t  nrun  = TWr - 32 * (int32_t)l;
@@ -505,34 +510,41 @@ __device__ __forceinline__ bool rows_item(const gb_raster_args &A, int32_t *smem
             /* walk the occupied positions left to right (the winding left of
                position p includes its count): non-zero fills cover w != 0;
                strokes blend once per covering triangle, so pass k covers
-               w > k, the first four passes' masks in this walk */
+               w > k, the first two passes' masks in this walk */
             const bool stroke = kind == GB_DRAW_STROKE;
-            uint32_t   c1 = 0, c2 = 0, c3 = 0, c4 = 0, start = 0;
+            uint32_t   c1 = 0, c2 = 0, start = 0;
             int32_t    w = incl, kmax = 0;
-            for (uint32_t b = m; b; b &= b - 1) {
-                const uint32_t p = __ffs(b) - 1;
-                const uint32_t r = bit_range(start, p);
-                c1 |= (stroke ? w > 0 : w != 0) ? r : 0u;
-                c2 |= w > 1 ? r : 0u;
-                c3 |= w > 2 ? r : 0u;
-                c4 |= w > 3 ? r : 0u;
-                kmax = max(kmax, w);
-                w -= cget((l << 5) + p);
-                start = p + 1;
-            }
-            if (start < 32) {
-                const uint32_t r = bit_range(start, 31);
-                c1 |= (stroke ? w > 0 : w != 0) ? r : 0u;
-                c2 |= w > 1 ? r : 0u;
-                c3 |= w > 2 ? r : 0u;
-                c4 |= w > 3 ? r : 0u;
-                kmax = max(kmax, w);
+            if (!stroke) {
+                for (uint32_t b = m; b; b &= b - 1) {
+                    const uint32_t p = __ffs(b) - 1;
+                    c1 |= w != 0 ? bit_range(start, p) : 0u;
+                    w -= cget((l << 5) + p);
+                    start = p + 1;
+                }
+                if (start < 32 && w != 0)
+                    c1 |= bit_range(start, 31);
+            } else {
+                for (uint32_t b = m; b; b &= b - 1) {
+                    const uint32_t p = __ffs(b) - 1;
+                    const uint32_t r = bit_range(start, p);
+                    c1 |= w > 0 ? r : 0u;
+                    c2 |= w > 1 ? r : 0u;
+                    kmax = max(kmax, w);
+                    w -= cget((l << 5) + p);
+                    start = p + 1;
+                }
+                if (start < 32) {
+                    const uint32_t r = bit_range(start, 31);
+                    c1 |= w > 0 ? r : 0u;
+                    c2 |= w > 1 ? r : 0u;
+                    kmax = max(kmax, w);
+                }
             }
             if (!dbg) {
                 const int32_t kw = stroke ? __reduce_max_sync(0xFFFFFFFFu, kmax) : 1;
                 for (int32_t rep = 0; rep < kw; rep++) {
-                    uint32_t cv = rep == 0 ? c1 : rep == 1 ? c2 : rep == 2 ? c3 : c4;
-                    if (rep >= 4) { /* five or more covering triangles: walk again */
+                    uint32_t cv = rep == 0 ? c1 : c2;
+                    if (rep >= 2) { /* three or more covering triangles: walk again */
                         int32_t  ww = incl;
                         uint32_t st = 0;
                         cv          = 0;
