@@ -479,6 +479,27 @@ def test_gpu_tiled_matches_whole_canvas(gb, tile):
 
 
 @pytest.mark.gpu
+def test_gpu_small_curves_flatten_bit_exact(gb):
+    """scenes of small curves (the glyph construction: a few points per
+    segment) flatten one lane per segment: the points, their order and the
+    segment offsets equal the reference's flattening bit for bit, tiled or
+    not"""
+    scene, par, _ = scenes.analytic_glyph_scene(n_outlines=300, n_strokes=30, size=160)
+    f32, _, seg = ar.Reference(scene).flatten(par["ctrl"])
+    assert len(f32) <= 8 * len(scene["seg_kind"])  # the lane-per-segment case
+    for tile in (0, 64):
+        A = gb.Analytic(scene, tile=tile)
+        p = {k: _dev(v) for k, v in par.items()}
+        A.forward(p["ctrl"], p["colors"], p["widths"])
+        A.forward(p["ctrl"], p["colors"], p["widths"])  # the second forward runs in the chosen mode
+        assert A.sync() == 0
+        pts, off = A.points()
+        assert np.array_equal(off, seg)
+        assert np.array_equal(pts.view(np.uint32), f32.view(np.uint32))
+        A.destroy()
+
+
+@pytest.mark.gpu
 def test_gpu_tiled_glyph_crop_matches_fp64(gb):
     """the large glyph configuration's analytic construction on a 192 x 192
     crop at its density (440 quadratic outlines with holes, 44 closed

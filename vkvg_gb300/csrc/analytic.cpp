@@ -12,16 +12,17 @@
  * only the first forward waits for it, to size the point buffer.
  *
  * A tiled scene (create_tiled) keeps the same kernels and runs each of them
- * once over every square tile of the canvas: after the flattening, every
- * layer's box in tiles (from its points, strokes widened by half their
- * width), a flag per (tile, layer), one exclusive scan of the flags and a
- * compaction give the (tile, layer) pairs, tile by tile in scene order; the
- * per-tile counts are read back (the one synchronisation of a tiled
- * forward) to place every tile's area planes and checkpoints in one
- * buffer, all kept resident for the backward.  A coverage block takes its
- * pair's tile and plane from the pair index, a compositing block its tile
- * from its block index.  A layer is zero outside its box, so a tile's
- * composite over its own layers equals the whole canvas's there.
+ * once over every square tile of the canvas.  After the flattening, every
+ * layer's box in pixels (from its points, strokes widened by half their
+ * width; a layer's area is exactly zero outside it), a flag per (tile,
+ * layer), one exclusive scan of the flags and a compaction give the (tile,
+ * layer) pairs, tile by tile in scene order, each with the layer's box inside
+ * the tile; a pair's area plane covers only that box (planes placed by a
+ * scan of their sizes).  The per-tile counts and the box total are read back
+ * (the one synchronisation of a tiled forward) to size the planes and every
+ * tile's checkpoints, all kept resident for the backward.  A coverage block
+ * covers its pair's box; a compositing thread one pixel of a tile, reading a
+ * layer's plane where the pixel lies in its box and zero elsewhere.
  */
 #include "analytic.h"
 #include "host.h"
@@ -58,11 +59,11 @@ struct _vkvg_gb300_analytic_t {
        offsets (pinned, then on the device), and the scene the tiled launches
        take (TS: every tile at once) */
     uint32_t  tile = 0, ntx = 1, nty = 1;
-    DevBuf    d_box, d_flags, d_fpos, d_fscan, d_list, d_ptile, d_tinfo;
+    DevBuf    d_box, d_tot, d_flags, d_fpos, d_fscan, d_list, d_ptile, d_pbox, d_psize, d_poff, d_pscan, d_tinfo;
     PinnedBuf h_tiles, h_tinfo;
     ak_scene  TS{};
     /* the last forward */
-    bool         have_fwd = false, sized = false;
+    bool         have_fwd = false, sized = false, lane_flat = false;
     const float *f_ctrl = nullptr, *f_colors = nullptr, *f_widths = nullptr, *f_target = nullptr;
 };
 
@@ -201,7 +202,7 @@ VkvgAnalytic create_scene(uint32_t width, uint32_t height, uint32_t tile, const 
              a->d_ckpt.grow(sizeof(float4) * np * std::max<size_t>(nchk, 1)) && a->d_loss_part.grow(sizeof(float) * nbk) &&
              a->d_color_part.grow(sizeof(float4) * (size_t)(np + 127) / 128 * std::max<uint32_t>(a->nlayers, 1));
     else
-        ok = ok && a->d_box.grow(sizeof(int4) * std::max<uint32_t>(a->nlayers, 1));
+        ok = ok && a->d_box.grow(sizeof(int4) * std::max<uint32_t>(a->nlayers, 1)) && a->d_tot.grow(8);
     ok = ok && cudaMemset(a->d_status.p, 0, 4) == cudaSuccess;
     if (!ok) {
         vkvg_gb300_analytic_destroy(a);
@@ -254,7 +255,8 @@ void vkvg_gb300_analytic_destroy(VkvgAnalytic a) {
                     &a->d_path_s0,  &a->d_layer_path, &a->d_layer_stroke, &a->d_cnt, &a->d_off, &a->d_scan,
                     &a->d_pts, &a->d_pt_nb, &a->d_area, &a->d_ckpt, &a->d_canvas, &a->d_loss_part, &a->d_loss,
                     &a->d_color_part, &a->d_gpts, &a->d_status, &a->d_box, &a->d_flags, &a->d_fpos, &a->d_fscan,
-                    &a->d_list, &a->d_ptile, &a->d_tinfo};
+                    &a->d_list, &a->d_ptile, &a->d_tinfo, &a->d_tot, &a->d_pbox, &a->d_psize, &a->d_poff,
+                    &a->d_pscan};
     for (DevBuf *b : bs)
         b->release();
     a->h_mon.release();
@@ -288,9 +290,10 @@ vkvg_status_t vkvg_gb300_analytic_set_stream(VkvgAnalytic a, void *stream) {
 } /* extern "C" */
 
 namespace {
-/* tiled scenes: the (tile, layer) pairs, every tile's pairs and planes, the
-   buffers sized for them and the scene of the tiled launches (after the
-   flattening of this forward) */
+/* tiled scenes: the (tile, layer) pairs with each layer's box inside each
+   tile, their area planes (one per pair, covering only its box), every
+   tile's pairs and checkpoints, the buffers sized for them and the scene of
+   the tiled launches (after the flattening of this forward) */
 cudaError_t tile_setup(VkvgAnalytic a, const float *widths) {
     cudaStream_t   st = a->stream;
     const uint32_t nt = a->ntx * a->nty, nl = a->nlayers;
@@ -298,43 +301,56 @@ cudaError_t tile_setup(VkvgAnalytic a, const float *widths) {
     if (n >= 0xFFFFFFFFull)
         return cudaErrorMemoryAllocation; /* positions are 32-bit */
     if (!a->d_flags.grow(4 * std::max<uint64_t>(n, 1)) || !a->d_fpos.grow(4 * (n + 1)) ||
-        !a->d_fscan.grow(4 * gb_scan_scratch_words((uint32_t)n) + 64) || !a->h_tiles.grow(4 * ((size_t)nt + 2)) ||
+        !a->d_fscan.grow(4 * gb_scan_scratch_words((uint32_t)n) + 64) || !a->h_tiles.grow(4 * ((size_t)nt + 4)) ||
         !a->h_tinfo.grow(sizeof(ak_tile_info) * nt) || !a->d_tinfo.grow(sizeof(ak_tile_info) * nt))
         return cudaErrorMemoryAllocation;
     ak_bufs     B = bufs(a);
-    cudaError_t e = ak_launch_layer_boxes(st, a->S, B, widths, a->tile, a->ntx, a->nty, a->d_box.as<int4>());
+    cudaError_t e = cudaMemsetAsync(a->d_tot.p, 0, 8, st);
     if (e == cudaSuccess)
-        e = ak_launch_tile_flags(st, nl, nt, a->ntx, a->d_box.as<int4>(), a->d_flags.as<uint32_t>());
+        e = ak_launch_layer_boxes(st, a->S, B, widths, a->d_box.as<int4>(), a->d_tot.as<unsigned long long>());
+    if (e == cudaSuccess)
+        e = ak_launch_tile_flags(st, nl, nt, a->ntx, a->tile, a->d_box.as<int4>(), a->d_flags.as<uint32_t>());
     if (e == cudaSuccess)
         e = gb_exclusive_scan_flags(st, a->d_flags.as<uint32_t>(), (uint32_t)n, a->d_fpos.as<uint32_t>(),
                                     a->d_fscan.as<uint32_t>());
     uint32_t *h = (uint32_t *)a->h_tiles.p;
-    if (e == cudaSuccess) /* the position of every tile's first (tile, layer) entry, and the total */
+    if (e == cudaSuccess) /* the position of every tile's first pair, the pair total, the box pixel total */
         e = cudaMemcpy2DAsync(h, 4, a->d_fpos.p, (size_t)nl * 4, 4, nt, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(h + nt, a->d_fpos.as<uint32_t>() + n, 4, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(h + nt + 2, a->d_tot.p, 8, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess)
         e = cudaStreamSynchronize(st);
     gb_count_launch(5);
     if (e != cudaSuccess)
         return e;
-    const uint32_t total = h[nt];
-    if (!a->d_list.grow(4 * (size_t)std::max<uint32_t>(total, 1)) ||
-        !a->d_ptile.grow(4 * (size_t)std::max<uint32_t>(total, 1)))
+    const uint32_t     total = h[nt];
+    unsigned long long area;
+    memcpy(&area, h + nt + 2, sizeof area);
+    if (area >= 0xFFFFFFFFull) /* plane offsets are 32-bit element counts */
         return cudaErrorMemoryAllocation;
-    e = ak_launch_tile_lists(st, n, nl, a->d_flags.as<uint32_t>(), a->d_fpos.as<uint32_t>(), a->d_list.as<uint32_t>(),
-                             a->d_ptile.as<uint32_t>());
-    gb_count_launch(1);
-    /* every tile's planes: a tile of tw x th pixels and c layers holds c
-       area planes and ceil(c / AK_CHUNK) checkpoint planes of tw x th */
+    const size_t np1 = (size_t)std::max<uint32_t>(total, 1);
+    if (!a->d_list.grow(4 * np1) || !a->d_ptile.grow(4 * np1) || !a->d_pbox.grow(8 * np1) ||
+        !a->d_psize.grow(4 * np1) || !a->d_poff.grow(4 * (np1 + 1)) ||
+        !a->d_pscan.grow(4 * gb_scan_scratch_words(total) + 64))
+        return cudaErrorMemoryAllocation;
+    e = ak_launch_tile_lists(st, n, nl, a->ntx, a->tile, a->d_box.as<int4>(), a->d_flags.as<uint32_t>(),
+                             a->d_fpos.as<uint32_t>(), a->d_list.as<uint32_t>(), a->d_ptile.as<uint32_t>(),
+                             a->d_pbox.as<uint2>(), a->d_psize.as<uint32_t>());
+    if (e == cudaSuccess) /* every pair's plane: the running sum of the box sizes */
+        e = gb_exclusive_scan(st, a->d_psize.as<uint32_t>(), total, a->d_poff.as<uint32_t>(),
+                              a->d_pscan.as<uint32_t>());
+    gb_count_launch(4);
+    /* every tile's checkpoints: a tile of tw x th pixels and c layers holds
+       ceil(c / AK_CHUNK) planes of tw x th */
     ak_tile_info *ti   = (ak_tile_info *)a->h_tinfo.p;
-    size_t        area = 0, ckpt = 0;
+    size_t        ckpt = 0;
     for (uint32_t t = 0; t < nt; t++) {
         const uint32_t tw = std::min(a->tile, a->W - (t % a->ntx) * a->tile);
         const uint32_t th = std::min(a->tile, a->H - (t / a->ntx) * a->tile);
         const size_t   px = (size_t)tw * th, cnt = (t + 1 < nt ? h[t + 1] : total) - h[t];
-        ti[t].first = h[t], ti[t].count = (uint32_t)cnt, ti[t].area = area, ti[t].ckpt = ckpt;
-        area += px * cnt;
+        ti[t].first = h[t], ti[t].count = (uint32_t)cnt, ti[t].ckpt = ckpt;
         ckpt += px * ((cnt + AK_CHUNK - 1) / AK_CHUNK);
     }
     ak_scene &T = a->TS;
@@ -346,6 +362,8 @@ cudaError_t tile_setup(VkvgAnalytic a, const float *widths) {
     T.nlayers    = total;
     T.layer_map  = a->d_list.as<uint32_t>();
     T.pair_tile  = a->d_ptile.as<uint32_t>();
+    T.pair_box   = a->d_pbox.as<uint2>();
+    T.pair_off   = a->d_poff.as<uint32_t>();
     T.tinfo      = a->d_tinfo.as<ak_tile_info>();
     if (!a->d_area.grow(sizeof(float) * std::max<size_t>(area, 1)) ||
         !a->d_ckpt.grow(sizeof(float4) * std::max<size_t>(ckpt, 1)) ||
@@ -372,7 +390,7 @@ vkvg_status_t vkvg_gb300_analytic_forward(VkvgAnalytic a, const float *ctrl, con
     const float2 *c2 = (const float2 *)ctrl;
     if (a->timing)
         cudaEventRecord(a->ev[0], st);
-    cudaError_t e = ak_launch_flat_count(st, a->S, c2, a->d_cnt.as<uint32_t>());
+    cudaError_t e = ak_launch_flat_count(st, a->S, c2, a->d_cnt.as<uint32_t>(), a->lane_flat);
     if (e == cudaSuccess)
         e = gb_exclusive_scan(st, a->d_cnt.as<uint32_t>(), a->nseg, a->d_off.as<uint32_t>(), a->d_scan.as<uint32_t>());
     gb_count_launch(4);
@@ -386,10 +404,13 @@ vkvg_status_t vkvg_gb300_analytic_forward(VkvgAnalytic a, const float *ctrl, con
         if (!size_points(a, mon[1]))
             return a->pending = VKVG_STATUS_NO_MEMORY;
         a->sized = true;
+        /* small curves (at most 8 points per segment on average): a lane per
+           segment walks them with fewer idle lanes than a warp per segment */
+        a->lane_flat = (uint64_t)mon[1] <= 8ull * a->nseg;
     }
     ak_bufs B = bufs(a);
     e         = ak_launch_flat_emit(st, a->S, c2, B.off, a->d_pts.as<float2>(), a->d_pt_nb.as<uint2>(), a->cap,
-                                    B.status);
+                                    B.status, a->lane_flat);
     if (a->tile && e == cudaSuccess) { /* tiled: the (tile, layer) pairs, then one launch for all tiles */
         e = tile_setup(a, widths);
         B = bufs(a); /* the planes were sized (and may have moved) for this forward's pairs */
@@ -469,7 +490,7 @@ vkvg_status_t vkvg_gb300_analytic_backward(VkvgAnalytic a, const float *d_canvas
     }
     if (e == cudaSuccess)
         e = ak_launch_flat_bwd(st, a->S, (const float2 *)a->f_ctrl, B.off, a->cap, a->d_gpts.as<float2>(),
-                               (float2 *)d_ctrl);
+                               (float2 *)d_ctrl, a->lane_flat);
     if (a->timing)
         cudaEventRecord(a->ev[7], st);
     gb_count_launch(4);

@@ -288,15 +288,15 @@ __device__ __forceinline__ void neighbours(const ak_scene &, const ak_bufs &B, u
 /* ---------------------------------------------------------- windows */
 
 /* the part of the canvas a block covers: the canvas, or one tile (its
-   origin, size, layers and plane offsets) */
+   origin, size, layers and checkpoint offset) */
 struct ak_win {
     uint32_t x0, y0, W, H, nl, first;
-    size_t   area, ckpt;
+    size_t   ckpt;
 };
 __device__ __forceinline__ ak_win ak_window(const ak_scene &S, uint32_t t) {
     ak_win w;
     if (!S.tiles) {
-        w.x0 = w.y0 = 0, w.W = S.W, w.H = S.H, w.nl = S.nlayers, w.first = 0, w.area = w.ckpt = 0;
+        w.x0 = w.y0 = 0, w.W = S.W, w.H = S.H, w.nl = S.nlayers, w.first = 0, w.ckpt = 0;
         return w;
     }
     const ak_tile_info ti = S.tinfo[t];
@@ -306,9 +306,39 @@ __device__ __forceinline__ ak_win ak_window(const ak_scene &S, uint32_t t) {
     w.H     = min(S.tiles, S.CH - w.y0);
     w.nl    = ti.count;
     w.first = ti.first;
-    w.area  = (size_t)ti.area;
     w.ckpt  = (size_t)ti.ckpt;
     return w;
+}
+/* where window layer q's area plane lies: its first element and its box in
+   the window (the whole window, or a tiled pair's box inside its tile) */
+struct ak_plane {
+    size_t   base;
+    uint32_t x0, y0, w, h;
+};
+__device__ __forceinline__ ak_plane ak_plane_of(const ak_scene &S, const ak_win &w, uint32_t q);
+/* the plane element of window pixel (x, y), or -1 where the plane does not
+   reach (the layer's area is zero there) */
+__device__ __forceinline__ long long ak_plane_at(const ak_plane &P, uint32_t x, uint32_t y) {
+    const uint32_t dx = x - P.x0, dy = y - P.y0;
+    return dx < P.w && dy < P.h ? (long long)(P.base + (size_t)dy * P.w + dx) : -1ll;
+}
+/* warp 0 of a block: the chunk's layers whose plane reaches the block's
+   window rows [ry0, ry1] (every layer without tiles), in order, into
+   act[0, *nact); lane q < n holds layer q's plane */
+__device__ __forceinline__ void ak_chunk_active(const ak_plane &P, bool has, uint32_t ry0, uint32_t ry1,
+                                                uint8_t *act, int *nact) {
+    const uint32_t lane = threadIdx.x & 31;
+    const bool     on   = has && P.y0 <= ry1 && P.y0 + P.h > ry0;
+    const uint32_t m    = __ballot_sync(0xffffffffu, on);
+    if (on)
+        act[__popc(m & ((1u << lane) - 1u))] = (uint8_t)lane;
+    if (lane == 0)
+        *nact = __popc(m);
+}
+/* a (tile, layer) pair's box inside its tile: x0, y0, w, h */
+__device__ __forceinline__ uint4 ak_pair_box(const ak_scene &S, uint32_t j) {
+    const uint2 b = S.pair_box[j];
+    return make_uint4(b.x & 0xFFFFu, b.x >> 16, b.y & 0xFFFFu, b.y >> 16);
 }
 /* blocks of n pixels per window (the canvas, or a tile) */
 __host__ __device__ __forceinline__ uint32_t window_blocks(const ak_scene &S, uint32_t n) {
@@ -318,16 +348,38 @@ __host__ __device__ __forceinline__ uint32_t window_blocks(const ak_scene &S, ui
 __device__ __forceinline__ uint32_t ak_layer(const ak_scene &S, const ak_win &w, uint32_t l) {
     return S.layer_map ? S.layer_map[w.first + l] : l;
 }
-/* a coverage block's window and window layer: blockIdx.x is the layer, or
-   the (tile, layer) pair of a tiled scene */
-__device__ __forceinline__ ak_win ak_cover_window(const ak_scene &S, uint32_t &l) {
+__device__ __forceinline__ ak_plane ak_plane_of(const ak_scene &S, const ak_win &w, uint32_t q) {
+    ak_plane P;
+    if (!S.tiles) {
+        P.base = (size_t)q * w.W * w.H, P.x0 = P.y0 = 0, P.w = w.W, P.h = w.H;
+        return P;
+    }
+    const uint4 bx = ak_pair_box(S, w.first + q);
+    P.base = S.pair_off[w.first + q], P.x0 = bx.x, P.y0 = bx.y, P.w = bx.z, P.h = bx.w;
+    return P;
+}
+/* a coverage block's window, its scene layer and its area plane:
+   blockIdx.x is the layer (the window is the canvas), or the (tile, layer)
+   pair of a tiled scene (the window is the layer's box inside the tile) */
+__device__ __forceinline__ ak_win ak_cover_window(const ak_scene &S, const ak_bufs &B, uint32_t &lg, float *&plane) {
     const uint32_t j = blockIdx.x;
     if (!S.tiles) {
-        l = j;
+        lg    = j;
+        plane = B.area + (size_t)j * S.W * S.H;
         return ak_window(S, 0);
     }
-    const ak_win w = ak_window(S, S.pair_tile[j]);
-    l              = j - w.first;
+    const uint32_t t  = S.pair_tile[j];
+    const uint4    bx = ak_pair_box(S, j);
+    ak_win         w;
+    w.x0  = (t % S.ntx) * S.tiles + bx.x;
+    w.y0  = (t / S.ntx) * S.tiles + bx.y;
+    w.W   = bx.z;
+    w.H   = bx.w;
+    w.nl  = 1;
+    w.first = j;
+    w.ckpt  = 0;
+    lg    = S.layer_map[j];
+    plane = B.area + S.pair_off[j];
     return w;
 }
 
@@ -412,10 +464,11 @@ __global__ void __launch_bounds__(AK_THREADS) ak_cover(ak_scene S, ak_bufs B, co
     int     *acc   = reinterpret_cast<int *>(slots + AK_THREADS);
     __shared__ int nslot;
     /* grid: layers or (tile, layer) pairs (x, up to 2^31) by bands (y) */
-    uint32_t     l;
-    const ak_win w = ak_cover_window(S, l);
+    uint32_t     lg;
+    float       *plane;
+    const ak_win w = ak_cover_window(S, B, lg, plane);
     if (blockIdx.y * S.band >= w.H)
-        return; /* a band below a tile at the canvas's bottom edge */
+        return; /* a band below the window (a tile's layer box is lower than the tile) */
     ak_band bd{(int)(blockIdx.y * S.band), 0, (int)w.W, B.status};
     bd.y1    = min((int)w.H, bd.y0 + (int)S.band);
     int rows = bd.y1 - bd.y0, W1 = w.W + 1;
@@ -423,7 +476,6 @@ __global__ void __launch_bounds__(AK_THREADS) ak_cover(ak_scene S, ak_bufs B, co
         acc[i] = 0;
     const float2 org = v2((float)w.x0, (float)w.y0);
     if (B.off[S.nseg] <= B.cap) {
-        const uint32_t lg = ak_layer(S, w, l);
         uint32_t p = S.layer_path[lg];
         bool     stroke = S.layer_stroke[lg] != 0;
         int      E      = stroke ? 7 : 1;
@@ -448,7 +500,7 @@ __global__ void __launch_bounds__(AK_THREADS) ak_cover(ak_scene S, ak_bufs B, co
     __syncthreads();
     /* row prefix sums, one warp per row, 32 cells per step */
     uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    float   *out  = B.area + w.area + ((size_t)l * w.H + bd.y0) * w.W;
+    float   *out  = plane + (size_t)bd.y0 * w.W;
     for (int r = warp; r < rows; r += AK_THREADS / 32) {
         int carry = 0;
         for (uint32_t c = 0; c < w.W; c += 32) {
@@ -491,33 +543,48 @@ __device__ __forceinline__ float block_sum(float v, float *red) {
 __global__ void __launch_bounds__(AK_THREADS)
     ak_composite(ak_scene S, ak_bufs B, const float4 *__restrict__ colors, const float4 *__restrict__ target,
                  float *__restrict__ loss_part) {
-    __shared__ float4 col[AK_CHUNK];
-    __shared__ float  red[AK_THREADS / 32];
+    __shared__ float4   col[AK_CHUNK];
+    __shared__ ak_plane pl[AK_CHUNK];
+    __shared__ uint8_t  act[AK_CHUNK];
+    __shared__ int      nact;
+    __shared__ float    red[AK_THREADS / 32];
     /* grid: the window's pixel blocks, window after window */
     const uint32_t bpw = window_blocks(S, AK_THREADS), b = blockIdx.x % bpw;
     const ak_win   w   = ak_window(S, blockIdx.x / bpw);
     size_t         np = (size_t)w.W * w.H, px = (size_t)b * AK_THREADS + threadIdx.x;
     bool           valid = px < np;
+    const uint32_t x = valid ? (uint32_t)(px % w.W) : 0u, y = valid ? (uint32_t)(px / w.W) : 0u;
+    /* the block's window rows: a layer whose plane misses them all leaves
+       the block's pixels unchanged (coverage zero) and is passed over */
+    const uint32_t ry0 = (uint32_t)((size_t)b * AK_THREADS / w.W), ry1 = (uint32_t)(((size_t)b * AK_THREADS + AK_THREADS - 1) / w.W);
     float4         C     = S.bg;
     float4        *ckpt  = B.ckpt + w.ckpt;
-    const float   *area  = B.area + w.area;
     for (uint32_t lb = 0; lb < w.nl; lb += AK_CHUNK) {
         uint32_t n = min((uint32_t)AK_CHUNK, w.nl - lb);
         __syncthreads();
-        if (threadIdx.x < n)
-            col[threadIdx.x] = colors[S.layer_path[ak_layer(S, w, lb + threadIdx.x)]];
+        if (threadIdx.x < 32) {
+            ak_plane P{};
+            if (threadIdx.x < n) {
+                col[threadIdx.x] = colors[S.layer_path[ak_layer(S, w, lb + threadIdx.x)]];
+                pl[threadIdx.x]  = P = ak_plane_of(S, w, lb + threadIdx.x);
+            }
+            ak_chunk_active(P, threadIdx.x < n, ry0, ry1, act, &nact);
+        }
         __syncthreads();
         if (!valid)
             continue;
         ckpt[(size_t)(lb / AK_CHUNK) * np + px] = C;
-        float A[AK_CHUNK];
+        const int na = nact;
+        float     A[AK_CHUNK];
 #pragma unroll
-        for (int q = 0; q < AK_CHUNK; q++)
-            A[q] = q < (int)n ? area[(size_t)(lb + q) * np + px] : 0.f;
+        for (int i = 0; i < AK_CHUNK; i++) {
+            const long long k = i < na ? ak_plane_at(pl[act[i]], x, y) : -1ll;
+            A[i]              = k >= 0 ? B.area[k] : 0.f;
+        }
 #pragma unroll
-        for (int q = 0; q < AK_CHUNK; q++)
-            if (q < (int)n)
-                C = blend(cover(A[q]), col[q], C);
+        for (int i = 0; i < AK_CHUNK; i++)
+            if (i < na)
+                C = blend(cover(A[i]), col[act[i]], C);
     }
     float        s  = 0.f;
     const size_t cp = valid ? ((size_t)w.y0 + px / w.W) * S.CW + w.x0 + px % w.W : 0; /* on the canvas */
@@ -571,7 +638,10 @@ __device__ __forceinline__ float warp_reduce_scatter32(float (&v)[32]) {
 __global__ void __launch_bounds__(AK_CB_THREADS)
     ak_composite_bwd(ak_scene S, ak_bufs B, const float4 *__restrict__ colors, const float4 *__restrict__ target,
                      const float4 *__restrict__ d_canvas, float *__restrict__ color_part) {
-    __shared__ float4 col[AK_CHUNK];
+    __shared__ float4   col[AK_CHUNK];
+    __shared__ ak_plane pl[AK_CHUNK];
+    __shared__ uint8_t  act[AK_CHUNK];
+    __shared__ int      nact;
     __shared__ float4 sB[AK_CHUNK][AK_CB_THREADS]; /* colour under each layer of the chunk */
     __shared__ float  sA[AK_CHUNK][AK_CB_THREADS]; /* the chunk's areas */
     __shared__ float  red[AK_CB_THREADS / 32][AK_CHUNK * 4];
@@ -582,7 +652,12 @@ __global__ void __launch_bounds__(AK_CB_THREADS)
     bool           valid = px < np;
     float4         g     = make_float4(0.f, 0.f, 0.f, 0.f);
     const float4  *ckpt  = B.ckpt + w.ckpt;
-    float         *area  = B.area + w.area;
+    const uint32_t x = valid ? (uint32_t)(px % w.W) : 0u, y = valid ? (uint32_t)(px / w.W) : 0u;
+    /* the block's window rows: layers whose planes miss them are passed over
+       (no coverage, no gradient, no colour partial: the reduction reads a
+       layer's partials only from the blocks its plane reaches) */
+    const uint32_t ry0 = (uint32_t)((size_t)b * AK_CB_THREADS / w.W);
+    const uint32_t ry1 = (uint32_t)(((size_t)b * AK_CB_THREADS + AK_CB_THREADS - 1) / w.W);
     if (valid) {
         const size_t cp = ((size_t)w.y0 + px / w.W) * S.CW + w.x0 + px % w.W; /* on the canvas */
         if (d_canvas) {
@@ -599,43 +674,60 @@ __global__ void __launch_bounds__(AK_CB_THREADS)
     for (uint32_t ch = nch; ch-- > 0;) {
         uint32_t lb = ch * AK_CHUNK, n = min((uint32_t)AK_CHUNK, w.nl - lb);
         __syncthreads();
-        if (threadIdx.x < n)
-            col[threadIdx.x] = colors[S.layer_path[ak_layer(S, w, lb + threadIdx.x)]];
+        if (threadIdx.x < 32) {
+            ak_plane P{};
+            if (threadIdx.x < n) {
+                col[threadIdx.x] = colors[S.layer_path[ak_layer(S, w, lb + threadIdx.x)]];
+                pl[threadIdx.x]  = P = ak_plane_of(S, w, lb + threadIdx.x);
+            }
+            ak_chunk_active(P, threadIdx.x < n, ry0, ry1, act, &nact);
+        }
         __syncthreads();
-        float4       Bc = valid ? ckpt[(size_t)ch * np + px] : make_float4(0.f, 0.f, 0.f, 0.f);
-        const float *ap = area + (size_t)lb * np + px;
+        const int na = nact; /* the chunk's active layers act[0, na), in order */
+        if (na == 0)
+            continue; /* every layer of the chunk leaves these pixels alone */
+        float4 Bc = valid ? ckpt[(size_t)ch * np + px] : make_float4(0.f, 0.f, 0.f, 0.f);
         {
             float A[AK_CHUNK];
 #pragma unroll
-            for (int q = 0; q < AK_CHUNK; q++)
-                A[q] = (valid && q < (int)n) ? ap[(size_t)q * np] : 0.f;
+            for (int i = 0; i < AK_CHUNK; i++) {
+                const long long k = (valid && i < na) ? ak_plane_at(pl[act[i]], x, y) : -1ll;
+                A[i]              = k >= 0 ? B.area[k] : 0.f;
+            }
 #pragma unroll
-            for (int q = 0; q < AK_CHUNK; q++) {
-                sB[q][threadIdx.x] = Bc;
-                sA[q][threadIdx.x] = A[q];
-                if (q < (int)n)
-                    Bc = blend(cover(A[q]), col[q], Bc);
+            for (int i = 0; i < AK_CHUNK; i++) {
+                if (i < na) {
+                    sB[i][threadIdx.x] = Bc;
+                    sA[i][threadIdx.x] = A[i];
+                    Bc                 = blend(cover(A[i]), col[act[i]], Bc);
+                }
             }
         }
-        /* two halves of 8 layers, top half first; colour partials per half */
+        /* the active layers in groups of 8, top group first; colour partials per group */
 #pragma unroll
         for (int hf = 1; hf >= 0; hf--) {
+            if (hf * 8 >= na)
+                continue;
             float dc[32];
 #pragma unroll
             for (int q8 = 7; q8 >= 0; q8--) {
-                int q = hf * 8 + q8;
+                const int i = hf * 8 + q8;
                 dc[4 * q8] = dc[4 * q8 + 1] = dc[4 * q8 + 2] = dc[4 * q8 + 3] = 0.f;
-                if (q >= (int)n)
+                if (i >= na)
                     continue;
-                float4 c  = col[q], Bq = sB[q][threadIdx.x];
-                float  Aq = sA[q][threadIdx.x];
+                const int q  = act[i];
+                float4    c  = col[q], Bq = sB[i][threadIdx.x];
+                float     Aq = sA[i][threadIdx.x];
                 float  al = cover(Aq);
                 float  gB = g.x * Bq.x + g.y * Bq.y + g.z * Bq.z + g.w * Bq.w;
                 float  gc = g.x * c.x + g.y * c.y + g.z * c.z + g.w * c.w;
                 float  da = T * (gc - c.w * gB);
                 float  gA = fabsf(Aq) < 1.f ? (Aq > 0.f ? da : Aq < 0.f ? -da : 0.f) : 0.f;
-                if (valid)
-                    area[(size_t)(lb + q) * np + px] = gA;
+                if (valid) {
+                    const long long k = ak_plane_at(pl[q], x, y);
+                    if (k >= 0)
+                        B.area[k] = gA;
+                }
                 float ta = T * al;
                 dc[4 * q8] = ta * g.x, dc[4 * q8 + 1] = ta * g.y, dc[4 * q8 + 2] = ta * g.z;
                 dc[4 * q8 + 3] = ta * (g.w - gB);
@@ -644,14 +736,14 @@ __global__ void __launch_bounds__(AK_CB_THREADS)
             red[warp][hf * 32 + lane] = warp_reduce_scatter32(dc);
         }
         __syncthreads();
-        if (threadIdx.x < n * 4) {
+        if ((int)threadIdx.x < na * 4) {
             float s = 0.f;
             for (int k = 0; k < AK_CB_THREADS / 32; k++)
                 s += red[k][threadIdx.x];
             /* one window: [block][layer][channel]; tiled: [pair][block of the tile][channel] */
-            const uint32_t q = threadIdx.x >> 2, c = threadIdx.x & 3;
+            const uint32_t q = act[threadIdx.x >> 2], c = threadIdx.x & 3;
             const size_t   i = S.tiles ? ((size_t)(w.first + lb + q) * bpw + b) * 4 + c
-                                       : ((size_t)b * S.nlayers + lb) * 4 + threadIdx.x;
+                                       : ((size_t)b * S.nlayers + lb + q) * 4 + c;
             color_part[i] = s;
         }
     }
@@ -673,20 +765,20 @@ __global__ void __launch_bounds__(AK_THREADS)
     float   *gs    = reinterpret_cast<float *>(eg + AK_THREADS * 7);
     __shared__ float red[AK_THREADS / 32];
     __shared__ int   nslot;
-    uint32_t         l;
-    const ak_win     w = ak_cover_window(S, l);
+    uint32_t         lg;
+    float           *plane;
+    const ak_win     w = ak_cover_window(S, B, lg, plane);
     if (blockIdx.y * S.band >= w.H)
-        return; /* a band below a tile at the canvas's bottom edge */
+        return; /* a band below the window */
     ak_band bd{(int)(blockIdx.y * S.band), 0, (int)w.W, B.status};
     bd.y1             = min((int)w.H, bd.y0 + (int)S.band);
     int          rows = bd.y1 - bd.y0;
-    const float *src  = B.area + w.area + ((size_t)l * w.H + bd.y0) * w.W;
+    const float *src  = plane + (size_t)bd.y0 * w.W;
     for (int i = threadIdx.x; i < rows * (int)w.W; i += AK_THREADS)
         gs[i] = src[i];
     if (B.off[S.nseg] > B.cap)
         return;
     const float2   org = v2((float)w.x0, (float)w.y0);
-    const uint32_t lg  = ak_layer(S, w, l);
     uint32_t p      = S.layer_path[lg];
     bool     stroke = S.layer_stroke[lg] != 0;
     int      E      = stroke ? 7 : 1;
@@ -770,10 +862,16 @@ __global__ void ak_reduce_colors(ak_scene S, uint32_t nblocks, const float *__re
     if (t >= S.nlayers * 4)
         return;
     float s = 0.f;
-    if (S.tiles) /* t: (pair, channel); the pair's partials are contiguous */
-        for (uint32_t b = 0; b < nblocks; b++)
-            s += part[((size_t)(t >> 2) * nblocks + b) * 4 + (t & 3)];
-    else
+    if (S.tiles) { /* t: (pair, channel); the blocks of rows the pair's plane reaches wrote partials */
+        const uint32_t j = t >> 2, tl = S.pair_tile[j];
+        const uint32_t W  = min(S.tiles, S.CW - (tl % S.ntx) * S.tiles);
+        const uint2    bx = S.pair_box[j];
+        const uint32_t y0 = bx.x >> 16, h = bx.y >> 16;
+        const uint32_t b0 = (uint32_t)((size_t)y0 * W / AK_CB_THREADS);
+        const uint32_t b1 = (uint32_t)(((size_t)(y0 + h) * W - 1) / AK_CB_THREADS);
+        for (uint32_t b = b0; b <= b1 && b < nblocks; b++)
+            s += part[((size_t)j * nblocks + b) * 4 + (t & 3)];
+    } else
         for (uint32_t b = 0; b < nblocks; b++)
             s += part[(size_t)b * S.nlayers * 4 + t];
     const uint32_t l = t >> 2;
@@ -793,10 +891,14 @@ __global__ void ak_reduce_loss(uint32_t nblocks, float scale, const float *__res
 /* ------------------------------------------------------------- tiling */
 
 /* one warp per scene layer: the box of its path's flattened points in
-   tiles, a stroke's widened by half its width and one pixel (its rectangles
-   and bevels reach at most half the width from a point) */
-__global__ void ak_layer_boxes(ak_scene S, ak_bufs B, const float *__restrict__ widths, uint32_t tile, uint32_t ntx,
-                               uint32_t nty, int4 *__restrict__ box) {
+   pixels (x0, y0, x1, y1 inclusive, clipped to the canvas; x0 > x1 when
+   empty), a stroke's widened by half its width and one pixel (its
+   rectangles and bevels reach at most half the width from a point), a
+   fill's by one pixel (the winding of a closed contour, and with it every
+   area the coverage deposits, is exactly zero outside its points' box);
+   the boxes' pixel total is added to *total */
+__global__ void ak_layer_boxes(ak_scene S, ak_bufs B, const float *__restrict__ widths, int4 *__restrict__ box,
+                               unsigned long long *__restrict__ total) {
     const uint32_t l = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (l >= S.nlayers)
         return;
@@ -818,43 +920,53 @@ __global__ void ak_layer_boxes(ak_scene S, ak_bufs B, const float *__restrict__ 
     }
     if (lane)
         return;
-    /* the winding of a closed contour is zero outside its points' box, so a
-       fill's areas stay inside it (a pixel of margin) */
     const bool  stroke = S.layer_stroke[l] != 0;
     const float pad    = stroke ? 0.5f * fabsf(widths[p]) + 1.f : 1.f;
     int4        b      = make_int4(1, 1, 0, 0); /* empty */
     if (x0 <= x1 && isfinite(pad)) {
-        const float fx0 = x0 - pad, fx1 = x1 + pad, fy0 = y0 - pad, fy1 = y1 + pad;
-        const float lim = (float)max(ntx, nty) * (float)tile;
-        const int   tx0 = (int)floorf(fminf(fmaxf(fx0, 0.f), lim) / (float)tile);
-        const int   tx1 = (int)floorf(fminf(fmaxf(fx1, 0.f), lim) / (float)tile);
-        const int   ty0 = (int)floorf(fminf(fmaxf(fy0, 0.f), lim) / (float)tile);
-        const int   ty1 = (int)floorf(fminf(fmaxf(fy1, 0.f), lim) / (float)tile);
-        if (fx1 >= 0.f && fy1 >= 0.f && fy0 < (float)(nty * tile) && fx0 < (float)(ntx * tile))
-            b = make_int4(tx0, ty0, min(tx1, (int)ntx - 1), min(ty1, (int)nty - 1));
+        /* clamped in float first: the box may reach far beyond the canvas */
+        const float W = (float)S.CW, H = (float)S.CH;
+        const float fx0 = fminf(fmaxf(floorf(x0 - pad), 0.f), W), fx1 = fminf(fmaxf(floorf(x1 + pad), -1.f), W - 1.f);
+        const float fy0 = fminf(fmaxf(floorf(y0 - pad), 0.f), H), fy1 = fminf(fmaxf(floorf(y1 + pad), -1.f), H - 1.f);
+        if (fx0 <= fx1 && fy0 <= fy1)
+            b = make_int4((int)fx0, (int)fy0, (int)fx1, (int)fy1);
     }
     box[l] = b;
+    if (b.x <= b.z)
+        atomicAdd(total, (unsigned long long)(b.z - b.x + 1) * (unsigned long long)(b.w - b.y + 1));
 }
 
-__global__ void ak_tile_flags(uint32_t nlayers, uint64_t n, uint32_t ntx, const int4 *__restrict__ box,
+/* flags[t * nlayers + l] = 1 when layer l's box meets tile t */
+__global__ void ak_tile_flags(uint32_t nlayers, uint64_t n, uint32_t ntx, uint32_t tile, const int4 *__restrict__ box,
                               uint32_t *__restrict__ flags) {
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n)
         return;
     const uint32_t t = (uint32_t)(i / nlayers), l = (uint32_t)(i % nlayers);
-    const int      tx = (int)(t % ntx), ty = (int)(t / ntx);
-    const int4     b  = box[l];
-    flags[i]          = tx >= b.x && tx <= b.z && ty >= b.y && ty <= b.w ? 1u : 0u;
+    const int      tx0 = (int)((t % ntx) * tile), ty0 = (int)((t / ntx) * tile);
+    const int4     b   = box[l];
+    flags[i] = b.x <= tx0 + (int)tile - 1 && b.z >= tx0 && b.y <= ty0 + (int)tile - 1 && b.w >= ty0 ? 1u : 0u;
 }
 
-__global__ void ak_tile_lists(uint64_t n, uint32_t nlayers, const uint32_t *__restrict__ flags,
-                              const uint32_t *__restrict__ pos, uint32_t *__restrict__ list,
-                              uint32_t *__restrict__ tile) {
+/* the (tile, layer) pairs in order: for flagged entry i its layer, tile,
+   box inside the tile (x0 | y0 << 16, w | h << 16, tile coordinates) and
+   pixel count */
+__global__ void ak_tile_lists(uint64_t n, uint32_t nlayers, uint32_t ntx, uint32_t tile, const int4 *__restrict__ box,
+                              const uint32_t *__restrict__ flags, const uint32_t *__restrict__ pos,
+                              uint32_t *__restrict__ list, uint32_t *__restrict__ ptile, uint2 *__restrict__ pbox,
+                              uint32_t *__restrict__ psize) {
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n && flags[i]) {
-        list[pos[i]] = (uint32_t)(i % nlayers);
-        tile[pos[i]] = (uint32_t)(i / nlayers);
-    }
+    if (i >= n || !flags[i])
+        return;
+    const uint32_t t = (uint32_t)(i / nlayers), l = (uint32_t)(i % nlayers), j = pos[i];
+    const int      tx0 = (int)((t % ntx) * tile), ty0 = (int)((t / ntx) * tile);
+    const int4     b   = box[l];
+    const int      x0 = max(b.x, tx0) - tx0, x1 = min(b.z, tx0 + (int)tile - 1) - tx0;
+    const int      y0 = max(b.y, ty0) - ty0, y1 = min(b.w, ty0 + (int)tile - 1) - ty0;
+    list[j]  = l;
+    ptile[j] = t;
+    pbox[j]  = make_uint2((uint32_t)x0 | (uint32_t)y0 << 16, (uint32_t)(x1 - x0 + 1) | (uint32_t)(y1 - y0 + 1) << 16);
+    psize[j] = (uint32_t)((x1 - x0 + 1) * (y1 - y0 + 1));
 }
 
 __global__ void ak_adam(float *__restrict__ p, const float *__restrict__ g, float *__restrict__ m,
@@ -930,23 +1042,25 @@ cudaError_t ak_launch_reduce(cudaStream_t st, const ak_scene &S, uint32_t nblock
         ak_reduce_loss<<<1, AK_THREADS, 0, st>>>(nblocks, 1.f / (float)((size_t)S.CW * S.CH * 4), loss_part, loss);
     return cudaGetLastError();
 }
-cudaError_t ak_launch_layer_boxes(cudaStream_t st, const ak_scene &S, const ak_bufs &B, const float *widths,
-                                  uint32_t tile, uint32_t ntx, uint32_t nty, int4 *box) {
+cudaError_t ak_launch_layer_boxes(cudaStream_t st, const ak_scene &S, const ak_bufs &B, const float *widths, int4 *box,
+                                  unsigned long long *total) {
     if (S.nlayers)
-        ak_layer_boxes<<<(S.nlayers * 32 + 255) / 256, 256, 0, st>>>(S, B, widths, tile, ntx, nty, box);
+        ak_layer_boxes<<<(S.nlayers * 32 + 255) / 256, 256, 0, st>>>(S, B, widths, box, total);
     return cudaGetLastError();
 }
-cudaError_t ak_launch_tile_flags(cudaStream_t st, uint32_t nlayers, uint32_t ntiles, uint32_t ntx, const int4 *box,
-                                 uint32_t *flags) {
+cudaError_t ak_launch_tile_flags(cudaStream_t st, uint32_t nlayers, uint32_t ntiles, uint32_t ntx, uint32_t tile,
+                                 const int4 *box, uint32_t *flags) {
     const uint64_t n = (uint64_t)nlayers * ntiles;
     if (n)
-        ak_tile_flags<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(nlayers, n, ntx, box, flags);
+        ak_tile_flags<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(nlayers, n, ntx, tile, box, flags);
     return cudaGetLastError();
 }
-cudaError_t ak_launch_tile_lists(cudaStream_t st, uint64_t n, uint32_t nlayers, const uint32_t *flags,
-                                 const uint32_t *pos, uint32_t *list, uint32_t *tile) {
+cudaError_t ak_launch_tile_lists(cudaStream_t st, uint64_t n, uint32_t nlayers, uint32_t ntx, uint32_t tile,
+                                 const int4 *box, const uint32_t *flags, const uint32_t *pos, uint32_t *list,
+                                 uint32_t *ptile, uint2 *pbox, uint32_t *psize) {
     if (n)
-        ak_tile_lists<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, nlayers, flags, pos, list, tile);
+        ak_tile_lists<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, nlayers, ntx, tile, box, flags, pos, list, ptile,
+                                                                     pbox, psize);
     return cudaGetLastError();
 }
 cudaError_t ak_launch_adam(cudaStream_t st, float *param, const float *grad, float *m, float *v, uint32_t n, float lr,

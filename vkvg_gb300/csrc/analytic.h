@@ -21,10 +21,10 @@
 #define AK_CHUNK 16 /* layers per compositing checkpoint */
 
 /* a tile of a tiled scene: its first (tile, layer) pair, the number of its
-   layers, and the offsets (in elements) of its area planes and checkpoints */
+   layers, and the offset (in elements) of its checkpoints */
 struct ak_tile_info {
     uint32_t           first, count;
-    unsigned long long area, ckpt;
+    unsigned long long ckpt;
 };
 
 struct ak_scene {
@@ -35,11 +35,16 @@ struct ak_scene {
        tile side): every launch covers all tiles at once; W = H = tiles, nbands
        the bands of a tile, nlayers the number of (tile, layer) pairs (tile
        by tile, each tile's layers in scene order), layer_map[j] the scene
-       layer of pair j, pair_tile[j] its tile, tinfo[t] tile t's pairs and
-       planes, ntx the tiles across, ntiles the tiles in all */
+       layer of pair j, pair_tile[j] its tile, pair_box[j] the layer's box
+       inside the tile (x0 | y0 << 16, w | h << 16: its area plane covers
+       only that box, the layer's area being zero outside it), pair_off[j]
+       the plane's first element, tinfo[t] tile t's pairs and checkpoints,
+       ntx the tiles across, ntiles the tiles in all */
     uint32_t            CW, CH, tiles, ntx, ntiles;
     const uint32_t     *layer_map;
     const uint32_t     *pair_tile;
+    const uint2        *pair_box;
+    const uint32_t     *pair_off;
     const ak_tile_info *tinfo;
     const uint8_t  *seg_kind;     /* nseg */
     const uint32_t *seg_cp;       /* nseg: first control point */
@@ -63,11 +68,12 @@ struct ak_bufs {
     uint32_t       *status;
 };
 
-cudaError_t ak_launch_flat_count(cudaStream_t st, const ak_scene &S, const float2 *ctrl, uint32_t *cnt);
+/* lanes: one lane per segment (scenes of small curves) instead of a warp */
+cudaError_t ak_launch_flat_count(cudaStream_t st, const ak_scene &S, const float2 *ctrl, uint32_t *cnt, bool lanes);
 cudaError_t ak_launch_flat_emit(cudaStream_t st, const ak_scene &S, const float2 *ctrl, const uint32_t *off,
-                                float2 *pts, uint2 *pt_nb, uint32_t cap, uint32_t *status);
+                                float2 *pts, uint2 *pt_nb, uint32_t cap, uint32_t *status, bool lanes);
 cudaError_t ak_launch_flat_bwd(cudaStream_t st, const ak_scene &S, const float2 *ctrl, const uint32_t *off,
-                               uint32_t cap, const float2 *gpts, float2 *gctrl);
+                               uint32_t cap, const float2 *gpts, float2 *gctrl, bool lanes);
 
 uint32_t    ak_band_rows(uint32_t W);
 size_t      ak_cover_smem(uint32_t W);
@@ -80,18 +86,21 @@ cudaError_t ak_launch_cover_bwd(cudaStream_t st, const ak_scene &S, const ak_buf
                                 float2 *gpts, float *gwidth);
 cudaError_t ak_launch_reduce(cudaStream_t st, const ak_scene &S, uint32_t nblocks, const float4 *color_part,
                              float4 *d_colors, const float *loss_part, float *loss);
-/* tiled scenes: per scene layer its box in tiles (x0, y0, x1, y1 inclusive;
-   x0 > x1 when empty), from its flattened points (strokes widened by half
-   their width plus a pixel) */
-cudaError_t ak_launch_layer_boxes(cudaStream_t st, const ak_scene &S, const ak_bufs &B, const float *widths,
-                                  uint32_t tile, uint32_t ntx, uint32_t nty, int4 *box);
-/* flags[t * nlayers + l] = 1 when layer l's box holds tile t */
-cudaError_t ak_launch_tile_flags(cudaStream_t st, uint32_t nlayers, uint32_t ntiles, uint32_t ntx, const int4 *box,
-                                 uint32_t *flags);
-/* list[pos[i]] = i % nlayers and tile[pos[i]] = i / nlayers where flags[i]
-   (pos: exclusive scan of the flags) */
-cudaError_t ak_launch_tile_lists(cudaStream_t st, uint64_t n, uint32_t nlayers, const uint32_t *flags,
-                                 const uint32_t *pos, uint32_t *list, uint32_t *tile);
+/* tiled scenes: per scene layer its box in pixels (x0, y0, x1, y1
+   inclusive, clipped to the canvas; x0 > x1 when empty), from its flattened
+   points (strokes widened by half their width plus a pixel, fills by a
+   pixel), the boxes' pixel total added to *total */
+cudaError_t ak_launch_layer_boxes(cudaStream_t st, const ak_scene &S, const ak_bufs &B, const float *widths, int4 *box,
+                                  unsigned long long *total);
+/* flags[t * nlayers + l] = 1 when layer l's box meets tile t */
+cudaError_t ak_launch_tile_flags(cudaStream_t st, uint32_t nlayers, uint32_t ntiles, uint32_t ntx, uint32_t tile,
+                                 const int4 *box, uint32_t *flags);
+/* for each flagged entry i (pos: exclusive scan of the flags), pair pos[i]:
+   its layer i % nlayers, its tile i / nlayers, the layer's box inside the
+   tile and its pixel count */
+cudaError_t ak_launch_tile_lists(cudaStream_t st, uint64_t n, uint32_t nlayers, uint32_t ntx, uint32_t tile,
+                                 const int4 *box, const uint32_t *flags, const uint32_t *pos, uint32_t *list,
+                                 uint32_t *ptile, uint2 *pbox, uint32_t *psize);
 cudaError_t ak_launch_adam(cudaStream_t st, float *param, const float *grad, float *m, float *v, uint32_t n, float lr,
                            float beta1, float beta2, float eps, uint32_t step, float lo, float hi);
 /* pixel blocks of ak_composite (loss partials) and of ak_composite_bwd per

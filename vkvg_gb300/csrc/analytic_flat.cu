@@ -12,7 +12,9 @@
  *
  * Cubics are walked breadth first by the warp (gb_bezier_warp), or serially
  * by one lane when the tree outgrows the warp's buffers; both give vkvg's
- * points in vkvg's order.
+ * points in vkvg's order.  Scenes of small curves (a few points per
+ * segment on average) take one lane per segment instead, each walking its
+ * cubic serially.
  *
  * The backward pass walks the same subdivision again instead of storing it:
  * every emitted point is the blossom of its sub-curve interval, a fixed
@@ -212,19 +214,101 @@ __global__ void __launch_bounds__(32 * AK_FW) ak_flat_bwd(ak_scene S, const floa
     }
 }
 
-cudaError_t ak_launch_flat_count(cudaStream_t st, const ak_scene &S, const float2 *ctrl, uint32_t *cnt) {
-    if (S.nseg)
+/* One lane per segment, each walking its cubic serially: for scenes of
+   small curves (a few points each), where a warp per segment would leave
+   most lanes idle.  The same points in the same order. */
+#define AK_LT 256 /* lanes per block */
+
+__global__ void __launch_bounds__(AK_LT) ak_flat_count_lane(ak_scene S, const float2 *__restrict__ ctrl,
+                                                           uint32_t *__restrict__ cnt) {
+    const uint32_t s = blockIdx.x * AK_LT + threadIdx.x;
+    if (s >= S.nseg)
+        return;
+    float2   p, c[4];
+    uint32_t n = seg_start(S, ctrl, s, p) ? 1u : 0u;
+    if (S.seg_kind[s] == AK_SEG_CUBIC && ak_cubic_cp(S, ctrl, s, c)) {
+        ak_cnt_emit e{0};
+        gb_bezier_walk<false>(AK_TOL, c[0].x, c[0].y, c[1].x, c[1].y, c[2].x, c[2].y, c[3].x, c[3].y, e);
+        n += e.n;
+    }
+    cnt[s] = n;
+}
+
+__global__ void __launch_bounds__(AK_LT) ak_flat_emit_lane(ak_scene S, const float2 *__restrict__ ctrl,
+                                                          const uint32_t *__restrict__ off, float2 *__restrict__ pts,
+                                                          uint2 *__restrict__ pt_nb, uint32_t cap,
+                                                          uint32_t *__restrict__ status) {
+    const uint32_t s = blockIdx.x * AK_LT + threadIdx.x;
+    if (off[S.nseg] > cap) {
+        if (blockIdx.x == 0 && threadIdx.x == 0)
+            atomicOr(status, AK_ERR_POINTS);
+        return;
+    }
+    if (s >= S.nseg)
+        return;
+    float2         p, c[4];
+    const uint32_t cont = S.seg_contour[s];
+    const uint32_t c0 = off[S.cont_s0[cont]], c1 = off[S.cont_s0[cont + 1]];
+    uint32_t       o  = off[s];
+    if (seg_start(S, ctrl, s, p)) {
+        pts[o] = p, pt_nb[o] = ak_nb(o, c0, c1);
+        o++;
+    }
+    if (S.seg_kind[s] == AK_SEG_CUBIC && ak_cubic_cp(S, ctrl, s, c)) {
+        ak_pt_emit e{pts, pt_nb, o, c0, c1};
+        gb_bezier_walk<false>(AK_TOL, c[0].x, c[0].y, c[1].x, c[1].y, c[2].x, c[2].y, c[3].x, c[3].y, e);
+    }
+}
+
+__global__ void __launch_bounds__(AK_LT) ak_flat_bwd_lane(ak_scene S, const float2 *__restrict__ ctrl,
+                                                         const uint32_t *__restrict__ off, uint32_t cap,
+                                                         const float2 *__restrict__ gpts,
+                                                         float2 *__restrict__ gctrl) {
+    const uint32_t s = blockIdx.x * AK_LT + threadIdx.x;
+    if (s >= S.nseg || off[S.nseg] > cap)
+        return;
+    uint32_t     c0 = S.seg_cp[s], o = off[s];
+    float2       p, c[4];
+    ak_grad_emit e;
+    e.g = gpts;
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+        e.gc[k] = make_float2(0.f, 0.f);
+    if (seg_start(S, ctrl, s, p))
+        e.gc[0] = gpts[o++];
+    e.o              = o;
+    const bool cubic = S.seg_kind[s] == AK_SEG_CUBIC;
+    if (cubic && ak_cubic_cp(S, ctrl, s, c))
+        gb_bezier_walk<true>(AK_TOL, c[0].x, c[0].y, c[1].x, c[1].y, c[2].x, c[2].y, c[3].x, c[3].y, e);
+    atomicAdd(&gctrl[c0].x, e.gc[0].x), atomicAdd(&gctrl[c0].y, e.gc[0].y);
+    if (cubic) {
+        atomicAdd(&gctrl[c0 + 1].x, e.gc[1].x), atomicAdd(&gctrl[c0 + 1].y, e.gc[1].y);
+        atomicAdd(&gctrl[c0 + 2].x, e.gc[2].x), atomicAdd(&gctrl[c0 + 2].y, e.gc[2].y);
+        const uint32_t ce = S.seg_end[s];
+        atomicAdd(&gctrl[ce].x, e.gc[3].x), atomicAdd(&gctrl[ce].y, e.gc[3].y);
+    }
+}
+
+cudaError_t ak_launch_flat_count(cudaStream_t st, const ak_scene &S, const float2 *ctrl, uint32_t *cnt, bool lanes) {
+    if (S.nseg && lanes)
+        ak_flat_count_lane<<<(S.nseg + AK_LT - 1) / AK_LT, AK_LT, 0, st>>>(S, ctrl, cnt);
+    else if (S.nseg)
         ak_flat_count<<<(S.nseg + AK_FW - 1) / AK_FW, 32 * AK_FW, 0, st>>>(S, ctrl, cnt);
     return cudaGetLastError();
 }
 cudaError_t ak_launch_flat_emit(cudaStream_t st, const ak_scene &S, const float2 *ctrl, const uint32_t *off,
-                                float2 *pts, uint2 *pt_nb, uint32_t cap, uint32_t *status) {
-    ak_flat_emit<<<(S.nseg + AK_FW - 1) / AK_FW + 1, 32 * AK_FW, 0, st>>>(S, ctrl, off, pts, pt_nb, cap, status);
+                                float2 *pts, uint2 *pt_nb, uint32_t cap, uint32_t *status, bool lanes) {
+    if (lanes)
+        ak_flat_emit_lane<<<(S.nseg + AK_LT - 1) / AK_LT + 1, AK_LT, 0, st>>>(S, ctrl, off, pts, pt_nb, cap, status);
+    else
+        ak_flat_emit<<<(S.nseg + AK_FW - 1) / AK_FW + 1, 32 * AK_FW, 0, st>>>(S, ctrl, off, pts, pt_nb, cap, status);
     return cudaGetLastError();
 }
 cudaError_t ak_launch_flat_bwd(cudaStream_t st, const ak_scene &S, const float2 *ctrl, const uint32_t *off,
-                               uint32_t cap, const float2 *gpts, float2 *gctrl) {
-    if (S.nseg)
+                               uint32_t cap, const float2 *gpts, float2 *gctrl, bool lanes) {
+    if (S.nseg && lanes)
+        ak_flat_bwd_lane<<<(S.nseg + AK_LT - 1) / AK_LT, AK_LT, 0, st>>>(S, ctrl, off, cap, gpts, gctrl);
+    else if (S.nseg)
         ak_flat_bwd<<<(S.nseg + AK_FW - 1) / AK_FW, 32 * AK_FW, 0, st>>>(S, ctrl, off, cap, gpts, gctrl);
     return cudaGetLastError();
 }
