@@ -73,6 +73,8 @@ def parse():
     p.add_argument("--no-analytic", action="store_true", help="skip the differentiable analytic-coverage workload")
     p.add_argument("--no-glyphs", action="store_true", help="skip the 4096x4096 glyph workload")
     p.add_argument("--svg-shapes", type=int, default=600, help="shapes of the SVG ingestion workload (0: skip)")
+    p.add_argument("--analytic-glyphs-only", action="store_true",
+                   help="run only the glyph scene's analytic forward + backward and print its entry (profiling)")
     p.add_argument("--adam-steps", type=int, default=200, help="Adam steps of the differentiable workload")
     return p.parse_args()
 
@@ -670,6 +672,11 @@ def main():
     from vkvg_gb300 import scenes
 
     torch.cuda.set_device(local)
+    if a.analytic_glyphs_only:
+        buf = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+        gb._build.build()
+        print(json.dumps(analytic_glyph_bench(a, gb, torch, np, buf.zero_)))
+        return
     dist = None
     if world > 1:
         import torch.distributed as dist

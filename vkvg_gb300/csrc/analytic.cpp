@@ -196,7 +196,7 @@ VkvgAnalytic create_scene(uint32_t width, uint32_t height, uint32_t tile, const 
     ok = ok && a->d_cnt.grow(4 * ((size_t)nseg + 1)) && a->d_off.grow(4 * ((size_t)nseg + 1)) &&
          a->d_scan.grow(4 * gb_scan_scratch_words(nseg + 1)) && a->d_canvas.grow(sizeof(float4) * np) &&
          a->d_loss.grow(sizeof(float)) && a->d_status.grow(4) && a->h_mon.grow(8) &&
-         size_points(a, std::max<uint32_t>(64 * nseg, 65536));
+         size_points(a, 65536) /* the first forward sizes it */;
     if (!tile) /* one window: its planes are sized now */
         ok = ok && a->d_area.grow(sizeof(float) * np * std::max<uint32_t>(a->nlayers, 1)) &&
              a->d_ckpt.grow(sizeof(float4) * np * std::max<size_t>(nchk, 1)) && a->d_loss_part.grow(sizeof(float) * nbk) &&
