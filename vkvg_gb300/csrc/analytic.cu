@@ -463,58 +463,65 @@ __global__ void __launch_bounds__(AK_THREADS) ak_cover(ak_scene S, ak_bufs B, co
     ak_slot *slots = reinterpret_cast<ak_slot *>(ak_smem);
     int     *acc   = reinterpret_cast<int *>(slots + AK_THREADS);
     __shared__ int nslot;
-    /* grid: layers or (tile, layer) pairs (x, up to 2^31) by bands (y) */
-    uint32_t     lg;
-    float       *plane;
-    const ak_win w = ak_cover_window(S, B, lg, plane);
-    if (blockIdx.y * S.band >= w.H)
-        return; /* a band below the window (a tile's layer box is lower than the tile) */
-    ak_band bd{(int)(blockIdx.y * S.band), 0, (int)w.W, B.status};
-    bd.y1    = min((int)w.H, bd.y0 + (int)S.band);
-    int rows = bd.y1 - bd.y0, W1 = w.W + 1;
-    for (int i = threadIdx.x; i < rows * W1; i += AK_THREADS)
-        acc[i] = 0;
-    const float2 org = v2((float)w.x0, (float)w.y0);
-    if (B.off[S.nseg] <= B.cap) {
-        uint32_t p = S.layer_path[lg];
-        bool     stroke = S.layer_stroke[lg] != 0;
-        int      E      = stroke ? 7 : 1;
-        float    h      = 0.5f * widths[p];
-        uint32_t p1     = B.off[S.path_s0[p + 1]];
-        for (uint32_t base = B.off[S.path_s0[p]]; base < p1; base += AK_THREADS) {
-            if (threadIdx.x == 0)
-                nslot = 0;
-            __syncthreads();
-            gather_slots(S, B, bd, org, stroke, true, h, base + threadIdx.x, p1, slots, &nslot);
-            __syncthreads();
-            int ne = nslot * E;
-            for (int t = threadIdx.x; t < ne; t += AK_THREADS) {
-                float2 a, b;
-                const ak_slot &sl = slots[t / E];
-                if (slot_edge(sl, stroke, t % E, a, b))
-                    edge_fwd(acc, bd, a, b, sl.o);
+    /* grid: layers by bands (one window), or one block per (tile, layer)
+       pair, which takes its box in bands as tall as the accumulator holds at
+       the box's width (most glyph boxes in one) */
+    uint32_t       lg;
+    float         *plane;
+    const ak_win   w    = ak_cover_window(S, B, lg, plane);
+    const uint32_t bh   = S.tiles ? (S.band * (S.W + 1)) / (w.W + 1) : S.band;
+    const uint32_t nb   = S.tiles ? (w.H + bh - 1) / bh : 1u;
+    const int      W1   = w.W + 1;
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const float2   org  = v2((float)w.x0, (float)w.y0);
+    for (uint32_t bi = 0; bi < nb; bi++) {
+        const uint32_t band = S.tiles ? bi : blockIdx.y;
+        ak_band        bd{(int)(band * bh), 0, (int)w.W, B.status};
+        bd.y1    = min((int)w.H, bd.y0 + (int)bh);
+        int rows = bd.y1 - bd.y0;
+        __syncthreads(); /* the previous band's prefix sums have read the accumulator */
+        for (int i = threadIdx.x; i < rows * W1; i += AK_THREADS)
+            acc[i] = 0;
+        if (B.off[S.nseg] <= B.cap) {
+            uint32_t p = S.layer_path[lg];
+            bool     stroke = S.layer_stroke[lg] != 0;
+            int      E      = stroke ? 7 : 1;
+            float    h      = 0.5f * widths[p];
+            uint32_t p1     = B.off[S.path_s0[p + 1]];
+            for (uint32_t base = B.off[S.path_s0[p]]; base < p1; base += AK_THREADS) {
+                if (threadIdx.x == 0)
+                    nslot = 0;
+                __syncthreads();
+                gather_slots(S, B, bd, org, stroke, true, h, base + threadIdx.x, p1, slots, &nslot);
+                __syncthreads();
+                int ne = nslot * E;
+                for (int t = threadIdx.x; t < ne; t += AK_THREADS) {
+                    float2 a, b;
+                    const ak_slot &sl = slots[t / E];
+                    if (slot_edge(sl, stroke, t % E, a, b))
+                        edge_fwd(acc, bd, a, b, sl.o);
+                }
+                __syncthreads();
             }
-            __syncthreads();
         }
-    }
-    __syncthreads();
-    /* row prefix sums, one warp per row, 32 cells per step */
-    uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    float   *out  = plane + (size_t)bd.y0 * w.W;
-    for (int r = warp; r < rows; r += AK_THREADS / 32) {
-        int carry = 0;
-        for (uint32_t c = 0; c < w.W; c += 32) {
-            uint32_t i = c + lane;
-            int      x = i < w.W ? acc[r * W1 + i] : 0;
+        __syncthreads();
+        /* row prefix sums, one warp per row, 32 cells per step */
+        float *out = plane + (size_t)bd.y0 * w.W;
+        for (int r = warp; r < rows; r += AK_THREADS / 32) {
+            int carry = 0;
+            for (uint32_t c = 0; c < w.W; c += 32) {
+                uint32_t i = c + lane;
+                int      x = i < w.W ? acc[r * W1 + i] : 0;
 #pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                int t = __shfl_up_sync(0xffffffffu, x, o);
-                if (lane >= (uint32_t)o)
-                    x += t;
+                for (int o = 1; o < 32; o <<= 1) {
+                    int t = __shfl_up_sync(0xffffffffu, x, o);
+                    if (lane >= (uint32_t)o)
+                        x += t;
+                }
+                if (i < w.W)
+                    out[(size_t)r * w.W + i] = (float)(carry + x) * AK_FIX_INV;
+                carry += __shfl_sync(0xffffffffu, x, 31);
             }
-            if (i < w.W)
-                out[(size_t)r * w.W + i] = (float)(carry + x) * AK_FIX_INV;
-            carry += __shfl_sync(0xffffffffu, x, 31);
         }
     }
 }
@@ -765,25 +772,30 @@ __global__ void __launch_bounds__(AK_THREADS)
     float   *gs    = reinterpret_cast<float *>(eg + AK_THREADS * 7);
     __shared__ float red[AK_THREADS / 32];
     __shared__ int   nslot;
-    uint32_t         lg;
-    float           *plane;
-    const ak_win     w = ak_cover_window(S, B, lg, plane);
-    if (blockIdx.y * S.band >= w.H)
-        return; /* a band below the window */
-    ak_band bd{(int)(blockIdx.y * S.band), 0, (int)w.W, B.status};
-    bd.y1             = min((int)w.H, bd.y0 + (int)S.band);
-    int          rows = bd.y1 - bd.y0;
-    const float *src  = plane + (size_t)bd.y0 * w.W;
-    for (int i = threadIdx.x; i < rows * (int)w.W; i += AK_THREADS)
-        gs[i] = src[i];
+    /* the grid of ak_cover: a pair's block takes its box in bands as tall as
+       the gradient buffer holds at the box's width */
+    uint32_t       lg;
+    float         *plane;
+    const ak_win   w  = ak_cover_window(S, B, lg, plane);
+    const uint32_t bh = S.tiles ? (S.band * S.W) / w.W : S.band;
+    const uint32_t nb = S.tiles ? (w.H + bh - 1) / bh : 1u;
     if (B.off[S.nseg] > B.cap)
         return;
-    const float2   org = v2((float)w.x0, (float)w.y0);
-    uint32_t p      = S.layer_path[lg];
-    bool     stroke = S.layer_stroke[lg] != 0;
-    int      E      = stroke ? 7 : 1;
-    float    h      = 0.5f * widths[p], gh = 0.f;
-    uint32_t p1     = B.off[S.path_s0[p + 1]];
+    const float2 org    = v2((float)w.x0, (float)w.y0);
+    uint32_t     p      = S.layer_path[lg];
+    bool         stroke = S.layer_stroke[lg] != 0;
+    int          E      = stroke ? 7 : 1;
+    float        h      = 0.5f * widths[p], gh = 0.f;
+    uint32_t     p1     = B.off[S.path_s0[p + 1]];
+    for (uint32_t bi = 0; bi < nb; bi++) {
+    const uint32_t band = S.tiles ? bi : blockIdx.y;
+    ak_band        bd{(int)(band * bh), 0, (int)w.W, B.status};
+    bd.y1             = min((int)w.H, bd.y0 + (int)bh);
+    int          rows = bd.y1 - bd.y0;
+    const float *src  = plane + (size_t)bd.y0 * w.W;
+    __syncthreads(); /* the previous band's edges have read the buffer */
+    for (int i = threadIdx.x; i < rows * (int)w.W; i += AK_THREADS)
+        gs[i] = src[i];
     for (uint32_t base = B.off[S.path_s0[p]]; base < p1; base += AK_THREADS) {
         if (threadIdx.x == 0)
             nslot = 0;
@@ -848,6 +860,7 @@ __global__ void __launch_bounds__(AK_THREADS)
         }
         __syncthreads();
     }
+    } /* bands */
     if (stroke) {
         float s = block_sum<AK_THREADS>(gh, red);
         if (threadIdx.x == 0 && s != 0.f)
@@ -1003,8 +1016,8 @@ cudaError_t ak_launch_cover(cudaStream_t st, const ak_scene &S, const ak_bufs &B
     size_t smem = cover_fwd_smem(S.W, S.band);
     if (smem > 48 * 1024)
         cudaFuncSetAttribute(ak_cover, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (S.nlayers)
-        ak_cover<<<dim3(S.nlayers, S.nbands), AK_THREADS, smem, st>>>(S, B, widths);
+    if (S.nlayers) /* tiled: one block per pair, which walks its box's bands */
+        ak_cover<<<dim3(S.nlayers, S.tiles ? 1u : S.nbands), AK_THREADS, smem, st>>>(S, B, widths);
     return cudaGetLastError();
 }
 static uint32_t windows(const ak_scene &S) { return S.tiles ? S.ntiles : 1u; }
@@ -1030,7 +1043,7 @@ cudaError_t ak_launch_cover_bwd(cudaStream_t st, const ak_scene &S, const ak_buf
     if (smem > 48 * 1024)
         cudaFuncSetAttribute(ak_cover_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (S.nlayers)
-        ak_cover_bwd<<<dim3(S.nlayers, S.nbands), AK_THREADS, smem, st>>>(S, B, widths, gpts, gwidth);
+        ak_cover_bwd<<<dim3(S.nlayers, S.tiles ? 1u : S.nbands), AK_THREADS, smem, st>>>(S, B, widths, gpts, gwidth);
     return cudaGetLastError();
 }
 cudaError_t ak_launch_reduce(cudaStream_t st, const ak_scene &S, uint32_t nblocks, const float4 *color_part,
