@@ -187,7 +187,7 @@ def cpu_sample(n_paths, size, threads, reps=1):
     return n_paths / min(times), min(times)
 
 
-def analytic_glyph_bench(a, gb, torch, np, flush, tile=128):
+def analytic_glyph_bench(a, gb, torch, np, flush, tile=128, cpu=False):
     """The large glyph configuration in the differentiable analytic mode
     (4096x4096 fp32 canvas, 200,000 quadratic outlines elevated to cubics,
     20,000 closed strokes, seed 5; the target is the same construction from
@@ -259,9 +259,57 @@ def analytic_glyph_bench(a, gb, torch, np, flush, tile=128):
            "outline_grad_norm": {"on_curve": float(np.linalg.norm(gP)), "off_curve": float(np.linalg.norm(gQ))},
            "timing": "CUDA events on the scene's stream, L2 flushed before each, median of 3",
            "checked": "tests/test_analytic.py: tiled == whole canvas; the construction on a 192x192 crop against the "
-                      "FP64 reference"}
+                      "FP64 reference; outline gradients on a 128x128 crop against FP64 central differences"}
     A.destroy()
+    if cpu:
+        out["grad_error_crop"] = glyph_crop_fd(gb, torch, np, scenes)
     return out
+
+
+def glyph_crop_fd(gb, torch, np, scenes, n=24):
+    """The glyph construction on a 128x128 crop (200 outlines, 20 strokes,
+    tiles of 64): the GPU gradients of n random outline coordinates
+    (on-curve and off-curve points, through the quadratic elevation)
+    against FP64 central differences of the CPU reference at h = 1e-3 px
+    (coordinates whose differences at h and 10 h disagree, a flattening that
+    changes within h, are replaced by the next draw)."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import analytic_ref as ar
+
+    scene, par, quad = scenes.analytic_glyph_scene(n_outlines=200, n_strokes=20, size=128)
+    tscene, tpar, _ = scenes.analytic_glyph_scene(seed=6, n_outlines=200, n_strokes=20, size=128)
+    target, _ = ar.Reference(tscene).forward(tpar["ctrl"], tpar["colors"], tpar["widths"])
+    R = ar.Reference(scene)
+    A = gb.Analytic(scene, tile=64)
+    d = {k: torch.tensor(v, device="cuda") for k, v in par.items()}
+    A.forward(d["ctrl"], d["colors"], d["widths"], torch.tensor(target.astype(np.float32), device="cuda"))
+    gc = A.backward()[0].cpu().numpy().astype(np.float64)
+    assert A.sync() == 0
+    A.destroy()
+    gP, gQ = scenes.elevate_adjoint(quad, gc)
+
+    def fd(which, k, axis, h):
+        out = []
+        for sgn in (1.0, -1.0):
+            P, Q = quad["P"].astype(np.float64), quad["Q"].astype(np.float64)
+            (P if which == 0 else Q)[k, axis] += sgn * h
+            out.append(R.forward(scenes.elevate(quad, P, Q), par["colors"], par["widths"], target)[1])
+        return (out[0] - out[1]) / (2 * h)
+
+    rng = np.random.default_rng(7)
+    rows, skipped = [], 0
+    while len(rows) < n:
+        which, k, axis = int(rng.integers(2)), int(rng.integers(len(quad["P"]))), int(rng.integers(2))
+        f1, f2 = fd(which, k, axis, 1e-3), fd(which, k, axis, 1e-2)
+        if abs(f1 - f2) > 2e-3 * max(abs(f1), 1e-9):
+            skipped += 1
+            continue
+        rows.append(((gP if which == 0 else gQ)[k, axis], f1))
+    an, ref = np.array(rows).T
+    err = np.abs(an - ref) / np.maximum(np.abs(ref), 1e-3 * np.abs(ref).max())
+    return {"max_rel": float(err.max()), "median_rel": float(np.median(err)), "coordinates": n,
+            "not_smooth_replaced": skipped, "h_px": 1e-3,
+            "rel": "|g - fd| / max(|fd|, 1e-3 max|fd|)", "crop": "128x128, 200 outlines, 20 strokes, tiles of 64"}
 
 
 def cpu_scene_time(sc, threads, reps=3):
@@ -675,7 +723,7 @@ def main():
     if a.analytic_glyphs_only:
         buf = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
         gb._build.build()
-        print(json.dumps(analytic_glyph_bench(a, gb, torch, np, buf.zero_)))
+        print(json.dumps(analytic_glyph_bench(a, gb, torch, np, buf.zero_, cpu=not a.no_cpu)))
         return
     dist = None
     if world > 1:
@@ -856,7 +904,7 @@ def main():
     if not a.no_analytic and world == 1:
         analytic = analytic_bench(a, gb, torch, np, l2_flush, cpu=rank == 0 and not a.no_cpu)
         if not a.no_glyphs:
-            analytic["glyphs"] = analytic_glyph_bench(a, gb, torch, np, l2_flush)
+            analytic["glyphs"] = analytic_glyph_bench(a, gb, torch, np, l2_flush, cpu=rank == 0 and not a.no_cpu)
 
     # ---- the small polygon configuration as stated
     small = small_polygon_bench(a, gb, L, np, l2_flush) if world == 1 else None

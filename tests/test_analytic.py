@@ -478,6 +478,51 @@ def test_gpu_tiled_matches_whole_canvas(gb, tile):
         assert err < 1e-4, (name, err)
 
 
+def _quad_fd(R, scene, quad, par, target, which, k, axis, h):
+    """FP64 central difference of the loss in one outline coordinate (an
+    on-curve point, which 0, or an off-curve one, which 1) through the
+    quadratic elevation"""
+    out = []
+    for sgn in (1.0, -1.0):
+        P, Q = quad["P"].astype(np.float64), quad["Q"].astype(np.float64)
+        (P if which == 0 else Q)[k, axis] += sgn * h
+        ctrl = scenes.elevate(quad, P, Q)  # float64 points: elevated in float64
+        out.append(R.forward(ctrl, par["colors"], par["widths"], target)[1])
+    return (out[0] - out[1]) / (2 * h)
+
+
+@pytest.mark.gpu
+def test_gpu_glyph_crop_outline_gradients_match_fd(gb):
+    """the glyph construction on a 128 x 128 crop, tiled: the gradients of 24
+    random outline coordinates (on-curve and off-curve points, through the
+    quadratic elevation) against FP64 central differences at h = 1e-3 px,
+    relative error |g - fd| / max(|fd|, 1e-3 max|fd|) within the analytic
+    mode's bar; a coordinate whose differences at h and h/10 disagree (a
+    flattening that changes within h: not differentiable there) is replaced
+    by the next draw"""
+    scene, par, quad = scenes.analytic_glyph_scene(n_outlines=200, n_strokes=20, size=128)
+    tscene, tpar, _ = scenes.analytic_glyph_scene(seed=6, n_outlines=200, n_strokes=20, size=128)
+    target, _ = ar.Reference(tscene).forward(tpar["ctrl"], tpar["colors"], tpar["widths"])
+    R = ar.Reference(scene)
+    _, _, (gc, _, _) = _gpu_eval_tiled(gb, scene, par, target, 64)
+    gP, gQ = scenes.elevate_adjoint(quad, gc)
+    rng = np.random.default_rng(7)
+    n = len(quad["P"])
+    rows = []
+    while len(rows) < 24:
+        which, k, axis = int(rng.integers(2)), int(rng.integers(n)), int(rng.integers(2))
+        f1 = _quad_fd(R, scene, quad, par, target, which, k, axis, 1e-3)
+        f2 = _quad_fd(R, scene, quad, par, target, which, k, axis, 1e-2)
+        if abs(f1 - f2) > 2e-3 * max(abs(f1), 1e-9):
+            continue  # not smooth within h
+        rows.append(((gP if which == 0 else gQ)[k, axis], f1))
+    an, fd = np.array(rows).T
+    floor = 1e-3 * np.abs(fd).max()
+    err = rel_err(an, fd, floor)
+    print("glyph crop outline FD check: max rel err %.3g, median %.3g" % (err.max(), np.median(err)))
+    assert err.max() < GRAD_TOL
+
+
 @pytest.mark.gpu
 def test_gpu_small_curves_flatten_bit_exact(gb):
     """scenes of small curves (the glyph construction: a few points per

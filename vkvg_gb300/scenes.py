@@ -922,13 +922,15 @@ def analytic_glyph_scene(seed=5, n_outlines=200000, n_strokes=20000, size=4096, 
 def elevate(quad, P=None, Q=None):
     """cubic control points [segments * 3][2] of the quadratic segments
     (start p, p + 2/3 (q - p), p' + 2/3 (q - p') with p' the next on-curve
-    point), in float32"""
+    point), in float32, or in float64 when P or Q is float64"""
     import numpy as np
 
-    P = np.asarray(quad["P"] if P is None else P, np.float32)
-    Q = np.asarray(quad["Q"] if Q is None else Q, np.float32)
-    t = np.float32(2.0 / 3.0)
-    out = np.empty((len(P), 3, 2), np.float32)
+    P = quad["P"] if P is None else P
+    Q = quad["Q"] if Q is None else Q
+    dt = np.float64 if np.float64 in (np.asarray(P).dtype, np.asarray(Q).dtype) else np.float32
+    P, Q = np.asarray(P, dt), np.asarray(Q, dt)
+    t = dt(2.0 / 3.0)
+    out = np.empty((len(P), 3, 2), dt)
     out[:, 0] = P
     np.subtract(Q, P, out=out[:, 1])
     out[:, 1] *= t
