@@ -73,6 +73,8 @@ def parse():
     p.add_argument("--no-analytic", action="store_true", help="skip the differentiable analytic-coverage workload")
     p.add_argument("--no-glyphs", action="store_true", help="skip the 4096x4096 glyph workload")
     p.add_argument("--svg-shapes", type=int, default=600, help="shapes of the SVG ingestion workload (0: skip)")
+    p.add_argument("--glyph-size", type=int, default=4096,
+                   help="side of the glyph workload; smaller sides keep its density (profiling crops)")
     p.add_argument("--analytic-glyphs-only", action="store_true",
                    help="run only the glyph scene's analytic forward + backward and print its entry (profiling)")
     p.add_argument("--adam-steps", type=int, default=200, help="Adam steps of the differentiable workload")
@@ -583,7 +585,9 @@ def glyph_bench(a, gb, L, np, flush):
     from vkvg_gb300 import scenes
 
     t0 = time.perf_counter()
-    g = scenes.glyph_streams(seed=5)
+    side = a.glyph_size  # a crop keeps the scene's density
+    dens = (side / 4096.0) ** 2
+    g = scenes.glyph_streams(seed=5, size=side, n_outlines=int(200000 * dens), n_strokes=int(20000 * dens))
     gen_s = time.perf_counter() - t0
     cm, ar = g["cmds"], g["args"]
     size = g["width"]
@@ -631,8 +635,8 @@ def glyph_bench(a, gb, L, np, flush):
         e2e()
     e_ms = (time.perf_counter() - t0) / 2 * 1e3
     paths = g["outlines"] + g["strokes"]
-    out = {"workload": "glyphs 4096x4096 msaa4 (seed 5): %d quadratic outlines with holes (NON_ZERO), %d round-join "
-                       "strokes, %d quads, one linear gradient" % (g["outlines"], g["strokes"], g["quads"]),
+    out = {"workload": "glyphs %dx%d msaa4 (seed 5): %d quadratic outlines with holes (NON_ZERO), %d round-join "
+                       "strokes, %d quads, one linear gradient" % (size, size, g["outlines"], g["strokes"], g["quads"]),
            "paths_per_s": paths / (ms / 1e3), "ms_per_frame": ms, "mpx_per_s": size * size / (ms / 1e3) / 1e6,
            "stage_ms": {"flatten": tot[0] / n, "stroke": tot[1] / n, "setup_bin": tot[2] / n, "raster": tot[3] / n},
            "flattened_points": int(stats[1]), "stroke_vertices": int(stats[2]), "bin_units": int(stats[5]),
