@@ -547,12 +547,16 @@ __device__ __forceinline__ float block_sum(float v, float *red) {
     return s;
 }
 
+/* TILED: the tiles of a tiled scene (layers read through their planes'
+   boxes, per-chunk lists of the layers reaching the block); else the one
+   window, every layer's plane the whole canvas */
+template <bool TILED>
 __global__ void __launch_bounds__(AK_THREADS)
     ak_composite(ak_scene S, ak_bufs B, const float4 *__restrict__ colors, const float4 *__restrict__ target,
                  float *__restrict__ loss_part) {
     __shared__ float4   col[AK_CHUNK];
-    __shared__ ak_plane pl[AK_CHUNK];
-    __shared__ uint8_t  act[AK_CHUNK];
+    __shared__ ak_plane pl[TILED ? AK_CHUNK : 1];
+    __shared__ uint8_t  act[TILED ? AK_CHUNK : 1];
     __shared__ int      nact;
     __shared__ float    red[AK_THREADS / 32];
     /* grid: the window's pixel blocks, window after window */
@@ -569,29 +573,35 @@ __global__ void __launch_bounds__(AK_THREADS)
     for (uint32_t lb = 0; lb < w.nl; lb += AK_CHUNK) {
         uint32_t n = min((uint32_t)AK_CHUNK, w.nl - lb);
         __syncthreads();
-        if (threadIdx.x < 32) {
+        if (TILED && threadIdx.x < 32) {
             ak_plane P{};
             if (threadIdx.x < n) {
                 col[threadIdx.x] = colors[S.layer_path[ak_layer(S, w, lb + threadIdx.x)]];
                 pl[threadIdx.x]  = P = ak_plane_of(S, w, lb + threadIdx.x);
             }
             ak_chunk_active(P, threadIdx.x < n, ry0, ry1, act, &nact);
+        } else if (!TILED && threadIdx.x < n) {
+            col[threadIdx.x] = colors[S.layer_path[lb + threadIdx.x]];
         }
         __syncthreads();
         if (!valid)
             continue;
         ckpt[(size_t)(lb / AK_CHUNK) * np + px] = C;
-        const int na = nact;
+        const int na = TILED ? nact : (int)n;
         float     A[AK_CHUNK];
 #pragma unroll
         for (int i = 0; i < AK_CHUNK; i++) {
-            const long long k = i < na ? ak_plane_at(pl[act[i]], x, y) : -1ll;
-            A[i]              = k >= 0 ? B.area[k] : 0.f;
+            if (TILED) {
+                const long long k = i < na ? ak_plane_at(pl[act[i]], x, y) : -1ll;
+                A[i]              = k >= 0 ? B.area[k] : 0.f;
+            } else {
+                A[i] = i < na ? B.area[(size_t)(lb + i) * np + px] : 0.f;
+            }
         }
 #pragma unroll
         for (int i = 0; i < AK_CHUNK; i++)
             if (i < na)
-                C = blend(cover(A[i]), col[act[i]], C);
+                C = blend(cover(A[i]), col[TILED ? act[i] : i], C);
     }
     float        s  = 0.f;
     const size_t cp = valid ? ((size_t)w.y0 + px / w.W) * S.CW + w.x0 + px % w.W : 0; /* on the canvas */
@@ -642,12 +652,13 @@ __device__ __forceinline__ float warp_reduce_scatter32(float (&v)[32]) {
 
 #define AK_CB_THREADS 128 /* pixels per compositing-adjoint block */
 
+template <bool TILED>
 __global__ void __launch_bounds__(AK_CB_THREADS)
     ak_composite_bwd(ak_scene S, ak_bufs B, const float4 *__restrict__ colors, const float4 *__restrict__ target,
                      const float4 *__restrict__ d_canvas, float *__restrict__ color_part) {
     __shared__ float4   col[AK_CHUNK];
-    __shared__ ak_plane pl[AK_CHUNK];
-    __shared__ uint8_t  act[AK_CHUNK];
+    __shared__ ak_plane pl[TILED ? AK_CHUNK : 1];
+    __shared__ uint8_t  act[TILED ? AK_CHUNK : 1];
     __shared__ int      nact;
     __shared__ float4 sB[AK_CHUNK][AK_CB_THREADS]; /* colour under each layer of the chunk */
     __shared__ float  sA[AK_CHUNK][AK_CB_THREADS]; /* the chunk's areas */
@@ -681,16 +692,18 @@ __global__ void __launch_bounds__(AK_CB_THREADS)
     for (uint32_t ch = nch; ch-- > 0;) {
         uint32_t lb = ch * AK_CHUNK, n = min((uint32_t)AK_CHUNK, w.nl - lb);
         __syncthreads();
-        if (threadIdx.x < 32) {
+        if (TILED && threadIdx.x < 32) {
             ak_plane P{};
             if (threadIdx.x < n) {
                 col[threadIdx.x] = colors[S.layer_path[ak_layer(S, w, lb + threadIdx.x)]];
                 pl[threadIdx.x]  = P = ak_plane_of(S, w, lb + threadIdx.x);
             }
             ak_chunk_active(P, threadIdx.x < n, ry0, ry1, act, &nact);
+        } else if (!TILED && threadIdx.x < n) {
+            col[threadIdx.x] = colors[S.layer_path[lb + threadIdx.x]];
         }
         __syncthreads();
-        const int na = nact; /* the chunk's active layers act[0, na), in order */
+        const int na = TILED ? nact : (int)n; /* the chunk's active layers act[0, na), in order */
         if (na == 0)
             continue; /* every layer of the chunk leaves these pixels alone */
         float4 Bc = valid ? ckpt[(size_t)ch * np + px] : make_float4(0.f, 0.f, 0.f, 0.f);
@@ -698,15 +711,19 @@ __global__ void __launch_bounds__(AK_CB_THREADS)
             float A[AK_CHUNK];
 #pragma unroll
             for (int i = 0; i < AK_CHUNK; i++) {
-                const long long k = (valid && i < na) ? ak_plane_at(pl[act[i]], x, y) : -1ll;
-                A[i]              = k >= 0 ? B.area[k] : 0.f;
+                if (TILED) {
+                    const long long k = (valid && i < na) ? ak_plane_at(pl[act[i]], x, y) : -1ll;
+                    A[i]              = k >= 0 ? B.area[k] : 0.f;
+                } else {
+                    A[i] = (valid && i < na) ? B.area[(size_t)(lb + i) * np + px] : 0.f;
+                }
             }
 #pragma unroll
             for (int i = 0; i < AK_CHUNK; i++) {
                 if (i < na) {
                     sB[i][threadIdx.x] = Bc;
                     sA[i][threadIdx.x] = A[i];
-                    Bc                 = blend(cover(A[i]), col[act[i]], Bc);
+                    Bc                 = blend(cover(A[i]), col[TILED ? act[i] : i], Bc);
                 }
             }
         }
@@ -722,7 +739,7 @@ __global__ void __launch_bounds__(AK_CB_THREADS)
                 dc[4 * q8] = dc[4 * q8 + 1] = dc[4 * q8 + 2] = dc[4 * q8 + 3] = 0.f;
                 if (i >= na)
                     continue;
-                const int q  = act[i];
+                const int q  = TILED ? act[i] : i;
                 float4    c  = col[q], Bq = sB[i][threadIdx.x];
                 float     Aq = sA[i][threadIdx.x];
                 float  al = cover(Aq);
@@ -731,7 +748,7 @@ __global__ void __launch_bounds__(AK_CB_THREADS)
                 float  da = T * (gc - c.w * gB);
                 float  gA = fabsf(Aq) < 1.f ? (Aq > 0.f ? da : Aq < 0.f ? -da : 0.f) : 0.f;
                 if (valid) {
-                    const long long k = ak_plane_at(pl[q], x, y);
+                    const long long k = TILED ? ak_plane_at(pl[q], x, y) : (long long)((size_t)(lb + q) * np + px);
                     if (k >= 0)
                         B.area[k] = gA;
                 }
@@ -748,7 +765,7 @@ __global__ void __launch_bounds__(AK_CB_THREADS)
             for (int k = 0; k < AK_CB_THREADS / 32; k++)
                 s += red[k][threadIdx.x];
             /* one window: [block][layer][channel]; tiled: [pair][block of the tile][channel] */
-            const uint32_t q = act[threadIdx.x >> 2], c = threadIdx.x & 3;
+            const uint32_t q = TILED ? act[threadIdx.x >> 2] : threadIdx.x >> 2, c = threadIdx.x & 3;
             const size_t   i = S.tiles ? ((size_t)(w.first + lb + q) * bpw + b) * 4 + c
                                        : ((size_t)b * S.nlayers + lb + q) * 4 + c;
             color_part[i] = s;
@@ -1024,7 +1041,10 @@ static uint32_t windows(const ak_scene &S) { return S.tiles ? S.ntiles : 1u; }
 uint32_t ak_pixel_blocks_all(const ak_scene &S) { return ak_pixel_blocks(S) * windows(S); }
 cudaError_t ak_launch_composite(cudaStream_t st, const ak_scene &S, const ak_bufs &B, const float4 *colors,
                                 const float4 *target, float *loss_part) {
-    ak_composite<<<ak_pixel_blocks_all(S), AK_THREADS, 0, st>>>(S, B, colors, target, loss_part);
+    if (S.tiles)
+        ak_composite<true><<<ak_pixel_blocks_all(S), AK_THREADS, 0, st>>>(S, B, colors, target, loss_part);
+    else
+        ak_composite<false><<<ak_pixel_blocks_all(S), AK_THREADS, 0, st>>>(S, B, colors, target, loss_part);
     return cudaGetLastError();
 }
 uint32_t ak_composite_bwd_blocks(const ak_scene &S) {
@@ -1033,8 +1053,12 @@ uint32_t ak_composite_bwd_blocks(const ak_scene &S) {
 size_t ak_color_partials(const ak_scene &S) { return (size_t)ak_composite_bwd_blocks(S) * S.nlayers; }
 cudaError_t ak_launch_composite_bwd(cudaStream_t st, const ak_scene &S, const ak_bufs &B, const float4 *colors,
                                     const float4 *target, const float4 *d_canvas, float4 *color_part) {
-    ak_composite_bwd<<<ak_composite_bwd_blocks(S) * windows(S), AK_CB_THREADS, 0, st>>>(
-        S, B, colors, target, d_canvas, reinterpret_cast<float *>(color_part));
+    if (S.tiles)
+        ak_composite_bwd<true><<<ak_composite_bwd_blocks(S) * windows(S), AK_CB_THREADS, 0, st>>>(
+            S, B, colors, target, d_canvas, reinterpret_cast<float *>(color_part));
+    else
+        ak_composite_bwd<false><<<ak_composite_bwd_blocks(S), AK_CB_THREADS, 0, st>>>(
+            S, B, colors, target, d_canvas, reinterpret_cast<float *>(color_part));
     return cudaGetLastError();
 }
 cudaError_t ak_launch_cover_bwd(cudaStream_t st, const ak_scene &S, const ak_bufs &B, const float *widths,
