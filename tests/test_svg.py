@@ -126,6 +126,28 @@ def test_parser_matches_nanosvg_on_seeded_documents(gbl):
     assert same > 0.9 * total  # most coordinates are bit-identical as well
 
 
+@pytest.mark.parametrize("name", ["seed1", "seed2", "seed3", "seed4", "quirks5", "quirks6"])
+def test_render_of_reader_parse_equals_render_of_nanosvg_parse(gbl, vko, name):
+    """vkvg's walk over this reader's shapes and over nanoSVG's (the
+    fixtures), both rendered by the oracle at 4x MSAA: the same image, byte
+    for byte (the GPU equals the oracle on the reader's shapes,
+    test_svg_render_bit_exact)"""
+    mg = _golden()
+    text = dict(mg.documents())[name]
+    g = np.load(os.path.join(GOLDEN, "svg_%s.npz" % name))
+    (w, h), mine = _parse(gbl, text)
+    imgs = []
+    for shapes in (mg.unpack(g), mine):
+        o = vko.OracleSurface(w, h, 4)
+        c = o.context()
+        c.set_source_rgb(1.0, 1.0, 1.0)
+        c.paint()
+        svg_render.render(c, shapes)
+        c.flush()
+        imgs.append(o.image())
+    assert np.array_equal(imgs[0], imgs[1])
+
+
 def _one(gbl, body, size='width="100" height="100"'):
     (w, h), shapes = _parse(gbl, ('<svg %s>%s</svg>' % (size, body)).encode())
     return (w, h), shapes
