@@ -524,6 +524,22 @@ def test_gpu_glyph_crop_outline_gradients_match_fd(gb):
 
 
 @pytest.mark.gpu
+def test_gpu_tiled_pairs_beyond_32_bits_report_no_memory(gb):
+    """a tiled scene whose (tile, layer) entries reach 2^32 (65,536 tiles of
+    16 px on a 4096 x 4096 canvas by 65,536 layers): the forward reports
+    VKVG_STATUS_NO_MEMORY before sizing anything, and the scene stays usable
+    for its status"""
+    scene, par = scenes.analytic_scene(seed=9, n_paths=32768, n_cubics=1, size=4096)
+    A = gb.Analytic(scene, tile=16)
+    assert A.nlayers == 65536
+    p = {k: _dev(v) for k, v in par.items()}
+    with pytest.raises(gb.VkvgError, match="status 1"):
+        A.forward(p["ctrl"], p["colors"], p["widths"])
+    assert A.sync() == 1  # VKVG_STATUS_NO_MEMORY
+    A.destroy()
+
+
+@pytest.mark.gpu
 def test_gpu_small_curves_flatten_bit_exact(gb):
     """scenes of small curves (the glyph construction: a few points per
     segment) flatten one lane per segment: the points, their order and the

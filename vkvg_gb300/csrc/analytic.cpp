@@ -79,9 +79,12 @@ template <class T> bool upload(DevBuf &b, const std::vector<T> &v) {
 vkvg_status_t fail(VkvgAnalytic a, cudaError_t e) {
     if (e == cudaSuccess)
         return VKVG_STATUS_SUCCESS;
+    /* an allocation that failed (or a tiled scene whose pairs or planes
+       outgrow 32-bit offsets) is NO_MEMORY; anything else a device error */
+    const vkvg_status_t st = e == cudaErrorMemoryAllocation ? VKVG_STATUS_NO_MEMORY : VKVG_STATUS_DEVICE_ERROR;
     if (a->pending == VKVG_STATUS_SUCCESS)
-        a->pending = VKVG_STATUS_DEVICE_ERROR;
-    return VKVG_STATUS_DEVICE_ERROR;
+        a->pending = st;
+    return st;
 }
 
 bool size_points(VkvgAnalytic a, uint32_t need) {
