@@ -19,6 +19,11 @@ def available():
     return build_ref.available()
 
 
+def reference_dir():
+    """the reference tree the recipe reads (VKVG_REFERENCE or its default)"""
+    return build_ref.REFERENCE
+
+
 def lib():
     global _lib
     if _lib is None:

@@ -12,7 +12,7 @@ measures the difference at every stage:
 
 * cubics whose subdivision differs (point count or points);
 * draws whose vertex counts differ, and the largest vertex difference on
-  draws with equal counts (north-star bar 1e-3 px);
+  draws with equal counts (the vertex bar, 1e-3 px);
 * per-sample winding / covering counts of the draws whose geometry differs;
 * the final samples and image (bar: within 1/255 on 99.9 % of channels and
   within 2/255 everywhere).

@@ -217,7 +217,7 @@ def test_portable_math_vs_libm():
     """vkvg calls the C library's atan2f/acosf/cosf/sinf; the oracle and the
     kernels use one portable implementation so host and device agree bit for
     bit.  Measure what the substitution changes on a curve-and-stroke scene
-    and require it to stay inside the benchmark spec's tolerance for images
+    and require it to stay inside the drop-in's image tolerance
     (<= 1/255 on 99.9 % of pixel channels, <= 2/255 everywhere)."""
     sc = scenes.curve_heavy(n_paths=24, size=192, seed=1, n_min=3, n_max=8)
     L = ob.lib()

@@ -25,7 +25,7 @@ import svg_render
 from vkvg_gb300 import scenes
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-REFERENCE = os.environ.get("VKVG_REFERENCE", "/root/reference")
+REFERENCE = nsvg_ref.reference_dir()  # the reference tree, where present (oracle/build_ref.py)
 REF_FILES = sorted(glob.glob(os.path.join(REFERENCE, "tests", "data", "*.svg")) +
                    glob.glob(os.path.join(REFERENCE, "doc", "*.svg")) +
                    glob.glob(os.path.join(REFERENCE, "doc", "images", "*.svg")))
