@@ -230,7 +230,8 @@ cudaError_t run_batch(VkvgBatch b, bool sized, const RasterParams &p) {
     bool wide = false; /* the draws' x extents, for every tile width a candidate uses (down to 128 pixels) */
     for (const gb_surf &s : b->tab)
         wide |= s.W > gb_raster_tile_width(3);
-    BCK(pl.geometry(b->merged, b->d_tab.as<gb_surf>(), b->ncells, b->every, wide, b->samples, false, sized));
+    BCK(pl.geometry(b->merged, b->d_tab.as<gb_surf>(), (uint32_t)b->tab.size(), b->ncells, b->every, wide,
+                    b->samples, false, sized));
     if (!sized)
         BCK(build_items(b));
     const int      nw   = p.form;

@@ -140,6 +140,7 @@ typedef struct {
 
 /* bands: 16 sample rows (4 pixel rows at 4x MSAA, 16 at 1x) */
 #define GB_BAND_ROWS 16
+#define GB_CELL_EVERY 0x80000000u /* a (band, draw) cell count's mark: the draw acts on every band */
 #define GB_RASTER_TILE_W 1024 /* pixels of a raster tile (one CTA's columns) */
 #define GB_TILE_W    256
 

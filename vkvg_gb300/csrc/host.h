@@ -127,9 +127,9 @@ struct Pipeline {
     /* every_cells: the cells of the draws that act on every band of their
        surface (kinds after STROKE), a bound the draw lists are sized by;
        wide: a surface is wider than one raster tile (the raster then reads
-       the draws' x extents) */
-    cudaError_t geometry(const FrameHost &f, const gb_surf *surfs, uint64_t ncells, uint64_t every_cells, bool wide,
-                         uint32_t S, bool timing, bool sized);
+       the draws' x extents); surfs: the nsurf surfaces' table on the device */
+    cudaError_t geometry(const FrameHost &f, const gb_surf *surfs, uint32_t nsurf, uint64_t ncells,
+                         uint64_t every_cells, bool wide, uint32_t S, bool timing, bool sized);
     /* K1 only: flatten the uploaded segments (for vkvg_path_extents) */
     cudaError_t flatten_only();
 };

@@ -113,21 +113,33 @@ cudaError_t gb_launch_stroke_tris(cudaStream_t st, uint32_t ntris, uint32_t ndra
                                   const uint32_t *sdraw_id, const uint32_t *draw_vbase, const gb_draw *draws,
                                   const float2 *verts, const uint32_t *inds, const gb_surf *surfs, int4 *tri_a,
                                   int4 *tri_b, uint32_t *tri_draw, uint4 *tri_idx, int4 *edges, uint32_t *edge_draw);
+/* scatter 0: count each edge into its (band, draw) cells (and, where given,
+   fold the draws' x extents into dbox/dcnt, the record total into the 32
+   partial sums of total); scatter 1: write the records at the cells'
+   advancing offsets */
 cudaError_t gb_launch_bin(cudaStream_t st, int scatter, uint32_t nedges, const int4 *edges, const uint32_t *edge_draw,
                           const gb_draw *draws, const gb_surf *surfs, uint32_t samples, uint32_t *cell, int4 *recs,
                           uint32_t nunits, int2 *dbox, uint32_t *dcnt, unsigned long long *total);
-/* counts[c] = 1 in every band's cell of the draws that act on all bands
-   (kinds after STROKE): with the cells' record counts, the cells the raster
-   visits are then the nonzero entries */
+/* counts[c] |= GB_CELL_EVERY in every band's cell of the draws that act on
+   all bands (kinds after STROKE): with the cells' record counts, the cells
+   the raster visits are then the nonzero entries */
 cudaError_t gb_launch_cell_flags(cudaStream_t st, uint32_t ndraws, const gb_draw *draws, const gb_surf *surfs,
                                  uint32_t *counts);
 /* stats[0] += clipped pixel width x edges of each fill and stroke draw, stats[1] += its edges */
 cudaError_t gb_launch_draw_width_stats(cudaStream_t st, uint32_t ndraws, const gb_draw *draws, const int2 *dbox,
                                        const uint32_t *dcnt, uint32_t W, unsigned long long *stats);
-/* *mx = max(*mx, cnt[0 .. ncells)) */
-cudaError_t gb_launch_cells_max(cudaStream_t st, uint32_t ncells, const uint32_t *cnt, uint32_t *mx);
-/* alist[pos[c]] = c for the cells whose pos[c + 1] != pos[c] */
-cudaError_t gb_launch_cell_compact(cudaStream_t st, uint32_t ncells, const uint32_t *pos, uint32_t *alist);
+/* From the cells' counts (bit 31: GB_CELL_EVERY), in two launchers over the
+   same scratch (gb_cells_scratch_words(ncells)): _reduce sums each tile of
+   cells (records, active cells) and folds the heaviest cell into *mx where
+   given; _lists then writes off[c] = the exclusive sum of the record counts
+   before cell c, off[ncells] the total; alist = the active cells (nonzero
+   counts) in cell order; apos[c] = the number of active cells before c, at
+   every band's first cell of each of the nsurf surfaces and at ncells. */
+size_t      gb_cells_scratch_words(uint64_t ncells);
+cudaError_t gb_launch_cells_reduce(cudaStream_t st, uint64_t ncells, const uint32_t *counts, uint32_t *scratch,
+                                   uint32_t *mx);
+cudaError_t gb_launch_cells_lists(cudaStream_t st, uint64_t ncells, const uint32_t *counts, uint32_t *scratch,
+                                  uint32_t *off, uint32_t *alist, uint32_t *apos, const gb_surf *surfs, uint32_t nsurf);
 
 /* narrow: 1 the 256-pixel raster form (4 warps, 4 CTAs per SM), 2 the
    128-pixel one (2 warps, 8 CTAs per SM), 0 the 1024-pixel one (16 warps,

@@ -214,8 +214,8 @@ static cudaError_t scan(Pipeline &pl, const uint32_t *in, uint32_t n, uint32_t *
    frame into the cells of its surface table (ncells cells in all).  With
    sized, the sizes of a previous run of the same frame are reused and nothing
    is read back, so the sequence can be captured in a CUDA graph. */
-cudaError_t Pipeline::geometry(const FrameHost &f, const gb_surf *surfs, uint64_t ncells, uint64_t every_cells,
-                               bool wide, uint32_t S, bool timing, bool sized) {
+cudaError_t Pipeline::geometry(const FrameHost &f, const gb_surf *surfs, uint32_t nsurf, uint64_t ncells,
+                               uint64_t every_cells, bool wide, uint32_t S, bool timing, bool sized) {
     const uint8_t *I        = (const uint8_t *)in.p;
     auto           U        = [&](size_t o) { return (const uint32_t *)(I + o); };
     const uint32_t *seg_inf = U(o_seg_info);
@@ -372,45 +372,49 @@ cudaError_t Pipeline::geometry(const FrameHost &f, const gb_surf *surfs, uint64_
         CK(cudaMemsetAsync(dbox.p, 0x7F, (size_t)(ndraw + 1) * 8, st));
         CK(cudaMemsetAsync(dcnt, 0, (size_t)(ndraw + 1) * 4, st));
     }
-    /* status bytes 256-511: the record total in 64 bits, as 32 partial sums,
-       against the scan's wrap */
+    /* status bytes 256-511: the record total in 64 bits, as 32 partial
+       sums; a one-surface frame's edge-weighted mean draw width (status
+       words 4..7) and heaviest cell (word 8) pick the raster form */
     unsigned long long *total64 = (unsigned long long *)(status.as<uint8_t>() + 256);
+    const bool          stats   = stats_w && !sized;
     if (!sized)
         CK(cudaMemsetAsync(total64, 0, 256, st));
+    if (stats)
+        CK(cudaMemsetAsync(status.as<uint32_t>() + 4, 0, 20, st));
     CK(gb_launch_bin(st, 0, nedge_all, edges.as<int4>(), edge_draw.as<uint32_t>(), draws, surfs, S,
                      cells.as<uint32_t>(), nullptr, 0u, wide ? dbox.as<int2>() : nullptr, dcnt,
                      sized ? nullptr : total64));
     gb_count_launch(nedge_all ? 1 : 0);
-    /* a one-surface frame's edge-weighted mean draw width (status words 4..7)
-       and heaviest cell (word 8) pick the raster form */
-    const bool stats = stats_w && !sized;
-    if (stats) {
-        CK(cudaMemsetAsync(status.as<uint32_t>() + 4, 0, 20, st));
-        if (wide)
-            CK(gb_launch_draw_width_stats(st, ndraw, draws, dbox.as<int2>(), dcnt, stats_w,
-                                          (unsigned long long *)(status.as<uint32_t>() + 4)));
-        CK(gb_launch_cells_max(st, (uint32_t)ncells, cells.as<uint32_t>(), status.as<uint32_t>() + 8));
-        gb_count_launch((wide && ndraw ? 1 : 0) + (ncells ? 1 : 0));
+    if (stats && wide) {
+        CK(gb_launch_draw_width_stats(st, ndraw, draws, dbox.as<int2>(), dcnt, stats_w,
+                                      (unsigned long long *)(status.as<uint32_t>() + 4)));
+        gb_count_launch(ndraw ? 1 : 0);
     }
-    CK(scan(*this, cells.as<uint32_t>(), (uint32_t)ncells, cursor.as<uint32_t>() + 1));
+    /* the every-band draws' marks, then the cells' tile sums (an active cell
+       holds a record unit or belongs to an every-band draw) */
+    GROW(scratch, gb_cells_scratch_words(ncells) * 4 + 64);
+    CK(gb_launch_cell_flags(st, ndraw, draws, surfs, cells.as<uint32_t>()));
+    CK(gb_launch_cells_reduce(st, ncells, cells.as<uint32_t>(), scratch.as<uint32_t>(),
+                              stats ? status.as<uint32_t>() + 8 : nullptr));
+    gb_count_launch((ndraw ? 1 : 0) + (ncells ? 1 : 0));
     if (!sized) {
-        CK(cudaMemcpyAsync(rb.p, cursor.as<uint32_t>() + 1 + ncells, 4, cudaMemcpyDeviceToHost, st));
         CK(cudaMemcpyAsync((uint8_t *)rb.p + 256, total64, 256, cudaMemcpyDeviceToHost, st));
         if (stats)
             CK(cudaMemcpyAsync((uint8_t *)rb.p + 8, status.as<uint32_t>() + 4, 20, cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
         uint64_t ws[2] = {0, 0};
         uint32_t mxc   = 0;
-        memcpy(hv, rb.p, 4);
         memcpy(ws, (uint8_t *)rb.p + 8, 16);
         memcpy(&mxc, (uint8_t *)rb.p + 24, 4);
         uint64_t tot = 0, part[32];
         memcpy(part, (uint8_t *)rb.p + 256, 256);
         for (uint64_t v : part)
             tot += v;
-        if (tot != (uint64_t)hv[0]) /* more than 2^32 - 1 bin records: beyond the 32-bit offsets */
+        /* record offsets are 32-bit and a cell's count keeps bit 31 for its
+           every-band mark */
+        if (tot >= (uint64_t)GB_CELL_EVERY)
             return cudaErrorMemoryAllocation;
-        nunits   = hv[0];
+        nunits   = (uint32_t)tot;
         max_cell = stats ? mxc : 0xFFFFFFFFu;
         /* narrow tiles (256 pixels; 128 when every cell fits 128 units) when
            every cell fits the narrow form's staging buffer (480 units)
@@ -425,26 +429,18 @@ cudaError_t Pipeline::geometry(const FrameHost &f, const gb_surf *surfs, uint64_
         row_draws  = stats && wide && ws[1] && ws[0] > 640u * ws[1];
         mean_width = ws[1] ? (double)ws[0] / (double)ws[1] : 0.0;
     }
+    /* the cells' record offsets and the raster's per-band draw lists in one
+       more pass over the counts, then the records */
     GROW(recs, (size_t)(nunits + 1) * 16);
+    GROW(apos, (ncells + 1) * 4);
+    GROW(alist, (size_t)(nunits + every_cells + 1) * 4);
+    CK(gb_launch_cells_lists(st, ncells, cells.as<uint32_t>(), scratch.as<uint32_t>(), cursor.as<uint32_t>() + 1,
+                             alist.as<uint32_t>(), apos.as<uint32_t>(), surfs, nsurf));
+    gb_count_launch(ncells ? 2 : 0);
     CK(gb_launch_bin(st, 1, nedge_all, edges.as<int4>(), edge_draw.as<uint32_t>(), draws, surfs, S,
                      cursor.as<uint32_t>() + 1, recs.as<int4>(), nunits, nullptr, nullptr, nullptr));
     gb_count_launch(nedge_all ? 1 : 0);
     std::swap(cells, cursor); /* cells <- the offsets (kept for the raster); cursor is free */
-    /* the raster's per-band draw lists: the active cells, band-major, in
-       draw order, from the cells' record counts (now in cursor, a nonzero
-       count marks an active cell) and the every-band draws' cells */
-    GROW(apos, (ncells + 1) * 4);
-    CK(gb_launch_cell_flags(st, ndraw, draws, surfs, cursor.as<uint32_t>()));
-    if (!scratch.grow(gb_scan_scratch_words((uint32_t)ncells) * 4 + 64))
-        return cudaErrorMemoryAllocation;
-    CK(gb_exclusive_scan_flags(st, cursor.as<uint32_t>(), (uint32_t)ncells, apos.as<uint32_t>(),
-                               scratch.as<uint32_t>()));
-    gb_count_launch(ncells ? 3 : 0);
-    /* an active cell holds a record unit or belongs to an every-band draw */
-    GROW(alist, (size_t)(nunits + every_cells + 1) * 4);
-    CK(gb_launch_cell_compact(st, (uint32_t)ncells, apos.as<uint32_t>(), alist.as<uint32_t>()));
-    gb_count_launch(ncells ? 1 : 0);
-    gb_count_launch(ndraw ? 1 : 0);
     if (timing)
         CK(cudaEventRecord(evs[3], st));
     return cudaSuccess;
@@ -490,7 +486,7 @@ cudaError_t Pipeline::run(const FrameHost &f, _vkvg_surface_t *surf, bool timing
     for (const gb_draw &d : f.draws)
         every += d.kind > GB_DRAW_STROKE ? nbands : 0u;
     stats_w = W;
-    CK(geometry(f, surf_tab.as<gb_surf>(), (uint64_t)nbands * ndraw, every, W > gb_raster_tile_width(3), S, timing,
+    CK(geometry(f, surf_tab.as<gb_surf>(), 1u, (uint64_t)nbands * ndraw, every, W > gb_raster_tile_width(3), S, timing,
                 false));
     stats_w = 0;
 

@@ -358,43 +358,210 @@ __global__ void gb_draw_width_stats(uint32_t ndraws, const gb_draw *__restrict__
 
 /* *mx = max(*mx, the largest cell count): the heaviest (band, draw) cell,
    which one raster CTA works through on its own */
-__global__ void gb_cells_max(uint32_t ncells, const uint32_t *__restrict__ cnt, uint32_t *__restrict__ mx) {
-    __shared__ uint32_t s_m[32];
-    uint32_t            m = 0;
-    for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < ncells; c += (size_t)gridDim.x * blockDim.x)
-        m = max(m, cnt[c]);
-    m = __reduce_max_sync(0xFFFFFFFFu, m);
-    if ((threadIdx.x & 31u) == 0)
-        s_m[threadIdx.x >> 5] = m;
-    __syncthreads();
-    if (threadIdx.x < 32) {
-        m = threadIdx.x < (blockDim.x >> 5) ? s_m[threadIdx.x] : 0u;
-        m = __reduce_max_sync(0xFFFFFFFFu, m);
-        if (threadIdx.x == 0 && m)
-            atomicMax(mx, m);
-    }
-}
-
-/* Active cells, for the raster's per-band draw lists: a cell is active when
-   it holds records (its record count, scanned as a flag); the draws that act
-   on every band (paint, clear, the clip kinds) are active in every band of
-   their surface: their cells' counts are set to 1. */
+/* The draws that act on every band (paint, clear, the clip kinds) are
+   active in every band of their surface: their cells' counts get
+   GB_CELL_EVERY (bit 31; record counts stay below it, the frame's record
+   total being limited to 2^31 - 1). */
 __global__ void gb_cell_flags_every_band(uint32_t ndraws, const gb_draw *__restrict__ draws,
-                                         const gb_surf *__restrict__ surfs, uint32_t *__restrict__ flags) {
+                                         const gb_surf *__restrict__ surfs, uint32_t *__restrict__ counts) {
     const uint32_t d = blockIdx.x * blockDim.x + threadIdx.x;
     if (d >= ndraws || draws[d].kind <= GB_DRAW_STROKE)
         return;
     const gb_surf &sf = surfs[draws[d].surf];
     for (uint32_t b = 0; b < sf.nbands; b++)
-        flags[sf.cell0 + (uint64_t)b * sf.ndraws + (d - sf.draw0)] = 1u;
+        counts[sf.cell0 + (uint64_t)b * sf.ndraws + (d - sf.draw0)] |= GB_CELL_EVERY;
 }
-/* alist[pos[c]] = c for every active cell c (pos: exclusive scan of the flags) */
-__global__ void gb_cell_compact(uint32_t ncells, const uint32_t *__restrict__ pos, uint32_t *__restrict__ alist) {
-    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c < ncells) {
-        const uint32_t p = pos[c];
-        if (pos[c + 1] != p)
-            alist[p] = c;
+
+/* The cells' record offsets and the raster's per-band draw lists, in two
+   sweeps over the cell counts (band-major, draw-minor; bit 31 marks an
+   every-band draw's cell): a cell's records start at the exclusive sum of
+   the record counts before it (off), an active cell (one with records or
+   with the mark) takes the next entry of alist, in cell order, so every
+   band's entries are its active draws in draw order, and apos gets, at
+   each band's first cell of every surface, the band's first alist entry
+   (the raster reads apos only there and at the surface's end).  A tile of
+   8192 cells per block: a warp takes 512 consecutive cells as 16 rows of 32
+   (coalesced loads), summing counts with a warp scan and ranking active
+   cells with a ballot per row. */
+#define CELL_THREADS 512
+#define CELL_ITEMS   16
+#define CELL_TILE    (CELL_THREADS * CELL_ITEMS)
+
+__global__ void __launch_bounds__(CELL_THREADS) gb_cells_reduce(uint64_t n, const uint32_t *__restrict__ cnt,
+                                                                uint2 *__restrict__ bsum, uint32_t *__restrict__ mx) {
+    __shared__ uint32_t s_s[CELL_THREADS / 32], s_a[CELL_THREADS / 32], s_m[CELL_THREADS / 32];
+    const uint32_t      lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
+    const uint64_t      base = (uint64_t)blockIdx.x * CELL_TILE + (uint64_t)w * (32u * CELL_ITEMS) + lane;
+    uint32_t            s = 0, a = 0, m = 0;
+#pragma unroll
+    for (int k = 0; k < CELL_ITEMS; k++) {
+        const uint64_t c = base + 32u * (uint32_t)k;
+        const uint32_t v = c < n ? cnt[c] : 0u;
+        s += v & ~GB_CELL_EVERY;
+        a += v != 0u ? 1u : 0u;
+        m = max(m, v & ~GB_CELL_EVERY);
+    }
+    s = __reduce_add_sync(0xFFFFFFFFu, s);
+    a = __reduce_add_sync(0xFFFFFFFFu, a);
+    m = __reduce_max_sync(0xFFFFFFFFu, m);
+    if (lane == 0) {
+        s_s[w] = s;
+        s_a[w] = a;
+        s_m[w] = m;
+    }
+    __syncthreads();
+    if (w == 0) {
+        s = lane < CELL_THREADS / 32 ? s_s[lane] : 0u;
+        a = lane < CELL_THREADS / 32 ? s_a[lane] : 0u;
+        m = lane < CELL_THREADS / 32 ? s_m[lane] : 0u;
+        s = __reduce_add_sync(0xFFFFFFFFu, s);
+        a = __reduce_add_sync(0xFFFFFFFFu, a);
+        m = __reduce_max_sync(0xFFFFFFFFu, m);
+        if (lane == 0) {
+            bsum[blockIdx.x] = make_uint2(s, a);
+            if (mx && m)
+                atomicMax(mx, m);
+        }
+    }
+}
+
+/* one block: exclusive scan of the nb tiles' (records, active cells) in
+   place, the totals at bsum[nb]; each thread sums a run of consecutive tiles */
+__global__ void __launch_bounds__(1024) gb_cells_prefix(uint32_t nb, uint2 *__restrict__ bsum) {
+    __shared__ uint32_t s_s[32], s_a[32];
+    const uint32_t      per = (nb + 1023u) / 1024u, i0 = min(threadIdx.x * per, nb), i1 = min(i0 + per, nb);
+    const uint32_t      lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
+    uint32_t            s = 0, a = 0;
+    for (uint32_t i = i0; i < i1; i++) {
+        const uint2 v = bsum[i];
+        s += v.x;
+        a += v.y;
+    }
+    /* inclusive warp scans, then the warps' totals */
+    uint32_t is = s, ia = a;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t ts = __shfl_up_sync(0xFFFFFFFFu, is, o), ta = __shfl_up_sync(0xFFFFFFFFu, ia, o);
+        if (lane >= (uint32_t)o) {
+            is += ts;
+            ia += ta;
+        }
+    }
+    if (lane == 31) {
+        s_s[w] = is;
+        s_a[w] = ia;
+    }
+    __syncthreads();
+    if (w == 0) {
+        uint32_t vs = s_s[lane], va = s_a[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t ts = __shfl_up_sync(0xFFFFFFFFu, vs, o), ta = __shfl_up_sync(0xFFFFFFFFu, va, o);
+            if (lane >= (uint32_t)o) {
+                vs += ts;
+                va += ta;
+            }
+        }
+        s_s[lane] = vs;
+        s_a[lane] = va;
+    }
+    __syncthreads();
+    uint32_t rs = (w ? s_s[w - 1] : 0u) + is - s, ra = (w ? s_a[w - 1] : 0u) + ia - a;
+    for (uint32_t i = i0; i < i1; i++) {
+        const uint2 v = bsum[i];
+        bsum[i]       = make_uint2(rs, ra);
+        rs += v.x;
+        ra += v.y;
+    }
+    if (threadIdx.x == 1023u)
+        bsum[nb] = make_uint2(rs, ra);
+}
+
+__global__ void __launch_bounds__(CELL_THREADS)
+    gb_cells_apply(uint64_t n, const uint32_t *__restrict__ cnt, const uint2 *__restrict__ bsum,
+                   uint32_t *__restrict__ off, uint32_t *__restrict__ alist, uint32_t *__restrict__ apos,
+                   const gb_surf *__restrict__ surfs, uint32_t nsurf) {
+    __shared__ uint32_t s_pos[CELL_TILE]; /* per cell: active cells before it in the tile */
+    __shared__ uint32_t s_s[CELL_THREADS / 32], s_a[CELL_THREADS / 32];
+    const uint32_t      lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
+    const uint64_t      c0   = (uint64_t)blockIdx.x * CELL_TILE;
+    const uint64_t      base = c0 + (uint64_t)w * (32u * CELL_ITEMS) + lane;
+    uint32_t            v[CELL_ITEMS], s = 0, a = 0;
+#pragma unroll
+    for (int k = 0; k < CELL_ITEMS; k++) {
+        const uint64_t c = base + 32u * (uint32_t)k;
+        v[k]             = c < n ? cnt[c] : 0u;
+        s += v[k] & ~GB_CELL_EVERY;
+        a += v[k] != 0u ? 1u : 0u;
+    }
+    s = __reduce_add_sync(0xFFFFFFFFu, s);
+    a = __reduce_add_sync(0xFFFFFFFFu, a);
+    if (lane == 0) {
+        s_s[w] = s;
+        s_a[w] = a;
+    }
+    __syncthreads();
+    const uint2 bp = bsum[blockIdx.x];
+    uint32_t    rs = bp.x, ra = 0;
+    for (uint32_t j = 0; j < w; j++) {
+        rs += s_s[j];
+        ra += s_a[j];
+    }
+    const uint32_t lt = (1u << lane) - 1u;
+#pragma unroll
+    for (int k = 0; k < CELL_ITEMS; k++) {
+        const uint32_t cn  = v[k] & ~GB_CELL_EVERY;
+        uint32_t       inc = cn;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, inc, o);
+            if (lane >= (uint32_t)o)
+                inc += t;
+        }
+        const uint32_t am = __ballot_sync(0xFFFFFFFFu, v[k] != 0u);
+        const uint32_t ea = ra + (uint32_t)__popc(am & lt);
+        const uint64_t c  = base + 32u * (uint32_t)k;
+        if (c < n) {
+            off[c]            = rs + inc - cn;
+            s_pos[c - c0]     = ea;
+            if (v[k])
+                alist[bp.y + ea] = (uint32_t)c;
+        }
+        rs += __shfl_sync(0xFFFFFFFFu, inc, 31);
+        ra += (uint32_t)__popc(am);
+    }
+    __syncthreads();
+    /* the band starts inside this tile, surface by surface (the surfaces'
+       cells are consecutive ranges in table order) */
+    const uint64_t c1 = min(c0 + (uint64_t)CELL_TILE, n);
+    uint32_t       lo = 0, hi = nsurf;
+    while (lo < hi) { /* the first surface whose cells end after c0 */
+        const uint32_t mid = (lo + hi) >> 1;
+        const gb_surf &S   = surfs[mid];
+        if (S.cell0 + (uint64_t)S.nbands * S.ndraws <= c0)
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    for (uint32_t si = lo; si < nsurf; si++) {
+        const gb_surf &S = surfs[si];
+        if (S.cell0 >= c1)
+            break;
+        const uint64_t nd = S.ndraws;
+        if (!nd)
+            continue;
+        const uint64_t kf = S.cell0 >= c0 ? 0u : (c0 - S.cell0 + nd - 1u) / nd;
+        for (uint64_t k = kf + threadIdx.x; k <= S.nbands; k += CELL_THREADS) {
+            const uint64_t c = S.cell0 + k * nd;
+            if (c >= c1)
+                break;
+            apos[c] = bp.y + s_pos[c - c0];
+        }
+    }
+    if (blockIdx.x == gridDim.x - 1u && threadIdx.x == 0) {
+        const uint2 t = bsum[gridDim.x];
+        off[n]        = t.x;
+        apos[n]       = t.y;
     }
 }
 /* out[i] = src[idx[i]] */
@@ -465,16 +632,24 @@ cudaError_t gb_launch_draw_width_stats(cudaStream_t st, uint32_t ndraws, const g
         gb_draw_width_stats<<<(ndraws + 255) / 256, 256, 0, st>>>(ndraws, draws, dbox, dcnt, (int32_t)W, stats);
     return cudaGetLastError();
 }
-cudaError_t gb_launch_cells_max(cudaStream_t st, uint32_t ncells, const uint32_t *cnt, uint32_t *mx) {
-    if (ncells) {
-        const uint32_t nb = std::min<uint32_t>((ncells + 255) / 256, 2048u);
-        gb_cells_max<<<nb, 256, 0, st>>>(ncells, cnt, mx);
-    }
+size_t gb_cells_scratch_words(uint64_t ncells) { return 2 * ((ncells + CELL_TILE - 1) / CELL_TILE + 1); }
+cudaError_t gb_launch_cells_reduce(cudaStream_t st, uint64_t ncells, const uint32_t *counts, uint32_t *scratch,
+                                   uint32_t *mx) {
+    if (ncells)
+        gb_cells_reduce<<<(uint32_t)((ncells + CELL_TILE - 1) / CELL_TILE), CELL_THREADS, 0, st>>>(
+            ncells, counts, (uint2 *)scratch, mx);
     return cudaGetLastError();
 }
-cudaError_t gb_launch_cell_compact(cudaStream_t st, uint32_t ncells, const uint32_t *pos, uint32_t *alist) {
-    if (ncells)
-        gb_cell_compact<<<(ncells + 255) / 256, 256, 0, st>>>(ncells, pos, alist);
+cudaError_t gb_launch_cells_lists(cudaStream_t st, uint64_t ncells, const uint32_t *counts, uint32_t *scratch,
+                                  uint32_t *off, uint32_t *alist, uint32_t *apos, const gb_surf *surfs, uint32_t nsurf) {
+    if (!ncells) {
+        cudaError_t e = cudaMemsetAsync(off, 0, 4, st);
+        return e != cudaSuccess ? e : cudaMemsetAsync(apos, 0, 4, st);
+    }
+    const uint32_t nb = (uint32_t)((ncells + CELL_TILE - 1) / CELL_TILE);
+    uint2         *bs = (uint2 *)scratch;
+    gb_cells_prefix<<<1, 1024, 0, st>>>(nb, bs);
+    gb_cells_apply<<<nb, CELL_THREADS, 0, st>>>(ncells, counts, bs, off, alist, apos, surfs, nsurf);
     return cudaGetLastError();
 }
 }
