@@ -60,8 +60,35 @@ __device__ __forceinline__ int2 gb_snap(const gb_vp &m, float2 p, bool *finite) 
     return make_int2(gb_to_fixed(nx * m.hw + m.hw), gb_to_fixed(ny * m.hh + m.hh));
 }
 
-__device__ __forceinline__ uint32_t gb_find(const uint32_t *__restrict__ off, uint32_t n, uint32_t e) {
-    uint32_t lo = 0, hi = n;
+/* the largest i in [lo, hi) with off[i] <= e (off non-decreasing, off[lo] <= e),
+   by the whole warp: 32 probes a step, so a few dependent loads */
+__device__ __forceinline__ uint32_t gb_warp_find(const uint32_t *__restrict__ off, uint32_t lo, uint32_t hi,
+                                                 uint32_t e) {
+    const uint32_t lane = threadIdx.x & 31u;
+    while (hi - lo > 1) {
+        const uint32_t step = (hi - lo + 31u) / 32u;
+        const uint32_t i    = lo + lane * step;
+        const uint32_t m    = __ballot_sync(0xFFFFFFFFu, i < hi && off[i] <= e) | 1u;
+        lo += (31u - (uint32_t)__clz(m)) * step;
+        hi = min(hi, lo + step);
+    }
+    return lo;
+}
+/* the block's items [i0, i1] lie in ranges [p0, p1] of off (n ranges):
+   warp 0 finds both ends */
+__device__ __forceinline__ void gb_block_range(const uint32_t *__restrict__ off, uint32_t n, uint32_t i0,
+                                               uint32_t i1, uint32_t *s_p) {
+    if (threadIdx.x < 32) {
+        const uint32_t p0 = gb_warp_find(off, 0, n, i0);
+        const uint32_t p1 = gb_warp_find(off, p0, n, i1);
+        if (threadIdx.x == 0)
+            s_p[0] = p0, s_p[1] = p1;
+    }
+    __syncthreads();
+}
+__device__ __forceinline__ uint32_t gb_find(const uint32_t *__restrict__ off, uint32_t n, uint32_t e,
+                                            uint32_t lo = 0) {
+    uint32_t hi = n;
     while (hi - lo > 1) {
         uint32_t mid = (lo + hi) >> 1;
         if (off[mid] <= e)
@@ -88,10 +115,14 @@ __global__ void gb_fill_edges(uint32_t nedges, uint32_t npairs, const uint32_t *
                               const uint32_t *__restrict__ sub_npts, const float2 *__restrict__ pts,
                               const gb_surf *__restrict__ surfs, int4 *__restrict__ edges,
                               uint32_t *__restrict__ edge_draw) {
-    uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+    /* the block's edges lie in pairs [p0, p1]: two searches over all pairs,
+       then each thread's search within them */
+    __shared__ uint32_t s_p[2];
+    const uint32_t      e0 = blockIdx.x * blockDim.x, e = e0 + threadIdx.x;
+    gb_block_range(e_off, npairs, e0, min(e0 + blockDim.x, nedges) - 1u, s_p);
     if (e >= nedges)
         return;
-    uint32_t p = gb_find(e_off, npairs, e);
+    uint32_t p = gb_find(e_off, s_p[1] + 1u, e, s_p[0]);
     uint32_t s = pair_sub[p], d = pair_draw[p];
     uint32_t j = e - e_off[p], n = sub_npts[s], first = sub_pt0[s];
     const gb_surf &sf = surfs[draws[d].surf];
@@ -110,10 +141,12 @@ __global__ void gb_stroke_tris(uint32_t ntris, uint32_t ndraw_s, const uint32_t 
                                int4 *__restrict__ tri_a,
                                int4 *__restrict__ tri_b, uint32_t *__restrict__ tri_draw,
                                uint4 *__restrict__ tri_idx) {
-    uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    __shared__ uint32_t s_p[2];
+    const uint32_t      t0 = blockIdx.x * blockDim.x, t = t0 + threadIdx.x;
+    gb_block_range(draw_tri0, ndraw_s, t0, min(t0 + blockDim.x, ntris) - 1u, s_p);
     if (t >= ntris)
         return;
-    uint32_t k  = gb_find(draw_tri0, ndraw_s, t);
+    uint32_t k  = gb_find(draw_tri0, s_p[1] + 1u, t, s_p[0]);
     uint32_t d  = sdraw_id[k];
     const gb_surf &sf = surfs[draws[d].surf];
     gb_vp          m  = make_vp(draws[d], sf.W, sf.H);
@@ -233,8 +266,9 @@ __device__ __forceinline__ bool gb_prim_bands(int32_t ylo, int32_t yhi, int32_t 
    (x0, y0, x1, y1) into every (band, draw) cell of its surface it touches,
    so that a cell is one contiguous block of 16-byte records the raster can
    stage with a single bulk copy.  The counting pass also folds every edge's
-   x extent into its draw's box (min x, -max x), one atomic per warp where
-   the warp's edges belong to one draw.  Every edge that is not horizontal
+   x extent into its draw's box (min x, -max x), one set of atomics per draw
+   of a warp (per block where the block's edges belong to one draw).  Every
+   edge that is not horizontal
    counts, binned or not: a draw is passed over in a tile only when all of
    the edges that can cross a row lie right of the tile (a net zero on every
    row) or all left of it. */
@@ -273,10 +307,22 @@ __global__ void gb_bin_edges(uint32_t nedges, const int4 *__restrict__ edges, co
             s_nmx[w] = wnmx;
             s_n[w]   = wn;
         }
-        if (!wu && xb) {
-            atomicMin(&dbox[d].x, mn);
-            atomicMin(&dbox[d].y, nmx);
-            atomicAdd(&dcnt[d], 1u);
+        if (!wu) { /* a warp of several draws: one set of atomics per draw (they come in runs) */
+            bool left = xb;
+            while (__any_sync(0xFFFFFFFFu, left)) {
+                const uint32_t lead = __ffs(__ballot_sync(0xFFFFFFFFu, left)) - 1u;
+                const uint32_t dl   = __shfl_sync(0xFFFFFFFFu, dk, lead);
+                const bool     mine = left && dk == dl;
+                const int32_t  rmn  = __reduce_min_sync(0xFFFFFFFFu, mine ? mn : 0x7FFFFFFF);
+                const int32_t  rnmx = __reduce_min_sync(0xFFFFFFFFu, mine ? nmx : 0x7FFFFFFF);
+                const uint32_t rn   = __popc(__ballot_sync(0xFFFFFFFFu, mine));
+                if ((threadIdx.x & 31u) == lead) {
+                    atomicMin(&dbox[dl].x, rmn);
+                    atomicMin(&dbox[dl].y, rnmx);
+                    atomicAdd(&dcnt[dl], rn);
+                }
+                left = left && !mine;
+            }
         }
         __syncthreads();
         if (threadIdx.x < 32) {
@@ -369,7 +415,7 @@ __global__ void gb_cell_flags_every_band(uint32_t ndraws, const gb_draw *__restr
         return;
     const gb_surf &sf = surfs[draws[d].surf];
     for (uint32_t b = 0; b < sf.nbands; b++)
-        counts[sf.cell0 + (uint64_t)b * sf.ndraws + (d - sf.draw0)] |= GB_CELL_EVERY;
+        atomicOr(&counts[sf.cell0 + (uint64_t)b * sf.ndraws + (d - sf.draw0)], GB_CELL_EVERY); /* no read back */
 }
 
 /* The cells' record offsets and the raster's per-band draw lists, in two
