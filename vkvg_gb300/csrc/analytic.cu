@@ -17,7 +17,9 @@
  *   ak_composite  one thread per pixel: coverage min(1, |A|) per layer,
  *                 premultiplied source-over in layer order onto the
  *                 background, the colour under every AK_CHUNK-th layer kept
- *                 as a checkpoint, canvas and per-block loss partials.
+ *                 as a checkpoint, canvas and per-block loss partials (in a
+ *                 tiled scene, every AK_CHUNK-th of the layers reaching the
+ *                 block).
  * Backward (K8):
  *   ak_composite_bwd  one thread per pixel, chunks of AK_CHUNK layers from the
  *                 top: the chunk's under-colours are recomputed from its
@@ -39,6 +41,7 @@
 #include <math_constants.h>
 
 #define AK_THREADS 256
+#define AK_CB_THREADS 128 /* pixels per compositing-adjoint block (and tiled compositing block) */
 
 __device__ __forceinline__ float2 v2(float x, float y) { return make_float2(x, y); }
 __device__ __forceinline__ float2 operator+(float2 a, float2 b) { return v2(a.x + b.x, a.y + b.y); }
@@ -322,19 +325,6 @@ __device__ __forceinline__ long long ak_plane_at(const ak_plane &P, uint32_t x, 
     const uint32_t dx = x - P.x0, dy = y - P.y0;
     return dx < P.w && dy < P.h ? (long long)(P.base + (size_t)dy * P.w + dx) : -1ll;
 }
-/* warp 0 of a block: the chunk's layers whose plane reaches the block's
-   window rows [ry0, ry1] (every layer without tiles), in order, into
-   act[0, *nact); lane q < n holds layer q's plane */
-__device__ __forceinline__ void ak_chunk_active(const ak_plane &P, bool has, uint32_t ry0, uint32_t ry1,
-                                                uint8_t *act, int *nact) {
-    const uint32_t lane = threadIdx.x & 31;
-    const bool     on   = has && P.y0 <= ry1 && P.y0 + P.h > ry0;
-    const uint32_t m    = __ballot_sync(0xffffffffu, on);
-    if (on)
-        act[__popc(m & ((1u << lane) - 1u))] = (uint8_t)lane;
-    if (lane == 0)
-        *nact = __popc(m);
-}
 /* a (tile, layer) pair's box inside its tile: x0, y0, w, h */
 __device__ __forceinline__ uint4 ak_pair_box(const ak_scene &S, uint32_t j) {
     const uint2 b = S.pair_box[j];
@@ -547,61 +537,150 @@ __device__ __forceinline__ float block_sum(float v, float *red) {
     return s;
 }
 
+/* Tiled compositing walks, per block, only the layers whose planes reach the
+   block's window rows, packed AK_CHUNK to a chunk: warp 0 scans the tile's
+   layers 32 at a time (plane, activity and colour of each), compacts the
+   active ones into a window in shared memory and hands them out a chunk at
+   a time, bottom up for the forward and top down for the adjoint.  Chunk c
+   of a block holds its active layers [16 c, 16 c + 16), the same in both
+   passes (the blocks cover the same pixels), so the forward's checkpoint c
+   is the colour under the adjoint's chunk c; the forward leaves the block's
+   active count in blk_na for the adjoint. */
+struct ak_pend {
+    ak_plane p[32];
+    float4   c[32];
+    uint32_t l[32];
+};
+struct ak_scan {
+    uint32_t next;     /* bottom up: the next layer to scan; top down: the end of the unscanned layers */
+    int      np, pos;  /* active layers in the window, handed out */
+};
+/* warp 0: layers [l0, l0 + 32) of the window (those below lim) into pd */
+__device__ __forceinline__ int ak_scan_window(const ak_scene &S, const ak_win &w, const float4 *__restrict__ colors,
+                                              uint32_t ry0, uint32_t ry1, uint32_t l0, uint32_t lim, ak_pend &pd) {
+    const uint32_t lane = threadIdx.x & 31u, l = l0 + lane;
+    ak_plane       P{};
+    bool           on = false;
+    if (l < lim) {
+        P  = ak_plane_of(S, w, l);
+        on = P.y0 <= ry1 && P.y0 + P.h > ry0;
+    }
+    float4 c = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (on)
+        c = colors[S.layer_path[ak_layer(S, w, l)]];
+    const uint32_t m = __ballot_sync(0xffffffffu, on);
+    if (on) {
+        const int k = __popc(m & ((1u << lane) - 1u));
+        pd.p[k] = P, pd.c[k] = c, pd.l[k] = l;
+    }
+    __syncwarp();
+    return __popc(m);
+}
+/* warp 0: the next chunk of up to `want` active layers, in layer order, into
+   (col, pl, cl)[0, *nact); UP: from the bottom, else from the top */
+template <bool UP>
+__device__ __forceinline__ void ak_fill_chunk(const ak_scene &S, const ak_win &w, const float4 *__restrict__ colors,
+                                              uint32_t ry0, uint32_t ry1, ak_scan &sc, ak_pend &pd, int want,
+                                              float4 *col, ak_plane *pl, uint32_t *cl, int *nact) {
+    const uint32_t lane = threadIdx.x & 31u;
+    int            cnt  = 0;
+    while (cnt < want) {
+        if (sc.pos == sc.np) {
+            if (UP ? sc.next >= w.nl : sc.next == 0)
+                break;
+            const uint32_t l0 = UP ? sc.next : (sc.next > 32u ? sc.next - 32u : 0u);
+            sc.np             = ak_scan_window(S, w, colors, ry0, ry1, l0, UP ? w.nl : sc.next, pd);
+            sc.pos            = 0;
+            sc.next           = UP ? sc.next + 32u : l0;
+            continue;
+        }
+        const int take = min(want - cnt, sc.np - sc.pos);
+        if ((int)lane < take) {
+            /* bottom up: the window's lowest remaining, placed after the
+               chunk's; top down: its highest remaining, placed below them */
+            const int src = UP ? sc.pos + (int)lane : sc.np - sc.pos - take + (int)lane;
+            const int dst = UP ? cnt + (int)lane : want - cnt - take + (int)lane;
+            col[dst] = pd.c[src], pl[dst] = pd.p[src], cl[dst] = pd.l[src];
+        }
+        cnt += take, sc.pos += take;
+        __syncwarp();
+    }
+    if (lane == 0)
+        *nact = cnt;
+}
+
 /* TILED: the tiles of a tiled scene (layers read through their planes'
-   boxes, per-chunk lists of the layers reaching the block); else the one
+   boxes, packed chunks of the layers reaching the block); else the one
    window, every layer's plane the whole canvas */
 template <bool TILED>
-__global__ void __launch_bounds__(AK_THREADS)
+__global__ void __launch_bounds__(TILED ? AK_CB_THREADS : AK_THREADS)
     ak_composite(ak_scene S, ak_bufs B, const float4 *__restrict__ colors, const float4 *__restrict__ target,
                  float *__restrict__ loss_part) {
+    constexpr int       NT = TILED ? AK_CB_THREADS : AK_THREADS;
     __shared__ float4   col[AK_CHUNK];
     __shared__ ak_plane pl[TILED ? AK_CHUNK : 1];
-    __shared__ uint8_t  act[TILED ? AK_CHUNK : 1];
+    __shared__ uint32_t cl[TILED ? AK_CHUNK : 1];
+    __shared__ ak_pend  pend;
     __shared__ int      nact;
-    __shared__ float    red[AK_THREADS / 32];
+    __shared__ float    red[NT / 32];
     /* grid: the window's pixel blocks, window after window */
-    const uint32_t bpw = window_blocks(S, AK_THREADS), b = blockIdx.x % bpw;
+    const uint32_t bpw = window_blocks(S, NT), b = blockIdx.x % bpw;
     const ak_win   w   = ak_window(S, blockIdx.x / bpw);
-    size_t         np = (size_t)w.W * w.H, px = (size_t)b * AK_THREADS + threadIdx.x;
+    size_t         np = (size_t)w.W * w.H, px = (size_t)b * NT + threadIdx.x;
     bool           valid = px < np;
     const uint32_t x = valid ? (uint32_t)(px % w.W) : 0u, y = valid ? (uint32_t)(px / w.W) : 0u;
     /* the block's window rows: a layer whose plane misses them all leaves
        the block's pixels unchanged (coverage zero) and is passed over */
-    const uint32_t ry0 = (uint32_t)((size_t)b * AK_THREADS / w.W), ry1 = (uint32_t)(((size_t)b * AK_THREADS + AK_THREADS - 1) / w.W);
+    const uint32_t ry0 = (uint32_t)((size_t)b * NT / w.W), ry1 = (uint32_t)(((size_t)b * NT + NT - 1) / w.W);
     float4         C     = S.bg;
     float4        *ckpt  = B.ckpt + w.ckpt;
-    for (uint32_t lb = 0; lb < w.nl; lb += AK_CHUNK) {
-        uint32_t n = min((uint32_t)AK_CHUNK, w.nl - lb);
-        __syncthreads();
-        if (TILED && threadIdx.x < 32) {
-            ak_plane P{};
-            if (threadIdx.x < n) {
-                col[threadIdx.x] = colors[S.layer_path[ak_layer(S, w, lb + threadIdx.x)]];
-                pl[threadIdx.x]  = P = ak_plane_of(S, w, lb + threadIdx.x);
-            }
-            ak_chunk_active(P, threadIdx.x < n, ry0, ry1, act, &nact);
-        } else if (!TILED && threadIdx.x < n) {
-            col[threadIdx.x] = colors[S.layer_path[lb + threadIdx.x]];
-        }
-        __syncthreads();
-        if (!valid)
-            continue;
-        ckpt[(size_t)(lb / AK_CHUNK) * np + px] = C;
-        const int na = TILED ? nact : (int)n;
-        float     A[AK_CHUNK];
+    if (TILED) {
+        ak_scan  sc{0u, 0, 0};
+        uint32_t tot = 0;
+        for (uint32_t c = 0;; c++) {
+            __syncthreads();
+            if (threadIdx.x < 32)
+                ak_fill_chunk<true>(S, w, colors, ry0, ry1, sc, pend, AK_CHUNK, col, pl, cl, &nact);
+            __syncthreads();
+            const int na = nact;
+            if (na == 0)
+                break;
+            tot += (uint32_t)na;
+            if (!valid)
+                continue;
+            ckpt[(size_t)c * np + px] = C;
+            float A[AK_CHUNK];
 #pragma unroll
-        for (int i = 0; i < AK_CHUNK; i++) {
-            if (TILED) {
-                const long long k = i < na ? ak_plane_at(pl[act[i]], x, y) : -1ll;
+            for (int i = 0; i < AK_CHUNK; i++) {
+                const long long k = i < na ? ak_plane_at(pl[i], x, y) : -1ll;
                 A[i]              = k >= 0 ? B.area[k] : 0.f;
-            } else {
-                A[i] = i < na ? B.area[(size_t)(lb + i) * np + px] : 0.f;
             }
-        }
 #pragma unroll
-        for (int i = 0; i < AK_CHUNK; i++)
-            if (i < na)
-                C = blend(cover(A[i]), col[TILED ? act[i] : i], C);
+            for (int i = 0; i < AK_CHUNK; i++)
+                if (i < na)
+                    C = blend(cover(A[i]), col[i], C);
+        }
+        if (threadIdx.x == 0)
+            B.blk_na[blockIdx.x] = tot;
+    } else {
+        for (uint32_t lb = 0; lb < w.nl; lb += AK_CHUNK) {
+            uint32_t n = min((uint32_t)AK_CHUNK, w.nl - lb);
+            __syncthreads();
+            if (threadIdx.x < n)
+                col[threadIdx.x] = colors[S.layer_path[lb + threadIdx.x]];
+            __syncthreads();
+            if (!valid)
+                continue;
+            ckpt[(size_t)(lb / AK_CHUNK) * np + px] = C;
+            float A[AK_CHUNK];
+#pragma unroll
+            for (int i = 0; i < AK_CHUNK; i++)
+                A[i] = i < (int)n ? B.area[(size_t)(lb + i) * np + px] : 0.f;
+#pragma unroll
+            for (int i = 0; i < AK_CHUNK; i++)
+                if (i < (int)n)
+                    C = blend(cover(A[i]), col[i], C);
+        }
     }
     float        s  = 0.f;
     const size_t cp = valid ? ((size_t)w.y0 + px / w.W) * S.CW + w.x0 + px % w.W : 0; /* on the canvas */
@@ -614,7 +693,7 @@ __global__ void __launch_bounds__(AK_THREADS)
         }
     }
     if (target) {
-        s = block_sum<AK_THREADS>(s, red);
+        s = block_sum<NT>(s, red);
         if (threadIdx.x == 0)
             loss_part[blockIdx.x] = s;
     }
@@ -650,15 +729,14 @@ __device__ __forceinline__ float warp_reduce_scatter32(float (&v)[32]) {
     return v[0];
 }
 
-#define AK_CB_THREADS 128 /* pixels per compositing-adjoint block */
-
 template <bool TILED>
 __global__ void __launch_bounds__(AK_CB_THREADS)
     ak_composite_bwd(ak_scene S, ak_bufs B, const float4 *__restrict__ colors, const float4 *__restrict__ target,
                      const float4 *__restrict__ d_canvas, float *__restrict__ color_part) {
     __shared__ float4   col[AK_CHUNK];
     __shared__ ak_plane pl[TILED ? AK_CHUNK : 1];
-    __shared__ uint8_t  act[TILED ? AK_CHUNK : 1];
+    __shared__ uint32_t cl[TILED ? AK_CHUNK : 1];
+    __shared__ ak_pend  pend;
     __shared__ int      nact;
     __shared__ float4 sB[AK_CHUNK][AK_CB_THREADS]; /* colour under each layer of the chunk */
     __shared__ float  sA[AK_CHUNK][AK_CB_THREADS]; /* the chunk's areas */
@@ -687,32 +765,31 @@ __global__ void __launch_bounds__(AK_CB_THREADS)
         }
     }
     float    T    = 1.f; /* transmittance of the layers above */
-    uint32_t nch  = (w.nl + AK_CHUNK - 1) / AK_CHUNK;
     uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    /* chunks from the top: tiled, the block's packed chunks of active layers
+       (the forward's count; the top one holds the remainder); else chunks of
+       AK_CHUNK layers */
+    const uint32_t ntot = TILED ? B.blk_na[blockIdx.x] : w.nl;
+    uint32_t       nch  = (ntot + AK_CHUNK - 1) / AK_CHUNK;
+    ak_scan        sc{w.nl, 0, 0};
     for (uint32_t ch = nch; ch-- > 0;) {
-        uint32_t lb = ch * AK_CHUNK, n = min((uint32_t)AK_CHUNK, w.nl - lb);
+        const uint32_t lb = ch * AK_CHUNK, n = min((uint32_t)AK_CHUNK, ntot - lb);
         __syncthreads();
-        if (TILED && threadIdx.x < 32) {
-            ak_plane P{};
-            if (threadIdx.x < n) {
-                col[threadIdx.x] = colors[S.layer_path[ak_layer(S, w, lb + threadIdx.x)]];
-                pl[threadIdx.x]  = P = ak_plane_of(S, w, lb + threadIdx.x);
-            }
-            ak_chunk_active(P, threadIdx.x < n, ry0, ry1, act, &nact);
-        } else if (!TILED && threadIdx.x < n) {
+        if (TILED && threadIdx.x < 32)
+            ak_fill_chunk<false>(S, w, colors, ry0, ry1, sc, pend, (int)n, col, pl, cl, &nact);
+        else if (!TILED && threadIdx.x < n)
             col[threadIdx.x] = colors[S.layer_path[lb + threadIdx.x]];
-        }
         __syncthreads();
-        const int na = TILED ? nact : (int)n; /* the chunk's active layers act[0, na), in order */
+        const int na = TILED ? nact : (int)n; /* the chunk's layers [0, na), in order */
         if (na == 0)
-            continue; /* every layer of the chunk leaves these pixels alone */
+            continue;
         float4 Bc = valid ? ckpt[(size_t)ch * np + px] : make_float4(0.f, 0.f, 0.f, 0.f);
         {
             float A[AK_CHUNK];
 #pragma unroll
             for (int i = 0; i < AK_CHUNK; i++) {
                 if (TILED) {
-                    const long long k = (valid && i < na) ? ak_plane_at(pl[act[i]], x, y) : -1ll;
+                    const long long k = (valid && i < na) ? ak_plane_at(pl[i], x, y) : -1ll;
                     A[i]              = k >= 0 ? B.area[k] : 0.f;
                 } else {
                     A[i] = (valid && i < na) ? B.area[(size_t)(lb + i) * np + px] : 0.f;
@@ -723,11 +800,11 @@ __global__ void __launch_bounds__(AK_CB_THREADS)
                 if (i < na) {
                     sB[i][threadIdx.x] = Bc;
                     sA[i][threadIdx.x] = A[i];
-                    Bc                 = blend(cover(A[i]), col[TILED ? act[i] : i], Bc);
+                    Bc                 = blend(cover(A[i]), col[i], Bc);
                 }
             }
         }
-        /* the active layers in groups of 8, top group first; colour partials per group */
+        /* the chunk's layers in groups of 8, top group first; colour partials per group */
 #pragma unroll
         for (int hf = 1; hf >= 0; hf--) {
             if (hf * 8 >= na)
@@ -739,16 +816,15 @@ __global__ void __launch_bounds__(AK_CB_THREADS)
                 dc[4 * q8] = dc[4 * q8 + 1] = dc[4 * q8 + 2] = dc[4 * q8 + 3] = 0.f;
                 if (i >= na)
                     continue;
-                const int q  = TILED ? act[i] : i;
-                float4    c  = col[q], Bq = sB[i][threadIdx.x];
-                float     Aq = sA[i][threadIdx.x];
+                float4 c = col[i], Bq = sB[i][threadIdx.x];
+                float  Aq = sA[i][threadIdx.x];
                 float  al = cover(Aq);
                 float  gB = g.x * Bq.x + g.y * Bq.y + g.z * Bq.z + g.w * Bq.w;
                 float  gc = g.x * c.x + g.y * c.y + g.z * c.z + g.w * c.w;
                 float  da = T * (gc - c.w * gB);
                 float  gA = fabsf(Aq) < 1.f ? (Aq > 0.f ? da : Aq < 0.f ? -da : 0.f) : 0.f;
                 if (valid) {
-                    const long long k = TILED ? ak_plane_at(pl[q], x, y) : (long long)((size_t)(lb + q) * np + px);
+                    const long long k = TILED ? ak_plane_at(pl[i], x, y) : (long long)((size_t)(lb + i) * np + px);
                     if (k >= 0)
                         B.area[k] = gA;
                 }
@@ -765,8 +841,8 @@ __global__ void __launch_bounds__(AK_CB_THREADS)
             for (int k = 0; k < AK_CB_THREADS / 32; k++)
                 s += red[k][threadIdx.x];
             /* one window: [block][layer][channel]; tiled: [pair][block of the tile][channel] */
-            const uint32_t q = TILED ? act[threadIdx.x >> 2] : threadIdx.x >> 2, c = threadIdx.x & 3;
-            const size_t   i = S.tiles ? ((size_t)(w.first + lb + q) * bpw + b) * 4 + c
+            const uint32_t q = threadIdx.x >> 2, c = threadIdx.x & 3;
+            const size_t   i = S.tiles ? ((size_t)(w.first + cl[q]) * bpw + b) * 4 + c
                                        : ((size_t)b * S.nlayers + lb + q) * 4 + c;
             color_part[i] = s;
         }
@@ -1015,7 +1091,12 @@ __global__ void ak_adam(float *__restrict__ p, const float *__restrict__ g, floa
 
 /* ------------------------------------------------------------ launchers */
 
-uint32_t ak_pixel_blocks(const ak_scene &S) { return (uint32_t)(((size_t)S.W * S.H + AK_THREADS - 1) / AK_THREADS); }
+/* compositing blocks per window: 256 pixels, or 128 in a tiled scene (its
+   forward and adjoint blocks cover the same pixels) */
+uint32_t ak_pixel_blocks(const ak_scene &S) {
+    const uint32_t nt = S.tiles ? AK_CB_THREADS : AK_THREADS;
+    return (uint32_t)(((size_t)S.W * S.H + nt - 1) / nt);
+}
 uint32_t ak_band_rows(uint32_t W) { return W <= AK_BAND_WIDE_MAX ? 32u : 16u; }
 static size_t cover_fwd_smem(uint32_t W, uint32_t band) {
     return sizeof(ak_slot) * AK_THREADS + sizeof(int) * band * (W + 1);
@@ -1042,7 +1123,7 @@ uint32_t ak_pixel_blocks_all(const ak_scene &S) { return ak_pixel_blocks(S) * wi
 cudaError_t ak_launch_composite(cudaStream_t st, const ak_scene &S, const ak_bufs &B, const float4 *colors,
                                 const float4 *target, float *loss_part) {
     if (S.tiles)
-        ak_composite<true><<<ak_pixel_blocks_all(S), AK_THREADS, 0, st>>>(S, B, colors, target, loss_part);
+        ak_composite<true><<<ak_pixel_blocks_all(S), AK_CB_THREADS, 0, st>>>(S, B, colors, target, loss_part);
     else
         ak_composite<false><<<ak_pixel_blocks_all(S), AK_THREADS, 0, st>>>(S, B, colors, target, loss_part);
     return cudaGetLastError();

@@ -66,6 +66,7 @@ struct ak_bufs {
     float4         *ckpt;    /* ceil(nlayers / AK_CHUNK) * W * H: colour under every chunk */
     float4         *canvas;  /* W * H */
     uint32_t       *status;
+    uint32_t       *blk_na;  /* tiled scenes: per compositing block, its active layers (forward -> adjoint) */
 };
 
 /* lanes: one lane per segment (scenes of small curves) instead of a warp */
