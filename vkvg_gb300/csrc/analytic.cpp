@@ -362,7 +362,7 @@ cudaError_t tile_setup(VkvgAnalytic a, const float *widths) {
     T           = a->S;
     T.tiles = a->tile, T.ntx = a->ntx, T.ntiles = nt;
     T.W = T.H    = a->tile;
-    T.band       = ak_band_rows(a->tile);
+    T.band       = std::min(16u, ak_band_rows(a->tile)); /* the pairs' accumulators: a small box fits one band */
     T.nbands     = (a->tile + T.band - 1) / T.band;
     T.nlayers    = total;
     T.layer_map  = a->d_list.as<uint32_t>();

@@ -448,10 +448,13 @@ __device__ __forceinline__ bool slot_edge(const ak_slot &o, bool stroke, int e, 
 
 /* ------------------------------------------------------------- forward */
 
-__global__ void __launch_bounds__(AK_THREADS) ak_cover(ak_scene S, ak_bufs B, const float *__restrict__ widths) {
+/* NT threads: 256 for layers by bands, 128 for the small (tile, layer) pairs
+   (more of them in flight per SM) */
+template <int NT>
+__global__ void __launch_bounds__(NT) ak_cover(ak_scene S, ak_bufs B, const float *__restrict__ widths) {
     extern __shared__ __align__(16) unsigned char ak_smem[];
     ak_slot *slots = reinterpret_cast<ak_slot *>(ak_smem);
-    int     *acc   = reinterpret_cast<int *>(slots + AK_THREADS);
+    int     *acc   = reinterpret_cast<int *>(slots + NT);
     __shared__ int nslot;
     /* grid: layers by bands (one window), or one block per (tile, layer)
        pair, which takes its box in bands as tall as the accumulator holds at
@@ -470,7 +473,7 @@ __global__ void __launch_bounds__(AK_THREADS) ak_cover(ak_scene S, ak_bufs B, co
         bd.y1    = min((int)w.H, bd.y0 + (int)bh);
         int rows = bd.y1 - bd.y0;
         __syncthreads(); /* the previous band's prefix sums have read the accumulator */
-        for (int i = threadIdx.x; i < rows * W1; i += AK_THREADS)
+        for (int i = threadIdx.x; i < rows * W1; i += NT)
             acc[i] = 0;
         if (B.off[S.nseg] <= B.cap) {
             uint32_t p = S.layer_path[lg];
@@ -478,14 +481,14 @@ __global__ void __launch_bounds__(AK_THREADS) ak_cover(ak_scene S, ak_bufs B, co
             int      E      = stroke ? 7 : 1;
             float    h      = 0.5f * widths[p];
             uint32_t p1     = B.off[S.path_s0[p + 1]];
-            for (uint32_t base = B.off[S.path_s0[p]]; base < p1; base += AK_THREADS) {
+            for (uint32_t base = B.off[S.path_s0[p]]; base < p1; base += NT) {
                 if (threadIdx.x == 0)
                     nslot = 0;
                 __syncthreads();
                 gather_slots(S, B, bd, org, stroke, true, h, base + threadIdx.x, p1, slots, &nslot);
                 __syncthreads();
                 int ne = nslot * E;
-                for (int t = threadIdx.x; t < ne; t += AK_THREADS) {
+                for (int t = threadIdx.x; t < ne; t += NT) {
                     float2 a, b;
                     const ak_slot &sl = slots[t / E];
                     if (slot_edge(sl, stroke, t % E, a, b))
@@ -497,7 +500,7 @@ __global__ void __launch_bounds__(AK_THREADS) ak_cover(ak_scene S, ak_bufs B, co
         __syncthreads();
         /* row prefix sums, one warp per row, 32 cells per step */
         float *out = plane + (size_t)bd.y0 * w.W;
-        for (int r = warp; r < rows; r += AK_THREADS / 32) {
+        for (int r = warp; r < rows; r += NT / 32) {
             int carry = 0;
             for (uint32_t c = 0; c < w.W; c += 32) {
                 uint32_t i = c + lane;
@@ -856,14 +859,15 @@ __device__ __forceinline__ void add_grad(float2 *g, float2 v) {
     }
 }
 
-__global__ void __launch_bounds__(AK_THREADS)
+template <int NT>
+__global__ void __launch_bounds__(NT)
     ak_cover_bwd(ak_scene S, ak_bufs B, const float *__restrict__ widths, float2 *__restrict__ gpts,
                  float *__restrict__ gwidth) {
     extern __shared__ __align__(16) unsigned char ak_smem[];
     ak_slot *slots = reinterpret_cast<ak_slot *>(ak_smem);
-    float4  *eg    = reinterpret_cast<float4 *>(slots + AK_THREADS); /* per slot edge: dL/da, dL/db */
-    float   *gs    = reinterpret_cast<float *>(eg + AK_THREADS * 7);
-    __shared__ float red[AK_THREADS / 32];
+    float4  *eg    = reinterpret_cast<float4 *>(slots + NT); /* per slot edge: dL/da, dL/db */
+    float   *gs    = reinterpret_cast<float *>(eg + NT * 7);
+    __shared__ float red[NT / 32];
     __shared__ int   nslot;
     /* the grid of ak_cover: a pair's block takes its box in bands as tall as
        the gradient buffer holds at the box's width */
@@ -887,16 +891,16 @@ __global__ void __launch_bounds__(AK_THREADS)
     int          rows = bd.y1 - bd.y0;
     const float *src  = plane + (size_t)bd.y0 * w.W;
     __syncthreads(); /* the previous band's edges have read the buffer */
-    for (int i = threadIdx.x; i < rows * (int)w.W; i += AK_THREADS)
+    for (int i = threadIdx.x; i < rows * (int)w.W; i += NT)
         gs[i] = src[i];
-    for (uint32_t base = B.off[S.path_s0[p]]; base < p1; base += AK_THREADS) {
+    for (uint32_t base = B.off[S.path_s0[p]]; base < p1; base += NT) {
         if (threadIdx.x == 0)
             nslot = 0;
         __syncthreads();
         gather_slots(S, B, bd, org, stroke, false, h, base + threadIdx.x, p1, slots, &nslot);
         __syncthreads();
         int ns = nslot, ne = ns * E;
-        for (int t = threadIdx.x; t < ne; t += AK_THREADS) {
+        for (int t = threadIdx.x; t < ne; t += NT) {
             float2 a, b, ga = v2(0.f, 0.f), gb = v2(0.f, 0.f);
             const ak_slot &sl = slots[t / E];
             if (slot_edge(sl, stroke, t % E, a, b))
@@ -955,7 +959,7 @@ __global__ void __launch_bounds__(AK_THREADS)
     }
     } /* bands */
     if (stroke) {
-        float s = block_sum<AK_THREADS>(gh, red);
+        float s = block_sum<NT>(gh, red);
         if (threadIdx.x == 0 && s != 0.f)
             atomicAdd(&gwidth[p], 0.5f * s);
     }
@@ -1098,25 +1102,33 @@ uint32_t ak_pixel_blocks(const ak_scene &S) {
     return (uint32_t)(((size_t)S.W * S.H + nt - 1) / nt);
 }
 uint32_t ak_band_rows(uint32_t W) { return W <= AK_BAND_WIDE_MAX ? 32u : 16u; }
-static size_t cover_fwd_smem(uint32_t W, uint32_t band) {
-    return sizeof(ak_slot) * AK_THREADS + sizeof(int) * band * (W + 1);
+static size_t cover_fwd_smem(uint32_t W, uint32_t band, uint32_t nt) {
+    return sizeof(ak_slot) * nt + sizeof(int) * band * (W + 1);
 }
-static size_t cover_bwd_smem(uint32_t W, uint32_t band) {
-    return sizeof(ak_slot) * AK_THREADS + sizeof(float4) * AK_THREADS * 7 + sizeof(float) * band * W;
+static size_t cover_bwd_smem(uint32_t W, uint32_t band, uint32_t nt) {
+    return sizeof(ak_slot) * nt + sizeof(float4) * nt * 7 + sizeof(float) * band * W;
 }
 size_t ak_cover_smem(uint32_t W) {
     uint32_t band = ak_band_rows(W);
-    size_t   fwd = cover_fwd_smem(W, band), bwd = cover_bwd_smem(W, band);
+    size_t   fwd = cover_fwd_smem(W, band, AK_THREADS), bwd = cover_bwd_smem(W, band, AK_THREADS);
     return fwd > bwd ? fwd : bwd;
 }
+/* tiled scenes take the small blocks */
+static uint32_t cover_threads(const ak_scene &S) { return S.tiles ? AK_CB_THREADS : AK_THREADS; }
 
-cudaError_t ak_launch_cover(cudaStream_t st, const ak_scene &S, const ak_bufs &B, const float *widths) {
-    size_t smem = cover_fwd_smem(S.W, S.band);
+template <int NT> static cudaError_t launch_cover(cudaStream_t st, const ak_scene &S, const ak_bufs &B, const float *widths) {
+    const size_t smem = cover_fwd_smem(S.W, S.band, NT);
     if (smem > 48 * 1024)
-        cudaFuncSetAttribute(ak_cover, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (S.nlayers) /* tiled: one block per pair, which walks its box's bands */
-        ak_cover<<<dim3(S.nlayers, S.tiles ? 1u : S.nbands), AK_THREADS, smem, st>>>(S, B, widths);
+        cudaFuncSetAttribute(ak_cover<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    /* tiled: one block per pair, which walks its box's bands */
+    ak_cover<NT><<<dim3(S.nlayers, S.tiles ? 1u : S.nbands), NT, smem, st>>>(S, B, widths);
     return cudaGetLastError();
+}
+cudaError_t ak_launch_cover(cudaStream_t st, const ak_scene &S, const ak_bufs &B, const float *widths) {
+    if (!S.nlayers)
+        return cudaSuccess;
+    return cover_threads(S) == AK_CB_THREADS ? launch_cover<AK_CB_THREADS>(st, S, B, widths)
+                                             : launch_cover<AK_THREADS>(st, S, B, widths);
 }
 static uint32_t windows(const ak_scene &S) { return S.tiles ? S.ntiles : 1u; }
 uint32_t ak_pixel_blocks_all(const ak_scene &S) { return ak_pixel_blocks(S) * windows(S); }
@@ -1142,14 +1154,21 @@ cudaError_t ak_launch_composite_bwd(cudaStream_t st, const ak_scene &S, const ak
             S, B, colors, target, d_canvas, reinterpret_cast<float *>(color_part));
     return cudaGetLastError();
 }
+template <int NT>
+static cudaError_t launch_cover_bwd(cudaStream_t st, const ak_scene &S, const ak_bufs &B, const float *widths,
+                                    float2 *gpts, float *gwidth) {
+    const size_t smem = cover_bwd_smem(S.W, S.band, NT);
+    if (smem > 48 * 1024)
+        cudaFuncSetAttribute(ak_cover_bwd<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    ak_cover_bwd<NT><<<dim3(S.nlayers, S.tiles ? 1u : S.nbands), NT, smem, st>>>(S, B, widths, gpts, gwidth);
+    return cudaGetLastError();
+}
 cudaError_t ak_launch_cover_bwd(cudaStream_t st, const ak_scene &S, const ak_bufs &B, const float *widths,
                                 float2 *gpts, float *gwidth) {
-    size_t smem = cover_bwd_smem(S.W, S.band);
-    if (smem > 48 * 1024)
-        cudaFuncSetAttribute(ak_cover_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (S.nlayers)
-        ak_cover_bwd<<<dim3(S.nlayers, S.tiles ? 1u : S.nbands), AK_THREADS, smem, st>>>(S, B, widths, gpts, gwidth);
-    return cudaGetLastError();
+    if (!S.nlayers)
+        return cudaSuccess;
+    return cover_threads(S) == AK_CB_THREADS ? launch_cover_bwd<AK_CB_THREADS>(st, S, B, widths, gpts, gwidth)
+                                             : launch_cover_bwd<AK_THREADS>(st, S, B, widths, gpts, gwidth);
 }
 cudaError_t ak_launch_reduce(cudaStream_t st, const ak_scene &S, uint32_t nblocks, const float4 *color_part,
                              float4 *d_colors, const float *loss_part, float *loss) {
