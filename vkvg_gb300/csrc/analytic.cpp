@@ -60,7 +60,7 @@ struct _vkvg_gb300_analytic_t {
        take (TS: every tile at once) */
     uint32_t  tile = 0, ntx = 1, nty = 1;
     DevBuf    d_box, d_tot, d_flags, d_fpos, d_fscan, d_list, d_ptile, d_pbox, d_psize, d_poff, d_pscan, d_tinfo,
-              d_blkna;
+              d_blkna, d_blist;
     PinnedBuf h_tiles, h_tinfo;
     ak_scene  TS{};
     /* the last forward */
@@ -110,6 +110,7 @@ ak_bufs bufs(VkvgAnalytic a) {
     B.canvas  = a->d_canvas.as<float4>();
     B.status  = a->d_status.as<uint32_t>();
     B.blk_na  = a->d_blkna.as<uint32_t>();
+    B.blist   = a->d_blist.as<uint32_t>();
     return B;
 }
 
@@ -261,7 +262,7 @@ void vkvg_gb300_analytic_destroy(VkvgAnalytic a) {
                     &a->d_pts, &a->d_pt_nb, &a->d_area, &a->d_ckpt, &a->d_canvas, &a->d_loss_part, &a->d_loss,
                     &a->d_color_part, &a->d_gpts, &a->d_status, &a->d_box, &a->d_flags, &a->d_fpos, &a->d_fscan,
                     &a->d_list, &a->d_ptile, &a->d_tinfo, &a->d_tot, &a->d_pbox, &a->d_psize, &a->d_poff,
-                    &a->d_pscan, &a->d_blkna};
+                    &a->d_pscan, &a->d_blkna, &a->d_blist};
     for (DevBuf *b : bs)
         b->release();
     a->h_mon.release();
@@ -374,6 +375,7 @@ cudaError_t tile_setup(VkvgAnalytic a, const float *widths) {
         !a->d_ckpt.grow(sizeof(float4) * std::max<size_t>(ckpt, 1)) ||
         !a->d_loss_part.grow(sizeof(float) * ak_pixel_blocks_all(T)) ||
         !a->d_blkna.grow(sizeof(uint32_t) * ak_pixel_blocks_all(T)) ||
+        !a->d_blist.grow(sizeof(uint32_t) * std::max<size_t>((size_t)total * ak_pixel_blocks(T), 1)) ||
         !a->d_color_part.grow(sizeof(float4) * std::max<size_t>(ak_color_partials(T), 1)))
         return cudaErrorMemoryAllocation;
     if (e == cudaSuccess) /* pinned, copied in stream order before the launches that read it */

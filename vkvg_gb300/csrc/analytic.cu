@@ -541,75 +541,52 @@ __device__ __forceinline__ float block_sum(float v, float *red) {
 }
 
 /* Tiled compositing walks, per block, only the layers whose planes reach the
-   block's window rows, packed AK_CHUNK to a chunk: warp 0 scans the tile's
-   layers 32 at a time (plane, activity and colour of each), compacts the
-   active ones into a window in shared memory and hands them out a chunk at
-   a time, bottom up for the forward and top down for the adjoint.  Chunk c
-   of a block holds its active layers [16 c, 16 c + 16), the same in both
-   passes (the blocks cover the same pixels), so the forward's checkpoint c
-   is the colour under the adjoint's chunk c; the forward leaves the block's
-   active count in blk_na for the adjoint. */
-struct ak_pend {
-    ak_plane p[32];
-    float4   c[32];
-    uint32_t l[32];
-};
-struct ak_scan {
-    uint32_t next;     /* bottom up: the next layer to scan; top down: the end of the unscanned layers */
-    int      np, pos;  /* active layers in the window, handed out */
-};
-/* warp 0: layers [l0, l0 + 32) of the window (those below lim) into pd */
-__device__ __forceinline__ int ak_scan_window(const ak_scene &S, const ak_win &w, const float4 *__restrict__ colors,
-                                              uint32_t ry0, uint32_t ry1, uint32_t l0, uint32_t lim, ak_pend &pd) {
-    const uint32_t lane = threadIdx.x & 31u, l = l0 + lane;
-    ak_plane       P{};
-    bool           on = false;
-    if (l < lim) {
-        P  = ak_plane_of(S, w, l);
-        on = P.y0 <= ry1 && P.y0 + P.h > ry0;
-    }
-    float4 c = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (on)
-        c = colors[S.layer_path[ak_layer(S, w, l)]];
-    const uint32_t m = __ballot_sync(0xffffffffu, on);
-    if (on) {
-        const int k = __popc(m & ((1u << lane) - 1u));
-        pd.p[k] = P, pd.c[k] = c, pd.l[k] = l;
-    }
-    __syncwarp();
-    return __popc(m);
+   block's window rows, packed AK_CHUNK to a chunk.  ak_block_lists lists
+   them first (one warp per compositing block, 32 layers of its tile a
+   step, compacted with a ballot); chunk c of a block holds its listed
+   layers [16 c, 16 c + 16) in the forward and in the adjoint alike (their
+   blocks cover the same pixels), so the forward's checkpoint c is the
+   colour under the adjoint's chunk c. */
+__device__ __forceinline__ size_t ak_blist_base(const ak_win &w, uint32_t bpw, uint32_t b) {
+    return (size_t)w.first * bpw + (size_t)b * w.nl;
 }
-/* warp 0: the next chunk of up to `want` active layers, in layer order, into
-   (col, pl, cl)[0, *nact); UP: from the bottom, else from the top */
-template <bool UP>
-__device__ __forceinline__ void ak_fill_chunk(const ak_scene &S, const ak_win &w, const float4 *__restrict__ colors,
-                                              uint32_t ry0, uint32_t ry1, ak_scan &sc, ak_pend &pd, int want,
-                                              float4 *col, ak_plane *pl, uint32_t *cl, int *nact) {
-    const uint32_t lane = threadIdx.x & 31u;
-    int            cnt  = 0;
-    while (cnt < want) {
-        if (sc.pos == sc.np) {
-            if (UP ? sc.next >= w.nl : sc.next == 0)
-                break;
-            const uint32_t l0 = UP ? sc.next : (sc.next > 32u ? sc.next - 32u : 0u);
-            sc.np             = ak_scan_window(S, w, colors, ry0, ry1, l0, UP ? w.nl : sc.next, pd);
-            sc.pos            = 0;
-            sc.next           = UP ? sc.next + 32u : l0;
-            continue;
+__global__ void __launch_bounds__(128) ak_block_lists(ak_scene S, ak_bufs B, uint32_t nblocks) {
+    const uint32_t gb = blockIdx.x * 4u + (threadIdx.x >> 5), lane = threadIdx.x & 31u;
+    if (gb >= nblocks)
+        return;
+    const uint32_t bpw = window_blocks(S, AK_CB_THREADS), b = gb % bpw;
+    const ak_win   w   = ak_window(S, gb / bpw);
+    const uint32_t ry0 = (uint32_t)((size_t)b * AK_CB_THREADS / w.W);
+    const uint32_t ry1 = (uint32_t)(((size_t)b * AK_CB_THREADS + AK_CB_THREADS - 1) / w.W);
+    uint32_t      *out = B.blist + ak_blist_base(w, bpw, b);
+    uint32_t       n   = 0;
+    for (uint32_t l0 = 0; l0 < w.nl; l0 += 32) {
+        const uint32_t l  = l0 + lane;
+        bool           on = false;
+        if (l < w.nl) {
+            const uint4 bx = ak_pair_box(S, w.first + l);
+            on             = bx.y <= ry1 && bx.y + bx.w > ry0;
         }
-        const int take = min(want - cnt, sc.np - sc.pos);
-        if ((int)lane < take) {
-            /* bottom up: the window's lowest remaining, placed after the
-               chunk's; top down: its highest remaining, placed below them */
-            const int src = UP ? sc.pos + (int)lane : sc.np - sc.pos - take + (int)lane;
-            const int dst = UP ? cnt + (int)lane : want - cnt - take + (int)lane;
-            col[dst] = pd.c[src], pl[dst] = pd.p[src], cl[dst] = pd.l[src];
-        }
-        cnt += take, sc.pos += take;
-        __syncwarp();
+        const uint32_t m = __ballot_sync(0xffffffffu, on);
+        if (on)
+            out[n + __popc(m & ((1u << lane) - 1u))] = l;
+        n += __popc(m);
     }
     if (lane == 0)
-        *nact = cnt;
+        B.blk_na[gb] = n;
+}
+/* threads [0, n) of a block: chunk entries [e0, e0 + n) of the block's list
+   into (col, pl, cl) */
+__device__ __forceinline__ void ak_load_chunk(const ak_scene &S, const ak_win &w, const float4 *__restrict__ colors,
+                                              const uint32_t *__restrict__ list, uint32_t e0, uint32_t n,
+                                              float4 *col, ak_plane *pl, uint32_t *cl) {
+    const uint32_t i = threadIdx.x;
+    if (i < n) {
+        const uint32_t l = list[e0 + i];
+        cl[i]            = l;
+        pl[i]            = ak_plane_of(S, w, l);
+        col[i]           = colors[S.layer_path[ak_layer(S, w, l)]];
+    }
 }
 
 /* TILED: the tiles of a tiled scene (layers read through their planes'
@@ -623,8 +600,6 @@ __global__ void __launch_bounds__(TILED ? AK_CB_THREADS : AK_THREADS)
     __shared__ float4   col[AK_CHUNK];
     __shared__ ak_plane pl[TILED ? AK_CHUNK : 1];
     __shared__ uint32_t cl[TILED ? AK_CHUNK : 1];
-    __shared__ ak_pend  pend;
-    __shared__ int      nact;
     __shared__ float    red[NT / 32];
     /* grid: the window's pixel blocks, window after window */
     const uint32_t bpw = window_blocks(S, NT), b = blockIdx.x % bpw;
@@ -632,23 +607,16 @@ __global__ void __launch_bounds__(TILED ? AK_CB_THREADS : AK_THREADS)
     size_t         np = (size_t)w.W * w.H, px = (size_t)b * NT + threadIdx.x;
     bool           valid = px < np;
     const uint32_t x = valid ? (uint32_t)(px % w.W) : 0u, y = valid ? (uint32_t)(px / w.W) : 0u;
-    /* the block's window rows: a layer whose plane misses them all leaves
-       the block's pixels unchanged (coverage zero) and is passed over */
-    const uint32_t ry0 = (uint32_t)((size_t)b * NT / w.W), ry1 = (uint32_t)(((size_t)b * NT + NT - 1) / w.W);
     float4         C     = S.bg;
     float4        *ckpt  = B.ckpt + w.ckpt;
     if (TILED) {
-        ak_scan  sc{0u, 0, 0};
-        uint32_t tot = 0;
-        for (uint32_t c = 0;; c++) {
+        const uint32_t  ntot = B.blk_na[blockIdx.x];
+        const uint32_t *list = B.blist + ak_blist_base(w, bpw, b);
+        for (uint32_t c = 0; c * AK_CHUNK < ntot; c++) {
+            const int na = (int)min((uint32_t)AK_CHUNK, ntot - c * AK_CHUNK);
             __syncthreads();
-            if (threadIdx.x < 32)
-                ak_fill_chunk<true>(S, w, colors, ry0, ry1, sc, pend, AK_CHUNK, col, pl, cl, &nact);
+            ak_load_chunk(S, w, colors, list, c * AK_CHUNK, (uint32_t)na, col, pl, cl);
             __syncthreads();
-            const int na = nact;
-            if (na == 0)
-                break;
-            tot += (uint32_t)na;
             if (!valid)
                 continue;
             ckpt[(size_t)c * np + px] = C;
@@ -663,8 +631,6 @@ __global__ void __launch_bounds__(TILED ? AK_CB_THREADS : AK_THREADS)
                 if (i < na)
                     C = blend(cover(A[i]), col[i], C);
         }
-        if (threadIdx.x == 0)
-            B.blk_na[blockIdx.x] = tot;
     } else {
         for (uint32_t lb = 0; lb < w.nl; lb += AK_CHUNK) {
             uint32_t n = min((uint32_t)AK_CHUNK, w.nl - lb);
@@ -739,8 +705,6 @@ __global__ void __launch_bounds__(AK_CB_THREADS)
     __shared__ float4   col[AK_CHUNK];
     __shared__ ak_plane pl[TILED ? AK_CHUNK : 1];
     __shared__ uint32_t cl[TILED ? AK_CHUNK : 1];
-    __shared__ ak_pend  pend;
-    __shared__ int      nact;
     __shared__ float4 sB[AK_CHUNK][AK_CB_THREADS]; /* colour under each layer of the chunk */
     __shared__ float  sA[AK_CHUNK][AK_CB_THREADS]; /* the chunk's areas */
     __shared__ float  red[AK_CB_THREADS / 32][AK_CHUNK * 4];
@@ -752,11 +716,6 @@ __global__ void __launch_bounds__(AK_CB_THREADS)
     float4         g     = make_float4(0.f, 0.f, 0.f, 0.f);
     const float4  *ckpt  = B.ckpt + w.ckpt;
     const uint32_t x = valid ? (uint32_t)(px % w.W) : 0u, y = valid ? (uint32_t)(px / w.W) : 0u;
-    /* the block's window rows: layers whose planes miss them are passed over
-       (no coverage, no gradient, no colour partial: the reduction reads a
-       layer's partials only from the blocks its plane reaches) */
-    const uint32_t ry0 = (uint32_t)((size_t)b * AK_CB_THREADS / w.W);
-    const uint32_t ry1 = (uint32_t)(((size_t)b * AK_CB_THREADS + AK_CB_THREADS - 1) / w.W);
     if (valid) {
         const size_t cp = ((size_t)w.y0 + px / w.W) * S.CW + w.x0 + px % w.W; /* on the canvas */
         if (d_canvas) {
@@ -769,23 +728,24 @@ __global__ void __launch_bounds__(AK_CB_THREADS)
     }
     float    T    = 1.f; /* transmittance of the layers above */
     uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    /* chunks from the top: tiled, the block's packed chunks of active layers
-       (the forward's count; the top one holds the remainder); else chunks of
-       AK_CHUNK layers */
-    const uint32_t ntot = TILED ? B.blk_na[blockIdx.x] : w.nl;
-    uint32_t       nch  = (ntot + AK_CHUNK - 1) / AK_CHUNK;
-    ak_scan        sc{w.nl, 0, 0};
+    /* chunks from the top: tiled, the block's listed layers (the layers
+       whose planes reach its rows: a layer outside them has no coverage, no
+       gradient and no colour partial here, and the reduction reads a
+       layer's partials only from the blocks its plane reaches) in chunks of
+       AK_CHUNK, the top one holding the remainder; else chunks of AK_CHUNK
+       layers */
+    const uint32_t  ntot = TILED ? B.blk_na[blockIdx.x] : w.nl;
+    const uint32_t *list = TILED ? B.blist + ak_blist_base(w, bpw, b) : nullptr;
+    uint32_t        nch  = (ntot + AK_CHUNK - 1) / AK_CHUNK;
     for (uint32_t ch = nch; ch-- > 0;) {
         const uint32_t lb = ch * AK_CHUNK, n = min((uint32_t)AK_CHUNK, ntot - lb);
         __syncthreads();
-        if (TILED && threadIdx.x < 32)
-            ak_fill_chunk<false>(S, w, colors, ry0, ry1, sc, pend, (int)n, col, pl, cl, &nact);
-        else if (!TILED && threadIdx.x < n)
+        if (TILED)
+            ak_load_chunk(S, w, colors, list, lb, n, col, pl, cl);
+        else if (threadIdx.x < n)
             col[threadIdx.x] = colors[S.layer_path[lb + threadIdx.x]];
         __syncthreads();
-        const int na = TILED ? nact : (int)n; /* the chunk's layers [0, na), in order */
-        if (na == 0)
-            continue;
+        const int na = (int)n; /* the chunk's layers [0, na), in order */
         float4 Bc = valid ? ckpt[(size_t)ch * np + px] : make_float4(0.f, 0.f, 0.f, 0.f);
         {
             float A[AK_CHUNK];
@@ -1134,8 +1094,11 @@ static uint32_t windows(const ak_scene &S) { return S.tiles ? S.ntiles : 1u; }
 uint32_t ak_pixel_blocks_all(const ak_scene &S) { return ak_pixel_blocks(S) * windows(S); }
 cudaError_t ak_launch_composite(cudaStream_t st, const ak_scene &S, const ak_bufs &B, const float4 *colors,
                                 const float4 *target, float *loss_part) {
-    if (S.tiles)
-        ak_composite<true><<<ak_pixel_blocks_all(S), AK_CB_THREADS, 0, st>>>(S, B, colors, target, loss_part);
+    if (S.tiles) {
+        const uint32_t nb = ak_pixel_blocks_all(S);
+        ak_block_lists<<<(nb + 3) / 4, 128, 0, st>>>(S, B, nb);
+        ak_composite<true><<<nb, AK_CB_THREADS, 0, st>>>(S, B, colors, target, loss_part);
+    }
     else
         ak_composite<false><<<ak_pixel_blocks_all(S), AK_THREADS, 0, st>>>(S, B, colors, target, loss_part);
     return cudaGetLastError();

@@ -66,7 +66,9 @@ struct ak_bufs {
     float4         *ckpt;    /* ceil(nlayers / AK_CHUNK) * W * H: colour under every chunk */
     float4         *canvas;  /* W * H */
     uint32_t       *status;
-    uint32_t       *blk_na;  /* tiled scenes: per compositing block, its active layers (forward -> adjoint) */
+    uint32_t       *blk_na;  /* tiled scenes: per compositing block, how many layers reach its rows */
+    uint32_t       *blist;   /* tiled scenes: those layers (tile-local, in order); block b of tile t
+                                from (first pair of t) * blocks per tile + b * (pairs of t) */
 };
 
 /* lanes: one lane per segment (scenes of small curves) instead of a warp */
