@@ -14,11 +14,12 @@
  * A tiled scene (create_tiled) keeps the same kernels and runs each of them
  * once over every square tile of the canvas.  After the flattening, every
  * layer's box in pixels (from its points, strokes widened by half their
- * width; a layer's area is exactly zero outside it), a flag per (tile,
- * layer), one exclusive scan of the flags and a compaction give the (tile,
- * layer) pairs, tile by tile in scene order, each with the layer's box inside
- * the tile; a pair's area plane covers only that box (planes placed by a
- * scan of their sizes).  The per-tile counts and the box total are read back
+ * width; a layer's area is exactly zero outside it), two sweeps over every
+ * (tile, layer) entry, testing the boxes as they go (counts per run of
+ * entries and per tile, then a scan of the runs and the compaction), give
+ * the (tile, layer) pairs, tile by tile in scene order, each with the
+ * layer's box inside the tile; a pair's area plane covers only that box
+ * (planes placed by a scan of their sizes).  The per-tile counts and the box total are read back
  * (the one synchronisation of a tiled forward) to size the planes and every
  * tile's checkpoints, all kept resident for the backward.  A coverage block
  * covers its pair's box; a compositing thread one pixel of a tile, reading a
@@ -54,13 +55,14 @@ struct _vkvg_gb300_analytic_t {
     bool        timing = false;
     cudaEvent_t ev[8]  = {};
     /* tiled scenes: tile side (0: one window, the whole canvas), tiles
-       across and down, per-layer boxes, flags and their scan, the (tile,
-       layer) pairs' scene layers and tiles, per tile its pairs and plane
-       offsets (pinned, then on the device), and the scene the tiled launches
-       take (TS: every tile at once) */
+       across and down, per-layer boxes, per run of (tile, layer) entries
+       its pair count (d_flags) and their scan (d_fpos), per tile its pair
+       count, the pairs' scene layers and tiles, per tile its pairs and
+       plane offsets (pinned, then on the device), and the scene the tiled
+       launches take (TS: every tile at once) */
     uint32_t  tile = 0, ntx = 1, nty = 1;
     DevBuf    d_box, d_tot, d_flags, d_fpos, d_fscan, d_list, d_ptile, d_pbox, d_psize, d_poff, d_pscan, d_tinfo,
-              d_blkna, d_blist;
+              d_blkna, d_blist, d_tcount;
     PinnedBuf h_tiles, h_tinfo;
     ak_scene  TS{};
     /* the last forward */
@@ -262,7 +264,7 @@ void vkvg_gb300_analytic_destroy(VkvgAnalytic a) {
                     &a->d_pts, &a->d_pt_nb, &a->d_area, &a->d_ckpt, &a->d_canvas, &a->d_loss_part, &a->d_loss,
                     &a->d_color_part, &a->d_gpts, &a->d_status, &a->d_box, &a->d_flags, &a->d_fpos, &a->d_fscan,
                     &a->d_list, &a->d_ptile, &a->d_tinfo, &a->d_tot, &a->d_pbox, &a->d_psize, &a->d_poff,
-                    &a->d_pscan, &a->d_blkna, &a->d_blist};
+                    &a->d_pscan, &a->d_blkna, &a->d_blist, &a->d_tcount};
     for (DevBuf *b : bs)
         b->release();
     a->h_mon.release();
@@ -304,59 +306,68 @@ cudaError_t tile_setup(VkvgAnalytic a, const float *widths) {
     cudaStream_t   st = a->stream;
     const uint32_t nt = a->ntx * a->nty, nl = a->nlayers;
     const uint64_t n  = (uint64_t)nt * nl;
-    if (n >= 0xFFFFFFFFull)
-        return cudaErrorMemoryAllocation; /* positions are 32-bit */
-    if (!a->d_flags.grow(4 * std::max<uint64_t>(n, 1)) || !a->d_fpos.grow(4 * (n + 1)) ||
-        !a->d_fscan.grow(4 * gb_scan_scratch_words((uint32_t)n) + 64) || !a->h_tiles.grow(4 * ((size_t)nt + 4)) ||
-        !a->h_tinfo.grow(sizeof(ak_tile_info) * nt) || !a->d_tinfo.grow(sizeof(ak_tile_info) * nt))
+    const uint32_t nr = ak_tile_runs(n);
+    if (!a->d_flags.grow(4 * ((size_t)nr + 1)) || !a->d_fpos.grow(4 * ((size_t)nr + 1)) ||
+        !a->d_fscan.grow(4 * gb_scan_scratch_words(nr) + 64) || !a->d_tcount.grow(4 * (size_t)nt) ||
+        !a->h_tiles.grow(4 * ((size_t)nt + 4)) || !a->h_tinfo.grow(sizeof(ak_tile_info) * nt) ||
+        !a->d_tinfo.grow(sizeof(ak_tile_info) * nt))
         return cudaErrorMemoryAllocation;
     ak_bufs     B = bufs(a);
     cudaError_t e = cudaMemsetAsync(a->d_tot.p, 0, 8, st);
     if (e == cudaSuccess)
+        e = cudaMemsetAsync(a->d_tcount.p, 0, 4 * (size_t)nt, st);
+    if (e == cudaSuccess)
         e = ak_launch_layer_boxes(st, a->S, B, widths, a->d_box.as<int4>(), a->d_tot.as<unsigned long long>());
+    /* every tile's pair count and every run's, the boxes tested as the
+       entries go by (no flag per entry is stored) */
     if (e == cudaSuccess)
-        e = ak_launch_tile_flags(st, nl, nt, a->ntx, a->tile, a->d_box.as<int4>(), a->d_flags.as<uint32_t>());
-    if (e == cudaSuccess)
-        e = gb_exclusive_scan_flags(st, a->d_flags.as<uint32_t>(), (uint32_t)n, a->d_fpos.as<uint32_t>(),
-                                    a->d_fscan.as<uint32_t>());
+        e = ak_launch_tile_count(st, n, nl, a->ntx, a->tile, a->d_box.as<int4>(), a->d_flags.as<uint32_t>(),
+                                 a->d_tcount.as<uint32_t>());
     uint32_t *h = (uint32_t *)a->h_tiles.p;
-    if (e == cudaSuccess) /* the position of every tile's first pair, the pair total, the box pixel total */
-        e = cudaMemcpy2DAsync(h, 4, a->d_fpos.p, (size_t)nl * 4, 4, nt, cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess)
-        e = cudaMemcpyAsync(h + nt, a->d_fpos.as<uint32_t>() + n, 4, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) /* the tiles' pair counts, the box pixel total */
+        e = cudaMemcpyAsync(h, a->d_tcount.p, 4 * (size_t)nt, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(h + nt + 2, a->d_tot.p, 8, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess)
         e = cudaStreamSynchronize(st);
-    gb_count_launch(5);
+    gb_count_launch(2);
     if (e != cudaSuccess)
         return e;
-    const uint32_t     total = h[nt];
+    uint64_t total64 = 0;
+    for (uint32_t t = 0; t < nt; t++)
+        total64 += h[t];
     unsigned long long area;
     memcpy(&area, h + nt + 2, sizeof area);
-    if (area >= 0xFFFFFFFFull) /* plane offsets are 32-bit element counts */
+    /* pair positions and plane offsets are 32-bit */
+    if (total64 >= 0xFFFFFFFFull || area >= 0xFFFFFFFFull)
         return cudaErrorMemoryAllocation;
-    const size_t np1 = (size_t)std::max<uint32_t>(total, 1);
+    const uint32_t total = (uint32_t)total64;
+    const size_t   np1   = (size_t)std::max<uint32_t>(total, 1);
     if (!a->d_list.grow(4 * np1) || !a->d_ptile.grow(4 * np1) || !a->d_pbox.grow(8 * np1) ||
         !a->d_psize.grow(4 * np1) || !a->d_poff.grow(4 * (np1 + 1)) ||
         !a->d_pscan.grow(4 * gb_scan_scratch_words(total) + 64))
         return cudaErrorMemoryAllocation;
-    e = ak_launch_tile_lists(st, n, nl, a->ntx, a->tile, a->d_box.as<int4>(), a->d_flags.as<uint32_t>(),
-                             a->d_fpos.as<uint32_t>(), a->d_list.as<uint32_t>(), a->d_ptile.as<uint32_t>(),
-                             a->d_pbox.as<uint2>(), a->d_psize.as<uint32_t>());
+    /* the runs' first pairs, then the pairs in (tile, layer) order */
+    e = gb_exclusive_scan(st, a->d_flags.as<uint32_t>(), nr, a->d_fpos.as<uint32_t>(), a->d_fscan.as<uint32_t>());
+    if (e == cudaSuccess)
+        e = ak_launch_tile_lists(st, n, nl, a->ntx, a->tile, a->d_box.as<int4>(), a->d_fpos.as<uint32_t>(),
+                                 a->d_list.as<uint32_t>(), a->d_ptile.as<uint32_t>(), a->d_pbox.as<uint2>(),
+                                 a->d_psize.as<uint32_t>());
     if (e == cudaSuccess) /* every pair's plane: the running sum of the box sizes */
         e = gb_exclusive_scan(st, a->d_psize.as<uint32_t>(), total, a->d_poff.as<uint32_t>(),
                               a->d_pscan.as<uint32_t>());
-    gb_count_launch(4);
-    /* every tile's checkpoints: a tile of tw x th pixels and c layers holds
-       ceil(c / AK_CHUNK) planes of tw x th */
-    ak_tile_info *ti   = (ak_tile_info *)a->h_tinfo.p;
-    size_t        ckpt = 0;
+    gb_count_launch((nr ? 3 : 0) + (n ? 1 : 0) + (total ? 3 : 0));
+    /* every tile's first pair and checkpoints: a tile of tw x th pixels and
+       c layers holds ceil(c / AK_CHUNK) planes of tw x th */
+    ak_tile_info *ti    = (ak_tile_info *)a->h_tinfo.p;
+    size_t        ckpt  = 0;
+    uint32_t      first = 0;
     for (uint32_t t = 0; t < nt; t++) {
         const uint32_t tw = std::min(a->tile, a->W - (t % a->ntx) * a->tile);
         const uint32_t th = std::min(a->tile, a->H - (t / a->ntx) * a->tile);
-        const size_t   px = (size_t)tw * th, cnt = (t + 1 < nt ? h[t + 1] : total) - h[t];
-        ti[t].first = h[t], ti[t].count = (uint32_t)cnt, ti[t].ckpt = ckpt;
+        const size_t   px = (size_t)tw * th, cnt = h[t];
+        ti[t].first = first, ti[t].count = (uint32_t)cnt, ti[t].ckpt = ckpt;
+        first += (uint32_t)cnt;
         ckpt += px * ((cnt + AK_CHUNK - 1) / AK_CHUNK);
     }
     ak_scene &T = a->TS;

@@ -1007,36 +1007,93 @@ __global__ void ak_layer_boxes(ak_scene S, ak_bufs B, const float *__restrict__ 
 }
 
 /* flags[t * nlayers + l] = 1 when layer l's box meets tile t */
-__global__ void ak_tile_flags(uint32_t nlayers, uint64_t n, uint32_t ntx, uint32_t tile, const int4 *__restrict__ box,
-                              uint32_t *__restrict__ flags) {
-    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n)
-        return;
-    const uint32_t t = (uint32_t)(i / nlayers), l = (uint32_t)(i % nlayers);
-    const int      tx0 = (int)((t % ntx) * tile), ty0 = (int)((t / ntx) * tile);
-    const int4     b   = box[l];
-    flags[i] = b.x <= tx0 + (int)tile - 1 && b.z >= tx0 && b.y <= ty0 + (int)tile - 1 && b.w >= ty0 ? 1u : 0u;
+/* (tile, layer) entries: a block takes a run of AK_TP_RUN entries, a warp 512
+   of them as 16 rows of 32 (coalesced box loads), each lane stepping its
+   entry's (tile, layer) by 32 a row */
+#define AK_TP_THREADS 512
+#define AK_TP_ROWS    (AK_TP_RUN / AK_TP_THREADS)
+struct ak_tp_it {
+    uint32_t t, l;
+};
+__device__ __forceinline__ ak_tp_it ak_tp_first(uint64_t i, uint32_t nl) {
+    return ak_tp_it{(uint32_t)(i / nl), (uint32_t)(i % nl)};
 }
-
-/* the (tile, layer) pairs in order: for flagged entry i its layer, tile,
-   box inside the tile (x0 | y0 << 16, w | h << 16, tile coordinates) and
-   pixel count */
-__global__ void ak_tile_lists(uint64_t n, uint32_t nlayers, uint32_t ntx, uint32_t tile, const int4 *__restrict__ box,
-                              const uint32_t *__restrict__ flags, const uint32_t *__restrict__ pos,
-                              uint32_t *__restrict__ list, uint32_t *__restrict__ ptile, uint2 *__restrict__ pbox,
-                              uint32_t *__restrict__ psize) {
-    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n || !flags[i])
-        return;
-    const uint32_t t = (uint32_t)(i / nlayers), l = (uint32_t)(i % nlayers), j = pos[i];
-    const int      tx0 = (int)((t % ntx) * tile), ty0 = (int)((t / ntx) * tile);
-    const int4     b   = box[l];
-    const int      x0 = max(b.x, tx0) - tx0, x1 = min(b.z, tx0 + (int)tile - 1) - tx0;
-    const int      y0 = max(b.y, ty0) - ty0, y1 = min(b.w, ty0 + (int)tile - 1) - ty0;
-    list[j]  = l;
-    ptile[j] = t;
-    pbox[j]  = make_uint2((uint32_t)x0 | (uint32_t)y0 << 16, (uint32_t)(x1 - x0 + 1) | (uint32_t)(y1 - y0 + 1) << 16);
-    psize[j] = (uint32_t)((x1 - x0 + 1) * (y1 - y0 + 1));
+__device__ __forceinline__ void ak_tp_step(ak_tp_it &e, uint32_t nl) {
+    e.l += 32u;
+    while (e.l >= nl)
+        e.l -= nl, e.t++;
+}
+__device__ __forceinline__ bool ak_tp_hit(const int4 &b, uint32_t t, uint32_t ntx, uint32_t tile) {
+    const int tx0 = (int)((t % ntx) * tile), ty0 = (int)((t / ntx) * tile);
+    return b.x <= tx0 + (int)tile - 1 && b.z >= tx0 && b.y <= ty0 + (int)tile - 1 && b.w >= ty0;
+}
+__global__ void __launch_bounds__(AK_TP_THREADS)
+    ak_tile_count(uint64_t n, uint32_t nl, uint32_t ntx, uint32_t tile, const int4 *__restrict__ box,
+                  uint32_t *__restrict__ bsum, uint32_t *__restrict__ tcount) {
+    __shared__ uint32_t s_w[AK_TP_THREADS / 32];
+    const uint32_t      lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
+    const uint64_t      i0   = (uint64_t)blockIdx.x * AK_TP_RUN + (uint64_t)w * (32u * AK_TP_ROWS) + lane;
+    ak_tp_it            e    = ak_tp_first(i0, nl);
+    uint32_t            cnt  = 0;
+    for (int k = 0; k < AK_TP_ROWS; k++) {
+        const uint64_t i   = i0 + 32u * (uint32_t)k;
+        const bool     hit = i < n && ak_tp_hit(box[e.l], e.t, ntx, tile);
+        if (hit)
+            atomicAdd(&tcount[e.t], 1u);
+        cnt += __popc(__ballot_sync(0xffffffffu, hit));
+        ak_tp_step(e, nl);
+    }
+    if (lane == 0)
+        s_w[w] = cnt;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        uint32_t v = threadIdx.x < AK_TP_THREADS / 32 ? s_w[threadIdx.x] : 0u;
+        v          = __reduce_add_sync(0xffffffffu, v);
+        if (threadIdx.x == 0)
+            bsum[blockIdx.x] = v;
+    }
+}
+__global__ void __launch_bounds__(AK_TP_THREADS)
+    ak_tile_lists(uint64_t n, uint32_t nl, uint32_t ntx, uint32_t tile, const int4 *__restrict__ box,
+                  const uint32_t *__restrict__ bpos, uint32_t *__restrict__ list, uint32_t *__restrict__ ptile,
+                  uint2 *__restrict__ pbox, uint32_t *__restrict__ psize) {
+    __shared__ uint32_t s_w[AK_TP_THREADS / 32];
+    const uint32_t      lane = threadIdx.x & 31u, w = threadIdx.x >> 5, lt = (1u << lane) - 1u;
+    const uint64_t      i0   = (uint64_t)blockIdx.x * AK_TP_RUN + (uint64_t)w * (32u * AK_TP_ROWS) + lane;
+    ak_tp_it            e    = ak_tp_first(i0, nl);
+    uint32_t            hits = 0, cnt = 0; /* bit k: this lane's entry of row k is a pair */
+    for (int k = 0; k < AK_TP_ROWS; k++) {
+        const uint64_t i   = i0 + 32u * (uint32_t)k;
+        const bool     hit = i < n && ak_tp_hit(box[e.l], e.t, ntx, tile);
+        hits |= (hit ? 1u : 0u) << k;
+        cnt += __popc(__ballot_sync(0xffffffffu, hit));
+        ak_tp_step(e, nl);
+    }
+    if (lane == 0)
+        s_w[w] = cnt;
+    __syncthreads();
+    uint32_t j = bpos[blockIdx.x];
+    for (uint32_t q = 0; q < w; q++)
+        j += s_w[q];
+    e = ak_tp_first(i0, nl);
+    for (int k = 0; k < AK_TP_ROWS; k++) {
+        const bool     hit = (hits >> k) & 1u;
+        const uint32_t m   = __ballot_sync(0xffffffffu, hit);
+        if (hit) {
+            const uint32_t p   = j + __popc(m & lt);
+            const int      tx0 = (int)((e.t % ntx) * tile), ty0 = (int)((e.t / ntx) * tile);
+            const int4     b   = box[e.l];
+            const int      x0 = max(b.x, tx0) - tx0, x1 = min(b.z, tx0 + (int)tile - 1) - tx0;
+            const int      y0 = max(b.y, ty0) - ty0, y1 = min(b.w, ty0 + (int)tile - 1) - ty0;
+            list[p]  = e.l;
+            ptile[p] = e.t;
+            pbox[p]  = make_uint2((uint32_t)x0 | (uint32_t)y0 << 16,
+                                  (uint32_t)(x1 - x0 + 1) | (uint32_t)(y1 - y0 + 1) << 16);
+            psize[p] = (uint32_t)((x1 - x0 + 1) * (y1 - y0 + 1));
+        }
+        j += __popc(m);
+        ak_tp_step(e, nl);
+    }
 }
 
 __global__ void ak_adam(float *__restrict__ p, const float *__restrict__ g, float *__restrict__ m,
@@ -1148,19 +1205,19 @@ cudaError_t ak_launch_layer_boxes(cudaStream_t st, const ak_scene &S, const ak_b
         ak_layer_boxes<<<(S.nlayers * 32 + 255) / 256, 256, 0, st>>>(S, B, widths, box, total);
     return cudaGetLastError();
 }
-cudaError_t ak_launch_tile_flags(cudaStream_t st, uint32_t nlayers, uint32_t ntiles, uint32_t ntx, uint32_t tile,
-                                 const int4 *box, uint32_t *flags) {
-    const uint64_t n = (uint64_t)nlayers * ntiles;
+uint32_t ak_tile_runs(uint64_t n) { return (uint32_t)((n + AK_TP_RUN - 1) / AK_TP_RUN); }
+cudaError_t ak_launch_tile_count(cudaStream_t st, uint64_t n, uint32_t nlayers, uint32_t ntx, uint32_t tile,
+                                 const int4 *box, uint32_t *bsum, uint32_t *tcount) {
     if (n)
-        ak_tile_flags<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(nlayers, n, ntx, tile, box, flags);
+        ak_tile_count<<<ak_tile_runs(n), AK_TP_THREADS, 0, st>>>(n, nlayers, ntx, tile, box, bsum, tcount);
     return cudaGetLastError();
 }
 cudaError_t ak_launch_tile_lists(cudaStream_t st, uint64_t n, uint32_t nlayers, uint32_t ntx, uint32_t tile,
-                                 const int4 *box, const uint32_t *flags, const uint32_t *pos, uint32_t *list,
-                                 uint32_t *ptile, uint2 *pbox, uint32_t *psize) {
+                                 const int4 *box, const uint32_t *bpos, uint32_t *list, uint32_t *ptile, uint2 *pbox,
+                                 uint32_t *psize) {
     if (n)
-        ak_tile_lists<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, nlayers, ntx, tile, box, flags, pos, list, ptile,
-                                                                     pbox, psize);
+        ak_tile_lists<<<ak_tile_runs(n), AK_TP_THREADS, 0, st>>>(n, nlayers, ntx, tile, box, bpos, list, ptile, pbox,
+                                                                   psize);
     return cudaGetLastError();
 }
 cudaError_t ak_launch_adam(cudaStream_t st, float *param, const float *grad, float *m, float *v, uint32_t n, float lr,

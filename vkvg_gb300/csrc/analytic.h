@@ -95,15 +95,21 @@ cudaError_t ak_launch_reduce(cudaStream_t st, const ak_scene &S, uint32_t nblock
    pixel), the boxes' pixel total added to *total */
 cudaError_t ak_launch_layer_boxes(cudaStream_t st, const ak_scene &S, const ak_bufs &B, const float *widths, int4 *box,
                                   unsigned long long *total);
-/* flags[t * nlayers + l] = 1 when layer l's box meets tile t */
-cudaError_t ak_launch_tile_flags(cudaStream_t st, uint32_t nlayers, uint32_t ntiles, uint32_t ntx, uint32_t tile,
-                                 const int4 *box, uint32_t *flags);
-/* for each flagged entry i (pos: exclusive scan of the flags), pair pos[i]:
-   its layer i % nlayers, its tile i / nlayers, the layer's box inside the
-   tile and its pixel count */
+/* The (tile, layer) pairs, entry i = t * nlayers + l of every tile and layer
+   (a pair when layer l's box meets tile t), in two sweeps that test the
+   boxes as they go: _count sums each run of AK_TP_RUN entries into
+   bsum[run] and counts each tile's pairs into tcount[t] (zeroed by the
+   caller); after an exclusive scan of bsum into bpos, _lists writes pair
+   bpos-rank of every hit: its layer, its tile, the layer's box inside the
+   tile (x0 | y0 << 16, w | h << 16) and its pixel count.  Runs:
+   ak_tile_runs(n). */
+#define AK_TP_RUN 8192
+uint32_t    ak_tile_runs(uint64_t n);
+cudaError_t ak_launch_tile_count(cudaStream_t st, uint64_t n, uint32_t nlayers, uint32_t ntx, uint32_t tile,
+                                 const int4 *box, uint32_t *bsum, uint32_t *tcount);
 cudaError_t ak_launch_tile_lists(cudaStream_t st, uint64_t n, uint32_t nlayers, uint32_t ntx, uint32_t tile,
-                                 const int4 *box, const uint32_t *flags, const uint32_t *pos, uint32_t *list,
-                                 uint32_t *ptile, uint2 *pbox, uint32_t *psize);
+                                 const int4 *box, const uint32_t *bpos, uint32_t *list, uint32_t *ptile, uint2 *pbox,
+                                 uint32_t *psize);
 cudaError_t ak_launch_adam(cudaStream_t st, float *param, const float *grad, float *m, float *v, uint32_t n, float lr,
                            float beta1, float beta2, float eps, uint32_t step, float lo, float hi);
 /* pixel blocks of ak_composite (loss partials) and of ak_composite_bwd per
