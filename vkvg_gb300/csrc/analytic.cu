@@ -312,19 +312,6 @@ __device__ __forceinline__ ak_win ak_window(const ak_scene &S, uint32_t t) {
     w.ckpt  = (size_t)ti.ckpt;
     return w;
 }
-/* where window layer q's area plane lies: its first element and its box in
-   the window (the whole window, or a tiled pair's box inside its tile) */
-struct ak_plane {
-    size_t   base;
-    uint32_t x0, y0, w, h;
-};
-__device__ __forceinline__ ak_plane ak_plane_of(const ak_scene &S, const ak_win &w, uint32_t q);
-/* the plane element of window pixel (x, y), or -1 where the plane does not
-   reach (the layer's area is zero there) */
-__device__ __forceinline__ long long ak_plane_at(const ak_plane &P, uint32_t x, uint32_t y) {
-    const uint32_t dx = x - P.x0, dy = y - P.y0;
-    return dx < P.w && dy < P.h ? (long long)(P.base + (size_t)dy * P.w + dx) : -1ll;
-}
 /* a (tile, layer) pair's box inside its tile: x0, y0, w, h */
 __device__ __forceinline__ uint4 ak_pair_box(const ak_scene &S, uint32_t j) {
     const uint2 b = S.pair_box[j];
@@ -333,20 +320,6 @@ __device__ __forceinline__ uint4 ak_pair_box(const ak_scene &S, uint32_t j) {
 /* blocks of n pixels per window (the canvas, or a tile) */
 __host__ __device__ __forceinline__ uint32_t window_blocks(const ak_scene &S, uint32_t n) {
     return (uint32_t)(((size_t)S.W * S.H + n - 1) / n);
-}
-/* the scene layer of window layer l */
-__device__ __forceinline__ uint32_t ak_layer(const ak_scene &S, const ak_win &w, uint32_t l) {
-    return S.layer_map ? S.layer_map[w.first + l] : l;
-}
-__device__ __forceinline__ ak_plane ak_plane_of(const ak_scene &S, const ak_win &w, uint32_t q) {
-    ak_plane P;
-    if (!S.tiles) {
-        P.base = (size_t)q * w.W * w.H, P.x0 = P.y0 = 0, P.w = w.W, P.h = w.H;
-        return P;
-    }
-    const uint4 bx = ak_pair_box(S, w.first + q);
-    P.base = S.pair_off[w.first + q], P.x0 = bx.x, P.y0 = bx.y, P.w = bx.z, P.h = bx.w;
-    return P;
 }
 /* a coverage block's window, its scene layer and its area plane:
    blockIdx.x is the layer (the window is the canvas), or the (tile, layer)
@@ -575,17 +548,30 @@ __global__ void __launch_bounds__(128) ak_block_lists(ak_scene S, ak_bufs B, uin
     if (lane == 0)
         B.blk_na[gb] = n;
 }
-/* threads [0, n) of a block: chunk entries [e0, e0 + n) of the block's list
-   into (col, pl, cl) */
-__device__ __forceinline__ void ak_load_chunk(const ak_scene &S, const ak_win &w, const float4 *__restrict__ colors,
-                                              const uint32_t *__restrict__ list, uint32_t e0, uint32_t n,
-                                              float4 *col, ak_plane *pl, uint32_t *cl) {
+/* A listed layer as the compositing kernels keep it in shared memory: its
+   pair's plane offset and box inside the tile (x0 | y0 << 16, w | h << 16),
+   its tile-local index and colour.  A block loads AK_WIN entries of its list
+   at a time (one thread each), so the dependent loads behind an entry
+   (list, pair, path, colour) are paid once per AK_WIN / AK_CHUNK chunks. */
+#define AK_WIN 64
+struct ak_tplane {
+    uint32_t base, xy, wh;
+};
+__device__ __forceinline__ long long ak_tplane_at(const ak_tplane &P, uint32_t x, uint32_t y) {
+    const uint32_t dx = x - (P.xy & 0xFFFFu), dy = y - (P.xy >> 16), pw = P.wh & 0xFFFFu;
+    return dx < pw && dy < (P.wh >> 16) ? (long long)P.base + (long long)dy * pw + dx : -1ll;
+}
+/* threads [0, n) of a block: list entries [e0, e0 + n) into (col, pl, cl) */
+__device__ __forceinline__ void ak_load_window(const ak_scene &S, const ak_win &w, const float4 *__restrict__ colors,
+                                               const uint32_t *__restrict__ list, uint32_t e0, uint32_t n,
+                                               float4 *col, ak_tplane *pl, uint32_t *cl) {
     const uint32_t i = threadIdx.x;
     if (i < n) {
-        const uint32_t l = list[e0 + i];
-        cl[i]            = l;
-        pl[i]            = ak_plane_of(S, w, l);
-        col[i]           = colors[S.layer_path[ak_layer(S, w, l)]];
+        const uint32_t l = list[e0 + i], j = w.first + l;
+        const uint2    bx = S.pair_box[j];
+        cl[i]             = l;
+        pl[i]             = ak_tplane{S.pair_off[j], bx.x, bx.y};
+        col[i]            = colors[S.layer_path[S.layer_map[j]]];
     }
 }
 
@@ -596,11 +582,11 @@ template <bool TILED>
 __global__ void __launch_bounds__(TILED ? AK_CB_THREADS : AK_THREADS)
     ak_composite(ak_scene S, ak_bufs B, const float4 *__restrict__ colors, const float4 *__restrict__ target,
                  float *__restrict__ loss_part) {
-    constexpr int       NT = TILED ? AK_CB_THREADS : AK_THREADS;
-    __shared__ float4   col[AK_CHUNK];
-    __shared__ ak_plane pl[TILED ? AK_CHUNK : 1];
-    __shared__ uint32_t cl[TILED ? AK_CHUNK : 1];
-    __shared__ float    red[NT / 32];
+    constexpr int        NT = TILED ? AK_CB_THREADS : AK_THREADS;
+    __shared__ float4    col[TILED ? AK_WIN : AK_CHUNK];
+    __shared__ ak_tplane pl[TILED ? AK_WIN : 1];
+    __shared__ uint32_t  cl[TILED ? AK_WIN : 1];
+    __shared__ float     red[NT / 32];
     /* grid: the window's pixel blocks, window after window */
     const uint32_t bpw = window_blocks(S, NT), b = blockIdx.x % bpw;
     const ak_win   w   = ak_window(S, blockIdx.x / bpw);
@@ -613,23 +599,26 @@ __global__ void __launch_bounds__(TILED ? AK_CB_THREADS : AK_THREADS)
         const uint32_t  ntot = B.blk_na[blockIdx.x];
         const uint32_t *list = B.blist + ak_blist_base(w, bpw, b);
         for (uint32_t c = 0; c * AK_CHUNK < ntot; c++) {
-            const int na = (int)min((uint32_t)AK_CHUNK, ntot - c * AK_CHUNK);
-            __syncthreads();
-            ak_load_chunk(S, w, colors, list, c * AK_CHUNK, (uint32_t)na, col, pl, cl);
-            __syncthreads();
+            const uint32_t e0 = c * AK_CHUNK, wb = e0 % AK_WIN;
+            const int      na = (int)min((uint32_t)AK_CHUNK, ntot - e0);
+            if (wb == 0) {
+                __syncthreads();
+                ak_load_window(S, w, colors, list, e0, min((uint32_t)AK_WIN, ntot - e0), col, pl, cl);
+                __syncthreads();
+            }
             if (!valid)
                 continue;
             ckpt[(size_t)c * np + px] = C;
             float A[AK_CHUNK];
 #pragma unroll
             for (int i = 0; i < AK_CHUNK; i++) {
-                const long long k = i < na ? ak_plane_at(pl[i], x, y) : -1ll;
+                const long long k = i < na ? ak_tplane_at(pl[wb + i], x, y) : -1ll;
                 A[i]              = k >= 0 ? B.area[k] : 0.f;
             }
 #pragma unroll
             for (int i = 0; i < AK_CHUNK; i++)
                 if (i < na)
-                    C = blend(cover(A[i]), col[i], C);
+                    C = blend(cover(A[i]), col[wb + i], C);
         }
     } else {
         for (uint32_t lb = 0; lb < w.nl; lb += AK_CHUNK) {
@@ -702,9 +691,9 @@ template <bool TILED>
 __global__ void __launch_bounds__(AK_CB_THREADS)
     ak_composite_bwd(ak_scene S, ak_bufs B, const float4 *__restrict__ colors, const float4 *__restrict__ target,
                      const float4 *__restrict__ d_canvas, float *__restrict__ color_part) {
-    __shared__ float4   col[AK_CHUNK];
-    __shared__ ak_plane pl[TILED ? AK_CHUNK : 1];
-    __shared__ uint32_t cl[TILED ? AK_CHUNK : 1];
+    __shared__ float4    col[TILED ? AK_WIN : AK_CHUNK];
+    __shared__ ak_tplane pl[TILED ? AK_WIN : 1];
+    __shared__ uint32_t  cl[TILED ? AK_WIN : 1];
     __shared__ float4 sB[AK_CHUNK][AK_CB_THREADS]; /* colour under each layer of the chunk */
     __shared__ float  sA[AK_CHUNK][AK_CB_THREADS]; /* the chunk's areas */
     __shared__ float  red[AK_CB_THREADS / 32][AK_CHUNK * 4];
@@ -737,13 +726,20 @@ __global__ void __launch_bounds__(AK_CB_THREADS)
     const uint32_t  ntot = TILED ? B.blk_na[blockIdx.x] : w.nl;
     const uint32_t *list = TILED ? B.blist + ak_blist_base(w, bpw, b) : nullptr;
     uint32_t        nch  = (ntot + AK_CHUNK - 1) / AK_CHUNK;
+    uint32_t        held = 0xFFFFFFFFu; /* the list window in shared memory */
     for (uint32_t ch = nch; ch-- > 0;) {
         const uint32_t lb = ch * AK_CHUNK, n = min((uint32_t)AK_CHUNK, ntot - lb);
+        const uint32_t wb = TILED ? lb % AK_WIN : 0u; /* the chunk's first entry in the window */
         __syncthreads();
-        if (TILED)
-            ak_load_chunk(S, w, colors, list, lb, n, col, pl, cl);
-        else if (threadIdx.x < n)
+        if (TILED) {
+            const uint32_t w0 = lb - wb;
+            if (w0 != held) {
+                ak_load_window(S, w, colors, list, w0, min((uint32_t)AK_WIN, ntot - w0), col, pl, cl);
+                held = w0;
+            }
+        } else if (threadIdx.x < n) {
             col[threadIdx.x] = colors[S.layer_path[lb + threadIdx.x]];
+        }
         __syncthreads();
         const int na = (int)n; /* the chunk's layers [0, na), in order */
         float4 Bc = valid ? ckpt[(size_t)ch * np + px] : make_float4(0.f, 0.f, 0.f, 0.f);
@@ -752,7 +748,7 @@ __global__ void __launch_bounds__(AK_CB_THREADS)
 #pragma unroll
             for (int i = 0; i < AK_CHUNK; i++) {
                 if (TILED) {
-                    const long long k = (valid && i < na) ? ak_plane_at(pl[i], x, y) : -1ll;
+                    const long long k = (valid && i < na) ? ak_tplane_at(pl[wb + i], x, y) : -1ll;
                     A[i]              = k >= 0 ? B.area[k] : 0.f;
                 } else {
                     A[i] = (valid && i < na) ? B.area[(size_t)(lb + i) * np + px] : 0.f;
@@ -763,7 +759,7 @@ __global__ void __launch_bounds__(AK_CB_THREADS)
                 if (i < na) {
                     sB[i][threadIdx.x] = Bc;
                     sA[i][threadIdx.x] = A[i];
-                    Bc                 = blend(cover(A[i]), col[i], Bc);
+                    Bc                 = blend(cover(A[i]), col[wb + i], Bc);
                 }
             }
         }
@@ -779,7 +775,7 @@ __global__ void __launch_bounds__(AK_CB_THREADS)
                 dc[4 * q8] = dc[4 * q8 + 1] = dc[4 * q8 + 2] = dc[4 * q8 + 3] = 0.f;
                 if (i >= na)
                     continue;
-                float4 c = col[i], Bq = sB[i][threadIdx.x];
+                float4 c = col[wb + i], Bq = sB[i][threadIdx.x];
                 float  Aq = sA[i][threadIdx.x];
                 float  al = cover(Aq);
                 float  gB = g.x * Bq.x + g.y * Bq.y + g.z * Bq.z + g.w * Bq.w;
@@ -787,7 +783,7 @@ __global__ void __launch_bounds__(AK_CB_THREADS)
                 float  da = T * (gc - c.w * gB);
                 float  gA = fabsf(Aq) < 1.f ? (Aq > 0.f ? da : Aq < 0.f ? -da : 0.f) : 0.f;
                 if (valid) {
-                    const long long k = TILED ? ak_plane_at(pl[i], x, y) : (long long)((size_t)(lb + i) * np + px);
+                    const long long k = TILED ? ak_tplane_at(pl[wb + i], x, y) : (long long)((size_t)(lb + i) * np + px);
                     if (k >= 0)
                         B.area[k] = gA;
                 }
@@ -805,7 +801,7 @@ __global__ void __launch_bounds__(AK_CB_THREADS)
                 s += red[k][threadIdx.x];
             /* one window: [block][layer][channel]; tiled: [pair][block of the tile][channel] */
             const uint32_t q = threadIdx.x >> 2, c = threadIdx.x & 3;
-            const size_t   i = S.tiles ? ((size_t)(w.first + cl[q]) * bpw + b) * 4 + c
+            const size_t   i = S.tiles ? ((size_t)(w.first + cl[wb + q]) * bpw + b) * 4 + c
                                        : ((size_t)b * S.nlayers + lb + q) * 4 + c;
             color_part[i] = s;
         }
