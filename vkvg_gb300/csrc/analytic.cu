@@ -1127,7 +1127,8 @@ size_t ak_cover_smem(uint32_t W) {
     return fwd > bwd ? fwd : bwd;
 }
 /* tiled scenes take the small blocks */
-static uint32_t cover_threads(const ak_scene &S) { return S.tiles ? AK_CB_THREADS : AK_THREADS; }
+#define AK_PAIR_THREADS 64
+static uint32_t cover_threads(const ak_scene &S) { return S.tiles ? AK_PAIR_THREADS : AK_THREADS; }
 
 template <int NT> static cudaError_t launch_cover(cudaStream_t st, const ak_scene &S, const ak_bufs &B, const float *widths) {
     const size_t smem = cover_fwd_smem(S.W, S.band, NT);
@@ -1140,7 +1141,7 @@ template <int NT> static cudaError_t launch_cover(cudaStream_t st, const ak_scen
 cudaError_t ak_launch_cover(cudaStream_t st, const ak_scene &S, const ak_bufs &B, const float *widths) {
     if (!S.nlayers)
         return cudaSuccess;
-    return cover_threads(S) == AK_CB_THREADS ? launch_cover<AK_CB_THREADS>(st, S, B, widths)
+    return cover_threads(S) == AK_PAIR_THREADS ? launch_cover<AK_PAIR_THREADS>(st, S, B, widths)
                                              : launch_cover<AK_THREADS>(st, S, B, widths);
 }
 static uint32_t windows(const ak_scene &S) { return S.tiles ? S.ntiles : 1u; }
@@ -1183,7 +1184,7 @@ cudaError_t ak_launch_cover_bwd(cudaStream_t st, const ak_scene &S, const ak_buf
                                 float2 *gpts, float *gwidth) {
     if (!S.nlayers)
         return cudaSuccess;
-    return cover_threads(S) == AK_CB_THREADS ? launch_cover_bwd<AK_CB_THREADS>(st, S, B, widths, gpts, gwidth)
+    return cover_threads(S) == AK_PAIR_THREADS ? launch_cover_bwd<AK_PAIR_THREADS>(st, S, B, widths, gpts, gwidth)
                                              : launch_cover_bwd<AK_THREADS>(st, S, B, widths, gpts, gwidth);
 }
 cudaError_t ak_launch_reduce(cudaStream_t st, const ak_scene &S, uint32_t nblocks, const float4 *color_part,
