@@ -109,7 +109,7 @@ struct Pipeline {
     int      narrow     = 0; /* the register-tile form geometry picked: 0 1024-pixel, 1 256-pixel, 2 128-pixel tiles */
     int      form_run   = -1; /* the raster form the last frame ran (as vkvg_gb300_debug_set_raster_form) */
     int      form_half  = 0;  /* the row form ran in half bands with 16-bit counters */
-    bool     row_draws  = false; /* the frame's draws span most of a 1024-pixel tile (the row form's case) */
+    bool     row_draws  = false; /* the row form's candidates: draws spanning most of a 1024-pixel tile, or few tiles */
     double   mean_width = 0.0;   /* edge-weighted mean draw width of a one-surface frame, pixels */
     bool     sparse_crossings(uint64_t ncells_run); /* records per active cell thin enough for the row form */
     uint32_t max_cell   = 0xFFFFFFFFu; /* record units of the heaviest cell (one-surface frames; else unknown) */

@@ -198,6 +198,14 @@ static cudaError_t readback_u32(Pipeline &pl, const uint32_t *dptr, uint32_t *ou
     memcpy(out, pl.rb.p, sizeof(uint32_t) * n);
     return cudaSuccess;
 }
+/* the current device's SM count (152 on a GB300 when the query fails) */
+static int sm_count() {
+    int dev = 0, n = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        n <= 0)
+        return 152;
+    return n;
+}
 static cudaError_t scan(Pipeline &pl, const uint32_t *in, uint32_t n, uint32_t *out) {
     if (!pl.scratch.grow(gb_scan_scratch_words(n) * 4 + 64))
         return cudaErrorMemoryAllocation;
@@ -424,9 +432,12 @@ cudaError_t Pipeline::geometry(const FrameHost &f, const gb_surf *surfs, uint32_
         const bool small = !wide || (ws[1] && ws[0] <= 384u * ws[1]);
         narrow           = !(stats && small) ? 0 : mxc <= 128u ? 2 : mxc <= 480u ? 1 : 0;
         /* candidates for the row form: draws that span most of a tile (mean
-           width over 640 pixels, weighted by edges); the raster launch then
-           checks how thinly their crossings spread */
-        row_draws  = stats && wide && ws[1] && ws[0] > 640u * ws[1];
+           width over 640 pixels, weighted by edges), or a surface whose
+           1024-pixel tiles give fewer CTAs than SMs (the row form's half
+           bands double them); the raster launch then checks how thinly
+           their crossings spread */
+        const uint64_t tile_ctas = (uint64_t)nbands * ((stats_w + 1023u) / 1024u);
+        row_draws = stats && wide && ws[1] && (ws[0] > 640u * ws[1] || tile_ctas < (uint64_t)sm_count());
         mean_width = ws[1] ? (double)ws[0] / (double)ws[1] : 0.0;
     }
     /* the cells' record offsets and the raster's per-band draw lists in one
