@@ -48,9 +48,6 @@ cudaError_t gb_launch_unpremultiply(cudaStream_t st, const uint32_t *in, size_t 
                                     uint32_t *out);
 size_t      gb_scan_scratch_words(uint32_t n);
 cudaError_t gb_exclusive_scan(cudaStream_t st, const uint32_t *in, uint32_t n, uint32_t *out, uint32_t *scratch);
-/* exclusive scan of (in != 0): positions of the nonzero entries, out[n] their count */
-cudaError_t gb_exclusive_scan_flags(cudaStream_t st, const uint32_t *in, uint32_t n, uint32_t *out,
-                                    uint32_t *scratch);
 
 cudaError_t gb_launch_flatten_count(cudaStream_t st, uint32_t nseg, const uint32_t *info, const float4 *a,
                                     const float4 *b, const float4 *c, const uint32_t *n, const uint32_t *aux,

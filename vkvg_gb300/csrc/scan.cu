@@ -47,15 +47,13 @@ __device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t *excl) 
     return total;
 }
 
-/* BIN: every nonzero input counts as 1 (a scan of flags read from counts) */
-template <bool BIN = false>
 __global__ void scan_block_sums(const uint32_t *__restrict__ in, uint32_t n, uint32_t *__restrict__ bsum) {
     uint32_t base = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_ITEMS;
     uint32_t s    = 0;
 #pragma unroll
     for (int k = 0; k < SCAN_ITEMS; k++)
         if (base + k < n)
-            s += BIN ? (in[base + k] != 0u ? 1u : 0u) : in[base + k];
+            s += in[base + k];
     uint32_t excl;
     uint32_t tot = block_excl_scan(s, &excl);
     if (threadIdx.x == 0)
@@ -76,7 +74,6 @@ __global__ void scan_block_prefix(uint32_t *__restrict__ bsum, uint32_t nb) {
     if (threadIdx.x == 0)
         bsum[nb] = carry;
 }
-template <bool BIN = false>
 __global__ void scan_apply(const uint32_t *__restrict__ in, uint32_t n, const uint32_t *__restrict__ bsum,
                            uint32_t *__restrict__ out) {
     uint32_t base = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_ITEMS;
@@ -84,8 +81,6 @@ __global__ void scan_apply(const uint32_t *__restrict__ in, uint32_t n, const ui
 #pragma unroll
     for (int k = 0; k < SCAN_ITEMS; k++) {
         v[k] = base + k < n ? in[base + k] : 0;
-        if (BIN)
-            v[k] = v[k] != 0u ? 1u : 0u;
         s += v[k];
     }
     uint32_t excl;
@@ -112,17 +107,6 @@ cudaError_t gb_exclusive_scan(cudaStream_t st, const uint32_t *in, uint32_t n, u
     scan_block_sums<<<nb, SCAN_THREADS, 0, st>>>(in, n, scratch);
     scan_block_prefix<<<1, SCAN_THREADS, 0, st>>>(scratch, nb);
     scan_apply<<<nb, SCAN_THREADS, 0, st>>>(in, n, scratch, out);
-    return cudaGetLastError();
-}
-/* out = exclusive scan of (in != 0), out[n] = their count */
-cudaError_t gb_exclusive_scan_flags(cudaStream_t st, const uint32_t *in, uint32_t n, uint32_t *out,
-                                    uint32_t *scratch) {
-    if (n == 0)
-        return cudaMemsetAsync(out, 0, sizeof(uint32_t), st);
-    uint32_t nb = (n + SCAN_TILE - 1) / SCAN_TILE;
-    scan_block_sums<true><<<nb, SCAN_THREADS, 0, st>>>(in, n, scratch);
-    scan_block_prefix<<<1, SCAN_THREADS, 0, st>>>(scratch, nb);
-    scan_apply<true><<<nb, SCAN_THREADS, 0, st>>>(in, n, scratch, out);
     return cudaGetLastError();
 }
 }
