@@ -305,8 +305,10 @@ namespace {
 cudaError_t tile_setup(VkvgAnalytic a, const float *widths) {
     cudaStream_t   st = a->stream;
     const uint32_t nt = a->ntx * a->nty, nl = a->nlayers;
-    const uint64_t n  = (uint64_t)nt * nl;
-    const uint32_t nr = ak_tile_runs(n);
+    const uint64_t nr64 = (uint64_t)nt * ((nl + AK_TP_LAYERS - 1) / AK_TP_LAYERS);
+    if (nr64 >= 0xFFFFFFFFull || (uint64_t)(nt + 7) / 8 > 65535u)
+        return cudaErrorMemoryAllocation; /* runs and the launch grid's tile groups */
+    const uint32_t nr = ak_tile_runs(nt, nl);
     if (!a->d_flags.grow(4 * ((size_t)nr + 1)) || !a->d_fpos.grow(4 * ((size_t)nr + 1)) ||
         !a->d_fscan.grow(4 * gb_scan_scratch_words(nr) + 64) || !a->d_tcount.grow(4 * (size_t)nt) ||
         !a->h_tiles.grow(4 * ((size_t)nt + 4)) || !a->h_tinfo.grow(sizeof(ak_tile_info) * nt) ||
@@ -321,7 +323,7 @@ cudaError_t tile_setup(VkvgAnalytic a, const float *widths) {
     /* every tile's pair count and every run's, the boxes tested as the
        entries go by (no flag per entry is stored) */
     if (e == cudaSuccess)
-        e = ak_launch_tile_count(st, n, nl, a->ntx, a->tile, a->d_box.as<int4>(), a->d_flags.as<uint32_t>(),
+        e = ak_launch_tile_count(st, nt, nl, a->ntx, a->tile, a->d_box.as<int4>(), a->d_flags.as<uint32_t>(),
                                  a->d_tcount.as<uint32_t>());
     uint32_t *h = (uint32_t *)a->h_tiles.p;
     if (e == cudaSuccess) /* the tiles' pair counts, the box pixel total */
@@ -350,13 +352,13 @@ cudaError_t tile_setup(VkvgAnalytic a, const float *widths) {
     /* the runs' first pairs, then the pairs in (tile, layer) order */
     e = gb_exclusive_scan(st, a->d_flags.as<uint32_t>(), nr, a->d_fpos.as<uint32_t>(), a->d_fscan.as<uint32_t>());
     if (e == cudaSuccess)
-        e = ak_launch_tile_lists(st, n, nl, a->ntx, a->tile, a->d_box.as<int4>(), a->d_fpos.as<uint32_t>(),
+        e = ak_launch_tile_lists(st, nt, nl, a->ntx, a->tile, a->d_box.as<int4>(), a->d_fpos.as<uint32_t>(),
                                  a->d_list.as<uint32_t>(), a->d_ptile.as<uint32_t>(), a->d_pbox.as<uint2>(),
                                  a->d_psize.as<uint32_t>());
     if (e == cudaSuccess) /* every pair's plane: the running sum of the box sizes */
         e = gb_exclusive_scan(st, a->d_psize.as<uint32_t>(), total, a->d_poff.as<uint32_t>(),
                               a->d_pscan.as<uint32_t>());
-    gb_count_launch((nr ? 3 : 0) + (n ? 1 : 0) + (total ? 3 : 0));
+    gb_count_launch((nr ? 4 : 0) + (total ? 3 : 0));
     /* every tile's first pair and checkpoints: a tile of tw x th pixels and
        c layers holds ceil(c / AK_CHUNK) planes of tw x th */
     ak_tile_info *ti    = (ak_tile_info *)a->h_tinfo.p;

@@ -1003,92 +1003,104 @@ __global__ void ak_layer_boxes(ak_scene S, ak_bufs B, const float *__restrict__ 
 }
 
 /* flags[t * nlayers + l] = 1 when layer l's box meets tile t */
-/* (tile, layer) entries: a block takes a run of AK_TP_RUN entries, a warp 512
-   of them as 16 rows of 32 (coalesced box loads), each lane stepping its
-   entry's (tile, layer) by 32 a row */
+/* (tile, layer) entries: a block takes AK_TP_TILES consecutive tiles and
+   AK_TP_LAYERS consecutive layers (one run per tile), a warp 512 of the
+   layers as 16 rows of 32 (coalesced box loads); each box is loaded once
+   and tested against the block's tiles */
 #define AK_TP_THREADS 512
-#define AK_TP_ROWS    (AK_TP_RUN / AK_TP_THREADS)
-struct ak_tp_it {
-    uint32_t t, l;
-};
-__device__ __forceinline__ ak_tp_it ak_tp_first(uint64_t i, uint32_t nl) {
-    return ak_tp_it{(uint32_t)(i / nl), (uint32_t)(i % nl)};
-}
-__device__ __forceinline__ void ak_tp_step(ak_tp_it &e, uint32_t nl) {
-    e.l += 32u;
-    while (e.l >= nl)
-        e.l -= nl, e.t++;
-}
+#define AK_TP_TILES   8
+#define AK_TP_ROWS    (AK_TP_LAYERS / AK_TP_THREADS)
 __device__ __forceinline__ bool ak_tp_hit(const int4 &b, uint32_t t, uint32_t ntx, uint32_t tile) {
     const int tx0 = (int)((t % ntx) * tile), ty0 = (int)((t / ntx) * tile);
     return b.x <= tx0 + (int)tile - 1 && b.z >= tx0 && b.y <= ty0 + (int)tile - 1 && b.w >= ty0;
 }
-__global__ void __launch_bounds__(AK_TP_THREADS)
-    ak_tile_count(uint64_t n, uint32_t nl, uint32_t ntx, uint32_t tile, const int4 *__restrict__ box,
-                  uint32_t *__restrict__ bsum, uint32_t *__restrict__ tcount) {
-    __shared__ uint32_t s_w[AK_TP_THREADS / 32];
-    const uint32_t      lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
-    const uint64_t      i0   = (uint64_t)blockIdx.x * AK_TP_RUN + (uint64_t)w * (32u * AK_TP_ROWS) + lane;
-    ak_tp_it            e    = ak_tp_first(i0, nl);
-    uint32_t            cnt  = 0;
+/* hits[tt] bit k: this lane's layer of row k meets tile t0 + tt; the warp's
+   pairs per tile into s_w[warp][tt] */
+__device__ __forceinline__ void ak_tp_sweep(uint32_t nt, uint32_t nl, uint32_t ntx, uint32_t tile,
+                                            const int4 *__restrict__ box, uint32_t t0, uint32_t l0,
+                                            uint32_t (&hits)[AK_TP_TILES], uint32_t (*s_w)[AK_TP_TILES]) {
+    const uint32_t lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
+    uint32_t       cnt[AK_TP_TILES];
+#pragma unroll
+    for (int tt = 0; tt < AK_TP_TILES; tt++)
+        hits[tt] = 0u, cnt[tt] = 0u;
     for (int k = 0; k < AK_TP_ROWS; k++) {
-        const uint64_t i   = i0 + 32u * (uint32_t)k;
-        const bool     hit = i < n && ak_tp_hit(box[e.l], e.t, ntx, tile);
-        if (hit)
-            atomicAdd(&tcount[e.t], 1u);
-        cnt += __popc(__ballot_sync(0xffffffffu, hit));
-        ak_tp_step(e, nl);
+        const uint32_t l  = l0 + w * (32u * AK_TP_ROWS) + 32u * (uint32_t)k + lane;
+        const bool     lv = l < nl;
+        const int4     b  = lv ? box[l] : make_int4(1, 1, 0, 0);
+#pragma unroll
+        for (int tt = 0; tt < AK_TP_TILES; tt++) {
+            const bool hit = lv && t0 + tt < nt && ak_tp_hit(b, t0 + tt, ntx, tile);
+            hits[tt] |= (hit ? 1u : 0u) << k;
+            cnt[tt] += __popc(__ballot_sync(0xffffffffu, hit));
+        }
     }
-    if (lane == 0)
-        s_w[w] = cnt;
+    if (lane == 0) {
+#pragma unroll
+        for (int tt = 0; tt < AK_TP_TILES; tt++)
+            s_w[w][tt] = cnt[tt];
+    }
     __syncthreads();
-    if (threadIdx.x < 32) {
-        uint32_t v = threadIdx.x < AK_TP_THREADS / 32 ? s_w[threadIdx.x] : 0u;
-        v          = __reduce_add_sync(0xffffffffu, v);
-        if (threadIdx.x == 0)
-            bsum[blockIdx.x] = v;
+}
+__global__ void __launch_bounds__(AK_TP_THREADS)
+    ak_tile_count(uint32_t nt, uint32_t nl, uint32_t ntx, uint32_t tile, const int4 *__restrict__ box,
+                  uint32_t *__restrict__ bsum, uint32_t *__restrict__ tcount) {
+    __shared__ uint32_t s_w[AK_TP_THREADS / 32][AK_TP_TILES];
+    const uint32_t      c = blockIdx.x, t0 = blockIdx.y * AK_TP_TILES, nch = gridDim.x;
+    uint32_t            hits[AK_TP_TILES];
+    ak_tp_sweep(nt, nl, ntx, tile, box, t0, c * AK_TP_LAYERS, hits, s_w);
+    if (threadIdx.x < AK_TP_TILES && t0 + threadIdx.x < nt) {
+        uint32_t v = 0;
+        for (int q = 0; q < AK_TP_THREADS / 32; q++)
+            v += s_w[q][threadIdx.x];
+        bsum[(size_t)(t0 + threadIdx.x) * nch + c] = v;
+        if (v)
+            atomicAdd(&tcount[t0 + threadIdx.x], v);
     }
 }
 __global__ void __launch_bounds__(AK_TP_THREADS)
-    ak_tile_lists(uint64_t n, uint32_t nl, uint32_t ntx, uint32_t tile, const int4 *__restrict__ box,
+    ak_tile_lists(uint32_t nt, uint32_t nl, uint32_t ntx, uint32_t tile, const int4 *__restrict__ box,
                   const uint32_t *__restrict__ bpos, uint32_t *__restrict__ list, uint32_t *__restrict__ ptile,
                   uint2 *__restrict__ pbox, uint32_t *__restrict__ psize) {
-    __shared__ uint32_t s_w[AK_TP_THREADS / 32];
+    __shared__ uint32_t s_w[AK_TP_THREADS / 32][AK_TP_TILES];
+    const uint32_t      c = blockIdx.x, t0 = blockIdx.y * AK_TP_TILES, nch = gridDim.x;
     const uint32_t      lane = threadIdx.x & 31u, w = threadIdx.x >> 5, lt = (1u << lane) - 1u;
-    const uint64_t      i0   = (uint64_t)blockIdx.x * AK_TP_RUN + (uint64_t)w * (32u * AK_TP_ROWS) + lane;
-    ak_tp_it            e    = ak_tp_first(i0, nl);
-    uint32_t            hits = 0, cnt = 0; /* bit k: this lane's entry of row k is a pair */
-    for (int k = 0; k < AK_TP_ROWS; k++) {
-        const uint64_t i   = i0 + 32u * (uint32_t)k;
-        const bool     hit = i < n && ak_tp_hit(box[e.l], e.t, ntx, tile);
-        hits |= (hit ? 1u : 0u) << k;
-        cnt += __popc(__ballot_sync(0xffffffffu, hit));
-        ak_tp_step(e, nl);
+    const uint32_t      l0   = c * AK_TP_LAYERS;
+    uint32_t            hits[AK_TP_TILES];
+    ak_tp_sweep(nt, nl, ntx, tile, box, t0, l0, hits, s_w);
+    uint32_t j[AK_TP_TILES]; /* this warp's next pair of each tile */
+#pragma unroll
+    for (int tt = 0; tt < AK_TP_TILES; tt++) {
+        j[tt] = t0 + tt < nt ? bpos[(size_t)(t0 + tt) * nch + c] : 0u;
+        for (uint32_t q = 0; q < w; q++)
+            j[tt] += s_w[q][tt];
     }
-    if (lane == 0)
-        s_w[w] = cnt;
-    __syncthreads();
-    uint32_t j = bpos[blockIdx.x];
-    for (uint32_t q = 0; q < w; q++)
-        j += s_w[q];
-    e = ak_tp_first(i0, nl);
     for (int k = 0; k < AK_TP_ROWS; k++) {
-        const bool     hit = (hits >> k) & 1u;
-        const uint32_t m   = __ballot_sync(0xffffffffu, hit);
-        if (hit) {
-            const uint32_t p   = j + __popc(m & lt);
-            const int      tx0 = (int)((e.t % ntx) * tile), ty0 = (int)((e.t / ntx) * tile);
-            const int4     b   = box[e.l];
-            const int      x0 = max(b.x, tx0) - tx0, x1 = min(b.z, tx0 + (int)tile - 1) - tx0;
-            const int      y0 = max(b.y, ty0) - ty0, y1 = min(b.w, ty0 + (int)tile - 1) - ty0;
-            list[p]  = e.l;
-            ptile[p] = e.t;
-            pbox[p]  = make_uint2((uint32_t)x0 | (uint32_t)y0 << 16,
-                                  (uint32_t)(x1 - x0 + 1) | (uint32_t)(y1 - y0 + 1) << 16);
-            psize[p] = (uint32_t)((x1 - x0 + 1) * (y1 - y0 + 1));
+        const uint32_t l = l0 + w * (32u * AK_TP_ROWS) + 32u * (uint32_t)k + lane;
+        int4           b = make_int4(0, 0, 0, 0);
+        bool           any = false;
+#pragma unroll
+        for (int tt = 0; tt < AK_TP_TILES; tt++)
+            any |= ((hits[tt] >> k) & 1u) != 0u;
+        if (any)
+            b = box[l];
+#pragma unroll
+        for (int tt = 0; tt < AK_TP_TILES; tt++) {
+            const bool     hit = (hits[tt] >> k) & 1u;
+            const uint32_t m   = __ballot_sync(0xffffffffu, hit);
+            if (hit) {
+                const uint32_t t = t0 + tt, p = j[tt] + __popc(m & lt);
+                const int      tx0 = (int)((t % ntx) * tile), ty0 = (int)((t / ntx) * tile);
+                const int      x0 = max(b.x, tx0) - tx0, x1 = min(b.z, tx0 + (int)tile - 1) - tx0;
+                const int      y0 = max(b.y, ty0) - ty0, y1 = min(b.w, ty0 + (int)tile - 1) - ty0;
+                list[p]  = l;
+                ptile[p] = t;
+                pbox[p]  = make_uint2((uint32_t)x0 | (uint32_t)y0 << 16,
+                                      (uint32_t)(x1 - x0 + 1) | (uint32_t)(y1 - y0 + 1) << 16);
+                psize[p] = (uint32_t)((x1 - x0 + 1) * (y1 - y0 + 1));
+            }
+            j[tt] += __popc(m);
         }
-        j += __popc(m);
-        ak_tp_step(e, nl);
     }
 }
 
@@ -1202,19 +1214,21 @@ cudaError_t ak_launch_layer_boxes(cudaStream_t st, const ak_scene &S, const ak_b
         ak_layer_boxes<<<(S.nlayers * 32 + 255) / 256, 256, 0, st>>>(S, B, widths, box, total);
     return cudaGetLastError();
 }
-uint32_t ak_tile_runs(uint64_t n) { return (uint32_t)((n + AK_TP_RUN - 1) / AK_TP_RUN); }
-cudaError_t ak_launch_tile_count(cudaStream_t st, uint64_t n, uint32_t nlayers, uint32_t ntx, uint32_t tile,
+static uint32_t tile_chunks(uint32_t nl) { return (nl + AK_TP_LAYERS - 1) / AK_TP_LAYERS; }
+uint32_t ak_tile_runs(uint32_t ntiles, uint32_t nlayers) { return ntiles * tile_chunks(nlayers); }
+cudaError_t ak_launch_tile_count(cudaStream_t st, uint32_t ntiles, uint32_t nlayers, uint32_t ntx, uint32_t tile,
                                  const int4 *box, uint32_t *bsum, uint32_t *tcount) {
-    if (n)
-        ak_tile_count<<<ak_tile_runs(n), AK_TP_THREADS, 0, st>>>(n, nlayers, ntx, tile, box, bsum, tcount);
+    if (ntiles && nlayers)
+        ak_tile_count<<<dim3(tile_chunks(nlayers), (ntiles + AK_TP_TILES - 1) / AK_TP_TILES), AK_TP_THREADS, 0, st>>>(
+            ntiles, nlayers, ntx, tile, box, bsum, tcount);
     return cudaGetLastError();
 }
-cudaError_t ak_launch_tile_lists(cudaStream_t st, uint64_t n, uint32_t nlayers, uint32_t ntx, uint32_t tile,
+cudaError_t ak_launch_tile_lists(cudaStream_t st, uint32_t ntiles, uint32_t nlayers, uint32_t ntx, uint32_t tile,
                                  const int4 *box, const uint32_t *bpos, uint32_t *list, uint32_t *ptile, uint2 *pbox,
                                  uint32_t *psize) {
-    if (n)
-        ak_tile_lists<<<ak_tile_runs(n), AK_TP_THREADS, 0, st>>>(n, nlayers, ntx, tile, box, bpos, list, ptile, pbox,
-                                                                   psize);
+    if (ntiles && nlayers)
+        ak_tile_lists<<<dim3(tile_chunks(nlayers), (ntiles + AK_TP_TILES - 1) / AK_TP_TILES), AK_TP_THREADS, 0, st>>>(
+            ntiles, nlayers, ntx, tile, box, bpos, list, ptile, pbox, psize);
     return cudaGetLastError();
 }
 cudaError_t ak_launch_adam(cudaStream_t st, float *param, const float *grad, float *m, float *v, uint32_t n, float lr,

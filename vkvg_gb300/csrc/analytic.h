@@ -95,19 +95,20 @@ cudaError_t ak_launch_reduce(cudaStream_t st, const ak_scene &S, uint32_t nblock
    pixel), the boxes' pixel total added to *total */
 cudaError_t ak_launch_layer_boxes(cudaStream_t st, const ak_scene &S, const ak_bufs &B, const float *widths, int4 *box,
                                   unsigned long long *total);
-/* The (tile, layer) pairs, entry i = t * nlayers + l of every tile and layer
-   (a pair when layer l's box meets tile t), in two sweeps that test the
-   boxes as they go: _count sums each run of AK_TP_RUN entries into
-   bsum[run] and counts each tile's pairs into tcount[t] (zeroed by the
-   caller); after an exclusive scan of bsum into bpos, _lists writes pair
-   bpos-rank of every hit: its layer, its tile, the layer's box inside the
-   tile (x0 | y0 << 16, w | h << 16) and its pixel count.  Runs:
-   ak_tile_runs(n). */
-#define AK_TP_RUN 8192
-uint32_t    ak_tile_runs(uint64_t n);
-cudaError_t ak_launch_tile_count(cudaStream_t st, uint64_t n, uint32_t nlayers, uint32_t ntx, uint32_t tile,
+/* The (tile, layer) pairs (layer l's box meets tile t), tile by tile in
+   layer order, in two sweeps that test the boxes as they go: a run is one
+   tile and AK_TP_LAYERS consecutive layers (run r = t * chunks + c,
+   chunks = ceil(nlayers / AK_TP_LAYERS)); _count sums every run's pairs
+   into bsum[r] and every tile's into tcount[t] (zeroed by the caller);
+   after an exclusive scan of bsum into bpos, _lists writes every pair at
+   its run's position plus its rank: its layer, its tile, the layer's box
+   inside the tile (x0 | y0 << 16, w | h << 16) and its pixel count.  Runs:
+   ak_tile_runs(ntiles, nlayers). */
+#define AK_TP_LAYERS 8192
+uint32_t    ak_tile_runs(uint32_t ntiles, uint32_t nlayers);
+cudaError_t ak_launch_tile_count(cudaStream_t st, uint32_t ntiles, uint32_t nlayers, uint32_t ntx, uint32_t tile,
                                  const int4 *box, uint32_t *bsum, uint32_t *tcount);
-cudaError_t ak_launch_tile_lists(cudaStream_t st, uint64_t n, uint32_t nlayers, uint32_t ntx, uint32_t tile,
+cudaError_t ak_launch_tile_lists(cudaStream_t st, uint32_t ntiles, uint32_t nlayers, uint32_t ntx, uint32_t tile,
                                  const int4 *box, const uint32_t *bpos, uint32_t *list, uint32_t *ptile, uint2 *pbox,
                                  uint32_t *psize);
 cudaError_t ak_launch_adam(cudaStream_t st, float *param, const float *grad, float *m, float *v, uint32_t n, float lr,
