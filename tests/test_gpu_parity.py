@@ -585,10 +585,10 @@ def _form_scenes():
     return out
 
 
-@pytest.mark.parametrize("form", [0, 1, 2, 3, 4])
+@pytest.mark.parametrize("form", [0, 1, 2, 3, 4, 5])
 def test_each_raster_form_bit_exact(gb, vko, raster_form, form):
-    """every raster form (the register tiles of 1024, 256 and 128 pixels and
-    the row form in half and whole bands) on solid, gradient (one source image and several), radial,
+    """every raster form (the register tiles of 1024, 256, 128 and 64 pixels
+    and the row form in half and whole bands) on solid, gradient (one source image and several), radial,
     surface-source and glyph scenes, one and four samples, a surface two
     tiles wide: the form asked for is the one that ran, and its samples and
     image equal the oracle's"""

@@ -128,7 +128,7 @@ vkvg_status_t vkvg_gb300_debug_stroke(VkvgContext ctx, uint32_t i, float *xy, ui
     return r;
 }
 
-void vkvg_gb300_debug_set_raster_form(int form) { gb_form_override.store(form >= 0 && form <= 4 ? form : -1); }
+void vkvg_gb300_debug_set_raster_form(int form) { gb_form_override.store(form >= 0 && form <= 5 ? form : -1); }
 int  vkvg_gb300_debug_raster_form(VkvgContext ctx) { return vkvg_status(ctx) ? -1 : ctx->pl.form_run; }
 void vkvg_gb300_debug_inject(int what, uint32_t value) {
     if (what == 0)
@@ -177,7 +177,8 @@ vkvg_status_t vkvg_gb300_debug_coverage(VkvgContext ctx, uint32_t i, int32_t *ou
     memset(&CA, 0, sizeof(CA));
     /* the form the frame itself ran (the register tile after a clipping frame) */
     const cudaError_t e =
-        p.form_run >= 3 ? gb_launch_raster_rows(p.st, &A, 0, p.form_half) : gb_launch_raster(p.st, &A, &CA, 0, 0, 0);
+        p.form_run == 3 || p.form_run == 4 ? gb_launch_raster_rows(p.st, &A, 0, p.form_half)
+                                           : gb_launch_raster(p.st, &A, &CA, 0, 0, 0);
     if (e != cudaSuccess)
         return VKVG_STATUS_DEVICE_ERROR;
     gb_count_launch(1);

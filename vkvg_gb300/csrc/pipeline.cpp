@@ -430,7 +430,7 @@ cudaError_t Pipeline::geometry(const FrameHost &f, const gb_surf *surfs, uint32_
            finish it sooner) and the draws that carry the edges are small next
            to a wide tile, or the surface is no wider than a narrow one */
         const bool small = !wide || (ws[1] && ws[0] <= 384u * ws[1]);
-        narrow           = !(stats && small) ? 0 : mxc <= 128u ? 2 : mxc <= 480u ? 1 : 0;
+        narrow           = !(stats && small) ? 0 : mxc <= 128u ? 5 : mxc <= 480u ? 1 : 0;
         /* candidates for the row form: draws that span most of a tile (mean
            width over 640 pixels, weighted by edges), or a surface whose
            1024-pixel tiles give fewer CTAs than SMs (the row form's half
@@ -497,7 +497,7 @@ cudaError_t Pipeline::run(const FrameHost &f, _vkvg_surface_t *surf, bool timing
     for (const gb_draw &d : f.draws)
         every += d.kind > GB_DRAW_STROKE ? nbands : 0u;
     stats_w = W;
-    CK(geometry(f, surf_tab.as<gb_surf>(), 1u, (uint64_t)nbands * ndraw, every, W > gb_raster_tile_width(3), S, timing,
+    CK(geometry(f, surf_tab.as<gb_surf>(), 1u, (uint64_t)nbands * ndraw, every, W > gb_raster_tile_width(4), S, timing,
                 false));
     stats_w = 0;
 
@@ -623,7 +623,7 @@ cudaError_t Pipeline::run(const FrameHost &f, _vkvg_surface_t *surf, bool timing
     int form     = gb_form_override.load();
     if (clip_use)
         form = 0; /* only the register tile carries the clip planes */
-    else if (form < 0 || form > 4)
+    else if (form < 0 || form > 5)
         form = narrow ? narrow : row_draws && sparse_crossings((uint64_t)nbands * ndraw) ? 3 : 0;
     if (form == 3 && max_cell >= 32768u)
         form = 4; /* 16-bit counters would not hold a cell's crossings: whole bands */
@@ -632,8 +632,8 @@ cudaError_t Pipeline::run(const FrameHost &f, _vkvg_surface_t *surf, bool timing
     /* the tiny form's small draws read cells of fewer than 64 record units
        from L2 instead of staging them (a bulk copy and a barrier wait per
        draw: the glyph scene's raster 11.23 -> 10.87 ms, no change above 64) */
-    A.stage_min = form == 2 ? 64u : 0u;
-    if (form >= 3)
+    A.stage_min = form == 2 || form == 5 ? 64u : 0u;
+    if (form == 3 || form == 4)
         CK(gb_launch_raster_rows(st, &A, ngrad > 0, form_half));
     else
         CK(gb_launch_raster(st, &A, &CA, ngrad > 0, clip_use, form));

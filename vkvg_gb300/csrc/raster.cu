@@ -66,15 +66,15 @@
 template <int NW> struct XT {
     static constexpr int W         = 64 * NW;
     static constexpr int THREADS   = 32 * NW;
-    static constexpr int MINB      = NW >= 16 ? 1 : NW >= 8 ? 2 : NW >= 4 ? 4 : 8; /* CTAs per SM */
+    static constexpr int MINB      = NW >= 16 ? 1 : NW >= 8 ? 2 : NW >= 4 ? 4 : NW >= 2 ? 8 : 16; /* CTAs per SM */
     static constexpr int PLANE     = GB_BAND_ROWS * W; /* one crossing counter per tile sample */
-    static constexpr int TOT_ROW   = (NW + 7) / 4 * 4; /* strip totals per row, padded (int4 rows, bank spread) */
+    static constexpr int TOT_ROW   = NW == 1 ? 4 : (NW + 7) / 4 * 4; /* strip totals per row, padded (int4 rows, bank spread) */
     static constexpr int TOT_SET   = GB_BAND_ROWS * TOT_ROW;
     static constexpr int S_TOT     = 2 * PLANE;
     static constexpr int S_FLAG    = S_TOT + 3 * TOT_SET;
     static constexpr int S_WORDS   = S_FLAG + 2 * NW;
-    static constexpr int STAGE_CAP = NW >= 8 ? 128 * NW : NW >= 4 ? 480 : 128; /* units per staging buffer */
-    static constexpr int S_STAGE   = S_WORDS;
+    static constexpr int STAGE_CAP = NW >= 8 ? 128 * NW : NW >= 4 ? 480 : NW >= 2 ? 128 : 64; /* units per staging buffer */
+    static constexpr int S_STAGE   = (S_WORDS + 3) / 4 * 4;
     static constexpr int S_CUR     = S_STAGE + 2 * STAGE_CAP * 4;
     static constexpr int S_MBAR    = S_CUR + NW * 192;
     static constexpr int S_RG      = S_MBAR + 4;
@@ -90,6 +90,7 @@ template <int NW> struct XT {
 #define XT_MID    8
 #define XT_NARROW 4
 #define XT_TINY   2
+#define XT_MICRO  1
 
 /* counter (or staged sample) of tile sample p in band row rr: each lane run
    of 32 samples is eight 16-byte slots, rotated by the row and the run's
@@ -1058,7 +1059,11 @@ template <int NW, bool GRAD, bool CLIP> cudaError_t raster_nw(cudaStream_t st, c
 }
 
 extern "C" uint32_t gb_raster_tile_width(int form) {
-    return form == 1 ? XT<XT_NARROW>::W : form == 2 ? XT<XT_MID>::W : form == 3 ? XT<XT_TINY>::W : XT<XT_WIDE>::W;
+    return form == 1   ? XT<XT_NARROW>::W
+           : form == 2 ? XT<XT_MID>::W
+           : form == 3 ? XT<XT_TINY>::W
+           : form == 4 ? XT<XT_MICRO>::W
+                       : XT<XT_WIDE>::W;
 }
 extern "C" cudaError_t gb_launch_raster_batch(cudaStream_t st, const gb_raster_args *a, const gb_surf *surfs,
                                              const uint4 *items, uint32_t nitems, uint32_t *queue, uint32_t nctas,
@@ -1076,6 +1081,8 @@ extern "C" cudaError_t gb_launch_raster(cudaStream_t st, const gb_raster_args *a
         return cudaSuccess;
     if (clipping)
         return gradients ? raster_nw<XT_WIDE, true, true>(st, a, c) : raster_nw<XT_WIDE, false, true>(st, a, c);
+    if (narrow == 5)
+        return gradients ? raster_nw<XT_MICRO, true, false>(st, a, c) : raster_nw<XT_MICRO, false, false>(st, a, c);
     if (narrow == 2)
         return gradients ? raster_nw<XT_TINY, true, false>(st, a, c) : raster_nw<XT_TINY, false, false>(st, a, c);
     if (narrow)
