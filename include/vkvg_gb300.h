@@ -120,8 +120,9 @@ vkvg_public vkvg_status_t vkvg_gb300_debug_coverage(VkvgContext ctx, uint32_t i,
    default), 0 the register tile of 1024 pixels, 1 of 256 pixels, 2 of 128
    pixels, 3 the row form in half bands (16-bit counters; frames whose
    heaviest cell holds 2^15 records or more run 4 instead), 4 the row form in
-   whole bands.  Frames with clipping always run the first.  And the form the
-   context's last flush ran (-1 before any). */
+   whole bands, 5 the register tile of 64 pixels.  Frames with clipping
+   always run the first.  And the form the context's last flush ran (-1
+   before any). */
 vkvg_public void vkvg_gb300_debug_set_raster_form(int form);
 vkvg_public int  vkvg_gb300_debug_raster_form(VkvgContext ctx);
 /* Failure injection for the tests, process-wide (no vkvg counterpart; vkvg's

@@ -106,7 +106,7 @@ struct Pipeline {
     uint32_t npts = 0, nev = 0, nverts = 0, ninds = 0, nedges = 0, ntris = 0, nunits = 0, nbands = 0;
     uint32_t dev_status = 0;
     uint32_t stats_w    = 0;     /* surface width of a one-surface frame: geometry measures its draws' widths */
-    int      narrow     = 0; /* the register-tile form geometry picked: 0 1024-pixel, 1 256-pixel, 2 128-pixel tiles */
+    int      narrow     = 0; /* the register-tile form geometry picked: 0 1024-pixel, 1 256-pixel, 5 64-pixel tiles */
     int      form_run   = -1; /* the raster form the last frame ran (as vkvg_gb300_debug_set_raster_form) */
     int      form_half  = 0;  /* the row form ran in half bands with 16-bit counters */
     bool     row_draws  = false; /* the row form's candidates: draws spanning most of a 1024-pixel tile, or few tiles */

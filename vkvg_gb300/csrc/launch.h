@@ -139,11 +139,12 @@ cudaError_t gb_launch_cells_lists(cudaStream_t st, uint64_t ncells, const uint32
                                   uint32_t *off, uint32_t *alist, uint32_t *apos, const gb_surf *surfs, uint32_t nsurf);
 
 /* narrow: 1 the 256-pixel raster form (4 warps, 4 CTAs per SM), 2 the
-   128-pixel one (2 warps, 8 CTAs per SM), 0 the 1024-pixel one (16 warps,
-   one CTA per SM); clipping frames run the last */
+   128-pixel one (2 warps, 8 CTAs per SM), 5 the 64-pixel one (one warp, 16
+   CTAs per SM), 0 the 1024-pixel one (16 warps, one CTA per SM); clipping
+   frames run the last */
 cudaError_t gb_launch_raster(cudaStream_t st, const gb_raster_args *a, const gb_clip_args *c, int gradients,
                              int clipping, int narrow);
-/* pixels per raster tile of a form: 0 wide (1024), 1 narrow (256), 2 middle (512), 3 tiny (128) */
+/* pixels per raster tile of a form: 0 wide (1024), 1 narrow (256), 2 middle (512), 3 tiny (128), 4 micro (64) */
 uint32_t gb_raster_tile_width(int form);
 /* out[i] = src[idx[i]] */
 cudaError_t gb_launch_gather_u32(cudaStream_t st, uint32_t n, const uint64_t *idx, const uint32_t *src,
