@@ -648,7 +648,7 @@ def glyph_bench(a, gb, L, np, flush):
     tgt = gb.Surface(dev, size, size)
     bt = L.vkvg_gb300_batch_create((C.c_void_p * 1)(frame), (C.c_void_p * 1)(tgt.h), 1)
     if bt:
-        for _ in range(14):
+        for _ in range(16):  # sizing, fourteen tuning runs, graph capture
             flush()
             assert L.vkvg_gb300_batch_execute(bt) == 0
         bms = []
@@ -875,7 +875,7 @@ def main():
         ta = (C.c_void_p * len(btarget))(*[s2.h for s2 in btarget])
         bt = L.vkvg_gb300_batch_create(fa, ta, len(bframes))
         assert bt
-        for _ in range(14):  # sizing, twelve tuning runs, graph capture
+        for _ in range(16):  # sizing, fourteen tuning runs, graph capture
             assert L.vkvg_gb300_batch_execute(bt) == 0
         torch.cuda.synchronize()
         t0 = time.perf_counter()

@@ -25,12 +25,13 @@ namespace {
 struct RasterParams {
     uint32_t stage_min;  /* cells of fewer record units skip the shared-memory stage */
     bool     cost_order; /* work list heaviest first (else surface, band, tile order) */
-    int      form;       /* tiles: 0 1024 pixels (one CTA per SM), 1 256 (four), 2 512 (two), 3 128 (eight) */
+    int      form;       /* tiles: 0 1024 pixels (one CTA per SM), 1 256 (four), 2 512 (two), 3 128 (eight),
+                            4 64 (sixteen) */
 };
-const RasterParams CANDIDATES[] = {{0, true, 0}, {8, true, 0}, {32, true, 0}, {0, false, 0}, {0, true, 2},
-                                   {8, true, 2}, {32, true, 2}, {0, true, 1}, {8, true, 1}, {32, true, 1},
-                                   {0, true, 3}, {32, true, 3}};
-constexpr int NFORMS = 4;
+const RasterParams CANDIDATES[] = {{0, true, 0},  {8, true, 0}, {32, true, 0}, {0, false, 0}, {0, true, 2},
+                                   {8, true, 2},  {32, true, 2}, {0, true, 1}, {8, true, 1},  {32, true, 1},
+                                   {0, true, 3},  {32, true, 3}, {64, true, 3}, {64, true, 4}};
+constexpr int NFORMS = 5;
 constexpr int      NCAND        = sizeof(CANDIDATES) / sizeof(CANDIDATES[0]);
 
 /* the tuner's choice per class of scene: surfaces, draws and record units,
@@ -229,7 +230,7 @@ cudaError_t run_batch(VkvgBatch b, bool sized, const RasterParams &p) {
     Pipeline &pl = b->pl;
     bool wide = false; /* the draws' x extents, for every tile width a candidate uses (down to 128 pixels) */
     for (const gb_surf &s : b->tab)
-        wide |= s.W > gb_raster_tile_width(3);
+        wide |= s.W > gb_raster_tile_width(4);
     BCK(pl.geometry(b->merged, b->d_tab.as<gb_surf>(), (uint32_t)b->tab.size(), b->ncells, b->every, wide,
                     b->samples, false, sized));
     if (!sized)

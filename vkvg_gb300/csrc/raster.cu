@@ -1041,6 +1041,8 @@ static cudaError_t raster_batch_form(cudaStream_t st, const gb_raster_args *a, c
         return raster_batch_nw<XT_MID, GRAD>(st, a, surfs, items, nitems, queue, nctas);
     if (form == 3)
         return raster_batch_nw<XT_TINY, GRAD>(st, a, surfs, items, nitems, queue, nctas);
+    if (form == 4)
+        return raster_batch_nw<XT_MICRO, GRAD>(st, a, surfs, items, nitems, queue, nctas);
     return raster_batch_nw<XT_WIDE, GRAD>(st, a, surfs, items, nitems, queue, nctas);
 }
 template <int NW, bool GRAD, bool CLIP> cudaError_t raster_nw(cudaStream_t st, const gb_raster_args *a,
