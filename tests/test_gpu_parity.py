@@ -616,3 +616,40 @@ def test_coverage_each_form_bit_exact(gb, vko, raster_form, form):
         g = ctx.debug_coverage(i)
         o = octx.coverage(j, sc["width"], sc["height"], sc["samples"], mode=0)
         assert np.array_equal(g, o), "draw %d: %d samples differ" % (i, int((g != o).sum()))
+
+
+def test_contexts_on_several_threads(gb):
+    """contexts on four host threads at once, one thread-aware device (each
+    context flushes on its own stream, each surface has its own lock): every
+    surface equals the same scene rendered alone, over three flushes each"""
+    import threading
+
+    scs = [scenes.api_mix(n_items=24, size=160, seed=40 + k) for k in range(4)]
+    alone = [pu.run_gpu(gb, sc, debug=False)[1].image().copy() for sc in scs]
+    dev = gb.Device(samples=4, thread_aware=True)
+    out, errs = [[] for _ in scs], []
+
+    def work(k):
+        try:
+            sc = scs[k]
+            for _ in range(3):
+                surf = gb.Surface(dev, sc["width"], sc["height"])
+                ctx = surf.context()
+                scenes.play(ctx, sc["ops"])
+                ctx.flush()
+                assert ctx.status() == 0
+                out[k].append(surf.image().copy())
+                ctx.destroy()
+        except Exception as e:  # reported on the main thread
+            errs.append((k, e))
+
+    threads = [threading.Thread(target=work, args=(k,)) for k in range(len(scs))]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert not errs, errs
+    for k in range(len(scs)):
+        assert len(out[k]) == 3
+        for img in out[k]:
+            assert np.array_equal(img, alone[k]), k

@@ -53,6 +53,8 @@
 
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 /* Tile geometry of a raster CTA of NW warps: NW strips of 64 pixels, 16
    sample rows.  Shared memory: 2 counter planes, 3 strip-total sets, 2 flag
    sets; then 2 staging buffers for a cell's records (16-byte units), the
@@ -1020,13 +1022,13 @@ extern "C" cudaError_t gb_launch_unpremultiply(cudaStream_t st, const uint32_t *
 template <int NW, bool GRAD>
 cudaError_t raster_batch_nw(cudaStream_t st, const gb_raster_args *a, const gb_surf *surfs, const uint4 *items,
                             uint32_t nitems, uint32_t *queue, uint32_t nctas) {
-    static bool configured = false;
-    if (!configured) {
+    static std::atomic<bool> configured{false}; /* set once; a second setter is harmless */
+    if (!configured.load(std::memory_order_acquire)) {
         cudaError_t e = cudaFuncSetAttribute(gb_raster_batch<NW, GRAD>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              XT<NW>::SMEM);
         if (e != cudaSuccess)
             return e;
-        configured = true;
+        configured.store(true, std::memory_order_release);
     }
     gb_raster_batch<NW, GRAD>
         <<<nctas * XT<NW>::MINB, XT<NW>::THREADS, XT<NW>::SMEM, st>>>(*a, surfs, items, nitems, queue);
@@ -1047,13 +1049,13 @@ static cudaError_t raster_batch_form(cudaStream_t st, const gb_raster_args *a, c
 }
 template <int NW, bool GRAD, bool CLIP> cudaError_t raster_nw(cudaStream_t st, const gb_raster_args *a,
                                                               const gb_clip_args *c) {
-    static bool configured = false;
-    if (!configured) {
+    static std::atomic<bool> configured{false}; /* set once; a second setter is harmless */
+    if (!configured.load(std::memory_order_acquire)) {
         cudaError_t e = cudaFuncSetAttribute(gb_raster<NW, GRAD, CLIP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              XT<NW>::SMEM);
         if (e != cudaSuccess)
             return e;
-        configured = true;
+        configured.store(true, std::memory_order_release);
     }
     dim3 grid((a->W + XT<NW>::W - 1) / XT<NW>::W, a->nbands);
     gb_raster<NW, GRAD, CLIP><<<grid, XT<NW>::THREADS, XT<NW>::SMEM, st>>>(*a, *c);

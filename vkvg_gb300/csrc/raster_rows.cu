@@ -48,6 +48,8 @@
 
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 namespace rw {
 constexpr int TW  = 1024; /* tile width in pixels (samples per row) */
 constexpr int HDR = 16;   /* header words per slot */
@@ -689,13 +691,13 @@ __global__ void __launch_bounds__(RW16::THREADS, 1)
 extern "C" uint32_t gb_raster_rows_tile_width() { return rw::TW; }
 
 template <class T, bool GRAD, bool DBG> static cudaError_t rows_launch(cudaStream_t st, const gb_raster_args *a) {
-    static bool configured = false;
-    if (!configured) {
+    static std::atomic<bool> configured{false}; /* set once; a second setter is harmless */
+    if (!configured.load(std::memory_order_acquire)) {
         const cudaError_t e =
             cudaFuncSetAttribute(gb_raster_rows<T, GRAD, DBG>, cudaFuncAttributeMaxDynamicSharedMemorySize, T::SMEM);
         if (e != cudaSuccess)
             return e;
-        configured = true;
+        configured.store(true, std::memory_order_release);
     }
     const dim3 grid((a->W + rw::TW - 1) / rw::TW, a->nbands * (GB_BAND_ROWS / T::ROWS));
     gb_raster_rows<T, GRAD, DBG><<<grid, T::THREADS, T::SMEM, st>>>(*a);
@@ -715,15 +717,15 @@ extern "C" cudaError_t gb_launch_raster_rows(cudaStream_t st, const gb_raster_ar
 extern "C" cudaError_t gb_launch_raster_rows_batch(cudaStream_t st, const gb_raster_args *a, const gb_surf *surfs,
                                                   const uint4 *items, uint32_t nitems, uint32_t *queue,
                                                   uint32_t nctas) {
-    static bool configured = false;
+    static std::atomic<bool> configured{false}; /* set once; a second setter is harmless */
     if (!nitems)
         return cudaSuccess;
-    if (!configured) {
+    if (!configured.load(std::memory_order_acquire)) {
         cudaError_t e =
             cudaFuncSetAttribute(gb_raster_rows_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, RW16::SMEM);
         if (e != cudaSuccess)
             return e;
-        configured = true;
+        configured.store(true, std::memory_order_release);
     }
     gb_raster_rows_batch<<<nctas, RW16::THREADS, RW16::SMEM, st>>>(*a, surfs, items, nitems, queue);
     return cudaGetLastError();
