@@ -263,6 +263,20 @@ def test_vkvg_clip_cases_bit_exact(gb, vko, name):
     assert np.array_equal(surf.image(), osurf.image())
 
 
+@pytest.mark.parametrize("name", [s["name"] for s in scenes.vkvg_demo_cases()])
+def test_vkvg_demo_cases_bit_exact(gb, vko, name):
+    """vkvg's single-sequence demo programs (tests/line_caps.c, stroke.c,
+    fill.c, fill_non_zero.c, dashes.c) at the harness's 512x512: geometry,
+    samples and image equal the oracle's"""
+    sc = [s for s in scenes.vkvg_demo_cases() if s["name"] == name][0]
+    dev, surf, ctx = pu.run_gpu(gb, sc)
+    osurf, octx = pu.run_oracle(vko, sc, threads=8)
+    assert ctx.debug_counts()[5] == 0 and ctx.status() == 0
+    assert not pu.compare_geometry(ctx, octx)
+    assert np.array_equal(surf.samples_rgba(), osurf.samples_rgba())
+    assert np.array_equal(surf.image(), osurf.image())
+
+
 @pytest.mark.parametrize("samples,flush_every", [(1, 0), (4, 2), (1, 3)])
 def test_clip_mix_variants_bit_exact(gb, vko, samples, flush_every):
     """the clip scene at one sample, and flushed every few items so the clip

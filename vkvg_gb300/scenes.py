@@ -311,6 +311,70 @@ def vkvg_clip_cases(width=1024, height=800, samples=4):
             for n, ops in out]
 
 
+def vkvg_demo_cases(width=512, height=512, samples=4):
+    """The call sequences of vkvg's single-sequence demo programs at their
+    harness's default 512x512 surface (tests/common/test.c:38-39; the
+    harness context of _initCtx, test.c:686-696: width 2, miter joins, butt
+    caps, no dash, non-zero fill, cleared): tests/line_caps.c (the three
+    caps on wide strokes, one stroke through several relative moves),
+    tests/stroke.c (closed and open polylines, a wide line, a half-turn arc,
+    a translucent wide diagonal, a rectangle), tests/fill.c (one concave
+    polygon in the harness context), tests/fill_non_zero.c (a square with a
+    square hole wound the other way, left empty under non-zero) and tests/dashes.c
+    (its first run: offset 0.2, four- and two-entry patterns with round caps
+    and joins, a zero-length dash), one scene each on a fresh surface."""
+    rgba = lambda r, g, b, a: ("set_source_rgba", float(r), float(g), float(b), float(a))
+    harness = [("set_line_width", 2.0), ("set_line_join", 0), ("set_line_cap", 0), ("set_dash", [], 0.0),
+               ("set_fill_rule", 1), ("clear",)]
+    out = []
+    x, y, dx, dy = 20.0, 20.0, 40.0, 60.0
+    caps = [rgba(0.9, 0.9, 0.9, 1), ("paint",), ("set_line_width", 30.0), rgba(0, 0, 0, 1),
+            ("move_to", x, y), ("rel_line_to", 0.0, dy), ("stroke",), ("set_line_cap", 2),
+            ("move_to", x + dx, y), ("rel_line_to", 0.0, dy), ("stroke",), ("set_line_cap", 1),
+            ("move_to", x + 2 * dx, y), ("rel_line_to", 0.0, dy), ("rel_move_to", dx, -dy), ("rel_line_to", dx, dy),
+            ("rel_move_to", dx, -dy / 2.0), ("rel_line_to", dx, 0.0), ("rel_move_to", dx, dy / 2.0),
+            ("rel_line_to", dx, -dy), ("rel_move_to", dx, dy), ("rel_line_to", 0.0, -dy),
+            ("rel_move_to", dx * 2.0, dy), ("rel_line_to", -dx, -dy), ("rel_move_to", dx * 3.0, dy / 2.0),
+            ("rel_line_to", -dx, 0.0), ("stroke",), ("set_line_cap", 0), ("set_line_width", 1.0), rgba(1, 0, 0, 1),
+            ("move_to", x, y), ("rel_line_to", 0.0, dy), ("rel_move_to", dx, -dy), ("rel_line_to", 0.0, dy),
+            ("rel_move_to", dx, -dy), ("rel_line_to", 0.0, dy), ("stroke",)]
+    out.append(("line_caps", caps))
+    pif = 3.14159265358979323846
+    stroke = [("set_line_width", 1.0), rgba(1, 0, 0, 1), ("move_to", 200.5, 200.5), ("line_to", 400.5, 200.5),
+              ("line_to", 400.5, 400.5), ("line_to", 200.5, 400.5), ("close_path",), ("stroke",),
+              rgba(0, 1, 0, 1), ("move_to", 300.5, 300.5), ("line_to", 500.5, 300.5), ("line_to", 500.5, 500.5),
+              ("line_to", 300.5, 500.5), ("stroke",), rgba(0.5, 1, 0, 1), ("move_to", 320.5, 320.5),
+              ("line_to", 520.5, 320.5), ("line_to", 520.5, 520.5), ("line_to", 320.5, 520.5), ("stroke",),
+              ("set_line_width", 40.0), rgba(0.5, 0.6, 1, 1), ("move_to", 700.0, 475.0), ("line_to", 400.0, 475.0),
+              ("stroke",), rgba(0, 0.5, 0.5, 0.5), ("move_to", 300.0, 200.0), ("arc", 200.0, 200.0, 100.0, 0.0, pif),
+              ("stroke",), ("set_line_width", 20.0), rgba(0.1, 0.1, 0.1, 0.5), ("move_to", 100.0, 60.0),
+              ("line_to", 400.0, 600.0), ("stroke",), rgba(1, 1, 1, 1), ("set_line_width", 1.0),
+              ("rectangle", 600.5, 200.5, 100.0, 60.0), ("stroke",)]
+    out.append(("stroke", stroke))
+    fill = harness + [rgba(0.1, 0.9, 0.1, 1), ("move_to", 100.0, 100.0), ("rel_line_to", 50.0, 200.0),
+                      ("rel_line_to", 150.0, -100.0), ("rel_line_to", 100.0, 200.0), ("rel_line_to", -100.0, 100.0),
+                      ("rel_line_to", -10.0, -100.0), ("rel_line_to", -190.0, -50.0), ("close_path",), ("fill",)]
+    out.append(("fill", fill))
+    nz = [("save",), ("set_line_width", 30.0), ("set_fill_rule", 1), rgba(0.1, 0.9, 0.1, 1),
+          ("move_to", 100.0, 100.0), ("rel_line_to", 200.0, 0.0), ("rel_line_to", 0.0, 150.0),
+          ("rel_line_to", -200.0, 0.0), ("close_path",), ("move_to", 150.0, 150.0), ("rel_line_to", 0.0, 50.0),
+          ("rel_line_to", 100.0, 0.0), ("rel_line_to", 0.0, -50.0), ("close_path",), ("fill",)]
+    out.append(("fill_non_zero", nz))
+    off = 0.2
+    path_a = [("move_to", 50.0, 50.0), ("rel_line_to", 500.0, 0.0), ("rel_line_to", 0.0, 200.0),
+              ("rel_line_to", 200.0, 0.0), ("rel_line_to", 0.0, 500.0), ("rel_line_to", -700.0, 0.0), ("close_path",)]
+    path_b = [("move_to", 100.0, 100.0), ("rel_line_to", 400.0, 0.0), ("rel_line_to", 0.0, 200.0),
+              ("rel_line_to", 200.0, 0.0), ("rel_line_to", 0.0, 400.0), ("rel_line_to", -600.0, 0.0), ("close_path",)]
+    dashes = ([("clear",), ("set_source_rgb", 1.0, 1.0, 1.0), ("paint",), ("set_line_cap", 1), ("set_line_join", 1),
+               ("set_dash", [100.0, 20.0, 20.0, 20.0], off), ("set_line_width", 4.0), ("set_source_rgb", 0.0, 0.0, 1.0)]
+              + path_a + [("stroke",), ("set_dash", [0.0, 20.0], off), ("set_source_rgb", 0.0, 1.0, 0.0)] + path_b
+              + [("stroke",), ("set_line_width", 10.0), ("set_source_rgb", 1.0, 0.0, 0.0),
+                 ("set_dash", [80.0, 20.0], off), ("rectangle", 200.0, 300.0, 200.0, 200.0), ("stroke",)])
+    out.append(("dashes", dashes))
+    return [{"name": n, "width": width, "height": height, "samples": samples, "ops": ops, "paths": 0}
+            for n, ops in out]
+
+
 def surface_mix(n_items=12, size=128, seed=23, samples=4):
     """Surface sources: two small drawn surfaces (one of odd size) used as
     sources with vkvg_set_source_surface offsets and as surface patterns with
