@@ -320,9 +320,15 @@ def vkvg_demo_cases(width=512, height=512, samples=4):
     tests/stroke.c (closed and open polylines, a wide line, a half-turn arc,
     a translucent wide diagonal, a rectangle), tests/fill.c (one concave
     polygon in the harness context), tests/fill_non_zero.c (a square with a
-    square hole wound the other way, left empty under non-zero) and tests/dashes.c
-    (its first run: offset 0.2, four- and two-entry patterns with round caps
-    and joins, a zero-length dash), one scene each on a fresh surface."""
+    square hole wound the other way, left empty under non-zero),
+    tests/dashes.c (its first run: offset 0.2, four- and two-entry patterns
+    with round caps and joins, a zero-length dash), tests/line_join.c (its
+    three functions: wide round joins on closed polylines, zigzags with
+    round then bevel joins under translations), tests/circles.c and
+    tests/arcs.c (full and partial arcs of growing radii, arc_negative,
+    scaled arcs, fill and stroke), one scene each on a fresh surface."""
+    import numpy as np
+
     rgba = lambda r, g, b, a: ("set_source_rgba", float(r), float(g), float(b), float(a))
     harness = [("set_line_width", 2.0), ("set_line_join", 0), ("set_line_cap", 0), ("set_dash", [], 0.0),
                ("set_fill_rule", 1), ("clear",)]
@@ -371,6 +377,64 @@ def vkvg_demo_cases(width=512, height=512, samples=4):
               + [("stroke",), ("set_line_width", 10.0), ("set_source_rgb", 1.0, 0.0, 0.0),
                  ("set_dash", [80.0, 20.0], off), ("rectangle", 200.0, 300.0, 200.0, 200.0), ("stroke",)])
     out.append(("dashes", dashes))
+    # tests/line_join.c: test, test2, test3
+    x, y = 250.0, 150.0
+    lj = [("set_line_width", 100.0), rgba(0, 1, 0, 1), ("set_line_join", 1), ("move_to", x, y),
+          ("rel_line_to", -50.0, 30.0), ("rel_line_to", 0.0, 60.0), ("rel_line_to", 50.0, 30.0), ("close_path",),
+          ("stroke",), rgba(0, 0, 1, 1), ("move_to", x + 250, y)]
+    lj += [("rel_line_to", float(a), float(b)) for a, b in ((50, -30), (50, 0), (50, 30), (0, 60), (-50, 70),
+                                                             (-50, 0), (-50, -70))]
+    out.append(("line_join", lj + [("close_path",), ("stroke",)]))
+    for name, starts, steps, shift in (
+            ("line_join2", ((100, 100), (200, 600), (400, 100), (500, 600)),
+             (((70, 50), (-70, 50)), ((70, -50), (-70, -50)), ((-70, 50), (70, 50)), ((-70, -50), (70, -50))), 5),
+            ("line_join3", ((100, 100), (500, 200), (100, 400), (500, 500)),
+             (((50, 70), (50, -70)), ((-50, 70), (-50, -70)), ((50, -70), (50, 70)), ((-50, -70), (-50, 70))), 4)):
+        ops = [("set_fill_rule", 0), ("set_line_width", 30.0), ("set_line_join", 1), ("translate", -50.0, -50.0),
+               ("set_source_rgb", 0.5, 0.0, 0.0)]
+        for _ in range(2):
+            for (sx, sy), (a, b) in zip(starts, steps):
+                ops.append(("move_to", float(sx), float(sy)))
+                for _ in range(shift):
+                    ops += [("rel_line_to", float(a[0]), float(a[1])), ("rel_line_to", float(b[0]), float(b[1]))]
+                ops.append(("stroke",))
+            ops += [("set_line_join", 2), ("translate", 500.0 if name == "line_join2" else 450.0, 0.0)]
+        out.append((name, ops))
+
+    # tests/circles.c and tests/arcs.c (float32 pi as M_PIF; the circles' x
+    # steps are exact in float32)
+    def growing(yc, count, sweep):
+        ops, xc = [], 2.0
+        for i in range(1, count):
+            xc += 0.5 * i
+            ops.append(("arc", xc + 2, float(yc), 0.5 * i, 0.0, sweep))
+            xc += 0.5 * i + 5
+        return ops
+    pif = float(np.float32(np.pi))
+    white, black = ("set_source_rgb", 1.0, 1.0, 1.0), ("set_source_rgb", 0.0, 0.0, 0.0)
+    out.append(("circles_fill_and_stroke", [("clear",), rgba(0, 0.1, 0.8, 0.5), ("set_line_width", 10.0),
+                                            ("arc", 300.0, 300.0, 150.0, 0.0, pif * 2), ("fill_preserve",),
+                                            ("stroke",)]))
+    out.append(("circles_sizes", [("clear",), white] + growing(100, 40, pif * 2) + [("fill",)] +
+                growing(200, 40, pif * 2) + [("stroke",), rgba(0, 0, 1, 0.4)] + growing(300, 40, pif * 2) +
+                [("fill_preserve",), ("set_line_width", 5.0), ("stroke",)]))
+    out.append(("circles_scaled_up", [("clear",), white, ("scale", 100.0, 100.0), ("arc", 2.0, 2.0, 0.5, 0.0, pif * 2),
+                                      ("stroke",)]))
+    out.append(("arcs_sizes", [white, ("paint",), black] + growing(100, 40, float(np.float32(pif * 1.5))) +
+                [("stroke",)]))
+    out.append(("arcs_scaled_up", [white, ("paint",), black, ("scale", 10.0, 10.0),
+                                   ("arc", 20.0, 20.0, 2.0, 0.0, pif / 2), ("stroke",)]))
+    arcs = [white, ("paint",), black, ("set_source_rgb", 1.0, 0.0, 1.0), ("set_line_width", 5.0),
+            ("arc", 100.0, 100.0, 20.0, 0.0, pif / 2), ("stroke",), ("set_source_rgb", 0.0, 1.0, 1.0),
+            ("arc_negative", 100.0, 100.0, 20.0, 0.0, pif / 2), ("stroke",), ("set_source_rgb", 1.0, 0.0, 1.0),
+            ("arc", 100.0, 200.0, 20.0, pif / 2, 0.0), ("stroke",), ("set_source_rgb", 0.0, 1.0, 1.0),
+            ("arc_negative", 100.0, 200.0, 20.0, pif / 2, 0.0), ("stroke",), ("set_source_rgb", 0.0, 0.0, 1.0),
+            ("set_line_width", 10.0), ("arc", 350.0, 100.0, 40.0, 0.0, pif * 2), ("stroke",),
+            ("set_source_rgb", 0.0, 1.0, 0.0), ("set_line_width", 1.0), ("arc", 150.0, 100.0, 3.5, 0.0, pif * 2),
+            ("stroke",), ("arc", 200.0, 200.0, 10.0, 0.0, pif * 2), ("fill",), ("set_source_rgb", 1.0, 0.0, 0.0),
+            ("scale", 3.0, 3.0), ("arc", 150.0, 100.0, 3.5, 0.0, pif * 2), ("stroke",),
+            ("arc", 200.0, 200.0, 10.0, 0.0, pif * 2), ("fill",)]
+    out.append(("arcs", arcs))
     return [{"name": n, "width": width, "height": height, "samples": samples, "ops": ops, "paths": 0}
             for n, ops in out]
 
