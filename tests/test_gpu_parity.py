@@ -266,8 +266,9 @@ def test_vkvg_clip_cases_bit_exact(gb, vko, name):
 @pytest.mark.parametrize("name", [s["name"] for s in scenes.vkvg_demo_cases()])
 def test_vkvg_demo_cases_bit_exact(gb, vko, name):
     """vkvg's single-sequence demo programs (tests/line_caps.c, stroke.c,
-    fill.c, fill_non_zero.c, dashes.c, line_join.c, circles.c, arcs.c) at the
-    harness's 512x512: geometry, samples and image equal the oracle's"""
+    fill.c, fill_non_zero.c, dashes.c, line_join.c, circles.c, arcs.c,
+    curve.c) at the harness's 512x512: geometry, samples and image equal the
+    oracle's"""
     sc = [s for s in scenes.vkvg_demo_cases() if s["name"] == name][0]
     dev, surf, ctx = pu.run_gpu(gb, sc)
     osurf, octx = pu.run_oracle(vko, sc, threads=8)

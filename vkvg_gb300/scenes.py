@@ -326,7 +326,9 @@ def vkvg_demo_cases(width=512, height=512, samples=4):
     three functions: wide round joins on closed polylines, zigzags with
     round then bevel joins under translations), tests/circles.c and
     tests/arcs.c (full and partial arcs of growing radii, arc_negative,
-    scaled arcs, fill and stroke), one scene each on a fresh surface."""
+    scaled arcs, fill and stroke) and tests/curve.c (its four fixed
+    sequences: curves, a rounded rectangle of arcs, self-crossing wide
+    strokes), one scene each on a fresh surface."""
     import numpy as np
 
     rgba = lambda r, g, b, a: ("set_source_rgba", float(r), float(g), float(b), float(a))
@@ -435,6 +437,33 @@ def vkvg_demo_cases(width=512, height=512, samples=4):
             ("scale", 3.0, 3.0), ("arc", 150.0, 100.0, 3.5, 0.0, pif * 2), ("stroke",),
             ("arc", 200.0, 200.0, 10.0, 0.0, pif * 2), ("fill",)]
     out.append(("arcs", arcs))
+    # tests/curve.c: test3, test, curved_rect, test2 (the random ones need the
+    # harness's generator and are left out)
+    out.append(("curve_test3", [("clear",), ("set_line_width", 20.0), ("set_source_rgb", 1.0, 0.0, 0.0),
+                                ("move_to", 80.0, 170.0), ("curve_to", 100.0, 170.0, 160.0, 171.0, 180.0, 170.0),
+                                ("close_path",), ("stroke",)]))
+    out.append(("curve_test", [("set_line_width", 20.0), ("scale", 2.0, 2.0), ("set_line_join", 2),
+                               ("set_source_rgb", 0.5, 0.0, 0.0), ("translate", 200.0, 30.0),
+                               ("arc", 200.0, 200.0, 20.0, 0.0, pif * 2), rgba(0.5, 0.0, 1.0, 0.5),
+                               ("move_to", 100.0, 100.0), ("line_to", 200.0, 100.0),
+                               ("curve_to", 250.0, 100.0, 300.0, 150.0, 300.0, 200.0), ("line_to", 300.0, 300.0),
+                               ("curve_to", 300.0, 350.0, 250.0, 400.0, 200.0, 400.0), ("line_to", 100.0, 400.0),
+                               ("curve_to", 50.0, 400.0, 10.0, 350.0, 10.0, 300.0), ("line_to", 10.0, 200.0),
+                               ("curve_to", 10.0, 150.0, 50.0, 100.0, 100.0, 100.0), ("fill_preserve",),
+                               rgba(0.1, 0.3, 0.7, 0.5), ("stroke",)]))
+    x, y, w, h, r = 50.0, 50.0, 150.0, 140.0, 30.0
+    hp, nhp = float(np.float32(np.pi / 2)), float(np.float32(-np.pi / 2))
+    out.append(("curve_curved_rect", [("scale", 2.0, 2.0), ("set_line_width", 15.0), rgba(0, 0.5, 0.4, 1),
+                                      ("move_to", x, y + r), ("arc", x + r, y + r, r, pif, nhp),
+                                      ("line_to", x + w - r, y), ("arc", x + w - r, y + r, r, nhp, 0.0),
+                                      ("line_to", x + w, y + h - r), ("arc", x + w - r, y + h - r, r, 0.0, hp),
+                                      ("line_to", x + r, y + h), ("arc", x + r, y + h - r, r, hp, pif),
+                                      ("line_to", x, y + r), ("close_path",), ("fill_preserve",),
+                                      rgba(0.5, 0, 0, 0.5), ("stroke",)]))
+    out.append(("curve_test2", [("move_to", 100.0, 400.0), ("curve_to", 100.0, 100.0, 600.0, 700.0, 600.0, 400.0),
+                                ("curve_to", 1000.0, 100.0, 100.0, 800.0, 1000.0, 800.0),
+                                ("curve_to", 1000.0, 500.0, 700.0, 500.0, 700.0, 100.0), ("close_path",),
+                                rgba(1, 0, 0, 1), ("set_line_width", 40.0), ("stroke",)]))
     return [{"name": n, "width": width, "height": height, "samples": samples, "ops": ops, "paths": 0}
             for n, ops in out]
 
