@@ -326,9 +326,13 @@ def vkvg_demo_cases(width=512, height=512, samples=4):
     three functions: wide round joins on closed polylines, zigzags with
     round then bevel joins under translations), tests/circles.c and
     tests/arcs.c (full and partial arcs of growing radii, arc_negative,
-    scaled arcs, fill and stroke) and tests/curve.c (its four fixed
+    scaled arcs, fill and stroke), tests/curve.c (its four fixed
     sequences: curves, a rounded rectangle of arcs, self-crossing wide
-    strokes), one scene each on a fresh surface."""
+    strokes), tests/colinear.c, fill_and_stroke.c, simple_paint.c (paints
+    under rotations and scales, with and without a path), compositing.c
+    (translucent fills, opacity), radial_gradient.c and gradient.c (linear
+    gradients on fills, strokes and paints, transformed, translucent stops),
+    one scene each on a fresh surface."""
     import numpy as np
 
     rgba = lambda r, g, b, a: ("set_source_rgba", float(r), float(g), float(b), float(a))
@@ -464,6 +468,57 @@ def vkvg_demo_cases(width=512, height=512, samples=4):
                                 ("curve_to", 1000.0, 100.0, 100.0, 800.0, 1000.0, 800.0),
                                 ("curve_to", 1000.0, 500.0, 700.0, 500.0, 700.0, 100.0), ("close_path",),
                                 rgba(1, 0, 0, 1), ("set_line_width", 40.0), ("stroke",)]))
+    # tests/colinear.c, fill_and_stroke.c, simple_paint.c, compositing.c,
+    # radial_gradient.c, gradient.c (vkvg's fragment stage ignores a
+    # gradient's extend mode, so its vkvg_pattern_set_extend calls change
+    # nothing and are left out)
+    out.append(("colinear", [rgba(0.7, 0.7, 0.7, 1), ("paint",), rgba(0, 1, 0, 1), ("set_line_width", 10.0),
+                             ("move_to", 100.0, 100.0), ("line_to", 100.0, 200.0), ("line_to", 100.0, 300.0),
+                             ("stroke",)]))
+    tri = lambda x0: [("move_to", x0, 100.0), ("rel_line_to", 50.0, -80.0), ("rel_line_to", 50.0, 80.0),
+                      ("close_path",)]
+    out.append(("fill_and_stroke", tri(100.0) + tri(300.0) + [("set_line_width", 10.0),
+                                                              ("set_source_rgb", 0.0, 0.0, 1.0), ("fill_preserve",),
+                                                              ("set_source_rgb", 1.0, 0.0, 0.0), ("stroke",)]))
+    red = rgba(1, 0, 0, 1)
+    rect = ("rectangle", 100.0, 100.0, 300.0, 200.0)
+    for name, ops in (("paint", [rgba(1, 0, 0, 0.5), ("paint",)]),
+                      ("paint_with_rotation", [("rotate", 45.0), red, ("paint",)]),
+                      ("paint_with_scale", [("scale", 0.2, 0.2), red, ("paint",)]),
+                      ("paint_rect", [red, rect, ("paint",)]),
+                      ("paint_rect_with_rotation", [("rotate", 45.0), red, rect, ("paint",)]),
+                      ("paint_rect_with_scale", [("scale", 0.2, 0.2), red, rect, ("paint",)])):
+        out.append(("simple_" + name, harness + ops))
+    out.append(("compositing", [("clear",), rgba(1, 0, 0, 0.5), ("rectangle", 100.0, 100.0, 200.0, 200.0), ("fill",),
+                                rgba(0, 0, 1, 0.5), ("rectangle", 200.0, 200.0, 200.0, 200.0), ("fill",)]))
+    out.append(("opacity", [("clear",), red, ("rectangle", 100.0, 100.0, 200.0, 200.0), ("fill",),
+                            ("set_opacity", 0.5), rgba(0, 0, 1, 1), ("rectangle", 200.0, 200.0, 200.0, 200.0),
+                            ("fill",)]))
+    out.append(("radial_gradient", [("set_source_radial", 250.0, 250.0, 0.0, 300.0, 300.0, 260.0,
+                                     [(0.0, 1.0, 0.0, 0.0, 1.0), (0.5, 0.0, 1.0, 0.0, 1.0),
+                                      (1.0, 0.0, 0.0, 0.0, 1.0)]), ("paint",)]))
+    rgb3 = [(0.0, 1.0, 0.0, 0.0, 1.0), (0.5, 0.0, 1.0, 0.0, 1.0), (1.0, 0.0, 0.0, 1.0, 1.0)]
+    grad = lambda x0: ("set_source_linear", x0, 0.0, 300.0, 0.0, rgb3)
+    gp = [("rectangle", 0.0, 0.0, 400.0, 460.0), grad(0.0), ("fill",), ("rectangle", 100.0, 200.0, 50.0, 50.0),
+          grad(100.0), ("fill",), ("rectangle", 10.0, 10.0, 300.0, 50.0),
+          ("set_source_linear", 10.0, 0.0, 300.0, 0.0, [(0.0, 0.0, 0.0, 1.0, 0.0), (1.0, 1.0, 0.0, 0.0, 1.0)]),
+          ("fill",), ("rectangle", 400.0, 200.0, 50.0, 50.0), grad(400.0), ("fill",),
+          ("rectangle", 500.0, 200.0, 50.0, 50.0), grad(500.0), ("fill",)]
+    out.append(("gradient_paint", harness + gp))
+    out.append(("gradient_paint_repeat", harness + [grad(0.0), ("paint",)]))
+    out.append(("gradient_test", harness + [grad(0.0), ("rectangle", 100.0, 100.0, 200.0, 200.0),
+                                            ("set_line_width", 20.0), ("stroke",)]))
+    out.append(("gradient_test2", harness + [("set_source_rgb", 1.0, 0.0, 0.0), ("paint",), ("set_line_width", 20.0),
+                                             ("set_source_linear", 100.0, 0.0, 300.0, 0.0,
+                                              [(0.0, 1.0, 1.0, 1.0, 1.0), (1.0, 1.0, 1.0, 0.0, 0.0)]),
+                                             ("rectangle", 100.0, 100.0, 200.0, 200.0), ("fill",)]))
+    out.append(("gradient_transform", harness + [("translate", 200.0, 100.0), ("rotate", 0.5), ("set_line_width", 20.0),
+                                                 ("set_source_linear", 0.0, 0.0, 400.0, 0.0, rgb3),
+                                                 ("rectangle", 0.0, 0.0, 400.0, 200.0), ("stroke",)]))
+    out.append(("gradient_alpha", harness + [("set_source_rgb", 0.0, 1.0, 0.0), ("paint",),
+                                             ("set_source_linear", 10.0, 0.0, 300.0, 0.0,
+                                              [(1.0, 1.0, 0.0, 0.0, 0.5), (1.0, 1.0, 0.0, 0.0, 0.5)]),
+                                             ("rectangle", 10.0, 10.0, 300.0, 200.0), ("fill",)]))
     return [{"name": n, "width": width, "height": height, "samples": samples, "ops": ops, "paths": 0}
             for n, ops in out]
 
