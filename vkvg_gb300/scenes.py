@@ -330,9 +330,9 @@ def vkvg_demo_cases(width=512, height=512, samples=4):
     sequences: curves, a rounded rectangle of arcs, self-crossing wide
     strokes), tests/colinear.c, fill_and_stroke.c, simple_paint.c (paints
     under rotations and scales, with and without a path), compositing.c
-    (translucent fills, opacity), radial_gradient.c and gradient.c (linear
+    (translucent fills, opacity), radial_gradient.c, gradient.c (linear
     gradients on fills, strokes and paints, transformed, translucent stops),
-    one scene each on a fresh surface."""
+    rect_fill.c and transform.c, one scene each on a fresh surface."""
     import numpy as np
 
     rgba = lambda r, g, b, a: ("set_source_rgba", float(r), float(g), float(b), float(a))
@@ -519,6 +519,22 @@ def vkvg_demo_cases(width=512, height=512, samples=4):
                                              ("set_source_linear", 10.0, 0.0, 300.0, 0.0,
                                               [(1.0, 1.0, 0.0, 0.0, 0.5), (1.0, 1.0, 0.0, 0.0, 0.5)]),
                                              ("rectangle", 10.0, 10.0, 300.0, 200.0), ("fill",)]))
+    # tests/rect_fill.c (both fill rules) and tests/transform.c
+    # (cairo_tests' first run: rotation 0.002, the 512x512 surface's centre)
+    sq = [rgba(0, 0, 1, 0.5), ("rectangle", 100.0, 100.0, 200.0, 200.0), ("fill",),
+          ("rectangle", 200.0, 200.0, 200.0, 200.0), rgba(1, 0, 0, 0.5), ("fill",)]
+    out.append(("rect_fill", [("clear",), ("set_fill_rule", 1)] + sq))
+    out.append(("rect_fill_evenodd", [("clear",), ("set_fill_rule", 0)] + sq))
+    a0, a1 = -100.0, 100.0
+    rounded = [("move_to", a0, 0.0), ("curve_to", a0, a0, a0, a0, 0.0, a0), ("curve_to", a1, a0, a1, a0, a1, 0.0),
+               ("curve_to", a1, a1, a1, a1, 0.0, a1), ("curve_to", a0, a1, a0, a1, a0, 0.0), ("close_path",),
+               ("set_source_rgb", 0.5, 0.5, 1.0), ("fill_preserve",), rgba(0.5, 0, 0, 0.5),
+               ("set_line_width", 10.0), ("stroke",)]
+    out.append(("transform_cairo", [("set_fill_rule", 0), rgba(1, 1, 1, 1), ("paint",), ("set_line_width", 10.0),
+                                    ("set_source_rgb", 0.0, 0.0, 1.0), ("translate", width / 2.0, height / 2.0),
+                                    ("rotate", float(np.float32(0.002))),
+                                    ("arc", 0.0, 0.0, 150.0, 0.0, float(np.float32(np.pi * 1.5))), ("stroke",)]
+                + rounded))
     return [{"name": n, "width": width, "height": height, "samples": samples, "ops": ops, "paths": 0}
             for n, ops in out]
 
