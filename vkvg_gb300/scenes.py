@@ -332,7 +332,8 @@ def vkvg_demo_cases(width=512, height=512, samples=4):
     under rotations and scales, with and without a path), compositing.c
     (translucent fills, opacity), radial_gradient.c, gradient.c (linear
     gradients on fills, strokes and paints, transformed, translucent stops),
-    rect_fill.c and transform.c, one scene each on a fresh surface."""
+    rect_fill.c, transform.c and bezier.c, one scene each on a fresh
+    surface."""
     import numpy as np
 
     rgba = lambda r, g, b, a: ("set_source_rgba", float(r), float(g), float(b), float(a))
@@ -535,6 +536,15 @@ def vkvg_demo_cases(width=512, height=512, samples=4):
                                     ("rotate", float(np.float32(0.002))),
                                     ("arc", 0.0, 0.0, 150.0, 0.0, float(np.float32(np.pi * 1.5))), ("stroke",)]
                 + rounded))
+    # tests/bezier.c (its first frame: the self-crossing cubic, no point
+    # hovered, at 4 samples instead of its 8)
+    pts = ((150.0, 150.0), (500.0, 340.0), (470.0, 150.0), (160.0, 350.0))
+    bz = [("clear",), ("set_line_width", 10.0), ("set_line_join", 0), ("set_line_cap", 0), ("move_to",) + pts[0],
+          ("curve_to",) + pts[1] + pts[2] + pts[3], rgba(1, 0, 0, 0.3), ("stroke",), ("flush",),
+          ("set_line_width", 1.0), rgba(0.5, 0.5, 0.5, 0.6)]
+    for px, py in pts:
+        bz += [("arc", px, py, 5.0, 0.0, pif * 2), ("fill_preserve",), ("stroke",)]
+    out.append(("bezier", bz + [("stroke",)]))
     return [{"name": n, "width": width, "height": height, "samples": samples, "ops": ops, "paths": 0}
             for n, ops in out]
 
