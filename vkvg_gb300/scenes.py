@@ -332,8 +332,8 @@ def vkvg_demo_cases(width=512, height=512, samples=4):
     under rotations and scales, with and without a path), compositing.c
     (translucent fills, opacity), radial_gradient.c, gradient.c (linear
     gradients on fills, strokes and paints, transformed, translucent stops),
-    rect_fill.c, transform.c and bezier.c, one scene each on a fresh
-    surface."""
+    rect_fill.c, transform.c, bezier.c and gradient2.c, one scene each on a
+    fresh surface."""
     import numpy as np
 
     rgba = lambda r, g, b, a: ("set_source_rgba", float(r), float(g), float(b), float(a))
@@ -545,6 +545,15 @@ def vkvg_demo_cases(width=512, height=512, samples=4):
     for px, py in pts:
         bz += [("arc", px, py, 5.0, 0.0, pif * 2), ("fill_preserve",), ("stroke",)]
     out.append(("bezier", bz + [("stroke",)]))
+    # tests/gradient2.c (its first frame, linear; and its radial pattern type)
+    stops4 = [(0.0, 1.0, 0.0, 0.0, 0.5), (0.3, 0.0, 1.0, 0.0, 0.5), (0.6, 0.0, 0.0, 1.0, 0.5), (1.0, 0.0, 0.0, 0.0, 0.5)]
+    marks = [("set_dash", [], 0.0), ("set_line_width", 1.0)]
+    for px, py in ((150.0, 150.0), (250.0, 150.0)):
+        marks += [rgba(1.0, 0.5, 0.5, 0.9), ("arc", px, py, 7.0, 0.0, pif * 2), ("fill_preserve",), ("stroke",)]
+    out.append(("gradient2_linear", [("clear",), ("set_source_linear", 150.0, 150.0, 250.0, 150.0, stops4),
+                                     ("paint",)] + marks))
+    out.append(("gradient2_radial", [("clear",), ("set_source_radial", 125.0, 125.0, 20.0, 150.0, 150.0, 100.0,
+                                                  stops4), ("paint",)] + marks))
     return [{"name": n, "width": width, "height": height, "samples": samples, "ops": ops, "paths": 0}
             for n, ops in out]
 
