@@ -269,7 +269,7 @@ def test_vkvg_demo_cases_bit_exact(gb, vko, name):
     fill.c, fill_non_zero.c, dashes.c, line_join.c, circles.c, arcs.c,
     curve.c, colinear.c, fill_and_stroke.c, simple_paint.c, compositing.c,
     radial_gradient.c, gradient.c, rect_fill.c, transform.c, bezier.c,
-    gradient2.c) at the
+    gradient2.c, inverse_colinear.c) at the
     harness's 512x512: geometry,
     samples and image equal the oracle's"""
     sc = [s for s in scenes.vkvg_demo_cases() if s["name"] == name][0]

@@ -332,8 +332,8 @@ def vkvg_demo_cases(width=512, height=512, samples=4):
     under rotations and scales, with and without a path), compositing.c
     (translucent fills, opacity), radial_gradient.c, gradient.c (linear
     gradients on fills, strokes and paints, transformed, translucent stops),
-    rect_fill.c, transform.c, bezier.c and gradient2.c, one scene each on a
-    fresh surface."""
+    rect_fill.c, transform.c, bezier.c, gradient2.c and inverse_colinear.c,
+    one scene each on a fresh surface."""
     import numpy as np
 
     rgba = lambda r, g, b, a: ("set_source_rgba", float(r), float(g), float(b), float(a))
@@ -554,6 +554,25 @@ def vkvg_demo_cases(width=512, height=512, samples=4):
                                      ("paint",)] + marks))
     out.append(("gradient2_radial", [("clear",), ("set_source_radial", 125.0, 125.0, 20.0, 150.0, 150.0, 100.0,
                                                   stops4), ("paint",)] + marks))
+    # tests/inverse_colinear.c: its first frame (a wide mitered polyline
+    # with sharp turns) and the settings its keys switch: closed with bevel
+    # joins; round joins and caps with its {0, 60} dash; arcs (arc_negative)
+    # at both ends
+    ipts = ((150.0, 150.0), (200.0, 300.0), (250.0, 150.0), (280.0, 350.0))
+    a15, api = float(np.float32(pif * 1.5)), pif
+
+    def inv(join, cap, closed, dash, arcs):
+        ops = [("clear",)] + ([("set_dash", [0.0, 60.0], 0.0)] if dash else []) + [
+            rgba(1, 0, 0, 0.3), ("set_line_width", 50.0), ("set_line_join", join), ("set_line_cap", cap),
+            ("set_miter_limit", 10.0)]
+        ops.append(("arc_negative", ipts[0][0], ipts[0][1], 200.0, a15, api) if arcs else ("move_to",) + ipts[0])
+        ops += [("line_to",) + p for p in ipts[1:-1]]
+        ops.append(("arc_negative", ipts[-1][0], ipts[-1][1], 200.0, a15, api) if arcs else ("line_to",) + ipts[-1])
+        return ops + ([("close_path",)] if closed else []) + [("stroke",)]
+    out.append(("inverse_colinear", inv(0, 0, False, False, False)))
+    out.append(("inverse_colinear_closed_bevel", inv(2, 0, True, False, False)))
+    out.append(("inverse_colinear_round_dash", inv(1, 1, False, True, False)))
+    out.append(("inverse_colinear_arcs", inv(0, 0, False, False, True)))
     return [{"name": n, "width": width, "height": height, "samples": samples, "ops": ops, "paths": 0}
             for n, ops in out]
 
