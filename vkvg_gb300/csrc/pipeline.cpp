@@ -629,10 +629,12 @@ cudaError_t Pipeline::run(const FrameHost &f, _vkvg_surface_t *surf, bool timing
         form = 4; /* 16-bit counters would not hold a cell's crossings: whole bands */
     form_run  = form;
     form_half = form == 3 ? 1 : 0;
-    /* the tiny form's small draws read cells of fewer than 64 record units
-       from L2 instead of staging them (a bulk copy and a barrier wait per
-       draw: the glyph scene's raster 11.23 -> 10.87 ms, no change above 64) */
-    A.stage_min = form == 2 || form == 5 ? 64u : 0u;
+    /* the small-draw forms read their smallest cells from L2 instead of
+       staging them (a bulk copy and a wait per draw): the tiny form cells
+       under 64 record units (glyph raster 11.23 -> 10.87 ms, no change
+       above 64), the micro form cells under 16 (10.31 ms at 64, 10.23 ms
+       staging every cell, 10.16 ms at 16) */
+    A.stage_min = form == 2 ? 64u : form == 5 ? 16u : 0u;
     if (form == 3 || form == 4)
         CK(gb_launch_raster_rows(st, &A, ngrad > 0, form_half));
     else
